@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Benchmark of the MOLOCH step: grid-point-steps per second on one GB300.
+
+Workload (default): the moist convection-permitting domain, 512 x 512 cross
+points x 41 levels, dx 3 km, dt 20 s, 4 acoustic substeps, FP64, with the
+seeded synthetic initial state of regcm_gb300.case.config1 (no netCDF input
+exists here; the recipe stands in for RegCM's ICBC files).  A step is one full
+MOLOCH model step (acoustic substeps, WAF advection of 10 fields, boundary
+relaxation, diagnostics, status update, mass budget).
+
+Our arm prints one JSON line with
+  value      device-resident gp-steps/s (CUDA events on the library stream),
+  e2e        the same metric through the C ABI with host buffers: per step
+             upload of the prognostic inputs from pinned memory, the step,
+             download of the full state,
+  roofline   the dominant kernel's algorithmic bytes / its average launch time
+             against the measured HBM copy bandwidth, plus ncu-style context,
+  cpu_baseline  the CPU oracle (FP64 C++ restatement of the reference, OpenMP
+             on all host cores) timed on a bounded sample of the same domain.
+`--impl reference` times that CPU implementation alone (the reference's own
+Fortran cannot be built here: no Fortran compiler, MPI or netCDF).
+
+Multi-GPU: replicas only (each rank advances its own domain; no data-path
+collective); value = all ranks' gp-steps / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "grid-point-steps/s"
+UNIT = "gp-steps/s"
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+# ---- clocks during the timed region ---------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not Path(self.path).exists():
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- algorithmic bytes per launch of each kernel group ---------------------
+def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None:
+    """Compulsory HBM words each launch must move, times the word size.
+
+    Counts follow the fusion contract 'each kernel reads its inputs and writes
+    its outputs once'; 2-D and 1-D arrays are ignored.  Per point (cross
+    point x level) of the launch's domain:
+      sound_div       u, v, rfmzu, rfmzv, fmz -> zdiv2, s                 7
+      sound_solve     zdiv2, s, w, pai, tetav, tetavf, fmz, fmzf
+                      -> w, pai, tetavf                                   11
+      sound_momentum  u, v, zdiv2, pai, tetav -> u, v                      7
+      adv_vertical    per field: field -> wz (2); shared s, zrfmu, zrfmd   2F+3
+      adv_horizontal  per field: field, wz -> out (3); shared u, v, fmz,
+                      rfmzu                                               3F+4
+    """
+    d = case.dims
+    pts = (d.jx - 1) * (d.iy - 1) * d.kz
+    inner = (d.jx - 3) * (d.iy - 3) * d.kz
+    words = {
+        "sound_div": 7 * pts,
+        "sound_solve": 11 * inner,
+        "sound_momentum": 7 * pts,
+        "adv_vertical": (2 * nadv_fields + 3) * pts,
+        "adv_horizontal": (3 * nadv_fields + 4) * pts,
+    }.get(name)
+    return None if words is None else float(words) * wbytes
+
+
+def n_adv_fields(case) -> int:
+    p, d = case.params, case.dims
+    return 6 + (d.nqx - 1 if p.ipptls > 0 else 0) + d.ntr
+
+
+def make_case(args, rank=0):
+    from regcm_gb300 import abi
+    from regcm_gb300 import case as cs
+    prec = abi.MLC_PREC_MIXED if args.precision == "mixed" else abi.MLC_PREC_FP64
+    if args.config == "c1":
+        return cs.config1(seed=1 + rank, precision=prec)
+    if args.config == "c0":
+        return cs.config0(seed=rank, precision=prec)
+    raise SystemExit(f"unknown config {args.config}")
+
+
+def workload_name(args):
+    return {"c1": "moloch-moist-512x512x41-dx3km-dt20-ns4",
+            "c0": "moloch-dry-64x64x30-dx12km-dt60-ns3"}[args.config]
+
+
+# ---- CPU oracle timing -------------------------------------------------------
+def time_oracle(case, steps: int, warmup: int = 1, budget_s: float = 30.0):
+    """gp-steps/s of the CPU oracle on `case` (all host threads)."""
+    from oracle.oracle import Oracle
+    o = Oracle(case)
+    t0 = time.perf_counter()
+    for _ in range(warmup):
+        o.step(1)
+    t1 = time.perf_counter()
+    per = (t1 - t0) / max(warmup, 1)
+    n = max(1, min(steps, int(budget_s / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    st, _ = o.step(n)
+    dt = time.perf_counter() - t0
+    o.close()
+    return case.points * n / dt, n, dt
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ---- the reference arm -------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    os.environ.setdefault("OMP_NUM_THREADS", str(cpu_threads()))
+    case = make_case(args)
+    value, n, dt = time_oracle(case, args.steps, warmup=max(1, min(args.warmup, 2)),
+                               budget_s=150.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": n, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / n,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": workload_name(args), "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+                         "kind": "port",
+                         "sample": f"{n} full steps of the {workload_name(args)} domain "
+                                   "(CPU oracle: C++ FP64 restatement of Main/mod_moloch.F90; the "
+                                   "reference Fortran needs gfortran, MPI and netCDF, absent here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---- our arm -----------------------------------------------------------------
+def pinned_like(arrays: dict) -> dict:
+    import torch
+    out = {}
+    for k, v in arrays.items():
+        t = torch.empty(v.size, dtype=torch.float64, pin_memory=True)
+        a = t.numpy().reshape(v.shape, order="F")
+        a[...] = v
+        out[k] = (a, t)
+    return out
+
+
+def run_ours(args, rank, world):
+    import torch
+    from regcm_gb300 import abi
+    from regcm_gb300.moloch import domain_from_case
+
+    lib = abi.load()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    case = make_case(args, rank)
+    dom = domain_from_case(case)
+    ctx = dom._ctx
+    lib.mlc_step_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.mlc_diag),
+                                   C.POINTER(C.c_float)]
+
+    class KT(C.Structure):
+        _fields_ = [("name", C.c_char * 32), ("launches", C.c_int32), ("ms", C.c_double)]
+
+    lib.mlc_profile_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(KT), C.c_int,
+                                      C.POINTER(C.c_int)]
+    # warm-up (records the step graphs)
+    dom.step(args.warmup)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    diag = abi.mlc_diag()
+    ms = C.c_float()
+    with ClockSampler(dev) as clk:
+        st = lib.mlc_step_timed(ctx, args.steps, C.byref(diag), C.byref(ms))
+    abi.check(st, "mlc_step_timed")
+    torch.cuda.synchronize()
+    t_dev = ms.value / 1000.0
+    if world > 1:
+        t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+        torch.distributed.barrier()
+    pts = case.points
+    value = pts * args.steps * world / t_dev
+    launches = dom.launches_per_step()
+
+    # per-kernel device times (eager steps, events around each kernel group)
+    ktab = (KT * 32)()
+    nk = C.c_int()
+    abi.check(lib.mlc_profile_steps(ctx, 2, ktab, 32, C.byref(nk)), "mlc_profile_steps")
+    kernels = {ktab[i].name.decode(): (ktab[i].launches, ktab[i].ms) for i in range(nk.value)}
+    total_k = sum(v[1] for v in kernels.values())
+    wbytes = 4 if args.precision == "mixed" else 8
+    nf = n_adv_fields(case)
+    dom_name = max(kernels, key=lambda k: kernels[k][1])
+    pk = peaks()
+    hbm_peak = float(pk.get("hbm_gbs", 6800.0))
+    bytes_per = kernel_bytes(dom_name, case, nf, wbytes)
+    nl, kms = kernels[dom_name]
+    roofline = {
+        "kernel": dom_name, "bound": "hbm", "unit": "GB/s",
+        "peak": hbm_peak, "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
+        "share_of_step": kms / total_k,
+        "traffic": None,
+    }
+    if bytes_per:
+        ach = bytes_per / (kms / nl / 1000.0) / 1e9
+        roofline.update({"achieved": ach, "frac": ach / hbm_peak, "algorithmic_bytes": bytes_per})
+    roofline["kernels_ms_per_step"] = {k: v[1] / 2.0 for k, v in sorted(
+        kernels.items(), key=lambda kv: -kv[1][1])}
+
+    # end-to-end through the C ABI with pinned host buffers
+    e2e = None
+    if rank == 0 or world > 1:
+        inputs = {k: case.state[k] for k in ("u", "v", "w", "pai", "tetav", "qx")}
+        if case.dims.ntr:
+            inputs["trac"] = case.state["trac"]
+        pin_in = pinned_like(inputs)
+        pin_out = pinned_like(case.empty_state())
+        sp_in = case.state_ptrs_of({k: v[0] for k, v in pin_in.items()})
+        sp_out = case.state_ptrs_of({k: v[0] for k, v in pin_out.items()})
+        h2d = sum(v[0].nbytes for v in pin_in.values())
+        d2h = sum(v[0].nbytes for v in pin_out.values())
+        ne = max(2, min(args.steps, 10))
+        dom.upload(sp_in)
+        dom.step(1)
+        dom.download(sp_out)
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            dom.upload(sp_in)
+            dom.step(1)
+            dom.download(sp_out)
+        te = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([te], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            te = float(t.item())
+        e2e = {"value": pts * ne * world / te, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": ne, "ms_per_step": 1000.0 * te / ne}
+    dom.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        os.environ.setdefault("OMP_NUM_THREADS", str(cpu_threads()))
+        cv, n, dt = time_oracle(case, steps=5, warmup=1, budget_s=20.0)
+        cpu = {"value": cv, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+               "kind": "port",
+               "sample": f"{n} full steps of the same domain on the CPU oracle (C++ FP64, OpenMP)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": workload_name(args), "points_per_domain": pts,
+                   "precision": args.precision, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (state > 1 GB)"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": launches * args.steps, "clocks": clk.summary(),
+        "diag": {"ps_min": diag.ps_min, "ps_max": diag.ps_max, "drymass": diag.drymass},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c1", choices=["c0", "c1"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

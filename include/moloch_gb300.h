@@ -1,0 +1,237 @@
+/*
+ * moloch_gb300.h -- C ABI of the GB300 (sm_103a) MOLOCH dynamical-core step.
+ *
+ * This library replaces the three public procedures of RegCM's MOLOCH module
+ *   public :: allocate_moloch, init_moloch, moloch      (Main/mod_moloch.F90:127)
+ * which take no arguments and work on module globals.  Here the same state is
+ * passed explicitly, as plain host pointers in the reference's own layout:
+ * Fortran column-major (j fastest, then i, then k, then species n), with the
+ * extents a one-process, non-periodic RegCM run gives them (every ga/gb halo
+ * collapses to zero, Main/mod_atm_interface.F90:204-233,286-309):
+ *
+ *   dot 2-D   (jx, iy)            msfu, msfv, msfx, ibnd_*
+ *   u points  (jx, iy-1[, kz])    u, hx, rfmzu, dub, ulat     (jde, ice)
+ *   v points  (jx-1, iy[, kz])    v, hy, rfmzv, dvb, vlat     (jce, ide)
+ *   cross     (jx-1, iy-1[, kz])  pai, tetav, t, tvirt, ux, vx, p, rho, qsat,
+ *                                 fmz, zeta, dz, xtb, xqb, xpaib, xlb, xib, ps
+ *   w levels  (jx-1, iy-1, kz+1)  w, fmzf
+ *   species   (jx-1, iy-1, kz, n) qx (n = nqx), trac and chib (n = ntr)
+ *
+ * jx and iy are the reference's dot-point extents (namelist dimparam); the
+ * cross-point grid is (jx-1) x (iy-1).  k = 1 is the model top.
+ *
+ * Status codes: 0 = OK, negative = error (mlc_strerror gives the text).  The
+ * Fortran shim maps a negative status to RegCM's fatal() the way the reference
+ * aborts (Share/mod_message.F90:86-99).  The library never frees caller memory.
+ * One context owns one CUDA stream and its device arena; a context is not
+ * thread-safe, distinct contexts may be driven from distinct host threads.
+ */
+#ifndef MOLOCH_GB300_H
+#define MOLOCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MLC_OK                 0
+#define MLC_ERR_INVALID       -1  /* bad argument, extent or parameter      */
+#define MLC_ERR_UNSUPPORTED   -2  /* option outside the built path          */
+#define MLC_ERR_CUDA          -3  /* CUDA runtime error                     */
+#define MLC_ERR_NOMEM         -4  /* device allocation failed               */
+#define MLC_ERR_STATE         -5  /* call order violated (e.g. no static)   */
+#define MLC_ERR_NONFINITE     -6  /* NaN/Inf in ps: "CFL VIOLATION"         */
+#define MLC_ERR_NODEVICE      -7  /* no CUDA device visible                 */
+#define MLC_ERR_BUDGET        -8  /* request exceeds the device budget      */
+#define MLC_ERR_TOO_LARGE     -9  /* size beyond a fixed maximum            */
+
+/* ---- precision modes --------------------------------------------------- */
+#define MLC_PREC_FP64   0  /* every field and operation in FP64            */
+#define MLC_PREC_MIXED  1  /* FP32 fields and horizontal stencils; FP64
+                              vertical implicit solve, Exner/pressure and
+                              mass budget sums                             */
+
+/* Domain extents.  Reference names in brackets. */
+typedef struct mlc_dims {
+  int32_t jx;    /* dot points west->east            [jx, dimparam]       */
+  int32_t iy;    /* dot points south->north          [iy, dimparam]       */
+  int32_t kz;    /* full levels, k=1 at the top      [kz]                 */
+  int32_t nqx;   /* water species in qx, qv first    [nqx, mod_params]    */
+  int32_t ntr;   /* passive tracers in trac (ichem=1 when > 0) [ntr]      */
+} mlc_dims;
+
+/* Run parameters (Share/mod_dynparam.F90:141-152,203-211,
+ * Main/mpplib/mod_runparams.F90).  Defaults: mlc_default_params(). */
+typedef struct mlc_params {
+  double  dtsec;          /* model step [s]                      [dtsec]   */
+  double  dx;             /* grid spacing [m]                    [dx]      */
+  double  mo_ztop;        /* model top [m]                       [mo_ztop] */
+  double  mo_h;           /* decay height of b(zeta) [m]         [mo_h]    */
+  double  mo_a0;          /* G(zeta) shape parameter             [mo_a0]   */
+  double  dtbdys;         /* boundary data interval [s]          [dtbdys]  */
+  int32_t mo_nadv;        /* advection steps per dt              [mo_nadv] */
+  int32_t mo_nsound;      /* acoustic substeps per advection step          */
+  int32_t mo_divdamp;     /* divergence damping on/off           [mo_divdamp]   */
+  int32_t mo_divfilter;   /* divergence filter on/off            [mo_divfilter] */
+  int32_t mo_top_nudge;   /* top nudging on/off                  [mo_top_nudge] */
+  int32_t mo_spectral_nudge; /* spectral nudging: must be 0 (not built)   */
+  int32_t do_apply_bdy;   /* lateral boundary relaxation on/off [do_apply_bdy] */
+  int32_t lrotllr;        /* ROTLLR projection branch            [iproj]   */
+  int32_t ipptls;         /* microphysics class: 0,1,2           [ipptls]  */
+  int32_t present_qc;     /* boundary data carries qc            [present_qc] */
+  int32_t present_qi;     /* boundary data carries qi            [present_qi] */
+  int32_t nspgx;          /* relaxation zone width, cross points [nspgx]   */
+  int32_t nspgd;          /* relaxation zone width, dot points   [nspgd]   */
+  int32_t nztop;          /* levels nudged at the top            [nztop]   */
+  int32_t debug_level;    /* > 0: mass budget every step         [debug_level] */
+  int32_t precision;      /* MLC_PREC_FP64 or MLC_PREC_MIXED               */
+} mlc_params;
+
+/* Time-invariant fields (host pointers, read once by mlc_bind_static).
+ * Reference: mddom%*, mo_atm%fmz/fmzf/rfmzu/rfmzv/zeta/dz, hefc, tnudge,
+ * ffilt, zita/zitah and ba_cr/ba_ud/ba_vd%ibnd. */
+typedef struct mlc_static_ptrs {
+  const double  *msfu, *msfv, *msfx;  /* (jx,iy) map factors               */
+  const double  *ulat;                /* (jx,iy-1) latitude of u points    */
+  const double  *vlat;                /* (jx-1,iy) latitude of v points    */
+  const double  *rlat;                /* (iy) row latitude (ROTLLR only)   */
+  const double  *hx;                  /* (jx,iy-1)  terrain slope at u     */
+  const double  *hy;                  /* (jx-1,iy)  terrain slope at v     */
+  const double  *fmz;                 /* (jx-1,iy-1,kz)                     */
+  const double  *fmzf;                /* (jx-1,iy-1,kz+1)                   */
+  const double  *rfmzu;               /* (jx,iy-1,kz)                       */
+  const double  *rfmzv;               /* (jx-1,iy,kz)                       */
+  const double  *zeta;                /* (jx-1,iy-1,kz) height above ground */
+  const double  *dz;                  /* (jx-1,iy-1,kz) layer depth         */
+  const double  *zita;                /* (kz+1) full-level zita             */
+  const double  *zitah;               /* (kz)   half-level zita             */
+  const double  *ffilt;               /* (kz) implicit-w sponge             */
+  const double  *hefc;                /* (nspgx,kz) relaxation weights      */
+  const double  *fcx;                 /* (nspgx) tracer relaxation weights  */
+  const double  *tnudge;              /* (kz) top-nudging profile           */
+  const int32_t *ibnd_cr;             /* (jx,iy) zone index, cross points   */
+  const int32_t *ibnd_ud;             /* (jx,iy) zone index, u points       */
+  const int32_t *ibnd_vd;             /* (jx,iy) zone index, v points       */
+} mlc_static_ptrs;
+
+/* Prognostic and diagnostic state (mo_atm fields, sfs%psa). */
+typedef struct mlc_state_ptrs {
+  double *u;      /* (jx,iy-1,kz)     */
+  double *v;      /* (jx-1,iy,kz)     */
+  double *w;      /* (jx-1,iy-1,kz+1) */
+  double *pai;    /* Exner function   */
+  double *tetav;  /* virtual potential temperature */
+  double *t;      /* temperature      */
+  double *tvirt;  /* virtual temperature */
+  double *ux;     /* u at cross points */
+  double *vx;     /* v at cross points */
+  double *p;      /* pressure         */
+  double *rho;    /* density          */
+  double *qsat;   /* saturation mixing ratio */
+  double *qx;     /* (jx-1,iy-1,kz,nqx) */
+  double *trac;   /* (jx-1,iy-1,kz,ntr), may be NULL when ntr = 0 */
+  double *ps;     /* (jx-1,iy-1) surface pressure */
+} mlc_state_ptrs;
+
+/* Lateral boundary data: index 0 = b0, 1 = b1 (v3dbound%b0/%b1). */
+typedef struct mlc_bdy_ptrs {
+  const double *xtb[2];   /* (jx-1,iy-1,kz) temperature        */
+  const double *xqb[2];   /* (jx-1,iy-1,kz) qv                 */
+  const double *xpaib[2]; /* (jx-1,iy-1,kz) Exner              */
+  const double *xlb[2];   /* (jx-1,iy-1,kz) qc (present_qc)    */
+  const double *xib[2];   /* (jx-1,iy-1,kz) qi (present_qi)    */
+  const double *dub[2];   /* (jx,iy-1,kz)   u                  */
+  const double *dvb[2];   /* (jx-1,iy,kz)   v                  */
+  const double *xpsb[2];  /* (jx-1,iy-1)    surface pressure   */
+  const double *chib[2];  /* (jx-1,iy-1,kz,ntr) tracers        */
+} mlc_bdy_ptrs;
+
+/* Per-step diagnostics (Main/mod_moloch.F90:407-422, Main/mod_massck.F90). */
+typedef struct mlc_diag {
+  double  ps_max, ps_min;   /* over interior cross points [Pa]          */
+  int32_t nonfinite;        /* 1 when ps max/min is NaN or Inf          */
+  int32_t steps_done;       /* steps completed by this call             */
+  double  drymass;          /* sum dx^2 dz rho, interior [kg]           */
+  double  dryadv;           /* dry-air boundary flux over dt [kg]       */
+  double  qmass;            /* sum of qx dx^2 dz rho, interior [kg]     */
+  double  qadv;             /* water boundary flux over dt [kg]         */
+  double  xbctime;          /* boundary clock after the call [s]        */
+} mlc_diag;
+
+typedef struct mlc_ctx mlc_ctx;
+
+/* Fill p with the reference defaults (mod_dynparam / mod_runparams). */
+void mlc_default_params(mlc_params *p);
+
+/* allocate_moloch (Main/mod_moloch.F90:159-199): validate extents and
+ * parameters, pick device 0 (or the current device), allocate the device
+ * arena.  No state is valid until mlc_bind_static + mlc_upload_state. */
+int mlc_create(const mlc_dims *dims, const mlc_params *params, mlc_ctx **out);
+
+/* The static half of init_moloch (Main/mod_moloch.F90:201-308) plus the
+ * fields compute_moloch_static leaves in mddom/mo_atm
+ * (Main/mod_params.F90:3316-3395): copied to the device once; the library
+ * derives coriolis, 1/m, m^2, G(zeta), xkdamp, xknu and bdywt{u,v,w}. */
+int mlc_bind_static(mlc_ctx *ctx, const mlc_static_ptrs *s);
+
+/* Copy the host state into the device arena (init from b0 or restart,
+ * Main/mod_init.F90:155-219).  Sets w(:,:,1) = 0 as init_moloch does. */
+int mlc_upload_state(mlc_ctx *ctx, const mlc_state_ptrs *st);
+
+/* Copy the device state back into the host arrays (NULL members skipped). */
+int mlc_download_state(mlc_ctx *ctx, const mlc_state_ptrs *st);
+
+/* Boundary arrays b0/b1 and the boundary clock (xbctime, dtbdys), the data
+ * bdyin (Main/mod_bdycod.F90:1079-1200) leaves for bdyval and morelax.  Each
+ * step advances xbctime by dtsec, as bdyval does (mod_bdycod.F90:2653). */
+int mlc_set_boundary(mlc_ctx *ctx, const mlc_bdy_ptrs *b, double xbctime,
+                     double dtbdys);
+
+/* moloch (Main/mod_moloch.F90:312-446) nsteps times: dynamical core,
+ * boundary relaxation, diagnostics, status update, mass budget (when
+ * debug_level > 0) and the NaN/Inf check on ps.  Physics is not part of
+ * this path: tendencies are zero.  out (optional) receives the diagnostics
+ * of the last step.  Returns MLC_ERR_NONFINITE when ps is not finite. */
+int mlc_step(mlc_ctx *ctx, int nsteps, mlc_diag *out);
+
+/* Release the device arena and stream. */
+void mlc_destroy(mlc_ctx *ctx);
+
+/* Text for a status code. */
+const char *mlc_strerror(int status);
+
+/* Device bytes one domain of these extents holds (for admission control). */
+size_t mlc_footprint_bytes(const mlc_dims *dims, int precision);
+
+/* ---- measurement and tracing (no counterpart in the reference, which
+ * times moloch with system_clock timers, Main/mpplib/mod_service.F90) ---- */
+
+/* mlc_step plus the device time of the steps, from CUDA events recorded on
+ * the context stream around the step launches. */
+int mlc_step_timed(mlc_ctx *ctx, int nsteps, mlc_diag *out, float *ms);
+
+typedef struct mlc_kernel_time {
+  char    name[32];
+  int32_t launches;
+  double  ms;
+} mlc_kernel_time;
+
+/* Run nsteps steps without graph replay, with events around every kernel
+ * group; returns the per-group launch count and total device time. */
+int mlc_profile_steps(mlc_ctx *ctx, int nsteps, mlc_kernel_time *out, int max_out,
+                      int *n_out);
+
+/* Kernels one step launches (known after the first step). */
+int mlc_launches_per_step(const mlc_ctx *ctx);
+
+/* Record steps into CUDA graphs (default 1) or launch them one by one (0). */
+int mlc_set_graphs(mlc_ctx *ctx, int on);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOLOCH_GB300_H */

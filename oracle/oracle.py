@@ -1,0 +1,95 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes access to the CPU oracle.
+
+The oracle is a C++ FP64 restatement of RegCM's MOLOCH step
+(oracle/moloch_oracle.cpp) and of its setup routines (oracle/oracle_setup.cpp).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
+as the checker; the product library never loads it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from regcm_gb300 import abi
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libmoloch_oracle.so"
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+        lib = C.CDLL(str(LIB))
+        P = C.POINTER
+        dp = P(C.c_double)
+        lib.orc_create.restype = C.c_void_p
+        lib.orc_create.argtypes = [P(abi.mlc_dims), P(abi.mlc_params)]
+        lib.orc_destroy.argtypes = [C.c_void_p]
+        lib.orc_bind_static.argtypes = [C.c_void_p, P(abi.mlc_static_ptrs)]
+        lib.orc_set_state.argtypes = [C.c_void_p, P(abi.mlc_state_ptrs)]
+        lib.orc_get_state.argtypes = [C.c_void_p, P(abi.mlc_state_ptrs)]
+        lib.orc_set_boundary.argtypes = [C.c_void_p, P(abi.mlc_bdy_ptrs), C.c_double, C.c_double]
+        lib.orc_step.argtypes = [C.c_void_p, C.c_int, P(abi.mlc_diag)]
+        lib.orc_sound_only.argtypes = [C.c_void_p]
+        lib.orc_get_work.argtypes = [C.c_void_p, C.c_int, dp]
+        lib.orc_setup_levels.argtypes = [C.c_int, C.c_double, dp, dp]
+        lib.orc_setup_metric.argtypes = [P(abi.mlc_dims), P(abi.mlc_params)] + [dp] * 16
+        lib.orc_relax_coefficients.argtypes = [C.c_int, C.c_double, C.c_double, dp]
+        lib.orc_setup_relaxation.argtypes = [P(abi.mlc_dims), P(abi.mlc_params), dp, dp, dp, dp,
+                                             dp, P(C.c_int)]
+        lib.orc_setup_boundaries.argtypes = [C.c_int] * 6 + [P(C.c_int32)]
+        lib.orc_paicompute.argtypes = [P(abi.mlc_dims)] + [dp] * 5 + [C.c_double, dp]
+        _lib = lib
+    return _lib
+
+
+class Oracle:
+    """One domain stepped by the CPU oracle."""
+
+    def __init__(self, case):
+        self.case = case
+        self.lib = load()
+        self.h = self.lib.orc_create(C.byref(case.dims), C.byref(case.params))
+        if not self.h:
+            raise RuntimeError("orc_create rejected the domain")
+        self._sp = case.static_ptrs()
+        assert self.lib.orc_bind_static(self.h, C.byref(self._sp)) == 0
+        self._st = case.state_ptrs()
+        assert self.lib.orc_set_state(self.h, C.byref(self._st)) == 0
+        self._bp = case.bdy_ptrs()
+        if case.params.do_apply_bdy:
+            assert self.lib.orc_set_boundary(self.h, C.byref(self._bp), case.xbctime,
+                                             case.params.dtbdys) == 0
+
+    def step(self, n=1):
+        d = abi.mlc_diag()
+        st = self.lib.orc_step(self.h, n, C.byref(d))
+        return st, d
+
+    def sound_only(self):
+        self.lib.orc_sound_only(self.h)
+
+    def state(self) -> dict:
+        out = self.case.empty_state()
+        sp = self.case.state_ptrs_of(out)
+        self.lib.orc_get_state(self.h, C.byref(sp))
+        return out
+
+    def work(self, which: int, shape):
+        a = np.zeros(shape, order="F")
+        self.lib.orc_get_work(self.h, which, abi.dptr(a))
+        return a
+
+    def close(self):
+        if self.h:
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

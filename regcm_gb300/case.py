@@ -1,0 +1,345 @@
+"""Synthetic MOLOCH domains: the stand-in for RegCM's terrain and ICBC input.
+
+RegCM reads its terrain and initial/boundary conditions from netCDF files made
+by its preprocessors; none exist here, so a ``Case`` builds the same arrays in
+memory from a seeded recipe:
+
+* Cartesian grid, map factors 1, f-plane at 45N, model top 25 km, uniform
+  zita spacing (Share/mod_zita.F90:54-86), mo_h = 8 km, mo_a0 = 0.
+* Gaussian hills h0*exp(-ln2*(r/(10 dx))^2) sampled at cross, u and v points
+  and stored as geopotential (Main/mod_params.F90:2436-2440).
+* US standard atmosphere T(z) and hydrostatic pressure (Share/mod_isaatm.F90:
+  27-69) at the terrain-following levels, Exner function by paicompute
+  (Main/mod_bdycod.F90:3762-3796), theta_v perturbed by seeded uniform noise.
+* Boundary data b0 = b1 = the initial state; the prognostic state is derived
+  from b0 the way init does (Main/mod_init.F90:155-219).
+* Lehmann relaxation weights (bdy_use_lehmann = .true.), top nudging on,
+  spectral nudging off, divergence damping and filter on.
+
+Static fields come from the library's own host setup (moloch_gb300_setup.h).
+Every array is a Fortran-ordered float64 numpy array with the extents of
+include/moloch_gb300.h.  Random numbers come from SplitMix64 so any consumer
+(the GPU library, the CPU oracle) sees identical bytes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+# Share/mod_constants.F90 (non-RCEMIP), the values of mlc_constants.h
+GRAV = 9.80665
+RGAS = ((6.02214076e23 * 1.3806490e-23) / 28.96454) * 1000.0
+CPD = 3.5 * RGAS
+EP1 = 28.96454 / 18.01528 - 1.0
+P00 = 1.0e5
+STDP = 1.013250e5
+STDT = 288.15
+LRATE = 0.00649
+CPOVR = CPD / RGAS
+
+
+def splitmix64(seed: int, n: int) -> np.ndarray:
+    """n uniform doubles in [0, 1) from SplitMix64 started at `seed`."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + \
+            np.arange(1, n + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def isa(height):
+    """US standard atmosphere T [K], p [Pa] for heights 0-32 km (mod_isaatm)."""
+    h = np.asarray(height, dtype=np.float64)
+    g_rl = GRAV / (RGAS * LRATE)
+    t11 = STDT - LRATE * 11000.0
+    p11 = STDP * (t11 / STDT) ** g_rl
+    p20 = p11 * np.exp(-GRAV * (20000.0 - 11000.0) / (RGAS * t11))
+    t = np.where(h <= 11000.0, STDT - LRATE * h,
+                 np.where(h <= 20000.0, t11, t11 + 0.001 * (h - 20000.0)))
+    p_low = STDP * (np.maximum(t, 1.0) / STDT) ** g_rl
+    p_mid = p11 * np.exp(-GRAV * (h - 11000.0) / (RGAS * t11))
+    p_up = p20 * (t / t11) ** (-(GRAV / (RGAS * 0.001)))
+    p = np.where(h <= 11000.0, p_low, np.where(h <= 20000.0, p_mid, p_up))
+    return t, p
+
+
+def pfwsat(t, p):
+    """Saturation mixing ratio through the library's own restatement."""
+    t = np.asfortranarray(t, dtype=np.float64)
+    p = np.asfortranarray(p, dtype=np.float64)
+    out = np.empty_like(t, order="F")
+    abi.check(abi.load().mlc_pfwsat(t.size, abi.dptr(t), abi.dptr(p), abi.dptr(out)), "mlc_pfwsat")
+    return out
+
+
+def _f(shape):
+    return np.zeros(shape, dtype=np.float64, order="F")
+
+
+@dataclass
+class Case:
+    """One domain: extents, run parameters, static fields, state, boundary."""
+    name: str
+    dims: abi.mlc_dims
+    params: abi.mlc_params
+    static: dict = field(default_factory=dict)
+    state: dict = field(default_factory=dict)
+    bdy: dict = field(default_factory=dict)
+    xbctime: float = 0.0
+
+    @property
+    def points(self) -> int:
+        """Cross points x levels: the grid points one model step advances."""
+        d = self.dims
+        return (d.jx - 1) * (d.iy - 1) * d.kz
+
+    # -- pointer structs (arrays stay owned by this object) ---------------
+    def static_ptrs(self) -> abi.mlc_static_ptrs:
+        s = abi.mlc_static_ptrs()
+        for n in abi.STATIC_FIELDS:
+            setattr(s, n, abi.dptr(self.static.get(n)))
+        for n in abi.IBND_FIELDS:
+            setattr(s, n, abi.iptr(self.static[n]))
+        return s
+
+    @staticmethod
+    def state_ptrs_of(state: dict) -> abi.mlc_state_ptrs:
+        s = abi.mlc_state_ptrs()
+        for n in abi.STATE_FIELDS:
+            setattr(s, n, abi.dptr(state.get(n)))
+        return s
+
+    def state_ptrs(self) -> abi.mlc_state_ptrs:
+        return self.state_ptrs_of(self.state)
+
+    def bdy_ptrs(self) -> abi.mlc_bdy_ptrs:
+        b = abi.mlc_bdy_ptrs()
+        for n in abi.BDY_FIELDS:
+            pair = self.bdy.get(n, (None, None))
+            arr = (C.POINTER(C.c_double) * 2)(abi.dptr(pair[0]), abi.dptr(pair[1]))
+            setattr(b, n, arr)
+        return b
+
+    def empty_state(self) -> dict:
+        """Arrays shaped like the state, for downloads."""
+        return {k: np.zeros_like(v, order="F") for k, v in self.state.items()}
+
+    def copy_state(self) -> dict:
+        return {k: np.array(v, order="F", copy=True) for k, v in self.state.items()}
+
+
+def default_params() -> abi.mlc_params:
+    p = abi.mlc_params()
+    abi.load().mlc_default_params(C.byref(p))
+    return p
+
+
+def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv: int = 1,
+          moist: bool = False, seed: int = 0, hills=None, wind=10.0, jet: bool = False,
+          theta_noise: float = 0.1, tracer: bool = False, precision: int = abi.MLC_PREC_FP64,
+          name: str = "case", debug_level: int = 1, lrotllr: bool = False,
+          apply_bdy: bool = True) -> Case:
+    """Build one synthetic domain of nx x ny cross points and kz levels."""
+    lib = abi.load()
+    jx, iy = nx + 1, ny + 1
+    nqx = 5 if moist else 2
+    ntr = 1 if tracer else 0
+    dims = abi.mlc_dims(jx, iy, kz, nqx, ntr)
+    p = default_params()
+    p.dtsec, p.dx = float(dt), float(dx)
+    p.mo_ztop, p.mo_h, p.mo_a0 = 25000.0, 8000.0, 0.0
+    p.mo_nadv, p.mo_nsound = nadv, nsound
+    p.mo_divdamp = p.mo_divfilter = p.mo_top_nudge = 1
+    p.mo_spectral_nudge = 0
+    p.do_apply_bdy = 1 if apply_bdy else 0
+    p.lrotllr = 1 if lrotllr else 0
+    p.ipptls = 2 if moist else 0
+    p.present_qc = 1 if moist else 0
+    p.present_qi = 1 if moist else 0
+    p.debug_level = debug_level
+    p.precision = precision
+    p.dtbdys = 6.0 * 3600.0
+    gx, gd = C.c_int(), C.c_int()
+    abi.check(lib.mlc_setup_nspg(jx, iy, dx / 1000.0, 1, 0, 0, C.byref(gx), C.byref(gd)),
+              "mlc_setup_nspg")
+    p.nspgx, p.nspgd = gx.value, gd.value
+
+    # ---- terrain (geopotential) at cross / u / v positions on (jx, iy) ----
+    xc = (np.arange(1, jx + 1) - 0.5) * dx
+    xd = (np.arange(1, jx + 1) - 1.0) * dx
+    yc = (np.arange(1, iy + 1) - 0.5) * dx
+    yd = (np.arange(1, iy + 1) - 1.0) * dx
+    if hills is None:
+        hills = [(0.5 * nx * dx, 0.5 * ny * dx, 500.0)]
+
+    def terrain(x, y):
+        X, Y = np.meshgrid(x, y, indexing="ij")
+        h = np.zeros_like(X)
+        for (cx, cy, h0) in hills:
+            r = np.hypot(X - cx, Y - cy)
+            h += h0 * np.exp(-math.log(2.0) * (r / (10.0 * dx)) ** 2)
+        return np.asfortranarray(h)
+
+    h_cross = terrain(xc, yc)
+    st = {}
+    st["ht"] = np.asfortranarray(h_cross * GRAV)
+    st["htu"] = np.asfortranarray(terrain(xd, yc) * GRAV)
+    st["htv"] = np.asfortranarray(terrain(xc, yd) * GRAV)
+    for n in ("msfu", "msfv", "msfx"):
+        st[n] = np.ones((jx, iy), dtype=np.float64, order="F")
+    st["ulat"] = np.full((jx, iy - 1), 45.0, order="F")
+    st["vlat"] = np.full((jx - 1, iy), 45.0, order="F")
+    st["rlat"] = np.full((iy,), 45.0, order="F")
+    zita, zitah = np.zeros(kz + 1), np.zeros(kz)
+    abi.check(lib.mlc_setup_levels(kz, p.mo_ztop, abi.dptr(zita), abi.dptr(zitah)),
+              "mlc_setup_levels")
+    st["zita"], st["zitah"] = zita, zitah
+    for n, shp in (("hx", (jx, iy - 1)), ("hy", (jx - 1, iy)), ("zeta", (jx - 1, iy - 1, kz)),
+                   ("fmz", (jx - 1, iy - 1, kz)), ("rfmzu", (jx, iy - 1, kz)),
+                   ("rfmzv", (jx - 1, iy, kz)), ("fmzf", (jx - 1, iy - 1, kz + 1)),
+                   ("zetaf", (jx - 1, iy - 1, kz + 1)), ("dz", (jx - 1, iy - 1, kz))):
+        st[n] = _f(shp)
+    abi.check(lib.mlc_setup_metric(C.byref(dims), C.byref(p), *[abi.dptr(st[n]) for n in (
+        "ht", "htu", "htv", "msfu", "msfv", "zita", "zitah", "hx", "hy", "zeta", "fmz",
+        "rfmzu", "rfmzv", "fmzf", "zetaf", "dz")]), "mlc_setup_metric")
+    st["hefc"] = _f((p.nspgx, kz))
+    st["fcx"] = _f((p.nspgx,))
+    st["tnudge"] = _f((kz,))
+    st["ffilt"] = _f((kz,))
+    st["gmeanz"] = _f((kz,))
+    abi.check(lib.mlc_setup_relaxation(C.byref(dims), C.byref(p), abi.dptr(st["zeta"]),
+                                       abi.dptr(st["hefc"]), abi.dptr(st["fcx"]),
+                                       abi.dptr(st["tnudge"]), abi.dptr(st["ffilt"]),
+                                       abi.dptr(st["gmeanz"])), "mlc_setup_relaxation")
+    for n, (lx, ly) in (("ibnd_cr", (0, 0)), ("ibnd_ud", (1, 0)), ("ibnd_vd", (0, 1))):
+        st[n] = np.zeros((jx, iy), dtype=np.int32, order="F")
+        abi.check(lib.mlc_setup_boundaries(jx, iy, lx, ly, p.nspgx, p.nspgd, abi.iptr(st[n])),
+                  "mlc_setup_boundaries")
+
+    # ---- atmosphere on cross points ----
+    rng_n = 0
+    cshape = (jx - 1, iy - 1, kz)
+    zabs = np.asfortranarray(h_cross[: jx - 1, : iy - 1, None] + st["zeta"])
+    t_isa, p_isa = isa(zabs)
+    t_isa = np.asfortranarray(t_isa)
+    _, ps_isa = isa(h_cross[: jx - 1, : iy - 1])
+    ps_isa = np.asfortranarray(ps_isa)
+    if moist:
+        noise = splitmix64(seed * 7919 + 1, int(np.prod(cshape))).reshape(cshape, order="F")
+        qv = 0.7 * pfwsat(t_isa, np.asfortranarray(p_isa)) * (1.0 + 0.1 * (noise - 0.5))
+        qv = np.asfortranarray(qv)
+    else:
+        qv = np.full(cshape, 1.0e-8, order="F")
+    pai = _f(cshape)
+    abi.check(lib.mlc_paicompute(C.byref(dims), C.byref(p), abi.dptr(ps_isa), abi.dptr(st["zeta"]),
+                                 abi.dptr(t_isa), abi.dptr(qv), abi.dptr(st["fmzf"]),
+                                 abi.dptr(zita), abi.dptr(pai)), "mlc_paicompute")
+    thv = t_isa * (1.0 + EP1 * qv) / pai
+    noise = splitmix64(seed * 7919 + 2, int(np.prod(cshape))).reshape(cshape, order="F")
+    inner = np.zeros(cshape, dtype=bool)
+    inner[1:-1, 1:-1, :] = True
+    thv = np.where(inner, thv + theta_noise * (2.0 * noise - 1.0), thv)
+    t_b = np.asfortranarray(thv * pai / (1.0 + EP1 * qv))
+
+    # winds: u on (jx, iy-1), v on (jx-1, iy)
+    if jet:
+        ly = (iy - 1) * dx
+        prof = 15.0 * np.sin(math.pi * yc[: iy - 1] / ly)
+        u_b = np.asfortranarray(np.broadcast_to(prof[None, :, None], (jx, iy - 1, kz)).copy())
+    else:
+        u_b = np.full((jx, iy - 1, kz), float(wind), order="F")
+    v_b = _f((jx - 1, iy, kz))
+
+    qx = _f((jx - 1, iy - 1, kz, nqx))
+    qx[..., 0] = qv
+    qc_b = None
+    qi_b = None
+    kk = np.arange(1, kz + 1)
+    J, I = np.meshgrid(np.arange(1, jx), np.arange(1, iy), indexing="ij")
+    if moist:
+        cen = splitmix64(seed * 7919 + 3, 3)
+        cj = 1 + p.nspgx + cen[0] * (nx - 2 * p.nspgx)
+        ci = 1 + p.nspgx + cen[1] * (ny - 2 * p.nspgx)
+        ck = kz - 4 - int(cen[2] * max(1, kz // 3))
+        patch = np.exp(-((J - cj) ** 2 + (I - ci) ** 2)[..., None] / (2 * 5.0 ** 2)
+                       - ((kk - ck) ** 2)[None, None, :] / (2 * 2.0 ** 2))
+        qc_b = np.asfortranarray(1.0e-4 * patch)
+        qi_b = _f(cshape)
+        qx[..., 1] = qc_b
+    trac = None
+    chib = None
+    if tracer:
+        cj, ci, ck = 0.5 * (jx - 1) + 0.5, 0.5 * (iy - 1) + 0.5, kz // 2
+        blob = np.exp(-((J - cj) ** 2 + (I - ci) ** 2)[..., None] / (2 * 5.0 ** 2)
+                      - ((kk - ck) ** 2)[None, None, :] / (2 * 2.0 ** 2))
+        trac = np.asfortranarray(blob[..., None])
+        chib = np.asfortranarray(trac.copy())
+
+    # ---- boundary data: b0 = b1 = initial fields ----
+    bdy = {
+        "xtb": (t_b, t_b), "xqb": (qv, qv), "xpaib": (pai, pai), "dub": (u_b, u_b),
+        "dvb": (v_b, v_b), "xpsb": (ps_isa, ps_isa),
+    }
+    if moist:
+        bdy["xlb"] = (qc_b, qc_b)
+        bdy["xib"] = (qi_b, qi_b)
+    if tracer:
+        bdy["chib"] = (chib, chib)
+
+    # ---- initial state from b0, Main/mod_init.F90:155-219 ----
+    tvirt = np.asfortranarray(t_b * (1.0 + EP1 * qv))
+    pres = np.asfortranarray(pai ** CPOVR * P00)
+    rho = np.asfortranarray(pres / (RGAS * t_b))
+    zk = st["zeta"][..., kz - 1]
+    psa = np.asfortranarray(pres[..., kz - 1] * np.exp(GRAV * zk / (RGAS * tvirt[..., kz - 1])))
+    state = {
+        "u": np.array(u_b, order="F"), "v": np.array(v_b, order="F"),
+        "w": _f((jx - 1, iy - 1, kz + 1)), "pai": np.array(pai, order="F"),
+        "tetav": np.asfortranarray(tvirt / pai), "t": np.array(t_b, order="F"),
+        "tvirt": tvirt, "ux": _f(cshape), "vx": _f(cshape), "p": pres, "rho": rho,
+        "qsat": pfwsat(t_b, pres), "qx": qx, "ps": psa,
+    }
+    if tracer:
+        state["trac"] = np.array(trac, order="F")
+    keep = {k: v for k, v in st.items()}
+    case = Case(name=name, dims=dims, params=p, static=keep, state=state, bdy=bdy)
+    return case
+
+
+# ---- the configurations of the benchmark suite ---------------------------
+
+def config0(nx=64, ny=64, kz=30, seed=0, **kw) -> Case:
+    """Plain dry dynamics: 64x64x30, dx 12 km, dt 60 s, 3 substeps, hill 500 m,
+    u = 10 m/s, theta noise +-0.1 K, one passive tracer blob."""
+    return build(nx, ny, kz, dx=12000.0, dt=60.0, nsound=3, moist=False, seed=seed,
+                 hills=[(0.5 * nx * 12000.0, 0.5 * ny * 12000.0, 500.0)], wind=10.0,
+                 theta_noise=0.1, tracer=True, name=f"c0_{nx}x{ny}x{kz}", **kw)
+
+
+def config1(nx=512, ny=512, kz=41, seed=1, **kw) -> Case:
+    """Moist convection-permitting: 512x512x41, dx 3 km, dt 20 s, 4 substeps,
+    3 seeded hills of 200-2000 m, qv at 70% RH, a qc patch, u jet 15 sin(y)."""
+    dx = 3000.0
+    r = splitmix64(seed * 104729 + 11, 9)
+    hills = []
+    for h in range(3):
+        cx = (0.2 + 0.6 * r[3 * h]) * nx * dx
+        cy = (0.2 + 0.6 * r[3 * h + 1]) * ny * dx
+        hills.append((cx, cy, 200.0 + 1800.0 * r[3 * h + 2]))
+    return build(nx, ny, kz, dx=dx, dt=20.0, nsound=4, moist=True, seed=seed, hills=hills,
+                 jet=True, theta_noise=0.1, tracer=False, name=f"c1_{nx}x{ny}x{kz}", **kw)
+
+
+def config2_member(m: int, nx=128, ny=128, kz=30, **kw) -> Case:
+    """Ensemble member m: config-0 recipe, theta noise +-0.5 K, wind U(5, 20)."""
+    wind = 5.0 + 15.0 * float(splitmix64(1000 + m, 1)[0])
+    return build(nx, ny, kz, dx=12000.0, dt=60.0, nsound=3, moist=False, seed=m,
+                 hills=[(0.5 * nx * 12000.0, 0.5 * ny * 12000.0, 500.0)], wind=wind,
+                 theta_noise=0.5, tracer=True, name=f"c2_m{m}", **kw)

@@ -1,0 +1,397 @@
+// mlc_advect.cu -- WAF flux-form advection of every advected field
+// (Main/mod_moloch.F90:767-1042, subroutines advection and wafone, with the
+// interpolations of :1445-1569 and local_flow_param :1571-1590).
+//
+//   adv_prep        u,v -> ux,vx (4th order, 2nd at the edges) and w -> wx.
+//   adv_vertical    per column and field: both vertical WAF passes
+//                   (do_vadvtwice) with the column in shared memory.
+//   adv_horizontal  per (32 x 8) tile, level and field: meridional then zonal
+//                   WAF.  The tile stages wz with a 2-point halo in shared
+//                   memory, builds the meridional fluxes and the intermediate
+//                   p0 on a 2-column halo, then the zonal fluxes and the
+//                   result, so each field is read and written once.  The
+//                   result goes to a second buffer because the halo columns
+//                   of a tile still need the field's old values.
+//   adv_curvature   curvature terms on ux, vx (skipped when they are zero at
+//                   every point: with uniform map factors the reference adds
+//                   an exact zero).
+//   adv_back        ux,vx -> u,v and wx -> w (4th order, 2nd at the edges).
+// Operand order follows the reference expression by expression.  The ratios
+// dtrdz*fmz/fmzf of the vertical passes are per-domain constants read from
+// arrays computed once with the same expression.
+#include "mlc_kernels.cuh"
+
+namespace mlc {
+
+namespace {
+
+constexpr int kTJ = 32, kTI = 8;
+
+// Main/mod_moloch.F90:1571-1590; minnum is the 4-byte real holding minden.
+template <class R> struct FlowEps;
+template <> struct FlowEps<double> {
+  static __device__ __forceinline__ double den() { return 1.0e-30; }
+  static __device__ __forceinline__ double num() { return (double)1.0e-30f; }
+};
+template <> struct FlowEps<float> {
+  static __device__ __forceinline__ float den() { return 1.0e-15f; }
+  static __device__ __forceinline__ float num() { return 1.0e-15f; }
+};
+
+template <class R>
+__device__ __forceinline__ R flow_param(R num, R den) {
+  if (fabs(den) < FlowEps<R>::den()) return fabs(num) < FlowEps<R>::num() ? R(1) : R(0);
+  return num / den;
+}
+
+// b = max(0, min(2, max(r, min(2r, 1)))) then zphi = is + zamu*b - is*b
+template <class R>
+__device__ __forceinline__ R waf_phi(R is, R zamu, R r) {
+  R m = fmin(R(2) * r, R(1));
+  R b = fmax(R(0), fmin(R(2), fmax(r, m)));
+  return is + zamu * b - is * b;
+}
+
+template <class R>
+__global__ void k_adv_prep(Geom g, const R *__restrict__ u, const R *__restrict__ v,
+                           const R *__restrict__ w, R *__restrict__ ux, R *__restrict__ vx,
+                           R *__restrict__ wx) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  if (j > jx - 1 || i > iy - 1) return;
+  const size_t ij = g.at2(j, i), PS = g.PS, S = (size_t)g.P;
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    // uvstagtouvx :1535-1549
+    R a;
+    if (j == 1) a = R(0.5) * (u[o] + u[o + 1]);
+    else if (j == jx - 1) a = R(0.5) * (u[o + 1] + u[o]);
+    else a = R(0.5625) * (u[o + 1] + u[o]) - R(0.0625) * (u[o + 2] + u[o - 1]);
+    ux[o] = a;
+    // :1553-1566
+    if (i == 1) a = R(0.5) * (v[o] + v[o + S]);
+    else if (i == iy - 1) a = R(0.5) * (v[o + S] + v[o]);
+    else a = R(0.5625) * (v[o + S] + v[o]) - R(0.0625) * (v[o + 2 * S] + v[o - S]);
+    vx[o] = a;
+    // zstagtoh :1445-1459
+    if (k == 1) a = R(0.5) * (w[o + PS] + w[o]);
+    else if (k == kz) a = R(0.5) * (w[o + PS] + w[o]);
+    else a = R(0.5625) * (w[o + PS] + w[o]) - R(0.0625) * (w[o + 2 * PS] + w[o - PS]);
+    wx[o] = a;
+  }
+}
+
+// Two vertical WAF passes for one column of one field (:858-922).
+template <class R>
+__global__ void k_adv_vertical(Geom g, Scal c, Stat<R> sa, const R *__restrict__ s, AdvTable<R> t) {
+  extern __shared__ unsigned char smem_raw[];
+  R *smem = reinterpret_cast<R *>(smem_raw);
+  const int nth = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int kz = g.kz;
+  R *col = smem;                                 // field column, levels 1..kz
+  R *flx = smem + (size_t)(kz + 2) * nth;        // wfw, interfaces 1..kz+1
+  R *sc = smem + (size_t)2 * (kz + 2) * nth;     // s, levels 1..kz+1
+#define COL(a, k) a[(size_t)(k) * nth + tid]
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int f = blockIdx.z;
+  if (j > g.jx - 1 || i > g.iy - 1) return;
+  const size_t ij = g.at2(j, i), PS = g.PS;
+  const R dtrdz = R(0.5) * (R(c.dtstepa) * R(c.rdzita));
+  const R *src = t.cur[f];
+  for (int k = 1; k <= kz; ++k) COL(col, k) = src[ij + (size_t)(k - 1) * PS];
+  for (int k = 1; k <= kz + 1; ++k) COL(sc, k) = s[ij + (size_t)(k - 1) * PS];
+  for (int pass = 0; pass < 2; ++pass) {
+    COL(flx, 1) = R(0);
+    COL(flx, kz + 1) = R(0);
+    for (int k = 1; k <= kz - 1; ++k) {
+      const R skp = COL(sc, k + 1);
+      const R zamu = skp * dtrdz;
+      R is;
+      int k1, k1p1;
+      if (zamu >= R(0)) {
+        is = R(1); k1 = k + 1; k1p1 = k1 + 1;
+        if (k1p1 > kz) k1p1 = kz;
+      } else {
+        is = R(-1); k1 = k - 1; k1p1 = k;
+        if (k1 < 1) k1 = 1;
+      }
+      const R r = flow_param<R>(COL(col, k1) - COL(col, k1p1), COL(col, k) - COL(col, k + 1));
+      const R zphi = waf_phi<R>(is, zamu, r);
+      COL(flx, k + 1) = R(0.5) * skp * ((R(1) + zphi) * COL(col, k + 1) + (R(1) - zphi) * COL(col, k));
+    }
+    for (int k = 1; k <= kz; ++k) {
+      const size_t o = ij + (size_t)(k - 1) * PS;
+      const R zrfmu = sa.zrfmu[o];
+      const R zrfmd = sa.zrfmd[o];
+      const R pk = COL(col, k);
+      const R zdv = (COL(sc, k) * zrfmu - COL(sc, k + 1) * zrfmd) * pk;
+      COL(col, k) = pk - COL(flx, k) * zrfmu + COL(flx, k + 1) * zrfmd + zdv;
+    }
+  }
+  R *dst = t.wz[f];
+  for (int k = 1; k <= kz; ++k) dst[ij + (size_t)(k - 1) * PS] = COL(col, k);
+#undef COL
+}
+
+// Meridional then zonal WAF for one tile (:984-1038; ROTLLR :926-983).
+template <class R>
+__global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Stat<R> sa,
+                                                            const R *__restrict__ u,
+                                                            const R *__restrict__ v, AdvTable<R> t) {
+  constexpr int WJ = kTJ + 4;  // columns J0-2 .. J0+TJ+1
+  __shared__ R wz_s[kTI + 4][WJ];      // rows I0-2 .. I0+TI+1
+  __shared__ R zpby_s[kTI + 1][WJ];    // rows I0 .. I0+TI
+  __shared__ R p0_s[kTI][WJ];          // rows I0 .. I0+TI-1
+  __shared__ R zpbw_s[kTI][kTJ + 1];   // columns J0 .. J0+TJ
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  const int nf = t.n;
+  const int f = blockIdx.z % nf;
+  const int k = blockIdx.z / nf + 1;
+  const int J0 = blockIdx.x * kTJ + 1, I0 = blockIdx.y * kTI + 1;
+  const int tid = threadIdx.y * kTJ + threadIdx.x;
+  const int nth = kTJ * kTI;
+  const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
+  const R *pp = t.cur[f] + ko;
+  const R *wz = t.wz[f] + ko;
+  R *out = t.out[f] + ko;
+  const R *uk = u + ko;
+  const R *vk = v + ko;
+  const R dta = R(c.dtstepa);
+  const R dtrdx = dta * R(c.rdx), dtrdy = dta * R(c.rdx);
+  const bool rot = c.lrotllr != 0;
+  const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
+  (void)kz;
+
+  // stage wz (cross points only; others are never read for valid outputs)
+  for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
+    const int rr = e / WJ, cc = e % WJ;
+    const int i = I0 - 2 + rr, j = J0 - 2 + cc;
+    R x = R(0);
+    if (i >= 1 && i <= iy - 1 && j >= 1 && j <= jx - 1) x = wz[g.at2(j, i)];
+    wz_s[rr][cc] = x;
+  }
+  __syncthreads();
+  // meridional fluxes zpby(j,i): j in jce, i in ici1..ice2
+  for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
+    const int rr = e / WJ, cc = e % WJ;
+    const int i = I0 + rr, j = J0 - 2 + cc;
+    R x = R(0);
+    if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 1) {
+      const size_t ij = g.at2(j, i);
+      const R vv = vk[ij];
+      const R zamu = rot ? vv * dtrdy : vv * sa.msfv[ij] * dtrdy;
+      R is;
+      int ih;
+      if (zamu > R(0)) { is = R(1); ih = i - 1; }
+      else { is = R(-1); ih = min(i + 1, imax); }
+      const int ihm1 = max(ih - 1, imin);
+      // shared-memory row of global row i is i - (I0 - 2)
+      const int b = 2 - I0;
+      const R r = flow_param<R>(wz_s[ih + b][cc] - wz_s[ihm1 + b][cc], wz_s[i + b][cc] - wz_s[i - 1 + b][cc]);
+      const R zphi = waf_phi<R>(is, zamu, r);
+      x = R(0.5) * vv * ((R(1) + zphi) * wz_s[i - 1 + b][cc] + (R(1) - zphi) * wz_s[i + b][cc]);
+    }
+    zpby_s[rr][cc] = x;
+  }
+  __syncthreads();
+  // p0(j,i): j in jce, i in ici
+  for (int e = tid; e < kTI * WJ; e += nth) {
+    const int rr = e / WJ, cc = e % WJ;
+    const int i = I0 + rr, j = J0 - 2 + cc;
+    R x = R(0);
+    if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
+      const size_t ij = g.at2(j, i), ijN = ij + (size_t)g.P;
+      const R fz = sa.fmz[ko + ij];
+      const R ppk = pp[ij];
+      const R wzk = wz_s[rr + 2][cc];
+      if (rot) {
+        const R zhxvtn = dtrdy * sa.rmv[ijN] * sa.msfx[ij];
+        const R zhxvts = dtrdy * sa.rmv[ij] * sa.msfx[ij];
+        const R zrfmn = zhxvtn * fz * sa.rfmzv[ko + ijN];
+        const R zrfms = zhxvts * fz * sa.rfmzv[ko + ij];
+        const R zdv = (vk[ijN] * zrfmn - vk[ij] * zrfms) * ppk;
+        x = wzk + (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
+      } else {
+        // rfmzu as in the reference (Main/mod_moloch.F90:1000-1001)
+        const R zrfmn = dtrdy * fz * sa.rfmzu[ko + ijN];
+        const R zrfms = dtrdy * fz * sa.rfmzu[ko + ij];
+        const R zdv = (vk[ijN] * sa.rmv[ijN] * zrfmn - vk[ij] * sa.rmv[ij] * zrfms) * ppk;
+        x = wzk + sa.mx2[ij] * (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
+      }
+    }
+    p0_s[rr][cc] = x;
+  }
+  __syncthreads();
+  // zonal fluxes zpbw(j,i): j in jci1..jce2, i in ici
+  for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
+    const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
+    const int i = I0 + rr, j = J0 + cc;
+    R x = R(0);
+    if (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
+      const size_t ij = g.at2(j, i);
+      const R uu = uk[ij];
+      const R zamu = uu * sa.msfu[ij] * dtrdx;
+      R is;
+      int jh;
+      if (zamu > R(0)) { is = R(1); jh = j - 1; }
+      else { is = R(-1); jh = min(j + 1, jmax); }
+      const int jhm1 = max(jh - 1, jmin);
+      const int b = 2 - J0;  // p0_s column of global column j is j - (J0 - 2)
+      const R r = flow_param<R>(p0_s[rr][jh + b] - p0_s[rr][jhm1 + b], p0_s[rr][j + b] - p0_s[rr][j - 1 + b]);
+      const R zphi = waf_phi<R>(is, zamu, r);
+      x = R(0.5) * uu * ((R(1) + zphi) * p0_s[rr][j - 1 + b] + (R(1) - zphi) * p0_s[rr][j + b]);
+    }
+    zpbw_s[rr][cc] = x;
+  }
+  __syncthreads();
+  // result on the tile: interior update, ring copied
+  {
+    const int rr = threadIdx.y, cc = threadIdx.x;
+    const int i = I0 + rr, j = J0 + cc;
+    if (i <= iy - 1 && j <= jx - 1) {
+      const size_t ij = g.at2(j, i);
+      const R ppk = pp[ij];
+      R x = ppk;
+      if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
+        const R fz = sa.fmz[ko + ij];
+        const R p0k = p0_s[rr][cc + 2];
+        if (rot) {
+          const R zcostx = dtrdx * sa.msfx[ij];
+          const R zrfmw = zcostx * fz * sa.rfmzu[ko + ij];
+          const R zrfme = zcostx * fz * sa.rfmzu[ko + ij + 1];
+          const R zdv = (uk[ij + 1] * zrfme - uk[ij] * zrfmw) * ppk;
+          x = p0k + zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv;
+        } else {
+          const R zrfmw = dtrdx * fz * sa.rfmzu[ko + ij];
+          const R zrfme = dtrdx * fz * sa.rfmzu[ko + ij + 1];
+          const R zdv = (uk[ij + 1] * sa.rmu[ij + 1] * zrfme - uk[ij] * sa.rmu[ij] * zrfmw) * ppk;
+          x = p0k + sa.mx2[ij] * (zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv);
+        }
+      }
+      out[ij] = x;
+    }
+  }
+}
+
+// :809-825
+template <class R>
+__global__ void k_adv_curvature(Geom g, Scal c, Stat<R> sa, R *__restrict__ ux, R *__restrict__ vx) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (j > g.jx - 2 || i > g.iy - 2) return;
+  const size_t ij = g.at2(j, i);
+  const R dta = R(c.dtstepa);
+  R tanx, tany;
+  if (c.lrotllr) {
+    const double dlat = kDegrad * 0.5 * (sa.rlat[i - 1] + sa.rlat[i]);
+    tanx = R(sin(dlat)) * sa.msfx[ij] * R(kRearthRad);
+    tany = tanx;
+  } else {
+    tanx = (sa.msfu[ij - 1] - sa.msfu[ij]) * R(c.rdx);
+    tany = (sa.msfv[ij - (size_t)g.P] - sa.msfv[ij]) * R(c.rdx);
+  }
+  for (int k = 1; k <= g.kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * g.PS;
+    R a = ux[o];
+    const R b = vx[o];
+    a = a + a * b * tanx * dta;
+    ux[o] = a;
+    vx[o] = b - a * a * tany * dta;
+  }
+}
+
+// uvxtouvstag :1477-1522 and htozstag :1461-1475
+template <class R>
+__global__ void k_adv_back(Geom g, const R *__restrict__ ux, const R *__restrict__ vx,
+                           const R *__restrict__ wx, R *__restrict__ u, R *__restrict__ v,
+                           R *__restrict__ w) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  if (j > jx || i > iy) return;
+  const size_t ij = g.at2(j, i), PS = g.PS, S = (size_t)g.P;
+  const bool do_u = (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2);
+  const bool do_v = (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 1);
+  const bool do_w = (j <= jx - 1 && i <= iy - 1);
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    if (do_u) {
+      R a;
+      if (j == jx - 1) a = R(0.5) * (ux[o - 1] + ux[o]);
+      else if (j == 2) a = R(0.5) * (ux[o] + ux[o - 1]);
+      else a = R(0.5625) * (ux[o] + ux[o - 1]) - R(0.0625) * (ux[o + 1] + ux[o - 2]);
+      u[o] = a;
+    }
+    if (do_v) {
+      R a;
+      if (i == iy - 1) a = R(0.5) * (vx[o - S] + vx[o]);
+      else if (i == 2) a = R(0.5) * (vx[o] + vx[o - S]);
+      else a = R(0.5625) * (vx[o] + vx[o - S]) - R(0.0625) * (vx[o + S] + vx[o - 2 * S]);
+      v[o] = a;
+    }
+    if (do_w && k >= 2) {
+      R a;
+      if (k == 2) a = R(0.5) * (wx[o] + wx[o - PS]);
+      else if (k == kz) a = R(0.5) * (wx[o] + wx[o - PS]);
+      else a = R(0.5625) * (wx[o] + wx[o - PS]) - R(0.0625) * (wx[o + PS] + wx[o - 2 * PS]);
+      w[o] = a;
+    }
+  }
+}
+
+inline dim3 grid2(int nj, int ni, dim3 b) {
+  return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y));
+}
+
+}  // namespace
+
+template <class R>
+void Launch<R>::adv_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
+  const dim3 b(32, 4);
+  k_adv_prep<R><<<grid2(g.jx - 1, g.iy - 1, b), b, 0, s>>>(g, st.u, st.v, st.w, st.ux, st.vx, wk.wx);
+}
+
+template <class R>
+void Launch<R>::adv_vertical(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
+                             const AdvTable<R> &t, cudaStream_t s) {
+  const dim3 b(32, 2);
+  const size_t smem = (size_t)3 * (g.kz + 2) * b.x * b.y * sizeof(R);
+  dim3 grd = grid2(g.jx - 1, g.iy - 1, b);
+  grd.z = (unsigned)t.n;
+  k_adv_vertical<R><<<grd, b, smem, s>>>(g, c, sa, wk.s, t);
+}
+
+template <class R>
+void Launch<R>::adv_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                               const AdvTable<R> &t, cudaStream_t s) {
+  dim3 grd((unsigned)((g.jx - 1 + kTJ - 1) / kTJ), (unsigned)((g.iy - 1 + kTI - 1) / kTI),
+           (unsigned)(t.n * g.kz));
+  k_adv_horizontal<R><<<grd, dim3(kTJ, kTI), 0, s>>>(g, c, sa, st.u, st.v, t);
+}
+
+template <class R>
+void Launch<R>::adv_curvature(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                              cudaStream_t s) {
+  const dim3 b(32, 4);
+  k_adv_curvature<R><<<grid2(g.jx - 3, g.iy - 3, b), b, 0, s>>>(g, c, sa, st.ux, st.vx);
+}
+
+template <class R>
+void Launch<R>::adv_back(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
+  const dim3 b(32, 4);
+  k_adv_back<R><<<grid2(g.jx, g.iy, b), b, 0, s>>>(g, st.ux, st.vx, wk.wx, st.u, st.v, st.w);
+}
+
+template <class R>
+cudaError_t Launch<R>::configure_advect() {
+  return cudaFuncSetAttribute(k_adv_vertical<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              200 * 1024);
+}
+
+template struct Launch<double>;
+template struct Launch<float>;
+
+}  // namespace mlc

@@ -1,0 +1,106 @@
+// mlc_constants.h -- physical constants of the MOLOCH path.
+//
+// Values and derivations of Share/mod_constants.F90 (non-RCEMIP build):
+// egrav :107, boltzk :115, navgdr :117, amd :130, amw :132, rgasmol :153,
+// rgas :161, cpd :181, cvd :185, derived ratios :225-233, tzero :241,
+// p00 :273, lrate :282, pi :301, degrad :307, earth radius :350-355,
+// rotation :358-360, ep1/ep2 :383-386.  Each derived value is the same IEEE
+// double operation the Fortran parameter expression performs, so host and
+// device code see bit-identical constants.
+#pragma once
+
+#ifdef __CUDACC__
+#define MLC_HD __host__ __device__
+#else
+#define MLC_HD
+#endif
+
+namespace mlc {
+
+constexpr double kGrav = 9.80665;
+constexpr double kBoltz = 1.3806490e-23;
+constexpr double kAvogadro = 6.02214076e23;
+constexpr double kAmd = 28.96454;
+constexpr double kAmw = 18.01528;
+constexpr double kRgasMol = kAvogadro * kBoltz;
+constexpr double kRgas = (kRgasMol / kAmd) * 1000.0;
+constexpr double kCpd = 3.5 * kRgas;
+constexpr double kCvd = 2.5 * kRgas;
+constexpr double kRegrav = 1.0 / kGrav;
+constexpr double kRcpd = 1.0 / kCpd;
+constexpr double kRovcp = kRgas * kRcpd;
+constexpr double kRdrcv = kRgas / kCvd;
+constexpr double kCpovr = kCpd / kRgas;
+constexpr double kGovr = kGrav / kRgas;
+constexpr double kGovcp = kGrav / kCpd;
+constexpr double kTzero = 273.15;
+constexpr double kP00 = 1.000000e5;
+constexpr double kLrate = 0.00649;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kDegrad = kPi / 180.0;
+constexpr double kEarthRad = 6.371229e6;
+constexpr double kRearthRad = 1.0 / kEarthRad;
+constexpr double kOmega2 = 2.0 * 7.2921159e-5;
+constexpr double kEp1 = kAmd / kAmw - 1.0;
+constexpr double kEp2 = kAmw / kAmd;
+
+// Main/mpplib/mod_runparams.F90:184-192 (qv, qc, qi, qr, qs, qg, qh, ...):
+// values below qxcheckval(n) are reset to qxzeroval(n) (0-based n here).
+MLC_HD inline double qx_check(int n) {
+  switch (n) {
+    case 0: return 1.0e-8;
+    case 7: return 1.0e10;
+    case 8: return 100.0;
+    case 9: return 0.01;
+    default: return 1.0e-16;
+  }
+}
+MLC_HD inline double qx_zero(int n) {
+  switch (n) {
+    case 0: return 1.0e-8;
+    case 7: return 1.0e10;
+    case 8: return 100.0;
+    case 9: return 0.01;
+    default: return 0.0;
+  }
+}
+
+// Height above which top nudging and the w sponge act (Main/mod_bdycod.F90:121).
+constexpr double kZzTop = 18000.0;
+// Sponge amplitude (Main/mod_init.F90:62).
+constexpr double kZfiltFac = 0.8;
+// Base damping coefficients (Main/mod_moloch.F90:147-148).
+constexpr double kNuMax = 0.125;
+constexpr double kDdamp = 0.850;
+
+// Flatau saturation mixing ratio in kg/kg, Share/pfwsat.inc:1-43.  The
+// polynomial is evaluated in Horner form from the highest coefficient, the
+// same nesting as the reference.
+MLC_HD inline double pfwsat(double t, double p) {
+  double td = t - kTzero;
+  td = td < -75.0 ? -75.0 : td;
+  td = td > 100.0 ? 100.0 : td;
+  double es;
+  if (td >= 0.0) {
+    es = 0.611213476e+03 + td * (0.444007856e+02 + td * (0.143064234e+01 +
+         td * (0.264461437e-01 + td * (0.305903558e-03 + td * (0.196237241e-05 +
+         td * (0.892344772e-08 + td * (-0.373208410e-10 + td * 0.209339997e-13)))))));
+  } else {
+    es = 0.611123516e+03 + td * (0.503109514e+02 + td * (0.188369801e+01 +
+         td * (0.420547422e-01 + td * (0.614396778e-03 + td * (0.602780717e-05 +
+         td * (0.387940929e-07 + td * (0.149436277e-09 + td * 0.262655803e-12)))))));
+  }
+  double cap = 0.15 * p;
+  es = cap < es ? cap : es;
+  return kEp2 * (es / (p - es));
+}
+
+// G(zeta) of Share/mod_zita.F90:105-115.
+MLC_HD inline double gzita(double zita, double ztop, double a0) {
+  double r = zita / ztop;
+  double r2 = r * r;
+  double r3 = r2 * r;
+  return ((0.0 - 1.0 * a0) * r - (3.0 - 2.0 * a0) * r2 + (2.0 - 1.0 * a0) * r3) + 1.0;
+}
+
+}  // namespace mlc

@@ -1,0 +1,97 @@
+// mlc_device.cuh -- device-side data layout and parameter blocks.
+//
+// Layout in HBM.  Every 3-D field of a domain, whatever its staggering, is
+// stored as planes of iy rows x P columns (P = jx rounded up to 128 bytes),
+// j fastest, then i, then k: element (j,i,k) of the reference's 1-based
+// arrays sits at (j-1) + (i-1)*P + (k-1)*P*iy.  Cross-point fields leave
+// column jx and row iy unused.  Rows start on 128-byte boundaries, so a warp
+// reading 32 consecutive j is one or two full cache lines, and one pitch and
+// plane stride serve every field of the domain.  w and fmzf hold kz+1 planes;
+// species arrays (qx, trac) are consecutive kz-plane blocks.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "mlc_constants.h"
+
+namespace mlc {
+
+struct Geom {
+  int jx, iy, kz, nqx, ntr;
+  int P;        // row pitch in elements
+  size_t PS;    // plane stride = P*iy
+  __host__ __device__ size_t at(int j, int i, int k) const {
+    return (size_t)(j - 1) + (size_t)(i - 1) * (size_t)P + (size_t)(k - 1) * PS;
+  }
+  __host__ __device__ size_t at2(int j, int i) const {
+    return (size_t)(j - 1) + (size_t)(i - 1) * (size_t)P;
+  }
+  __host__ __device__ size_t field3() const { return PS * (size_t)kz; }
+};
+
+// Scalars of one domain (all derived on the host once, in FP64).
+struct Scal {
+  double dx, rdx, dtsec, dt, dtstepa, dtsound, rdzita, dtbdys, rtb;
+  int nadv, nsound, divdamp, divfilter, top_nudge, apply_bdy, lrotllr, ipptls;
+  int present_qc, present_qi, nspgx, nztop, debug_level;
+  int hb_cr, hb_ud, hb_vd;  // relaxation zone non-empty (ba%havebound)
+  int curvature;            // curvature terms are not identically zero
+};
+
+// Time-invariant device arrays.  Metric arrays use the field type R.
+template <class R>
+struct Stat {
+  const R *fmz, *fmzf, *rfmzu, *rfmzv;   // 3-D
+  const R *zrfmu, *zrfmd;                // 3-D: (dtrdz*fmz)/fmzf(k), /fmzf(k+1)
+  const double *zeta, *dz;               // 3-D, FP64 (surface pressure, budget)
+  const R *hx, *hy;                      // 2-D
+  const R *msfu, *msfv, *msfx, *mx2, *rmu, *rmv, *coru, *corv;  // 2-D
+  const int32_t *ibnd_cr, *ibnd_ud, *ibnd_vd;                   // 2-D
+  const double *hefc;      // (nspgx, kz)
+  const double *fcx;       // (nspgx)
+  const double *tnudge, *ffilt, *gzitakh, *xkdamp, *xknu;      // (kz), 1-based via [k-1]
+  const double *gzitak;    // (kz+1)
+  const double *rlat;      // (iy)
+};
+
+// Prognostic and diagnostic state.
+template <class R>
+struct State {
+  R *u, *v, *w, *pai, *tetav, *t, *tvirt, *ux, *vx, *p, *rho, *qsat;
+  R *qx, *trac;  // species blocks
+  double *ps;    // 2-D, FP64
+};
+
+// Boundary data b0/b1 for one domain.
+template <class R>
+struct Bdy {
+  const R *xtb[2], *xqb[2], *xpaib[2], *xlb[2], *xib[2], *dub[2], *dvb[2], *chib[2];
+  const double *xpsb[2];
+};
+
+// Per-step device scratch that kernels of one step share.
+template <class R>
+struct Work {
+  R *s;        // (kz+1) planes
+  R *zdiv2;    // raw divergence (kz planes)
+  R *tetavf;   // (kz+1) planes, levels 2..kz used
+  R *u2, *v2;  // second buffers of the acoustic ping-pong
+  R *wx;       // w at half levels
+};
+
+// Boundary clock kept on the device so a captured step graph stays valid.
+struct Clock {
+  double xbctime;
+  int nonfinite;     // sticky: set when a non-finite ps is seen
+  int bad_step;      // step counter value at the first non-finite ps
+  int step;          // steps completed since the last reset
+  int pad;
+};
+
+// Mass budget and ps extrema of the last step (FP64).
+struct DiagDev {
+  double drymass, dryadv, qmass, qadv, ps_max, ps_min;
+  int nonfinite, pad;
+};
+
+}  // namespace mlc

@@ -1,0 +1,531 @@
+// mlc_end.cu -- the end of the MOLOCH step (Main/mod_moloch.F90:340-446):
+// virtual temperature and temperature, lateral boundary conditions
+// (boundary :448-529 with bdyval, motopnudge, morelax of Main/mod_bdycod.F90
+// and the tracer ring/relaxation of Main/chemlib/mod_che_bdyco.F90),
+// pressure, density and saturation diagnostics, surface pressure
+// extrapolation, status_update with zero tendencies, the mass budget of
+// Main/mod_massck.F90 and the NaN/Inf check on ps.
+//
+// The boundary clock lives on the device: bdyval blends with xbctime, then
+// the reference advances it by dtsec (Main/mod_bdycod.F90:2653) before
+// motopnudge and morelax blend again, so those read xbctime + dtsec; the
+// final reduction kernel stores the advanced clock.
+#include "mlc_kernels.cuh"
+
+namespace mlc {
+
+namespace {
+
+template <class R>
+__device__ __forceinline__ R qfactor(const R *qx, size_t o, size_t F, int ipptls) {
+  if (ipptls > 1) return R(1) + R(kEp1) * qx[o] - qx[o + F] - qx[o + 2 * F] - qx[o + 3 * F] - qx[o + 4 * F];
+  if (ipptls == 1) return R(1) + R(kEp1) * qx[o] - qx[o + F];
+  return R(1) + R(kEp1) * qx[o];
+}
+
+// dynamical_core :1121-1123 and tvirt_to_temp :1629-1648
+template <class R>
+__global__ void k_end_tvirt(Geom g, Scal c, State<R> st) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (j > g.jx - 1 || i > g.iy - 1) return;
+  const bool inner = j >= 2 && j <= g.jx - 2 && i >= 2 && i <= g.iy - 2;
+  const size_t ij = g.at2(j, i), F = g.field3();
+  for (int k = 1; k <= g.kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * g.PS;
+    const R tv = st.tetav[o] * st.pai[o];
+    st.tvirt[o] = tv;
+    if (inner) st.t[o] = tv / qfactor(st.qx, o, F, c.ipptls);
+  }
+}
+
+// bdyval, MOLOCH branch (Main/mod_bdycod.F90:1631-1860).  Phase 0 does the
+// west/east columns (corners excluded), phase 1 the south/north rows
+// (corners included), which read the corner values phase 0 left.
+template <class R>
+__global__ void k_bdy_ring(Geom g, Scal c, State<R> st, Bdy<R> bd, const Clock *clk, int phase) {
+  const int jx = g.jx, iy = g.iy;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;  // position along the side
+  const int k = blockIdx.y + 1;
+  const int side = blockIdx.z;                           // 0 = west/south, 1 = east/north
+  const double xb = clk->xbctime;
+  const double x1 = (xb + c.dt) * c.rtb;
+  const double x0 = 1.0 - x1;
+  const double cx1 = (xb + c.dt) / c.dtbdys;  // chem_bdyval_uncoupled
+  const double cx0 = 1.0 - cx1;
+  const R rx0 = R(x0), rx1 = R(x1);
+  const size_t PS = g.PS, F = g.field3(), ko = (size_t)(k - 1) * PS;
+  auto blend = [&](const R *const *b, size_t o) { return rx0 * b[0][o] + rx1 * b[1][o]; };
+  const int nqx = g.nqx;
+  if (phase == 0) {
+    const int i = idx + 2;  // i in idi = 2..iy-1 (v), ici = 2..iy-2 (others)
+    if (i > iy - 1) return;
+    const int jb = side == 0 ? 1 : jx - 1;   // jce1 / jce2
+    const int jd = side == 0 ? 1 : jx;       // jde1 / jde2
+    const int jin = side == 0 ? 2 : jx - 2;  // jci1 / jci2
+    const size_t ob = g.at2(jb, i) + ko, od = g.at2(jd, i) + ko, oi = g.at2(jin, i) + ko;
+    st.v[ob] = blend(bd.dvb, ob);
+    if (i > iy - 2) return;
+    if (k == 1) st.ps[g.at2(jb, i)] = x0 * bd.xpsb[0][g.at2(jb, i)] + x1 * bd.xpsb[1][g.at2(jb, i)];
+    const R un = blend(bd.dub, od);
+    st.u[od] = un;
+    st.t[ob] = blend(bd.xtb, ob);
+    st.pai[ob] = blend(bd.xpaib, ob);
+    st.qx[ob] = blend(bd.xqb, ob);
+    if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
+    if (c.present_qi && c.ipptls > 1) st.qx[ob + 2 * F] = blend(bd.xib, ob);
+    const bool inflow = side == 0 ? (un > R(0)) : (un < R(0));
+    for (int n = 1; n < nqx; ++n) {
+      if ((c.present_qc && n == 1) || (c.present_qi && n == 2)) continue;
+      const size_t on = (size_t)n * F;
+      st.qx[ob + on] = inflow ? R(qx_zero(n)) : st.qx[oi + on];
+    }
+    st.w[ob] = inflow ? R(0) : st.w[oi];
+    for (int n = 0; n < g.ntr; ++n) {
+      const size_t on = (size_t)n * F;
+      st.trac[ob + on] = R(cx0) * bd.chib[0][ob + on] + R(cx1) * bd.chib[1][ob + on];
+    }
+  } else {
+    const int j = idx + 1;  // j in jde = 1..jx (u), jce = 1..jx-1 (others)
+    if (j > jx) return;
+    const int ib = side == 0 ? 1 : iy - 1;   // ice1 / ice2
+    const int id = side == 0 ? 1 : iy;       // ide1 / ide2
+    const int iin = side == 0 ? 2 : iy - 2;  // ici1 / ici2
+    const size_t ou = g.at2(j, ib) + ko;
+    st.u[ou] = blend(bd.dub, ou);
+    if (j > jx - 1) return;
+    const size_t ob = g.at2(j, ib) + ko, od = g.at2(j, id) + ko, oi = g.at2(j, iin) + ko;
+    if (k == 1) st.ps[g.at2(j, ib)] = x0 * bd.xpsb[0][g.at2(j, ib)] + x1 * bd.xpsb[1][g.at2(j, ib)];
+    const R vn = blend(bd.dvb, od);
+    st.v[od] = vn;
+    st.t[ob] = blend(bd.xtb, ob);
+    st.pai[ob] = blend(bd.xpaib, ob);
+    st.qx[ob] = blend(bd.xqb, ob);
+    if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
+    if (c.present_qi && c.ipptls > 1) st.qx[ob + 2 * F] = blend(bd.xib, ob);
+    const bool inflow = side == 0 ? (vn > R(0)) : (vn < R(0));
+    for (int n = 1; n < nqx; ++n) {
+      if ((c.present_qc && n == 1) || (c.present_qi && n == 2)) continue;
+      const size_t on = (size_t)n * F;
+      st.qx[ob + on] = inflow ? R(qx_zero(n)) : st.qx[oi + on];
+    }
+    st.w[ob] = inflow ? R(0) : st.w[oi];
+    for (int n = 0; n < g.ntr; ++n) {
+      const size_t on = (size_t)n * F;
+      st.trac[ob + on] = R(cx0) * bd.chib[0][ob + on] + R(cx1) * bd.chib[1][ob + on];
+    }
+  }
+}
+
+// motopnudge (Main/mod_bdycod.F90:4049-4083) then morelax on every field
+// (boundary, Main/mod_moloch.F90:478-497), per point; the clock has already
+// moved by dtsec.
+template <class R>
+__global__ void k_bdy_relax(Geom g, Scal c, Stat<R> sa, State<R> st, Bdy<R> bd, const Clock *clk) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  if (j > jx - 1 || i > iy - 1) return;
+  const double xb = clk->xbctime + c.dtsec;
+  const double x1 = (xb + c.dt) * c.rtb;
+  const double x0 = 1.0 - x1;
+  const double cx1 = (xb + c.dt) / c.dtbdys;
+  const double cx0 = 1.0 - cx1;
+  const R rx0 = R(x0), rx1 = R(x1);
+  const double trtau = 1.0 / (2.0 * 3600.0);
+  const double wrtau = 1.0 / (3600.0 / 4.0);
+  const size_t ij = g.at2(j, i), PS = g.PS, F = g.field3();
+  const bool cr = j <= jx - 2 && i <= iy - 2;  // jci x ici
+  const bool up = i <= iy - 2;                 // jdi x ici
+  const bool vp = j <= jx - 2;                 // jci x idi
+  const int nsp = c.nspgx;
+  const int ibc = cr ? sa.ibnd_cr[ij] : -1;
+  const int ibu = up ? sa.ibnd_ud[ij] : -1;
+  const int ibv = vp ? sa.ibnd_vd[ij] : -1;
+  auto blend = [&](const R *const *b, size_t o) { return rx0 * b[0][o] + rx1 * b[1][o]; };
+  auto relax = [&](R f, R fext, int ib, int k) {
+    const R xf = R(sa.hefc[(size_t)(ib - 1) + (size_t)(k - 1) * nsp]);
+    return (R(1) - xf) * f + xf * fext;
+  };
+  if (cr && c.top_nudge) {
+    const size_t o = ij + PS;  // level 2
+    const R xf = R(wrtau * c.dtsec);
+    const R w2 = st.w[o];
+    const R fext = R(0) * w2;
+    st.w[o] = (R(1) - xf) * w2 + xf * fext;
+  }
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    const bool nud = c.top_nudge && k <= c.nztop;
+    const R xfn = nud ? R(sa.tnudge[k - 1] * trtau * c.dtsec) : R(0);
+    if (up) {
+      R f = st.u[o];
+      if (nud) f = (R(1) - xfn) * f + xfn * blend(bd.dub, o);
+      if (ibu > 0) f = relax(f, blend(bd.dub, o), ibu, k);
+      st.u[o] = f;
+    }
+    if (vp) {
+      R f = st.v[o];
+      if (nud) f = (R(1) - xfn) * f + xfn * blend(bd.dvb, o);
+      if (ibv > 0) f = relax(f, blend(bd.dvb, o), ibv, k);
+      st.v[o] = f;
+    }
+    if (!cr) continue;
+    {
+      R f = st.t[o];
+      if (nud) f = (R(1) - xfn) * f + xfn * blend(bd.xtb, o);
+      if (ibc > 0) f = relax(f, blend(bd.xtb, o), ibc, k);
+      st.t[o] = f;
+    }
+    if (ibc <= 0) continue;
+    st.pai[o] = relax(st.pai[o], blend(bd.xpaib, o), ibc, k);
+    st.qx[o] = relax(st.qx[o], blend(bd.xqb, o), ibc, k);
+    {
+      // morelax_fraction with frac = 0 (:3962-3993)
+      const R xf = R(sa.hefc[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp]);
+      const R f = st.w[o];
+      st.w[o] = (R(1) - xf) * f + xf * f * R(0);
+    }
+    if (c.ipptls > 0 && c.present_qc) st.qx[o + F] = relax(st.qx[o + F], blend(bd.xlb, o), ibc, k);
+    if (c.ipptls > 1 && c.present_qi) st.qx[o + 2 * F] = relax(st.qx[o + 2 * F], blend(bd.xib, o), ibc, k);
+    for (int n = 0; n < g.ntr; ++n) {
+      const size_t on = o + (size_t)n * F;
+      const R xf = R(sa.fcx[ibc - 1]);
+      const R fext = R(cx0) * bd.chib[0][on] + R(cx1) * bd.chib[1][on];
+      st.trac[on] = (R(1) - xf) * st.trac[on] + xf * fext;
+    }
+  }
+}
+
+// Cross-point work after the boundary: uvstagtouvx and temp_to_tvirt of
+// boundary (:520-523), p (:348-352), extrapolate_surface_pressure
+// (:1592-1606), then status_update (:1403-1443): q clamps, tvirt, tetav,
+// rho, qsat.  rho and qsat of :348-352 are recomputed from the same t and p
+// by status_update, so they are computed once, after it.
+template <class R>
+__global__ void k_end_cross(Geom g, Scal c, Stat<R> sa, State<R> st) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  if (j > jx - 1 || i > iy - 1) return;
+  const size_t ij = g.at2(j, i), PS = g.PS, F = g.field3(), S = (size_t)g.P;
+  const bool inner = j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2;
+  const int ipp = c.ipptls;
+  if (c.apply_bdy) {
+    for (int k = 1; k <= kz; ++k) {
+      const size_t o = ij + (size_t)(k - 1) * PS;
+      const R *u = st.u, *v = st.v;
+      R a;
+      if (j == 1) a = R(0.5) * (u[o] + u[o + 1]);
+      else if (j == jx - 1) a = R(0.5) * (u[o + 1] + u[o]);
+      else a = R(0.5625) * (u[o + 1] + u[o]) - R(0.0625) * (u[o + 2] + u[o - 1]);
+      st.ux[o] = a;
+      if (i == 1) a = R(0.5) * (v[o] + v[o + S]);
+      else if (i == iy - 1) a = R(0.5) * (v[o + S] + v[o]);
+      else a = R(0.5625) * (v[o + S] + v[o]) - R(0.0625) * (v[o + 2 * S] + v[o - S]);
+      st.vx[o] = a;
+    }
+  }
+  // pressure (FP64 Exner reconstruction)
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    st.p[o] = (R)(pow((double)st.pai[o], kCpovr) * kP00);
+  }
+  if (inner) {
+    // tvirt at kz-1, kz before the clamps: from the boundary's temp_to_tvirt,
+    // or tetav*pai of dynamical_core when the boundary is off
+    const size_t o1 = ij + (size_t)(kz - 2) * PS, o2 = ij + (size_t)(kz - 1) * PS;
+    double tv1, tv2;
+    if (c.apply_bdy) {
+      tv1 = (double)(st.t[o1] * qfactor(st.qx, o1, F, ipp));
+      tv2 = (double)(st.t[o2] * qfactor(st.qx, o2, F, ipp));
+    } else {
+      tv1 = (double)st.tvirt[o1];
+      tv2 = (double)st.tvirt[o2];
+    }
+    const double z1 = sa.zeta[o1], z2 = sa.zeta[o2];
+    double lrt = (tv1 - tv2) / (z1 - z2);
+    if (lrt < -kGovcp) lrt = -kGovcp;
+    else if (lrt > -0.005) lrt = 0.65 * lrt - 0.35 * kLrate;
+    const double tv = tv2 - lrt * 0.5 * z2;
+    st.ps[g.at2(j, i)] = (double)st.p[o2] * exp(kGovr * z2 / tv);
+  }
+  // status_update
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    if (inner) {
+      for (int n = 0; n < g.nqx; ++n) {
+        const size_t on = o + (size_t)n * F;
+        if (st.qx[on] < R(qx_check(n))) st.qx[on] = R(qx_zero(n));
+      }
+      for (int n = 0; n < g.ntr; ++n) {
+        const size_t on = o + (size_t)n * F;
+        if (st.trac[on] < R(0)) st.trac[on] = R(0);
+      }
+    }
+    const R tk = st.t[o];
+    const R tv = tk * qfactor(st.qx, o, F, ipp);
+    st.tvirt[o] = tv;
+    st.tetav[o] = tv / st.pai[o];
+    const R pk = st.p[o];
+    st.rho[o] = pk / (R(kRgas) * tk);
+    st.qsat[o] = (R)pfwsat((double)tk, (double)pk);
+  }
+}
+
+// uvxtouvstag at the end of status_update (:1440)
+template <class R>
+__global__ void k_end_uvstag(Geom g, const R *__restrict__ ux, const R *__restrict__ vx,
+                             R *__restrict__ u, R *__restrict__ v) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int jx = g.jx, iy = g.iy;
+  if (j > jx || i > iy) return;
+  const size_t ij = g.at2(j, i), PS = g.PS, S = (size_t)g.P;
+  const bool do_u = (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2);
+  const bool do_v = (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 1);
+  if (!do_u && !do_v) return;
+  for (int k = 1; k <= g.kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    if (do_u) {
+      R a;
+      if (j == jx - 1) a = R(0.5) * (ux[o - 1] + ux[o]);
+      else if (j == 2) a = R(0.5) * (ux[o] + ux[o - 1]);
+      else a = R(0.5625) * (ux[o] + ux[o - 1]) - R(0.0625) * (ux[o + 1] + ux[o - 2]);
+      u[o] = a;
+    }
+    if (do_v) {
+      R a;
+      if (i == iy - 1) a = R(0.5) * (vx[o - S] + vx[o]);
+      else if (i == 2) a = R(0.5) * (vx[o] + vx[o - S]);
+      else a = R(0.5625) * (vx[o] + vx[o - S]) - R(0.0625) * (vx[o + S] + vx[o - 2 * S]);
+      v[o] = a;
+    }
+  }
+}
+
+// Mass budget (Main/mod_massck.F90:77-170) and ps extrema.  Block b sums the
+// rows (i,k) it owns in a fixed order and writes seven partials; the single-
+// block pass then adds the partials in block order, so the result does not
+// depend on scheduling and a domain gives the same bits alone or in a batch.
+constexpr int kRedThreads = 256;
+constexpr int kNPart = 7;  // dry, dryadv, qmass, qadv, ps max, ps min, non-finite flag
+
+__device__ double block_sum(double x, double *sh) {
+  const int t = threadIdx.x;
+  sh[t] = x;
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (t < s) sh[t] = sh[t] + sh[t + s];
+    __syncthreads();
+  }
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+template <class R>
+__global__ void __launch_bounds__(kRedThreads) k_reduce_partial(Geom g, Scal c, Stat<R> sa,
+                                                                State<R> st, double *part,
+                                                                int rows_per_block) {
+  __shared__ double sh[kRedThreads];
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  const double dx = c.dx, dt = c.dt, dxsq = dx * dx;
+  const size_t F = g.field3();
+  double dry = 0, dadv = 0, qm = 0, qadv = 0, pmax = -INFINITY, pmin = INFINITY, bad = 0;
+  const int nrows = (iy - 1) * kz;  // rows (i in ice, k)
+  const int r0 = blockIdx.x * rows_per_block;
+  const bool budget = c.debug_level > 0;
+  for (int r = r0; r < min(r0 + rows_per_block, nrows); ++r) {
+    const int i = r % (iy - 1) + 1, k = r / (iy - 1) + 1;
+    const size_t ko = (size_t)(k - 1) * g.PS;
+    if (budget && i >= 2 && i <= iy - 2) {
+      for (int j = 2 + threadIdx.x; j <= jx - 2; j += kRedThreads) {
+        const size_t o = g.at2(j, i) + ko;
+        const double dzr = (double)sa.dz[o];
+        const double rh = (double)st.rho[o];
+        dry += dxsq * dzr * rh;
+        for (int n = 0; n < g.nqx; ++n) qm += (double)st.qx[o + (size_t)n * F] * dxsq * dzr * rh;
+      }
+    }
+    if (budget && threadIdx.x == 0) {
+      // west and east columns over i in ice (Main/mod_massck.F90:85-100)
+      const size_t ow = g.at2(1, i) + ko, oe = g.at2(jx - 1, i) + ko;
+      const double uw = (double)st.u[g.at2(1, i) + ko], ue = (double)st.u[g.at2(jx, i) + ko];
+      const double dzw = (double)sa.dz[ow], rw = (double)st.rho[ow];
+      const double dze = (double)sa.dz[oe], re = (double)st.rho[oe];
+      dadv += uw * dt * dx * dzw * rw;
+      dadv -= ue * dt * dx * dze * re;
+      for (int n = 0; n < g.nqx; ++n) {
+        qadv += (double)st.qx[ow + (size_t)n * F] * uw * dt * dx * dzw * rw;
+        qadv -= (double)st.qx[oe + (size_t)n * F] * ue * dt * dx * dze * re;
+      }
+    }
+    if (budget && (i == 1 || i == iy - 1)) {
+      // south (v at ide1) and north (v at ide2) rows, j in jci (:101-116)
+      const int iv = (i == 1) ? 1 : iy;
+      const bool south = (i == 1);
+      for (int j = 2 + threadIdx.x; j <= jx - 2; j += kRedThreads) {
+        const size_t o = g.at2(j, i) + ko;
+        const double vv = (double)st.v[g.at2(j, iv) + ko];
+        const double dzr = (double)sa.dz[o], rh = (double)st.rho[o];
+        const double fl = vv * dt * dx * dzr * rh;
+        dadv = south ? dadv + fl : dadv - fl;
+        for (int n = 0; n < g.nqx; ++n) {
+          const double q = (double)st.qx[o + (size_t)n * F] * vv * dt * dx * dzr * rh;
+          qadv = south ? qadv + q : qadv - q;
+        }
+      }
+    }
+    if (k == 1 && i >= 2 && i <= iy - 2) {
+      for (int j = 2 + threadIdx.x; j <= jx - 2; j += kRedThreads) {
+        const double x = st.ps[g.at2(j, i)];
+        if (!isfinite(x)) bad = 1;
+        else { pmax = fmax(pmax, x); pmin = fmin(pmin, x); }
+      }
+    }
+  }
+  dry = block_sum(dry, sh);
+  dadv = block_sum(dadv, sh);
+  qm = block_sum(qm, sh);
+  qadv = block_sum(qadv, sh);
+  bad = block_sum(bad, sh);
+  sh[threadIdx.x] = pmax;
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  pmax = sh[0];
+  __syncthreads();
+  sh[threadIdx.x] = pmin;
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  pmin = sh[0];
+  if (threadIdx.x == 0) {
+    double *p = part + (size_t)blockIdx.x * kNPart;
+    p[0] = dry; p[1] = dadv; p[2] = qm; p[3] = qadv; p[4] = pmax; p[5] = pmin; p[6] = bad;
+  }
+}
+
+__global__ void k_reduce_final(const double *part, int nblocks, DiagDev *diag, Clock *clk,
+                               double dtsec, int apply_bdy) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double a[4] = {0, 0, 0, 0}, pmax = -INFINITY, pmin = INFINITY;
+  bool bad = false;
+  for (int b = 0; b < nblocks; ++b) {
+    const double *p = part + (size_t)b * kNPart;
+    for (int q = 0; q < 4; ++q) a[q] += p[q];
+    pmax = fmax(pmax, p[4]);
+    pmin = fmin(pmin, p[5]);
+    if (p[6] != 0.0) bad = true;
+  }
+  diag->drymass = a[0]; diag->dryadv = a[1]; diag->qmass = a[2]; diag->qadv = a[3];
+  diag->ps_max = bad ? NAN : pmax;
+  diag->ps_min = bad ? NAN : pmin;
+  diag->nonfinite = bad ? 1 : 0;
+  if (bad && !clk->nonfinite) { clk->nonfinite = 1; clk->bad_step = clk->step; }
+  if (apply_bdy) clk->xbctime = clk->xbctime + dtsec;
+  clk->step = clk->step + 1;
+}
+
+template <class R>
+__global__ void k_unpack3(const double *__restrict__ src, R *__restrict__ dst, Geom g, int nj, int ni, int nk) {
+  const size_t n = (size_t)nj * ni * nk;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e % nj);
+    const size_t r = e / nj;
+    const int i = (int)(r % ni);
+    const int k = (int)(r / ni);
+    dst[(size_t)j + (size_t)i * g.P + (size_t)k * g.PS] = (R)src[e];
+  }
+}
+
+template <class R>
+__global__ void k_pack3(const R *__restrict__ src, double *__restrict__ dst, Geom g, int nj, int ni, int nk) {
+  const size_t n = (size_t)nj * ni * nk;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e % nj);
+    const size_t r = e / nj;
+    const int i = (int)(r % ni);
+    const int k = (int)(r / ni);
+    dst[e] = (double)src[(size_t)j + (size_t)i * g.P + (size_t)k * g.PS];
+  }
+}
+
+inline dim3 grid2(int nj, int ni, dim3 b) {
+  return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y));
+}
+
+inline int rows_per_block(const Geom &g) {
+  const int nrows = (g.iy - 1) * g.kz;
+  const int target = 152 * 4;
+  return (nrows + target - 1) / target;
+}
+
+}  // namespace
+
+int reduce_blocks(const Geom &g) {
+  const int nrows = (g.iy - 1) * g.kz;
+  const int rpb = rows_per_block(g);
+  return (nrows + rpb - 1) / rpb;
+}
+
+template <class R>
+void Launch<R>::end_tvirt(const Geom &g, const Scal &c, const State<R> &st, cudaStream_t s) {
+  const dim3 b(32, 4);
+  k_end_tvirt<R><<<grid2(g.jx - 1, g.iy - 1, b), b, 0, s>>>(g, c, st);
+}
+
+template <class R>
+void Launch<R>::bdy_ring(const Geom &g, const Scal &c, const State<R> &st, const Bdy<R> &bd,
+                         const Clock *clk, cudaStream_t s) {
+  const int nwe = g.iy - 2, nsn = g.jx;
+  k_bdy_ring<R><<<dim3((unsigned)((nwe + 63) / 64), (unsigned)g.kz, 2), 64, 0, s>>>(g, c, st, bd, clk, 0);
+  k_bdy_ring<R><<<dim3((unsigned)((nsn + 63) / 64), (unsigned)g.kz, 2), 64, 0, s>>>(g, c, st, bd, clk, 1);
+}
+
+template <class R>
+void Launch<R>::bdy_relax(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                          const Bdy<R> &bd, const Clock *clk, cudaStream_t s) {
+  const dim3 b(32, 4);
+  k_bdy_relax<R><<<grid2(g.jx - 2, g.iy - 2, b), b, 0, s>>>(g, c, sa, st, bd, clk);
+}
+
+template <class R>
+void Launch<R>::end_cross(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                          cudaStream_t s) {
+  const dim3 b(32, 4);
+  k_end_cross<R><<<grid2(g.jx - 1, g.iy - 1, b), b, 0, s>>>(g, c, sa, st);
+}
+
+template <class R>
+void Launch<R>::end_uvstag(const Geom &g, const State<R> &st, cudaStream_t s) {
+  const dim3 b(32, 4);
+  k_end_uvstag<R><<<grid2(g.jx, g.iy, b), b, 0, s>>>(g, st.ux, st.vx, st.u, st.v);
+}
+
+template <class R>
+void Launch<R>::end_reduce(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                           double *partials, int nblocks, DiagDev *diag, Clock *clk, cudaStream_t s) {
+  k_reduce_partial<R><<<nblocks, kRedThreads, 0, s>>>(g, c, sa, st, partials, rows_per_block(g));
+  k_reduce_final<<<1, 32, 0, s>>>(partials, nblocks, diag, clk, c.dtsec, c.apply_bdy);
+}
+
+template <class R>
+void Launch<R>::unpack3(const double *src, R *dst, const Geom &g, int nj, int ni, int nk, cudaStream_t s) {
+  k_unpack3<R><<<152 * 8, 256, 0, s>>>(src, dst, g, nj, ni, nk);
+}
+
+template <class R>
+void Launch<R>::pack3(const R *src, double *dst, const Geom &g, int nj, int ni, int nk, cudaStream_t s) {
+  k_pack3<R><<<152 * 8, 256, 0, s>>>(src, dst, g, nj, ni, nk);
+}
+
+template struct Launch<double>;
+template struct Launch<float>;
+
+}  // namespace mlc

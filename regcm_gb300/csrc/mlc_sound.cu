@@ -1,0 +1,312 @@
+// mlc_sound.cu -- the acoustic substeps of the MOLOCH step
+// (Main/mod_moloch.F90:531-765, subroutines sound, divergence_damping,
+// divergence_diffusion).
+//
+// One substep is three kernels:
+//   sound_div       per column of cross points: raw horizontal divergence
+//                   zdiv2 (Eq. 16) and the generalized vertical velocity s
+//                   (Eq. 10), s(kz+1) and the surface w.
+//   sound_solve     per interior column, one thread per column: the 5-point
+//                   divergence filter, the vertical divergence term, the
+//                   implicit w-Exner tridiagonal system (Eq. 19, Thomas
+//                   algorithm with the column held in shared memory), the
+//                   Exner update and, after the last substep, the completed s.
+//   sound_momentum  u and v (Eq. 17/18): divergence damping, Coriolis with
+//                   the substep's initial winds, pressure gradient with the new
+//                   Exner function, terrain term, relaxation-zone weight.  It
+//                   writes the other half of a ping-pong pair, which is how the
+//                   reference's ud/vd copies are kept without a copy.
+// Every expression keeps the reference's operands and association order; the
+// only departures are FMA contraction by the compiler and the relaxation
+// weight bdywt recomputed from ibnd and hefc instead of read from an array
+// (the same value, Main/mod_bdycod.F90:4033-4047).
+#include "mlc_kernels.cuh"
+
+namespace mlc {
+
+namespace {
+
+constexpr int kColX = 32;  // threads along j for column kernels
+constexpr int kColY = 4;   // threads along i
+
+__device__ __forceinline__ double relax_weight(const int32_t *ibnd, const double *hefc, int nsp,
+                                               size_t ij, int k) {
+  int ib = ibnd[ij];
+  return ib > 0 ? 1.0 - hefc[(size_t)(ib - 1) + (size_t)(k - 1) * nsp] : 1.0;
+}
+
+template <class R>
+__global__ void k_sound_prep(Geom g, const R *__restrict__ tetav, R *__restrict__ tetavf) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (j > g.jx - 1 || i > g.iy - 1) return;
+  // Main/mod_moloch.F90:564-566
+  R lo = tetav[g.at(j, i, 1)];
+  for (int k = 2; k <= g.kz; ++k) {
+    R hi = tetav[g.at(j, i, k)];
+    tetavf[g.at(j, i, k)] = R(0.5) * (lo + hi);
+    lo = hi;
+  }
+}
+
+// Main/mod_moloch.F90:582-618
+template <class R>
+__global__ void k_sound_div(Geom g, Scal c, Stat<R> sa, const R *__restrict__ u,
+                            const R *__restrict__ v, R *__restrict__ zdiv2, R *__restrict__ s,
+                            R *__restrict__ w) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (j > g.jx - 1 || i > g.iy - 1) return;
+  const int kz = g.kz;
+  const R dts = R(c.dtsound);
+  const R dtrdx = dts * R(c.rdx), dtrdy = dts * R(c.rdx);
+  const size_t ij = g.at2(j, i), ijE = g.at2(j + 1, i), ijN = g.at2(j, i + 1);
+  const bool interior = (j >= 2 && j <= g.jx - 2 && i >= 2 && i <= g.iy - 2);
+  const R rmu0 = sa.rmu[ij], rmu1 = sa.rmu[ijE], rmv0 = sa.rmv[ij], rmv1 = sa.rmv[ijN];
+  const R mfac = c.lrotllr ? sa.msfx[ij] : sa.mx2[ij];
+  R hx0 = 0, hx1 = 0, hy0 = 0, hy1 = 0;
+  if (interior) {
+    hx0 = sa.hx[ij]; hx1 = sa.hx[ijE]; hy0 = sa.hy[ij]; hy1 = sa.hy[ijN];
+  }
+  R um = 0, up = 0, vm = 0, vp = 0;  // level k-1 values
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = (size_t)(k - 1) * g.PS;
+    const R u0 = u[ij + o], u1 = u[ijE + o], v0 = v[ij + o], v1 = v[ijN + o];
+    R zum, zup;
+    if (c.lrotllr) {
+      zum = dtrdx * u0 * sa.rfmzu[ij + o];
+      zup = dtrdx * u1 * sa.rfmzu[ijE + o];
+    } else {
+      zum = dtrdx * u0 * sa.rfmzu[ij + o] * rmu0;
+      zup = dtrdx * u1 * sa.rfmzu[ijE + o] * rmu1;
+    }
+    const R zvm = dtrdy * v0 * sa.rfmzv[ij + o] * rmv0;
+    const R zvp = dtrdy * v1 * sa.rfmzv[ijN + o] * rmv1;
+    zdiv2[ij + o] = sa.fmz[ij + o] * mfac * ((zup - zum) + (zvp - zvm));
+    if (interior && k >= 2) {
+      const R zuh = (u0 + um) * hx0 + (u1 + up) * hx1;
+      const R zvh = (v0 + vm) * hy0 + (v1 + vp) * hy1;
+      s[ij + o] = -(R(0.25) * (zuh + zvh) * R(sa.gzitak[k - 1]));
+    }
+    if (interior && k == kz) {
+      const R zuh = u0 * hx0 + u1 * hx1;
+      const R zvh = v0 * hy0 + v1 * hy1;
+      const R skp1 = -(R(0.5) * (zuh + zvh));
+      s[ij + (size_t)kz * g.PS] = skp1;
+      w[ij + (size_t)kz * g.PS] = -skp1;
+    }
+    um = u0; up = u1; vm = v0; vp = v1;
+  }
+}
+
+// Main/mod_moloch.F90:531-543,627-671,728-734.  The column of one thread is
+// kept in shared memory laid out [level][thread] (consecutive threads hit
+// consecutive banks).  The recurrence runs in FP64 for either field type.
+template <class R>
+__global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ zraw,
+                              R *__restrict__ s, R *__restrict__ w, R *__restrict__ pai,
+                              const R *__restrict__ tetav, R *__restrict__ tetavf, int last) {
+  extern __shared__ double smem[];
+  const int nth = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int kz = g.kz;
+  double *zf = smem;                               // (kz+1) levels, index k
+  double *wp = smem + (size_t)(kz + 2) * nth;      // w after elimination, then final
+  double *wk = smem + (size_t)2 * (kz + 2) * nth;  // elimination multipliers
+#define COL(a, k) a[(size_t)(k) * nth + tid]
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (j > g.jx - 2 || i > g.iy - 2) return;
+  const double dts = c.dtsound;
+  const double dtrdz = dts * c.rdzita;
+  const double zcs2 = (dtrdz * dtrdz) * kRdrcv;
+  const size_t ij = g.at2(j, i);
+  const size_t PS = g.PS;
+  const size_t P = (size_t)g.P;
+
+  // filtered divergence plus the vertical part (:531-543, :627-630)
+  double sk = (double)s[ij];  // s(1) = 0 in the interior
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    double z = (double)zraw[o];
+    if (c.divfilter) {
+      const double lap = ((double)zraw[o - 1] + (double)zraw[o + 1] + (double)zraw[o - P] +
+                          (double)zraw[o + P] - 4.0 * z);
+      z = z + sa.xknu[k - 1] * lap;
+    }
+    const double skp1 = (double)s[o + PS];
+    const double bw = relax_weight(sa.ibnd_cr, sa.hefc, c.nspgx, ij, k);
+    z = z + bw * dtrdz * (double)sa.fmz[o] * (sk - skp1);
+    COL(zf, k) = z;
+    sk = skp1;
+  }
+
+  // elimination k = kz..2 (:634-656); wwkw(kz+1) = 0
+  double wnext = (double)w[ij + (size_t)kz * PS];  // w(kz+1) = -s(kz+1)
+  double wkp1 = 0.0;
+  double pai_k = (double)pai[ij + (size_t)(kz - 1) * PS];
+  double tet_k = (double)tetav[ij + (size_t)(kz - 1) * PS];
+  double fmz_k = (double)sa.fmz[ij + (size_t)(kz - 1) * PS];
+  for (int k = kz; k >= 2; --k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    const double pai_m = (double)pai[o - PS];
+    const double tet_m = (double)tetav[o - PS];
+    const double fmz_m = (double)sa.fmz[o - PS];
+    const double fmzf = (double)sa.fmzf[o];
+    const double wold = (double)w[o];
+    const double tvf = (double)tetavf[o] - wold * fmzf * dtrdz * (tet_m - tet_k);
+    tetavf[o] = (R)tvf;
+    const double zrom1w = kCpd * tvf * fmzf;
+    double zwexpl = wold - zrom1w * dtrdz * (pai_m - pai_k) - kGrav * dts;
+    zwexpl = zwexpl + kRdrcv * zrom1w * dtrdz * (pai_m * COL(zf, k - 1) - pai_k * COL(zf, k));
+    const double ff = sa.ffilt[k - 1];
+    const double zu = zcs2 * fmz_m * zrom1w * pai_m + ff;
+    const double zd = zcs2 * fmz_k * zrom1w * pai_k + ff;
+    const double zrapp = 1.0 / (1.0 + zd + zu - zd * wkp1);
+    wnext = zrapp * (zwexpl + zd * wnext);
+    wkp1 = zrapp * zu;
+    COL(wp, k) = wnext;
+    COL(wk, k) = wkp1;
+    pai_k = pai_m; tet_k = tet_m; fmz_k = fmz_m;
+  }
+  // back substitution k = 2..kz (:660-664)
+  double wprev = (double)w[ij];  // w(1) = 0
+  COL(wp, 1) = wprev;
+  for (int k = 2; k <= kz; ++k) {
+    wprev = COL(wp, k) + COL(wk, k) * wprev;
+    COL(wp, k) = wprev;
+    w[ij + (size_t)(k - 1) * PS] = (R)wprev;
+  }
+  COL(wp, kz + 1) = (double)w[ij + (size_t)kz * PS];
+  // Exner function (:668-671)
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    const double pk = (double)pai[o];
+    pai[o] = (R)(pk * (1.0 - kRdrcv * (COL(zf, k) + (dtrdz * (double)sa.fmz[o] *
+                                                     (COL(wp, k) - COL(wp, k + 1))))));
+  }
+  if (last) {
+    // complete s (:728-734)
+    for (int k = 2; k <= kz; ++k) {
+      const size_t o = ij + (size_t)(k - 1) * PS;
+      s[o] = (R)((COL(wp, k) + (double)s[o]) * (double)sa.fmzf[o]);
+    }
+    s[ij] = R(0);
+    s[ij + (size_t)kz * PS] = R(0);
+  }
+#undef COL
+}
+
+// Main/mod_moloch.F90:677-721 with divergence_damping :738-765 folded in
+template <class R>
+__global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict__ u_in,
+                                 const R *__restrict__ v_in, R *__restrict__ u_out,
+                                 R *__restrict__ v_out, const R *__restrict__ zraw,
+                                 const R *__restrict__ pai, const R *__restrict__ tetav) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (j > g.jx || i > g.iy) return;
+  const R dts = R(c.dtsound);
+  const R dtrdx = dts * R(c.rdx), dtrdy = dts * R(c.rdx);
+  const R dxrdt = R(c.dx) / dts;
+  const R zfz = R(kGrav) * dts;
+  const R halfcp = R(0.5) * R(kCpd);
+  const size_t ij = g.at2(j, i);
+  const size_t PS = g.PS;
+  const bool has_u = i <= g.iy - 1;
+  const bool has_v = j <= g.jx - 1;
+  const bool upd_u = has_u && j >= 2 && j <= g.jx - 1 && i >= 2 && i <= g.iy - 2;
+  const bool upd_v = has_v && j >= 2 && j <= g.jx - 2 && i >= 2 && i <= g.iy - 1;
+  R mu = 0, zcx = 0, hxk = 0, cor_u = 0, zcy = 0, hyk = 0, cor_v = 0, mv = 0;
+  if (upd_u) {
+    mu = sa.msfu[ij];
+    zcx = dtrdx * mu;
+    hxk = sa.hx[ij];
+    cor_u = sa.coru[ij];
+  }
+  if (upd_v) {
+    mv = sa.msfv[ij];
+    zcy = c.lrotllr ? dtrdy : dtrdy * mv;
+    hyk = sa.hy[ij];
+    cor_v = sa.corv[ij];
+  }
+  const size_t W = 1, S = (size_t)g.P;
+  for (int k = 1; k <= g.kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    const R gk = R(sa.gzitakh[k - 1]);
+    if (has_u) {
+      R un = u_in[o];
+      if (upd_u) {
+        if (c.divdamp) {
+          const R xdam = dxrdt * R(sa.xkdamp[k - 1]) * mu;
+          un = un + xdam * (zraw[o] - zraw[o - W]);
+        }
+        const R zrom1u = halfcp * (tetav[o - W] + tetav[o]);
+        const R zcor1u = cor_u * dts * v_in[o];
+        const R bw = R(relax_weight(sa.ibnd_ud, sa.hefc, c.nspgx, ij, k));
+        un = un + bw * (zcor1u - zfz * hxk * gk - zcx * zrom1u * (pai[o] - pai[o - W]));
+      }
+      u_out[o] = un;
+    }
+    if (has_v) {
+      R vn = v_in[o];
+      if (upd_v) {
+        if (c.divdamp) {
+          const R xdam = c.lrotllr ? dxrdt * R(sa.xkdamp[k - 1]) : dxrdt * R(sa.xkdamp[k - 1]) * mv;
+          vn = vn + xdam * (zraw[o] - zraw[o - S]);
+        }
+        const R zrom1v = halfcp * (tetav[o - S] + tetav[o]);
+        const R zcor1v = cor_v * dts * u_in[o];
+        const R bw = R(relax_weight(sa.ibnd_vd, sa.hefc, c.nspgx, ij, k));
+        vn = vn + bw * (-zcor1v - zfz * hyk * gk - zcy * zrom1v * (pai[o] - pai[o - S]));
+      }
+      v_out[o] = vn;
+    }
+  }
+}
+
+inline dim3 col_grid(int nj, int ni) {
+  return dim3((unsigned)((nj + kColX - 1) / kColX), (unsigned)((ni + kColY - 1) / kColY));
+}
+
+}  // namespace
+
+template <class R>
+void Launch<R>::sound_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
+  k_sound_prep<R><<<col_grid(g.jx - 1, g.iy - 1), dim3(kColX, kColY), 0, s>>>(g, st.tetav, wk.tetavf);
+}
+
+template <class R>
+void Launch<R>::sound_div(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                          const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s) {
+  k_sound_div<R><<<col_grid(g.jx - 1, g.iy - 1), dim3(kColX, kColY), 0, s>>>(
+      g, c, sa, b.u_in, b.v_in, wk.zdiv2, wk.s, st.w);
+}
+
+template <class R>
+void Launch<R>::sound_solve(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                            const Work<R> &wk, bool last, cudaStream_t s) {
+  const dim3 blk(32, 2);
+  const size_t smem = (size_t)3 * (g.kz + 2) * blk.x * blk.y * sizeof(double);
+  const dim3 grd((unsigned)((g.jx - 3 + blk.x - 1) / blk.x), (unsigned)((g.iy - 3 + blk.y - 1) / blk.y));
+  k_sound_solve<R><<<grd, blk, smem, s>>>(g, c, sa, wk.zdiv2, wk.s, st.w, st.pai, st.tetav,
+                                          wk.tetavf, last ? 1 : 0);
+}
+
+template <class R>
+void Launch<R>::sound_momentum(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                               const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s) {
+  k_sound_momentum<R><<<col_grid(g.jx, g.iy), dim3(kColX, kColY), 0, s>>>(
+      g, c, sa, b.u_in, b.v_in, b.u_out, b.v_out, wk.zdiv2, st.pai, st.tetav);
+}
+
+template <class R>
+cudaError_t Launch<R>::configure_sound() {
+  return cudaFuncSetAttribute(k_sound_solve<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              200 * 1024);
+}
+
+template struct Launch<double>;
+template struct Launch<float>;
+
+}  // namespace mlc

@@ -1,0 +1,140 @@
+"""Host mirror of RegCM's MOLOCH module interface over the C ABI.
+
+RegCM's module exposes three argument-less procedures,
+``public :: allocate_moloch, init_moloch, moloch`` (Main/mod_moloch.F90:127),
+called from param (Main/mod_params.F90:1979-1980), init
+(Main/mod_init.F90:922-923) and once per model step from RCM_run
+(Main/mod_regcm_interface.F90:274-275).  ``MolochDomain`` keeps the same three
+phases with the state passed explicitly, and the module-level functions of the
+same names drive one default domain the way the Fortran globals do.  Failures
+raise ``MolochError`` where the reference calls fatal(); a non-finite surface
+pressure raises ``CFLViolation`` ("CFL VIOLATION", Main/mod_moloch.F90:407-422).
+There is no CPU fallback: without the compiled library or a GPU every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import abi
+from .abi import MolochError
+
+__all__ = ["MolochDomain", "MolochError", "CFLViolation", "allocate_moloch", "init_moloch",
+           "moloch"]
+
+
+class CFLViolation(MolochError):
+    """Surface pressure became NaN or Inf (the reference stops the model)."""
+
+
+class MolochDomain:
+    """One MOLOCH domain resident on the GPU."""
+
+    def __init__(self, dims: abi.mlc_dims, params: abi.mlc_params):
+        self.lib = abi.load()
+        self.dims = dims
+        self.params = params
+        self._ctx = C.c_void_p()
+        abi.check(self.lib.mlc_create(C.byref(dims), C.byref(params), C.byref(self._ctx)),
+                  "allocate_moloch")
+        self._keep = []
+
+    # -- init_moloch -------------------------------------------------------
+    def bind_static(self, static_ptrs: abi.mlc_static_ptrs):
+        self._keep.append(static_ptrs)
+        abi.check(self.lib.mlc_bind_static(self._ctx, C.byref(static_ptrs)), "init_moloch(static)")
+
+    def upload(self, state_ptrs: abi.mlc_state_ptrs):
+        abi.check(self.lib.mlc_upload_state(self._ctx, C.byref(state_ptrs)), "init_moloch(state)")
+
+    def set_boundary(self, bdy_ptrs: abi.mlc_bdy_ptrs, xbctime: float, dtbdys: float):
+        self._keep.append(bdy_ptrs)
+        abi.check(self.lib.mlc_set_boundary(self._ctx, C.byref(bdy_ptrs), xbctime, dtbdys),
+                  "bdyin")
+
+    # -- moloch ------------------------------------------------------------
+    def step(self, nsteps: int = 1) -> abi.mlc_diag:
+        d = abi.mlc_diag()
+        st = self.lib.mlc_step(self._ctx, nsteps, C.byref(d))
+        if st == abi.MLC_ERR_NONFINITE:
+            raise CFLViolation(st, "moloch")
+        abi.check(st, "moloch")
+        return d
+
+    def download(self, state_ptrs: abi.mlc_state_ptrs):
+        abi.check(self.lib.mlc_download_state(self._ctx, C.byref(state_ptrs)), "download")
+
+    def launches_per_step(self) -> int:
+        f = self.lib.mlc_launches_per_step
+        f.restype = C.c_int
+        f.argtypes = [C.c_void_p]
+        return f(self._ctx)
+
+    def set_graphs(self, on: bool):
+        f = self.lib.mlc_set_graphs
+        f.argtypes = [C.c_void_p, C.c_int]
+        abi.check(f(self._ctx, 1 if on else 0), "mlc_set_graphs")
+
+    def close(self):
+        if self._ctx:
+            self.lib.mlc_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def domain_from_case(case) -> MolochDomain:
+    """allocate_moloch + init_moloch for a synthetic ``Case``."""
+    dom = MolochDomain(case.dims, case.params)
+    dom.bind_static(case.static_ptrs())
+    dom.upload(case.state_ptrs())
+    if case.params.do_apply_bdy:
+        dom.set_boundary(case.bdy_ptrs(), case.xbctime, case.params.dtbdys)
+    dom._case = case
+    return dom
+
+
+# ---- module-level entry points with the reference's names -----------------
+_default: MolochDomain | None = None
+_default_case = None
+
+
+def allocate_moloch(case) -> MolochDomain:
+    """Main/mod_moloch.F90:159-199: create the default domain for `case`."""
+    global _default, _default_case
+    if _default is not None:
+        _default.close()
+    _default = MolochDomain(case.dims, case.params)
+    _default_case = case
+    return _default
+
+
+def init_moloch() -> None:
+    """Main/mod_moloch.F90:201-308: bind static fields, state and boundary."""
+    if _default is None:
+        raise MolochError(abi.MLC_ERR_STATE, "init_moloch before allocate_moloch")
+    c = _default_case
+    _default.bind_static(c.static_ptrs())
+    _default.upload(c.state_ptrs())
+    if c.params.do_apply_bdy:
+        _default.set_boundary(c.bdy_ptrs(), c.xbctime, c.params.dtbdys)
+
+
+def moloch() -> abi.mlc_diag:
+    """Main/mod_moloch.F90:312-446: advance the default domain by one dt and
+    copy the state back into the case's arrays (the Fortran globals)."""
+    if _default is None:
+        raise MolochError(abi.MLC_ERR_STATE, "moloch before allocate_moloch")
+    d = _default.step(1)
+    _default.download(_default_case.state_ptrs())
+    return d

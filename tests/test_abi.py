@@ -1,0 +1,72 @@
+"""The C-ABI library loads without a GPU and exports every function that
+include/*.h declares; error paths that need no device behave like the
+reference's fatal() checks."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+from regcm_gb300 import abi
+
+HEADERS = sorted((Path(__file__).resolve().parent.parent / "include").glob("*.h"))
+
+
+def declared_functions():
+    names = set()
+    for h in HEADERS:
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+        for m in re.finditer(r"\b(?:int|void|size_t|const char\s*\*)\s*(mlc_\w+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_the_entry_points():
+    names = declared_functions()
+    for n in ("mlc_create", "mlc_bind_static", "mlc_upload_state", "mlc_download_state",
+              "mlc_set_boundary", "mlc_step", "mlc_destroy", "mlc_strerror"):
+        assert n in names
+
+
+@pytest.mark.parametrize("name", declared_functions())
+def test_library_exports(name):
+    lib = C.CDLL(str(abi.lib_path()))
+    assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_strerror_and_defaults():
+    lib = abi.load()
+    assert lib.mlc_strerror(abi.MLC_ERR_NONFINITE).decode().startswith("CFL VIOLATION")
+    p = abi.mlc_params()
+    lib.mlc_default_params(C.byref(p))
+    # reference defaults, Share/mod_dynparam.F90:203-211
+    assert (p.mo_ztop, p.mo_h, p.mo_a0, p.mo_nadv, p.mo_nsound) == (30000.0, 8000.0, 0.0, 2, 5)
+    assert p.mo_divdamp == p.mo_divfilter == p.mo_top_nudge == 1
+
+
+def test_create_rejects_bad_input_before_touching_the_device():
+    lib = abi.load()
+    p = abi.mlc_params()
+    lib.mlc_default_params(C.byref(p))
+    ctx = C.c_void_p()
+    # too few levels / spectral nudging requested / no output pointer
+    assert lib.mlc_create(C.byref(abi.mlc_dims(65, 65, 2, 2, 0)), C.byref(p), C.byref(ctx)) == \
+        abi.MLC_ERR_INVALID
+    p.mo_spectral_nudge = 1
+    assert lib.mlc_create(C.byref(abi.mlc_dims(65, 65, 30, 2, 0)), C.byref(p), C.byref(ctx)) == \
+        abi.MLC_ERR_UNSUPPORTED
+    p.mo_spectral_nudge = 0
+    p.ipptls = 2
+    assert lib.mlc_create(C.byref(abi.mlc_dims(65, 65, 30, 2, 0)), C.byref(p), C.byref(ctx)) == \
+        abi.MLC_ERR_INVALID  # ipptls 2 needs qv..qs
+
+
+def test_footprint_grows_with_domain():
+    lib = abi.load()
+    a = lib.mlc_footprint_bytes(C.byref(abi.mlc_dims(65, 65, 30, 2, 1)), abi.MLC_PREC_FP64)
+    b = lib.mlc_footprint_bytes(C.byref(abi.mlc_dims(513, 513, 41, 5, 0)), abi.MLC_PREC_FP64)
+    c = lib.mlc_footprint_bytes(C.byref(abi.mlc_dims(513, 513, 41, 5, 0)), abi.MLC_PREC_MIXED)
+    assert 0 < a < b and c < b

@@ -1,0 +1,143 @@
+"""GPU MOLOCH step (through the C ABI) against the CPU oracle.
+
+Tolerances are the ones the path is specified with: relative L2 per field
+<= 1e-12 after one step and <= 1e-9 after 100 steps, in FP64.  The GPU
+library contracts multiply-adds into FMAs and evaluates pow/exp with CUDA's
+libm, so agreement is to rounding, not bitwise.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from regcm_gb300 import case as cs
+from regcm_gb300.moloch import domain_from_case
+
+from .conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["u", "v", "w", "pai", "tetav", "t", "tvirt", "ux", "vx", "p", "rho", "qsat", "ps"]
+
+
+def field_errors(a: dict, b: dict, case) -> dict:
+    out = {}
+    for n in FIELDS:
+        out[n] = rel_l2(a[n], b[n])
+    nq = case.dims.nqx
+    for q in range(nq):
+        ref = b["qx"][..., q]
+        if np.linalg.norm(ref) > 1e-30:
+            out[f"qx{q}"] = rel_l2(a["qx"][..., q], ref)
+        else:
+            out[f"qx{q}"] = float(np.abs(a["qx"][..., q] - ref).max())
+    if case.dims.ntr:
+        out["trac"] = rel_l2(a["trac"], b["trac"])
+    return out
+
+
+def run_pair(case, nsteps, chunk=None):
+    dom = domain_from_case(case)
+    orc = Oracle(case)
+    chunk = chunk or nsteps
+    done = 0
+    while done < nsteps:
+        n = min(chunk, nsteps - done)
+        dg = dom.step(n)
+        st, do = orc.step(n)
+        assert st == 0
+        done += n
+    g = case.empty_state()
+    dom.download(case.state_ptrs_of(g))
+    o = orc.state()
+    dom.close()
+    orc.close()
+    return g, o, dg, do
+
+
+def small_dry(**kw):
+    return cs.build(24, 22, 12, dx=12000.0, dt=60.0, nsound=3, moist=False, seed=3,
+                    hills=[(12 * 12000.0, 11 * 12000.0, 600.0)], wind=10.0, theta_noise=0.3,
+                    tracer=True, name="small_dry", **kw)
+
+
+def small_moist(**kw):
+    return cs.build(40, 38, 14, dx=3000.0, dt=20.0, nsound=4, moist=True, seed=4,
+                    hills=[(20 * 3000.0, 18 * 3000.0, 1200.0), (8 * 3000.0, 30 * 3000.0, 400.0)],
+                    jet=True, theta_noise=0.2, name="small_moist", **kw)
+
+
+CASES = {
+    "dry_tracer": lambda: small_dry(),
+    "moist": lambda: small_moist(),
+    "rotllr": lambda: small_dry(lrotllr=True),
+    "no_bdy": lambda: small_dry(apply_bdy=False),
+    "nadv2": lambda: cs.build(24, 22, 12, dx=12000.0, dt=60.0, nsound=2, nadv=2, moist=False,
+                              seed=7, wind=15.0, tracer=True, name="nadv2"),
+    "moist_nsound5": lambda: cs.build(40, 36, 10, dx=3000.0, dt=20.0, nsound=5, moist=True,
+                                      seed=9, jet=True, name="moist5"),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_one_step(name):
+    case = CASES[name]()
+    g, o, dg, do = run_pair(case, 1)
+    err = field_errors(g, o, case)
+    bad = {k: v for k, v in err.items() if not v <= 1e-12}
+    assert not bad, f"{name}: {bad}"
+    # mass budget sums and ps extrema of the step (FP64 reductions)
+    for k in ("drymass", "qmass", "ps_max", "ps_min"):
+        assert abs(getattr(dg, k) - getattr(do, k)) <= 1e-12 * abs(getattr(do, k)), k
+    for k in ("dryadv", "qadv"):
+        assert abs(getattr(dg, k) - getattr(do, k)) <= 1e-9 * max(1.0, abs(do.drymass) * 1e-6), k
+    assert dg.xbctime == do.xbctime
+
+
+@pytest.mark.parametrize("name", ["dry_tracer", "moist"])
+def test_hundred_steps(name):
+    case = CASES[name]()
+    g, o, dg, do = run_pair(case, 100, chunk=25)
+    err = field_errors(g, o, case)
+    bad = {k: v for k, v in err.items() if not v <= 1e-9}
+    assert not bad, f"{name}: {bad}"
+
+
+def test_config0_full_size_ten_steps():
+    case = cs.config0()
+    g, o, dg, do = run_pair(case, 10)
+    err = field_errors(g, o, case)
+    bad = {k: v for k, v in err.items() if not v <= 1e-11}
+    assert not bad, bad
+
+
+def test_graph_replay_matches_eager_launches():
+    a = small_moist()
+    b = small_moist()
+    da = domain_from_case(a)
+    db = domain_from_case(b)
+    db.set_graphs(False)
+    for _ in range(3):
+        da.step(2)
+        db.step(2)
+    ga, gb = a.empty_state(), b.empty_state()
+    da.download(a.state_ptrs_of(ga))
+    db.download(b.state_ptrs_of(gb))
+    for n in ga:
+        assert np.array_equal(ga[n], gb[n]), n
+    assert da.launches_per_step() == db.launches_per_step() > 10
+
+
+def test_upload_download_round_trip():
+    case = small_moist()
+    dom = domain_from_case(case)
+    back = case.empty_state()
+    dom.download(case.state_ptrs_of(back))
+    for n, v in case.state.items():
+        if n == "w":
+            exp = v.copy()
+            exp[..., 0] = 0.0
+            assert np.array_equal(back[n], exp)
+        else:
+            assert np.array_equal(back[n], v), n
