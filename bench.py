@@ -146,15 +146,20 @@ def make_case(args, rank=0):
     from regcm_gb300 import case as cs
     prec = abi.MLC_PREC_MIXED if args.precision == "mixed" else abi.MLC_PREC_FP64
     if args.config == "c1":
-        return cs.config1(seed=1 + rank, precision=prec)
+        n = args.size or 512
+        return cs.config1(nx=n, ny=n, seed=1 + rank, precision=prec)
     if args.config == "c0":
-        return cs.config0(seed=rank, precision=prec)
+        n = args.size or 64
+        return cs.config0(nx=n, ny=n, seed=rank, precision=prec)
     raise SystemExit(f"unknown config {args.config}")
 
 
 def workload_name(args):
-    return {"c1": "moloch-moist-512x512x41-dx3km-dt20-ns4",
-            "c0": "moloch-dry-64x64x30-dx12km-dt60-ns3"}[args.config]
+    if args.config == "c1":
+        n = args.size or 512
+        return f"moloch-moist-{n}x{n}x41-dx3km-dt20-ns4"
+    n = args.size or 64
+    return f"moloch-dry-{n}x{n}x30-dx12km-dt60-ns3"
 
 
 # ---- CPU oracle timing -------------------------------------------------------
@@ -284,7 +289,7 @@ def run_ours(args, rank, world):
 
     # end-to-end through the C ABI with pinned host buffers
     e2e = None
-    if rank == 0 or world > 1:
+    if not args.no_e2e:
         inputs = {k: case.state[k] for k in ("u", "v", "w", "pai", "tetav", "qx")}
         if case.dims.ntr:
             inputs["trac"] = case.state["trac"]
@@ -347,6 +352,8 @@ def main():
     ap.add_argument("--config", default="c1", choices=["c0", "c1"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--size", type=int, default=0, help="cross points per side (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
