@@ -230,6 +230,24 @@ int mlc_launches_per_step(const mlc_ctx *ctx);
 /* Record steps into CUDA graphs (default 1) or launch them one by one (0). */
 int mlc_set_graphs(mlc_ctx *ctx, int on);
 
+/* ---- mass budget without allocation (no counterpart in the reference) --
+ * For callers that own their device memory and cannot let the library call
+ * cudaMalloc (a host model whose memory manager owns the device heap, code
+ * in callbacks or inside graph capture): the mass budget of
+ * Main/mod_massck.F90:77-170 from caller-owned DEVICE arrays in the packed
+ * layout above (rho, dz: cross 3-D; qx: cross 3-D x nqx; u, v: staggered
+ * 3-D; ps: cross 2-D).  out (device) receives 7 doubles: drymass, dryadv,
+ * qmass, qadv, ps max, ps min, non-finite flag.  dt is the model step.
+ * Partial sums live in a fixed 256 KiB file-scope device array, so domains
+ * with more than 32768 rows ((iy-1)*kz) get MLC_ERR_TOO_LARGE.  The first
+ * call on each device looks up that array's address: make it before any
+ * stream capture.  Kernels are enqueued on `stream` (a cudaStream_t, NULL =
+ * default stream) and the call returns without waiting; calls that overlap
+ * on the GPU share the array and race, so serialise them. */
+int mlc_mass_budget_noalloc(const mlc_dims *d, double dx, double dt, const double *rho,
+                            const double *dz, const double *qx, const double *u,
+                            const double *v, const double *ps, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
