@@ -319,6 +319,9 @@ def run_ours(args, rank, world):
                "d2h_bytes_per_step": d2h, "steps": ne, "ms_per_step": 1000.0 * te / ne}
     dom.close()
 
+    side = None
+    if args.precision == "fp64" and not args.no_mixed:
+        side = run_mixed_side(args, rank)
     if rank != 0:
         return
     cpu = None
@@ -336,11 +339,34 @@ def run_ours(args, rank, world):
         "config": {"workload": workload_name(args), "points_per_domain": pts,
                    "precision": args.precision, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (state > 1 GB)"},
-        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "side_by_side": side,
         "gpu_launches": launches * args.steps, "clocks": clk.summary(),
         "diag": {"ps_min": diag.ps_min, "ps_max": diag.ps_max, "drymass": diag.drymass},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_mixed_side(args, rank):
+    """The same workload in mixed precision (FP32 fields, FP64 solve/Exner/theta),
+    timed the same way, for the FP64-and-FP32 side-by-side report."""
+    import torch
+    from regcm_gb300 import abi
+    from regcm_gb300.moloch import domain_from_case
+    lib = abi.load()
+    import copy
+    margs = copy.copy(args)
+    margs.precision = "mixed"
+    case = make_case(margs, rank)
+    dom = domain_from_case(case)
+    dom.step(args.warmup)
+    diag = abi.mlc_diag()
+    ms = C.c_float()
+    abi.check(lib.mlc_step_timed(dom._ctx, args.steps, C.byref(diag), C.byref(ms)), "mixed")
+    dom.close()
+    torch.cuda.synchronize()
+    t = ms.value / 1000.0
+    return {"mixed": {"value": case.points * args.steps / t, "unit": UNIT,
+                      "ms_per_step": 1000.0 * t / args.steps, "dtype": "f32+f64"}}
 
 
 def main():
@@ -353,6 +379,7 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision side run")
     ap.add_argument("--size", type=int, default=0, help="cross points per side (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

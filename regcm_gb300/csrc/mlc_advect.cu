@@ -38,18 +38,32 @@ template <> struct FlowEps<float> {
   static __device__ __forceinline__ float num() { return 1.0e-15f; }
 };
 
-template <class R>
-__device__ __forceinline__ R flow_param(R num, R den) {
-  if (fabs(den) < FlowEps<R>::den()) return fabs(num) < FlowEps<R>::num() ? R(1) : R(0);
-  return num / den;
-}
-
-// b = max(0, min(2, max(r, min(2r, 1)))) then zphi = is + zamu*b - is*b
-template <class R>
-__device__ __forceinline__ R waf_phi(R is, R zamu, R r) {
-  R m = fmin(R(2) * r, R(1));
-  R b = fmax(R(0), fmin(R(2), fmax(r, m)));
-  return is + zamu * b - is * b;
+// WAF flux  hvel*((1+phi)*a + (1-phi)*c)  with  phi = is + zamu*b - is*b  and
+// the limiter  b = max(0, min(2, max(r, min(2r, 1))))  of  r = num/den
+// (local_flow_param, Main/mod_moloch.F90:1571-1590; the flux lines
+// :877-883, :986-993, :1017-1024).  In every use den = c - a, so
+//   (1+phi)*a + (1-phi)*c = (a + c) - phi*den,
+//   phi*den = is*den + (zamu - is)*B,   B = b*den,
+// and B is 0, 2*num, den, num or 2*den as r falls in (-inf,0], (0,1/2),
+// [1/2,1], (1,2) or [2,inf): the division num/den is never formed.  The
+// result equals the reference's to rounding (b is continuous in r, so the
+// region tests need no exact ties), at a third of the FP64 instructions.
+template <class T>
+__device__ __forceinline__ T waf_flux(T hvel, T is, T zamu, T a, T c, T num) {
+  const T den = c - a;
+  const T aden = fabs(den);
+  T B;
+  if (aden < FlowEps<T>::den()) {
+    B = fabs(num) < FlowEps<T>::num() ? den : T(0);  // r = 1 or r = 0
+  } else {
+    const T q = den < T(0) ? -num : num;  // r = q / |den|
+    if (q <= T(0)) B = T(0);
+    else if (q < T(0.5) * aden) B = num + num;
+    else if (q <= aden) B = den;
+    else if (q < T(2) * aden) B = num;
+    else B = den + den;
+  }
+  return hvel * ((a + c) - (is * den + (zamu - is) * B));
 }
 
 template <class R>
@@ -82,70 +96,71 @@ __global__ void k_adv_prep(Geom g, const R *__restrict__ u, const R *__restrict_
   }
 }
 
-// Two vertical WAF passes for one column of one field (:858-922).
-template <class R>
-__global__ void k_adv_vertical(Geom g, Scal c, Stat<R> sa, const R *__restrict__ s, AdvTable<R> t) {
+// Two vertical WAF passes for one column of one field (:858-922).  R is the
+// type of the winds and metric, T the type of the advected field and of the
+// arithmetic (T = R except for the FP64 Exner field of a mixed domain).
+template <class R, class T>
+__global__ void k_adv_vertical(Geom g, Scal c, Stat<R> sa, const R *__restrict__ s, AdvTable<T> t) {
   extern __shared__ unsigned char smem_raw[];
-  R *smem = reinterpret_cast<R *>(smem_raw);
+  T *smem = reinterpret_cast<T *>(smem_raw);
   const int nth = blockDim.x * blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int kz = g.kz;
-  R *col = smem;                                 // field column, levels 1..kz
-  R *flx = smem + (size_t)(kz + 2) * nth;        // wfw, interfaces 1..kz+1
-  R *sc = smem + (size_t)2 * (kz + 2) * nth;     // s, levels 1..kz+1
+  T *col = smem;                                 // field column, levels 1..kz
+  T *flx = smem + (size_t)(kz + 2) * nth;        // wfw, interfaces 1..kz+1
+  T *sc = smem + (size_t)2 * (kz + 2) * nth;     // s, levels 1..kz+1
 #define COL(a, k) a[(size_t)(k) * nth + tid]
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int f = blockIdx.z;
   if (j > g.jx - 1 || i > g.iy - 1) return;
   const size_t ij = g.at2(j, i), PS = g.PS;
-  const R dtrdz = R(0.5) * (R(c.dtstepa) * R(c.rdzita));
-  const R *src = t.cur[f];
+  const T dtrdz = T(0.5) * (T(c.dtstepa) * T(c.rdzita));
+  const T *src = t.cur[f];
   for (int k = 1; k <= kz; ++k) COL(col, k) = src[ij + (size_t)(k - 1) * PS];
-  for (int k = 1; k <= kz + 1; ++k) COL(sc, k) = s[ij + (size_t)(k - 1) * PS];
+  for (int k = 1; k <= kz + 1; ++k) COL(sc, k) = T(s[ij + (size_t)(k - 1) * PS]);
   for (int pass = 0; pass < 2; ++pass) {
-    COL(flx, 1) = R(0);
-    COL(flx, kz + 1) = R(0);
+    COL(flx, 1) = T(0);
+    COL(flx, kz + 1) = T(0);
     for (int k = 1; k <= kz - 1; ++k) {
-      const R skp = COL(sc, k + 1);
-      const R zamu = skp * dtrdz;
-      R is;
+      const T skp = COL(sc, k + 1);
+      const T zamu = skp * dtrdz;
+      T is;
       int k1, k1p1;
-      if (zamu >= R(0)) {
-        is = R(1); k1 = k + 1; k1p1 = k1 + 1;
+      if (zamu >= T(0)) {
+        is = T(1); k1 = k + 1; k1p1 = k1 + 1;
         if (k1p1 > kz) k1p1 = kz;
       } else {
-        is = R(-1); k1 = k - 1; k1p1 = k;
+        is = T(-1); k1 = k - 1; k1p1 = k;
         if (k1 < 1) k1 = 1;
       }
-      const R r = flow_param<R>(COL(col, k1) - COL(col, k1p1), COL(col, k) - COL(col, k + 1));
-      const R zphi = waf_phi<R>(is, zamu, r);
-      COL(flx, k + 1) = R(0.5) * skp * ((R(1) + zphi) * COL(col, k + 1) + (R(1) - zphi) * COL(col, k));
+      COL(flx, k + 1) = waf_flux<T>(T(0.5) * skp, is, zamu, COL(col, k + 1), COL(col, k),
+                                    COL(col, k1) - COL(col, k1p1));
     }
     for (int k = 1; k <= kz; ++k) {
       const size_t o = ij + (size_t)(k - 1) * PS;
-      const R zrfmu = sa.zrfmu[o];
-      const R zrfmd = sa.zrfmd[o];
-      const R pk = COL(col, k);
-      const R zdv = (COL(sc, k) * zrfmu - COL(sc, k + 1) * zrfmd) * pk;
+      const T zrfmu = T(sa.zrfmu[o]);
+      const T zrfmd = T(sa.zrfmd[o]);
+      const T pk = COL(col, k);
+      const T zdv = (COL(sc, k) * zrfmu - COL(sc, k + 1) * zrfmd) * pk;
       COL(col, k) = pk - COL(flx, k) * zrfmu + COL(flx, k + 1) * zrfmd + zdv;
     }
   }
-  R *dst = t.wz[f];
+  T *dst = t.wz[f];
   for (int k = 1; k <= kz; ++k) dst[ij + (size_t)(k - 1) * PS] = COL(col, k);
 #undef COL
 }
 
 // Meridional then zonal WAF for one tile (:984-1038; ROTLLR :926-983).
-template <class R>
+template <class R, class T>
 __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Stat<R> sa,
                                                             const R *__restrict__ u,
-                                                            const R *__restrict__ v, AdvTable<R> t) {
+                                                            const R *__restrict__ v, AdvTable<T> t) {
   constexpr int WJ = kTJ + 4;  // columns J0-2 .. J0+TJ+1
-  __shared__ R wz_s[kTI + 4][WJ];      // rows I0-2 .. I0+TI+1
-  __shared__ R zpby_s[kTI + 1][WJ];    // rows I0 .. I0+TI
-  __shared__ R p0_s[kTI][WJ];          // rows I0 .. I0+TI-1
-  __shared__ R zpbw_s[kTI][kTJ + 1];   // columns J0 .. J0+TJ
+  __shared__ T wz_s[kTI + 4][WJ];      // rows I0-2 .. I0+TI+1
+  __shared__ T zpby_s[kTI + 1][WJ];    // rows I0 .. I0+TI
+  __shared__ T p0_s[kTI][WJ];          // rows I0 .. I0+TI-1
+  __shared__ T zpbw_s[kTI][kTJ + 1];   // columns J0 .. J0+TJ
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   const int nf = t.n;
   const int f = blockIdx.z % nf;
@@ -154,13 +169,13 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
   const int tid = threadIdx.y * kTJ + threadIdx.x;
   const int nth = kTJ * kTI;
   const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
-  const R *pp = t.cur[f] + ko;
-  const R *wz = t.wz[f] + ko;
-  R *out = t.out[f] + ko;
+  const T *pp = t.cur[f] + ko;
+  const T *wz = t.wz[f] + ko;
+  T *out = t.out[f] + ko;
   const R *uk = u + ko;
   const R *vk = v + ko;
-  const R dta = R(c.dtstepa);
-  const R dtrdx = dta * R(c.rdx), dtrdy = dta * R(c.rdx);
+  const T dta = T(c.dtstepa);
+  const T dtrdx = dta * T(c.rdx), dtrdy = dta * T(c.rdx);
   const bool rot = c.lrotllr != 0;
   const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
   (void)kz;
@@ -169,7 +184,7 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
   for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
     const int rr = e / WJ, cc = e % WJ;
     const int i = I0 - 2 + rr, j = J0 - 2 + cc;
-    R x = R(0);
+    T x = T(0);
     if (i >= 1 && i <= iy - 1 && j >= 1 && j <= jx - 1) x = wz[g.at2(j, i)];
     wz_s[rr][cc] = x;
   }
@@ -178,21 +193,20 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
   for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
     const int rr = e / WJ, cc = e % WJ;
     const int i = I0 + rr, j = J0 - 2 + cc;
-    R x = R(0);
+    T x = T(0);
     if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 1) {
       const size_t ij = g.at2(j, i);
-      const R vv = vk[ij];
-      const R zamu = rot ? vv * dtrdy : vv * sa.msfv[ij] * dtrdy;
-      R is;
+      const T vv = T(vk[ij]);
+      const T zamu = rot ? vv * dtrdy : vv * T(sa.msfv[ij]) * dtrdy;
+      T is;
       int ih;
-      if (zamu > R(0)) { is = R(1); ih = i - 1; }
-      else { is = R(-1); ih = min(i + 1, imax); }
+      if (zamu > T(0)) { is = T(1); ih = i - 1; }
+      else { is = T(-1); ih = min(i + 1, imax); }
       const int ihm1 = max(ih - 1, imin);
       // shared-memory row of global row i is i - (I0 - 2)
       const int b = 2 - I0;
-      const R r = flow_param<R>(wz_s[ih + b][cc] - wz_s[ihm1 + b][cc], wz_s[i + b][cc] - wz_s[i - 1 + b][cc]);
-      const R zphi = waf_phi<R>(is, zamu, r);
-      x = R(0.5) * vv * ((R(1) + zphi) * wz_s[i - 1 + b][cc] + (R(1) - zphi) * wz_s[i + b][cc]);
+      x = waf_flux<T>(T(0.5) * vv, is, zamu, wz_s[i - 1 + b][cc], wz_s[i + b][cc],
+                      wz_s[ih + b][cc] - wz_s[ihm1 + b][cc]);
     }
     zpby_s[rr][cc] = x;
   }
@@ -201,25 +215,25 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
   for (int e = tid; e < kTI * WJ; e += nth) {
     const int rr = e / WJ, cc = e % WJ;
     const int i = I0 + rr, j = J0 - 2 + cc;
-    R x = R(0);
+    T x = T(0);
     if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
       const size_t ij = g.at2(j, i), ijN = ij + (size_t)g.P;
-      const R fz = sa.fmz[ko + ij];
-      const R ppk = pp[ij];
-      const R wzk = wz_s[rr + 2][cc];
+      const T fz = T(sa.fmz[ko + ij]);
+      const T ppk = pp[ij];
+      const T wzk = wz_s[rr + 2][cc];
       if (rot) {
-        const R zhxvtn = dtrdy * sa.rmv[ijN] * sa.msfx[ij];
-        const R zhxvts = dtrdy * sa.rmv[ij] * sa.msfx[ij];
-        const R zrfmn = zhxvtn * fz * sa.rfmzv[ko + ijN];
-        const R zrfms = zhxvts * fz * sa.rfmzv[ko + ij];
-        const R zdv = (vk[ijN] * zrfmn - vk[ij] * zrfms) * ppk;
+        const T zhxvtn = dtrdy * T(sa.rmv[ijN]) * T(sa.msfx[ij]);
+        const T zhxvts = dtrdy * T(sa.rmv[ij]) * T(sa.msfx[ij]);
+        const T zrfmn = zhxvtn * fz * T(sa.rfmzv[ko + ijN]);
+        const T zrfms = zhxvts * fz * T(sa.rfmzv[ko + ij]);
+        const T zdv = (T(vk[ijN]) * zrfmn - T(vk[ij]) * zrfms) * ppk;
         x = wzk + (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
       } else {
         // rfmzu as in the reference (Main/mod_moloch.F90:1000-1001)
-        const R zrfmn = dtrdy * fz * sa.rfmzu[ko + ijN];
-        const R zrfms = dtrdy * fz * sa.rfmzu[ko + ij];
-        const R zdv = (vk[ijN] * sa.rmv[ijN] * zrfmn - vk[ij] * sa.rmv[ij] * zrfms) * ppk;
-        x = wzk + sa.mx2[ij] * (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
+        const T zrfmn = dtrdy * fz * T(sa.rfmzu[ko + ijN]);
+        const T zrfms = dtrdy * fz * T(sa.rfmzu[ko + ij]);
+        const T zdv = (T(vk[ijN]) * T(sa.rmv[ijN]) * zrfmn - T(vk[ij]) * T(sa.rmv[ij]) * zrfms) * ppk;
+        x = wzk + T(sa.mx2[ij]) * (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
       }
     }
     p0_s[rr][cc] = x;
@@ -229,20 +243,19 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
   for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
     const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
     const int i = I0 + rr, j = J0 + cc;
-    R x = R(0);
+    T x = T(0);
     if (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
       const size_t ij = g.at2(j, i);
-      const R uu = uk[ij];
-      const R zamu = uu * sa.msfu[ij] * dtrdx;
-      R is;
+      const T uu = T(uk[ij]);
+      const T zamu = uu * T(sa.msfu[ij]) * dtrdx;
+      T is;
       int jh;
-      if (zamu > R(0)) { is = R(1); jh = j - 1; }
-      else { is = R(-1); jh = min(j + 1, jmax); }
+      if (zamu > T(0)) { is = T(1); jh = j - 1; }
+      else { is = T(-1); jh = min(j + 1, jmax); }
       const int jhm1 = max(jh - 1, jmin);
       const int b = 2 - J0;  // p0_s column of global column j is j - (J0 - 2)
-      const R r = flow_param<R>(p0_s[rr][jh + b] - p0_s[rr][jhm1 + b], p0_s[rr][j + b] - p0_s[rr][j - 1 + b]);
-      const R zphi = waf_phi<R>(is, zamu, r);
-      x = R(0.5) * uu * ((R(1) + zphi) * p0_s[rr][j - 1 + b] + (R(1) - zphi) * p0_s[rr][j + b]);
+      x = waf_flux<T>(T(0.5) * uu, is, zamu, p0_s[rr][j - 1 + b], p0_s[rr][j + b],
+                      p0_s[rr][jh + b] - p0_s[rr][jhm1 + b]);
     }
     zpbw_s[rr][cc] = x;
   }
@@ -253,22 +266,22 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
     const int i = I0 + rr, j = J0 + cc;
     if (i <= iy - 1 && j <= jx - 1) {
       const size_t ij = g.at2(j, i);
-      const R ppk = pp[ij];
-      R x = ppk;
+      const T ppk = pp[ij];
+      T x = ppk;
       if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
-        const R fz = sa.fmz[ko + ij];
-        const R p0k = p0_s[rr][cc + 2];
+        const T fz = T(sa.fmz[ko + ij]);
+        const T p0k = p0_s[rr][cc + 2];
         if (rot) {
-          const R zcostx = dtrdx * sa.msfx[ij];
-          const R zrfmw = zcostx * fz * sa.rfmzu[ko + ij];
-          const R zrfme = zcostx * fz * sa.rfmzu[ko + ij + 1];
-          const R zdv = (uk[ij + 1] * zrfme - uk[ij] * zrfmw) * ppk;
+          const T zcostx = dtrdx * T(sa.msfx[ij]);
+          const T zrfmw = zcostx * fz * T(sa.rfmzu[ko + ij]);
+          const T zrfme = zcostx * fz * T(sa.rfmzu[ko + ij + 1]);
+          const T zdv = (T(uk[ij + 1]) * zrfme - T(uk[ij]) * zrfmw) * ppk;
           x = p0k + zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv;
         } else {
-          const R zrfmw = dtrdx * fz * sa.rfmzu[ko + ij];
-          const R zrfme = dtrdx * fz * sa.rfmzu[ko + ij + 1];
-          const R zdv = (uk[ij + 1] * sa.rmu[ij + 1] * zrfme - uk[ij] * sa.rmu[ij] * zrfmw) * ppk;
-          x = p0k + sa.mx2[ij] * (zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv);
+          const T zrfmw = dtrdx * fz * T(sa.rfmzu[ko + ij]);
+          const T zrfme = dtrdx * fz * T(sa.rfmzu[ko + ij + 1]);
+          const T zdv = (T(uk[ij + 1]) * T(sa.rmu[ij + 1]) * zrfme - T(uk[ij]) * T(sa.rmu[ij]) * zrfmw) * ppk;
+          x = p0k + T(sa.mx2[ij]) * (zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv);
         }
       }
       out[ij] = x;
@@ -354,22 +367,46 @@ void Launch<R>::adv_prep(const Geom &g, const State<R> &st, const Work<R> &wk, c
   k_adv_prep<R><<<grid2(g.jx - 1, g.iy - 1, b), b, 0, s>>>(g, st.u, st.v, st.w, st.ux, st.vx, wk.wx);
 }
 
+template <class R, class T>
+void launch_vertical(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
+                     const AdvTable<T> &t, cudaStream_t s) {
+  const dim3 b(32, 2);
+  const size_t smem = (size_t)3 * (g.kz + 2) * b.x * b.y * sizeof(T);
+  dim3 grd = grid2(g.jx - 1, g.iy - 1, b);
+  grd.z = (unsigned)t.n;
+  k_adv_vertical<R, T><<<grd, b, smem, s>>>(g, c, sa, wk.s, t);
+}
+
+template <class R, class T>
+void launch_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                       const AdvTable<T> &t, cudaStream_t s) {
+  dim3 grd((unsigned)((g.jx - 1 + kTJ - 1) / kTJ), (unsigned)((g.iy - 1 + kTI - 1) / kTI),
+           (unsigned)(t.n * g.kz));
+  k_adv_horizontal<R, T><<<grd, dim3(kTJ, kTI), 0, s>>>(g, c, sa, st.u, st.v, t);
+}
+
 template <class R>
 void Launch<R>::adv_vertical(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
                              const AdvTable<R> &t, cudaStream_t s) {
-  const dim3 b(32, 2);
-  const size_t smem = (size_t)3 * (g.kz + 2) * b.x * b.y * sizeof(R);
-  dim3 grd = grid2(g.jx - 1, g.iy - 1, b);
-  grd.z = (unsigned)t.n;
-  k_adv_vertical<R><<<grd, b, smem, s>>>(g, c, sa, wk.s, t);
+  launch_vertical<R, R>(g, c, sa, wk, t, s);
 }
 
 template <class R>
 void Launch<R>::adv_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                                const AdvTable<R> &t, cudaStream_t s) {
-  dim3 grd((unsigned)((g.jx - 1 + kTJ - 1) / kTJ), (unsigned)((g.iy - 1 + kTI - 1) / kTI),
-           (unsigned)(t.n * g.kz));
-  k_adv_horizontal<R><<<grd, dim3(kTJ, kTI), 0, s>>>(g, c, sa, st.u, st.v, t);
+  launch_horizontal<R, R>(g, c, sa, st, t, s);
+}
+
+template <class R>
+void Launch<R>::adv_vertical_f64(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
+                                 const AdvTable<double> &t, cudaStream_t s) {
+  launch_vertical<R, double>(g, c, sa, wk, t, s);
+}
+
+template <class R>
+void Launch<R>::adv_horizontal_f64(const Geom &g, const Scal &c, const Stat<R> &sa,
+                                   const State<R> &st, const AdvTable<double> &t, cudaStream_t s) {
+  launch_horizontal<R, double>(g, c, sa, st, t, s);
 }
 
 template <class R>
@@ -387,8 +424,12 @@ void Launch<R>::adv_back(const Geom &g, const State<R> &st, const Work<R> &wk, c
 
 template <class R>
 cudaError_t Launch<R>::configure_advect() {
-  return cudaFuncSetAttribute(k_adv_vertical<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              200 * 1024);
+  cudaError_t e = cudaFuncSetAttribute(k_adv_vertical<R, R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_adv_vertical<R, double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  return e;
 }
 
 template struct Launch<double>;

@@ -8,6 +8,7 @@
 // double operation the Fortran parameter expression performs, so host and
 // device code see bit-identical constants.
 #pragma once
+#include <cmath>
 
 #ifdef __CUDACC__
 #define MLC_HD __host__ __device__
@@ -93,6 +94,14 @@ MLC_HD inline double pfwsat(double t, double p) {
   double cap = 0.15 * p;
   es = cap < es ? cap : es;
   return kEp2 * (es / (p - es));
+}
+
+// p = pai**(cp/R) * p00 (Main/mod_moloch.F90:349).  cp/R evaluates to 3.5
+// exactly in IEEE double (cpd = 3.5*rgas), so pai**3.5 = pai^3 * sqrt(pai):
+// three multiplies and a square root instead of pow, equal to a few ulp.
+static_assert(kCpovr == 3.5, "cp/R must be 3.5 for the pai^3*sqrt(pai) form");
+MLC_HD inline double exner_to_pressure(double pai) {
+  return pai * pai * pai * sqrt(pai) * kP00;
 }
 
 // G(zeta) of Share/mod_zita.F90:105-115.

@@ -45,18 +45,21 @@ template <class R>
 struct Arrays {
   State<R> st{};
   // second halves of the ping-pong pairs
-  R *u2, *v2, *tetav2, *pai2, *ux2, *vx2, *qx2, *trac2, *wx2;
+  R *u2, *v2, *ux2, *vx2, *qx2, *trac2, *wx2;
+  double *pai2, *tetav2;
   R *wz[kMaxAdv];
+  double *wz_pai, *wz_tet;  // wz of the FP64 fields of a mixed domain
   Work<R> wk{};
   Stat<R> sa{};
   Bdy<R> bd{};
   // writable views of the static arrays
   R *fmz, *fmzf, *rfmzu, *rfmzv, *zrfmu, *zrfmd, *hx, *hy, *msfu, *msfv, *msfx, *mx2, *rmu, *rmv,
       *coru, *corv;
+  double *fmz_d, *fmzf_d;
   double *zeta, *dz, *hefc, *fcx, *tnudge, *ffilt, *gzitakh, *xkdamp, *xknu, *gzitak, *rlat;
   int32_t *ibnd_cr, *ibnd_ud, *ibnd_vd;
-  R *bfield[2][8];  // xtb, xqb, xpaib, xlb, xib, dub, dvb, chib
-  double *xpsb[2];
+  R *bfield[2][8];  // xtb, xqb, (unused), xlb, xib, dub, dvb, chib
+  double *xpaib[2], *xpsb[2];
   double *staging;
   size_t staging_elems;
   double *partials;
@@ -81,21 +84,30 @@ void carve(Carver &cv, Arrays<R> &a, const Geom &g, const mlc_dims &d, const mlc
   const size_t F = g.field3(), F1 = g.PS * (size_t)(g.kz + 1), P2 = g.PS;
   State<R> &st = a.st;
   st.u = cv.take<R>(F); st.v = cv.take<R>(F); st.w = cv.take<R>(F1);
-  st.pai = cv.take<R>(F); st.tetav = cv.take<R>(F); st.t = cv.take<R>(F);
+  st.pai = cv.take<double>(F); st.tetav = cv.take<double>(F); st.t = cv.take<R>(F);
   st.tvirt = cv.take<R>(F); st.ux = cv.take<R>(F); st.vx = cv.take<R>(F);
   st.p = cv.take<R>(F); st.rho = cv.take<R>(F); st.qsat = cv.take<R>(F);
   st.qx = cv.take<R>(F * d.nqx);
   st.trac = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;
   st.ps = cv.take<double>(P2);
-  a.u2 = cv.take<R>(F); a.v2 = cv.take<R>(F); a.tetav2 = cv.take<R>(F); a.pai2 = cv.take<R>(F);
+  a.u2 = cv.take<R>(F); a.v2 = cv.take<R>(F); a.tetav2 = cv.take<double>(F); a.pai2 = cv.take<double>(F);
   a.ux2 = cv.take<R>(F); a.vx2 = cv.take<R>(F); a.qx2 = cv.take<R>(F * d.nqx);
   a.trac2 = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;
   a.wx2 = cv.take<R>(F);
   const int nadv = n_advected(d, p);
   for (int f = 0; f < kMaxAdv; ++f) a.wz[f] = f < nadv ? cv.take<R>(F) : nullptr;
-  a.wk.s = cv.take<R>(F1); a.wk.zdiv2 = cv.take<R>(F); a.wk.tetavf = cv.take<R>(F1);
+  a.wz_pai = sizeof(R) == sizeof(double) ? nullptr : cv.take<double>(F);
+  a.wz_tet = sizeof(R) == sizeof(double) ? nullptr : cv.take<double>(F);
+  a.wk.s = cv.take<R>(F1); a.wk.zdiv2 = cv.take<R>(F); a.wk.tetavf = cv.take<double>(F1);
   a.wk.wx = cv.take<R>(F);
   a.fmz = cv.take<R>(F); a.fmzf = cv.take<R>(F1); a.rfmzu = cv.take<R>(F); a.rfmzv = cv.take<R>(F);
+  if (sizeof(R) == sizeof(double)) {
+    a.fmz_d = reinterpret_cast<double *>(a.fmz);
+    a.fmzf_d = reinterpret_cast<double *>(a.fmzf);
+  } else {
+    a.fmz_d = cv.take<double>(F);
+    a.fmzf_d = cv.take<double>(F1);
+  }
   a.zrfmu = cv.take<R>(F); a.zrfmd = cv.take<R>(F);
   a.zeta = cv.take<double>(F); a.dz = cv.take<double>(F);
   a.hx = cv.take<R>(P2); a.hy = cv.take<R>(P2); a.msfu = cv.take<R>(P2); a.msfv = cv.take<R>(P2);
@@ -110,7 +122,8 @@ void carve(Carver &cv, Arrays<R> &a, const Geom &g, const mlc_dims &d, const mlc
   for (int b = 0; b < 2; ++b) {
     a.bfield[b][0] = cv.take<R>(F);                                   // xtb
     a.bfield[b][1] = cv.take<R>(F);                                   // xqb
-    a.bfield[b][2] = cv.take<R>(F);                                   // xpaib
+    a.bfield[b][2] = nullptr;
+    a.xpaib[b] = cv.take<double>(F);
     a.bfield[b][3] = (moist_b && p.present_qc) ? cv.take<R>(F) : nullptr;  // xlb
     a.bfield[b][4] = (moist_b && p.present_qi) ? cv.take<R>(F) : nullptr;  // xib
     a.bfield[b][5] = cv.take<R>(F);                                   // dub
@@ -129,6 +142,7 @@ template <class R>
 void bind_views(Arrays<R> &a) {
   Stat<R> &s = a.sa;
   s.fmz = a.fmz; s.fmzf = a.fmzf; s.rfmzu = a.rfmzu; s.rfmzv = a.rfmzv;
+  s.fmz_d = a.fmz_d; s.fmzf_d = a.fmzf_d;
   s.zrfmu = a.zrfmu; s.zrfmd = a.zrfmd; s.zeta = a.zeta; s.dz = a.dz;
   s.hx = a.hx; s.hy = a.hy; s.msfu = a.msfu; s.msfv = a.msfv; s.msfx = a.msfx; s.mx2 = a.mx2;
   s.rmu = a.rmu; s.rmv = a.rmv; s.coru = a.coru; s.corv = a.corv;
@@ -136,7 +150,7 @@ void bind_views(Arrays<R> &a) {
   s.hefc = a.hefc; s.fcx = a.fcx; s.tnudge = a.tnudge; s.ffilt = a.ffilt; s.gzitakh = a.gzitakh;
   s.xkdamp = a.xkdamp; s.xknu = a.xknu; s.gzitak = a.gzitak; s.rlat = a.rlat;
   for (int b = 0; b < 2; ++b) {
-    a.bd.xtb[b] = a.bfield[b][0]; a.bd.xqb[b] = a.bfield[b][1]; a.bd.xpaib[b] = a.bfield[b][2];
+    a.bd.xtb[b] = a.bfield[b][0]; a.bd.xqb[b] = a.bfield[b][1]; a.bd.xpaib[b] = a.xpaib[b];
     a.bd.xlb[b] = a.bfield[b][3]; a.bd.xib[b] = a.bfield[b][4]; a.bd.dub[b] = a.bfield[b][5];
     a.bd.dvb[b] = a.bfield[b][6]; a.bd.chib[b] = a.bfield[b][7]; a.bd.xpsb[b] = a.xpsb[b];
   }
@@ -210,7 +224,8 @@ template <class R>
 struct Roles {
   State<R> st;      // canonical state (current buffers)
   R *u_alt, *v_alt;
-  R *tetav_alt, *pai_alt, *ux_alt, *vx_alt, *qx_alt, *trac_alt, *wx_alt;
+  R *ux_alt, *vx_alt, *qx_alt, *trac_alt, *wx_alt;
+  double *pai_alt, *tetav_alt;
 };
 
 template <class R>
@@ -299,10 +314,17 @@ int enqueue_step(mlc_ctx *x, Arrays<R> &a, Recorder *rec = nullptr) {
     // ---- advection ----
     REC("adv_prep", L::adv_prep(g, r.st, wk, s)); ++nl;
     AdvTable<R> t{};
+    AdvTable<double> tp{};  // the FP64 fields (theta_v, Exner) of a mixed domain
     int n = 0;
     auto add = [&](const R *cur, R *out) { t.cur[n] = cur; t.wz[n] = a.wz[n]; t.out[n] = out; ++n; };
-    add(r.st.tetav, r.tetav_alt);
-    add(r.st.pai, r.pai_alt);
+    if constexpr (sizeof(R) == sizeof(double)) {
+      add(reinterpret_cast<const R *>(r.st.tetav), reinterpret_cast<R *>(r.tetav_alt));
+      add(reinterpret_cast<const R *>(r.st.pai), reinterpret_cast<R *>(r.pai_alt));
+    } else {
+      tp.cur[0] = r.st.tetav; tp.wz[0] = a.wz_tet; tp.out[0] = r.tetav_alt;
+      tp.cur[1] = r.st.pai; tp.wz[1] = a.wz_pai; tp.out[1] = r.pai_alt;
+      tp.n = 2;
+    }
     add(r.st.ux, r.ux_alt);
     add(r.st.vx, r.vx_alt);
     add(wk.wx, a.wx2);
@@ -313,6 +335,10 @@ int enqueue_step(mlc_ctx *x, Arrays<R> &a, Recorder *rec = nullptr) {
     t.n = n;
     REC("adv_vertical", L::adv_vertical(g, c, a.sa, wk, t, s)); ++nl;
     REC("adv_horizontal", L::adv_horizontal(g, c, a.sa, r.st, t, s)); ++nl;
+    if (tp.n) {
+      REC("adv_vertical_f64", L::adv_vertical_f64(g, c, a.sa, wk, tp, s)); ++nl;
+      REC("adv_horizontal_f64", L::adv_horizontal_f64(g, c, a.sa, r.st, tp, s)); ++nl;
+    }
     if (p.ipptls == 0 && d.nqx > 1) {
       // species that are not advected keep their values in the other buffer
       cudaMemcpyAsync(r.qx_alt + F, r.st.qx + F, (size_t)(d.nqx - 1) * F * sizeof(R),
@@ -447,6 +473,10 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
   // 3-D metric: one field at a time through the staging buffer
   MLC_CHK(put3<R>(x, SG, s->fmz, a.fmz, jx - 1, iy - 1, kz, 0));
   MLC_CHK(put3<R>(x, SG, s->fmzf, a.fmzf, jx - 1, iy - 1, kz + 1, 0));
+  if (sizeof(R) != sizeof(double)) {
+    MLC_CHK(put3<double>(x, SG, s->fmz, a.fmz_d, jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, SG, s->fmzf, a.fmzf_d, jx - 1, iy - 1, kz + 1, 0));
+  }
   MLC_CHK(put3<R>(x, SG, s->rfmzu, a.rfmzu, jx, iy - 1, kz, 0));
   MLC_CHK(put3<R>(x, SG, s->rfmzv, a.rfmzv, jx - 1, iy, kz, 0));
   MLC_CHK(put3<double>(x, SG, s->zeta, a.zeta, jx - 1, iy - 1, kz, 0));
@@ -547,9 +577,11 @@ int upload_state_impl(mlc_ctx *x, Arrays<R> &a, const mlc_state_ptrs *h) {
   MLC_CHK(put3<R>(x, SG, h->u, st.u, jx, iy - 1, kz, adv((size_t)jx * (iy - 1) * kz)));
   MLC_CHK(put3<R>(x, SG, h->v, st.v, jx - 1, iy, kz, adv((size_t)(jx - 1) * iy * kz)));
   MLC_CHK(put3<R>(x, SG, h->w, st.w, jx - 1, iy - 1, kz + 1, adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
-  R *f3[] = {st.pai, st.tetav, st.t, st.tvirt, st.ux, st.vx, st.p, st.rho, st.qsat};
-  const double *h3[] = {h->pai, h->tetav, h->t, h->tvirt, h->ux, h->vx, h->p, h->rho, h->qsat};
-  for (int q = 0; q < 9; ++q) MLC_CHK(put3<R>(x, SG, h3[q], f3[q], jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(put3<double>(x, SG, h->pai, st.pai, jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(put3<double>(x, SG, h->tetav, st.tetav, jx - 1, iy - 1, kz, adv(c3)));
+  R *f3[] = {st.t, st.tvirt, st.ux, st.vx, st.p, st.rho, st.qsat};
+  const double *h3[] = {h->t, h->tvirt, h->ux, h->vx, h->p, h->rho, h->qsat};
+  for (int q = 0; q < 7; ++q) MLC_CHK(put3<R>(x, SG, h3[q], f3[q], jx - 1, iy - 1, kz, adv(c3)));
   const size_t F = x->g.field3();
   for (int n = 0; n < d.nqx && h->qx; ++n)
     MLC_CHK(put3<R>(x, SG, h->qx + n * c3, st.qx + n * F, jx - 1, iy - 1, kz, adv(c3)));
@@ -577,9 +609,11 @@ int download_state_impl(mlc_ctx *x, Arrays<R> &a, const mlc_state_ptrs *h) {
   MLC_CHK(get3<R>(x, SG, st.u, h->u, jx, iy - 1, kz, adv((size_t)jx * (iy - 1) * kz)));
   MLC_CHK(get3<R>(x, SG, st.v, h->v, jx - 1, iy, kz, adv((size_t)(jx - 1) * iy * kz)));
   MLC_CHK(get3<R>(x, SG, st.w, h->w, jx - 1, iy - 1, kz + 1, adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
-  const R *f3[] = {st.pai, st.tetav, st.t, st.tvirt, st.ux, st.vx, st.p, st.rho, st.qsat};
-  double *h3[] = {h->pai, h->tetav, h->t, h->tvirt, h->ux, h->vx, h->p, h->rho, h->qsat};
-  for (int q = 0; q < 9; ++q) MLC_CHK(get3<R>(x, SG, f3[q], h3[q], jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(get3<double>(x, SG, st.pai, h->pai, jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(get3<double>(x, SG, st.tetav, h->tetav, jx - 1, iy - 1, kz, adv(c3)));
+  const R *f3[] = {st.t, st.tvirt, st.ux, st.vx, st.p, st.rho, st.qsat};
+  double *h3[] = {h->t, h->tvirt, h->ux, h->vx, h->p, h->rho, h->qsat};
+  for (int q = 0; q < 7; ++q) MLC_CHK(get3<R>(x, SG, f3[q], h3[q], jx - 1, iy - 1, kz, adv(c3)));
   const size_t F = x->g.field3();
   for (int n = 0; n < d.nqx && h->qx; ++n)
     MLC_CHK(get3<R>(x, SG, st.qx + n * F, h->qx + n * c3, jx - 1, iy - 1, kz, adv(c3)));
@@ -608,7 +642,7 @@ int set_boundary_impl(mlc_ctx *x, Arrays<R> &a, const mlc_bdy_ptrs *b) {
     if (d.ntr > 0 && !b->chib[s]) return MLC_ERR_INVALID;
     MLC_CHK(put3<R>(x, SG, b->xtb[s], a.bfield[s][0], jx - 1, iy - 1, kz, 0));
     MLC_CHK(put3<R>(x, SG, b->xqb[s], a.bfield[s][1], jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<R>(x, SG, b->xpaib[s], a.bfield[s][2], jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, SG, b->xpaib[s], a.xpaib[s], jx - 1, iy - 1, kz, 0));
     if (p.present_qc) MLC_CHK(put3<R>(x, SG, b->xlb[s], a.bfield[s][3], jx - 1, iy - 1, kz, 0));
     if (p.present_qi) MLC_CHK(put3<R>(x, SG, b->xib[s], a.bfield[s][4], jx - 1, iy - 1, kz, 0));
     MLC_CHK(put3<R>(x, SG, b->dub[s], a.bfield[s][5], jx, iy - 1, kz, 0));

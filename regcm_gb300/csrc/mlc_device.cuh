@@ -42,6 +42,7 @@ struct Scal {
 template <class R>
 struct Stat {
   const R *fmz, *fmzf, *rfmzu, *rfmzv;   // 3-D
+  const double *fmz_d, *fmzf_d;          // FP64 copies for the vertical solve
   const R *zrfmu, *zrfmd;                // 3-D: (dtrdz*fmz)/fmzf(k), /fmzf(k+1)
   const double *zeta, *dz;               // 3-D, FP64 (surface pressure, budget)
   const R *hx, *hy;                      // 2-D
@@ -55,9 +56,14 @@ struct Stat {
 };
 
 // Prognostic and diagnostic state.
+// The Exner function and theta_v are FP64 in both precision modes: in the
+// implicit w equation cp*theta_v*fmzf*dPi/dzeta nearly cancels g, and FP32
+// rounding of either factor (6e-8 relative) would leave a w forcing of
+// ~3e-6 m/s per substep, large against w itself.
 template <class R>
 struct State {
-  R *u, *v, *w, *pai, *tetav, *t, *tvirt, *ux, *vx, *p, *rho, *qsat;
+  R *u, *v, *w, *t, *tvirt, *ux, *vx, *p, *rho, *qsat;
+  double *pai, *tetav;
   R *qx, *trac;  // species blocks
   double *ps;    // 2-D, FP64
 };
@@ -65,8 +71,8 @@ struct State {
 // Boundary data b0/b1 for one domain.
 template <class R>
 struct Bdy {
-  const R *xtb[2], *xqb[2], *xpaib[2], *xlb[2], *xib[2], *dub[2], *dvb[2], *chib[2];
-  const double *xpsb[2];
+  const R *xtb[2], *xqb[2], *xlb[2], *xib[2], *dub[2], *dvb[2], *chib[2];
+  const double *xpaib[2], *xpsb[2];
 };
 
 // Per-step device scratch that kernels of one step share.
@@ -74,7 +80,7 @@ template <class R>
 struct Work {
   R *s;        // (kz+1) planes
   R *zdiv2;    // raw divergence (kz planes)
-  R *tetavf;   // (kz+1) planes, levels 2..kz used
+  double *tetavf;  // (kz+1) planes, levels 2..kz used (FP64: feeds the solve)
   R *u2, *v2;  // second buffers of the acoustic ping-pong
   R *wx;       // w at half levels
 };

@@ -33,7 +33,7 @@ __global__ void k_end_tvirt(Geom g, Scal c, State<R> st) {
   const size_t ij = g.at2(j, i), F = g.field3();
   for (int k = 1; k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * g.PS;
-    const R tv = st.tetav[o] * st.pai[o];
+    const R tv = R(st.tetav[o] * st.pai[o]);
     st.tvirt[o] = tv;
     if (inner) st.t[o] = tv / qfactor(st.qx, o, F, c.ipptls);
   }
@@ -70,7 +70,7 @@ __global__ void k_bdy_ring(Geom g, Scal c, State<R> st, Bdy<R> bd, const Clock *
     const R un = blend(bd.dub, od);
     st.u[od] = un;
     st.t[ob] = blend(bd.xtb, ob);
-    st.pai[ob] = blend(bd.xpaib, ob);
+    st.pai[ob] = x0 * bd.xpaib[0][ob] + x1 * bd.xpaib[1][ob];
     st.qx[ob] = blend(bd.xqb, ob);
     if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
     if (c.present_qi && c.ipptls > 1) st.qx[ob + 2 * F] = blend(bd.xib, ob);
@@ -99,7 +99,7 @@ __global__ void k_bdy_ring(Geom g, Scal c, State<R> st, Bdy<R> bd, const Clock *
     const R vn = blend(bd.dvb, od);
     st.v[od] = vn;
     st.t[ob] = blend(bd.xtb, ob);
-    st.pai[ob] = blend(bd.xpaib, ob);
+    st.pai[ob] = x0 * bd.xpaib[0][ob] + x1 * bd.xpaib[1][ob];
     st.qx[ob] = blend(bd.xqb, ob);
     if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
     if (c.present_qi && c.ipptls > 1) st.qx[ob + 2 * F] = blend(bd.xib, ob);
@@ -178,7 +178,11 @@ __global__ void k_bdy_relax(Geom g, Scal c, Stat<R> sa, State<R> st, Bdy<R> bd, 
       st.t[o] = f;
     }
     if (ibc <= 0) continue;
-    st.pai[o] = relax(st.pai[o], blend(bd.xpaib, o), ibc, k);
+    {
+      const double xf = sa.hefc[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
+      const double fext = x0 * bd.xpaib[0][o] + x1 * bd.xpaib[1][o];
+      st.pai[o] = (1.0 - xf) * st.pai[o] + xf * fext;
+    }
     st.qx[o] = relax(st.qx[o], blend(bd.xqb, o), ibc, k);
     {
       // morelax_fraction with frac = 0 (:3962-3993)
@@ -229,7 +233,7 @@ __global__ void k_end_cross(Geom g, Scal c, Stat<R> sa, State<R> st) {
   // pressure (FP64 Exner reconstruction)
   for (int k = 1; k <= kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
-    st.p[o] = (R)(pow((double)st.pai[o], kCpovr) * kP00);
+    st.p[o] = (R)exner_to_pressure(st.pai[o]);
   }
   if (inner) {
     // tvirt at kz-1, kz before the clamps: from the boundary's temp_to_tvirt,
@@ -266,7 +270,7 @@ __global__ void k_end_cross(Geom g, Scal c, Stat<R> sa, State<R> st) {
     const R tk = st.t[o];
     const R tv = tk * qfactor(st.qx, o, F, ipp);
     st.tvirt[o] = tv;
-    st.tetav[o] = tv / st.pai[o];
+    st.tetav[o] = (double)tv / st.pai[o];
     const R pk = st.p[o];
     st.rho[o] = pk / (R(kRgas) * tk);
     st.qsat[o] = (R)pfwsat((double)tk, (double)pk);

@@ -42,6 +42,11 @@ template <class R> struct Launch {
                            const AdvTable<R> &t, cudaStream_t s);
   static void adv_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                              const AdvTable<R> &t, cudaStream_t s);
+  // the same two passes for FP64 fields advected with this domain's winds
+  static void adv_vertical_f64(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
+                               const AdvTable<double> &t, cudaStream_t s);
+  static void adv_horizontal_f64(const Geom &g, const Scal &c, const Stat<R> &sa,
+                                 const State<R> &st, const AdvTable<double> &t, cudaStream_t s);
   static void adv_curvature(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                             cudaStream_t s);
   static void adv_back(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s);

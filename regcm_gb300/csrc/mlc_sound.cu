@@ -36,15 +36,15 @@ __device__ __forceinline__ double relax_weight(const int32_t *ibnd, const double
 }
 
 template <class R>
-__global__ void k_sound_prep(Geom g, const R *__restrict__ tetav, R *__restrict__ tetavf) {
+__global__ void k_sound_prep(Geom g, const double *__restrict__ tetav, double *__restrict__ tetavf) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
   // Main/mod_moloch.F90:564-566
-  R lo = tetav[g.at(j, i, 1)];
+  double lo = tetav[g.at(j, i, 1)];
   for (int k = 2; k <= g.kz; ++k) {
-    R hi = tetav[g.at(j, i, k)];
-    tetavf[g.at(j, i, k)] = R(0.5) * (lo + hi);
+    double hi = tetav[g.at(j, i, k)];
+    tetavf[g.at(j, i, k)] = 0.5 * (lo + hi);
     lo = hi;
   }
 }
@@ -104,8 +104,9 @@ __global__ void k_sound_div(Geom g, Scal c, Stat<R> sa, const R *__restrict__ u,
 // consecutive banks).  The recurrence runs in FP64 for either field type.
 template <class R>
 __global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ zraw,
-                              R *__restrict__ s, R *__restrict__ w, R *__restrict__ pai,
-                              const R *__restrict__ tetav, R *__restrict__ tetavf, int last) {
+                              R *__restrict__ s, R *__restrict__ w, double *__restrict__ pai,
+                              const double *__restrict__ tetav, double *__restrict__ tetavf,
+                              int last) {
   extern __shared__ double smem[];
   const int nth = blockDim.x * blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
@@ -136,7 +137,7 @@ __global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ 
     }
     const double skp1 = (double)s[o + PS];
     const double bw = relax_weight(sa.ibnd_cr, sa.hefc, c.nspgx, ij, k);
-    z = z + bw * dtrdz * (double)sa.fmz[o] * (sk - skp1);
+    z = z + bw * dtrdz * sa.fmz_d[o] * (sk - skp1);
     COL(zf, k) = z;
     sk = skp1;
   }
@@ -145,17 +146,17 @@ __global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ 
   double wnext = (double)w[ij + (size_t)kz * PS];  // w(kz+1) = -s(kz+1)
   double wkp1 = 0.0;
   double pai_k = (double)pai[ij + (size_t)(kz - 1) * PS];
-  double tet_k = (double)tetav[ij + (size_t)(kz - 1) * PS];
-  double fmz_k = (double)sa.fmz[ij + (size_t)(kz - 1) * PS];
+  double tet_k = tetav[ij + (size_t)(kz - 1) * PS];
+  double fmz_k = sa.fmz_d[ij + (size_t)(kz - 1) * PS];
   for (int k = kz; k >= 2; --k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     const double pai_m = (double)pai[o - PS];
-    const double tet_m = (double)tetav[o - PS];
-    const double fmz_m = (double)sa.fmz[o - PS];
-    const double fmzf = (double)sa.fmzf[o];
+    const double tet_m = tetav[o - PS];
+    const double fmz_m = sa.fmz_d[o - PS];
+    const double fmzf = sa.fmzf_d[o];
     const double wold = (double)w[o];
-    const double tvf = (double)tetavf[o] - wold * fmzf * dtrdz * (tet_m - tet_k);
-    tetavf[o] = (R)tvf;
+    const double tvf = tetavf[o] - wold * fmzf * dtrdz * (tet_m - tet_k);
+    tetavf[o] = tvf;
     const double zrom1w = kCpd * tvf * fmzf;
     double zwexpl = wold - zrom1w * dtrdz * (pai_m - pai_k) - kGrav * dts;
     zwexpl = zwexpl + kRdrcv * zrom1w * dtrdz * (pai_m * COL(zf, k - 1) - pai_k * COL(zf, k));
@@ -181,15 +182,15 @@ __global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ 
   // Exner function (:668-671)
   for (int k = 1; k <= kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
-    const double pk = (double)pai[o];
-    pai[o] = (R)(pk * (1.0 - kRdrcv * (COL(zf, k) + (dtrdz * (double)sa.fmz[o] *
-                                                     (COL(wp, k) - COL(wp, k + 1))))));
+    const double pk = pai[o];
+    pai[o] = pk * (1.0 - kRdrcv * (COL(zf, k) + (dtrdz * sa.fmz_d[o] *
+                                                 (COL(wp, k) - COL(wp, k + 1)))));
   }
   if (last) {
     // complete s (:728-734)
     for (int k = 2; k <= kz; ++k) {
       const size_t o = ij + (size_t)(k - 1) * PS;
-      s[o] = (R)((COL(wp, k) + (double)s[o]) * (double)sa.fmzf[o]);
+      s[o] = (R)((COL(wp, k) + (double)s[o]) * sa.fmzf_d[o]);
     }
     s[ij] = R(0);
     s[ij + (size_t)kz * PS] = R(0);
@@ -202,7 +203,7 @@ template <class R>
 __global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict__ u_in,
                                  const R *__restrict__ v_in, R *__restrict__ u_out,
                                  R *__restrict__ v_out, const R *__restrict__ zraw,
-                                 const R *__restrict__ pai, const R *__restrict__ tetav) {
+                                 const double *__restrict__ pai, const double *__restrict__ tetav) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx || i > g.iy) return;
@@ -241,10 +242,10 @@ __global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict
           const R xdam = dxrdt * R(sa.xkdamp[k - 1]) * mu;
           un = un + xdam * (zraw[o] - zraw[o - W]);
         }
-        const R zrom1u = halfcp * (tetav[o - W] + tetav[o]);
+        const R zrom1u = halfcp * R(tetav[o - W] + tetav[o]);
         const R zcor1u = cor_u * dts * v_in[o];
         const R bw = R(relax_weight(sa.ibnd_ud, sa.hefc, c.nspgx, ij, k));
-        un = un + bw * (zcor1u - zfz * hxk * gk - zcx * zrom1u * (pai[o] - pai[o - W]));
+        un = un + bw * (zcor1u - zfz * hxk * gk - zcx * zrom1u * R(pai[o] - pai[o - W]));
       }
       u_out[o] = un;
     }
@@ -255,10 +256,10 @@ __global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict
           const R xdam = c.lrotllr ? dxrdt * R(sa.xkdamp[k - 1]) : dxrdt * R(sa.xkdamp[k - 1]) * mv;
           vn = vn + xdam * (zraw[o] - zraw[o - S]);
         }
-        const R zrom1v = halfcp * (tetav[o - S] + tetav[o]);
+        const R zrom1v = halfcp * R(tetav[o - S] + tetav[o]);
         const R zcor1v = cor_v * dts * u_in[o];
         const R bw = R(relax_weight(sa.ibnd_vd, sa.hefc, c.nspgx, ij, k));
-        vn = vn + bw * (-zcor1v - zfz * hyk * gk - zcy * zrom1v * (pai[o] - pai[o - S]));
+        vn = vn + bw * (-zcor1v - zfz * hyk * gk - zcy * zrom1v * R(pai[o] - pai[o - S]));
       }
       v_out[o] = vn;
     }
