@@ -203,6 +203,24 @@ void mlc_destroy(mlc_ctx *ctx);
 /* Text for a status code. */
 const char *mlc_strerror(int status);
 
+/* ---- ensembles: several domains of the same extents and parameters (the
+ * members) advanced by the same kernel launches.  Member m's arrays sit at a
+ * fixed stride from member 0's, so one launch per kernel stage serves every
+ * member and one recorded graph replays the whole ensemble step.  Members
+ * may differ in any field (terrain, state, boundary data) but share the
+ * level set and dtbdys.  mlc_create is mlc_create_batch with nmem = 1 and the
+ * single-domain calls address member 0.  No counterpart in the reference,
+ * where an ensemble is a set of separate runs (Share/mod_ensemble.F90). */
+int mlc_create_batch(const mlc_dims *dims, const mlc_params *params, int nmem, mlc_ctx **out);
+int mlc_members(const mlc_ctx *ctx);
+int mlc_member_bind_static(mlc_ctx *ctx, int m, const mlc_static_ptrs *s);
+int mlc_member_upload_state(mlc_ctx *ctx, int m, const mlc_state_ptrs *st);
+int mlc_member_download_state(mlc_ctx *ctx, int m, const mlc_state_ptrs *st);
+int mlc_member_set_boundary(mlc_ctx *ctx, int m, const mlc_bdy_ptrs *b, double xbctime,
+                            double dtbdys);
+/* nsteps steps of every member; out (optional) receives nmem diagnostics. */
+int mlc_step_batch(mlc_ctx *ctx, int nsteps, mlc_diag *out);
+
 /* Device bytes one domain of these extents holds (for admission control). */
 size_t mlc_footprint_bytes(const mlc_dims *dims, int precision);
 

@@ -132,6 +132,16 @@ def _declare(lib):
         "mlc_setup_boundaries": (C.c_int, [C.c_int] * 6 + [_ip]),
         "mlc_paicompute": (C.c_int, [P(mlc_dims), P(mlc_params)] + [_dp] * 7),
         "mlc_pfwsat": (C.c_int, [C.c_size_t, _dp, _dp, _dp]),
+        "mlc_create_batch": (C.c_int, [P(mlc_dims), P(mlc_params), C.c_int, P(C.c_void_p)]),
+        "mlc_members": (C.c_int, [C.c_void_p]),
+        "mlc_member_bind_static": (C.c_int, [C.c_void_p, C.c_int, P(mlc_static_ptrs)]),
+        "mlc_member_upload_state": (C.c_int, [C.c_void_p, C.c_int, P(mlc_state_ptrs)]),
+        "mlc_member_download_state": (C.c_int, [C.c_void_p, C.c_int, P(mlc_state_ptrs)]),
+        "mlc_member_set_boundary": (C.c_int, [C.c_void_p, C.c_int, P(mlc_bdy_ptrs), C.c_double,
+                                              C.c_double]),
+        "mlc_step_batch": (C.c_int, [C.c_void_p, C.c_int, P(mlc_diag)]),
+        "mlc_launches_per_step": (C.c_int, [C.c_void_p]),
+        "mlc_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     }
     for name, (res, args) in sigs.items():
         try:

@@ -70,6 +70,9 @@ template <class R>
 __global__ void k_adv_prep(Geom g, const R *__restrict__ u, const R *__restrict__ v,
                            const R *__restrict__ w, R *__restrict__ ux, R *__restrict__ vx,
                            R *__restrict__ wx) {
+  const size_t mo = (size_t)blockIdx.z * g.mstride;
+  u = mshift(u, mo); v = mshift(v, mo); w = mshift(w, mo); ux = mshift(ux, mo); vx = mshift(vx, mo);
+  wx = mshift(wx, mo);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
@@ -112,11 +115,14 @@ __global__ void k_adv_vertical(Geom g, Scal c, Stat<R> sa, const R *__restrict__
 #define COL(a, k) a[(size_t)(k) * nth + tid]
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int f = blockIdx.z;
+  const int f = blockIdx.z % t.n;
+  const size_t mo = (size_t)(blockIdx.z / t.n) * g.mstride;
+  rebase(sa, mo);
+  s = mshift(s, mo);
   if (j > g.jx - 1 || i > g.iy - 1) return;
   const size_t ij = g.at2(j, i), PS = g.PS;
   const T dtrdz = T(0.5) * (T(c.dtstepa) * T(c.rdzita));
-  const T *src = t.cur[f];
+  const T *src = mshift(t.cur[f], mo);
   for (int k = 1; k <= kz; ++k) COL(col, k) = src[ij + (size_t)(k - 1) * PS];
   for (int k = 1; k <= kz + 1; ++k) COL(sc, k) = T(s[ij + (size_t)(k - 1) * PS]);
   for (int pass = 0; pass < 2; ++pass) {
@@ -146,7 +152,7 @@ __global__ void k_adv_vertical(Geom g, Scal c, Stat<R> sa, const R *__restrict__
       COL(col, k) = pk - COL(flx, k) * zrfmu + COL(flx, k + 1) * zrfmd + zdv;
     }
   }
-  T *dst = t.wz[f];
+  T *dst = mshift(t.wz[f], mo);
   for (int k = 1; k <= kz; ++k) dst[ij + (size_t)(k - 1) * PS] = COL(col, k);
 #undef COL
 }
@@ -164,21 +170,24 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   const int nf = t.n;
   const int f = blockIdx.z % nf;
-  const int k = blockIdx.z / nf + 1;
+  const int k = (blockIdx.z / nf) % kz + 1;
+  const size_t mo = (size_t)(blockIdx.z / (nf * kz)) * g.mstride;
+  rebase(sa, mo);
+  u = mshift(u, mo);
+  v = mshift(v, mo);
   const int J0 = blockIdx.x * kTJ + 1, I0 = blockIdx.y * kTI + 1;
   const int tid = threadIdx.y * kTJ + threadIdx.x;
   const int nth = kTJ * kTI;
   const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
-  const T *pp = t.cur[f] + ko;
-  const T *wz = t.wz[f] + ko;
-  T *out = t.out[f] + ko;
+  const T *pp = mshift(t.cur[f], mo) + ko;
+  const T *wz = mshift(t.wz[f], mo) + ko;
+  T *out = mshift(t.out[f], mo) + ko;
   const R *uk = u + ko;
   const R *vk = v + ko;
   const T dta = T(c.dtstepa);
   const T dtrdx = dta * T(c.rdx), dtrdy = dta * T(c.rdx);
   const bool rot = c.lrotllr != 0;
   const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
-  (void)kz;
 
   // stage wz (cross points only; others are never read for valid outputs)
   for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
@@ -292,6 +301,10 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
 // :809-825
 template <class R>
 __global__ void k_adv_curvature(Geom g, Scal c, Stat<R> sa, R *__restrict__ ux, R *__restrict__ vx) {
+  const size_t mo = (size_t)blockIdx.z * g.mstride;
+  rebase(sa, mo);
+  ux = mshift(ux, mo);
+  vx = mshift(vx, mo);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (j > g.jx - 2 || i > g.iy - 2) return;
@@ -321,6 +334,9 @@ template <class R>
 __global__ void k_adv_back(Geom g, const R *__restrict__ ux, const R *__restrict__ vx,
                            const R *__restrict__ wx, R *__restrict__ u, R *__restrict__ v,
                            R *__restrict__ w) {
+  const size_t mo = (size_t)blockIdx.z * g.mstride;
+  ux = mshift(ux, mo); vx = mshift(vx, mo); wx = mshift(wx, mo);
+  u = mshift(u, mo); v = mshift(v, mo); w = mshift(w, mo);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
@@ -355,8 +371,8 @@ __global__ void k_adv_back(Geom g, const R *__restrict__ ux, const R *__restrict
   }
 }
 
-inline dim3 grid2(int nj, int ni, dim3 b) {
-  return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y));
+inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
+  return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y), (unsigned)nmem);
 }
 
 }  // namespace
@@ -364,7 +380,7 @@ inline dim3 grid2(int nj, int ni, dim3 b) {
 template <class R>
 void Launch<R>::adv_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
   const dim3 b(32, 4);
-  k_adv_prep<R><<<grid2(g.jx - 1, g.iy - 1, b), b, 0, s>>>(g, st.u, st.v, st.w, st.ux, st.vx, wk.wx);
+  k_adv_prep<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, st.u, st.v, st.w, st.ux, st.vx, wk.wx);
 }
 
 template <class R, class T>
@@ -372,8 +388,8 @@ void launch_vertical(const Geom &g, const Scal &c, const Stat<R> &sa, const Work
                      const AdvTable<T> &t, cudaStream_t s) {
   const dim3 b(32, 2);
   const size_t smem = (size_t)3 * (g.kz + 2) * b.x * b.y * sizeof(T);
-  dim3 grd = grid2(g.jx - 1, g.iy - 1, b);
-  grd.z = (unsigned)t.n;
+  dim3 grd = grid2(g.jx - 1, g.iy - 1, b, 1);
+  grd.z = (unsigned)(t.n * g.nmem);
   k_adv_vertical<R, T><<<grd, b, smem, s>>>(g, c, sa, wk.s, t);
 }
 
@@ -381,7 +397,7 @@ template <class R, class T>
 void launch_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                        const AdvTable<T> &t, cudaStream_t s) {
   dim3 grd((unsigned)((g.jx - 1 + kTJ - 1) / kTJ), (unsigned)((g.iy - 1 + kTI - 1) / kTI),
-           (unsigned)(t.n * g.kz));
+           (unsigned)(t.n * g.kz * g.nmem));
   k_adv_horizontal<R, T><<<grd, dim3(kTJ, kTI), 0, s>>>(g, c, sa, st.u, st.v, t);
 }
 
@@ -413,13 +429,13 @@ template <class R>
 void Launch<R>::adv_curvature(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                               cudaStream_t s) {
   const dim3 b(32, 4);
-  k_adv_curvature<R><<<grid2(g.jx - 3, g.iy - 3, b), b, 0, s>>>(g, c, sa, st.ux, st.vx);
+  k_adv_curvature<R><<<grid2(g.jx - 3, g.iy - 3, b, g.nmem), b, 0, s>>>(g, c, sa, st.ux, st.vx);
 }
 
 template <class R>
 void Launch<R>::adv_back(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
   const dim3 b(32, 4);
-  k_adv_back<R><<<grid2(g.jx, g.iy, b), b, 0, s>>>(g, st.ux, st.vx, wk.wx, st.u, st.v, st.w);
+  k_adv_back<R><<<grid2(g.jx, g.iy, b, g.nmem), b, 0, s>>>(g, st.ux, st.vx, wk.wx, st.u, st.v, st.w);
 }
 
 template <class R>

@@ -131,8 +131,8 @@ void carve(Carver &cv, Arrays<R> &a, const Geom &g, const mlc_dims &d, const mlc
     a.bfield[b][7] = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;         // chib
     a.xpsb[b] = cv.take<double>(P2);
   }
+  a.staging = nullptr;  // one staging buffer per context, outside the member arenas
   a.staging_elems = state_elems(d);
-  a.staging = cv.take<double>(a.staging_elems);
   a.partials = cv.take<double>((size_t)reduce_blocks(g) * 8);
   a.clk = cv.take<Clock>(1);
   a.diag = cv.take<DiagDev>(1);
@@ -192,10 +192,15 @@ struct mlc_ctx {
   Geom g{};
   Scal c{};
   void *arena = nullptr;
-  size_t arena_bytes = 0;
-  Arrays<double> ad{};
+  double *staging = nullptr;  // layout conversion buffer shared by all members
+  size_t arena_bytes = 0;   // all members
+  size_t member_bytes = 0;  // one member's arena (the member stride)
+  int nmem = 1;
+  Arrays<double> ad{};      // member 0's views (kernels rebase by member)
   Arrays<float> af{};
+  std::vector<char> m_static, m_state, m_bdy;
   bool have_static = false, have_state = false, have_bdy = false;
+  double rdzita_set = 0.0, dtbdys_set = 0.0;
   int uv_role = 0;   // which buffer of the u/v pair is current
   int adv_role = 0;  // which buffer of the advected pairs is current
   cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -205,6 +210,17 @@ struct mlc_ctx {
 };
 
 namespace {
+
+// Views of member m's arrays (member 0's layout, m * member_bytes further).
+template <class R>
+Arrays<R> member_arrays(const mlc_ctx *x, int m) {
+  Arrays<R> a{};
+  Carver cv{static_cast<char *>(x->arena) + (size_t)m * x->member_bytes, 0};
+  carve<R>(cv, a, x->g, x->dims, x->prm);
+  bind_views<R>(a);
+  a.staging = x->staging;
+  return a;
+}
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return MLC_OK;
@@ -341,8 +357,9 @@ int enqueue_step(mlc_ctx *x, Arrays<R> &a, Recorder *rec = nullptr) {
     }
     if (p.ipptls == 0 && d.nqx > 1) {
       // species that are not advected keep their values in the other buffer
-      cudaMemcpyAsync(r.qx_alt + F, r.st.qx + F, (size_t)(d.nqx - 1) * F * sizeof(R),
-                      cudaMemcpyDeviceToDevice, s);
+      cudaMemcpy2DAsync(r.qx_alt + F, x->member_bytes, r.st.qx + F, x->member_bytes,
+                        (size_t)(d.nqx - 1) * F * sizeof(R), (size_t)x->nmem,
+                        cudaMemcpyDeviceToDevice, s);
     }
     x->adv_role ^= 1;
     Roles<R> r2 = roles_of(a, x->uv_role, x->adv_role);
@@ -530,7 +547,7 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
     for (size_t e = 0; e < nd; ++e) if (b[e] > 0) return 1;
     return 0;
   };
-  x->c.hb_cr = any_pos(s->ibnd_cr); x->c.hb_ud = any_pos(s->ibnd_ud); x->c.hb_vd = any_pos(s->ibnd_vd);
+  x->c.hb_cr |= any_pos(s->ibnd_cr); x->c.hb_ud |= any_pos(s->ibnd_ud); x->c.hb_vd |= any_pos(s->ibnd_vd);
   // the curvature terms vanish identically with uniform map factors
   {
     bool curv = p.lrotllr != 0;
@@ -539,7 +556,7 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
         const size_t e = (size_t)(j - 1) + (size_t)(i - 1) * jx;
         if ((s->msfu[e - 1] - s->msfu[e]) != 0.0 || (s->msfv[e - jx] - s->msfv[e]) != 0.0) curv = true;
       }
-    x->c.curvature = curv ? 1 : 0;
+    x->c.curvature |= curv ? 1 : 0;
   }
   // 1-D vertical arrays, Main/mod_moloch.F90:262-300
   std::vector<double> v1(kz + 1);
@@ -559,7 +576,6 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
   MLC_CHK(put1(x, s->hefc, a.hefc, (size_t)p.nspgx * kz));
   if (s->fcx) MLC_CHK(put1(x, s->fcx, a.fcx, p.nspgx));
   if (s->rlat) MLC_CHK(put1(x, s->rlat, a.rlat, iy));
-  x->c.rdzita = 1.0 / s->zita[kz - 1];
   MLC_TRY(cudaStreamSynchronize(x->stream));
   return MLC_OK;
 }
@@ -662,7 +678,7 @@ size_t footprint(const mlc_dims &d, const mlc_params &p, int elem) {
   Arrays<R> a{};
   Carver cv;
   carve<R>(cv, a, g, d, p);
-  return cv.off;
+  return cv.off + state_elems(d) * sizeof(double);
 }
 
 }  // namespace
@@ -723,17 +739,22 @@ size_t mlc_footprint_bytes(const mlc_dims *d, int precision) {
   return footprint<double>(*d, p, 8);
 }
 
-int mlc_create(const mlc_dims *dims, const mlc_params *params, mlc_ctx **out) {
+int mlc_create_batch(const mlc_dims *dims, const mlc_params *params, int nmem, mlc_ctx **out) {
   if (!out) return MLC_ERR_INVALID;
   *out = nullptr;
   int st = validate(dims, params);
   if (st != MLC_OK) return st;
+  if (nmem < 1 || nmem > 4096) return MLC_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return MLC_ERR_NODEVICE;
   std::unique_ptr<mlc_ctx> x(new (std::nothrow) mlc_ctx());
   if (!x) return MLC_ERR_NOMEM;
   x->dims = *dims;
   x->prm = *params;
+  x->nmem = nmem;
+  x->m_static.assign(nmem, 0);
+  x->m_state.assign(nmem, 0);
+  x->m_bdy.assign(nmem, 0);
   MLC_TRY(cudaGetDevice(&x->device));
   const bool mixed = params->precision == MLC_PREC_MIXED;
   x->g = make_geom(*dims, mixed ? 4 : 8);
@@ -763,16 +784,21 @@ int mlc_create(const mlc_dims *dims, const mlc_params *params, mlc_ctx **out) {
   Carver cv;
   if (mixed) carve<float>(cv, x->af, x->g, *dims, *params);
   else carve<double>(cv, x->ad, x->g, *dims, *params);
-  x->arena_bytes = cv.off;
+  x->member_bytes = cv.off;
+  x->arena_bytes = cv.off * (size_t)nmem;
+  x->g.nmem = nmem;
+  x->g.mstride = x->member_bytes;
   cudaError_t e = cudaMalloc(&x->arena, x->arena_bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&x->staging, state_elems(*dims) * sizeof(double));
   if (e != cudaSuccess) {
     cudaGetLastError();
+    if (x->arena) cudaFree(x->arena);
+  if (x->staging) cudaFree(x->staging);
     cudaStreamDestroy(x->stream);
     return MLC_ERR_NOMEM;
   }
-  Carver real{static_cast<char *>(x->arena), 0};
-  if (mixed) { carve<float>(real, x->af, x->g, *dims, *params); bind_views<float>(x->af); }
-  else { carve<double>(real, x->ad, x->g, *dims, *params); bind_views<double>(x->ad); }
+  if (mixed) x->af = member_arrays<float>(x.get(), 0);
+  else x->ad = member_arrays<double>(x.get(), 0);
   // every array starts at zero: s and w at the ring stay zero as the
   // reference's reset_tendencies and init_moloch leave them
   e = cudaMemsetAsync(x->arena, 0, x->arena_bytes, x->stream);
@@ -781,6 +807,7 @@ int mlc_create(const mlc_dims *dims, const mlc_params *params, mlc_ctx **out) {
   if (e == cudaSuccess) e = mixed ? Launch<float>::configure_advect() : Launch<double>::configure_advect();
   if (e != cudaSuccess) {
     cudaFree(x->arena);
+    cudaFree(x->staging);
     cudaStreamDestroy(x->stream);
     return cuda_status(e);
   }
@@ -788,74 +815,157 @@ int mlc_create(const mlc_dims *dims, const mlc_params *params, mlc_ctx **out) {
   return MLC_OK;
 }
 
-int mlc_bind_static(mlc_ctx *x, const mlc_static_ptrs *s) {
-  if (!x || !s) return MLC_ERR_INVALID;
+int mlc_create(const mlc_dims *dims, const mlc_params *params, mlc_ctx **out) {
+  return mlc_create_batch(dims, params, 1, out);
+}
+
+static void drop_graphs(mlc_ctx *x) {
   for (auto &gx : x->graph)
     if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
-  int st = x->prm.precision == MLC_PREC_MIXED ? bind_static_impl<float>(x, x->af, s)
-                                              : bind_static_impl<double>(x, x->ad, s);
-  if (st == MLC_OK) x->have_static = true;
+}
+
+static bool all_set(const std::vector<char> &v) {
+  for (char c : v)
+    if (!c) return false;
+  return true;
+}
+
+int mlc_member_bind_static(mlc_ctx *x, int m, const mlc_static_ptrs *s) {
+  if (!x || !s || m < 0 || m >= x->nmem) return MLC_ERR_INVALID;
+  if (!s->zita) return MLC_ERR_INVALID;
+  const double rdz = 1.0 / s->zita[x->dims.kz - 1];
+  if (x->rdzita_set != 0.0 && rdz != x->rdzita_set) return MLC_ERR_INVALID;  // members share levels
+  drop_graphs(x);
+  x->c.rdzita = rdz;
+  x->rdzita_set = rdz;
+  int st;
+  if (x->prm.precision == MLC_PREC_MIXED) {
+    Arrays<float> a = member_arrays<float>(x, m);
+    st = bind_static_impl<float>(x, a, s);
+  } else {
+    Arrays<double> a = member_arrays<double>(x, m);
+    st = bind_static_impl<double>(x, a, s);
+  }
+  if (st == MLC_OK) x->m_static[m] = 1;
+  x->have_static = all_set(x->m_static);
   return st;
 }
 
-int mlc_upload_state(mlc_ctx *x, const mlc_state_ptrs *h) {
-  if (!x || !h) return MLC_ERR_INVALID;
-  int st = x->prm.precision == MLC_PREC_MIXED ? upload_state_impl<float>(x, x->af, h)
-                                              : upload_state_impl<double>(x, x->ad, h);
-  if (st == MLC_OK) x->have_state = true;
+int mlc_bind_static(mlc_ctx *x, const mlc_static_ptrs *s) { return mlc_member_bind_static(x, 0, s); }
+
+int mlc_member_upload_state(mlc_ctx *x, int m, const mlc_state_ptrs *h) {
+  if (!x || !h || m < 0 || m >= x->nmem) return MLC_ERR_INVALID;
+  int st;
+  if (x->prm.precision == MLC_PREC_MIXED) {
+    Arrays<float> a = member_arrays<float>(x, m);
+    st = upload_state_impl<float>(x, a, h);
+  } else {
+    Arrays<double> a = member_arrays<double>(x, m);
+    st = upload_state_impl<double>(x, a, h);
+  }
+  if (st == MLC_OK) x->m_state[m] = 1;
+  x->have_state = all_set(x->m_state);
   return st;
+}
+
+int mlc_upload_state(mlc_ctx *x, const mlc_state_ptrs *h) { return mlc_member_upload_state(x, 0, h); }
+
+int mlc_member_download_state(mlc_ctx *x, int m, const mlc_state_ptrs *h) {
+  if (!x || !h || m < 0 || m >= x->nmem) return MLC_ERR_INVALID;
+  if (x->prm.precision == MLC_PREC_MIXED) {
+    Arrays<float> a = member_arrays<float>(x, m);
+    return download_state_impl<float>(x, a, h);
+  }
+  Arrays<double> a = member_arrays<double>(x, m);
+  return download_state_impl<double>(x, a, h);
 }
 
 int mlc_download_state(mlc_ctx *x, const mlc_state_ptrs *h) {
-  if (!x || !h) return MLC_ERR_INVALID;
-  return x->prm.precision == MLC_PREC_MIXED ? download_state_impl<float>(x, x->af, h)
-                                            : download_state_impl<double>(x, x->ad, h);
+  return mlc_member_download_state(x, 0, h);
 }
 
-int mlc_set_boundary(mlc_ctx *x, const mlc_bdy_ptrs *b, double xbctime, double dtbdys) {
-  if (!x || !b || !(dtbdys > 0)) return MLC_ERR_INVALID;
+int mlc_member_set_boundary(mlc_ctx *x, int m, const mlc_bdy_ptrs *b, double xbctime,
+                            double dtbdys) {
+  if (!x || !b || !(dtbdys > 0) || m < 0 || m >= x->nmem) return MLC_ERR_INVALID;
+  if (x->nmem > 1 && x->dtbdys_set != 0.0 && dtbdys != x->dtbdys_set) return MLC_ERR_INVALID;
+  x->dtbdys_set = dtbdys;
   x->prm.dtbdys = dtbdys;
   x->c.dtbdys = dtbdys;
   x->c.rtb = 1.0 / dtbdys;
-  // rtb/dtbdys are baked into recorded graphs: drop them
-  for (auto &gx : x->graph)
-    if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
-  int st = x->prm.precision == MLC_PREC_MIXED ? set_boundary_impl<float>(x, x->af, b)
-                                              : set_boundary_impl<double>(x, x->ad, b);
+  drop_graphs(x);  // rtb/dtbdys are baked into recorded graphs
+  int st;
+  Clock *dclk;
+  if (x->prm.precision == MLC_PREC_MIXED) {
+    Arrays<float> a = member_arrays<float>(x, m);
+    st = set_boundary_impl<float>(x, a, b);
+    dclk = a.clk;
+  } else {
+    Arrays<double> a = member_arrays<double>(x, m);
+    st = set_boundary_impl<double>(x, a, b);
+    dclk = a.clk;
+  }
   if (st != MLC_OK) return st;
   Clock clk{};
   clk.xbctime = xbctime;
-  Clock *dclk = x->prm.precision == MLC_PREC_MIXED ? x->af.clk : x->ad.clk;
   MLC_TRY(cudaMemcpyAsync(dclk, &clk, sizeof(Clock), cudaMemcpyHostToDevice, x->stream));
   MLC_TRY(cudaStreamSynchronize(x->stream));
-  x->have_bdy = true;
+  x->m_bdy[m] = 1;
+  x->have_bdy = all_set(x->m_bdy);
   return MLC_OK;
 }
 
-int mlc_step(mlc_ctx *x, int nsteps, mlc_diag *out) {
+int mlc_set_boundary(mlc_ctx *x, const mlc_bdy_ptrs *b, double xbctime, double dtbdys) {
+  return mlc_member_set_boundary(x, 0, b, xbctime, dtbdys);
+}
+
+// Diagnostics of every member after the last step (out has nmem entries).
+static int fetch_diags(mlc_ctx *x, int nsteps, mlc_diag *out) {
+  const bool mixed = x->prm.precision == MLC_PREC_MIXED;
+  const char *diag0 = reinterpret_cast<const char *>(mixed ? (void *)x->af.diag : (void *)x->ad.diag);
+  const char *clk0 = reinterpret_cast<const char *>(mixed ? (void *)x->af.clk : (void *)x->ad.clk);
+  std::vector<DiagDev> dd(x->nmem);
+  std::vector<Clock> ck(x->nmem);
+  MLC_TRY(cudaMemcpy2DAsync(dd.data(), sizeof(DiagDev), diag0, x->member_bytes, sizeof(DiagDev),
+                            x->nmem, cudaMemcpyDeviceToHost, x->stream));
+  MLC_TRY(cudaMemcpy2DAsync(ck.data(), sizeof(Clock), clk0, x->member_bytes, sizeof(Clock),
+                            x->nmem, cudaMemcpyDeviceToHost, x->stream));
+  MLC_TRY(cudaStreamSynchronize(x->stream));
+  bool bad = false;
+  for (int m = 0; m < x->nmem; ++m) {
+    if (ck[m].nonfinite) bad = true;
+    if (!out) continue;
+    out[m].ps_max = dd[m].ps_max;
+    out[m].ps_min = dd[m].ps_min;
+    out[m].nonfinite = ck[m].nonfinite;
+    out[m].steps_done = nsteps;
+    out[m].drymass = dd[m].drymass;
+    out[m].dryadv = dd[m].dryadv;
+    out[m].qmass = dd[m].qmass;
+    out[m].qadv = dd[m].qadv;
+    out[m].xbctime = ck[m].xbctime;
+  }
+  return bad ? MLC_ERR_NONFINITE : MLC_OK;
+}
+
+int mlc_step_batch(mlc_ctx *x, int nsteps, mlc_diag *out) {
   if (!x || nsteps < 0) return MLC_ERR_INVALID;
   if (!x->have_static || !x->have_state || (x->c.apply_bdy && !x->have_bdy)) return MLC_ERR_STATE;
   const bool mixed = x->prm.precision == MLC_PREC_MIXED;
   int st = mixed ? step_impl<float>(x, x->af, nsteps) : step_impl<double>(x, x->ad, nsteps);
   if (st != MLC_OK) return st;
-  DiagDev dd{};
-  Clock ck{};
-  MLC_TRY(cudaMemcpyAsync(&dd, mixed ? x->af.diag : x->ad.diag, sizeof(dd), cudaMemcpyDeviceToHost, x->stream));
-  MLC_TRY(cudaMemcpyAsync(&ck, mixed ? x->af.clk : x->ad.clk, sizeof(ck), cudaMemcpyDeviceToHost, x->stream));
-  MLC_TRY(cudaStreamSynchronize(x->stream));
-  if (out) {
-    out->ps_max = dd.ps_max;
-    out->ps_min = dd.ps_min;
-    out->nonfinite = ck.nonfinite;
-    out->steps_done = nsteps;
-    out->drymass = dd.drymass;
-    out->dryadv = dd.dryadv;
-    out->qmass = dd.qmass;
-    out->qadv = dd.qadv;
-    out->xbctime = ck.xbctime;
-  }
-  return ck.nonfinite ? MLC_ERR_NONFINITE : MLC_OK;
+  return fetch_diags(x, nsteps, out);
 }
+
+int mlc_step(mlc_ctx *x, int nsteps, mlc_diag *out) {
+  if (!x) return MLC_ERR_INVALID;
+  if (x->nmem == 1) return mlc_step_batch(x, nsteps, out);
+  std::vector<mlc_diag> all(x->nmem);
+  int st = mlc_step_batch(x, nsteps, all.data());
+  if (out && st != MLC_ERR_INVALID && st != MLC_ERR_STATE) *out = all[0];
+  return st;
+}
+
+int mlc_members(const mlc_ctx *x) { return x ? x->nmem : 0; }
 
 void mlc_destroy(mlc_ctx *x) {
   if (!x) return;
@@ -863,6 +973,7 @@ void mlc_destroy(mlc_ctx *x) {
     if (gx) cudaGraphExecDestroy(gx);
   if (x->stream) cudaStreamSynchronize(x->stream);
   if (x->arena) cudaFree(x->arena);
+  if (x->staging) cudaFree(x->staging);
   if (x->stream) cudaStreamDestroy(x->stream);
   delete x;
 }

@@ -20,6 +20,8 @@ struct Geom {
   int jx, iy, kz, nqx, ntr;
   int P;        // row pitch in elements
   size_t PS;    // plane stride = P*iy
+  int nmem;       // ensemble members advanced by one launch (1 = one domain)
+  size_t mstride; // bytes between consecutive members' arenas
   __host__ __device__ size_t at(int j, int i, int k) const {
     return (size_t)(j - 1) + (size_t)(i - 1) * (size_t)P + (size_t)(k - 1) * PS;
   }
@@ -99,5 +101,54 @@ struct DiagDev {
   double drymass, dryadv, qmass, qadv, ps_max, ps_min;
   int nonfinite, pad;
 };
+
+// ---- ensemble members -----------------------------------------------------
+// Every array of member m lives at member 0's address plus m * mstride, so a
+// kernel that serves all members rebases its pointer arguments once.
+template <class T>
+__device__ __forceinline__ T *mshift(T *p, size_t off) {
+  return p ? reinterpret_cast<T *>(reinterpret_cast<char *>(p) + off) : p;
+}
+template <class T>
+__device__ __forceinline__ const T *mshift(const T *p, size_t off) {
+  return p ? reinterpret_cast<const T *>(reinterpret_cast<const char *>(p) + off) : p;
+}
+
+template <class R>
+__device__ __forceinline__ void rebase(Stat<R> &s, size_t o) {
+  if (!o) return;
+  s.fmz = mshift(s.fmz, o); s.fmzf = mshift(s.fmzf, o); s.rfmzu = mshift(s.rfmzu, o);
+  s.rfmzv = mshift(s.rfmzv, o); s.fmz_d = mshift(s.fmz_d, o); s.fmzf_d = mshift(s.fmzf_d, o);
+  s.zrfmu = mshift(s.zrfmu, o); s.zrfmd = mshift(s.zrfmd, o); s.zeta = mshift(s.zeta, o);
+  s.dz = mshift(s.dz, o); s.hx = mshift(s.hx, o); s.hy = mshift(s.hy, o);
+  s.msfu = mshift(s.msfu, o); s.msfv = mshift(s.msfv, o); s.msfx = mshift(s.msfx, o);
+  s.mx2 = mshift(s.mx2, o); s.rmu = mshift(s.rmu, o); s.rmv = mshift(s.rmv, o);
+  s.coru = mshift(s.coru, o); s.corv = mshift(s.corv, o); s.ibnd_cr = mshift(s.ibnd_cr, o);
+  s.ibnd_ud = mshift(s.ibnd_ud, o); s.ibnd_vd = mshift(s.ibnd_vd, o); s.hefc = mshift(s.hefc, o);
+  s.fcx = mshift(s.fcx, o); s.tnudge = mshift(s.tnudge, o); s.ffilt = mshift(s.ffilt, o);
+  s.gzitakh = mshift(s.gzitakh, o); s.xkdamp = mshift(s.xkdamp, o); s.xknu = mshift(s.xknu, o);
+  s.gzitak = mshift(s.gzitak, o); s.rlat = mshift(s.rlat, o);
+}
+
+template <class R>
+__device__ __forceinline__ void rebase(State<R> &s, size_t o) {
+  if (!o) return;
+  s.u = mshift(s.u, o); s.v = mshift(s.v, o); s.w = mshift(s.w, o); s.t = mshift(s.t, o);
+  s.tvirt = mshift(s.tvirt, o); s.ux = mshift(s.ux, o); s.vx = mshift(s.vx, o);
+  s.p = mshift(s.p, o); s.rho = mshift(s.rho, o); s.qsat = mshift(s.qsat, o);
+  s.pai = mshift(s.pai, o); s.tetav = mshift(s.tetav, o); s.qx = mshift(s.qx, o);
+  s.trac = mshift(s.trac, o); s.ps = mshift(s.ps, o);
+}
+
+template <class R>
+__device__ __forceinline__ void rebase(Bdy<R> &b, size_t o) {
+  if (!o) return;
+  for (int q = 0; q < 2; ++q) {
+    b.xtb[q] = mshift(b.xtb[q], o); b.xqb[q] = mshift(b.xqb[q], o); b.xlb[q] = mshift(b.xlb[q], o);
+    b.xib[q] = mshift(b.xib[q], o); b.dub[q] = mshift(b.dub[q], o); b.dvb[q] = mshift(b.dvb[q], o);
+    b.chib[q] = mshift(b.chib[q], o); b.xpaib[q] = mshift(b.xpaib[q], o);
+    b.xpsb[q] = mshift(b.xpsb[q], o);
+  }
+}
 
 }  // namespace mlc

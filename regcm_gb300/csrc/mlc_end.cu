@@ -26,6 +26,7 @@ __device__ __forceinline__ R qfactor(const R *qx, size_t o, size_t F, int ipptls
 // dynamical_core :1121-1123 and tvirt_to_temp :1629-1648
 template <class R>
 __global__ void k_end_tvirt(Geom g, Scal c, State<R> st) {
+  rebase(st, (size_t)blockIdx.z * g.mstride);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
@@ -47,7 +48,13 @@ __global__ void k_bdy_ring(Geom g, Scal c, State<R> st, Bdy<R> bd, const Clock *
   const int jx = g.jx, iy = g.iy;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;  // position along the side
   const int k = blockIdx.y + 1;
-  const int side = blockIdx.z;                           // 0 = west/south, 1 = east/north
+  const int side = blockIdx.z & 1;                       // 0 = west/south, 1 = east/north
+  {
+    const size_t mo = (size_t)(blockIdx.z >> 1) * g.mstride;
+    rebase(st, mo);
+    rebase(bd, mo);
+    clk = mshift(clk, mo);
+  }
   const double xb = clk->xbctime;
   const double x1 = (xb + c.dt) * c.rtb;
   const double x0 = 1.0 - x1;
@@ -122,6 +129,13 @@ __global__ void k_bdy_ring(Geom g, Scal c, State<R> st, Bdy<R> bd, const Clock *
 // moved by dtsec.
 template <class R>
 __global__ void k_bdy_relax(Geom g, Scal c, Stat<R> sa, State<R> st, Bdy<R> bd, const Clock *clk) {
+  {
+    const size_t mo = (size_t)blockIdx.z * g.mstride;
+    rebase(sa, mo);
+    rebase(st, mo);
+    rebase(bd, mo);
+    clk = mshift(clk, mo);
+  }
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
@@ -208,6 +222,11 @@ __global__ void k_bdy_relax(Geom g, Scal c, Stat<R> sa, State<R> st, Bdy<R> bd, 
 // by status_update, so they are computed once, after it.
 template <class R>
 __global__ void k_end_cross(Geom g, Scal c, Stat<R> sa, State<R> st) {
+  {
+    const size_t mo = (size_t)blockIdx.z * g.mstride;
+    rebase(sa, mo);
+    rebase(st, mo);
+  }
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
@@ -281,6 +300,10 @@ __global__ void k_end_cross(Geom g, Scal c, Stat<R> sa, State<R> st) {
 template <class R>
 __global__ void k_end_uvstag(Geom g, const R *__restrict__ ux, const R *__restrict__ vx,
                              R *__restrict__ u, R *__restrict__ v) {
+  {
+    const size_t mo = (size_t)blockIdx.z * g.mstride;
+    ux = mshift(ux, mo); vx = mshift(vx, mo); u = mshift(u, mo); v = mshift(v, mo);
+  }
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jx = g.jx, iy = g.iy;
@@ -333,6 +356,12 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(Geom g, Scal c, 
                                                                 State<R> st, double *part,
                                                                 int rows_per_block) {
   __shared__ double sh[kRedThreads];
+  {
+    const size_t mo = (size_t)blockIdx.y * g.mstride;
+    rebase(sa, mo);
+    rebase(st, mo);
+    part = mshift(part, mo);
+  }
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   const double dx = c.dx, dt = c.dt, dxsq = dx * dx;
   const size_t F = g.field3();
@@ -416,8 +445,14 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(Geom g, Scal c, 
 }
 
 __global__ void k_reduce_final(const double *part, int nblocks, DiagDev *diag, Clock *clk,
-                               double dtsec, int apply_bdy) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+                               double dtsec, int apply_bdy, size_t mstride) {
+  if (threadIdx.x != 0) return;
+  {
+    const size_t mo = (size_t)blockIdx.x * mstride;
+    part = mshift(part, mo);
+    diag = mshift(diag, mo);
+    clk = mshift(clk, mo);
+  }
   double a[4] = {0, 0, 0, 0}, pmax = -INFINITY, pmin = INFINITY;
   bool bad = false;
   for (int b = 0; b < nblocks; ++b) {
@@ -460,8 +495,8 @@ __global__ void k_pack3(const R *__restrict__ src, double *__restrict__ dst, Geo
   }
 }
 
-inline dim3 grid2(int nj, int ni, dim3 b) {
-  return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y));
+inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
+  return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y), (unsigned)nmem);
 }
 
 inline int rows_per_block(const Geom &g) {
@@ -481,42 +516,45 @@ int reduce_blocks(const Geom &g) {
 template <class R>
 void Launch<R>::end_tvirt(const Geom &g, const Scal &c, const State<R> &st, cudaStream_t s) {
   const dim3 b(32, 4);
-  k_end_tvirt<R><<<grid2(g.jx - 1, g.iy - 1, b), b, 0, s>>>(g, c, st);
+  k_end_tvirt<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, c, st);
 }
 
 template <class R>
 void Launch<R>::bdy_ring(const Geom &g, const Scal &c, const State<R> &st, const Bdy<R> &bd,
                          const Clock *clk, cudaStream_t s) {
   const int nwe = g.iy - 2, nsn = g.jx;
-  k_bdy_ring<R><<<dim3((unsigned)((nwe + 63) / 64), (unsigned)g.kz, 2), 64, 0, s>>>(g, c, st, bd, clk, 0);
-  k_bdy_ring<R><<<dim3((unsigned)((nsn + 63) / 64), (unsigned)g.kz, 2), 64, 0, s>>>(g, c, st, bd, clk, 1);
+  const unsigned zz = 2u * (unsigned)g.nmem;
+  k_bdy_ring<R><<<dim3((unsigned)((nwe + 63) / 64), (unsigned)g.kz, zz), 64, 0, s>>>(g, c, st, bd, clk, 0);
+  k_bdy_ring<R><<<dim3((unsigned)((nsn + 63) / 64), (unsigned)g.kz, zz), 64, 0, s>>>(g, c, st, bd, clk, 1);
 }
 
 template <class R>
 void Launch<R>::bdy_relax(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                           const Bdy<R> &bd, const Clock *clk, cudaStream_t s) {
   const dim3 b(32, 4);
-  k_bdy_relax<R><<<grid2(g.jx - 2, g.iy - 2, b), b, 0, s>>>(g, c, sa, st, bd, clk);
+  k_bdy_relax<R><<<grid2(g.jx - 2, g.iy - 2, b, g.nmem), b, 0, s>>>(g, c, sa, st, bd, clk);
 }
 
 template <class R>
 void Launch<R>::end_cross(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                           cudaStream_t s) {
   const dim3 b(32, 4);
-  k_end_cross<R><<<grid2(g.jx - 1, g.iy - 1, b), b, 0, s>>>(g, c, sa, st);
+  k_end_cross<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, c, sa, st);
 }
 
 template <class R>
 void Launch<R>::end_uvstag(const Geom &g, const State<R> &st, cudaStream_t s) {
   const dim3 b(32, 4);
-  k_end_uvstag<R><<<grid2(g.jx, g.iy, b), b, 0, s>>>(g, st.ux, st.vx, st.u, st.v);
+  k_end_uvstag<R><<<grid2(g.jx, g.iy, b, g.nmem), b, 0, s>>>(g, st.ux, st.vx, st.u, st.v);
 }
 
 template <class R>
 void Launch<R>::end_reduce(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                            double *partials, int nblocks, DiagDev *diag, Clock *clk, cudaStream_t s) {
-  k_reduce_partial<R><<<nblocks, kRedThreads, 0, s>>>(g, c, sa, st, partials, rows_per_block(g));
-  k_reduce_final<<<1, 32, 0, s>>>(partials, nblocks, diag, clk, c.dtsec, c.apply_bdy);
+  k_reduce_partial<R><<<dim3((unsigned)nblocks, (unsigned)g.nmem), kRedThreads, 0, s>>>(
+      g, c, sa, st, partials, rows_per_block(g));
+  k_reduce_final<<<(unsigned)g.nmem, 32, 0, s>>>(partials, nblocks, diag, clk, c.dtsec, c.apply_bdy,
+                                                 g.mstride);
 }
 
 template <class R>

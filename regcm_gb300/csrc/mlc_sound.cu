@@ -37,6 +37,9 @@ __device__ __forceinline__ double relax_weight(const int32_t *ibnd, const double
 
 template <class R>
 __global__ void k_sound_prep(Geom g, const double *__restrict__ tetav, double *__restrict__ tetavf) {
+  const size_t mo = (size_t)blockIdx.z * g.mstride;
+  tetav = mshift(tetav, mo);
+  tetavf = mshift(tetavf, mo);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
@@ -54,6 +57,9 @@ template <class R>
 __global__ void k_sound_div(Geom g, Scal c, Stat<R> sa, const R *__restrict__ u,
                             const R *__restrict__ v, R *__restrict__ zdiv2, R *__restrict__ s,
                             R *__restrict__ w) {
+  const size_t mo = (size_t)blockIdx.z * g.mstride;
+  rebase(sa, mo);
+  u = mshift(u, mo); v = mshift(v, mo); zdiv2 = mshift(zdiv2, mo); s = mshift(s, mo); w = mshift(w, mo);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
@@ -115,6 +121,10 @@ __global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ 
   double *wp = smem + (size_t)(kz + 2) * nth;      // w after elimination, then final
   double *wk = smem + (size_t)2 * (kz + 2) * nth;  // elimination multipliers
 #define COL(a, k) a[(size_t)(k) * nth + tid]
+  const size_t mo = (size_t)blockIdx.z * g.mstride;
+  rebase(sa, mo);
+  zraw = mshift(zraw, mo); s = mshift(s, mo); w = mshift(w, mo); pai = mshift(pai, mo);
+  tetav = mshift(tetav, mo); tetavf = mshift(tetavf, mo);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (j > g.jx - 2 || i > g.iy - 2) return;
@@ -204,6 +214,10 @@ __global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict
                                  const R *__restrict__ v_in, R *__restrict__ u_out,
                                  R *__restrict__ v_out, const R *__restrict__ zraw,
                                  const double *__restrict__ pai, const double *__restrict__ tetav) {
+  const size_t mo = (size_t)blockIdx.z * g.mstride;
+  rebase(sa, mo);
+  u_in = mshift(u_in, mo); v_in = mshift(v_in, mo); u_out = mshift(u_out, mo);
+  v_out = mshift(v_out, mo); zraw = mshift(zraw, mo); pai = mshift(pai, mo); tetav = mshift(tetav, mo);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx || i > g.iy) return;
@@ -266,21 +280,22 @@ __global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict
   }
 }
 
-inline dim3 col_grid(int nj, int ni) {
-  return dim3((unsigned)((nj + kColX - 1) / kColX), (unsigned)((ni + kColY - 1) / kColY));
+inline dim3 col_grid(int nj, int ni, int nmem) {
+  return dim3((unsigned)((nj + kColX - 1) / kColX), (unsigned)((ni + kColY - 1) / kColY),
+              (unsigned)nmem);
 }
 
 }  // namespace
 
 template <class R>
 void Launch<R>::sound_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
-  k_sound_prep<R><<<col_grid(g.jx - 1, g.iy - 1), dim3(kColX, kColY), 0, s>>>(g, st.tetav, wk.tetavf);
+  k_sound_prep<R><<<col_grid(g.jx - 1, g.iy - 1, g.nmem), dim3(kColX, kColY), 0, s>>>(g, st.tetav, wk.tetavf);
 }
 
 template <class R>
 void Launch<R>::sound_div(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                           const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s) {
-  k_sound_div<R><<<col_grid(g.jx - 1, g.iy - 1), dim3(kColX, kColY), 0, s>>>(
+  k_sound_div<R><<<col_grid(g.jx - 1, g.iy - 1, g.nmem), dim3(kColX, kColY), 0, s>>>(
       g, c, sa, b.u_in, b.v_in, wk.zdiv2, wk.s, st.w);
 }
 
@@ -289,7 +304,8 @@ void Launch<R>::sound_solve(const Geom &g, const Scal &c, const Stat<R> &sa, con
                             const Work<R> &wk, bool last, cudaStream_t s) {
   const dim3 blk(32, 2);
   const size_t smem = (size_t)3 * (g.kz + 2) * blk.x * blk.y * sizeof(double);
-  const dim3 grd((unsigned)((g.jx - 3 + blk.x - 1) / blk.x), (unsigned)((g.iy - 3 + blk.y - 1) / blk.y));
+  const dim3 grd((unsigned)((g.jx - 3 + blk.x - 1) / blk.x), (unsigned)((g.iy - 3 + blk.y - 1) / blk.y),
+                 (unsigned)g.nmem);
   k_sound_solve<R><<<grd, blk, smem, s>>>(g, c, sa, wk.zdiv2, wk.s, st.w, st.pai, st.tetav,
                                           wk.tetavf, last ? 1 : 0);
 }
@@ -297,7 +313,7 @@ void Launch<R>::sound_solve(const Geom &g, const Scal &c, const Stat<R> &sa, con
 template <class R>
 void Launch<R>::sound_momentum(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                                const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s) {
-  k_sound_momentum<R><<<col_grid(g.jx, g.iy), dim3(kColX, kColY), 0, s>>>(
+  k_sound_momentum<R><<<col_grid(g.jx, g.iy, g.nmem), dim3(kColX, kColY), 0, s>>>(
       g, c, sa, b.u_in, b.v_in, b.u_out, b.v_out, wk.zdiv2, st.pai, st.tetav);
 }
 

@@ -19,8 +19,8 @@ import ctypes as C
 from . import abi
 from .abi import MolochError
 
-__all__ = ["MolochDomain", "MolochError", "CFLViolation", "allocate_moloch", "init_moloch",
-           "moloch"]
+__all__ = ["MolochDomain", "MolochBatch", "MolochError", "CFLViolation", "allocate_moloch",
+           "init_moloch", "moloch"]
 
 
 class CFLViolation(MolochError):
@@ -65,15 +65,10 @@ class MolochDomain:
         abi.check(self.lib.mlc_download_state(self._ctx, C.byref(state_ptrs)), "download")
 
     def launches_per_step(self) -> int:
-        f = self.lib.mlc_launches_per_step
-        f.restype = C.c_int
-        f.argtypes = [C.c_void_p]
-        return f(self._ctx)
+        return self.lib.mlc_launches_per_step(self._ctx)
 
     def set_graphs(self, on: bool):
-        f = self.lib.mlc_set_graphs
-        f.argtypes = [C.c_void_p, C.c_int]
-        abi.check(f(self._ctx, 1 if on else 0), "mlc_set_graphs")
+        abi.check(self.lib.mlc_set_graphs(self._ctx, 1 if on else 0), "mlc_set_graphs")
 
     def close(self):
         if self._ctx:
@@ -85,6 +80,68 @@ class MolochDomain:
 
     def __exit__(self, *exc):
         self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MolochBatch:
+    """An ensemble: nmem domains of the same extents and parameters advanced by
+    the same kernel launches (one launch per kernel stage for all members)."""
+
+    def __init__(self, cases):
+        if not cases:
+            raise ValueError("empty ensemble")
+        self.lib = abi.load()
+        self.cases = list(cases)
+        c0 = self.cases[0]
+        self.dims, self.params = c0.dims, c0.params
+        self._ctx = C.c_void_p()
+        abi.check(self.lib.mlc_create_batch(C.byref(c0.dims), C.byref(c0.params), len(self.cases),
+                                            C.byref(self._ctx)), "allocate_moloch(batch)")
+        self._keep = []
+        for m, c in enumerate(self.cases):
+            sp, bp = c.static_ptrs(), c.bdy_ptrs()
+            self._keep += [sp, bp]
+            abi.check(self.lib.mlc_member_bind_static(self._ctx, m, C.byref(sp)), "init_moloch")
+            abi.check(self.lib.mlc_member_upload_state(self._ctx, m, C.byref(c.state_ptrs())),
+                      "init_moloch(state)")
+            if c.params.do_apply_bdy:
+                abi.check(self.lib.mlc_member_set_boundary(self._ctx, m, C.byref(bp), c.xbctime,
+                                                           c.params.dtbdys), "bdyin")
+
+    @property
+    def nmem(self) -> int:
+        return len(self.cases)
+
+    def step(self, nsteps: int = 1):
+        diags = (abi.mlc_diag * self.nmem)()
+        st = self.lib.mlc_step_batch(self._ctx, nsteps, diags)
+        if st == abi.MLC_ERR_NONFINITE:
+            raise CFLViolation(st, "moloch(batch)")
+        abi.check(st, "moloch(batch)")
+        return list(diags)
+
+    def download(self, m: int, state_ptrs: abi.mlc_state_ptrs):
+        abi.check(self.lib.mlc_member_download_state(self._ctx, m, C.byref(state_ptrs)),
+                  "download")
+
+    def upload(self, m: int, state_ptrs: abi.mlc_state_ptrs):
+        abi.check(self.lib.mlc_member_upload_state(self._ctx, m, C.byref(state_ptrs)), "upload")
+
+    def set_graphs(self, on: bool):
+        abi.check(self.lib.mlc_set_graphs(self._ctx, 1 if on else 0), "mlc_set_graphs")
+
+    def launches_per_step(self) -> int:
+        return self.lib.mlc_launches_per_step(self._ctx)
+
+    def close(self):
+        if self._ctx:
+            self.lib.mlc_destroy(self._ctx)
+            self._ctx = C.c_void_p()
 
     def __del__(self):
         try:
