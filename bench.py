@@ -346,6 +346,95 @@ def run_ours(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_ensemble(args, rank, world):
+    """Ensemble workload: members of the dry recipe (128x128x30, dx 12 km,
+    dt 60 s, 3 substeps, theta noise +-0.5 K and wind U(5,20) per member)
+    advanced by one launch per kernel stage, autotuned launch shapes; next to
+    the plain single-domain FP64 path on one member."""
+    import torch
+    from regcm_gb300 import abi
+    from regcm_gb300 import case as cs
+    from regcm_gb300.moloch import MolochBatch, domain_from_case
+
+    class KT(C.Structure):
+        _fields_ = [("name", C.c_char * 32), ("launches", C.c_int32), ("ms", C.c_double)]
+
+    lib = abi.load()
+    lib.mlc_step_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.mlc_diag),
+                                   C.POINTER(C.c_float)]
+    lib.mlc_profile_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(KT), C.c_int,
+                                      C.POINTER(C.c_int)]
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    n = args.size or 128
+    nmem = args.members
+    prec = abi.MLC_PREC_FP64 if args.precision == "fp64" else abi.MLC_PREC_MIXED
+    cases = [cs.config2_member(rank * nmem + m, nx=n, ny=n, kz=30, precision=prec)
+             for m in range(nmem)]
+    pts = cases[0].points
+    batch = MolochBatch(cases)
+    batch.step(args.warmup)
+    tune = None if args.no_tune else batch.autotune(2)
+    batch.step(2)  # re-record graphs with the picked shapes
+    if world > 1:
+        torch.distributed.barrier()
+    diag = abi.mlc_diag()
+    ms = C.c_float()
+    with ClockSampler(dev) as clk:
+        abi.check(lib.mlc_step_timed(batch._ctx, args.steps, C.byref(diag), C.byref(ms)), "batch")
+    t_dev = ms.value / 1000.0
+    if world > 1:
+        t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = pts * nmem * args.steps * world / t_dev
+    ktab = (KT * 32)()
+    nk = C.c_int()
+    abi.check(lib.mlc_profile_steps(batch._ctx, 1, ktab, 32, C.byref(nk)), "profile")
+    kernels = {ktab[i].name.decode(): (ktab[i].launches, ktab[i].ms) for i in range(nk.value)}
+    launches = batch.launches_per_step()
+    batch.close()
+    # plain single-domain FP64 path on member 0's recipe
+    single = cs.config2_member(rank * nmem, nx=n, ny=n, kz=30, precision=abi.MLC_PREC_FP64)
+    d = domain_from_case(single)
+    d.step(args.warmup)
+    ms1 = C.c_float()
+    abi.check(lib.mlc_step_timed(d._ctx, args.steps, C.byref(diag), C.byref(ms1)), "single")
+    d.close()
+    plain = pts * args.steps / (ms1.value / 1000.0)
+    if rank != 0:
+        return
+    wbytes = 4 if prec == abi.MLC_PREC_MIXED else 8
+    dom_name = max(kernels, key=lambda k: kernels[k][1])
+    nl, kms = kernels[dom_name]
+    bytes_per = kernel_bytes(dom_name, cases[0], n_adv_fields(cases[0]), wbytes)
+    pk = peaks()
+    hbm_peak = float(pk.get("hbm_gbs", 6800.0))
+    roofline = {"kernel": dom_name, "bound": "hbm", "unit": "GB/s", "peak": hbm_peak,
+                "peak_source": "measured" if "hbm_gbs" in pk else "fallback", "traffic": None,
+                "share_of_step": kms / sum(v[1] for v in kernels.values()),
+                "kernels_ms_per_step": {k: v[1] for k, v in sorted(kernels.items(),
+                                                                     key=lambda kv: -kv[1][1])}}
+    if bytes_per:
+        ach = bytes_per * nmem / (kms / nl / 1000.0) / 1e9
+        roofline.update({"achieved": ach, "frac": ach / hbm_peak})
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if prec == abi.MLC_PREC_MIXED else "f64", "data": "synthetic",
+        "config": {"workload": f"moloch-ensemble-{nmem}x{n}x{n}x30-dx12km-dt60-ns3",
+                   "members": nmem, "points_per_member": pts, "precision": args.precision,
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2"},
+        "roofline": roofline, "gpu_launches": launches * args.steps,
+        "side_by_side": {"plain_fp64_single_domain": {"value": plain, "unit": UNIT},
+                         "ratio_to_plain_fp64": value / world / plain,
+                         "autotune": tune},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_mixed_side(args, rank):
     """The same workload in mixed precision (FP32 fields, FP64 solve/Exner/theta),
     timed the same way, for the FP64-and-FP32 side-by-side report."""
@@ -375,7 +464,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c1", choices=["c0", "c1"])
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
+    ap.add_argument("--members", type=int, default=64, help="ensemble members (config c2)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
@@ -390,6 +481,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.config == "c2":
+        run_ensemble(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1 and args.impl == "ours":

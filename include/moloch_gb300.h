@@ -221,6 +221,24 @@ int mlc_member_set_boundary(mlc_ctx *ctx, int m, const mlc_bdy_ptrs *b, double x
 /* nsteps steps of every member; out (optional) receives nmem diagnostics. */
 int mlc_step_batch(mlc_ctx *ctx, int nsteps, mlc_diag *out);
 
+/* Launch shapes picked by mlc_autotune, and the per-step device time of the
+ * tuned kernels against the fixed 32x8 configuration (column kernels and
+ * horizontal WAF tiles 32x8; solve and vertical WAF 32x2). */
+typedef struct mlc_tune_report {
+  int32_t col_x, col_y;      /* column kernels                        */
+  int32_t solve_x, solve_y;  /* implicit w-Exner solve                */
+  int32_t vert_x, vert_y;    /* vertical WAF passes                   */
+  int32_t htile;             /* horizontal WAF tile: 0 32x8, 1 32x4, 2 64x4, 3 16x8 */
+  double  ms_fixed;          /* tuned kernel groups, fixed shapes [ms/step] */
+  double  ms_tuned;          /* the same groups, picked shapes [ms/step]    */
+} mlc_tune_report;
+
+/* Try candidate launch shapes on this context's own state (snapshotted and
+ * restored, so the state is unchanged afterwards), keep the fastest per
+ * kernel group, and re-record the step graphs.  No counterpart in the
+ * reference. */
+int mlc_autotune(mlc_ctx *ctx, int steps_per_trial, mlc_tune_report *rep);
+
 /* Device bytes one domain of these extents holds (for admission control). */
 size_t mlc_footprint_bytes(const mlc_dims *dims, int precision);
 

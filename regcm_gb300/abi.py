@@ -80,6 +80,15 @@ class mlc_bdy_ptrs(C.Structure):
     _fields_ = [(n, _dp * 2) for n in BDY_FIELDS]
 
 
+class mlc_tune_report(C.Structure):
+    _fields_ = [("col_x", C.c_int32), ("col_y", C.c_int32), ("solve_x", C.c_int32),
+                ("solve_y", C.c_int32), ("vert_x", C.c_int32), ("vert_y", C.c_int32),
+                ("htile", C.c_int32), ("ms_fixed", C.c_double), ("ms_tuned", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class mlc_diag(C.Structure):
     _fields_ = [("ps_max", C.c_double), ("ps_min", C.c_double), ("nonfinite", C.c_int32),
                 ("steps_done", C.c_int32), ("drymass", C.c_double), ("dryadv", C.c_double),
@@ -142,6 +151,7 @@ def _declare(lib):
         "mlc_step_batch": (C.c_int, [C.c_void_p, C.c_int, P(mlc_diag)]),
         "mlc_launches_per_step": (C.c_int, [C.c_void_p]),
         "mlc_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+        "mlc_autotune": (C.c_int, [C.c_void_p, C.c_int, P(mlc_tune_report)]),
     }
     for name, (res, args) in sigs.items():
         try:

@@ -25,7 +25,6 @@ namespace mlc {
 
 namespace {
 
-constexpr int kTJ = 32, kTI = 8;
 
 // Main/mod_moloch.F90:1571-1590; minnum is the 4-byte real holding minden.
 template <class R> struct FlowEps;
@@ -158,7 +157,7 @@ __global__ void k_adv_vertical(Geom g, Scal c, Stat<R> sa, const R *__restrict__
 }
 
 // Meridional then zonal WAF for one tile (:984-1038; ROTLLR :926-983).
-template <class R, class T>
+template <class R, class T, int kTJ, int kTI>
 __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Stat<R> sa,
                                                             const R *__restrict__ u,
                                                             const R *__restrict__ v, AdvTable<T> t) {
@@ -379,26 +378,37 @@ inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
 
 template <class R>
 void Launch<R>::adv_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
-  const dim3 b(32, 4);
+  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
   k_adv_prep<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, st.u, st.v, st.w, st.ux, st.vx, wk.wx);
 }
 
 template <class R, class T>
 void launch_vertical(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
                      const AdvTable<T> &t, cudaStream_t s) {
-  const dim3 b(32, 2);
+  const dim3 b((unsigned)g.vert_x, (unsigned)g.vert_y);
   const size_t smem = (size_t)3 * (g.kz + 2) * b.x * b.y * sizeof(T);
   dim3 grd = grid2(g.jx - 1, g.iy - 1, b, 1);
   grd.z = (unsigned)(t.n * g.nmem);
   k_adv_vertical<R, T><<<grd, b, smem, s>>>(g, c, sa, wk.s, t);
 }
 
+template <class R, class T, int TJ, int TI>
+void launch_tile(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
+                 const AdvTable<T> &t, cudaStream_t s) {
+  dim3 grd((unsigned)((g.jx - 1 + TJ - 1) / TJ), (unsigned)((g.iy - 1 + TI - 1) / TI),
+           (unsigned)(t.n * g.kz * g.nmem));
+  k_adv_horizontal<R, T, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(g, c, sa, st.u, st.v, t);
+}
+
 template <class R, class T>
 void launch_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                        const AdvTable<T> &t, cudaStream_t s) {
-  dim3 grd((unsigned)((g.jx - 1 + kTJ - 1) / kTJ), (unsigned)((g.iy - 1 + kTI - 1) / kTI),
-           (unsigned)(t.n * g.kz * g.nmem));
-  k_adv_horizontal<R, T><<<grd, dim3(kTJ, kTI), 0, s>>>(g, c, sa, st.u, st.v, t);
+  switch (g.htile) {
+    case 1: launch_tile<R, T, 32, 4>(g, c, sa, st, t, s); break;
+    case 2: launch_tile<R, T, 64, 4>(g, c, sa, st, t, s); break;
+    case 3: launch_tile<R, T, 16, 8>(g, c, sa, st, t, s); break;
+    default: launch_tile<R, T, 32, 8>(g, c, sa, st, t, s); break;
+  }
 }
 
 template <class R>
@@ -428,13 +438,13 @@ void Launch<R>::adv_horizontal_f64(const Geom &g, const Scal &c, const Stat<R> &
 template <class R>
 void Launch<R>::adv_curvature(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                               cudaStream_t s) {
-  const dim3 b(32, 4);
+  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
   k_adv_curvature<R><<<grid2(g.jx - 3, g.iy - 3, b, g.nmem), b, 0, s>>>(g, c, sa, st.ux, st.vx);
 }
 
 template <class R>
 void Launch<R>::adv_back(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
-  const dim3 b(32, 4);
+  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
   k_adv_back<R><<<grid2(g.jx, g.iy, b, g.nmem), b, 0, s>>>(g, st.ux, st.vx, wk.wx, st.u, st.v, st.w);
 }
 

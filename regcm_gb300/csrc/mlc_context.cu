@@ -159,6 +159,11 @@ void bind_views(Arrays<R> &a) {
 Geom make_geom(const mlc_dims &d, int elem_bytes) {
   Geom g{};
   g.jx = d.jx; g.iy = d.iy; g.kz = d.kz; g.nqx = d.nqx; g.ntr = d.ntr;
+  g.nmem = 1;
+  g.col_x = 32; g.col_y = 4;
+  g.solve_x = 32; g.solve_y = 2;
+  g.vert_x = 32; g.vert_y = 2;
+  g.htile = 0;
   const int per_line = 128 / elem_bytes;
   g.P = (d.jx + per_line - 1) / per_line * per_line;
   g.PS = (size_t)g.P * d.iy;
@@ -1033,6 +1038,144 @@ int mlc_profile_steps(mlc_ctx *x, int nsteps, mlc_kernel_time *out, int max_out,
   }
   *n_out = n;
   return cuda_status(cudaGetLastError());
+}
+
+}  // extern "C"
+
+// ---- autotuner ------------------------------------------------------------
+namespace {
+
+const int kColCand[][2] = {{32, 4}, {32, 8}, {64, 2}, {64, 4}, {128, 1}, {16, 8}};
+const int kSolveCand[][2] = {{32, 2}, {32, 1}, {64, 1}, {32, 4}, {16, 4}};
+const int kVertCand[][2] = {{32, 2}, {32, 1}, {64, 1}, {32, 4}, {16, 4}};
+constexpr int kNCol = 6, kNSolve = 5, kNVert = 5, kNTile = 4;
+
+int group_of(const char *name) {
+  if (!std::strcmp(name, "sound_solve")) return 1;
+  if (!std::strncmp(name, "adv_vertical", 12)) return 2;
+  if (!std::strncmp(name, "adv_horizontal", 14)) return 3;
+  if (!std::strcmp(name, "bdy_ring") || !std::strcmp(name, "end_reduce")) return -1;
+  return 0;  // column kernels
+}
+
+bool shapes_fit(const Geom &g, int elem) {
+  const size_t col3 = (size_t)3 * (g.kz + 2) * sizeof(double);
+  if (col3 * g.solve_x * g.solve_y > 200 * 1024) return false;
+  if ((size_t)3 * (g.kz + 2) * elem * g.vert_x * g.vert_y > 200 * 1024) return false;
+  return g.col_x * g.col_y <= 1024;
+}
+
+// Per-group device time (ms) of `steps` eager steps with the shapes in x->g.
+template <class R>
+int time_groups(mlc_ctx *x, Arrays<R> &a, int steps, double ms[4]) {
+  Recorder rec;
+  rec.s = x->stream;
+  for (int n = 0; n < steps; ++n) enqueue_step<R>(x, a, &rec);
+  MLC_TRY(cudaStreamSynchronize(x->stream));
+  for (int q = 0; q < 4; ++q) ms[q] = 0.0;
+  for (auto &m : rec.marks) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, m.a, m.b);
+    const int gq = group_of(m.name);
+    if (gq >= 0) ms[gq] += t;
+  }
+  for (int q = 0; q < 4; ++q) ms[q] /= steps;
+  return cuda_status(cudaGetLastError());
+}
+
+template <class R>
+int autotune_impl(mlc_ctx *x, Arrays<R> &a, int steps, mlc_tune_report *rep) {
+  void *snap = nullptr;
+  if (cudaMalloc(&snap, x->arena_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return MLC_ERR_NOMEM;
+  }
+  const int uv0 = x->uv_role, adv0 = x->adv_role;
+  MLC_TRY(cudaMemcpyAsync(snap, x->arena, x->arena_bytes, cudaMemcpyDeviceToDevice, x->stream));
+  auto restore = [&]() {
+    cudaMemcpyAsync(x->arena, snap, x->arena_bytes, cudaMemcpyDeviceToDevice, x->stream);
+    x->uv_role = uv0;
+    x->adv_role = adv0;
+  };
+  const Geom base = x->g;
+  double best[4] = {1e30, 1e30, 1e30, 1e30};
+  int pick[4] = {0, 0, 0, 0};
+  int st = MLC_OK;
+  const int ntrial = 6;
+  for (int tr = 0; tr < ntrial && st == MLC_OK; ++tr) {
+    Geom g = base;
+    g.col_x = kColCand[tr % kNCol][0]; g.col_y = kColCand[tr % kNCol][1];
+    g.solve_x = kSolveCand[tr % kNSolve][0]; g.solve_y = kSolveCand[tr % kNSolve][1];
+    g.vert_x = kVertCand[tr % kNVert][0]; g.vert_y = kVertCand[tr % kNVert][1];
+    g.htile = tr % kNTile;
+    const bool fit = shapes_fit(g, (int)sizeof(R));
+    if (!fit) {  // fall back to the base solve/vertical shapes for this trial
+      g.solve_x = base.solve_x; g.solve_y = base.solve_y;
+      g.vert_x = base.vert_x; g.vert_y = base.vert_y;
+    }
+    x->g = g;
+    double ms[4];
+    restore();
+    st = time_groups<R>(x, a, 1, ms);  // first use of the shapes
+    if (st != MLC_OK) break;
+    restore();
+    st = time_groups<R>(x, a, steps, ms);
+    if (st != MLC_OK) break;
+    const int idx[4] = {tr % kNCol, fit ? tr % kNSolve : 0, fit ? tr % kNVert : 0, tr % kNTile};
+    for (int q = 0; q < 4; ++q)
+      if (ms[q] < best[q]) { best[q] = ms[q]; pick[q] = idx[q]; }
+  }
+  // the fixed reference configuration: 32 x 8 columns and tiles
+  Geom fixed = base;
+  fixed.col_x = 32; fixed.col_y = 8; fixed.htile = 0;
+  fixed.solve_x = 32; fixed.solve_y = 2; fixed.vert_x = 32; fixed.vert_y = 2;
+  double msf[4] = {0, 0, 0, 0}, mst[4] = {0, 0, 0, 0};
+  if (st == MLC_OK) {
+    x->g = fixed;
+    restore();
+    st = time_groups<R>(x, a, steps, msf);
+  }
+  Geom tuned = base;
+  tuned.col_x = kColCand[pick[0]][0]; tuned.col_y = kColCand[pick[0]][1];
+  tuned.solve_x = kSolveCand[pick[1]][0]; tuned.solve_y = kSolveCand[pick[1]][1];
+  tuned.vert_x = kVertCand[pick[2]][0]; tuned.vert_y = kVertCand[pick[2]][1];
+  tuned.htile = pick[3];
+  if (!shapes_fit(tuned, (int)sizeof(R))) tuned = base;
+  if (st == MLC_OK) {
+    x->g = tuned;
+    restore();
+    st = time_groups<R>(x, a, steps, mst);
+  }
+  restore();
+  cudaStreamSynchronize(x->stream);
+  cudaFree(snap);
+  if (st != MLC_OK) {
+    x->g = base;
+    return st;
+  }
+  x->g = tuned;
+  for (auto &gx : x->graph)
+    if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
+  if (rep) {
+    rep->col_x = tuned.col_x; rep->col_y = tuned.col_y;
+    rep->solve_x = tuned.solve_x; rep->solve_y = tuned.solve_y;
+    rep->vert_x = tuned.vert_x; rep->vert_y = tuned.vert_y;
+    rep->htile = tuned.htile;
+    rep->ms_fixed = msf[0] + msf[1] + msf[2] + msf[3];
+    rep->ms_tuned = mst[0] + mst[1] + mst[2] + mst[3];
+  }
+  return MLC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mlc_autotune(mlc_ctx *x, int steps, mlc_tune_report *rep) {
+  if (!x || steps < 1) return MLC_ERR_INVALID;
+  if (!x->have_static || !x->have_state || (x->c.apply_bdy && !x->have_bdy)) return MLC_ERR_STATE;
+  return x->prm.precision == MLC_PREC_MIXED ? autotune_impl<float>(x, x->af, steps, rep)
+                                            : autotune_impl<double>(x, x->ad, steps, rep);
 }
 
 // Kernels one mlc_step(ctx, 1) launches (for launch accounting).

@@ -22,6 +22,11 @@ struct Geom {
   size_t PS;    // plane stride = P*iy
   int nmem;       // ensemble members advanced by one launch (1 = one domain)
   size_t mstride; // bytes between consecutive members' arenas
+  // launch shapes (picked by the autotuner; defaults in mlc_context.cu)
+  int col_x, col_y;      // column kernels (threads along j, i)
+  int solve_x, solve_y;  // sound_solve
+  int vert_x, vert_y;    // adv_vertical
+  int htile;             // adv_horizontal tile: 0 32x8, 1 32x4, 2 64x4, 3 16x8
   __host__ __device__ size_t at(int j, int i, int k) const {
     return (size_t)(j - 1) + (size_t)(i - 1) * (size_t)P + (size_t)(k - 1) * PS;
   }

@@ -515,7 +515,7 @@ int reduce_blocks(const Geom &g) {
 
 template <class R>
 void Launch<R>::end_tvirt(const Geom &g, const Scal &c, const State<R> &st, cudaStream_t s) {
-  const dim3 b(32, 4);
+  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
   k_end_tvirt<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, c, st);
 }
 
@@ -531,20 +531,20 @@ void Launch<R>::bdy_ring(const Geom &g, const Scal &c, const State<R> &st, const
 template <class R>
 void Launch<R>::bdy_relax(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                           const Bdy<R> &bd, const Clock *clk, cudaStream_t s) {
-  const dim3 b(32, 4);
+  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
   k_bdy_relax<R><<<grid2(g.jx - 2, g.iy - 2, b, g.nmem), b, 0, s>>>(g, c, sa, st, bd, clk);
 }
 
 template <class R>
 void Launch<R>::end_cross(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                           cudaStream_t s) {
-  const dim3 b(32, 4);
+  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
   k_end_cross<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, c, sa, st);
 }
 
 template <class R>
 void Launch<R>::end_uvstag(const Geom &g, const State<R> &st, cudaStream_t s) {
-  const dim3 b(32, 4);
+  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
   k_end_uvstag<R><<<grid2(g.jx, g.iy, b, g.nmem), b, 0, s>>>(g, st.ux, st.vx, st.u, st.v);
 }
 

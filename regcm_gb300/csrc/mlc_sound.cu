@@ -26,8 +26,6 @@ namespace mlc {
 
 namespace {
 
-constexpr int kColX = 32;  // threads along j for column kernels
-constexpr int kColY = 4;   // threads along i
 
 __device__ __forceinline__ double relax_weight(const int32_t *ibnd, const double *hefc, int nsp,
                                                size_t ij, int k) {
@@ -280,29 +278,30 @@ __global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict
   }
 }
 
-inline dim3 col_grid(int nj, int ni, int nmem) {
-  return dim3((unsigned)((nj + kColX - 1) / kColX), (unsigned)((ni + kColY - 1) / kColY),
-              (unsigned)nmem);
+inline dim3 col_block(const Geom &g) { return dim3((unsigned)g.col_x, (unsigned)g.col_y); }
+inline dim3 col_grid(const Geom &g, int nj, int ni) {
+  return dim3((unsigned)((nj + g.col_x - 1) / g.col_x), (unsigned)((ni + g.col_y - 1) / g.col_y),
+              (unsigned)g.nmem);
 }
 
 }  // namespace
 
 template <class R>
 void Launch<R>::sound_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
-  k_sound_prep<R><<<col_grid(g.jx - 1, g.iy - 1, g.nmem), dim3(kColX, kColY), 0, s>>>(g, st.tetav, wk.tetavf);
+  k_sound_prep<R><<<col_grid(g, g.jx - 1, g.iy - 1), col_block(g), 0, s>>>(g, st.tetav, wk.tetavf);
 }
 
 template <class R>
 void Launch<R>::sound_div(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                           const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s) {
-  k_sound_div<R><<<col_grid(g.jx - 1, g.iy - 1, g.nmem), dim3(kColX, kColY), 0, s>>>(
+  k_sound_div<R><<<col_grid(g, g.jx - 1, g.iy - 1), col_block(g), 0, s>>>(
       g, c, sa, b.u_in, b.v_in, wk.zdiv2, wk.s, st.w);
 }
 
 template <class R>
 void Launch<R>::sound_solve(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                             const Work<R> &wk, bool last, cudaStream_t s) {
-  const dim3 blk(32, 2);
+  const dim3 blk((unsigned)g.solve_x, (unsigned)g.solve_y);
   const size_t smem = (size_t)3 * (g.kz + 2) * blk.x * blk.y * sizeof(double);
   const dim3 grd((unsigned)((g.jx - 3 + blk.x - 1) / blk.x), (unsigned)((g.iy - 3 + blk.y - 1) / blk.y),
                  (unsigned)g.nmem);
@@ -313,7 +312,7 @@ void Launch<R>::sound_solve(const Geom &g, const Scal &c, const Stat<R> &sa, con
 template <class R>
 void Launch<R>::sound_momentum(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
                                const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s) {
-  k_sound_momentum<R><<<col_grid(g.jx, g.iy, g.nmem), dim3(kColX, kColY), 0, s>>>(
+  k_sound_momentum<R><<<col_grid(g, g.jx, g.iy), col_block(g), 0, s>>>(
       g, c, sa, b.u_in, b.v_in, b.u_out, b.v_out, wk.zdiv2, st.pai, st.tetav);
 }
 

@@ -138,6 +138,11 @@ class MolochBatch:
     def launches_per_step(self) -> int:
         return self.lib.mlc_launches_per_step(self._ctx)
 
+    def autotune(self, steps_per_trial: int = 2) -> dict:
+        rep = abi.mlc_tune_report()
+        abi.check(self.lib.mlc_autotune(self._ctx, steps_per_trial, C.byref(rep)), "autotune")
+        return rep.as_dict()
+
     def close(self):
         if self._ctx:
             self.lib.mlc_destroy(self._ctx)

@@ -53,3 +53,20 @@ def test_batch_members_differ_and_graph_matches_eager():
         states.append(ga)
     # members carry their own winds and noise
     assert not np.array_equal(states[0]["u"], states[1]["u"])
+
+
+def test_autotune_keeps_state_and_results():
+    tuned = MolochBatch(members(abi.MLC_PREC_MIXED, 3))
+    plain = MolochBatch(members(abi.MLC_PREC_MIXED, 3))
+    rep = tuned.autotune(1)
+    assert rep["ms_tuned"] > 0 and rep["ms_fixed"] > 0
+    assert rep["col_x"] * rep["col_y"] <= 1024 and rep["htile"] in (0, 1, 2, 3)
+    tuned.step(4)
+    plain.step(4)
+    for m in range(3):
+        a = tuned.cases[m].empty_state()
+        tuned.download(m, tuned.cases[m].state_ptrs_of(a))
+        b = plain.cases[m].empty_state()
+        plain.download(m, plain.cases[m].state_ptrs_of(b))
+        for n in a:
+            assert np.array_equal(a[n], b[n]), (m, n)
