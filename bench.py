@@ -110,30 +110,36 @@ class ClockSampler:
 
 # ---- algorithmic bytes per launch of each kernel group ---------------------
 def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None:
-    """Compulsory HBM words each launch must move, times the word size.
+    """Compulsory HBM bytes each launch must move.
 
     Counts follow the fusion contract 'each kernel reads its inputs and writes
     its outputs once'; 2-D and 1-D arrays are ignored.  Per point (cross
-    point x level) of the launch's domain:
-      sound_div       u, v, rfmzu, rfmzv, fmz -> zdiv2, s                 7
-      sound_solve     zdiv2, s, w, pai, tetav, tetavf, fmz, fmzf
-                      -> w, pai, tetavf                                   11
-      sound_momentum  u, v, zdiv2, pai, tetav -> u, v                      7
-      adv_vertical    per field: field -> wz (2); shared s, zrfmu, zrfmd   2F+3
-      adv_horizontal  per field: field, wz -> out (3); shared u, v, fmz,
-                      rfmzu                                               3F+4
+    point x level) of the launch's domain, with R the field type (wbytes) and
+    D = FP64 (the Exner function and theta_v are FP64 in both precisions,
+    and the solve reads FP64 copies of fmz, fmzf):
+      sound_div       u, v, rfmzu, rfmzv, fmz -> zdiv2, s               7 R
+      sound_solve     zdiv2, s, w -> w                                  4 R
+                      pai, tetav, tetavf, fmz, fmzf -> pai, tetavf      7 D
+      sound_momentum  u, v, zdiv2 -> u, v                               5 R
+                      pai, tetav                                        2 D
+      adv_vertical    per field: field -> wz (2); shared s, zrfmu, zrfmd
+      adv_horizontal  per field: field, wz -> out (3); shared u, v, fmz, rfmzu
+    where theta_v and Exner are the FP64 fields.
     """
     d = case.dims
     pts = (d.jx - 1) * (d.iy - 1) * d.kz
     inner = (d.jx - 3) * (d.iy - 3) * d.kz
-    words = {
-        "sound_div": 7 * pts,
-        "sound_solve": 11 * inner,
-        "sound_momentum": 7 * pts,
-        "adv_vertical": (2 * nadv_fields + 3) * pts,
-        "adv_horizontal": (3 * nadv_fields + 4) * pts,
+    r, w = wbytes, 8
+    nd = 2                       # theta_v, Exner
+    nr = nadv_fields - nd        # fields of type R
+    by = {
+        "sound_div": 7 * r * pts,
+        "sound_solve": (4 * r + 7 * w) * inner,
+        "sound_momentum": (5 * r + 2 * w) * pts,
+        "adv_vertical": ((2 * nr + 3) * r + 2 * nd * w) * pts,
+        "adv_horizontal": ((3 * nr + 4) * r + 3 * nd * w) * pts,
     }.get(name)
-    return None if words is None else float(words) * wbytes
+    return None if by is None else float(by)
 
 
 def n_adv_fields(case) -> int:

@@ -203,23 +203,45 @@ void mlc_destroy(mlc_ctx *ctx);
 /* Text for a status code. */
 const char *mlc_strerror(int status);
 
-/* ---- ensembles: several domains of the same extents and parameters (the
- * members) advanced by the same kernel launches.  Member m's arrays sit at a
- * fixed stride from member 0's, so one launch per kernel stage serves every
- * member and one recorded graph replays the whole ensemble step.  Members
- * may differ in any field (terrain, state, boundary data) but share the
- * level set and dtbdys.  mlc_create is mlc_create_batch with nmem = 1 and the
- * single-domain calls address member 0.  No counterpart in the reference,
- * where an ensemble is a set of separate runs (Share/mod_ensemble.F90). */
+/* ---- ensembles, uneven batches and a serving pool: several domains (the
+ * members) advanced by the same kernel launches.  Each member owns its
+ * arena and is described to the kernels by one entry of a device table;
+ * every kernel stage is one launch whose grid covers the largest member, so
+ * one recorded graph replays the step of all members.  Members share the
+ * parameters (dt, substeps, options, precision) and may differ in anything
+ * else: extents, levels, terrain, state, boundary data and boundary clock.
+ * A member's result does not depend on the other members (bit for bit).
+ * mlc_create is mlc_create_batch with nmem = 1 and the single-domain calls
+ * address member 0.  No counterpart in the reference, where an ensemble is
+ * a set of separate runs (Share/mod_ensemble.F90). */
 int mlc_create_batch(const mlc_dims *dims, const mlc_params *params, int nmem, mlc_ctx **out);
+/* nmem members with extents dims[0..nmem-1]. */
+int mlc_create_multi(const mlc_dims *dims, const mlc_params *params, int nmem, mlc_ctx **out);
+/* Member slots of the context (the size of the diagnostics array). */
 int mlc_members(const mlc_ctx *ctx);
 int mlc_member_bind_static(mlc_ctx *ctx, int m, const mlc_static_ptrs *s);
 int mlc_member_upload_state(mlc_ctx *ctx, int m, const mlc_state_ptrs *st);
 int mlc_member_download_state(mlc_ctx *ctx, int m, const mlc_state_ptrs *st);
 int mlc_member_set_boundary(mlc_ctx *ctx, int m, const mlc_bdy_ptrs *b, double xbctime,
                             double dtbdys);
-/* nsteps steps of every member; out (optional) receives nmem diagnostics. */
+/* nsteps steps of every active member; out (optional) receives one entry per
+ * slot (steps_done = 0 for empty slots). */
 int mlc_step_batch(mlc_ctx *ctx, int nsteps, mlc_diag *out);
+
+/* Serving pool: a context of `capacity` empty slots whose members join and
+ * leave between steps (continuous batching).  A join allocates the member's
+ * arena from the context's stream-ordered pool; it is refused with
+ * MLC_ERR_BUDGET when the bytes held by all members would exceed
+ * budget_bytes (0: no bound) and with MLC_ERR_BUDGET when no slot is free.
+ * A joined member needs bind_static, upload_state and (with boundaries)
+ * set_boundary before the next step. */
+int mlc_create_pool(const mlc_params *params, int capacity, size_t budget_bytes, mlc_ctx **out);
+int mlc_pool_add(mlc_ctx *ctx, const mlc_dims *dims, int *slot);
+int mlc_pool_remove(mlc_ctx *ctx, int slot);
+/* Device bytes held by the members' arenas. */
+size_t mlc_pool_bytes(const mlc_ctx *ctx);
+/* Exact arena bytes of one member with these extents and parameters. */
+size_t mlc_member_footprint(const mlc_dims *dims, const mlc_params *params);
 
 /* Launch shapes picked by mlc_autotune, and the per-step device time of the
  * tuned kernels against the fixed 32x8 configuration (column kernels and

@@ -42,6 +42,9 @@ class mlc_dims(C.Structure):
     _fields_ = [("jx", C.c_int32), ("iy", C.c_int32), ("kz", C.c_int32),
                 ("nqx", C.c_int32), ("ntr", C.c_int32)]
 
+    def as_tuple(self):
+        return (self.jx, self.iy, self.kz, self.nqx, self.ntr)
+
 
 class mlc_params(C.Structure):
     _fields_ = [("dtsec", C.c_double), ("dx", C.c_double), ("mo_ztop", C.c_double),
@@ -152,6 +155,12 @@ def _declare(lib):
         "mlc_launches_per_step": (C.c_int, [C.c_void_p]),
         "mlc_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
         "mlc_autotune": (C.c_int, [C.c_void_p, C.c_int, P(mlc_tune_report)]),
+        "mlc_create_multi": (C.c_int, [P(mlc_dims), P(mlc_params), C.c_int, P(C.c_void_p)]),
+        "mlc_create_pool": (C.c_int, [P(mlc_params), C.c_int, C.c_size_t, P(C.c_void_p)]),
+        "mlc_pool_add": (C.c_int, [C.c_void_p, P(mlc_dims), P(C.c_int)]),
+        "mlc_pool_remove": (C.c_int, [C.c_void_p, C.c_int]),
+        "mlc_pool_bytes": (C.c_size_t, [C.c_void_p]),
+        "mlc_member_footprint": (C.c_size_t, [P(mlc_dims), P(mlc_params)]),
     }
     for name, (res, args) in sigs.items():
         try:

@@ -323,18 +323,55 @@ def config0(nx=64, ny=64, kz=30, seed=0, **kw) -> Case:
                  theta_noise=0.1, tracer=True, name=f"c0_{nx}x{ny}x{kz}", **kw)
 
 
-def config1(nx=512, ny=512, kz=41, seed=1, **kw) -> Case:
-    """Moist convection-permitting: 512x512x41, dx 3 km, dt 20 s, 4 substeps,
-    3 seeded hills of 200-2000 m, qv at 70% RH, a qc patch, u jet 15 sin(y)."""
-    dx = 3000.0
+def _moist(nx, ny, kz, seed, dx, dt, nsound, name, **kw) -> Case:
     r = splitmix64(seed * 104729 + 11, 9)
     hills = []
     for h in range(3):
         cx = (0.2 + 0.6 * r[3 * h]) * nx * dx
         cy = (0.2 + 0.6 * r[3 * h + 1]) * ny * dx
         hills.append((cx, cy, 200.0 + 1800.0 * r[3 * h + 2]))
-    return build(nx, ny, kz, dx=dx, dt=20.0, nsound=4, moist=True, seed=seed, hills=hills,
-                 jet=True, theta_noise=0.1, tracer=False, name=f"c1_{nx}x{ny}x{kz}", **kw)
+    return build(nx, ny, kz, dx=dx, dt=dt, nsound=nsound, moist=True, seed=seed, hills=hills,
+                 jet=True, theta_noise=0.1, tracer=False, name=name, **kw)
+
+
+def config1(nx=512, ny=512, kz=41, seed=1, **kw) -> Case:
+    """Moist convection-permitting: 512x512x41, dx 3 km, dt 20 s, 4 substeps,
+    3 seeded hills of 200-2000 m, qv at 70% RH, a qc patch, u jet 15 sin(y)."""
+    return _moist(nx, ny, kz, seed, 3000.0, 20.0, 4, f"c1_{nx}x{ny}x{kz}", **kw)
+
+
+def log_uniform_int(u: float, lo: int, hi: int) -> int:
+    return int(round(math.exp(math.log(lo) + u * (math.log(hi) - math.log(lo)))))
+
+
+def config3_dims(m: int):
+    """Extents of uneven-batch domain m: nx, ny log-uniform in 48-384
+    (independently), kz from {23, 30, 41}."""
+    r = splitmix64(3000 + m, 3)
+    nx = log_uniform_int(float(r[0]), 48, 384)
+    ny = log_uniform_int(float(r[1]), 48, 384)
+    kz = (23, 30, 41)[min(2, int(r[2] * 3))]
+    return nx, ny, kz
+
+
+def config3_member(m: int, scale: float = 1.0, **kw) -> Case:
+    """Uneven-batch domain m: the moist recipe at dx 12 km, dt 60 s, 3
+    substeps with its own seed; `scale` shrinks the horizontal extents (for
+    tests) with a floor of 24 cells."""
+    nx, ny, kz = config3_dims(m)
+    nx = max(24, int(round(nx * scale)))
+    ny = max(24, int(round(ny * scale)))
+    return _moist(nx, ny, kz, 3000 + m, 12000.0, 60.0, 3, f"c3_m{m}_{nx}x{ny}x{kz}", **kw)
+
+
+def config4_request(r: int, scale: float = 1.0, **kw):
+    """Serving request r: (case, steps).  nx = ny log-uniform in 32-512,
+    kz 30, steps uniform in 6-240, the moist recipe of the 3 km domain with
+    the request's seed; `scale` shrinks the extents (floor 24 cells)."""
+    u = splitmix64(4000 + r, 2)
+    n = max(24, int(round(log_uniform_int(float(u[0]), 32, 512) * scale)))
+    steps = 6 + min(234, int(u[1] * 235))
+    return _moist(n, n, 30, 4000 + r, 3000.0, 20.0, 4, f"c4_r{r}_{n}", **kw), steps
 
 
 def config2_member(m: int, nx=128, ny=128, kz=30, **kw) -> Case:

@@ -65,13 +65,75 @@ __device__ __forceinline__ T waf_flux(T hvel, T is, T zamu, T a, T c, T num) {
   return hvel * ((a + c) - (is * den + (zamu - is) * B));
 }
 
+// The advected fields of a member, in the reference's order (tetav, pai,
+// ux, vx, wx, qv, qx(iqfrst:nqx) when ipptls > 0, trac; advection,
+// Main/mod_moloch.F90:781-807).  Table 0 holds the fields of type R: all of
+// them in FP64, all but theta_v and Exner in a mixed member, whose two FP64
+// fields form table 1.  cur is the field's current half, out the other.
 template <class R>
-__global__ void k_adv_prep(Geom g, const R *__restrict__ u, const R *__restrict__ v,
-                           const R *__restrict__ w, R *__restrict__ ux, R *__restrict__ vx,
-                           R *__restrict__ wx) {
-  const size_t mo = (size_t)blockIdx.z * g.mstride;
-  u = mshift(u, mo); v = mshift(v, mo); w = mshift(w, mo); ux = mshift(ux, mo); vx = mshift(vx, mo);
-  wx = mshift(wx, mo);
+__device__ __forceinline__ int n_table_r(const Dom<R> &D) {
+  const int nfix = sizeof(R) == sizeof(double) ? 2 : 0;
+  return nfix + 4 + (D.c.ipptls > 0 ? D.g.nqx - 1 : 0) + D.g.ntr;
+}
+
+template <class R>
+__device__ __forceinline__ void field_r(const Dom<R> &D, int f, int adv, const R *&cur, R *&out) {
+  if (sizeof(R) == sizeof(double)) {
+    if (f == 0) { cur = (const R *)D.tetav[adv]; out = (R *)D.tetav[adv ^ 1]; return; }
+    if (f == 1) { cur = (const R *)D.pai[adv]; out = (R *)D.pai[adv ^ 1]; return; }
+    f -= 2;
+  }
+  const size_t F = D.g.field3();
+  switch (f) {
+    case 0: cur = D.ux[adv]; out = D.ux[adv ^ 1]; return;
+    case 1: cur = D.vx[adv]; out = D.vx[adv ^ 1]; return;
+    case 2: cur = D.wx[adv]; out = D.wx[adv ^ 1]; return;
+    case 3: cur = D.qx[adv]; out = D.qx[adv ^ 1]; return;
+    default: break;
+  }
+  f -= 4;
+  const int nq = D.c.ipptls > 0 ? D.g.nqx - 1 : 0;
+  if (f < nq) {
+    cur = D.qx[adv] + (size_t)(f + 1) * F;
+    out = D.qx[adv ^ 1] + (size_t)(f + 1) * F;
+    return;
+  }
+  f -= nq;
+  cur = D.trac[adv] + (size_t)f * F;
+  out = D.trac[adv ^ 1] + (size_t)f * F;
+}
+
+// The field set `set` of a member: 0 = the R table, 1 = the FP64 table.
+template <class R, class T>
+__device__ __forceinline__ void field_t(const Dom<R> &D, int set, int f, int adv, const T *&cur,
+                                        T *&out, T *&wz) {
+  if constexpr (sizeof(T) == sizeof(R)) {
+    const R *c0;
+    R *o0;
+    field_r<R>(D, f, adv, c0, o0);
+    cur = (const T *)c0;
+    out = (T *)o0;
+    wz = (T *)D.wz[f];
+  } else {
+    (void)set;
+    cur = f == 0 ? D.tetav[adv] : D.pai[adv];
+    out = f == 0 ? D.tetav[adv ^ 1] : D.pai[adv ^ 1];
+    wz = D.wz_d[f];
+  }
+}
+
+template <class R>
+__global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
+  const R *__restrict__ u = D.u[uv];
+  const R *__restrict__ v = D.v[uv];
+  const R *__restrict__ w = D.w;
+  R *__restrict__ ux = D.ux[adv];
+  R *__restrict__ vx = D.vx[adv];
+  R *__restrict__ wx = D.wx[adv];
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
@@ -102,26 +164,35 @@ __global__ void k_adv_prep(Geom g, const R *__restrict__ u, const R *__restrict_
 // type of the winds and metric, T the type of the advected field and of the
 // arithmetic (T = R except for the FP64 Exner field of a mixed domain).
 template <class R, class T>
-__global__ void k_adv_vertical(Geom g, Scal c, Stat<R> sa, const R *__restrict__ s, AdvTable<T> t) {
+__global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set, int advoff) {
   extern __shared__ unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int nth = blockDim.x * blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const Dom<R> &D = doms[blockIdx.z / nf];
+  if (!D.active) return;
+  const int f = blockIdx.z % nf;
+  if (set == 0 && f >= n_table_r(D)) return;  // a member with fewer species
+  const Geom g = D.g;
   const int kz = g.kz;
   T *col = smem;                                 // field column, levels 1..kz
   T *flx = smem + (size_t)(kz + 2) * nth;        // wfw, interfaces 1..kz+1
   T *sc = smem + (size_t)2 * (kz + 2) * nth;     // s, levels 1..kz+1
 #define COL(a, k) a[(size_t)(k) * nth + tid]
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const R *__restrict__ s = D.s;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const T *src;
+  T *outp, *dst;
+  field_t<R, T>(D, set, f, adv, src, outp, dst);
+  (void)outp;
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int f = blockIdx.z % t.n;
-  const size_t mo = (size_t)(blockIdx.z / t.n) * g.mstride;
-  rebase(sa, mo);
-  s = mshift(s, mo);
   if (j > g.jx - 1 || i > g.iy - 1) return;
   const size_t ij = g.at2(j, i), PS = g.PS;
   const T dtrdz = T(0.5) * (T(c.dtstepa) * T(c.rdzita));
-  const T *src = mshift(t.cur[f], mo);
+
   for (int k = 1; k <= kz; ++k) COL(col, k) = src[ij + (size_t)(k - 1) * PS];
   for (int k = 1; k <= kz + 1; ++k) COL(sc, k) = T(s[ij + (size_t)(k - 1) * PS]);
   for (int pass = 0; pass < 2; ++pass) {
@@ -151,36 +222,46 @@ __global__ void k_adv_vertical(Geom g, Scal c, Stat<R> sa, const R *__restrict__
       COL(col, k) = pk - COL(flx, k) * zrfmu + COL(flx, k + 1) * zrfmd + zdv;
     }
   }
-  T *dst = mshift(t.wz[f], mo);
+
   for (int k = 1; k <= kz; ++k) dst[ij + (size_t)(k - 1) * PS] = COL(col, k);
 #undef COL
 }
 
 // Meridional then zonal WAF for one tile (:984-1038; ROTLLR :926-983).
 template <class R, class T, int kTJ, int kTI>
-__global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Stat<R> sa,
-                                                            const R *__restrict__ u,
-                                                            const R *__restrict__ v, AdvTable<T> t) {
+__global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__restrict__ doms,
+                                                            int nf, int kzmax, int set, int uvoff,
+                                                            int advoff) {
   constexpr int WJ = kTJ + 4;  // columns J0-2 .. J0+TJ+1
   __shared__ T wz_s[kTI + 4][WJ];      // rows I0-2 .. I0+TI+1
   __shared__ T zpby_s[kTI + 1][WJ];    // rows I0 .. I0+TI
   __shared__ T p0_s[kTI][WJ];          // rows I0 .. I0+TI-1
   __shared__ T zpbw_s[kTI][kTJ + 1];   // columns J0 .. J0+TJ
-  const int jx = g.jx, iy = g.iy, kz = g.kz;
-  const int nf = t.n;
+  const Dom<R> &D = doms[blockIdx.z / (nf * kzmax)];
+  if (!D.active) return;
   const int f = blockIdx.z % nf;
-  const int k = (blockIdx.z / nf) % kz + 1;
-  const size_t mo = (size_t)(blockIdx.z / (nf * kz)) * g.mstride;
-  rebase(sa, mo);
-  u = mshift(u, mo);
-  v = mshift(v, mo);
+  if (set == 0 && f >= n_table_r(D)) return;
+  const int k = (blockIdx.z / nf) % kzmax + 1;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  if (k > kz) return;
+  const int J0c = blockIdx.x * kTJ + 1, I0c = blockIdx.y * kTI + 1;
+  if (J0c > jx - 1 || I0c > iy - 1) return;
+  const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
+  const R *__restrict__ u = D.u[uv];
+  const R *__restrict__ v = D.v[uv];
+  const T *cur0;
+  T *out0, *wz0;
+  field_t<R, T>(D, set, f, adv, cur0, out0, wz0);
   const int J0 = blockIdx.x * kTJ + 1, I0 = blockIdx.y * kTI + 1;
   const int tid = threadIdx.y * kTJ + threadIdx.x;
   const int nth = kTJ * kTI;
   const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
-  const T *pp = mshift(t.cur[f], mo) + ko;
-  const T *wz = mshift(t.wz[f], mo) + ko;
-  T *out = mshift(t.out[f], mo) + ko;
+  const T *pp = cur0 + ko;
+  const T *wz = wz0 + ko;
+  T *out = out0 + ko;
   const R *uk = u + ko;
   const R *vk = v + ko;
   const T dta = T(c.dtstepa);
@@ -297,13 +378,36 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(Geom g, Scal c, Sta
   }
 }
 
+// Species that are not advected (ipptls = 0: qx(iqfrst:nqx)) keep their
+// values when the advected fields move to the other half of their pairs.
+template <class R>
+__global__ void k_species_copy(const Dom<R> *__restrict__ doms, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (D.c.ipptls > 0 || j > g.jx - 1 || i > g.iy - 1) return;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const size_t F = g.field3(), ij = g.at2(j, i);
+  for (int n = 1; n < g.nqx; ++n)
+    for (int k = 1; k <= g.kz; ++k) {
+      const size_t o = ij + (size_t)(k - 1) * g.PS + (size_t)n * F;
+      D.qx[adv ^ 1][o] = D.qx[adv][o];
+    }
+}
+
 // :809-825
 template <class R>
-__global__ void k_adv_curvature(Geom g, Scal c, Stat<R> sa, R *__restrict__ ux, R *__restrict__ vx) {
-  const size_t mo = (size_t)blockIdx.z * g.mstride;
-  rebase(sa, mo);
-  ux = mshift(ux, mo);
-  vx = mshift(vx, mo);
+__global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active || !D.c.curvature) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  R *__restrict__ ux = D.ux[adv];
+  R *__restrict__ vx = D.vx[adv];
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (j > g.jx - 2 || i > g.iy - 2) return;
@@ -330,12 +434,17 @@ __global__ void k_adv_curvature(Geom g, Scal c, Stat<R> sa, R *__restrict__ ux, 
 
 // uvxtouvstag :1477-1522 and htozstag :1461-1475
 template <class R>
-__global__ void k_adv_back(Geom g, const R *__restrict__ ux, const R *__restrict__ vx,
-                           const R *__restrict__ wx, R *__restrict__ u, R *__restrict__ v,
-                           R *__restrict__ w) {
-  const size_t mo = (size_t)blockIdx.z * g.mstride;
-  ux = mshift(ux, mo); vx = mshift(vx, mo); wx = mshift(wx, mo);
-  u = mshift(u, mo); v = mshift(v, mo); w = mshift(w, mo);
+__global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
+  const R *__restrict__ ux = D.ux[adv];
+  const R *__restrict__ vx = D.vx[adv];
+  const R *__restrict__ wx = D.wx[adv];
+  R *__restrict__ u = D.u[uv];
+  R *__restrict__ v = D.v[uv];
+  R *__restrict__ w = D.w;
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
@@ -377,75 +486,69 @@ inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
 }  // namespace
 
 template <class R>
-void Launch<R>::adv_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
-  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
-  k_adv_prep<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, st.u, st.v, st.w, st.ux, st.vx, wk.wx);
+void Launch<R>::adv_prep(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  k_adv_prep<R><<<grid2(L.jx - 1, L.iy - 1, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R, class T>
-void launch_vertical(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
-                     const AdvTable<T> &t, cudaStream_t s) {
-  const dim3 b((unsigned)g.vert_x, (unsigned)g.vert_y);
-  const size_t smem = (size_t)3 * (g.kz + 2) * b.x * b.y * sizeof(T);
-  dim3 grd = grid2(g.jx - 1, g.iy - 1, b, 1);
-  grd.z = (unsigned)(t.n * g.nmem);
-  k_adv_vertical<R, T><<<grd, b, smem, s>>>(g, c, sa, wk.s, t);
+void launch_vertical(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int advoff,
+                     cudaStream_t s) {
+  const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
+  const size_t smem = (size_t)3 * (L.kz + 2) * b.x * b.y * sizeof(T);
+  dim3 grd = grid2(L.jx - 1, L.iy - 1, b, 1);
+  grd.z = (unsigned)(nf * L.nmem);
+  k_adv_vertical<R, T><<<grd, b, smem, s>>>(d, nf, set, advoff);
 }
 
 template <class R, class T, int TJ, int TI>
-void launch_tile(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                 const AdvTable<T> &t, cudaStream_t s) {
-  dim3 grd((unsigned)((g.jx - 1 + TJ - 1) / TJ), (unsigned)((g.iy - 1 + TI - 1) / TI),
-           (unsigned)(t.n * g.kz * g.nmem));
-  k_adv_horizontal<R, T, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(g, c, sa, st.u, st.v, t);
+void launch_tile(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int uvoff, int advoff,
+                 cudaStream_t s) {
+  dim3 grd((unsigned)((L.jx - 1 + TJ - 1) / TJ), (unsigned)((L.iy - 1 + TI - 1) / TI),
+           (unsigned)(nf * L.kz * L.nmem));
+  k_adv_horizontal<R, T, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(d, nf, L.kz, set, uvoff, advoff);
 }
 
 template <class R, class T>
-void launch_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                       const AdvTable<T> &t, cudaStream_t s) {
-  switch (g.htile) {
-    case 1: launch_tile<R, T, 32, 4>(g, c, sa, st, t, s); break;
-    case 2: launch_tile<R, T, 64, 4>(g, c, sa, st, t, s); break;
-    case 3: launch_tile<R, T, 16, 8>(g, c, sa, st, t, s); break;
-    default: launch_tile<R, T, 32, 8>(g, c, sa, st, t, s); break;
+void launch_horizontal(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int uvoff,
+                       int advoff, cudaStream_t s) {
+  switch (L.htile) {
+    case 1: launch_tile<R, T, 32, 4>(L, d, nf, set, uvoff, advoff, s); break;
+    case 2: launch_tile<R, T, 64, 4>(L, d, nf, set, uvoff, advoff, s); break;
+    case 3: launch_tile<R, T, 16, 8>(L, d, nf, set, uvoff, advoff, s); break;
+    default: launch_tile<R, T, 32, 8>(L, d, nf, set, uvoff, advoff, s); break;
   }
 }
 
 template <class R>
-void Launch<R>::adv_vertical(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
-                             const AdvTable<R> &t, cudaStream_t s) {
-  launch_vertical<R, R>(g, c, sa, wk, t, s);
+void Launch<R>::adv_vertical(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
+  launch_vertical<R, R>(L, d, L.nadv_r, 0, advoff, s);
+  if (L.nadv_d) launch_vertical<R, double>(L, d, L.nadv_d, 1, advoff, s);
 }
 
 template <class R>
-void Launch<R>::adv_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                               const AdvTable<R> &t, cudaStream_t s) {
-  launch_horizontal<R, R>(g, c, sa, st, t, s);
+void Launch<R>::adv_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                               cudaStream_t s) {
+  launch_horizontal<R, R>(L, d, L.nadv_r, 0, uvoff, advoff, s);
+  if (L.nadv_d) launch_horizontal<R, double>(L, d, L.nadv_d, 1, uvoff, advoff, s);
 }
 
 template <class R>
-void Launch<R>::adv_vertical_f64(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
-                                 const AdvTable<double> &t, cudaStream_t s) {
-  launch_vertical<R, double>(g, c, sa, wk, t, s);
+void Launch<R>::adv_species_copy(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  k_species_copy<R><<<grid2(L.jx - 1, L.iy - 1, b, L.nmem), b, 0, s>>>(d, advoff);
 }
 
 template <class R>
-void Launch<R>::adv_horizontal_f64(const Geom &g, const Scal &c, const Stat<R> &sa,
-                                   const State<R> &st, const AdvTable<double> &t, cudaStream_t s) {
-  launch_horizontal<R, double>(g, c, sa, st, t, s);
+void Launch<R>::adv_curvature(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  k_adv_curvature<R><<<grid2(L.jx - 3, L.iy - 3, b, L.nmem), b, 0, s>>>(d, advoff);
 }
 
 template <class R>
-void Launch<R>::adv_curvature(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                              cudaStream_t s) {
-  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
-  k_adv_curvature<R><<<grid2(g.jx - 3, g.iy - 3, b, g.nmem), b, 0, s>>>(g, c, sa, st.ux, st.vx);
-}
-
-template <class R>
-void Launch<R>::adv_back(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
-  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
-  k_adv_back<R><<<grid2(g.jx, g.iy, b, g.nmem), b, 0, s>>>(g, st.ux, st.vx, wk.wx, st.u, st.v, st.w);
+void Launch<R>::adv_back(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  k_adv_back<R><<<grid2(L.jx, L.iy, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R>

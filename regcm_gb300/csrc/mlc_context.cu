@@ -1,16 +1,21 @@
-// mlc_context.cu -- the C ABI of moloch_gb300.h: one context per domain.
+// mlc_context.cu -- the C ABI of moloch_gb300.h.
 //
-// A context owns one CUDA stream and one device arena (a single cudaMalloc
-// carved into 256-byte aligned arrays), holds the domain's static fields,
-// state, boundary data and scratch in the padded layout of mlc_device.cuh,
-// and steps it with the kernels of mlc_sound.cu, mlc_advect.cu and
-// mlc_end.cu.  A step is recorded once into a CUDA graph per buffer
-// arrangement (the acoustic and advection ping-pong pairs alternate between
-// at most two arrangements) and replayed; the boundary clock and the
-// diagnostics stay on the device so replays need no host work.
+// A context owns one CUDA stream, a stream-ordered memory pool and a table of
+// member slots.  A member is one domain: one allocation (its arena) carved
+// into 256-byte aligned arrays that hold its static fields, state, boundary
+// data and scratch in the padded layout of mlc_device.cuh.  The kernels of
+// mlc_sound.cu, mlc_advect.cu and mlc_end.cu read a device table with one
+// descriptor Dom<R> per active member, so each kernel stage is one launch for
+// all members whatever their extents.  The boundary clocks, diagnostics and
+// ping-pong buffer roles stay on the device (the last kernel of a step
+// advances them), so one recorded CUDA graph replays every step; it is
+// recorded again only when the launch geometry changes (members joining or
+// leaving, new launch shapes).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -26,6 +31,7 @@ namespace {
 
 constexpr size_t kAlign = 256;
 constexpr int kMaxLevels = 128;
+constexpr int kMaxSlots = 4096;
 
 size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
@@ -41,37 +47,15 @@ struct Carver {
   }
 };
 
-template <class R>
-struct Arrays {
-  State<R> st{};
-  // second halves of the ping-pong pairs
-  R *u2, *v2, *ux2, *vx2, *qx2, *trac2, *wx2;
-  double *pai2, *tetav2;
-  R *wz[kMaxAdv];
-  double *wz_pai, *wz_tet;  // wz of the FP64 fields of a mixed domain
-  Work<R> wk{};
-  Stat<R> sa{};
-  Bdy<R> bd{};
-  // writable views of the static arrays
-  R *fmz, *fmzf, *rfmzu, *rfmzv, *zrfmu, *zrfmd, *hx, *hy, *msfu, *msfv, *msfx, *mx2, *rmu, *rmv,
-      *coru, *corv;
-  double *fmz_d, *fmzf_d;
-  double *zeta, *dz, *hefc, *fcx, *tnudge, *ffilt, *gzitakh, *xkdamp, *xknu, *gzitak, *rlat;
-  int32_t *ibnd_cr, *ibnd_ud, *ibnd_vd;
-  R *bfield[2][8];  // xtb, xqb, (unused), xlb, xib, dub, dvb, chib
-  double *xpaib[2], *xpsb[2];
-  double *staging;
-  size_t staging_elems;
-  double *partials;
-  Clock *clk;
-  DiagDev *diag;
-};
+template <class T>
+T *W(const T *p) { return const_cast<T *>(p); }
 
-int n_advected(const mlc_dims &d, const mlc_params &p) {
-  // tetav, pai, ux, vx, wx, qv, qx(iqfrst:nqx) when ipptls > 0, trac
-  return 6 + (p.ipptls > 0 ? d.nqx - 1 : 0) + d.ntr;
+// Advected fields of type R per member (the table order of mlc_advect.cu).
+int n_table_r(const mlc_dims &d, const mlc_params &p, bool f64) {
+  return (f64 ? 2 : 0) + 4 + (p.ipptls > 0 ? d.nqx - 1 : 0) + d.ntr;
 }
 
+// Doubles of the packed state of one domain (the staging buffer's size).
 size_t state_elems(const mlc_dims &d) {
   const size_t c2 = (size_t)(d.jx - 1) * (d.iy - 1);
   const size_t u3 = (size_t)d.jx * (d.iy - 1) * d.kz, v3 = (size_t)(d.jx - 1) * d.iy * d.kz;
@@ -79,152 +63,123 @@ size_t state_elems(const mlc_dims &d) {
   return u3 + v3 + c2 * (d.kz + 1) + c3 * (9 + d.nqx + d.ntr) + c2;
 }
 
-template <class R>
-void carve(Carver &cv, Arrays<R> &a, const Geom &g, const mlc_dims &d, const mlc_params &p) {
-  const size_t F = g.field3(), F1 = g.PS * (size_t)(g.kz + 1), P2 = g.PS;
-  State<R> &st = a.st;
-  st.u = cv.take<R>(F); st.v = cv.take<R>(F); st.w = cv.take<R>(F1);
-  st.pai = cv.take<double>(F); st.tetav = cv.take<double>(F); st.t = cv.take<R>(F);
-  st.tvirt = cv.take<R>(F); st.ux = cv.take<R>(F); st.vx = cv.take<R>(F);
-  st.p = cv.take<R>(F); st.rho = cv.take<R>(F); st.qsat = cv.take<R>(F);
-  st.qx = cv.take<R>(F * d.nqx);
-  st.trac = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;
-  st.ps = cv.take<double>(P2);
-  a.u2 = cv.take<R>(F); a.v2 = cv.take<R>(F); a.tetav2 = cv.take<double>(F); a.pai2 = cv.take<double>(F);
-  a.ux2 = cv.take<R>(F); a.vx2 = cv.take<R>(F); a.qx2 = cv.take<R>(F * d.nqx);
-  a.trac2 = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;
-  a.wx2 = cv.take<R>(F);
-  const int nadv = n_advected(d, p);
-  for (int f = 0; f < kMaxAdv; ++f) a.wz[f] = f < nadv ? cv.take<R>(F) : nullptr;
-  a.wz_pai = sizeof(R) == sizeof(double) ? nullptr : cv.take<double>(F);
-  a.wz_tet = sizeof(R) == sizeof(double) ? nullptr : cv.take<double>(F);
-  a.wk.s = cv.take<R>(F1); a.wk.zdiv2 = cv.take<R>(F); a.wk.tetavf = cv.take<double>(F1);
-  a.wk.wx = cv.take<R>(F);
-  a.fmz = cv.take<R>(F); a.fmzf = cv.take<R>(F1); a.rfmzu = cv.take<R>(F); a.rfmzv = cv.take<R>(F);
-  if (sizeof(R) == sizeof(double)) {
-    a.fmz_d = reinterpret_cast<double *>(a.fmz);
-    a.fmzf_d = reinterpret_cast<double *>(a.fmzf);
-  } else {
-    a.fmz_d = cv.take<double>(F);
-    a.fmzf_d = cv.take<double>(F1);
-  }
-  a.zrfmu = cv.take<R>(F); a.zrfmd = cv.take<R>(F);
-  a.zeta = cv.take<double>(F); a.dz = cv.take<double>(F);
-  a.hx = cv.take<R>(P2); a.hy = cv.take<R>(P2); a.msfu = cv.take<R>(P2); a.msfv = cv.take<R>(P2);
-  a.msfx = cv.take<R>(P2); a.mx2 = cv.take<R>(P2); a.rmu = cv.take<R>(P2); a.rmv = cv.take<R>(P2);
-  a.coru = cv.take<R>(P2); a.corv = cv.take<R>(P2);
-  a.ibnd_cr = cv.take<int32_t>(P2); a.ibnd_ud = cv.take<int32_t>(P2); a.ibnd_vd = cv.take<int32_t>(P2);
-  a.hefc = cv.take<double>((size_t)p.nspgx * d.kz); a.fcx = cv.take<double>(p.nspgx);
-  a.tnudge = cv.take<double>(d.kz); a.ffilt = cv.take<double>(d.kz); a.gzitakh = cv.take<double>(d.kz);
-  a.xkdamp = cv.take<double>(d.kz); a.xknu = cv.take<double>(d.kz); a.gzitak = cv.take<double>(d.kz + 1);
-  a.rlat = cv.take<double>(d.iy);
-  const bool moist_b = p.present_qc || p.present_qi;
-  for (int b = 0; b < 2; ++b) {
-    a.bfield[b][0] = cv.take<R>(F);                                   // xtb
-    a.bfield[b][1] = cv.take<R>(F);                                   // xqb
-    a.bfield[b][2] = nullptr;
-    a.xpaib[b] = cv.take<double>(F);
-    a.bfield[b][3] = (moist_b && p.present_qc) ? cv.take<R>(F) : nullptr;  // xlb
-    a.bfield[b][4] = (moist_b && p.present_qi) ? cv.take<R>(F) : nullptr;  // xib
-    a.bfield[b][5] = cv.take<R>(F);                                   // dub
-    a.bfield[b][6] = cv.take<R>(F);                                   // dvb
-    a.bfield[b][7] = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;         // chib
-    a.xpsb[b] = cv.take<double>(P2);
-  }
-  a.staging = nullptr;  // one staging buffer per context, outside the member arenas
-  a.staging_elems = state_elems(d);
-  a.partials = cv.take<double>((size_t)reduce_blocks(g) * 8);
-  a.clk = cv.take<Clock>(1);
-  a.diag = cv.take<DiagDev>(1);
-}
-
-template <class R>
-void bind_views(Arrays<R> &a) {
-  Stat<R> &s = a.sa;
-  s.fmz = a.fmz; s.fmzf = a.fmzf; s.rfmzu = a.rfmzu; s.rfmzv = a.rfmzv;
-  s.fmz_d = a.fmz_d; s.fmzf_d = a.fmzf_d;
-  s.zrfmu = a.zrfmu; s.zrfmd = a.zrfmd; s.zeta = a.zeta; s.dz = a.dz;
-  s.hx = a.hx; s.hy = a.hy; s.msfu = a.msfu; s.msfv = a.msfv; s.msfx = a.msfx; s.mx2 = a.mx2;
-  s.rmu = a.rmu; s.rmv = a.rmv; s.coru = a.coru; s.corv = a.corv;
-  s.ibnd_cr = a.ibnd_cr; s.ibnd_ud = a.ibnd_ud; s.ibnd_vd = a.ibnd_vd;
-  s.hefc = a.hefc; s.fcx = a.fcx; s.tnudge = a.tnudge; s.ffilt = a.ffilt; s.gzitakh = a.gzitakh;
-  s.xkdamp = a.xkdamp; s.xknu = a.xknu; s.gzitak = a.gzitak; s.rlat = a.rlat;
-  for (int b = 0; b < 2; ++b) {
-    a.bd.xtb[b] = a.bfield[b][0]; a.bd.xqb[b] = a.bfield[b][1]; a.bd.xpaib[b] = a.xpaib[b];
-    a.bd.xlb[b] = a.bfield[b][3]; a.bd.xib[b] = a.bfield[b][4]; a.bd.dub[b] = a.bfield[b][5];
-    a.bd.dvb[b] = a.bfield[b][6]; a.bd.chib[b] = a.bfield[b][7]; a.bd.xpsb[b] = a.xpsb[b];
-  }
-}
-
 Geom make_geom(const mlc_dims &d, int elem_bytes) {
   Geom g{};
   g.jx = d.jx; g.iy = d.iy; g.kz = d.kz; g.nqx = d.nqx; g.ntr = d.ntr;
-  g.nmem = 1;
-  g.col_x = 32; g.col_y = 4;
-  g.solve_x = 32; g.solve_y = 2;
-  g.vert_x = 32; g.vert_y = 2;
-  g.htile = 0;
   const int per_line = 128 / elem_bytes;
   g.P = (d.jx + per_line - 1) / per_line * per_line;
   g.PS = (size_t)g.P * d.iy;
   return g;
 }
 
-int validate(const mlc_dims *d, const mlc_params *p) {
-  if (!d || !p) return MLC_ERR_INVALID;
-  if (d->jx < 10 || d->iy < 10 || d->kz < 4 || d->kz > kMaxLevels) return MLC_ERR_INVALID;
-  if (d->nqx < 2 || d->nqx > 10 || d->ntr < 0 || d->ntr > 8) return MLC_ERR_INVALID;
+Scal make_scal(const mlc_params &p) {
+  Scal c{};
+  c.dx = p.dx;
+  c.rdx = 1.0 / p.dx;
+  c.dtsec = p.dtsec;
+  c.dt = p.dtsec;
+  c.dtstepa = p.dtsec / (double)p.mo_nadv;
+  c.dtsound = c.dtstepa / (double)p.mo_nsound;
+  c.dtbdys = p.dtbdys;
+  c.rtb = 1.0 / p.dtbdys;
+  c.nadv = p.mo_nadv;
+  c.nsound = p.mo_nsound;
+  c.divdamp = p.mo_divdamp;
+  c.divfilter = p.mo_divfilter;
+  c.top_nudge = p.mo_top_nudge;
+  c.apply_bdy = p.do_apply_bdy;
+  c.lrotllr = p.lrotllr;
+  c.ipptls = p.ipptls;
+  c.present_qc = p.present_qc;
+  c.present_qi = p.present_qi;
+  c.nspgx = p.nspgx;
+  c.nztop = p.mo_top_nudge ? p.nztop : 0;
+  c.debug_level = p.debug_level;
+  return c;
+}
+
+// Lay out one member's arrays.  Both halves of every ping-pong pair, one wz
+// scratch field per advected field, the FP64 copies of the vertical metric
+// for the solve of a mixed member, boundary pairs b0/b1 and the reduction
+// partials.
+template <class R>
+void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const mlc_params &p) {
+  const bool f64 = sizeof(R) == sizeof(double);
+  const size_t F = g.field3(), F1 = g.PS * (size_t)(g.kz + 1), P2 = g.PS;
+  for (int h = 0; h < 2; ++h) {
+    D.u[h] = cv.take<R>(F); D.v[h] = cv.take<R>(F);
+    D.ux[h] = cv.take<R>(F); D.vx[h] = cv.take<R>(F); D.wx[h] = cv.take<R>(F);
+    D.qx[h] = cv.take<R>(F * d.nqx);
+    D.trac[h] = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;
+    D.pai[h] = cv.take<double>(F); D.tetav[h] = cv.take<double>(F);
+  }
+  D.w = cv.take<R>(F1); D.t = cv.take<R>(F); D.tvirt = cv.take<R>(F); D.p = cv.take<R>(F);
+  D.rho = cv.take<R>(F); D.qsat = cv.take<R>(F); D.ps = cv.take<double>(P2);
+  D.s = cv.take<R>(F1); D.zdiv2 = cv.take<R>(F); D.tetavf = cv.take<double>(F1);
+  const int nr = n_table_r(d, p, f64);
+  for (int f = 0; f < kMaxFields; ++f) D.wz[f] = f < nr ? cv.take<R>(F) : nullptr;
+  for (int f = 0; f < 2; ++f) D.wz_d[f] = f64 ? nullptr : cv.take<double>(F);
+  Stat<R> &s = D.sa;
+  s.fmz = cv.take<R>(F); s.fmzf = cv.take<R>(F1); s.rfmzu = cv.take<R>(F); s.rfmzv = cv.take<R>(F);
+  if (f64) {
+    s.fmz_d = reinterpret_cast<const double *>(s.fmz);
+    s.fmzf_d = reinterpret_cast<const double *>(s.fmzf);
+  } else {
+    s.fmz_d = cv.take<double>(F);
+    s.fmzf_d = cv.take<double>(F1);
+  }
+  s.zrfmu = cv.take<R>(F); s.zrfmd = cv.take<R>(F);
+  s.zeta = cv.take<double>(F); s.dz = cv.take<double>(F);
+  s.hx = cv.take<R>(P2); s.hy = cv.take<R>(P2); s.msfu = cv.take<R>(P2); s.msfv = cv.take<R>(P2);
+  s.msfx = cv.take<R>(P2); s.mx2 = cv.take<R>(P2); s.rmu = cv.take<R>(P2); s.rmv = cv.take<R>(P2);
+  s.coru = cv.take<R>(P2); s.corv = cv.take<R>(P2);
+  s.ibnd_cr = cv.take<int32_t>(P2); s.ibnd_ud = cv.take<int32_t>(P2); s.ibnd_vd = cv.take<int32_t>(P2);
+  s.hefc = cv.take<double>((size_t)p.nspgx * d.kz); s.fcx = cv.take<double>(p.nspgx);
+  s.tnudge = cv.take<double>(d.kz); s.ffilt = cv.take<double>(d.kz); s.gzitakh = cv.take<double>(d.kz);
+  s.xkdamp = cv.take<double>(d.kz); s.xknu = cv.take<double>(d.kz); s.gzitak = cv.take<double>(d.kz + 1);
+  s.rlat = cv.take<double>(d.iy);
+  Bdy<R> &b = D.bd;
+  for (int h = 0; h < 2; ++h) {
+    b.xtb[h] = cv.take<R>(F); b.xqb[h] = cv.take<R>(F); b.xpaib[h] = cv.take<double>(F);
+    b.xlb[h] = p.present_qc ? cv.take<R>(F) : nullptr;
+    b.xib[h] = p.present_qi ? cv.take<R>(F) : nullptr;
+    b.dub[h] = cv.take<R>(F); b.dvb[h] = cv.take<R>(F);
+    b.chib[h] = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;
+    b.xpsb[h] = cv.take<double>(P2);
+  }
+  D.red_blocks = reduce_blocks(g);
+  D.rows_per_block = reduce_rows_per_block(g);
+  D.partials = cv.take<double>((size_t)D.red_blocks * 8);
+}
+
+template <class R>
+size_t arena_bytes(const mlc_dims &d, const mlc_params &p) {
+  Dom<R> D{};
+  Carver cv;
+  carve_dom<R>(cv, D, make_geom(d, (int)sizeof(R)), d, p);
+  return cv.off;
+}
+
+int validate_params(const mlc_params *p) {
+  if (!p) return MLC_ERR_INVALID;
   if (!(p->dtsec > 0) || !(p->dx > 0) || !(p->mo_ztop > 0) || p->mo_nadv < 1 || p->mo_nsound < 1)
     return MLC_ERR_INVALID;
   if (!(p->dtbdys > 0) || p->nspgx < 3 || p->nspgd < 3) return MLC_ERR_INVALID;
   if (p->ipptls < 0 || p->ipptls > 2) return MLC_ERR_UNSUPPORTED;
-  if (p->ipptls == 2 && d->nqx < 5) return MLC_ERR_INVALID;
   if (p->mo_spectral_nudge) return MLC_ERR_UNSUPPORTED;
   if (p->precision != MLC_PREC_FP64 && p->precision != MLC_PREC_MIXED) return MLC_ERR_INVALID;
-  if (n_advected(*d, *p) > kMaxAdv) return MLC_ERR_UNSUPPORTED;
-  // the tracer relaxation assumes disjoint south/north and west/east bands
-  if (d->ntr > 0 && (d->jx - 1 < 2 * p->nspgx || d->iy - 1 < 2 * p->nspgx)) return MLC_ERR_UNSUPPORTED;
   return MLC_OK;
 }
 
-}  // namespace
-
-struct mlc_ctx {
-  mlc_dims dims{};
-  mlc_params prm{};
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  Geom g{};
-  Scal c{};
-  void *arena = nullptr;
-  double *staging = nullptr;  // layout conversion buffer shared by all members
-  size_t arena_bytes = 0;   // all members
-  size_t member_bytes = 0;  // one member's arena (the member stride)
-  int nmem = 1;
-  Arrays<double> ad{};      // member 0's views (kernels rebase by member)
-  Arrays<float> af{};
-  std::vector<char> m_static, m_state, m_bdy;
-  bool have_static = false, have_state = false, have_bdy = false;
-  double rdzita_set = 0.0, dtbdys_set = 0.0;
-  int uv_role = 0;   // which buffer of the u/v pair is current
-  int adv_role = 0;  // which buffer of the advected pairs is current
-  cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
-  bool use_graphs = true;
-  int launches_per_step = 0;
-  double xbctime_host = 0.0;
-};
-
-namespace {
-
-// Views of member m's arrays (member 0's layout, m * member_bytes further).
-template <class R>
-Arrays<R> member_arrays(const mlc_ctx *x, int m) {
-  Arrays<R> a{};
-  Carver cv{static_cast<char *>(x->arena) + (size_t)m * x->member_bytes, 0};
-  carve<R>(cv, a, x->g, x->dims, x->prm);
-  bind_views<R>(a);
-  a.staging = x->staging;
-  return a;
+int validate_dims(const mlc_dims *d, const mlc_params *p) {
+  if (!d) return MLC_ERR_INVALID;
+  if (d->jx < 10 || d->iy < 10 || d->kz < 4 || d->kz > kMaxLevels) return MLC_ERR_INVALID;
+  if (d->nqx < 2 || d->nqx > 10 || d->ntr < 0 || d->ntr > 8) return MLC_ERR_INVALID;
+  if (p->ipptls == 2 && d->nqx < 5) return MLC_ERR_INVALID;
+  if (n_table_r(*d, *p, true) > kMaxFields) return MLC_ERR_UNSUPPORTED;
+  // the tracer relaxation assumes disjoint south/north and west/east bands
+  if (d->ntr > 0 && (d->jx - 1 < 2 * p->nspgx || d->iy - 1 < 2 * p->nspgx)) return MLC_ERR_UNSUPPORTED;
+  return MLC_OK;
 }
 
 int cuda_status(cudaError_t e) {
@@ -234,37 +189,175 @@ int cuda_status(cudaError_t e) {
   return MLC_ERR_CUDA;
 }
 
-#define MLC_TRY(x)                              \
-  do {                                          \
-    cudaError_t e_ = (x);                       \
+#define MLC_TRY(x)                                 \
+  do {                                             \
+    cudaError_t e_ = (x);                          \
     if (e_ != cudaSuccess) return cuda_status(e_); \
   } while (0)
 
-// Pointers of the current buffer arrangement.
-template <class R>
-struct Roles {
-  State<R> st;      // canonical state (current buffers)
-  R *u_alt, *v_alt;
-  R *ux_alt, *vx_alt, *qx_alt, *trac_alt, *wx_alt;
-  double *pai_alt, *tetav_alt;
+#define MLC_CHK(x)               \
+  do {                           \
+    int s_ = (x);                \
+    if (s_ != MLC_OK) return s_; \
+  } while (0)
+
+struct Member {
+  bool used = false;
+  mlc_dims dims{};
+  Geom g{};
+  Scal c{};
+  void *raw = nullptr;   // the allocation (returned to the pool on removal)
+  char *base = nullptr;  // 256-byte aligned start of the arena
+  size_t bytes = 0;      // arena bytes
+  Dom<double> dd{};      // descriptor of an FP64 member
+  Dom<float> df{};       // descriptor of a mixed member
+  bool have_static = false, have_state = false, have_bdy = false;
 };
 
-template <class R>
-Roles<R> roles_of(const Arrays<R> &a, int uv_role, int adv_role) {
-  Roles<R> r{};
-  r.st = a.st;
-  if (uv_role) { r.st.u = a.u2; r.st.v = a.v2; r.u_alt = a.st.u; r.v_alt = a.st.v; }
-  else { r.u_alt = a.u2; r.v_alt = a.v2; }
-  if (adv_role) {
-    r.st.tetav = a.tetav2; r.st.pai = a.pai2; r.st.ux = a.ux2; r.st.vx = a.vx2; r.st.qx = a.qx2;
-    r.st.trac = a.trac2;
-    r.tetav_alt = a.st.tetav; r.pai_alt = a.st.pai; r.ux_alt = a.st.ux; r.vx_alt = a.st.vx;
-    r.qx_alt = a.st.qx; r.trac_alt = a.st.trac;
-  } else {
-    r.tetav_alt = a.tetav2; r.pai_alt = a.pai2; r.ux_alt = a.ux2; r.vx_alt = a.vx2;
-    r.qx_alt = a.qx2; r.trac_alt = a.trac2;
+template <class R> Dom<R> &dom_of(Member &m);
+template <> Dom<double> &dom_of<double>(Member &m) { return m.dd; }
+template <> Dom<float> &dom_of<float>(Member &m) { return m.df; }
+
+// What a recorded step graph depends on besides the device table contents.
+struct GraphKey {
+  LaunchGeom L;
+  int any_copy;   // some member keeps non-advected species (ipptls = 0)
+  int any_curv;   // some member has non-zero curvature terms
+};
+
+}  // namespace
+
+struct mlc_ctx {
+  mlc_params prm{};
+  bool mixed = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;
+  std::vector<Member> mem;     // slots
+  Clock *clks = nullptr;       // device, one per slot
+  DiagDev *diags = nullptr;    // device, one per slot
+  void *table = nullptr;       // device descriptor table (active members in slot order)
+  double *staging = nullptr;   // layout conversion buffer shared by all members
+  size_t staging_elems = 0;
+  size_t budget = 0;           // bound on the bytes of all member arenas (0: none)
+  size_t in_use = 0;           // bytes of all member arenas
+  GraphKey key{};              // launch geometry and shapes of the next step
+  bool table_dirty = true;
+  cudaGraphExec_t graph = nullptr;
+  GraphKey graph_key{};        // what the recorded graph was recorded with
+  bool graph_valid = false;
+  bool use_graphs = true;
+  int launches_per_step = 0;
+};
+
+namespace {
+
+bool member_ok(const mlc_ctx *x, int m) {
+  return x && m >= 0 && m < (int)x->mem.size() && x->mem[m].used;
+}
+
+// Grow the shared staging buffer to hold the packed state of extents d.
+int ensure_staging(mlc_ctx *x, const mlc_dims &d) {
+  const size_t need = state_elems(d);
+  if (need <= x->staging_elems) return MLC_OK;
+  if (x->staging) MLC_TRY(cudaFreeAsync(x->staging, x->stream));
+  x->staging = nullptr;
+  x->staging_elems = 0;
+  void *p = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(&p, need * sizeof(double), x->pool, x->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return MLC_ERR_NOMEM;
   }
-  return r;
+  x->staging = static_cast<double *>(p);
+  x->staging_elems = need;
+  return MLC_OK;
+}
+
+// Give slot `slot` a member of extents d: allocate and zero its arena, reset
+// its clock and diagnostics.  Every array starts at zero: s and w at the ring
+// stay zero, as the reference's reset_tendencies and init_moloch leave them.
+int add_member(mlc_ctx *x, int slot, const mlc_dims &d) {
+  MLC_CHK(validate_dims(&d, &x->prm));
+  Member m{};
+  m.dims = d;
+  m.g = make_geom(d, x->mixed ? 4 : 8);
+  m.c = make_scal(x->prm);
+  m.bytes = x->mixed ? arena_bytes<float>(d, x->prm) : arena_bytes<double>(d, x->prm);
+  if (x->budget && x->in_use + m.bytes > x->budget) return MLC_ERR_BUDGET;
+  MLC_CHK(ensure_staging(x, d));
+  cudaError_t e = cudaMallocFromPoolAsync(&m.raw, m.bytes + kAlign, x->pool, x->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return MLC_ERR_NOMEM;
+  }
+  m.base = reinterpret_cast<char *>(align_up(reinterpret_cast<uintptr_t>(m.raw)));
+  Carver cv{m.base, 0};
+  if (x->mixed) carve_dom<float>(cv, m.df, m.g, d, x->prm);
+  else carve_dom<double>(cv, m.dd, m.g, d, x->prm);
+  MLC_TRY(cudaMemsetAsync(m.base, 0, m.bytes, x->stream));
+  MLC_TRY(cudaMemsetAsync(x->clks + slot, 0, sizeof(Clock), x->stream));
+  MLC_TRY(cudaMemsetAsync(x->diags + slot, 0, sizeof(DiagDev), x->stream));
+  MLC_TRY(cudaStreamSynchronize(x->stream));
+  m.used = true;
+  x->mem[slot] = m;
+  x->in_use += m.bytes;
+  x->table_dirty = true;
+  return MLC_OK;
+}
+
+int remove_member(mlc_ctx *x, int slot) {
+  Member &m = x->mem[slot];
+  // stream order puts the release after every step already enqueued
+  MLC_TRY(cudaFreeAsync(m.raw, x->stream));
+  x->in_use -= m.bytes;
+  m = Member{};
+  x->table_dirty = true;
+  return MLC_OK;
+}
+
+// Upload the descriptor table of the active members and derive the launch
+// geometry (maxima over the members; the launch shapes are kept).
+template <class R>
+int refresh(mlc_ctx *x) {
+  if (!x->table_dirty) return MLC_OK;
+  std::vector<Dom<R>> t;
+  t.reserve(x->mem.size());
+  GraphKey k = x->key;
+  LaunchGeom &L = k.L;
+  L.jx = L.iy = L.kz = 0;
+  L.nadv_r = 0;
+  L.nadv_d = x->mixed ? 2 : 0;
+  L.red_blocks = 0;
+  k.any_copy = 0;
+  k.any_curv = 0;
+  for (size_t slot = 0; slot < x->mem.size(); ++slot) {
+    Member &m = x->mem[slot];
+    if (!m.used) continue;
+    Dom<R> D = dom_of<R>(m);
+    D.g = m.g;
+    D.c = m.c;
+    D.clk = x->clks + slot;
+    D.diag = x->diags + slot;
+    D.active = 1;
+    t.push_back(D);
+    L.jx = std::max(L.jx, m.g.jx);
+    L.iy = std::max(L.iy, m.g.iy);
+    L.kz = std::max(L.kz, m.g.kz);
+    L.nadv_r = std::max(L.nadv_r, n_table_r(m.dims, x->prm, !x->mixed));
+    L.red_blocks = std::max(L.red_blocks, D.red_blocks);
+    if (x->prm.ipptls == 0 && m.dims.nqx > 1) k.any_copy = 1;
+    if (m.c.curvature) k.any_curv = 1;
+  }
+  L.nmem = (int)t.size();
+  if (!t.empty()) {
+    MLC_TRY(cudaMemcpyAsync(x->table, t.data(), t.size() * sizeof(Dom<R>), cudaMemcpyHostToDevice,
+                            x->stream));
+    MLC_TRY(cudaStreamSynchronize(x->stream));
+  }
+  x->key = k;
+  x->table_dirty = false;
+  return MLC_OK;
 }
 
 // Optional per-launch event recorder (eager steps only, never captured).
@@ -295,196 +388,182 @@ struct Recorder {
   }
 };
 
-#define REC(name, call) \
-  do {                  \
+#define REC(name, call)        \
+  do {                         \
     if (rec) rec->begin(name); \
-    call;               \
-    if (rec) rec->end(); \
+    call;                      \
+    if (rec) rec->end();       \
   } while (0)
 
-// Enqueue one model step (Main/mod_moloch.F90:312-446) on the context stream.
-// Returns the number of kernels launched; updates the roles it leaves.
+// Enqueue one model step (Main/mod_moloch.F90:312-446) of every active
+// member on the context stream; returns the number of kernels launched.
+// The offsets count the acoustic substeps (uvoff) and advection rounds
+// (advoff) since the step began; with the roles in each member's clock they
+// name the buffers every launch works on.
 template <class R>
-int enqueue_step(mlc_ctx *x, Arrays<R> &a, Recorder *rec = nullptr) {
-  using L = Launch<R>;
-  const Geom &g = x->g;
-  const Scal &c = x->c;
+int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
+  using K = Launch<R>;
+  const LaunchGeom &L = x->key.L;
+  const Dom<R> *d = static_cast<const Dom<R> *>(x->table);
   cudaStream_t s = x->stream;
+  const int nadv = x->prm.mo_nadv, nsound = x->prm.mo_nsound;
+  const int nv = L.nadv_d ? 2 : 1;  // FP64 theta_v/Exner launches of a mixed step
   int nl = 0;
-  const mlc_dims &d = x->dims;
-  const mlc_params &p = x->prm;
-  const size_t F = g.field3();
-  for (int nadv = 0; nadv < c.nadv; ++nadv) {
-    Roles<R> r = roles_of(a, x->uv_role, x->adv_role);
-    Work<R> wk = a.wk;
-    // ---- sound ----
-    REC("sound_prep", L::sound_prep(g, r.st, wk, s)); ++nl;
-    R *ucur = r.st.u, *vcur = r.st.v, *ualt = r.u_alt, *valt = r.v_alt;
-    for (int ns = 0; ns < c.nsound; ++ns) {
-      SoundBufs<R> b{ucur, vcur, ualt, valt};
-      State<R> st = r.st;
-      st.u = ucur; st.v = vcur;
-      REC("sound_div", L::sound_div(g, c, a.sa, st, wk, b, s)); ++nl;
-      REC("sound_solve", L::sound_solve(g, c, a.sa, st, wk, ns == c.nsound - 1, s)); ++nl;
-      REC("sound_momentum", L::sound_momentum(g, c, a.sa, st, wk, b, s)); ++nl;
-      std::swap(ucur, ualt);
-      std::swap(vcur, valt);
+  for (int r = 0; r < nadv; ++r) {
+    // ---- sound (Main/mod_moloch.F90:531-765) ----
+    REC("sound_prep", K::sound_prep(L, d, r, s)); ++nl;
+    for (int n = 0; n < nsound; ++n) {
+      const int uvoff = r * nsound + n;
+      REC("sound_div", K::sound_div(L, d, uvoff, s)); ++nl;
+      REC("sound_solve", K::sound_solve(L, d, uvoff, r, n == nsound - 1, s)); ++nl;
+      REC("sound_momentum", K::sound_momentum(L, d, uvoff, r, s)); ++nl;
     }
-    if (c.nsound & 1) x->uv_role ^= 1;
-    r.st.u = ucur; r.st.v = vcur;
-    // ---- advection ----
-    REC("adv_prep", L::adv_prep(g, r.st, wk, s)); ++nl;
-    AdvTable<R> t{};
-    AdvTable<double> tp{};  // the FP64 fields (theta_v, Exner) of a mixed domain
-    int n = 0;
-    auto add = [&](const R *cur, R *out) { t.cur[n] = cur; t.wz[n] = a.wz[n]; t.out[n] = out; ++n; };
-    if constexpr (sizeof(R) == sizeof(double)) {
-      add(reinterpret_cast<const R *>(r.st.tetav), reinterpret_cast<R *>(r.tetav_alt));
-      add(reinterpret_cast<const R *>(r.st.pai), reinterpret_cast<R *>(r.pai_alt));
-    } else {
-      tp.cur[0] = r.st.tetav; tp.wz[0] = a.wz_tet; tp.out[0] = r.tetav_alt;
-      tp.cur[1] = r.st.pai; tp.wz[1] = a.wz_pai; tp.out[1] = r.pai_alt;
-      tp.n = 2;
-    }
-    add(r.st.ux, r.ux_alt);
-    add(r.st.vx, r.vx_alt);
-    add(wk.wx, a.wx2);
-    add(r.st.qx, r.qx_alt);
-    if (p.ipptls > 0)
-      for (int q = 1; q < d.nqx; ++q) add(r.st.qx + q * F, r.qx_alt + q * F);
-    for (int q = 0; q < d.ntr; ++q) add(r.st.trac + q * F, r.trac_alt + q * F);
-    t.n = n;
-    REC("adv_vertical", L::adv_vertical(g, c, a.sa, wk, t, s)); ++nl;
-    REC("adv_horizontal", L::adv_horizontal(g, c, a.sa, r.st, t, s)); ++nl;
-    if (tp.n) {
-      REC("adv_vertical_f64", L::adv_vertical_f64(g, c, a.sa, wk, tp, s)); ++nl;
-      REC("adv_horizontal_f64", L::adv_horizontal_f64(g, c, a.sa, r.st, tp, s)); ++nl;
-    }
-    if (p.ipptls == 0 && d.nqx > 1) {
-      // species that are not advected keep their values in the other buffer
-      cudaMemcpy2DAsync(r.qx_alt + F, x->member_bytes, r.st.qx + F, x->member_bytes,
-                        (size_t)(d.nqx - 1) * F * sizeof(R), (size_t)x->nmem,
-                        cudaMemcpyDeviceToDevice, s);
-    }
-    x->adv_role ^= 1;
-    Roles<R> r2 = roles_of(a, x->uv_role, x->adv_role);
-    Work<R> wk2 = wk;
-    wk2.wx = a.wx2;
-    if (c.curvature) { REC("adv_curvature", L::adv_curvature(g, c, a.sa, r2.st, s)); ++nl; }
-    REC("adv_back", L::adv_back(g, r2.st, wk2, s)); ++nl;
-    // wx is scratch: its advected copy lives in wx2 and both roles of the
-    // pair are rebuilt from w each advection step, so no swap is kept.
+    // ---- advection (Main/mod_moloch.F90:767-1042) ----
+    const int uvo = (r + 1) * nsound;
+    REC("adv_prep", K::adv_prep(L, d, uvo, r, s)); ++nl;
+    REC("adv_vertical", K::adv_vertical(L, d, r, s)); nl += nv;
+    REC("adv_horizontal", K::adv_horizontal(L, d, uvo, r, s)); nl += nv;
+    if (x->key.any_copy) { REC("adv_species_copy", K::adv_species_copy(L, d, r, s)); ++nl; }
+    if (x->key.any_curv) { REC("adv_curvature", K::adv_curvature(L, d, r + 1, s)); ++nl; }
+    REC("adv_back", K::adv_back(L, d, uvo, r + 1, s)); ++nl;
   }
-  Roles<R> r = roles_of(a, x->uv_role, x->adv_role);
-  // ---- step end ----
-  REC("end_tvirt", L::end_tvirt(g, c, r.st, s)); ++nl;
-  if (c.apply_bdy) {
-    REC("bdy_ring", L::bdy_ring(g, c, r.st, a.bd, a.clk, s)); nl += 2;
-    REC("bdy_relax", L::bdy_relax(g, c, a.sa, r.st, a.bd, a.clk, s)); ++nl;
+  // ---- step end (Main/mod_moloch.F90:340-446) ----
+  const int uvo = nadv * nsound, ao = nadv;
+  REC("end_tvirt", K::end_tvirt(L, d, ao, s)); ++nl;
+  if (x->prm.do_apply_bdy) {
+    REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); nl += 2;
+    REC("bdy_relax", K::bdy_relax(L, d, uvo, ao, s)); ++nl;
   }
-  REC("end_cross", L::end_cross(g, c, a.sa, r.st, s)); ++nl;
-  REC("end_uvstag", L::end_uvstag(g, r.st, s)); ++nl;
-  REC("end_reduce", L::end_reduce(g, c, a.sa, r.st, a.partials, reduce_blocks(g), a.diag, a.clk, s)); nl += 2;
+  REC("end_cross", K::end_cross(L, d, uvo, ao, s)); ++nl;
+  REC("end_uvstag", K::end_uvstag(L, d, uvo, ao, s)); ++nl;
+  REC("end_reduce", K::end_reduce(L, d, uvo, ao, s)); nl += 2;
   return nl;
 }
 
+// Record the step into the context's graph: update the executable graph in
+// place when the topology allows, instantiate a new one otherwise.
 template <class R>
-int step_impl(mlc_ctx *x, Arrays<R> &a, int nsteps) {
-  for (int n = 0; n < nsteps; ++n) {
-    const int key = x->uv_role * 2 + x->adv_role;
-    if (x->use_graphs) {
-      if (!x->graph[key]) {
-        const int uv0 = x->uv_role, adv0 = x->adv_role;
-        cudaGraph_t gr = nullptr;
-        MLC_TRY(cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal));
-        x->launches_per_step = enqueue_step<R>(x, a);
-        cudaError_t e = cudaStreamEndCapture(x->stream, &gr);
-        if (e != cudaSuccess) return cuda_status(e);
-        cudaGraphExec_t ex = nullptr;
-        e = cudaGraphInstantiate(&ex, gr, 0);
-        cudaGraphDestroy(gr);
-        if (e != cudaSuccess) return cuda_status(e);
-        x->graph[key] = ex;
-        x->uv_role = uv0;  // replay below moves the roles
-        x->adv_role = adv0;
-      }
-      MLC_TRY(cudaGraphLaunch(x->graph[key], x->stream));
-      // the roles a step leaves are fixed: replay the bookkeeping only
-      for (int m = 0; m < x->c.nadv; ++m) {
-        if (x->c.nsound & 1) x->uv_role ^= 1;
-        x->adv_role ^= 1;
-      }
+int record(mlc_ctx *x) {
+  cudaGraph_t gr = nullptr;
+  MLC_TRY(cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal));
+  const int nl = enqueue_step<R>(x);
+  cudaError_t e = cudaStreamEndCapture(x->stream, &gr);
+  if (e != cudaSuccess) return cuda_status(e);
+  bool updated = false;
+  if (x->graph) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(x->graph, gr, &info) == cudaSuccess) {
+      updated = true;
     } else {
-      x->launches_per_step = enqueue_step<R>(x, a);
+      cudaGetLastError();
+      cudaGraphExecDestroy(x->graph);
+      x->graph = nullptr;
     }
+  }
+  if (!updated) {
+    e = cudaGraphInstantiate(&x->graph, gr, 0);
+    if (e != cudaSuccess) {
+      x->graph = nullptr;
+      cudaGraphDestroy(gr);
+      return cuda_status(e);
+    }
+  }
+  cudaGraphDestroy(gr);
+  x->graph_key = x->key;
+  x->graph_valid = true;
+  x->launches_per_step = nl;
+  return MLC_OK;
+}
+
+bool ready(const mlc_ctx *x) {
+  for (const Member &m : x->mem)
+    if (m.used && (!m.have_static || !m.have_state || (x->prm.do_apply_bdy && !m.have_bdy)))
+      return false;
+  return true;
+}
+
+template <class R>
+int step_impl(mlc_ctx *x, int nsteps) {
+  MLC_CHK(refresh<R>(x));
+  if (x->key.L.nmem == 0 || nsteps == 0) return MLC_OK;
+  if (x->use_graphs) {
+    if (!x->graph_valid || std::memcmp(&x->graph_key, &x->key, sizeof(GraphKey)) != 0)
+      MLC_CHK(record<R>(x));
+    for (int n = 0; n < nsteps; ++n) MLC_TRY(cudaGraphLaunch(x->graph, x->stream));
+  } else {
+    for (int n = 0; n < nsteps; ++n) x->launches_per_step = enqueue_step<R>(x);
   }
   return cuda_status(cudaGetLastError());
 }
 
+int step_any(mlc_ctx *x, int nsteps) {
+  return x->mixed ? step_impl<float>(x, nsteps) : step_impl<double>(x, nsteps);
+}
+
 // ---- host <-> device transfers -------------------------------------------
+
+Clock get_clock(mlc_ctx *x, int slot, int *st) {
+  Clock c{};
+  cudaError_t e = cudaMemcpyAsync(&c, x->clks + slot, sizeof(Clock), cudaMemcpyDeviceToHost, x->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(x->stream);
+  *st = cuda_status(e);
+  return c;
+}
 
 // Copy a packed (Fortran extents nj x ni x nk) host array into the padded
 // device layout through the staging buffer at element offset `soff`.  One
 // stream orders every copy and (un)pack, so consecutive fields may reuse the
 // same staging slice.
-struct Staging {
-  double *p;
-  size_t n;
-};
-
 template <class R>
-int put3(mlc_ctx *x, Staging sg, const double *h, R *dst, int nj, int ni, int nk, size_t soff) {
+int put3(mlc_ctx *x, const Geom &g, const double *h, R *dst, int nj, int ni, int nk, size_t soff) {
   if (!h) return MLC_OK;
   const size_t n = (size_t)nj * ni * nk;
-  if (soff + n > sg.n) return MLC_ERR_INVALID;
-  MLC_TRY(cudaMemcpyAsync(sg.p + soff, h, n * sizeof(double), cudaMemcpyHostToDevice, x->stream));
-  Launch<R>::unpack3(sg.p + soff, dst, x->g, nj, ni, nk, x->stream);
+  if (soff + n > x->staging_elems) return MLC_ERR_INVALID;
+  MLC_TRY(cudaMemcpyAsync(x->staging + soff, h, n * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+  Launch<R>::unpack3(x->staging + soff, dst, g, nj, ni, nk, x->stream);
   return MLC_OK;
 }
 
 template <class R>
-int get3(mlc_ctx *x, Staging sg, const R *src, double *h, int nj, int ni, int nk, size_t soff) {
+int get3(mlc_ctx *x, const Geom &g, const R *src, double *h, int nj, int ni, int nk, size_t soff) {
   if (!h) return MLC_OK;
   const size_t n = (size_t)nj * ni * nk;
-  if (soff + n > sg.n) return MLC_ERR_INVALID;
-  Launch<R>::pack3(src, sg.p + soff, x->g, nj, ni, nk, x->stream);
-  MLC_TRY(cudaMemcpyAsync(h, sg.p + soff, n * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
+  if (soff + n > x->staging_elems) return MLC_ERR_INVALID;
+  Launch<R>::pack3(src, x->staging + soff, g, nj, ni, nk, x->stream);
+  MLC_TRY(cudaMemcpyAsync(h, x->staging + soff, n * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
   return MLC_OK;
 }
 
 // 2-D padded copy of a small host array (built on the host, then one copy).
 template <class T>
-int put2_host(mlc_ctx *x, const T *h, T *dst, int nj, int ni) {
-  std::vector<T> tmp((size_t)x->g.PS, T(0));
+int put2_host(mlc_ctx *x, const Geom &g, const T *h, T *dst, int nj, int ni) {
+  std::vector<T> tmp((size_t)g.PS, T(0));
   for (int i = 0; i < ni; ++i)
-    for (int j = 0; j < nj; ++j) tmp[(size_t)j + (size_t)i * x->g.P] = h[(size_t)j + (size_t)i * nj];
+    for (int j = 0; j < nj; ++j) tmp[(size_t)j + (size_t)i * g.P] = h[(size_t)j + (size_t)i * nj];
   MLC_TRY(cudaMemcpyAsync(dst, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, x->stream));
   return cuda_status(cudaStreamSynchronize(x->stream));
 }
 
 template <class R>
-int put2r(mlc_ctx *x, const std::vector<double> &h, R *dst, int nj, int ni) {
+int put2r(mlc_ctx *x, const Geom &g, const std::vector<double> &h, const R *dst, int nj, int ni) {
   std::vector<R> tmp((size_t)nj * ni);
   for (size_t e = 0; e < tmp.size(); ++e) tmp[e] = (R)h[e];
-  return put2_host<R>(x, tmp.data(), dst, nj, ni);
+  return put2_host<R>(x, g, tmp.data(), W(dst), nj, ni);
 }
 
-int put1(mlc_ctx *x, const double *h, double *dst, size_t n) {
-  MLC_TRY(cudaMemcpyAsync(dst, h, n * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+int put1(mlc_ctx *x, const double *h, const double *dst, size_t n) {
+  MLC_TRY(cudaMemcpyAsync(W(dst), h, n * sizeof(double), cudaMemcpyHostToDevice, x->stream));
   return cuda_status(cudaStreamSynchronize(x->stream));
 }
 
-#define MLC_CHK(x)              \
-  do {                          \
-    int s_ = (x);               \
-    if (s_ != MLC_OK) return s_; \
-  } while (0)
-
 template <class R>
-int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
-  const Staging SG{a.staging, a.staging_elems};
-  const mlc_dims &d = x->dims;
+int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
+  const Dom<R> &D = dom_of<R>(mb);
+  const Stat<R> &a = D.sa;
+  const Geom &g = mb.g;
+  const mlc_dims &d = mb.dims;
   const mlc_params &p = x->prm;
+  Scal &c = mb.c;
   const int jx = d.jx, iy = d.iy, kz = d.kz;
   if (!s->msfu || !s->msfv || !s->msfx || !s->ulat || !s->vlat || !s->hx || !s->hy || !s->fmz ||
       !s->fmzf || !s->rfmzu || !s->rfmzv || !s->zeta || !s->dz || !s->zita || !s->zitah ||
@@ -492,21 +571,27 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
     return MLC_ERR_INVALID;
   if (d.ntr > 0 && !s->fcx) return MLC_ERR_INVALID;
   if (p.lrotllr && !s->rlat) return MLC_ERR_INVALID;
+  // zone indices address rows 1..nspgx of hefc/fcx: reject anything else
+  const size_t nd = (size_t)jx * iy;
+  for (const int32_t *b : {s->ibnd_cr, s->ibnd_ud, s->ibnd_vd})
+    for (size_t e = 0; e < nd; ++e)
+      if (b[e] > p.nspgx || b[e] == 0 || b[e] < -1) return MLC_ERR_INVALID;
+  c.rdzita = 1.0 / s->zita[kz - 1];
   // 3-D metric: one field at a time through the staging buffer
-  MLC_CHK(put3<R>(x, SG, s->fmz, a.fmz, jx - 1, iy - 1, kz, 0));
-  MLC_CHK(put3<R>(x, SG, s->fmzf, a.fmzf, jx - 1, iy - 1, kz + 1, 0));
+  MLC_CHK(put3<R>(x, g, s->fmz, W(a.fmz), jx - 1, iy - 1, kz, 0));
+  MLC_CHK(put3<R>(x, g, s->fmzf, W(a.fmzf), jx - 1, iy - 1, kz + 1, 0));
   if (sizeof(R) != sizeof(double)) {
-    MLC_CHK(put3<double>(x, SG, s->fmz, a.fmz_d, jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<double>(x, SG, s->fmzf, a.fmzf_d, jx - 1, iy - 1, kz + 1, 0));
+    MLC_CHK(put3<double>(x, g, s->fmz, W(a.fmz_d), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, g, s->fmzf, W(a.fmzf_d), jx - 1, iy - 1, kz + 1, 0));
   }
-  MLC_CHK(put3<R>(x, SG, s->rfmzu, a.rfmzu, jx, iy - 1, kz, 0));
-  MLC_CHK(put3<R>(x, SG, s->rfmzv, a.rfmzv, jx - 1, iy, kz, 0));
-  MLC_CHK(put3<double>(x, SG, s->zeta, a.zeta, jx - 1, iy - 1, kz, 0));
-  MLC_CHK(put3<double>(x, SG, s->dz, a.dz, jx - 1, iy - 1, kz, 0));
+  MLC_CHK(put3<R>(x, g, s->rfmzu, W(a.rfmzu), jx, iy - 1, kz, 0));
+  MLC_CHK(put3<R>(x, g, s->rfmzv, W(a.rfmzv), jx - 1, iy, kz, 0));
+  MLC_CHK(put3<double>(x, g, s->zeta, W(a.zeta), jx - 1, iy - 1, kz, 0));
+  MLC_CHK(put3<double>(x, g, s->dz, W(a.dz), jx - 1, iy - 1, kz, 0));
   // vertical WAF ratios (dtrdz*fmz)/fmzf, Main/mod_moloch.F90:888-889
   {
     const double mo_dzita = s->zita[kz - 1];
-    const double dtrdz = 0.5 * (x->c.dtstepa * (1.0 / mo_dzita));
+    const double dtrdz = 0.5 * (c.dtstepa * (1.0 / mo_dzita));
     const size_t c2 = (size_t)(jx - 1) * (iy - 1);
     std::vector<double> zu(c2 * kz), zd(c2 * kz);
     for (int k = 0; k < kz; ++k)
@@ -515,44 +600,39 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
         zu[e + c2 * k] = dtrdz * fz / s->fmzf[e + c2 * k];
         zd[e + c2 * k] = dtrdz * fz / s->fmzf[e + c2 * (k + 1)];
       }
-    MLC_CHK(put3<R>(x, SG, zu.data(), a.zrfmu, jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<R>(x, SG, zd.data(), a.zrfmd, jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<R>(x, g, zu.data(), W(a.zrfmu), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<R>(x, g, zd.data(), W(a.zrfmd), jx - 1, iy - 1, kz, 0));
     MLC_TRY(cudaStreamSynchronize(x->stream));
   }
   // 2-D fields and init_moloch derivations (Main/mod_moloch.F90:258-271)
-  const size_t nd = (size_t)jx * iy;
   std::vector<double> t2(nd);
   auto copy2 = [&](const double *h, size_t n) { t2.assign(h, h + n); };
-  copy2(s->msfu, nd); MLC_CHK(put2r<R>(x, t2, a.msfu, jx, iy));
-  copy2(s->msfv, nd); MLC_CHK(put2r<R>(x, t2, a.msfv, jx, iy));
-  copy2(s->msfx, nd); MLC_CHK(put2r<R>(x, t2, a.msfx, jx, iy));
+  copy2(s->msfu, nd); MLC_CHK(put2r<R>(x, g, t2, a.msfu, jx, iy));
+  copy2(s->msfv, nd); MLC_CHK(put2r<R>(x, g, t2, a.msfv, jx, iy));
+  copy2(s->msfx, nd); MLC_CHK(put2r<R>(x, g, t2, a.msfx, jx, iy));
   for (size_t e = 0; e < nd; ++e) t2[e] = s->msfx[e] * s->msfx[e];
-  MLC_CHK(put2r<R>(x, t2, a.mx2, jx, iy));
+  MLC_CHK(put2r<R>(x, g, t2, a.mx2, jx, iy));
   for (size_t e = 0; e < nd; ++e) t2[e] = 1.0 / s->msfu[e];
-  MLC_CHK(put2r<R>(x, t2, a.rmu, jx, iy));
+  MLC_CHK(put2r<R>(x, g, t2, a.rmu, jx, iy));
   for (size_t e = 0; e < nd; ++e) t2[e] = 1.0 / s->msfv[e];
-  MLC_CHK(put2r<R>(x, t2, a.rmv, jx, iy));
-  copy2(s->hx, (size_t)jx * (iy - 1)); MLC_CHK(put2r<R>(x, t2, a.hx, jx, iy - 1));
-  copy2(s->hy, (size_t)(jx - 1) * iy); MLC_CHK(put2r<R>(x, t2, a.hy, jx - 1, iy));
+  MLC_CHK(put2r<R>(x, g, t2, a.rmv, jx, iy));
+  copy2(s->hx, (size_t)jx * (iy - 1)); MLC_CHK(put2r<R>(x, g, t2, a.hx, jx, iy - 1));
+  copy2(s->hy, (size_t)(jx - 1) * iy); MLC_CHK(put2r<R>(x, g, t2, a.hy, jx - 1, iy));
   t2.resize((size_t)jx * (iy - 1));
   for (size_t e = 0; e < t2.size(); ++e) t2[e] = kOmega2 * std::sin(s->ulat[e] * kDegrad);
-  MLC_CHK(put2r<R>(x, t2, a.coru, jx, iy - 1));
+  MLC_CHK(put2r<R>(x, g, t2, a.coru, jx, iy - 1));
   t2.resize((size_t)(jx - 1) * iy);
   for (size_t e = 0; e < t2.size(); ++e) t2[e] = kOmega2 * std::sin(s->vlat[e] * kDegrad);
-  MLC_CHK(put2r<R>(x, t2, a.corv, jx - 1, iy));
-  MLC_CHK(put2_host<int32_t>(x, s->ibnd_cr, a.ibnd_cr, jx, iy));
-  MLC_CHK(put2_host<int32_t>(x, s->ibnd_ud, a.ibnd_ud, jx, iy));
-  MLC_CHK(put2_host<int32_t>(x, s->ibnd_vd, a.ibnd_vd, jx, iy));
-  // zone indices address rows 1..nspgx of hefc/fcx: reject anything else
-  for (const int32_t *b : {s->ibnd_cr, s->ibnd_ud, s->ibnd_vd})
-    for (size_t e = 0; e < nd; ++e)
-      if (b[e] > p.nspgx || b[e] == 0 || b[e] < -1) return MLC_ERR_INVALID;
+  MLC_CHK(put2r<R>(x, g, t2, a.corv, jx - 1, iy));
+  MLC_CHK(put2_host<int32_t>(x, g, s->ibnd_cr, W(a.ibnd_cr), jx, iy));
+  MLC_CHK(put2_host<int32_t>(x, g, s->ibnd_ud, W(a.ibnd_ud), jx, iy));
+  MLC_CHK(put2_host<int32_t>(x, g, s->ibnd_vd, W(a.ibnd_vd), jx, iy));
   // the relaxation zones are non-empty (ba%havebound)
   auto any_pos = [&](const int32_t *b) {
     for (size_t e = 0; e < nd; ++e) if (b[e] > 0) return 1;
     return 0;
   };
-  x->c.hb_cr |= any_pos(s->ibnd_cr); x->c.hb_ud |= any_pos(s->ibnd_ud); x->c.hb_vd |= any_pos(s->ibnd_vd);
+  c.hb_cr = any_pos(s->ibnd_cr); c.hb_ud = any_pos(s->ibnd_ud); c.hb_vd = any_pos(s->ibnd_vd);
   // the curvature terms vanish identically with uniform map factors
   {
     bool curv = p.lrotllr != 0;
@@ -561,7 +641,7 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
         const size_t e = (size_t)(j - 1) + (size_t)(i - 1) * jx;
         if ((s->msfu[e - 1] - s->msfu[e]) != 0.0 || (s->msfv[e - jx] - s->msfv[e]) != 0.0) curv = true;
       }
-    x->c.curvature |= curv ? 1 : 0;
+    c.curvature = curv ? 1 : 0;
   }
   // 1-D vertical arrays, Main/mod_moloch.F90:262-300
   std::vector<double> v1(kz + 1);
@@ -577,7 +657,16 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
   MLC_CHK(put1(x, v1.data(), a.xknu, kz));
   MLC_CHK(put1(x, s->ffilt, a.ffilt, kz));
   if (s->tnudge) MLC_CHK(put1(x, s->tnudge, a.tnudge, kz));
-  else MLC_TRY(cudaMemsetAsync(a.tnudge, 0, kz * sizeof(double), x->stream));
+  else MLC_TRY(cudaMemsetAsync(W(a.tnudge), 0, kz * sizeof(double), x->stream));
+  // Levels nudged at the top: the member's own nztop, the last level with a
+  // non-zero tnudge (bdyin sets tnudge > 0 exactly on levels 1..nztop,
+  // Main/mod_bdycod.F90:507-537).  A level with tnudge = 0 would be left
+  // unchanged by the nudging anyway, so members of one context may differ
+  // in levels and terrain without sharing one nztop.
+  c.nztop = 0;
+  if (p.mo_top_nudge && s->tnudge)
+    for (int k = 1; k <= kz; ++k)
+      if (s->tnudge[k - 1] != 0.0) c.nztop = k;
   MLC_CHK(put1(x, s->hefc, a.hefc, (size_t)p.nspgx * kz));
   if (s->fcx) MLC_CHK(put1(x, s->fcx, a.fcx, p.nspgx));
   if (s->rlat) MLC_CHK(put1(x, s->rlat, a.rlat, iy));
@@ -586,104 +675,218 @@ int bind_static_impl(mlc_ctx *x, Arrays<R> &a, const mlc_static_ptrs *s) {
 }
 
 template <class R>
-int upload_state_impl(mlc_ctx *x, Arrays<R> &a, const mlc_state_ptrs *h) {
-  const Staging SG{a.staging, a.staging_elems};
-  const mlc_dims &d = x->dims;
-  const int jx = d.jx, iy = d.iy, kz = d.kz;
-  Roles<R> r = roles_of(a, x->uv_role, x->adv_role);
-  State<R> &st = r.st;
+int upload_state_impl(mlc_ctx *x, int slot, const mlc_state_ptrs *h) {
+  Member &mb = x->mem[slot];
+  int cst;
+  const Clock ck = get_clock(x, slot, &cst);
+  MLC_CHK(cst);
+  const State<R> st = state_of(dom_of<R>(mb), ck.uv_role, ck.adv_role);
+  const Geom &g = mb.g;
+  const int jx = mb.dims.jx, iy = mb.dims.iy, kz = mb.dims.kz;
   size_t off = 0;
   const size_t c3 = (size_t)(jx - 1) * (iy - 1) * kz;
   auto adv = [&](size_t n) { size_t o = off; off += n; return o; };
-  MLC_CHK(put3<R>(x, SG, h->u, st.u, jx, iy - 1, kz, adv((size_t)jx * (iy - 1) * kz)));
-  MLC_CHK(put3<R>(x, SG, h->v, st.v, jx - 1, iy, kz, adv((size_t)(jx - 1) * iy * kz)));
-  MLC_CHK(put3<R>(x, SG, h->w, st.w, jx - 1, iy - 1, kz + 1, adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
-  MLC_CHK(put3<double>(x, SG, h->pai, st.pai, jx - 1, iy - 1, kz, adv(c3)));
-  MLC_CHK(put3<double>(x, SG, h->tetav, st.tetav, jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(put3<R>(x, g, h->u, st.u, jx, iy - 1, kz, adv((size_t)jx * (iy - 1) * kz)));
+  MLC_CHK(put3<R>(x, g, h->v, st.v, jx - 1, iy, kz, adv((size_t)(jx - 1) * iy * kz)));
+  MLC_CHK(put3<R>(x, g, h->w, st.w, jx - 1, iy - 1, kz + 1, adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
+  MLC_CHK(put3<double>(x, g, h->pai, st.pai, jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(put3<double>(x, g, h->tetav, st.tetav, jx - 1, iy - 1, kz, adv(c3)));
   R *f3[] = {st.t, st.tvirt, st.ux, st.vx, st.p, st.rho, st.qsat};
   const double *h3[] = {h->t, h->tvirt, h->ux, h->vx, h->p, h->rho, h->qsat};
-  for (int q = 0; q < 7; ++q) MLC_CHK(put3<R>(x, SG, h3[q], f3[q], jx - 1, iy - 1, kz, adv(c3)));
-  const size_t F = x->g.field3();
-  for (int n = 0; n < d.nqx && h->qx; ++n)
-    MLC_CHK(put3<R>(x, SG, h->qx + n * c3, st.qx + n * F, jx - 1, iy - 1, kz, adv(c3)));
-  for (int n = 0; n < d.ntr && h->trac; ++n)
-    MLC_CHK(put3<R>(x, SG, h->trac + n * c3, st.trac + n * F, jx - 1, iy - 1, kz, adv(c3)));
+  for (int q = 0; q < 7; ++q) MLC_CHK(put3<R>(x, g, h3[q], f3[q], jx - 1, iy - 1, kz, adv(c3)));
+  const size_t F = g.field3();
+  for (int n = 0; n < mb.dims.nqx && h->qx; ++n)
+    MLC_CHK(put3<R>(x, g, h->qx + n * c3, st.qx + n * F, jx - 1, iy - 1, kz, adv(c3)));
+  for (int n = 0; n < mb.dims.ntr && h->trac; ++n)
+    MLC_CHK(put3<R>(x, g, h->trac + n * c3, st.trac + n * F, jx - 1, iy - 1, kz, adv(c3)));
   if (h->ps) {
     const size_t c2 = (size_t)(jx - 1) * (iy - 1);
-    MLC_CHK(put3<double>(x, SG, h->ps, st.ps, jx - 1, iy - 1, 1, adv(c2)));
+    MLC_CHK(put3<double>(x, g, h->ps, st.ps, jx - 1, iy - 1, 1, adv(c2)));
   }
   // init_moloch: w(:,:,1) = 0 (Main/mod_moloch.F90:264-266)
-  if (h->w) MLC_TRY(cudaMemsetAsync(st.w, 0, x->g.PS * sizeof(R), x->stream));
+  if (h->w) MLC_TRY(cudaMemsetAsync(st.w, 0, g.PS * sizeof(R), x->stream));
   return cuda_status(cudaStreamSynchronize(x->stream));
 }
 
 template <class R>
-int download_state_impl(mlc_ctx *x, Arrays<R> &a, const mlc_state_ptrs *h) {
-  const Staging SG{a.staging, a.staging_elems};
-  const mlc_dims &d = x->dims;
-  const int jx = d.jx, iy = d.iy, kz = d.kz;
-  Roles<R> r = roles_of(a, x->uv_role, x->adv_role);
-  const State<R> &st = r.st;
+int download_state_impl(mlc_ctx *x, int slot, const mlc_state_ptrs *h) {
+  Member &mb = x->mem[slot];
+  int cst;
+  const Clock ck = get_clock(x, slot, &cst);
+  MLC_CHK(cst);
+  const State<R> st = state_of(dom_of<R>(mb), ck.uv_role, ck.adv_role);
+  const Geom &g = mb.g;
+  const int jx = mb.dims.jx, iy = mb.dims.iy, kz = mb.dims.kz;
   size_t off = 0;
   const size_t c3 = (size_t)(jx - 1) * (iy - 1) * kz;
   auto adv = [&](size_t n) { size_t o = off; off += n; return o; };
-  MLC_CHK(get3<R>(x, SG, st.u, h->u, jx, iy - 1, kz, adv((size_t)jx * (iy - 1) * kz)));
-  MLC_CHK(get3<R>(x, SG, st.v, h->v, jx - 1, iy, kz, adv((size_t)(jx - 1) * iy * kz)));
-  MLC_CHK(get3<R>(x, SG, st.w, h->w, jx - 1, iy - 1, kz + 1, adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
-  MLC_CHK(get3<double>(x, SG, st.pai, h->pai, jx - 1, iy - 1, kz, adv(c3)));
-  MLC_CHK(get3<double>(x, SG, st.tetav, h->tetav, jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(get3<R>(x, g, st.u, h->u, jx, iy - 1, kz, adv((size_t)jx * (iy - 1) * kz)));
+  MLC_CHK(get3<R>(x, g, st.v, h->v, jx - 1, iy, kz, adv((size_t)(jx - 1) * iy * kz)));
+  MLC_CHK(get3<R>(x, g, st.w, h->w, jx - 1, iy - 1, kz + 1, adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
+  MLC_CHK(get3<double>(x, g, st.pai, h->pai, jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(get3<double>(x, g, st.tetav, h->tetav, jx - 1, iy - 1, kz, adv(c3)));
   const R *f3[] = {st.t, st.tvirt, st.ux, st.vx, st.p, st.rho, st.qsat};
   double *h3[] = {h->t, h->tvirt, h->ux, h->vx, h->p, h->rho, h->qsat};
-  for (int q = 0; q < 7; ++q) MLC_CHK(get3<R>(x, SG, f3[q], h3[q], jx - 1, iy - 1, kz, adv(c3)));
-  const size_t F = x->g.field3();
-  for (int n = 0; n < d.nqx && h->qx; ++n)
-    MLC_CHK(get3<R>(x, SG, st.qx + n * F, h->qx + n * c3, jx - 1, iy - 1, kz, adv(c3)));
-  for (int n = 0; n < d.ntr && h->trac; ++n)
-    MLC_CHK(get3<R>(x, SG, st.trac + n * F, h->trac + n * c3, jx - 1, iy - 1, kz, adv(c3)));
+  for (int q = 0; q < 7; ++q) MLC_CHK(get3<R>(x, g, f3[q], h3[q], jx - 1, iy - 1, kz, adv(c3)));
+  const size_t F = g.field3();
+  for (int n = 0; n < mb.dims.nqx && h->qx; ++n)
+    MLC_CHK(get3<R>(x, g, st.qx + n * F, h->qx + n * c3, jx - 1, iy - 1, kz, adv(c3)));
+  for (int n = 0; n < mb.dims.ntr && h->trac; ++n)
+    MLC_CHK(get3<R>(x, g, st.trac + n * F, h->trac + n * c3, jx - 1, iy - 1, kz, adv(c3)));
   if (h->ps) {
     const size_t c2 = (size_t)(jx - 1) * (iy - 1);
-    MLC_CHK(get3<double>(x, SG, st.ps, h->ps, jx - 1, iy - 1, 1, adv(c2)));
+    MLC_CHK(get3<double>(x, g, st.ps, h->ps, jx - 1, iy - 1, 1, adv(c2)));
   }
   return cuda_status(cudaStreamSynchronize(x->stream));
 }
 
 template <class R>
-int set_boundary_impl(mlc_ctx *x, Arrays<R> &a, const mlc_bdy_ptrs *b) {
-  const Staging SG{a.staging, a.staging_elems};
-  const mlc_dims &d = x->dims;
+int set_boundary_impl(mlc_ctx *x, Member &mb, const mlc_bdy_ptrs *b) {
+  const Bdy<R> &a = dom_of<R>(mb).bd;
+  const Geom &g = mb.g;
+  const mlc_dims &d = mb.dims;
   const mlc_params &p = x->prm;
   const int jx = d.jx, iy = d.iy, kz = d.kz;
   const size_t c3 = (size_t)(jx - 1) * (iy - 1) * kz;
-  const size_t F = x->g.field3();
+  const size_t F = g.field3();
   for (int s = 0; s < 2; ++s) {
     if (!b->xtb[s] || !b->xqb[s] || !b->xpaib[s] || !b->dub[s] || !b->dvb[s] || !b->xpsb[s])
       return MLC_ERR_INVALID;
     if (p.present_qc && !b->xlb[s]) return MLC_ERR_INVALID;
     if (p.present_qi && !b->xib[s]) return MLC_ERR_INVALID;
     if (d.ntr > 0 && !b->chib[s]) return MLC_ERR_INVALID;
-    MLC_CHK(put3<R>(x, SG, b->xtb[s], a.bfield[s][0], jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<R>(x, SG, b->xqb[s], a.bfield[s][1], jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<double>(x, SG, b->xpaib[s], a.xpaib[s], jx - 1, iy - 1, kz, 0));
-    if (p.present_qc) MLC_CHK(put3<R>(x, SG, b->xlb[s], a.bfield[s][3], jx - 1, iy - 1, kz, 0));
-    if (p.present_qi) MLC_CHK(put3<R>(x, SG, b->xib[s], a.bfield[s][4], jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<R>(x, SG, b->dub[s], a.bfield[s][5], jx, iy - 1, kz, 0));
-    MLC_CHK(put3<R>(x, SG, b->dvb[s], a.bfield[s][6], jx - 1, iy, kz, 0));
+  }
+  for (int s = 0; s < 2; ++s) {
+    MLC_CHK(put3<R>(x, g, b->xtb[s], W(a.xtb[s]), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<R>(x, g, b->xqb[s], W(a.xqb[s]), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, g, b->xpaib[s], W(a.xpaib[s]), jx - 1, iy - 1, kz, 0));
+    if (p.present_qc) MLC_CHK(put3<R>(x, g, b->xlb[s], W(a.xlb[s]), jx - 1, iy - 1, kz, 0));
+    if (p.present_qi) MLC_CHK(put3<R>(x, g, b->xib[s], W(a.xib[s]), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<R>(x, g, b->dub[s], W(a.dub[s]), jx, iy - 1, kz, 0));
+    MLC_CHK(put3<R>(x, g, b->dvb[s], W(a.dvb[s]), jx - 1, iy, kz, 0));
     for (int n = 0; n < d.ntr; ++n)
-      MLC_CHK(put3<R>(x, SG, b->chib[s] + n * c3, a.bfield[s][7] + n * F, jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<double>(x, SG, b->xpsb[s], a.xpsb[s], jx - 1,
-                         iy - 1, 1, 0));
+      MLC_CHK(put3<R>(x, g, b->chib[s] + n * c3, W(a.chib[s]) + n * F, jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, g, b->xpsb[s], W(a.xpsb[s]), jx - 1, iy - 1, 1, 0));
     MLC_TRY(cudaStreamSynchronize(x->stream));
   }
   return MLC_OK;
 }
 
-template <class R>
-size_t footprint(const mlc_dims &d, const mlc_params &p, int elem) {
-  Geom g = make_geom(d, elem);
-  Arrays<R> a{};
-  Carver cv;
-  carve<R>(cv, a, g, d, p);
-  return cv.off + state_elems(d) * sizeof(double);
+void release(mlc_ctx *x) {
+  if (!x) return;
+  if (x->stream) cudaStreamSynchronize(x->stream);
+  if (x->graph) cudaGraphExecDestroy(x->graph);
+  for (Member &m : x->mem)
+    if (m.raw) cudaFreeAsync(m.raw, x->stream);
+  if (x->staging) cudaFreeAsync(x->staging, x->stream);
+  if (x->stream) cudaStreamSynchronize(x->stream);
+  if (x->clks) cudaFree(x->clks);
+  if (x->diags) cudaFree(x->diags);
+  if (x->table) cudaFree(x->table);
+  if (x->pool) cudaMemPoolDestroy(x->pool);
+  if (x->stream) cudaStreamDestroy(x->stream);
+  delete x;
+}
+
+// A context with `capacity` empty slots.
+int create_common(const mlc_params *params, int capacity, size_t budget, mlc_ctx **out) {
+  if (!out) return MLC_ERR_INVALID;
+  *out = nullptr;
+  MLC_CHK(validate_params(params));
+  if (capacity < 1 || capacity > kMaxSlots) return MLC_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return MLC_ERR_NODEVICE;
+  }
+  mlc_ctx *x = new (std::nothrow) mlc_ctx();
+  if (!x) return MLC_ERR_NOMEM;
+  x->prm = *params;
+  x->mixed = params->precision == MLC_PREC_MIXED;
+  x->budget = budget;
+  x->mem.assign(capacity, Member{});
+  LaunchGeom &L = x->key.L;
+  L.col_x = 32; L.col_y = 4;
+  L.solve_x = 32; L.solve_y = 2;
+  L.vert_x = 32; L.vert_y = 2;
+  L.htile = 0;
+  cudaError_t e = cudaGetDevice(&x->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = x->device;
+    e = cudaMemPoolCreate(&x->pool, &props);
+  }
+  if (e == cudaSuccess) {
+    // keep freed member arenas in the pool for the next join
+    uint64_t keep = UINT64_MAX;
+    e = cudaMemPoolSetAttribute(x->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&x->clks, capacity * sizeof(Clock));
+  if (e == cudaSuccess) e = cudaMalloc(&x->diags, capacity * sizeof(DiagDev));
+  if (e == cudaSuccess)
+    e = cudaMalloc(&x->table, capacity * std::max(sizeof(Dom<double>), sizeof(Dom<float>)));
+  if (e == cudaSuccess) e = cudaMemsetAsync(x->clks, 0, capacity * sizeof(Clock), x->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(x->diags, 0, capacity * sizeof(DiagDev), x->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(x->stream);
+  if (e == cudaSuccess) e = x->mixed ? Launch<float>::configure_sound() : Launch<double>::configure_sound();
+  if (e == cudaSuccess) e = x->mixed ? Launch<float>::configure_advect() : Launch<double>::configure_advect();
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    release(x);
+    return cuda_status(e);
+  }
+  *out = x;
+  return MLC_OK;
+}
+
+int create_members(const mlc_dims *dims, int stride, const mlc_params *params, int nmem, mlc_ctx **out) {
+  if (!out) return MLC_ERR_INVALID;
+  *out = nullptr;
+  if (!dims || nmem < 1 || nmem > kMaxSlots) return MLC_ERR_INVALID;
+  MLC_CHK(validate_params(params));
+  for (int m = 0; m < nmem; ++m) MLC_CHK(validate_dims(dims + (size_t)m * stride, params));
+  mlc_ctx *x = nullptr;
+  MLC_CHK(create_common(params, nmem, 0, &x));
+  for (int m = 0; m < nmem; ++m) {
+    const int st = add_member(x, m, dims[(size_t)m * stride]);
+    if (st != MLC_OK) {
+      release(x);
+      return st;
+    }
+  }
+  *out = x;
+  return MLC_OK;
+}
+
+// Diagnostics of every slot after the last step (out has one entry per slot).
+int fetch_diags(mlc_ctx *x, int nsteps, mlc_diag *out) {
+  const size_t n = x->mem.size();
+  std::vector<DiagDev> dd(n);
+  std::vector<Clock> ck(n);
+  MLC_TRY(cudaMemcpyAsync(dd.data(), x->diags, n * sizeof(DiagDev), cudaMemcpyDeviceToHost, x->stream));
+  MLC_TRY(cudaMemcpyAsync(ck.data(), x->clks, n * sizeof(Clock), cudaMemcpyDeviceToHost, x->stream));
+  MLC_TRY(cudaStreamSynchronize(x->stream));
+  bool bad = false;
+  for (size_t m = 0; m < n; ++m) {
+    const bool used = x->mem[m].used;
+    if (used && ck[m].nonfinite) bad = true;
+    if (!out) continue;
+    std::memset(&out[m], 0, sizeof(out[m]));
+    if (!used) continue;
+    out[m].ps_max = dd[m].ps_max;
+    out[m].ps_min = dd[m].ps_min;
+    out[m].nonfinite = ck[m].nonfinite;
+    out[m].steps_done = nsteps;
+    out[m].drymass = dd[m].drymass;
+    out[m].dryadv = dd[m].dryadv;
+    out[m].qmass = dd[m].qmass;
+    out[m].qadv = dd[m].qadv;
+    out[m].xbctime = ck[m].xbctime;
+  }
+  return bad ? MLC_ERR_NONFINITE : MLC_OK;
 }
 
 }  // namespace
@@ -728,194 +931,111 @@ const char *mlc_strerror(int st) {
     case MLC_ERR_STATE: return "call order violated (static fields, state or boundary missing)";
     case MLC_ERR_NONFINITE: return "CFL VIOLATION: non-finite surface pressure";
     case MLC_ERR_NODEVICE: return "no CUDA device";
-    case MLC_ERR_BUDGET: return "request exceeds the device memory budget";
+    case MLC_ERR_BUDGET: return "request exceeds the device memory budget or the free slots";
     case MLC_ERR_TOO_LARGE: return "size beyond the fixed maximum";
     default: return "unknown status";
   }
 }
 
 size_t mlc_footprint_bytes(const mlc_dims *d, int precision) {
+  if (!d) return 0;
   mlc_params p;
   mlc_default_params(&p);
   p.ipptls = d->nqx >= 5 ? 2 : 1;
   p.present_qc = p.present_qi = 1;
   p.nspgx = 34;
-  if (precision == MLC_PREC_MIXED) return footprint<float>(*d, p, 4);
-  return footprint<double>(*d, p, 8);
+  const size_t arena = precision == MLC_PREC_MIXED ? arena_bytes<float>(*d, p) : arena_bytes<double>(*d, p);
+  return arena + kAlign + state_elems(*d) * sizeof(double);
+}
+
+size_t mlc_member_footprint(const mlc_dims *d, const mlc_params *p) {
+  if (!d || !p) return 0;
+  const size_t arena = p->precision == MLC_PREC_MIXED ? arena_bytes<float>(*d, *p) : arena_bytes<double>(*d, *p);
+  return arena;
 }
 
 int mlc_create_batch(const mlc_dims *dims, const mlc_params *params, int nmem, mlc_ctx **out) {
-  if (!out) return MLC_ERR_INVALID;
-  *out = nullptr;
-  int st = validate(dims, params);
-  if (st != MLC_OK) return st;
-  if (nmem < 1 || nmem > 4096) return MLC_ERR_INVALID;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return MLC_ERR_NODEVICE;
-  std::unique_ptr<mlc_ctx> x(new (std::nothrow) mlc_ctx());
-  if (!x) return MLC_ERR_NOMEM;
-  x->dims = *dims;
-  x->prm = *params;
-  x->nmem = nmem;
-  x->m_static.assign(nmem, 0);
-  x->m_state.assign(nmem, 0);
-  x->m_bdy.assign(nmem, 0);
-  MLC_TRY(cudaGetDevice(&x->device));
-  const bool mixed = params->precision == MLC_PREC_MIXED;
-  x->g = make_geom(*dims, mixed ? 4 : 8);
-  Scal &c = x->c;
-  c.dx = params->dx;
-  c.rdx = 1.0 / params->dx;
-  c.dtsec = params->dtsec;
-  c.dt = params->dtsec;
-  c.dtstepa = params->dtsec / (double)params->mo_nadv;
-  c.dtsound = c.dtstepa / (double)params->mo_nsound;
-  c.dtbdys = params->dtbdys;
-  c.rtb = 1.0 / params->dtbdys;
-  c.nadv = params->mo_nadv;
-  c.nsound = params->mo_nsound;
-  c.divdamp = params->mo_divdamp;
-  c.divfilter = params->mo_divfilter;
-  c.top_nudge = params->mo_top_nudge;
-  c.apply_bdy = params->do_apply_bdy;
-  c.lrotllr = params->lrotllr;
-  c.ipptls = params->ipptls;
-  c.present_qc = params->present_qc;
-  c.present_qi = params->present_qi;
-  c.nspgx = params->nspgx;
-  c.nztop = params->mo_top_nudge ? params->nztop : 0;
-  c.debug_level = params->debug_level;
-  MLC_TRY(cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking));
-  Carver cv;
-  if (mixed) carve<float>(cv, x->af, x->g, *dims, *params);
-  else carve<double>(cv, x->ad, x->g, *dims, *params);
-  x->member_bytes = cv.off;
-  x->arena_bytes = cv.off * (size_t)nmem;
-  x->g.nmem = nmem;
-  x->g.mstride = x->member_bytes;
-  cudaError_t e = cudaMalloc(&x->arena, x->arena_bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&x->staging, state_elems(*dims) * sizeof(double));
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    if (x->arena) cudaFree(x->arena);
-  if (x->staging) cudaFree(x->staging);
-    cudaStreamDestroy(x->stream);
-    return MLC_ERR_NOMEM;
-  }
-  if (mixed) x->af = member_arrays<float>(x.get(), 0);
-  else x->ad = member_arrays<double>(x.get(), 0);
-  // every array starts at zero: s and w at the ring stay zero as the
-  // reference's reset_tendencies and init_moloch leave them
-  e = cudaMemsetAsync(x->arena, 0, x->arena_bytes, x->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(x->stream);
-  if (e == cudaSuccess) e = mixed ? Launch<float>::configure_sound() : Launch<double>::configure_sound();
-  if (e == cudaSuccess) e = mixed ? Launch<float>::configure_advect() : Launch<double>::configure_advect();
-  if (e != cudaSuccess) {
-    cudaFree(x->arena);
-    cudaFree(x->staging);
-    cudaStreamDestroy(x->stream);
-    return cuda_status(e);
-  }
-  *out = x.release();
-  return MLC_OK;
+  return create_members(dims, 0, params, nmem, out);
+}
+
+int mlc_create_multi(const mlc_dims *dims, const mlc_params *params, int nmem, mlc_ctx **out) {
+  return create_members(dims, 1, params, nmem, out);
 }
 
 int mlc_create(const mlc_dims *dims, const mlc_params *params, mlc_ctx **out) {
-  return mlc_create_batch(dims, params, 1, out);
+  return create_members(dims, 0, params, 1, out);
 }
 
-static void drop_graphs(mlc_ctx *x) {
-  for (auto &gx : x->graph)
-    if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
+int mlc_create_pool(const mlc_params *params, int capacity, size_t budget_bytes, mlc_ctx **out) {
+  return create_common(params, capacity, budget_bytes, out);
 }
 
-static bool all_set(const std::vector<char> &v) {
-  for (char c : v)
-    if (!c) return false;
-  return true;
+int mlc_pool_add(mlc_ctx *x, const mlc_dims *dims, int *slot) {
+  if (!x || !dims || !slot) return MLC_ERR_INVALID;
+  *slot = -1;
+  for (size_t m = 0; m < x->mem.size(); ++m)
+    if (!x->mem[m].used) {
+      MLC_CHK(add_member(x, (int)m, *dims));
+      *slot = (int)m;
+      return MLC_OK;
+    }
+  return MLC_ERR_BUDGET;
 }
+
+int mlc_pool_remove(mlc_ctx *x, int slot) {
+  if (!member_ok(x, slot)) return MLC_ERR_INVALID;
+  return remove_member(x, slot);
+}
+
+size_t mlc_pool_bytes(const mlc_ctx *x) { return x ? x->in_use : 0; }
 
 int mlc_member_bind_static(mlc_ctx *x, int m, const mlc_static_ptrs *s) {
-  if (!x || !s || m < 0 || m >= x->nmem) return MLC_ERR_INVALID;
+  if (!member_ok(x, m) || !s) return MLC_ERR_INVALID;
   if (!s->zita) return MLC_ERR_INVALID;
-  const double rdz = 1.0 / s->zita[x->dims.kz - 1];
-  if (x->rdzita_set != 0.0 && rdz != x->rdzita_set) return MLC_ERR_INVALID;  // members share levels
-  drop_graphs(x);
-  x->c.rdzita = rdz;
-  x->rdzita_set = rdz;
-  int st;
-  if (x->prm.precision == MLC_PREC_MIXED) {
-    Arrays<float> a = member_arrays<float>(x, m);
-    st = bind_static_impl<float>(x, a, s);
-  } else {
-    Arrays<double> a = member_arrays<double>(x, m);
-    st = bind_static_impl<double>(x, a, s);
-  }
-  if (st == MLC_OK) x->m_static[m] = 1;
-  x->have_static = all_set(x->m_static);
+  Member &mb = x->mem[m];
+  const int st = x->mixed ? bind_static_impl<float>(x, mb, s) : bind_static_impl<double>(x, mb, s);
+  x->table_dirty = true;
+  if (st == MLC_OK) mb.have_static = true;
   return st;
 }
 
 int mlc_bind_static(mlc_ctx *x, const mlc_static_ptrs *s) { return mlc_member_bind_static(x, 0, s); }
 
 int mlc_member_upload_state(mlc_ctx *x, int m, const mlc_state_ptrs *h) {
-  if (!x || !h || m < 0 || m >= x->nmem) return MLC_ERR_INVALID;
-  int st;
-  if (x->prm.precision == MLC_PREC_MIXED) {
-    Arrays<float> a = member_arrays<float>(x, m);
-    st = upload_state_impl<float>(x, a, h);
-  } else {
-    Arrays<double> a = member_arrays<double>(x, m);
-    st = upload_state_impl<double>(x, a, h);
-  }
-  if (st == MLC_OK) x->m_state[m] = 1;
-  x->have_state = all_set(x->m_state);
+  if (!member_ok(x, m) || !h) return MLC_ERR_INVALID;
+  const int st = x->mixed ? upload_state_impl<float>(x, m, h) : upload_state_impl<double>(x, m, h);
+  if (st == MLC_OK) x->mem[m].have_state = true;
   return st;
 }
 
 int mlc_upload_state(mlc_ctx *x, const mlc_state_ptrs *h) { return mlc_member_upload_state(x, 0, h); }
 
 int mlc_member_download_state(mlc_ctx *x, int m, const mlc_state_ptrs *h) {
-  if (!x || !h || m < 0 || m >= x->nmem) return MLC_ERR_INVALID;
-  if (x->prm.precision == MLC_PREC_MIXED) {
-    Arrays<float> a = member_arrays<float>(x, m);
-    return download_state_impl<float>(x, a, h);
-  }
-  Arrays<double> a = member_arrays<double>(x, m);
-  return download_state_impl<double>(x, a, h);
+  if (!member_ok(x, m) || !h) return MLC_ERR_INVALID;
+  return x->mixed ? download_state_impl<float>(x, m, h) : download_state_impl<double>(x, m, h);
 }
 
 int mlc_download_state(mlc_ctx *x, const mlc_state_ptrs *h) {
   return mlc_member_download_state(x, 0, h);
 }
 
+// bdyin: new b0/b1 and the boundary clock.  The member's step counter, buffer
+// roles and non-finite flag are kept.
 int mlc_member_set_boundary(mlc_ctx *x, int m, const mlc_bdy_ptrs *b, double xbctime,
                             double dtbdys) {
-  if (!x || !b || !(dtbdys > 0) || m < 0 || m >= x->nmem) return MLC_ERR_INVALID;
-  if (x->nmem > 1 && x->dtbdys_set != 0.0 && dtbdys != x->dtbdys_set) return MLC_ERR_INVALID;
-  x->dtbdys_set = dtbdys;
-  x->prm.dtbdys = dtbdys;
-  x->c.dtbdys = dtbdys;
-  x->c.rtb = 1.0 / dtbdys;
-  drop_graphs(x);  // rtb/dtbdys are baked into recorded graphs
-  int st;
-  Clock *dclk;
-  if (x->prm.precision == MLC_PREC_MIXED) {
-    Arrays<float> a = member_arrays<float>(x, m);
-    st = set_boundary_impl<float>(x, a, b);
-    dclk = a.clk;
-  } else {
-    Arrays<double> a = member_arrays<double>(x, m);
-    st = set_boundary_impl<double>(x, a, b);
-    dclk = a.clk;
-  }
-  if (st != MLC_OK) return st;
-  Clock clk{};
-  clk.xbctime = xbctime;
-  MLC_TRY(cudaMemcpyAsync(dclk, &clk, sizeof(Clock), cudaMemcpyHostToDevice, x->stream));
+  if (!member_ok(x, m) || !b || !(dtbdys > 0)) return MLC_ERR_INVALID;
+  Member &mb = x->mem[m];
+  MLC_CHK(x->mixed ? set_boundary_impl<float>(x, mb, b) : set_boundary_impl<double>(x, mb, b));
+  int cst;
+  Clock ck = get_clock(x, m, &cst);
+  MLC_CHK(cst);
+  ck.xbctime = xbctime;
+  MLC_TRY(cudaMemcpyAsync(x->clks + m, &ck, sizeof(Clock), cudaMemcpyHostToDevice, x->stream));
   MLC_TRY(cudaStreamSynchronize(x->stream));
-  x->m_bdy[m] = 1;
-  x->have_bdy = all_set(x->m_bdy);
+  mb.c.dtbdys = dtbdys;
+  mb.c.rtb = 1.0 / dtbdys;
+  mb.have_bdy = true;
+  x->table_dirty = true;
   return MLC_OK;
 }
 
@@ -923,77 +1043,40 @@ int mlc_set_boundary(mlc_ctx *x, const mlc_bdy_ptrs *b, double xbctime, double d
   return mlc_member_set_boundary(x, 0, b, xbctime, dtbdys);
 }
 
-// Diagnostics of every member after the last step (out has nmem entries).
-static int fetch_diags(mlc_ctx *x, int nsteps, mlc_diag *out) {
-  const bool mixed = x->prm.precision == MLC_PREC_MIXED;
-  const char *diag0 = reinterpret_cast<const char *>(mixed ? (void *)x->af.diag : (void *)x->ad.diag);
-  const char *clk0 = reinterpret_cast<const char *>(mixed ? (void *)x->af.clk : (void *)x->ad.clk);
-  std::vector<DiagDev> dd(x->nmem);
-  std::vector<Clock> ck(x->nmem);
-  MLC_TRY(cudaMemcpy2DAsync(dd.data(), sizeof(DiagDev), diag0, x->member_bytes, sizeof(DiagDev),
-                            x->nmem, cudaMemcpyDeviceToHost, x->stream));
-  MLC_TRY(cudaMemcpy2DAsync(ck.data(), sizeof(Clock), clk0, x->member_bytes, sizeof(Clock),
-                            x->nmem, cudaMemcpyDeviceToHost, x->stream));
-  MLC_TRY(cudaStreamSynchronize(x->stream));
-  bool bad = false;
-  for (int m = 0; m < x->nmem; ++m) {
-    if (ck[m].nonfinite) bad = true;
-    if (!out) continue;
-    out[m].ps_max = dd[m].ps_max;
-    out[m].ps_min = dd[m].ps_min;
-    out[m].nonfinite = ck[m].nonfinite;
-    out[m].steps_done = nsteps;
-    out[m].drymass = dd[m].drymass;
-    out[m].dryadv = dd[m].dryadv;
-    out[m].qmass = dd[m].qmass;
-    out[m].qadv = dd[m].qadv;
-    out[m].xbctime = ck[m].xbctime;
-  }
-  return bad ? MLC_ERR_NONFINITE : MLC_OK;
-}
-
 int mlc_step_batch(mlc_ctx *x, int nsteps, mlc_diag *out) {
   if (!x || nsteps < 0) return MLC_ERR_INVALID;
-  if (!x->have_static || !x->have_state || (x->c.apply_bdy && !x->have_bdy)) return MLC_ERR_STATE;
-  const bool mixed = x->prm.precision == MLC_PREC_MIXED;
-  int st = mixed ? step_impl<float>(x, x->af, nsteps) : step_impl<double>(x, x->ad, nsteps);
-  if (st != MLC_OK) return st;
+  if (!ready(x)) return MLC_ERR_STATE;
+  MLC_CHK(step_any(x, nsteps));
   return fetch_diags(x, nsteps, out);
 }
 
 int mlc_step(mlc_ctx *x, int nsteps, mlc_diag *out) {
   if (!x) return MLC_ERR_INVALID;
-  if (x->nmem == 1) return mlc_step_batch(x, nsteps, out);
-  std::vector<mlc_diag> all(x->nmem);
-  int st = mlc_step_batch(x, nsteps, all.data());
+  std::vector<mlc_diag> all(x->mem.size());
+  const int st = mlc_step_batch(x, nsteps, all.data());
   if (out && st != MLC_ERR_INVALID && st != MLC_ERR_STATE) *out = all[0];
   return st;
 }
 
-int mlc_members(const mlc_ctx *x) { return x ? x->nmem : 0; }
+int mlc_members(const mlc_ctx *x) { return x ? (int)x->mem.size() : 0; }
 
-void mlc_destroy(mlc_ctx *x) {
-  if (!x) return;
-  for (auto &gx : x->graph)
-    if (gx) cudaGraphExecDestroy(gx);
-  if (x->stream) cudaStreamSynchronize(x->stream);
-  if (x->arena) cudaFree(x->arena);
-  if (x->staging) cudaFree(x->staging);
-  if (x->stream) cudaStreamDestroy(x->stream);
-  delete x;
-}
+void mlc_destroy(mlc_ctx *x) { release(x); }
 
 // mlc_step with the device time of the steps measured by CUDA events on the
 // context stream (bracketing exactly the step launches).
 int mlc_step_timed(mlc_ctx *x, int nsteps, mlc_diag *out, float *ms) {
-  if (!x || !ms) return MLC_ERR_INVALID;
-  if (!x->have_static || !x->have_state || (x->c.apply_bdy && !x->have_bdy)) return MLC_ERR_STATE;
+  if (!x || !ms || nsteps < 0) return MLC_ERR_INVALID;
+  if (!ready(x)) return MLC_ERR_STATE;
+  // descriptor upload and graph recording happen before the timed region
+  MLC_CHK(step_any(x, 0));
+  if (x->use_graphs && x->key.L.nmem > 0 &&
+      (!x->graph_valid || std::memcmp(&x->graph_key, &x->key, sizeof(GraphKey)) != 0))
+    MLC_CHK(x->mixed ? record<float>(x) : record<double>(x));
   cudaEvent_t e0, e1;
   MLC_TRY(cudaEventCreate(&e0));
   MLC_TRY(cudaEventCreate(&e1));
   MLC_TRY(cudaEventRecord(e0, x->stream));
-  const bool mixed = x->prm.precision == MLC_PREC_MIXED;
-  int st = mixed ? step_impl<float>(x, x->af, nsteps) : step_impl<double>(x, x->ad, nsteps);
+  int st = step_any(x, nsteps);
   if (st == MLC_OK) {
     cudaEventRecord(e1, x->stream);
     cudaEventSynchronize(e1);
@@ -1011,14 +1094,15 @@ int mlc_step_timed(mlc_ctx *x, int nsteps, mlc_diag *out, float *ms) {
 // launch group on the context stream).  Fills up to max_out entries.
 int mlc_profile_steps(mlc_ctx *x, int nsteps, mlc_kernel_time *out, int max_out, int *n_out) {
   if (!x || !out || !n_out) return MLC_ERR_INVALID;
-  if (!x->have_static || !x->have_state || (x->c.apply_bdy && !x->have_bdy)) return MLC_ERR_STATE;
+  if (!ready(x)) return MLC_ERR_STATE;
+  MLC_CHK(step_any(x, 0));
   Recorder rec;
   rec.s = x->stream;
-  const bool mixed = x->prm.precision == MLC_PREC_MIXED;
-  for (int n = 0; n < nsteps; ++n) {
-    if (mixed) enqueue_step<float>(x, x->af, &rec);
-    else enqueue_step<double>(x, x->ad, &rec);
-  }
+  if (x->key.L.nmem > 0)
+    for (int n = 0; n < nsteps; ++n) {
+      if (x->mixed) enqueue_step<float>(x, &rec);
+      else enqueue_step<double>(x, &rec);
+    }
   MLC_TRY(cudaStreamSynchronize(x->stream));
   int n = 0;
   for (auto &m : rec.marks) {
@@ -1052,25 +1136,25 @@ constexpr int kNCol = 6, kNSolve = 5, kNVert = 5, kNTile = 4;
 
 int group_of(const char *name) {
   if (!std::strcmp(name, "sound_solve")) return 1;
-  if (!std::strncmp(name, "adv_vertical", 12)) return 2;
-  if (!std::strncmp(name, "adv_horizontal", 14)) return 3;
+  if (!std::strcmp(name, "adv_vertical")) return 2;
+  if (!std::strcmp(name, "adv_horizontal")) return 3;
   if (!std::strcmp(name, "bdy_ring") || !std::strcmp(name, "end_reduce")) return -1;
   return 0;  // column kernels
 }
 
-bool shapes_fit(const Geom &g, int elem) {
-  const size_t col3 = (size_t)3 * (g.kz + 2) * sizeof(double);
-  if (col3 * g.solve_x * g.solve_y > 200 * 1024) return false;
-  if ((size_t)3 * (g.kz + 2) * elem * g.vert_x * g.vert_y > 200 * 1024) return false;
-  return g.col_x * g.col_y <= 1024;
+bool shapes_fit(const LaunchGeom &L) {
+  const size_t col3 = (size_t)3 * (L.kz + 2) * sizeof(double);
+  if (col3 * L.solve_x * L.solve_y > 200 * 1024) return false;
+  if (col3 * L.vert_x * L.vert_y > 200 * 1024) return false;
+  return L.col_x * L.col_y <= 1024;
 }
 
-// Per-group device time (ms) of `steps` eager steps with the shapes in x->g.
+// Per-group device time (ms) of `steps` eager steps with the shapes in x->key.L.
 template <class R>
-int time_groups(mlc_ctx *x, Arrays<R> &a, int steps, double ms[4]) {
+int time_groups(mlc_ctx *x, int steps, double ms[4]) {
   Recorder rec;
   rec.s = x->stream;
-  for (int n = 0; n < steps; ++n) enqueue_step<R>(x, a, &rec);
+  for (int n = 0; n < steps; ++n) enqueue_step<R>(x, &rec);
   MLC_TRY(cudaStreamSynchronize(x->stream));
   for (int q = 0; q < 4; ++q) ms[q] = 0.0;
   for (auto &m : rec.marks) {
@@ -1083,79 +1167,89 @@ int time_groups(mlc_ctx *x, Arrays<R> &a, int steps, double ms[4]) {
   return cuda_status(cudaGetLastError());
 }
 
+void set_shapes(LaunchGeom &L, int col, int solve, int vert, int tile) {
+  L.col_x = kColCand[col][0]; L.col_y = kColCand[col][1];
+  L.solve_x = kSolveCand[solve][0]; L.solve_y = kSolveCand[solve][1];
+  L.vert_x = kVertCand[vert][0]; L.vert_y = kVertCand[vert][1];
+  L.htile = tile;
+}
+
 template <class R>
-int autotune_impl(mlc_ctx *x, Arrays<R> &a, int steps, mlc_tune_report *rep) {
-  void *snap = nullptr;
-  if (cudaMalloc(&snap, x->arena_bytes) != cudaSuccess) {
+int autotune_impl(mlc_ctx *x, int steps, mlc_tune_report *rep) {
+  MLC_CHK(refresh<R>(x));
+  if (x->key.L.nmem == 0) return MLC_ERR_STATE;
+  // snapshot every member's arena and the clocks; each trial starts from it
+  size_t total = x->mem.size() * sizeof(Clock);
+  for (const Member &m : x->mem)
+    if (m.used) total += m.bytes;
+  char *snap = nullptr;
+  if (cudaMallocFromPoolAsync(reinterpret_cast<void **>(&snap), total, x->pool, x->stream) != cudaSuccess) {
     cudaGetLastError();
     return MLC_ERR_NOMEM;
   }
-  const int uv0 = x->uv_role, adv0 = x->adv_role;
-  MLC_TRY(cudaMemcpyAsync(snap, x->arena, x->arena_bytes, cudaMemcpyDeviceToDevice, x->stream));
-  auto restore = [&]() {
-    cudaMemcpyAsync(x->arena, snap, x->arena_bytes, cudaMemcpyDeviceToDevice, x->stream);
-    x->uv_role = uv0;
-    x->adv_role = adv0;
+  auto copy_all = [&](bool save) {
+    size_t off = 0;
+    for (const Member &m : x->mem) {
+      if (!m.used) continue;
+      if (save) cudaMemcpyAsync(snap + off, m.base, m.bytes, cudaMemcpyDeviceToDevice, x->stream);
+      else cudaMemcpyAsync(m.base, snap + off, m.bytes, cudaMemcpyDeviceToDevice, x->stream);
+      off += m.bytes;
+    }
+    const size_t nc = x->mem.size() * sizeof(Clock);
+    if (save) cudaMemcpyAsync(snap + off, x->clks, nc, cudaMemcpyDeviceToDevice, x->stream);
+    else cudaMemcpyAsync(x->clks, snap + off, nc, cudaMemcpyDeviceToDevice, x->stream);
   };
-  const Geom base = x->g;
+  copy_all(true);
+  const LaunchGeom base = x->key.L;
   double best[4] = {1e30, 1e30, 1e30, 1e30};
   int pick[4] = {0, 0, 0, 0};
   int st = MLC_OK;
   const int ntrial = 6;
   for (int tr = 0; tr < ntrial && st == MLC_OK; ++tr) {
-    Geom g = base;
-    g.col_x = kColCand[tr % kNCol][0]; g.col_y = kColCand[tr % kNCol][1];
-    g.solve_x = kSolveCand[tr % kNSolve][0]; g.solve_y = kSolveCand[tr % kNSolve][1];
-    g.vert_x = kVertCand[tr % kNVert][0]; g.vert_y = kVertCand[tr % kNVert][1];
-    g.htile = tr % kNTile;
-    const bool fit = shapes_fit(g, (int)sizeof(R));
-    if (!fit) {  // fall back to the base solve/vertical shapes for this trial
-      g.solve_x = base.solve_x; g.solve_y = base.solve_y;
-      g.vert_x = base.vert_x; g.vert_y = base.vert_y;
+    LaunchGeom L = base;
+    int idx[4] = {tr % kNCol, tr % kNSolve, tr % kNVert, tr % kNTile};
+    set_shapes(L, idx[0], idx[1], idx[2], idx[3]);
+    if (!shapes_fit(L)) {  // keep the base solve/vertical shapes for this trial
+      L.solve_x = base.solve_x; L.solve_y = base.solve_y;
+      L.vert_x = base.vert_x; L.vert_y = base.vert_y;
+      idx[1] = idx[2] = 0;
     }
-    x->g = g;
+    x->key.L = L;
     double ms[4];
-    restore();
-    st = time_groups<R>(x, a, 1, ms);  // first use of the shapes
+    copy_all(false);
+    st = time_groups<R>(x, 1, ms);  // first use of the shapes
     if (st != MLC_OK) break;
-    restore();
-    st = time_groups<R>(x, a, steps, ms);
+    copy_all(false);
+    st = time_groups<R>(x, steps, ms);
     if (st != MLC_OK) break;
-    const int idx[4] = {tr % kNCol, fit ? tr % kNSolve : 0, fit ? tr % kNVert : 0, tr % kNTile};
     for (int q = 0; q < 4; ++q)
       if (ms[q] < best[q]) { best[q] = ms[q]; pick[q] = idx[q]; }
   }
-  // the fixed reference configuration: 32 x 8 columns and tiles
-  Geom fixed = base;
-  fixed.col_x = 32; fixed.col_y = 8; fixed.htile = 0;
-  fixed.solve_x = 32; fixed.solve_y = 2; fixed.vert_x = 32; fixed.vert_y = 2;
+  // the fixed configuration: 32 x 8 columns and tiles, 32 x 2 solve/vertical
+  LaunchGeom fixed = base;
+  set_shapes(fixed, 1, 0, 0, 0);
   double msf[4] = {0, 0, 0, 0}, mst[4] = {0, 0, 0, 0};
   if (st == MLC_OK) {
-    x->g = fixed;
-    restore();
-    st = time_groups<R>(x, a, steps, msf);
+    x->key.L = fixed;
+    copy_all(false);
+    st = time_groups<R>(x, steps, msf);
   }
-  Geom tuned = base;
-  tuned.col_x = kColCand[pick[0]][0]; tuned.col_y = kColCand[pick[0]][1];
-  tuned.solve_x = kSolveCand[pick[1]][0]; tuned.solve_y = kSolveCand[pick[1]][1];
-  tuned.vert_x = kVertCand[pick[2]][0]; tuned.vert_y = kVertCand[pick[2]][1];
-  tuned.htile = pick[3];
-  if (!shapes_fit(tuned, (int)sizeof(R))) tuned = base;
+  LaunchGeom tuned = base;
+  set_shapes(tuned, pick[0], pick[1], pick[2], pick[3]);
+  if (!shapes_fit(tuned)) tuned = base;
   if (st == MLC_OK) {
-    x->g = tuned;
-    restore();
-    st = time_groups<R>(x, a, steps, mst);
+    x->key.L = tuned;
+    copy_all(false);
+    st = time_groups<R>(x, steps, mst);
   }
-  restore();
+  copy_all(false);
+  cudaFreeAsync(snap, x->stream);
   cudaStreamSynchronize(x->stream);
-  cudaFree(snap);
   if (st != MLC_OK) {
-    x->g = base;
+    x->key.L = base;
     return st;
   }
-  x->g = tuned;
-  for (auto &gx : x->graph)
-    if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
+  x->key.L = tuned;  // the graph is recorded again at the next step
   if (rep) {
     rep->col_x = tuned.col_x; rep->col_y = tuned.col_y;
     rep->solve_x = tuned.solve_x; rep->solve_y = tuned.solve_y;
@@ -1173,9 +1267,8 @@ extern "C" {
 
 int mlc_autotune(mlc_ctx *x, int steps, mlc_tune_report *rep) {
   if (!x || steps < 1) return MLC_ERR_INVALID;
-  if (!x->have_static || !x->have_state || (x->c.apply_bdy && !x->have_bdy)) return MLC_ERR_STATE;
-  return x->prm.precision == MLC_PREC_MIXED ? autotune_impl<float>(x, x->af, steps, rep)
-                                            : autotune_impl<double>(x, x->ad, steps, rep);
+  if (!ready(x)) return MLC_ERR_STATE;
+  return x->mixed ? autotune_impl<float>(x, steps, rep) : autotune_impl<double>(x, steps, rep);
 }
 
 // Kernels one mlc_step(ctx, 1) launches (for launch accounting).

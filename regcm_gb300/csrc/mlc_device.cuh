@@ -20,13 +20,6 @@ struct Geom {
   int jx, iy, kz, nqx, ntr;
   int P;        // row pitch in elements
   size_t PS;    // plane stride = P*iy
-  int nmem;       // ensemble members advanced by one launch (1 = one domain)
-  size_t mstride; // bytes between consecutive members' arenas
-  // launch shapes (picked by the autotuner; defaults in mlc_context.cu)
-  int col_x, col_y;      // column kernels (threads along j, i)
-  int solve_x, solve_y;  // sound_solve
-  int vert_x, vert_y;    // adv_vertical
-  int htile;             // adv_horizontal tile: 0 32x8, 1 32x4, 2 64x4, 3 16x8
   __host__ __device__ size_t at(int j, int i, int k) const {
     return (size_t)(j - 1) + (size_t)(i - 1) * (size_t)P + (size_t)(k - 1) * PS;
   }
@@ -92,12 +85,16 @@ struct Work {
   R *wx;       // w at half levels
 };
 
-// Boundary clock kept on the device so a captured step graph stays valid.
+// Boundary clock and buffer roles kept on the device, so a recorded step
+// graph replays unchanged: the last kernel of a step advances the clock and
+// flips the ping-pong roles.
 struct Clock {
   double xbctime;
   int nonfinite;     // sticky: set when a non-finite ps is seen
   int bad_step;      // step counter value at the first non-finite ps
   int step;          // steps completed since the last reset
+  int uv_role;       // half of the u/v pairs holding the state at step start
+  int adv_role;      // half of the advected-field pairs holding the state
   int pad;
 };
 
@@ -107,53 +104,40 @@ struct DiagDev {
   int nonfinite, pad;
 };
 
-// ---- ensemble members -----------------------------------------------------
-// Every array of member m lives at member 0's address plus m * mstride, so a
-// kernel that serves all members rebases its pointer arguments once.
-template <class T>
-__device__ __forceinline__ T *mshift(T *p, size_t off) {
-  return p ? reinterpret_cast<T *>(reinterpret_cast<char *>(p) + off) : p;
-}
-template <class T>
-__device__ __forceinline__ const T *mshift(const T *p, size_t off) {
-  return p ? reinterpret_cast<const T *>(reinterpret_cast<const char *>(p) + off) : p;
-}
-
+// ---- one member (domain) as the kernels see it -----------------------------
+// Both halves of every ping-pong pair are listed; the roles in *clk pick the
+// current half.  Members of one launch may have different extents.
+constexpr int kMaxFields = 24;
 template <class R>
-__device__ __forceinline__ void rebase(Stat<R> &s, size_t o) {
-  if (!o) return;
-  s.fmz = mshift(s.fmz, o); s.fmzf = mshift(s.fmzf, o); s.rfmzu = mshift(s.rfmzu, o);
-  s.rfmzv = mshift(s.rfmzv, o); s.fmz_d = mshift(s.fmz_d, o); s.fmzf_d = mshift(s.fmzf_d, o);
-  s.zrfmu = mshift(s.zrfmu, o); s.zrfmd = mshift(s.zrfmd, o); s.zeta = mshift(s.zeta, o);
-  s.dz = mshift(s.dz, o); s.hx = mshift(s.hx, o); s.hy = mshift(s.hy, o);
-  s.msfu = mshift(s.msfu, o); s.msfv = mshift(s.msfv, o); s.msfx = mshift(s.msfx, o);
-  s.mx2 = mshift(s.mx2, o); s.rmu = mshift(s.rmu, o); s.rmv = mshift(s.rmv, o);
-  s.coru = mshift(s.coru, o); s.corv = mshift(s.corv, o); s.ibnd_cr = mshift(s.ibnd_cr, o);
-  s.ibnd_ud = mshift(s.ibnd_ud, o); s.ibnd_vd = mshift(s.ibnd_vd, o); s.hefc = mshift(s.hefc, o);
-  s.fcx = mshift(s.fcx, o); s.tnudge = mshift(s.tnudge, o); s.ffilt = mshift(s.ffilt, o);
-  s.gzitakh = mshift(s.gzitakh, o); s.xkdamp = mshift(s.xkdamp, o); s.xknu = mshift(s.xknu, o);
-  s.gzitak = mshift(s.gzitak, o); s.rlat = mshift(s.rlat, o);
-}
+struct Dom {
+  Geom g;
+  Scal c;
+  Stat<R> sa;
+  Bdy<R> bd;
+  R *u[2], *v[2], *ux[2], *vx[2], *qx[2], *trac[2], *wx[2];
+  double *pai[2], *tetav[2];
+  R *w, *t, *tvirt, *p, *rho, *qsat;
+  double *ps;
+  R *s, *zdiv2;
+  double *tetavf;
+  R *wz[kMaxFields];     // per advected R field
+  double *wz_d[2];       // per advected FP64 field (theta_v, Exner) of a mixed member
+  Clock *clk;
+  DiagDev *diag;
+  double *partials;
+  int red_blocks, rows_per_block;
+  int active;            // 0: an empty slot, every block returns at once
+};
 
+// The state with the roles the launch works on.
 template <class R>
-__device__ __forceinline__ void rebase(State<R> &s, size_t o) {
-  if (!o) return;
-  s.u = mshift(s.u, o); s.v = mshift(s.v, o); s.w = mshift(s.w, o); s.t = mshift(s.t, o);
-  s.tvirt = mshift(s.tvirt, o); s.ux = mshift(s.ux, o); s.vx = mshift(s.vx, o);
-  s.p = mshift(s.p, o); s.rho = mshift(s.rho, o); s.qsat = mshift(s.qsat, o);
-  s.pai = mshift(s.pai, o); s.tetav = mshift(s.tetav, o); s.qx = mshift(s.qx, o);
-  s.trac = mshift(s.trac, o); s.ps = mshift(s.ps, o);
-}
-
-template <class R>
-__device__ __forceinline__ void rebase(Bdy<R> &b, size_t o) {
-  if (!o) return;
-  for (int q = 0; q < 2; ++q) {
-    b.xtb[q] = mshift(b.xtb[q], o); b.xqb[q] = mshift(b.xqb[q], o); b.xlb[q] = mshift(b.xlb[q], o);
-    b.xib[q] = mshift(b.xib[q], o); b.dub[q] = mshift(b.dub[q], o); b.dvb[q] = mshift(b.dvb[q], o);
-    b.chib[q] = mshift(b.chib[q], o); b.xpaib[q] = mshift(b.xpaib[q], o);
-    b.xpsb[q] = mshift(b.xpsb[q], o);
-  }
+__host__ __device__ __forceinline__ State<R> state_of(const Dom<R> &D, int uv, int adv) {
+  State<R> st;
+  st.u = D.u[uv]; st.v = D.v[uv]; st.w = D.w; st.t = D.t; st.tvirt = D.tvirt;
+  st.ux = D.ux[adv]; st.vx = D.vx[adv]; st.p = D.p; st.rho = D.rho; st.qsat = D.qsat;
+  st.pai = D.pai[adv]; st.tetav = D.tetav[adv]; st.qx = D.qx[adv]; st.trac = D.trac[adv];
+  st.ps = D.ps;
+  return st;
 }
 
 }  // namespace mlc

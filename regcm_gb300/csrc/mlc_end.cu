@@ -25,8 +25,12 @@ __device__ __forceinline__ R qfactor(const R *qx, size_t o, size_t F, int ipptls
 
 // dynamical_core :1121-1123 and tvirt_to_temp :1629-1648
 template <class R>
-__global__ void k_end_tvirt(Geom g, Scal c, State<R> st) {
-  rebase(st, (size_t)blockIdx.z * g.mstride);
+__global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const State<R> st = state_of(D, 0, (D.clk->adv_role + advoff) & 1);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
@@ -44,17 +48,19 @@ __global__ void k_end_tvirt(Geom g, Scal c, State<R> st) {
 // west/east columns (corners excluded), phase 1 the south/north rows
 // (corners included), which read the corner values phase 0 left.
 template <class R>
-__global__ void k_bdy_ring(Geom g, Scal c, State<R> st, Bdy<R> bd, const Clock *clk, int phase) {
+__global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int phase) {
+  const Dom<R> &D = doms[blockIdx.z >> 1];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Bdy<R> &bd = D.bd;
+  const Clock *clk = D.clk;
+  const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
   const int jx = g.jx, iy = g.iy;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;  // position along the side
   const int k = blockIdx.y + 1;
+  if (k > g.kz) return;                                  // a member with fewer levels
   const int side = blockIdx.z & 1;                       // 0 = west/south, 1 = east/north
-  {
-    const size_t mo = (size_t)(blockIdx.z >> 1) * g.mstride;
-    rebase(st, mo);
-    rebase(bd, mo);
-    clk = mshift(clk, mo);
-  }
   const double xb = clk->xbctime;
   const double x1 = (xb + c.dt) * c.rtb;
   const double x0 = 1.0 - x1;
@@ -128,14 +134,15 @@ __global__ void k_bdy_ring(Geom g, Scal c, State<R> st, Bdy<R> bd, const Clock *
 // (boundary, Main/mod_moloch.F90:478-497), per point; the clock has already
 // moved by dtsec.
 template <class R>
-__global__ void k_bdy_relax(Geom g, Scal c, Stat<R> sa, State<R> st, Bdy<R> bd, const Clock *clk) {
-  {
-    const size_t mo = (size_t)blockIdx.z * g.mstride;
-    rebase(sa, mo);
-    rebase(st, mo);
-    rebase(bd, mo);
-    clk = mshift(clk, mo);
-  }
+__global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const Bdy<R> &bd = D.bd;
+  const Clock *clk = D.clk;
+  const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
@@ -221,12 +228,13 @@ __global__ void k_bdy_relax(Geom g, Scal c, Stat<R> sa, State<R> st, Bdy<R> bd, 
 // rho, qsat.  rho and qsat of :348-352 are recomputed from the same t and p
 // by status_update, so they are computed once, after it.
 template <class R>
-__global__ void k_end_cross(Geom g, Scal c, Stat<R> sa, State<R> st) {
-  {
-    const size_t mo = (size_t)blockIdx.z * g.mstride;
-    rebase(sa, mo);
-    rebase(st, mo);
-  }
+__global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
@@ -298,12 +306,15 @@ __global__ void k_end_cross(Geom g, Scal c, Stat<R> sa, State<R> st) {
 
 // uvxtouvstag at the end of status_update (:1440)
 template <class R>
-__global__ void k_end_uvstag(Geom g, const R *__restrict__ ux, const R *__restrict__ vx,
-                             R *__restrict__ u, R *__restrict__ v) {
-  {
-    const size_t mo = (size_t)blockIdx.z * g.mstride;
-    ux = mshift(ux, mo); vx = mshift(vx, mo); u = mshift(u, mo); v = mshift(v, mo);
-  }
+__global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
+  const R *__restrict__ ux = D.ux[adv];
+  const R *__restrict__ vx = D.vx[adv];
+  R *__restrict__ u = D.u[uv];
+  R *__restrict__ v = D.v[uv];
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jx = g.jx, iy = g.iy;
@@ -352,16 +363,18 @@ __device__ double block_sum(double x, double *sh) {
 }
 
 template <class R>
-__global__ void __launch_bounds__(kRedThreads) k_reduce_partial(Geom g, Scal c, Stat<R> sa,
-                                                                State<R> st, double *part,
-                                                                int rows_per_block) {
+__global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__restrict__ doms,
+                                                                int uvoff, int advoff) {
   __shared__ double sh[kRedThreads];
-  {
-    const size_t mo = (size_t)blockIdx.y * g.mstride;
-    rebase(sa, mo);
-    rebase(st, mo);
-    part = mshift(part, mo);
-  }
+  const Dom<R> &D = doms[blockIdx.y];
+  if (!D.active) return;
+  if ((int)blockIdx.x >= D.red_blocks) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
+  double *part = D.partials;
+  const int rows_per_block = D.rows_per_block;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   const double dx = c.dx, dt = c.dt, dxsq = dx * dx;
   const size_t F = g.field3();
@@ -444,15 +457,19 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(Geom g, Scal c, 
   }
 }
 
-__global__ void k_reduce_final(const double *part, int nblocks, DiagDev *diag, Clock *clk,
-                               double dtsec, int apply_bdy, size_t mstride) {
+// Per member: add the partials in block order, store the diagnostics, then
+// advance the boundary clock and the buffer roles to the next step's.
+template <class R>
+__global__ void k_reduce_final(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
   if (threadIdx.x != 0) return;
-  {
-    const size_t mo = (size_t)blockIdx.x * mstride;
-    part = mshift(part, mo);
-    diag = mshift(diag, mo);
-    clk = mshift(clk, mo);
-  }
+  const Dom<R> &D = doms[blockIdx.x];
+  if (!D.active) return;
+  const double *part = D.partials;
+  const int nblocks = D.red_blocks;
+  DiagDev *diag = D.diag;
+  Clock *clk = D.clk;
+  const double dtsec = D.c.dtsec;
+  const int apply_bdy = D.c.apply_bdy;
   double a[4] = {0, 0, 0, 0}, pmax = -INFINITY, pmin = INFINITY;
   bool bad = false;
   for (int b = 0; b < nblocks; ++b) {
@@ -469,6 +486,8 @@ __global__ void k_reduce_final(const double *part, int nblocks, DiagDev *diag, C
   if (bad && !clk->nonfinite) { clk->nonfinite = 1; clk->bad_step = clk->step; }
   if (apply_bdy) clk->xbctime = clk->xbctime + dtsec;
   clk->step = clk->step + 1;
+  clk->uv_role = (clk->uv_role + uvoff) & 1;
+  clk->adv_role = (clk->adv_role + advoff) & 1;
 }
 
 template <class R>
@@ -499,62 +518,58 @@ inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
   return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y), (unsigned)nmem);
 }
 
-inline int rows_per_block(const Geom &g) {
+}  // namespace
+
+int reduce_rows_per_block(const Geom &g) {
   const int nrows = (g.iy - 1) * g.kz;
   const int target = 152 * 4;
   return (nrows + target - 1) / target;
 }
 
-}  // namespace
-
 int reduce_blocks(const Geom &g) {
   const int nrows = (g.iy - 1) * g.kz;
-  const int rpb = rows_per_block(g);
+  const int rpb = reduce_rows_per_block(g);
   return (nrows + rpb - 1) / rpb;
 }
 
 template <class R>
-void Launch<R>::end_tvirt(const Geom &g, const Scal &c, const State<R> &st, cudaStream_t s) {
-  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
-  k_end_tvirt<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, c, st);
+void Launch<R>::end_tvirt(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  k_end_tvirt<R><<<grid2(L.jx - 1, L.iy - 1, b, L.nmem), b, 0, s>>>(d, advoff);
 }
 
 template <class R>
-void Launch<R>::bdy_ring(const Geom &g, const Scal &c, const State<R> &st, const Bdy<R> &bd,
-                         const Clock *clk, cudaStream_t s) {
-  const int nwe = g.iy - 2, nsn = g.jx;
-  const unsigned zz = 2u * (unsigned)g.nmem;
-  k_bdy_ring<R><<<dim3((unsigned)((nwe + 63) / 64), (unsigned)g.kz, zz), 64, 0, s>>>(g, c, st, bd, clk, 0);
-  k_bdy_ring<R><<<dim3((unsigned)((nsn + 63) / 64), (unsigned)g.kz, zz), 64, 0, s>>>(g, c, st, bd, clk, 1);
+void Launch<R>::bdy_ring(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+  const int nwe = L.iy - 2, nsn = L.jx;
+  const unsigned zz = 2u * (unsigned)L.nmem;
+  k_bdy_ring<R><<<dim3((unsigned)((nwe + 63) / 64), (unsigned)L.kz, zz), 64, 0, s>>>(d, uvoff, advoff, 0);
+  k_bdy_ring<R><<<dim3((unsigned)((nsn + 63) / 64), (unsigned)L.kz, zz), 64, 0, s>>>(d, uvoff, advoff, 1);
 }
 
 template <class R>
-void Launch<R>::bdy_relax(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                          const Bdy<R> &bd, const Clock *clk, cudaStream_t s) {
-  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
-  k_bdy_relax<R><<<grid2(g.jx - 2, g.iy - 2, b, g.nmem), b, 0, s>>>(g, c, sa, st, bd, clk);
+void Launch<R>::bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  k_bdy_relax<R><<<grid2(L.jx - 2, L.iy - 2, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R>
-void Launch<R>::end_cross(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                          cudaStream_t s) {
-  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
-  k_end_cross<R><<<grid2(g.jx - 1, g.iy - 1, b, g.nmem), b, 0, s>>>(g, c, sa, st);
+void Launch<R>::end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  k_end_cross<R><<<grid2(L.jx - 1, L.iy - 1, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R>
-void Launch<R>::end_uvstag(const Geom &g, const State<R> &st, cudaStream_t s) {
-  const dim3 b((unsigned)g.col_x, (unsigned)g.col_y);
-  k_end_uvstag<R><<<grid2(g.jx, g.iy, b, g.nmem), b, 0, s>>>(g, st.ux, st.vx, st.u, st.v);
+void Launch<R>::end_uvstag(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  k_end_uvstag<R><<<grid2(L.jx, L.iy, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R>
-void Launch<R>::end_reduce(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                           double *partials, int nblocks, DiagDev *diag, Clock *clk, cudaStream_t s) {
-  k_reduce_partial<R><<<dim3((unsigned)nblocks, (unsigned)g.nmem), kRedThreads, 0, s>>>(
-      g, c, sa, st, partials, rows_per_block(g));
-  k_reduce_final<<<(unsigned)g.nmem, 32, 0, s>>>(partials, nblocks, diag, clk, c.dtsec, c.apply_bdy,
-                                                 g.mstride);
+void Launch<R>::end_reduce(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                           cudaStream_t s) {
+  k_reduce_partial<R><<<dim3((unsigned)L.red_blocks, (unsigned)L.nmem), kRedThreads, 0, s>>>(
+      d, uvoff, advoff);
+  k_reduce_final<R><<<(unsigned)L.nmem, 32, 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R>

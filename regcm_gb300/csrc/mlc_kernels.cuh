@@ -1,4 +1,12 @@
 // mlc_kernels.cuh -- launch interface between the step driver and the kernels.
+//
+// Every kernel serves all members of a context in one launch: blockIdx.z (or
+// blockIdx.y for the reduction) selects the member, whose descriptor Dom<R>
+// (extents, parameters, pointers) sits in a device array.  Grids cover the
+// largest member; blocks outside a smaller member's extent return at once.
+// Buffer roles are read from each member's device clock plus the offsets a
+// launch passes (uvoff acoustic substeps, advoff advection rounds since the
+// step began), so one recorded graph replays every step.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -6,22 +14,16 @@
 
 namespace mlc {
 
-// Advected fields of one advection step: each is read from `cur`, its two
-// vertical WAF passes go to `wz`, and the horizontal passes write `out`.
-constexpr int kMaxAdv = 24;
-template <class R>
-struct AdvTable {
-  const R *cur[kMaxAdv];
-  R *wz[kMaxAdv];
-  R *out[kMaxAdv];
-  int n;
-};
-
-// Buffers of one substep of the acoustic loop.
-template <class R>
-struct SoundBufs {
-  const R *u_in, *v_in;  // state at the start of the substep (ud, vd)
-  R *u_out, *v_out;      // state at its end
+// Extents of a launch (maxima over the members) and the launch shapes.
+struct LaunchGeom {
+  int jx, iy, kz, nmem;
+  int col_x, col_y;      // column kernels
+  int solve_x, solve_y;  // sound_solve
+  int vert_x, vert_y;    // adv_vertical
+  int htile;             // adv_horizontal tile: 0 32x8, 1 32x4, 2 64x4, 3 16x8
+  int nadv_r;            // advected fields of type R per member
+  int nadv_d;            // advected FP64 fields per member (mixed: theta_v, Exner)
+  int red_blocks;        // reduction blocks of the largest member
 };
 
 template <class R> struct Launch {
@@ -29,47 +31,37 @@ template <class R> struct Launch {
   static cudaError_t configure_sound();
   static cudaError_t configure_advect();
   // ---- sound (Main/mod_moloch.F90:545-765) ----
-  static void sound_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s);
-  static void sound_div(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                        const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s);
-  static void sound_solve(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                          const Work<R> &wk, bool last, cudaStream_t s);
-  static void sound_momentum(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                             const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s);
+  static void sound_prep(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
+  static void sound_div(const LaunchGeom &L, const Dom<R> *d, int uvoff, cudaStream_t s);
+  static void sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, bool last,
+                          cudaStream_t s);
+  static void sound_momentum(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                             cudaStream_t s);
   // ---- advection (Main/mod_moloch.F90:767-1042) ----
-  static void adv_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s);
-  static void adv_vertical(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
-                           const AdvTable<R> &t, cudaStream_t s);
-  static void adv_horizontal(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                             const AdvTable<R> &t, cudaStream_t s);
-  // the same two passes for FP64 fields advected with this domain's winds
-  static void adv_vertical_f64(const Geom &g, const Scal &c, const Stat<R> &sa, const Work<R> &wk,
-                               const AdvTable<double> &t, cudaStream_t s);
-  static void adv_horizontal_f64(const Geom &g, const Scal &c, const Stat<R> &sa,
-                                 const State<R> &st, const AdvTable<double> &t, cudaStream_t s);
-  static void adv_curvature(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                            cudaStream_t s);
-  static void adv_back(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s);
+  static void adv_prep(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  static void adv_vertical(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
+  static void adv_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                             cudaStream_t s);
+  static void adv_species_copy(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
+  static void adv_curvature(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
+  static void adv_back(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   // ---- step end (Main/mod_moloch.F90:340-446, mod_bdycod.F90) ----
-  static void end_tvirt(const Geom &g, const Scal &c, const State<R> &st, cudaStream_t s);
-  static void bdy_ring(const Geom &g, const Scal &c, const State<R> &st, const Bdy<R> &bd,
-                       const Clock *clk, cudaStream_t s);
-  static void bdy_relax(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                        const Bdy<R> &bd, const Clock *clk, cudaStream_t s);
-  static void end_cross(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                        cudaStream_t s);
-  static void end_uvstag(const Geom &g, const State<R> &st, cudaStream_t s);
-  static void end_reduce(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                         double *partials, int nblocks, DiagDev *diag, Clock *clk,
+  static void end_tvirt(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
+  static void bdy_ring(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  static void bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  static void end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  static void end_uvstag(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  static void end_reduce(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                          cudaStream_t s);
-  // ---- layout conversion ----
+  // ---- layout conversion (one member, from the host) ----
   static void unpack3(const double *src, R *dst, const Geom &g, int nj, int ni, int nk,
                       cudaStream_t s);
   static void pack3(const R *src, double *dst, const Geom &g, int nj, int ni, int nk,
                     cudaStream_t s);
 };
 
-// Blocks the reduction of end_reduce uses for a geometry.
+// Reduction blocks and rows per block the mass budget uses for a geometry.
 int reduce_blocks(const Geom &g);
+int reduce_rows_per_block(const Geom &g);
 
 }  // namespace mlc

@@ -34,10 +34,13 @@ __device__ __forceinline__ double relax_weight(const int32_t *ibnd, const double
 }
 
 template <class R>
-__global__ void k_sound_prep(Geom g, const double *__restrict__ tetav, double *__restrict__ tetavf) {
-  const size_t mo = (size_t)blockIdx.z * g.mstride;
-  tetav = mshift(tetav, mo);
-  tetavf = mshift(tetavf, mo);
+__global__ void k_sound_prep(const Dom<R> *__restrict__ doms, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const double *__restrict__ tetav = D.tetav[adv];
+  double *__restrict__ tetavf = D.tetavf;
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
@@ -52,12 +55,18 @@ __global__ void k_sound_prep(Geom g, const double *__restrict__ tetav, double *_
 
 // Main/mod_moloch.F90:582-618
 template <class R>
-__global__ void k_sound_div(Geom g, Scal c, Stat<R> sa, const R *__restrict__ u,
-                            const R *__restrict__ v, R *__restrict__ zdiv2, R *__restrict__ s,
-                            R *__restrict__ w) {
-  const size_t mo = (size_t)blockIdx.z * g.mstride;
-  rebase(sa, mo);
-  u = mshift(u, mo); v = mshift(v, mo); zdiv2 = mshift(zdiv2, mo); s = mshift(s, mo); w = mshift(w, mo);
+__global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int uv = (D.clk->uv_role + uvoff) & 1;
+  const R *__restrict__ u = D.u[uv];
+  const R *__restrict__ v = D.v[uv];
+  R *__restrict__ zdiv2 = D.zdiv2;
+  R *__restrict__ s = D.s;
+  R *__restrict__ w = D.w;
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
@@ -107,10 +116,19 @@ __global__ void k_sound_div(Geom g, Scal c, Stat<R> sa, const R *__restrict__ u,
 // kept in shared memory laid out [level][thread] (consecutive threads hit
 // consecutive banks).  The recurrence runs in FP64 for either field type.
 template <class R>
-__global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ zraw,
-                              R *__restrict__ s, R *__restrict__ w, double *__restrict__ pai,
-                              const double *__restrict__ tetav, double *__restrict__ tetavf,
-                              int last) {
+__global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const R *__restrict__ zraw = D.zdiv2;
+  R *__restrict__ s = D.s;
+  R *__restrict__ w = D.w;
+  double *__restrict__ pai = D.pai[adv];
+  const double *__restrict__ tetav = D.tetav[adv];
+  double *__restrict__ tetavf = D.tetavf;
   extern __shared__ double smem[];
   const int nth = blockDim.x * blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
@@ -119,10 +137,6 @@ __global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ 
   double *wp = smem + (size_t)(kz + 2) * nth;      // w after elimination, then final
   double *wk = smem + (size_t)2 * (kz + 2) * nth;  // elimination multipliers
 #define COL(a, k) a[(size_t)(k) * nth + tid]
-  const size_t mo = (size_t)blockIdx.z * g.mstride;
-  rebase(sa, mo);
-  zraw = mshift(zraw, mo); s = mshift(s, mo); w = mshift(w, mo); pai = mshift(pai, mo);
-  tetav = mshift(tetav, mo); tetavf = mshift(tetavf, mo);
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (j > g.jx - 2 || i > g.iy - 2) return;
@@ -208,14 +222,21 @@ __global__ void k_sound_solve(Geom g, Scal c, Stat<R> sa, const R *__restrict__ 
 
 // Main/mod_moloch.F90:677-721 with divergence_damping :738-765 folded in
 template <class R>
-__global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict__ u_in,
-                                 const R *__restrict__ v_in, R *__restrict__ u_out,
-                                 R *__restrict__ v_out, const R *__restrict__ zraw,
-                                 const double *__restrict__ pai, const double *__restrict__ tetav) {
-  const size_t mo = (size_t)blockIdx.z * g.mstride;
-  rebase(sa, mo);
-  u_in = mshift(u_in, mo); v_in = mshift(v_in, mo); u_out = mshift(u_out, mo);
-  v_out = mshift(v_out, mo); zraw = mshift(zraw, mo); pai = mshift(pai, mo); tetav = mshift(tetav, mo);
+__global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int uv = (D.clk->uv_role + uvoff) & 1;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const R *__restrict__ u_in = D.u[uv];
+  const R *__restrict__ v_in = D.v[uv];
+  R *__restrict__ u_out = D.u[uv ^ 1];
+  R *__restrict__ v_out = D.v[uv ^ 1];
+  const R *__restrict__ zraw = D.zdiv2;
+  const double *__restrict__ pai = D.pai[adv];
+  const double *__restrict__ tetav = D.tetav[adv];
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx || i > g.iy) return;
@@ -278,42 +299,39 @@ __global__ void k_sound_momentum(Geom g, Scal c, Stat<R> sa, const R *__restrict
   }
 }
 
-inline dim3 col_block(const Geom &g) { return dim3((unsigned)g.col_x, (unsigned)g.col_y); }
-inline dim3 col_grid(const Geom &g, int nj, int ni) {
-  return dim3((unsigned)((nj + g.col_x - 1) / g.col_x), (unsigned)((ni + g.col_y - 1) / g.col_y),
-              (unsigned)g.nmem);
+inline dim3 col_block(const LaunchGeom &L) { return dim3((unsigned)L.col_x, (unsigned)L.col_y); }
+inline dim3 col_grid(const LaunchGeom &L, int nj, int ni) {
+  return dim3((unsigned)((nj + L.col_x - 1) / L.col_x), (unsigned)((ni + L.col_y - 1) / L.col_y),
+              (unsigned)L.nmem);
 }
 
 }  // namespace
 
 template <class R>
-void Launch<R>::sound_prep(const Geom &g, const State<R> &st, const Work<R> &wk, cudaStream_t s) {
-  k_sound_prep<R><<<col_grid(g, g.jx - 1, g.iy - 1), col_block(g), 0, s>>>(g, st.tetav, wk.tetavf);
+void Launch<R>::sound_prep(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
+  k_sound_prep<R><<<col_grid(L, L.jx - 1, L.iy - 1), col_block(L), 0, s>>>(d, advoff);
 }
 
 template <class R>
-void Launch<R>::sound_div(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                          const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s) {
-  k_sound_div<R><<<col_grid(g, g.jx - 1, g.iy - 1), col_block(g), 0, s>>>(
-      g, c, sa, b.u_in, b.v_in, wk.zdiv2, wk.s, st.w);
+void Launch<R>::sound_div(const LaunchGeom &L, const Dom<R> *d, int uvoff, cudaStream_t s) {
+  k_sound_div<R><<<col_grid(L, L.jx - 1, L.iy - 1), col_block(L), 0, s>>>(d, uvoff);
 }
 
 template <class R>
-void Launch<R>::sound_solve(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                            const Work<R> &wk, bool last, cudaStream_t s) {
-  const dim3 blk((unsigned)g.solve_x, (unsigned)g.solve_y);
-  const size_t smem = (size_t)3 * (g.kz + 2) * blk.x * blk.y * sizeof(double);
-  const dim3 grd((unsigned)((g.jx - 3 + blk.x - 1) / blk.x), (unsigned)((g.iy - 3 + blk.y - 1) / blk.y),
-                 (unsigned)g.nmem);
-  k_sound_solve<R><<<grd, blk, smem, s>>>(g, c, sa, wk.zdiv2, wk.s, st.w, st.pai, st.tetav,
-                                          wk.tetavf, last ? 1 : 0);
+void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, bool last,
+                            cudaStream_t s) {
+  (void)uvoff;
+  const dim3 blk((unsigned)L.solve_x, (unsigned)L.solve_y);
+  const size_t smem = (size_t)3 * (L.kz + 2) * blk.x * blk.y * sizeof(double);
+  const dim3 grd((unsigned)((L.jx - 3 + blk.x - 1) / blk.x), (unsigned)((L.iy - 3 + blk.y - 1) / blk.y),
+                 (unsigned)L.nmem);
+  k_sound_solve<R><<<grd, blk, smem, s>>>(d, advoff, last ? 1 : 0);
 }
 
 template <class R>
-void Launch<R>::sound_momentum(const Geom &g, const Scal &c, const Stat<R> &sa, const State<R> &st,
-                               const Work<R> &wk, const SoundBufs<R> &b, cudaStream_t s) {
-  k_sound_momentum<R><<<col_grid(g, g.jx, g.iy), col_block(g), 0, s>>>(
-      g, c, sa, b.u_in, b.v_in, b.u_out, b.v_out, wk.zdiv2, st.pai, st.tetav);
+void Launch<R>::sound_momentum(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                               cudaStream_t s) {
+  k_sound_momentum<R><<<col_grid(L, L.jx, L.iy), col_block(L), 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R>

@@ -19,7 +19,7 @@ import ctypes as C
 from . import abi
 from .abi import MolochError
 
-__all__ = ["MolochDomain", "MolochBatch", "MolochError", "CFLViolation", "allocate_moloch",
+__all__ = ["MolochDomain", "MolochBatch", "MolochPool", "MolochError", "CFLViolation", "allocate_moloch",
            "init_moloch", "moloch"]
 
 
@@ -88,9 +88,33 @@ class MolochDomain:
             pass
 
 
+_SHARED_PARAMS = ("dtsec", "dx", "mo_ztop", "mo_h", "mo_a0", "mo_nadv", "mo_nsound",
+                  "mo_divdamp", "mo_divfilter", "mo_top_nudge", "mo_spectral_nudge",
+                  "do_apply_bdy", "lrotllr", "ipptls", "present_qc", "present_qi", "nspgx",
+                  "nspgd", "debug_level", "precision")
+
+
+def _same_params(a: abi.mlc_params, b: abi.mlc_params) -> bool:
+    """Members of one context share every parameter but the per-domain ones
+    (nztop follows each domain's levels, dtbdys comes with its boundary)."""
+    return all(getattr(a, f) == getattr(b, f) for f in _SHARED_PARAMS)
+
+
+def _load_member(lib, ctx, m, c, keep):
+    sp, bp = c.static_ptrs(), c.bdy_ptrs()
+    keep += [sp, bp]
+    abi.check(lib.mlc_member_bind_static(ctx, m, C.byref(sp)), "init_moloch")
+    abi.check(lib.mlc_member_upload_state(ctx, m, C.byref(c.state_ptrs())), "init_moloch(state)")
+    if c.params.do_apply_bdy:
+        abi.check(lib.mlc_member_set_boundary(ctx, m, C.byref(bp), c.xbctime, c.params.dtbdys),
+                  "bdyin")
+
+
 class MolochBatch:
-    """An ensemble: nmem domains of the same extents and parameters advanced by
-    the same kernel launches (one launch per kernel stage for all members)."""
+    """Domains advanced by the same kernel launches (one launch per kernel
+    stage for all members).  Members share the run parameters; their extents
+    may differ (an uneven batch), in which case each launch covers the
+    largest member and smaller members' blocks return at once."""
 
     def __init__(self, cases):
         if not cases:
@@ -98,20 +122,23 @@ class MolochBatch:
         self.lib = abi.load()
         self.cases = list(cases)
         c0 = self.cases[0]
+        for c in self.cases[1:]:
+            if not _same_params(c.params, c0.params):
+                raise ValueError(f"member {c.name} does not share the run parameters of {c0.name}")
         self.dims, self.params = c0.dims, c0.params
         self._ctx = C.c_void_p()
-        abi.check(self.lib.mlc_create_batch(C.byref(c0.dims), C.byref(c0.params), len(self.cases),
-                                            C.byref(self._ctx)), "allocate_moloch(batch)")
+        n = len(self.cases)
+        same = all(tuple(c.dims.as_tuple()) == tuple(c0.dims.as_tuple()) for c in self.cases)
+        if same:
+            st = self.lib.mlc_create_batch(C.byref(c0.dims), C.byref(c0.params), n,
+                                           C.byref(self._ctx))
+        else:
+            arr = (abi.mlc_dims * n)(*[c.dims for c in self.cases])
+            st = self.lib.mlc_create_multi(arr, C.byref(c0.params), n, C.byref(self._ctx))
+        abi.check(st, "allocate_moloch(batch)")
         self._keep = []
         for m, c in enumerate(self.cases):
-            sp, bp = c.static_ptrs(), c.bdy_ptrs()
-            self._keep += [sp, bp]
-            abi.check(self.lib.mlc_member_bind_static(self._ctx, m, C.byref(sp)), "init_moloch")
-            abi.check(self.lib.mlc_member_upload_state(self._ctx, m, C.byref(c.state_ptrs())),
-                      "init_moloch(state)")
-            if c.params.do_apply_bdy:
-                abi.check(self.lib.mlc_member_set_boundary(self._ctx, m, C.byref(bp), c.xbctime,
-                                                           c.params.dtbdys), "bdyin")
+            _load_member(self.lib, self._ctx, m, c, self._keep)
 
     @property
     def nmem(self) -> int:
@@ -124,6 +151,13 @@ class MolochBatch:
             raise CFLViolation(st, "moloch(batch)")
         abi.check(st, "moloch(batch)")
         return list(diags)
+
+    def step_timed(self, nsteps: int = 1) -> float:
+        """Steps every member; returns the device milliseconds of the steps."""
+        ms = C.c_float()
+        d = abi.mlc_diag()
+        abi.check(self.lib.mlc_step_timed(self._ctx, nsteps, C.byref(d), C.byref(ms)), "moloch")
+        return ms.value
 
     def download(self, m: int, state_ptrs: abi.mlc_state_ptrs):
         abi.check(self.lib.mlc_member_download_state(self._ctx, m, C.byref(state_ptrs)),
@@ -142,6 +176,78 @@ class MolochBatch:
         rep = abi.mlc_tune_report()
         abi.check(self.lib.mlc_autotune(self._ctx, steps_per_trial, C.byref(rep)), "autotune")
         return rep.as_dict()
+
+    def close(self):
+        if self._ctx:
+            self.lib.mlc_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MolochPool:
+    """A serving pool: `capacity` member slots whose domains join and leave
+    between steps (continuous batching), under a bound on the device bytes
+    all member arenas hold.  ``join`` returns the slot or None when the
+    budget or the slots are exhausted."""
+
+    def __init__(self, params: abi.mlc_params, capacity: int, budget_bytes: int = 0):
+        self.lib = abi.load()
+        self.params = params
+        self._ctx = C.c_void_p()
+        abi.check(self.lib.mlc_create_pool(C.byref(params), capacity, budget_bytes,
+                                           C.byref(self._ctx)), "mlc_create_pool")
+        self.capacity = capacity
+        self.cases = {}
+        self._keep = {}
+
+    def footprint(self, dims: abi.mlc_dims) -> int:
+        return self.lib.mlc_member_footprint(C.byref(dims), C.byref(self.params))
+
+    def bytes_in_use(self) -> int:
+        return self.lib.mlc_pool_bytes(self._ctx)
+
+    def join(self, case):
+        if not _same_params(case.params, self.params):
+            raise ValueError(f"{case.name} does not share the pool's run parameters")
+        slot = C.c_int(-1)
+        st = self.lib.mlc_pool_add(self._ctx, C.byref(case.dims), C.byref(slot))
+        if st == abi.MLC_ERR_BUDGET:
+            return None
+        abi.check(st, "mlc_pool_add")
+        keep = []
+        try:
+            _load_member(self.lib, self._ctx, slot.value, case, keep)
+        except Exception:
+            self.lib.mlc_pool_remove(self._ctx, slot.value)
+            raise
+        self.cases[slot.value] = case
+        self._keep[slot.value] = keep
+        return slot.value
+
+    def leave(self, slot: int):
+        abi.check(self.lib.mlc_pool_remove(self._ctx, slot), "mlc_pool_remove")
+        self.cases.pop(slot, None)
+        self._keep.pop(slot, None)
+
+    def step(self, nsteps: int = 1):
+        diags = (abi.mlc_diag * self.capacity)()
+        st = self.lib.mlc_step_batch(self._ctx, nsteps, diags)
+        if st == abi.MLC_ERR_NONFINITE:
+            raise CFLViolation(st, "moloch(pool)")
+        abi.check(st, "moloch(pool)")
+        return list(diags)
+
+    def download(self, slot: int, state_ptrs: abi.mlc_state_ptrs):
+        abi.check(self.lib.mlc_member_download_state(self._ctx, slot, C.byref(state_ptrs)),
+                  "download")
+
+    def launches_per_step(self) -> int:
+        return self.lib.mlc_launches_per_step(self._ctx)
 
     def close(self):
         if self._ctx:

@@ -1,0 +1,180 @@
+"""Serving MOLOCH integrations: admission by device-memory footprint and
+continuous batching over one ``MolochPool``.
+
+A request is an initial state (a ``Case``) and a number of model steps.
+Requests wait in arrival order; the head of the queue joins the pool as soon
+as its arena fits the byte budget and a slot is free (first come, first
+served: a large request at the head is not overtaken).  Every iteration
+advances all resident members by one model step with one graph launch; a
+member that has done its steps is copied back to the host and leaves, and its
+bytes go to the next request in the queue.  A member's result does not
+depend on the other members, so a request gets the same answer alone and in
+the mix.
+
+No counterpart in the reference, where each integration is a separate run of
+the model executable (Main/mod_regcm_interface.F90).
+"""
+from __future__ import annotations
+
+import time
+from collections import deque
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .moloch import MolochPool, domain_from_case
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float            # seconds after the start of the stream
+    steps: int
+    make: object              # callable returning the request's Case
+    case: object = None
+    slot: int = -1
+    done_steps: int = 0
+    t_admit: float = 0.0
+    t_done: float = 0.0
+    result: dict = field(default_factory=dict)
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.arrival
+
+
+def poisson_arrivals(rate: float, n: int, seed: int) -> np.ndarray:
+    """n arrival times of a Poisson stream of `rate` per second."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, n))
+
+
+def _prefetch(reqs, pool_exec, depth):
+    """Build the next `depth` requests' cases in worker threads (the client
+    preparing its payload before it arrives)."""
+    futures = {}
+    nxt = 0
+
+    def fill():
+        nonlocal nxt
+        while nxt < len(reqs) and len(futures) < depth:
+            r = reqs[nxt]
+            futures[r.rid] = pool_exec.submit(r.make)
+            nxt += 1
+
+    def get(r):
+        fill()
+        c = futures.pop(r.rid).result()
+        fill()
+        return c
+
+    fill()
+    return get
+
+
+def serve_stream(reqs, params, budget_bytes: int, capacity: int = 256,
+                 keep_results: bool = False, prefetch: int = 8, workers: int = 8):
+    """Serve `reqs` (sorted by arrival) in real time.  Returns a summary dict;
+    each request gets t_admit, t_done and (keep_results) its final state."""
+    pool = MolochPool(params, capacity, budget_bytes)
+    queue = deque()
+    active = {}
+    pending = deque(reqs)
+    ex = ThreadPoolExecutor(max_workers=workers)
+    get_case = _prefetch(reqs, ex, prefetch)
+    steps_run = 0
+    gp_steps = 0
+    max_resident = 0
+    late = 0.0
+    t0 = time.perf_counter()
+
+    def now():
+        return time.perf_counter() - t0
+
+    while pending or queue or active:
+        t = now()
+        while pending and pending[0].arrival <= t:
+            r = pending.popleft()
+            r.case = get_case(r)
+            late = max(late, now() - r.arrival)
+            queue.append(r)
+        # admission in arrival order while the head fits
+        while queue:
+            r = queue[0]
+            slot = pool.join(r.case)
+            if slot is None:
+                if not active:
+                    raise ValueError(f"request {r.rid} needs {pool.footprint(r.case.dims)} bytes, "
+                                     f"more than the budget of {budget_bytes}")
+                break
+            queue.popleft()
+            r.slot = slot
+            r.t_admit = now()
+            active[slot] = r
+        if not active:
+            if pending:
+                dt = pending[0].arrival - now()
+                if dt > 0:
+                    time.sleep(dt)
+            continue
+        pool.step(1)
+        steps_run += 1
+        max_resident = max(max_resident, len(active))
+        for slot in list(active):
+            r = active[slot]
+            r.done_steps += 1
+            gp_steps += r.case.points
+            if r.done_steps >= r.steps:
+                out = r.case.empty_state() if keep_results else {"ps": r.case.empty_state()["ps"]}
+                pool.download(slot, r.case.state_ptrs_of(out))
+                r.t_done = now()
+                if keep_results:
+                    r.result = out
+                pool.leave(slot)
+                del active[slot]
+                r.case = None  # release the host arrays
+    makespan = now()
+    ex.shutdown()
+    pool.close()
+    lat = np.array([r.latency for r in reqs])
+    return {"requests": len(reqs), "makespan_s": makespan, "gp_steps": gp_steps,
+            "value": gp_steps / makespan, "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+            "pool_steps": steps_run, "max_resident": max_resident,
+            "max_payload_lag_s": late}
+
+
+def serve_one_at_a_time(reqs, make_fp64, workers: int = 8, prefetch: int = 4):
+    """The same stream served by the plain FP64 single-domain path, one
+    request after another in arrival order: each request's service time is
+    measured (create, load, steps, result copy, release) and the first-come
+    first-served queue gives its latency."""
+    ex = ThreadPoolExecutor(max_workers=workers)
+    fp64_reqs = [Request(r.rid, r.arrival, r.steps, make_fp64(r)) for r in reqs]
+    get_case = _prefetch(fp64_reqs, ex, prefetch)
+    finish = 0.0
+    lat = []
+    gp = 0
+    busy = 0.0
+    for r in fp64_reqs:
+        c = get_case(r)
+        t = time.perf_counter()
+        d = domain_from_case(c)
+        d.step(r.steps)
+        out = {"ps": c.empty_state()["ps"]}
+        d.download(c.state_ptrs_of(out))
+        d.close()
+        service = time.perf_counter() - t
+        start = max(r.arrival, finish)
+        finish = start + service
+        lat.append(finish - r.arrival)
+        gp += c.points * r.steps
+        busy += service
+    ex.shutdown()
+    lat = np.array(lat)
+    return {"requests": len(reqs), "makespan_s": finish, "busy_s": busy, "gp_steps": gp,
+            "value": gp / finish, "service_rate": gp / busy,
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean())}
