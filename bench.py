@@ -441,6 +441,168 @@ def run_ensemble(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def rel_l2(a, b) -> float:
+    import numpy as np
+    d = np.linalg.norm((np.asarray(a) - np.asarray(b)).ravel())
+    n = np.linalg.norm(np.asarray(b).ravel())
+    return float(d / n) if n > 0 else float(d)
+
+
+def run_uneven(args, rank, world):
+    """Uneven batch: `members` domains with nx, ny log-uniform in 48-384 and kz
+    from {23, 30, 41} (moist recipe, dx 12 km, dt 60 s, 3 substeps, own seeds)
+    advanced together in mixed precision with autotuned launch shapes.  A
+    sample of every 10th domain is run alone on the plain FP64 path: its
+    throughput is the comparison, its final state the per-domain error
+    reference (the FP64 path matches the CPU oracle to 1e-12 in the tests)."""
+    import numpy as np
+    import torch
+    from regcm_gb300 import abi
+    from regcm_gb300 import case as cs
+    from regcm_gb300.moloch import MolochBatch, domain_from_case
+
+    lib = abi.load()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    nmem = args.members or 200
+    ids = [rank * nmem + m for m in range(nmem)]
+    prec = abi.MLC_PREC_FP64 if args.precision == "fp64" else abi.MLC_PREC_MIXED
+
+    def mk(i, p=prec):
+        return cs.config3_member(i, precision=p)
+
+    dims, pts = [], []
+    for i in ids:
+        nx, ny, kz = cs.config3_dims(i)
+        dims.append(abi.mlc_dims(nx + 1, ny + 1, kz, 5, 0))
+        pts.append(nx * ny * kz)
+    params = mk(ids[0]).params
+    t_build = time.perf_counter()
+    batch = MolochBatch.lazy(dims, params, lambda m: mk(ids[m]))
+    t_build = time.perf_counter() - t_build
+    batch.step(args.warmup)
+    tune = None if args.no_tune else batch.autotune(1)  # state is kept
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(dev) as clk:
+        ms = batch.step_timed(args.steps)
+    t_dev = ms / 1000.0
+    value = sum(pts) * args.steps * world / t_dev
+    launches = batch.launches_per_step()
+    sample = list(range(0, nmem, 10))
+    errs = {n: [] for n in ("tetav", "u", "v", "w", "qv")}
+    plain_gp, plain_t = 0, 0.0
+    for m in sample:
+        c = mk(ids[m])
+        got = c.empty_state()
+        batch.download(m, c.state_ptrs_of(got))
+        c64 = mk(ids[m], abi.MLC_PREC_FP64)
+        d = domain_from_case(c64)
+        d.step(args.warmup)
+        ms1 = C.c_float()
+        diag = abi.mlc_diag()
+        abi.check(lib.mlc_step_timed(d._ctx, args.steps, C.byref(diag), C.byref(ms1)), "plain")
+        ref = c64.empty_state()
+        d.download(c64.state_ptrs_of(ref))
+        d.close()
+        plain_gp += c64.points * args.steps
+        plain_t += ms1.value / 1000.0
+        for n in ("tetav", "u", "v", "w"):
+            errs[n].append(rel_l2(got[n], ref[n]))
+        errs["qv"].append(rel_l2(got["qx"][..., 0], ref["qx"][..., 0]))
+    batch.close()
+    if rank != 0:
+        return
+    plain = plain_gp / plain_t
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if prec == abi.MLC_PREC_MIXED else "f64", "data": "synthetic",
+        "config": {"workload": f"moloch-uneven-{nmem}-domains-nx,ny~logU(48,384)-kz{{23,30,41}}"
+                               "-dx12km-dt60-ns3",
+                   "members": nmem, "points_total": sum(pts), "points_min": min(pts),
+                   "points_max": max(pts), "precision": args.precision,
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2"},
+        "gpu_launches": launches * args.steps,
+        "side_by_side": {"plain_fp64_one_domain_at_a_time": {"value": plain, "unit": UNIT,
+                                                             "sample_domains": len(sample)},
+                         "ratio_to_plain_fp64": value / world / plain, "autotune": tune},
+        "per_domain_rel_l2_vs_fp64": {n: {"max": max(v), "median": float(np.median(v))}
+                                      for n, v in errs.items()},
+        "host_load_s": t_build,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args, rank, world):
+    """Serving stream: Poisson arrivals at each rate, `requests` requests of
+    nx = ny log-uniform in 32-512, kz 30, 6-240 steps, the moist 3 km recipe
+    with the request's seed, admitted by arena bytes under the budget and
+    batched per step in mixed precision; next to the same stream served one
+    request at a time by the plain FP64 path (service times measured once,
+    first-come first-served latencies per rate)."""
+    import torch
+    from regcm_gb300 import abi
+    from regcm_gb300 import case as cs
+    from regcm_gb300.serve import Request, poisson_arrivals, serve_one_at_a_time, serve_stream
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    rates = [float(r) for r in args.rates.split(",")]
+    nreq = args.requests
+    budget = int(args.budget_gb * 1e9)
+    prec = abi.MLC_PREC_FP64 if args.precision == "fp64" else abi.MLC_PREC_MIXED
+    params = cs.config4_request(0, scale=0.05, precision=prec)[0].params
+    steps = [cs.config4_request(r, scale=0.05)[1] for r in range(nreq)]
+    out = {}
+    with ClockSampler(dev) as clk:
+        for lam in rates:
+            arr = poisson_arrivals(lam, nreq, seed=int(lam * 1000) + 7)
+            reqs = [Request(r, float(arr[r]), steps[r],
+                            (lambda r=r: cs.config4_request(r, precision=prec)[0]))
+                    for r in range(nreq)]
+            out[lam] = serve_stream(reqs, params, budget, capacity=args.capacity)
+        # one request at a time, plain FP64 (service times do not depend on the rate)
+        arr = poisson_arrivals(rates[0], nreq, seed=int(rates[0] * 1000) + 7)
+        base_reqs = [Request(r, float(arr[r]), steps[r], None) for r in range(nreq)]
+        one = serve_one_at_a_time(
+            base_reqs, lambda r: (lambda rid=r.rid: cs.config4_request(rid)[0]))
+    if rank != 0:
+        return
+    # the FP64 queue's latencies at every rate from the measured service times
+    base = {}
+    svc = one.pop("service_s")
+    for lam in rates:
+        arr = poisson_arrivals(lam, nreq, seed=int(lam * 1000) + 7)
+        fin, lat = 0.0, []
+        for a, s in zip(arr, svc):
+            fin = max(a, fin) + s
+            lat.append(fin - a)
+        import numpy as np
+        lat = np.array(lat)
+        base[lam] = {"value": one["gp_steps"] / fin, "p50_s": float(np.percentile(lat, 50)),
+                     "p99_s": float(np.percentile(lat, 99))}
+    head = out[rates[-1]]
+    line = {
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world,
+        "steps": int(sum(steps)), "warmup": 0, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if prec == abi.MLC_PREC_MIXED else "f64", "data": "synthetic",
+        "config": {"workload": f"moloch-serving-poisson-{nreq}req-nx~logU(32,512)-kz30-steps~U(6,240)",
+                   "rates_per_s": rates, "budget_bytes": budget, "capacity": args.capacity,
+                   "precision": args.precision, "requests_per_rate": nreq,
+                   "parallelism": f"replicas{world}"},
+        "serving": {str(l): v for l, v in out.items()},
+        "plain_fp64_one_at_a_time": {"service_rate": one["service_rate"],
+                                     "per_rate": {str(l): v for l, v in base.items()}},
+        "ratio_to_plain_fp64": {str(l): out[l]["value"] / base[l]["value"] for l in rates},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_mixed_side(args, rank):
     """The same workload in mixed precision (FP32 fields, FP64 solve/Exner/theta),
     timed the same way, for the FP64-and-FP32 side-by-side report."""
@@ -470,8 +632,13 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
-    ap.add_argument("--members", type=int, default=64, help="ensemble members (config c2)")
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"])
+    ap.add_argument("--members", type=int, default=0,
+                    help="ensemble members (c2: 64) or domains (c3: 200)")
+    ap.add_argument("--rates", default="2,8,32", help="arrival rates per second (c4)")
+    ap.add_argument("--requests", type=int, default=200, help="requests per rate (c4)")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="arena budget (c4)")
+    ap.add_argument("--capacity", type=int, default=256, help="member slots (c4)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
@@ -488,7 +655,12 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
     elif args.config == "c2":
+        args.members = args.members or 64
         run_ensemble(args, rank, world)
+    elif args.config == "c3":
+        run_uneven(args, rank, world)
+    elif args.config == "c4":
+        run_serving(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1 and args.impl == "ours":

@@ -203,6 +203,10 @@ void mlc_destroy(mlc_ctx *ctx);
 /* Text for a status code. */
 const char *mlc_strerror(int status);
 
+/* Text of the CUDA error behind the last MLC_ERR_CUDA / MLC_ERR_NOMEM
+ * returned on the calling thread. */
+const char *mlc_last_error(void);
+
 /* ---- ensembles, uneven batches and a serving pool: several domains (the
  * members) advanced by the same kernel launches.  Each member owns its
  * arena and is described to the kernels by one entry of a device table;

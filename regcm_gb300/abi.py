@@ -133,6 +133,7 @@ def _declare(lib):
         "mlc_step": (C.c_int, [C.c_void_p, C.c_int, P(mlc_diag)]),
         "mlc_destroy": (None, [C.c_void_p]),
         "mlc_strerror": (C.c_char_p, [C.c_int]),
+        "mlc_last_error": (C.c_char_p, []),
         "mlc_footprint_bytes": (C.c_size_t, [P(mlc_dims), C.c_int]),
         "mlc_setup_levels": (C.c_int, [C.c_int, C.c_double, _dp, _dp]),
         "mlc_setup_nspg": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
@@ -194,6 +195,8 @@ class MolochError(RuntimeError):
     def __init__(self, status: int, where: str):
         self.status = status
         msg = load().mlc_strerror(status).decode()
+        if status in (MLC_ERR_CUDA, MLC_ERR_NOMEM):
+            msg += f" [{load().mlc_last_error().decode()}]"
         super().__init__(f"{where}: {msg} (status {status})")
 
 

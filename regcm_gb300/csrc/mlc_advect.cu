@@ -169,9 +169,12 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int nth = blockDim.x * blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  const Dom<R> &D = doms[blockIdx.z / nf];
+  // grid: x = field x tiles along j, y = tiles along i, z = member
+  const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
-  const int f = blockIdx.z % nf;
+  const int tiles_j = gridDim.x / nf;
+  const int f = blockIdx.x / tiles_j;
+  const int bj = blockIdx.x - f * tiles_j;
   if (set == 0 && f >= n_table_r(D)) return;  // a member with fewer species
   const Geom g = D.g;
   const int kz = g.kz;
@@ -187,7 +190,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   T *outp, *dst;
   field_t<R, T>(D, set, f, adv, src, outp, dst);
   (void)outp;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = bj * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
   const size_t ij = g.at2(j, i), PS = g.PS;
@@ -230,24 +233,26 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
 // Meridional then zonal WAF for one tile (:984-1038; ROTLLR :926-983).
 template <class R, class T, int kTJ, int kTI>
 __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__restrict__ doms,
-                                                            int nf, int kzmax, int set, int uvoff,
-                                                            int advoff) {
+                                                            int nf, int tiles_j, int set,
+                                                            int uvoff, int advoff) {
   constexpr int WJ = kTJ + 4;  // columns J0-2 .. J0+TJ+1
   __shared__ T wz_s[kTI + 4][WJ];      // rows I0-2 .. I0+TI+1
   __shared__ T zpby_s[kTI + 1][WJ];    // rows I0 .. I0+TI
   __shared__ T p0_s[kTI][WJ];          // rows I0 .. I0+TI-1
   __shared__ T zpbw_s[kTI][kTJ + 1];   // columns J0 .. J0+TJ
-  const Dom<R> &D = doms[blockIdx.z / (nf * kzmax)];
+  // grid: x = tiles along j and i, y = field x level, z = member
+  const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
-  const int f = blockIdx.z % nf;
+  const int f = blockIdx.y % nf;
   if (set == 0 && f >= n_table_r(D)) return;
-  const int k = (blockIdx.z / nf) % kzmax + 1;
+  const int k = blockIdx.y / nf + 1;
+  const int bj = blockIdx.x % tiles_j, bi = blockIdx.x / tiles_j;
   const Geom g = D.g;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   if (k > kz) return;
-  const int J0c = blockIdx.x * kTJ + 1, I0c = blockIdx.y * kTI + 1;
+  const int J0c = bj * kTJ + 1, I0c = bi * kTI + 1;
   if (J0c > jx - 1 || I0c > iy - 1) return;
   const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
   const R *__restrict__ u = D.u[uv];
@@ -255,7 +260,7 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
   const T *cur0;
   T *out0, *wz0;
   field_t<R, T>(D, set, f, adv, cur0, out0, wz0);
-  const int J0 = blockIdx.x * kTJ + 1, I0 = blockIdx.y * kTI + 1;
+  const int J0 = J0c, I0 = I0c;
   const int tid = threadIdx.y * kTJ + threadIdx.x;
   const int nth = kTJ * kTI;
   const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
@@ -496,17 +501,17 @@ void launch_vertical(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int 
                      cudaStream_t s) {
   const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
   const size_t smem = (size_t)3 * (L.kz + 2) * b.x * b.y * sizeof(T);
-  dim3 grd = grid2(L.jx - 1, L.iy - 1, b, 1);
-  grd.z = (unsigned)(nf * L.nmem);
+  dim3 grd = grid2(L.jx - 1, L.iy - 1, b, L.nmem);
+  grd.x *= (unsigned)nf;
   k_adv_vertical<R, T><<<grd, b, smem, s>>>(d, nf, set, advoff);
 }
 
 template <class R, class T, int TJ, int TI>
 void launch_tile(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int uvoff, int advoff,
                  cudaStream_t s) {
-  dim3 grd((unsigned)((L.jx - 1 + TJ - 1) / TJ), (unsigned)((L.iy - 1 + TI - 1) / TI),
-           (unsigned)(nf * L.kz * L.nmem));
-  k_adv_horizontal<R, T, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(d, nf, L.kz, set, uvoff, advoff);
+  const int tj = (L.jx - 1 + TJ - 1) / TJ, ti = (L.iy - 1 + TI - 1) / TI;
+  const dim3 grd((unsigned)(tj * ti), (unsigned)(nf * L.kz), (unsigned)L.nmem);
+  k_adv_horizontal<R, T, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(d, nf, tj, set, uvoff, advoff);
 }
 
 template <class R, class T>

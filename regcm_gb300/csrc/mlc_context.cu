@@ -32,6 +32,10 @@ namespace {
 constexpr size_t kAlign = 256;
 constexpr int kMaxLevels = 128;
 constexpr int kMaxSlots = 4096;
+constexpr int kMaxExtent = 32768;
+
+// Text of the last failing CUDA call on this thread (mlc_last_error).
+thread_local const char *g_last_error = "no error";
 
 size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
@@ -174,6 +178,9 @@ int validate_params(const mlc_params *p) {
 int validate_dims(const mlc_dims *d, const mlc_params *p) {
   if (!d) return MLC_ERR_INVALID;
   if (d->jx < 10 || d->iy < 10 || d->kz < 4 || d->kz > kMaxLevels) return MLC_ERR_INVALID;
+  // With these bounds (and at most kMaxSlots members) every grid dimension of
+  // every launch stays within CUDA's limits (y and z below 65536).
+  if (d->jx > kMaxExtent || d->iy > kMaxExtent) return MLC_ERR_TOO_LARGE;
   if (d->nqx < 2 || d->nqx > 10 || d->ntr < 0 || d->ntr > 8) return MLC_ERR_INVALID;
   if (p->ipptls == 2 && d->nqx < 5) return MLC_ERR_INVALID;
   if (n_table_r(*d, *p, true) > kMaxFields) return MLC_ERR_UNSUPPORTED;
@@ -184,6 +191,7 @@ int validate_dims(const mlc_dims *d, const mlc_params *p) {
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return MLC_OK;
+  g_last_error = cudaGetErrorString(e);
   if (e == cudaErrorMemoryAllocation) return MLC_ERR_NOMEM;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return MLC_ERR_NODEVICE;
   return MLC_ERR_CUDA;
@@ -1270,6 +1278,8 @@ int mlc_autotune(mlc_ctx *x, int steps, mlc_tune_report *rep) {
   if (!ready(x)) return MLC_ERR_STATE;
   return x->mixed ? autotune_impl<float>(x, steps, rep) : autotune_impl<double>(x, steps, rep);
 }
+
+const char *mlc_last_error(void) { return g_last_error; }
 
 // Kernels one mlc_step(ctx, 1) launches (for launch accounting).
 int mlc_launches_per_step(const mlc_ctx *x) { return x ? x->launches_per_step : 0; }

@@ -140,6 +140,29 @@ class MolochBatch:
         for m, c in enumerate(self.cases):
             _load_member(self.lib, self._ctx, m, c, self._keep)
 
+    @classmethod
+    def lazy(cls, dims, params, make):
+        """A batch of len(dims) members whose cases are built one at a time by
+        make(m), loaded and dropped (bounded host memory for large batches).
+        ``cases`` holds None for every member."""
+        self = cls.__new__(cls)
+        self.lib = abi.load()
+        n = len(dims)
+        self.cases = [None] * n
+        self.dims, self.params = dims[0], params
+        self._ctx = C.c_void_p()
+        arr = (abi.mlc_dims * n)(*dims)
+        abi.check(self.lib.mlc_create_multi(arr, C.byref(params), n, C.byref(self._ctx)),
+                  "allocate_moloch(batch)")
+        self._keep = []
+        for m in range(n):
+            c = make(m)
+            if c.dims.as_tuple() != dims[m].as_tuple() or not _same_params(c.params, params):
+                raise ValueError(f"member {m} does not match its declared extents/parameters")
+            keep = []
+            _load_member(self.lib, self._ctx, m, c, keep)
+        return self
+
     @property
     def nmem(self) -> int:
         return len(self.cases)

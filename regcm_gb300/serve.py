@@ -74,76 +74,114 @@ def _prefetch(reqs, pool_exec, depth):
     return get
 
 
+class _Clock:
+    """Server time.  'wall': seconds since the start.  'service': the sum of
+    the durations of the server's own operations (joins, steps, result
+    copies, departures), jumping forward to the next arrival when idle; the
+    time the client takes to build a payload is not server time, so a load
+    generator slower than the server does not thin the arrival stream."""
+
+    def __init__(self, mode: str):
+        if mode not in ("wall", "service"):
+            raise ValueError(mode)
+        self.mode = mode
+        self.t0 = time.perf_counter()
+        self.srv = 0.0
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0 if self.mode == "wall" else self.srv
+
+    def run(self, fn, *a):
+        t = time.perf_counter()
+        out = fn(*a)
+        self.srv += time.perf_counter() - t
+        return out
+
+    def idle_until(self, t: float):
+        if self.mode == "wall":
+            dt = t - self.now()
+            if dt > 0:
+                time.sleep(dt)
+        else:
+            self.srv = max(self.srv, t)
+
+
 def serve_stream(reqs, params, budget_bytes: int, capacity: int = 256,
-                 keep_results: bool = False, prefetch: int = 8, workers: int = 8):
-    """Serve `reqs` (sorted by arrival) in real time.  Returns a summary dict;
-    each request gets t_admit, t_done and (keep_results) its final state."""
+                 keep_results: bool = False, prefetch: int = 8, workers: int = 8,
+                 clock: str = "service", max_chunk: int = 16):
+    """Serve `reqs` (sorted by arrival).  Returns a summary dict; each request
+    gets t_admit, t_done and (keep_results) its final state.
+
+    Resident members advance together in chunks of steps: a chunk ends when
+    the first member finishes, or about when the next request arrives (from
+    the last measured step time), and is at most `max_chunk` steps."""
     pool = MolochPool(params, capacity, budget_bytes)
     queue = deque()
     active = {}
     pending = deque(reqs)
     ex = ThreadPoolExecutor(max_workers=workers)
     get_case = _prefetch(reqs, ex, prefetch)
+    clk = _Clock(clock)
     steps_run = 0
     gp_steps = 0
     max_resident = 0
-    late = 0.0
-    t0 = time.perf_counter()
-
-    def now():
-        return time.perf_counter() - t0
+    step_s = 0.0
+    joins = 0
 
     while pending or queue or active:
-        t = now()
+        t = clk.now()
         while pending and pending[0].arrival <= t:
             r = pending.popleft()
             r.case = get_case(r)
-            late = max(late, now() - r.arrival)
             queue.append(r)
         # admission in arrival order while the head fits
         while queue:
             r = queue[0]
-            slot = pool.join(r.case)
+            slot = clk.run(pool.join, r.case)
             if slot is None:
                 if not active:
                     raise ValueError(f"request {r.rid} needs {pool.footprint(r.case.dims)} bytes, "
                                      f"more than the budget of {budget_bytes}")
                 break
+            joins += 1
             queue.popleft()
             r.slot = slot
-            r.t_admit = now()
+            r.t_admit = clk.now()
             active[slot] = r
         if not active:
             if pending:
-                dt = pending[0].arrival - now()
-                if dt > 0:
-                    time.sleep(dt)
+                clk.idle_until(pending[0].arrival)
             continue
-        pool.step(1)
-        steps_run += 1
+        chunk = min(max_chunk, min(r.steps - r.done_steps for r in active.values()))
+        if pending and step_s > 0:
+            ahead = pending[0].arrival - clk.now()
+            chunk = max(1, min(chunk, int(ahead / step_s) + 1))
+        t = time.perf_counter()
+        clk.run(pool.step, chunk)
+        step_s = (time.perf_counter() - t) / chunk
+        steps_run += chunk
         max_resident = max(max_resident, len(active))
         for slot in list(active):
             r = active[slot]
-            r.done_steps += 1
-            gp_steps += r.case.points
+            r.done_steps += chunk
+            gp_steps += r.case.points * chunk
             if r.done_steps >= r.steps:
                 out = r.case.empty_state() if keep_results else {"ps": r.case.empty_state()["ps"]}
-                pool.download(slot, r.case.state_ptrs_of(out))
-                r.t_done = now()
+                clk.run(pool.download, slot, r.case.state_ptrs_of(out))
+                clk.run(pool.leave, slot)
+                r.t_done = clk.now()
                 if keep_results:
                     r.result = out
-                pool.leave(slot)
                 del active[slot]
                 r.case = None  # release the host arrays
-    makespan = now()
+    makespan = clk.now()
     ex.shutdown()
     pool.close()
     lat = np.array([r.latency for r in reqs])
-    return {"requests": len(reqs), "makespan_s": makespan, "gp_steps": gp_steps,
+    return {"requests": len(reqs), "clock": clock, "makespan_s": makespan, "gp_steps": gp_steps,
             "value": gp_steps / makespan, "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
-            "pool_steps": steps_run, "max_resident": max_resident,
-            "max_payload_lag_s": late}
+            "pool_steps": steps_run, "joins": joins, "max_resident": max_resident}
 
 
 def serve_one_at_a_time(reqs, make_fp64, workers: int = 8, prefetch: int = 4):
@@ -156,6 +194,7 @@ def serve_one_at_a_time(reqs, make_fp64, workers: int = 8, prefetch: int = 4):
     get_case = _prefetch(fp64_reqs, ex, prefetch)
     finish = 0.0
     lat = []
+    svc = []
     gp = 0
     busy = 0.0
     for r in fp64_reqs:
@@ -167,6 +206,7 @@ def serve_one_at_a_time(reqs, make_fp64, workers: int = 8, prefetch: int = 4):
         d.download(c.state_ptrs_of(out))
         d.close()
         service = time.perf_counter() - t
+        svc.append(service)
         start = max(r.arrival, finish)
         finish = start + service
         lat.append(finish - r.arrival)
@@ -175,6 +215,6 @@ def serve_one_at_a_time(reqs, make_fp64, workers: int = 8, prefetch: int = 4):
     ex.shutdown()
     lat = np.array(lat)
     return {"requests": len(reqs), "makespan_s": finish, "busy_s": busy, "gp_steps": gp,
-            "value": gp / finish, "service_rate": gp / busy,
+            "value": gp / finish, "service_rate": gp / busy, "service_s": svc,
             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "mean_s": float(lat.mean())}
