@@ -484,6 +484,289 @@ __global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advof
   }
 }
 
+// ---- increment form for the FP64 fields (theta_v, Exner) of a mixed member --
+//
+// The WAF update is linear in the advected field once the limiter regions
+// are fixed, and the regions depend on differences only.  So every flux can
+// be formed from values relative to a reference r:
+//   F(a - r, c - r, num) = F(a, c, num) - 2*hvel*r,
+// and a cell's update relative to its own value needs only neighbour
+// differences and the cell's own increment, all small numbers that FP32
+// carries to ~1e-7 of the increment (not of the field).  FP64 is left for the
+// neighbour differences, for the terms where the scheme does not preserve a
+// constant field (the model top of the vertical pass, where the flux through
+// kz+1 is zero but s(kz+1) is not; non-uniform map factors in the horizontal
+// passes) and for the final sum field + increment.  Fluxes are formed once
+// per interface, relative to the cell below (south, west) of it, and moved to
+// the other cell's reference by -2*hvel*(its value - the first cell's).
+
+// Both vertical passes (Main/mod_moloch.F90:858-922).  Writes the increment
+// dz = (field after the passes) - field, in FP64.
+template <class R>
+__global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff) {
+  extern __shared__ float vsm[];
+  const int nth = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const int tiles_j = gridDim.x / 2;
+  const int f = blockIdx.x / tiles_j;
+  const int bj = blockIdx.x - f * tiles_j;
+  const Geom g = D.g;
+  const int kz = g.kz;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const double *__restrict__ src = f == 0 ? D.tetav[adv] : D.pai[adv];
+  double *__restrict__ dst = D.wz_d[f];
+  const R *__restrict__ s = D.s;
+  const int j = bj * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (j > g.jx - 1 || i > g.iy - 1) return;
+#define DZ(k) vsm[(size_t)(k) * nth + tid]                  // v(k+1) - v(k), k = 1..kz-1
+#define E(k) vsm[(size_t)(kz + 1 + (k)) * nth + tid]        // increment, k = 1..kz
+  const size_t ij = g.at2(j, i), PS = g.PS;
+  const float dtrdz = 0.5f * (float(c.dtstepa) * float(c.rdzita));
+  double vlo = src[ij];
+  const double v1 = vlo;
+  for (int k = 1; k <= kz - 1; ++k) {
+    const double vhi = src[ij + (size_t)k * PS];
+    DZ(k) = float(vhi - vlo);
+    vlo = vhi;
+  }
+  const double vtop = vlo;
+  for (int k = 1; k <= kz; ++k) E(k) = 0.f;
+  // FP32 parts of the bottom and top cells, and their FP64 constant parts
+  float eb32 = 0.f, et32 = 0.f;
+  double hb = 0.0, ht = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    float fb = 0.f;                    // flux below cell k, relative to cell k
+    float e_km1 = 0.f, e_k = E(1), e_kp1 = kz >= 2 ? E(2) : 0.f;
+    float sk = float(s[ij]);
+    for (int k = 1; k <= kz; ++k) {
+      const size_t o = ij + (size_t)(k - 1) * PS;
+      const float e_kp2 = k + 2 <= kz ? E(k + 2) : 0.f;
+      const float skp = float(s[o + PS]);
+      float fa = 0.f, fup = 0.f;       // flux above (relative to k), same moved to k+1
+      if (k <= kz - 1) {
+        const float zamu = skp * dtrdz;
+        const float dzk = DZ(k);
+        float is, num;
+        if (zamu >= 0.f) {
+          is = 1.f;
+          num = k + 2 <= kz ? (e_kp1 - e_kp2) - DZ(k + 1) : 0.f;
+        } else {
+          is = -1.f;
+          num = k >= 2 ? (e_km1 - e_k) - DZ(k - 1) : 0.f;
+        }
+        fa = waf_flux<float>(0.5f * skp, is, zamu, dzk + e_kp1, e_k, num);
+        fup = fa - skp * dzk;
+      }
+      const float zrfmu = float(sa.zrfmu[o]), zrfmd = float(sa.zrfmd[o]);
+      const float upd = -fb * zrfmu + fa * zrfmd + (sk * zrfmu - skp * zrfmd) * e_k;
+      float en;
+      if (k == 1 || k == kz) {
+        // constant part: k = kz has no flux through kz+1, k = 1 none through 1
+        const double kap = k == kz ? -(double)skp * (double)zrfmd : (double)sk * (double)zrfmu;
+        const double vk = k == kz ? vtop : v1;
+        if (k == kz) { et32 += upd; ht += vk * kap; en = et32 + float(ht); }
+        else { eb32 += upd; hb += vk * kap; en = eb32 + float(hb); }
+      } else {
+        en = e_k + upd;
+      }
+      E(k) = en;                       // old E(k) lives on in e_km1 below
+      e_km1 = e_k; e_k = e_kp1; e_kp1 = e_kp2;
+      fb = fup;
+      sk = skp;
+    }
+  }
+  for (int k = 1; k <= kz; ++k) {
+    double d;
+    if (k == kz) d = (double)et32 + ht;
+    else if (k == 1) d = (double)eb32 + hb;
+    else d = (double)E(k);
+    dst[ij + (size_t)(k - 1) * PS] = d;
+  }
+#undef DZ
+#undef E
+}
+
+// Meridional then zonal WAF of one tile (:984-1038; ROTLLR :926-983) in
+// increment form.  pp is the field at the start of the advection step, dz
+// its vertical increment; out = pp + dz + (meridional + zonal increments).
+template <class R, int kTJ, int kTI>
+__global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal_inc(const Dom<R> *__restrict__ doms,
+                                                                int tiles_j, int uvoff,
+                                                                int advoff) {
+  constexpr int WJ = kTJ + 4;          // columns J0-2 .. J0+TJ+1
+  __shared__ double pp_s[kTI + 4][WJ];  // rows I0-2 .. I0+TI+1
+  __shared__ float dz_s[kTI + 4][WJ];   // vertical increment
+  __shared__ float dy_s[kTI + 3][WJ];   // pp(i+1) - pp(i), rows I0-2 .. I0+TI
+  __shared__ float fy_s[kTI + 1][WJ];   // meridional flux at i, relative to pp(i-1)
+  __shared__ float ey_s[kTI][WJ];       // p0 - pp, rows I0 .. I0+TI-1
+  __shared__ float hy_s[kTI][WJ];       // meridional increment alone
+  __shared__ float dx_s[kTI][kTJ + 3];  // pp(j+1) - pp(j), columns J0-2 .. J0+TJ
+  __shared__ float fx_s[kTI][kTJ + 1];  // zonal flux at j, relative to pp(j-1)
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const int f = blockIdx.y & 1;
+  const int k = (blockIdx.y >> 1) + 1;
+  const int bj = blockIdx.x % tiles_j, bi = blockIdx.x / tiles_j;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  if (k > kz) return;
+  const int J0 = bj * kTJ + 1, I0 = bi * kTI + 1;
+  if (J0 > jx - 1 || I0 > iy - 1) return;
+  const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
+  const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
+  const double *__restrict__ pp = (f == 0 ? D.tetav[adv] : D.pai[adv]) + ko;
+  double *__restrict__ out = (f == 0 ? D.tetav[adv ^ 1] : D.pai[adv ^ 1]) + ko;
+  const double *__restrict__ dzg = D.wz_d[f] + ko;
+  const R *__restrict__ uk = D.u[uv] + ko;
+  const R *__restrict__ vk = D.v[uv] + ko;
+  const int tid = threadIdx.y * kTJ + threadIdx.x;
+  const int nth = kTJ * kTI;
+  const float dta = float(c.dtstepa);
+  const float dtrdx = dta * float(c.rdx), dtrdy = dta * float(c.rdx);
+  const bool rot = c.lrotllr != 0;
+  const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
+
+  for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
+    const int rr = e / WJ, cc = e % WJ;
+    const int i = I0 - 2 + rr, j = J0 - 2 + cc;
+    double x = 0.0, z = 0.0;
+    if (i >= 1 && i <= iy - 1 && j >= 1 && j <= jx - 1) {
+      const size_t ij = g.at2(j, i);
+      x = pp[ij];
+      z = dzg[ij];
+    }
+    pp_s[rr][cc] = x;
+    dz_s[rr][cc] = float(z);
+  }
+  __syncthreads();
+  for (int e = tid; e < (kTI + 3) * WJ; e += nth) {
+    const int rr = e / WJ, cc = e % WJ;
+    dy_s[rr][cc] = float(pp_s[rr + 1][cc] - pp_s[rr][cc]);
+  }
+  for (int e = tid; e < kTI * (kTJ + 3); e += nth) {
+    const int rr = e / (kTJ + 3), cc = e % (kTJ + 3);
+    dx_s[rr][cc] = float(pp_s[rr + 2][cc + 1] - pp_s[rr + 2][cc]);
+  }
+  __syncthreads();
+  // meridional fluxes at interface rows i = I0 .. I0+TI, relative to pp(i-1)
+  for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
+    const int rr = e / WJ, cc = e % WJ;
+    const int i = I0 + rr, j = J0 - 2 + cc;
+    float x = 0.f;
+    if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 1) {
+      const size_t ij = g.at2(j, i);
+      const float vv = float(vk[ij]);
+      const float zamu = rot ? vv * dtrdy : vv * float(sa.msfv[ij]) * dtrdy;
+      float is;
+      int ih;
+      if (zamu > 0.f) { is = 1.f; ih = i - 1; }
+      else { is = -1.f; ih = min(i + 1, imax); }
+      const int ihm1 = max(ih - 1, imin);
+      const int b = 2 - I0;  // tile row of global row i is i + b
+      const float dpp = ih != ihm1 ? dy_s[ihm1 + b][cc] : 0.f;
+      const float num = (dz_s[ih + b][cc] - dz_s[ihm1 + b][cc]) + dpp;
+      x = waf_flux<float>(0.5f * vv, is, zamu, dz_s[i - 1 + b][cc],
+                          dz_s[i + b][cc] + dy_s[i - 1 + b][cc], num);
+    }
+    fy_s[rr][cc] = x;
+  }
+  __syncthreads();
+  // p0 - pp on rows I0 .. I0+TI-1
+  for (int e = tid; e < kTI * WJ; e += nth) {
+    const int rr = e / WJ, cc = e % WJ;
+    const int i = I0 + rr, j = J0 - 2 + cc;
+    float hy = 0.f;
+    if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
+      const size_t ij = g.at2(j, i), ijN = ij + (size_t)g.P;
+      const float fz = float(sa.fmz[ko + ij]);
+      const float vs = float(vk[ij]), vn = float(vk[ijN]);
+      const float fs = fy_s[rr][cc] - vs * dy_s[rr + 1][cc];  // moved to pp(i)
+      const float fn = fy_s[rr + 1][cc];
+      if (rot) {
+        const float zhxvtn = dtrdy * float(sa.rmv[ijN]) * float(sa.msfx[ij]);
+        const float zhxvts = dtrdy * float(sa.rmv[ij]) * float(sa.msfx[ij]);
+        const float zrfmn = zhxvtn * fz * float(sa.rfmzv[ko + ijN]);
+        const float zrfms = zhxvts * fz * float(sa.rfmzv[ko + ij]);
+        hy = fs * zrfms - fn * zrfmn;
+      } else {
+        const float zrfmn = dtrdy * fz * float(sa.rfmzu[ko + ijN]);
+        const float zrfms = dtrdy * fz * float(sa.rfmzu[ko + ij]);
+        const float mx2 = float(sa.mx2[ij]);
+        const float rs = float(sa.rmv[ij]), rn = float(sa.rmv[ijN]);
+        hy = mx2 * (fs * zrfms - fn * zrfmn);
+        if (rs != 1.f || rn != 1.f)
+          hy += float(pp_s[rr + 2][cc] *
+                      (double)(mx2 * (vs * zrfms * (1.f - rs) - vn * zrfmn * (1.f - rn))));
+      }
+    }
+    hy_s[rr][cc] = hy;
+    ey_s[rr][cc] = dz_s[rr + 2][cc] + hy;
+  }
+  __syncthreads();
+  // zonal fluxes at interface columns j = J0 .. J0+TJ, relative to pp(j-1)
+  for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
+    const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
+    const int i = I0 + rr, j = J0 + cc;
+    float x = 0.f;
+    if (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
+      const size_t ij = g.at2(j, i);
+      const float uu = float(uk[ij]);
+      const float zamu = uu * float(sa.msfu[ij]) * dtrdx;
+      float is;
+      int jh;
+      if (zamu > 0.f) { is = 1.f; jh = j - 1; }
+      else { is = -1.f; jh = min(j + 1, jmax); }
+      const int jhm1 = max(jh - 1, jmin);
+      const int b = 2 - J0;  // ey_s / dx_s column of global column j is j + b
+      const float dpp = jh != jhm1 ? dx_s[rr][jhm1 + b] : 0.f;
+      const float num = (ey_s[rr][jh + b] - ey_s[rr][jhm1 + b]) + dpp;
+      x = waf_flux<float>(0.5f * uu, is, zamu, ey_s[rr][j - 1 + b],
+                          ey_s[rr][j + b] + dx_s[rr][j - 1 + b], num);
+    }
+    fx_s[rr][cc] = x;
+  }
+  __syncthreads();
+  {
+    const int rr = threadIdx.y, cc = threadIdx.x;
+    const int i = I0 + rr, j = J0 + cc;
+    if (i <= iy - 1 && j <= jx - 1) {
+      const size_t ij = g.at2(j, i);
+      const double ppk = pp_s[rr + 2][cc + 2];
+      double x = ppk;
+      if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
+        const float fz = float(sa.fmz[ko + ij]);
+        const float uw = float(uk[ij]), ue = float(uk[ij + 1]);
+        const float fw = fx_s[rr][cc] - uw * dx_s[rr][cc + 1];  // moved to pp(j)
+        const float fe = fx_s[rr][cc + 1];
+        float hx;
+        if (rot) {
+          const float zcostx = dtrdx * float(sa.msfx[ij]);
+          const float zrfmw = zcostx * fz * float(sa.rfmzu[ko + ij]);
+          const float zrfme = zcostx * fz * float(sa.rfmzu[ko + ij + 1]);
+          hx = fw * zrfmw - fe * zrfme;
+        } else {
+          const float zrfmw = dtrdx * fz * float(sa.rfmzu[ko + ij]);
+          const float zrfme = dtrdx * fz * float(sa.rfmzu[ko + ij + 1]);
+          const float mx2 = float(sa.mx2[ij]);
+          const float rw = float(sa.rmu[ij]), re = float(sa.rmu[ij + 1]);
+          hx = mx2 * (fw * zrfmw - fe * zrfme);
+          if (rw != 1.f || re != 1.f)
+            hx += float(ppk * (double)(mx2 * (uw * zrfmw * (1.f - rw) - ue * zrfme * (1.f - re))));
+        }
+        x = ppk + dzg[ij] + (double)(hy_s[rr][cc + 2] + hx);
+      }
+      out[ij] = x;
+    }
+  }
+}
+
 inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
   return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y), (unsigned)nmem);
 }
@@ -526,16 +809,46 @@ void launch_horizontal(const LaunchGeom &L, const Dom<R> *d, int nf, int set, in
 }
 
 template <class R>
+void launch_vertical_inc(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
+  const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
+  const size_t smem = (size_t)2 * (L.kz + 2) * b.x * b.y * sizeof(float);
+  dim3 grd = grid2(L.jx - 1, L.iy - 1, b, L.nmem);
+  grd.x *= 2u;
+  k_adv_vertical_inc<R><<<grd, b, smem, s>>>(d, advoff);
+}
+
+template <class R, int TJ, int TI>
+void launch_tile_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+  const int tj = (L.jx - 1 + TJ - 1) / TJ, ti = (L.iy - 1 + TI - 1) / TI;
+  const dim3 grd((unsigned)(tj * ti), (unsigned)(2 * L.kz), (unsigned)L.nmem);
+  k_adv_horizontal_inc<R, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(d, tj, uvoff, advoff);
+}
+
+template <class R>
+void launch_horizontal_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                           cudaStream_t s) {
+  switch (L.htile) {
+    case 1: launch_tile_inc<R, 32, 4>(L, d, uvoff, advoff, s); break;
+    case 2: launch_tile_inc<R, 64, 4>(L, d, uvoff, advoff, s); break;
+    case 3: launch_tile_inc<R, 16, 8>(L, d, uvoff, advoff, s); break;
+    default: launch_tile_inc<R, 32, 8>(L, d, uvoff, advoff, s); break;
+  }
+}
+
+// The FP64 fields of a mixed member (L.nadv_d = 2) use the increment form.
+template <class R>
 void Launch<R>::adv_vertical(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   launch_vertical<R, R>(L, d, L.nadv_r, 0, advoff, s);
-  if (L.nadv_d) launch_vertical<R, double>(L, d, L.nadv_d, 1, advoff, s);
+  if constexpr (sizeof(R) == sizeof(float))
+    if (L.nadv_d) launch_vertical_inc<R>(L, d, advoff, s);
 }
 
 template <class R>
 void Launch<R>::adv_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                                cudaStream_t s) {
   launch_horizontal<R, R>(L, d, L.nadv_r, 0, uvoff, advoff, s);
-  if (L.nadv_d) launch_horizontal<R, double>(L, d, L.nadv_d, 1, uvoff, advoff, s);
+  if constexpr (sizeof(R) == sizeof(float))
+    if (L.nadv_d) launch_horizontal_inc<R>(L, d, uvoff, advoff, s);
 }
 
 template <class R>
@@ -560,9 +873,10 @@ template <class R>
 cudaError_t Launch<R>::configure_advect() {
   cudaError_t e = cudaFuncSetAttribute(k_adv_vertical<R, R>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_adv_vertical<R, double>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if constexpr (sizeof(R) == sizeof(float))
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_adv_vertical_inc<R>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   return e;
 }
 

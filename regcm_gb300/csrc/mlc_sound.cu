@@ -220,6 +220,121 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
 #undef COL
 }
 
+// The solve of a mixed member (same equations as k_sound_solve).  FP64 is
+// kept where rounding is amplified: theta_v at half levels, the hydrostatic
+// balance -cp*theta_v*fmzf*dtrdz*(pai(k-1) - pai(k)) - g*dts of the w
+// equation (two terms of ~g*dts whose difference drives w), and the Exner
+// update, formed as pai - pai*increment.  The divergence filter, the
+// elimination coefficients, the recurrence and the back substitution are
+// O(1)-conditioned and run in FP32.
+template <class R>
+__global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const R *__restrict__ zraw = D.zdiv2;
+  R *__restrict__ s = D.s;
+  R *__restrict__ w = D.w;
+  double *__restrict__ pai = D.pai[adv];
+  const double *__restrict__ tetav = D.tetav[adv];
+  double *__restrict__ tetavf = D.tetavf;
+  extern __shared__ float msm[];
+  const int nth = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int kz = g.kz;
+  float *zf = msm;
+  float *wp = msm + (size_t)(kz + 2) * nth;
+  float *wk = msm + (size_t)2 * (kz + 2) * nth;
+#define COL(a, k) a[(size_t)(k) * nth + tid]
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (j > g.jx - 2 || i > g.iy - 2) return;
+  const double dts_d = c.dtsound;
+  const double dtrdz_d = dts_d * c.rdzita;
+  const float dtrdz = float(dtrdz_d);
+  const float zcs2 = float((dtrdz_d * dtrdz_d) * kRdrcv);
+  const float rdrcv = float(kRdrcv);
+  const double gdts = kGrav * dts_d;
+  const size_t ij = g.at2(j, i);
+  const size_t PS = g.PS;
+  const size_t P = (size_t)g.P;
+  const int32_t ib = sa.ibnd_cr[ij];
+
+  float sk = float(s[ij]);
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    float z = float(zraw[o]);
+    if (c.divfilter) {
+      const float lap = (float(zraw[o - 1]) + float(zraw[o + 1]) + float(zraw[o - P]) +
+                         float(zraw[o + P]) - 4.f * z);
+      z = z + float(sa.xknu[k - 1]) * lap;
+    }
+    const float skp1 = float(s[o + PS]);
+    const float bw = ib > 0 ? float(1.0 - sa.hefc[(size_t)(ib - 1) + (size_t)(k - 1) * c.nspgx]) : 1.f;
+    z = z + bw * dtrdz * float(sa.fmz[o]) * (sk - skp1);
+    COL(zf, k) = z;
+    sk = skp1;
+  }
+
+  float wnext = float(w[ij + (size_t)kz * PS]);
+  float wkp1 = 0.f;
+  double pai_k = pai[ij + (size_t)(kz - 1) * PS];
+  double tet_k = tetav[ij + (size_t)(kz - 1) * PS];
+  float pk_f = float(pai_k);
+  float fmz_k = float(sa.fmz[ij + (size_t)(kz - 1) * PS]);
+  for (int k = kz; k >= 2; --k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    const double pai_m = pai[o - PS];
+    const double tet_m = tetav[o - PS];
+    const float fmz_m = float(sa.fmz[o - PS]);
+    const double fmzf = sa.fmzf_d[o];
+    const float wold = float(w[o]);
+    const float corr = wold * float(fmzf) * dtrdz * float(tet_m - tet_k);
+    const double tvf = tetavf[o] - (double)corr;
+    tetavf[o] = tvf;
+    const double zrom1w = kCpd * tvf * fmzf;
+    float zwexpl = wold + float(-(zrom1w * dtrdz_d * (pai_m - pai_k)) - gdts);
+    const float zr = float(zrom1w);
+    const float pm_f = float(pai_m);
+    zwexpl = zwexpl + rdrcv * zr * dtrdz * (pm_f * COL(zf, k - 1) - pk_f * COL(zf, k));
+    const float ff = float(sa.ffilt[k - 1]);
+    const float zu = zcs2 * fmz_m * zr * pm_f + ff;
+    const float zd = zcs2 * fmz_k * zr * pk_f + ff;
+    const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
+    wnext = zrapp * (zwexpl + zd * wnext);
+    wkp1 = zrapp * zu;
+    COL(wp, k) = wnext;
+    COL(wk, k) = wkp1;
+    pai_k = pai_m; tet_k = tet_m; pk_f = pm_f; fmz_k = fmz_m;
+  }
+  float wprev = float(w[ij]);
+  COL(wp, 1) = wprev;
+  for (int k = 2; k <= kz; ++k) {
+    wprev = COL(wp, k) + COL(wk, k) * wprev;
+    COL(wp, k) = wprev;
+    w[ij + (size_t)(k - 1) * PS] = (R)wprev;
+  }
+  COL(wp, kz + 1) = float(w[ij + (size_t)kz * PS]);
+  for (int k = 1; k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    const double pk = pai[o];
+    const float inc = rdrcv * (COL(zf, k) + (dtrdz * float(sa.fmz[o]) * (COL(wp, k) - COL(wp, k + 1))));
+    pai[o] = fma(-pk, (double)inc, pk);
+  }
+  if (last) {
+    for (int k = 2; k <= kz; ++k) {
+      const size_t o = ij + (size_t)(k - 1) * PS;
+      s[o] = (R)((COL(wp, k) + float(s[o])) * float(sa.fmzf[o]));
+    }
+    s[ij] = R(0);
+    s[ij + (size_t)kz * PS] = R(0);
+  }
+#undef COL
+}
+
 // Main/mod_moloch.F90:677-721 with divergence_damping :738-765 folded in
 template <class R>
 __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
@@ -322,10 +437,13 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
                             cudaStream_t s) {
   (void)uvoff;
   const dim3 blk((unsigned)L.solve_x, (unsigned)L.solve_y);
-  const size_t smem = (size_t)3 * (L.kz + 2) * blk.x * blk.y * sizeof(double);
   const dim3 grd((unsigned)((L.jx - 3 + blk.x - 1) / blk.x), (unsigned)((L.iy - 3 + blk.y - 1) / blk.y),
                  (unsigned)L.nmem);
-  k_sound_solve<R><<<grd, blk, smem, s>>>(d, advoff, last ? 1 : 0);
+  const size_t cols = (size_t)3 * (L.kz + 2) * blk.x * blk.y;
+  if constexpr (sizeof(R) == sizeof(float))
+    k_sound_solve_mixed<R><<<grd, blk, cols * sizeof(float), s>>>(d, advoff, last ? 1 : 0);
+  else
+    k_sound_solve<R><<<grd, blk, cols * sizeof(double), s>>>(d, advoff, last ? 1 : 0);
 }
 
 template <class R>
@@ -336,8 +454,12 @@ void Launch<R>::sound_momentum(const LaunchGeom &L, const Dom<R> *d, int uvoff, 
 
 template <class R>
 cudaError_t Launch<R>::configure_sound() {
-  return cudaFuncSetAttribute(k_sound_solve<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              200 * 1024);
+  if constexpr (sizeof(R) == sizeof(float))
+    return cudaFuncSetAttribute(k_sound_solve_mixed<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                200 * 1024);
+  else
+    return cudaFuncSetAttribute(k_sound_solve<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                200 * 1024);
 }
 
 template struct Launch<double>;

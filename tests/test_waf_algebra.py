@@ -74,3 +74,228 @@ def test_region_ties_and_tiny_denominators():
                 <= 1e-15 * 3.0 * 2.25
     for num in (0.0, 1e-31, 1e-3):
         assert ref_flux(2.0, 1.0, 0.2, 5.0, 5.0, num) == new_flux(2.0, 1.0, 0.2, 5.0, 5.0, num)
+
+
+# ---- increment form (the FP64 fields of a mixed member) --------------------
+# The kernels advect theta_v and Exner relative to each cell's own value:
+# fluxes from neighbour differences, moved between the two cells of an
+# interface by -2*hvel*(difference), constant parts kept apart where the
+# scheme does not preserve a constant (model top; non-uniform map factors).
+# Evaluated in FP64, the increment form equals the direct form to rounding.
+
+def vertical_direct(v, s, zu, zd, dtrdz):
+    kz = len(v)
+    col = v.copy()
+    for _ in range(2):
+        flx = np.zeros(kz + 1)
+        for k in range(1, kz):            # interface k+1 (1-based), flx index k
+            skp = s[k]                     # s(k+1)
+            zamu = skp * dtrdz
+            if zamu >= 0:
+                is_, k1, k1p1 = 1.0, k + 1, min(k + 2, kz)
+            else:
+                is_, k1, k1p1 = -1.0, max(k - 1, 1), k
+            flx[k] = ref_flux(0.5 * skp, is_, zamu, col[k], col[k - 1], col[k1 - 1] - col[k1p1 - 1])
+        new = col.copy()
+        for k in range(kz):
+            pk = col[k]
+            zdv = (s[k] * zu[k] - s[k + 1] * zd[k]) * pk
+            new[k] = pk - flx[k] * zu[k] + flx[k + 1] * zd[k] + zdv
+        col = new
+    return col
+
+
+def vertical_increment(v, s, zu, zd, dtrdz):
+    kz = len(v)
+    dz = np.diff(v)                        # dz[k-1] = v(k+1) - v(k)
+    e = np.zeros(kz)
+    eb32 = et32 = hb = ht = 0.0
+    for _ in range(2):
+        fb = 0.0
+        new = e.copy()
+        for k in range(1, kz + 1):
+            sk, skp = s[k - 1], s[k]
+            fa = fup = 0.0
+            if k <= kz - 1:
+                zamu = skp * dtrdz
+                ek, ekp1 = e[k - 1], e[k]
+                if zamu >= 0:
+                    is_ = 1.0
+                    num = (ekp1 - e[k + 1]) - dz[k] if k + 2 <= kz else 0.0
+                else:
+                    is_ = -1.0
+                    num = (e[k - 2] - ek) - dz[k - 2] if k >= 2 else 0.0
+                fa = new_flux(0.5 * skp, is_, zamu, dz[k - 1] + ekp1, ek, num)
+                fup = fa - skp * dz[k - 1]
+            upd = -fb * zu[k - 1] + fa * zd[k - 1] + (sk * zu[k - 1] - skp * zd[k - 1]) * e[k - 1]
+            if k == kz:
+                et32 += upd
+                ht += v[k - 1] * (-skp * zd[k - 1])
+                new[k - 1] = et32 + ht
+            elif k == 1:
+                eb32 += upd
+                hb += v[0] * (sk * zu[0])
+                new[0] = eb32 + hb
+            else:
+                new[k - 1] = e[k - 1] + upd
+            fb = fup
+        e = new
+    return v + e
+
+
+def test_vertical_increment_form_equals_direct():
+    rng = np.random.default_rng(7)
+    worst = 0.0
+    for _ in range(300):
+        kz = int(rng.integers(4, 14))
+        v = 300.0 + np.cumsum(rng.uniform(0.0, 8.0, kz)) + rng.normal(0, 0.5, kz)
+        s = rng.normal(0, 0.4, kz + 1)
+        s[0] = 0.0 if rng.uniform() < 0.7 else s[0]   # s(1) = 0 in the interior
+        zu = rng.uniform(0.02, 0.3, kz)
+        zd = rng.uniform(0.02, 0.3, kz)
+        dtrdz = rng.uniform(0.05, 0.6)
+        a = vertical_direct(v, s, zu, zd, dtrdz)
+        b = vertical_increment(v, s, zu, zd, dtrdz)
+        worst = max(worst, float(np.max(np.abs(a - b)) / np.max(np.abs(v))))
+    assert worst < 1e-13, worst
+
+
+def horizontal_direct(pp, wz, u, v, msfu, msfv, mx2, rmu, rmv, zfac, rot, dtr):
+    """Meridional then zonal WAF on (ny, nx) cross points, 1-based rows i and
+    columns j as the kernels; zfac stands for fmz*rfmz* (one per point)."""
+    ny, nx = pp.shape
+    iy, jx = ny + 1, nx + 1
+    imin, imax, jmin, jmax = 1, iy - 1, 1, jx - 1
+    P = lambda a, j, i: a[i - 1, j - 1]
+    zpby = np.zeros((iy + 1, jx + 1))
+    for i in range(2, iy):
+        for j in range(1, jx):
+            vv = v[i - 1, j - 1]
+            zamu = vv * dtr if rot else vv * msfv[i - 1, j - 1] * dtr
+            if zamu > 0:
+                is_, ih = 1.0, i - 1
+            else:
+                is_, ih = -1.0, min(i + 1, imax)
+            ihm1 = max(ih - 1, imin)
+            zpby[i, j] = ref_flux(0.5 * vv, is_, zamu, P(wz, j, i - 1), P(wz, j, i),
+                                  P(wz, j, ih) - P(wz, j, ihm1))
+    p0 = np.zeros((iy + 1, jx + 1))
+    for i in range(2, iy - 1):
+        for j in range(1, jx):
+            zn, zs = dtr * zfac[i, j - 1], dtr * zfac[i - 1, j - 1]
+            vs, vn = v[i - 1, j - 1], v[i, j - 1]
+            if rot:
+                zdv = (vn * zn - vs * zs) * P(pp, j, i)
+                p0[i, j] = P(wz, j, i) + (zpby[i, j] * zs - zpby[i + 1, j] * zn + zdv)
+            else:
+                zdv = (vn * rmv[i, j - 1] * zn - vs * rmv[i - 1, j - 1] * zs) * P(pp, j, i)
+                p0[i, j] = P(wz, j, i) + mx2[i - 1, j - 1] * (zpby[i, j] * zs - zpby[i + 1, j] * zn + zdv)
+    out = pp.copy()
+    zpbw = np.zeros((iy + 1, jx + 1))
+    for i in range(2, iy - 1):
+        for j in range(2, jx):
+            uu = u[i - 1, j - 1]
+            zamu = uu * msfu[i - 1, j - 1] * dtr
+            if zamu > 0:
+                is_, jh = 1.0, j - 1
+            else:
+                is_, jh = -1.0, min(j + 1, jmax)
+            jhm1 = max(jh - 1, jmin)
+            zpbw[i, j] = ref_flux(0.5 * uu, is_, zamu, p0[i, j - 1], p0[i, j], p0[i, jh] - p0[i, jhm1])
+        for j in range(2, jx - 1):
+            zw, ze = dtr * zfac[i - 1, j - 1], dtr * zfac[i - 1, j]
+            uw, ue = u[i - 1, j - 1], u[i - 1, j]
+            if rot:
+                zdv = (ue * ze - uw * zw) * P(pp, j, i)
+                out[i - 1, j - 1] = p0[i, j] + zpbw[i, j] * zw - zpbw[i, j + 1] * ze + zdv
+            else:
+                zdv = (ue * rmu[i - 1, j] * ze - uw * rmu[i - 1, j - 1] * zw) * P(pp, j, i)
+                out[i - 1, j - 1] = p0[i, j] + mx2[i - 1, j - 1] * (zpbw[i, j] * zw - zpbw[i, j + 1] * ze + zdv)
+    return out
+
+
+def horizontal_increment(pp, wz, u, v, msfu, msfv, mx2, rmu, rmv, zfac, rot, dtr):
+    ny, nx = pp.shape
+    iy, jx = ny + 1, nx + 1
+    imin, imax, jmin, jmax = 1, iy - 1, 1, jx - 1
+    P = lambda a, j, i: a[i - 1, j - 1]
+    dz = wz - pp
+    dy = lambda j, i: P(pp, j, i + 1) - P(pp, j, i)
+    dx = lambda j, i: P(pp, j + 1, i) - P(pp, j, i)
+    fy = np.zeros((iy + 1, jx + 1))            # relative to pp(i-1)
+    for i in range(2, iy):
+        for j in range(1, jx):
+            vv = v[i - 1, j - 1]
+            zamu = vv * dtr if rot else vv * msfv[i - 1, j - 1] * dtr
+            if zamu > 0:
+                is_, ih = 1.0, i - 1
+            else:
+                is_, ih = -1.0, min(i + 1, imax)
+            ihm1 = max(ih - 1, imin)
+            dpp = dy(j, ihm1) if ih != ihm1 else 0.0
+            num = (P(dz, j, ih) - P(dz, j, ihm1)) + dpp
+            fy[i, j] = new_flux(0.5 * vv, is_, zamu, P(dz, j, i - 1), P(dz, j, i) + dy(j, i - 1), num)
+    hy = np.zeros((iy + 1, jx + 1))
+    ey = np.zeros((iy + 1, jx + 1))
+    for i in range(2, iy - 1):
+        for j in range(1, jx):
+            zn, zs = dtr * zfac[i, j - 1], dtr * zfac[i - 1, j - 1]
+            vs, vn = v[i - 1, j - 1], v[i, j - 1]
+            fs = fy[i, j] - vs * dy(j, i - 1)
+            fn = fy[i + 1, j]
+            if rot:
+                h = fs * zs - fn * zn
+            else:
+                m, rs, rn = mx2[i - 1, j - 1], rmv[i - 1, j - 1], rmv[i, j - 1]
+                h = m * (fs * zs - fn * zn) + P(pp, j, i) * (m * (vs * zs * (1 - rs) - vn * zn * (1 - rn)))
+            hy[i, j] = h
+            ey[i, j] = P(dz, j, i) + h
+    out = pp.copy()
+    for i in range(2, iy - 1):
+        fx = np.zeros(jx + 1)
+        for j in range(2, jx):
+            uu = u[i - 1, j - 1]
+            zamu = uu * msfu[i - 1, j - 1] * dtr
+            if zamu > 0:
+                is_, jh = 1.0, j - 1
+            else:
+                is_, jh = -1.0, min(j + 1, jmax)
+            jhm1 = max(jh - 1, jmin)
+            dpp = dx(jhm1, i) if jh != jhm1 else 0.0
+            num = (ey[i, jh] - ey[i, jhm1]) + dpp
+            fx[j] = new_flux(0.5 * uu, is_, zamu, ey[i, j - 1], ey[i, j] + dx(j - 1, i), num)
+        for j in range(2, jx - 1):
+            zw, ze = dtr * zfac[i - 1, j - 1], dtr * zfac[i - 1, j]
+            uw, ue = u[i - 1, j - 1], u[i - 1, j]
+            fw = fx[j] - uw * dx(j - 1, i)
+            fe = fx[j + 1]
+            if rot:
+                h = fw * zw - fe * ze
+            else:
+                m, rw, re = mx2[i - 1, j - 1], rmu[i - 1, j - 1], rmu[i - 1, j]
+                h = m * (fw * zw - fe * ze) + P(pp, j, i) * (m * (uw * zw * (1 - rw) - ue * ze * (1 - re)))
+            out[i - 1, j - 1] = P(pp, j, i) + P(dz, j, i) + (hy[i, j] + h)
+    return out
+
+
+def test_horizontal_increment_form_equals_direct():
+    rng = np.random.default_rng(11)
+    worst = 0.0
+    for trial in range(24):
+        ny, nx = int(rng.integers(5, 11)), int(rng.integers(5, 11))
+        pp = 300.0 + rng.normal(0, 3.0, (ny, nx)) + np.linspace(0, 5, nx)[None, :]
+        wz = pp + rng.normal(0, 0.2, (ny, nx))
+        shp = (ny + 1, nx + 1)
+        u, v = rng.normal(0, 8, shp), rng.normal(0, 8, shp)
+        uniform = trial % 3 == 0
+        msfu = np.ones(shp) if uniform else rng.uniform(0.97, 1.03, shp)
+        msfv = np.ones(shp) if uniform else rng.uniform(0.97, 1.03, shp)
+        mx2 = np.ones(shp) if uniform else rng.uniform(0.95, 1.05, shp)
+        rmu, rmv = 1.0 / msfu, 1.0 / msfv
+        zfac = rng.uniform(0.9, 1.1, shp)
+        rot = trial % 4 == 1
+        dtr = rng.uniform(0.002, 0.01)
+        a = horizontal_direct(pp, wz, u, v, msfu, msfv, mx2, rmu, rmv, zfac, rot, dtr)
+        b = horizontal_increment(pp, wz, u, v, msfu, msfv, mx2, rmu, rmv, zfac, rot, dtr)
+        worst = max(worst, float(np.max(np.abs(a - b)) / 300.0))
+    assert worst < 1e-13, worst
