@@ -96,12 +96,35 @@ MLC_HD inline double pfwsat(double t, double p) {
   return kEp2 * (es / (p - es));
 }
 
+// pfwsat in FP32 for the diagnostics of a mixed member (stored in FP32).
+MLC_HD inline float pfwsat_f(float t, float p) {
+  float td = t - float(kTzero);
+  td = td < -75.f ? -75.f : td;
+  td = td > 100.f ? 100.f : td;
+  float es;
+  if (td >= 0.f) {
+    es = 0.611213476e+03f + td * (0.444007856e+02f + td * (0.143064234e+01f +
+         td * (0.264461437e-01f + td * (0.305903558e-03f + td * (0.196237241e-05f +
+         td * (0.892344772e-08f + td * (-0.373208410e-10f + td * 0.209339997e-13f)))))));
+  } else {
+    es = 0.611123516e+03f + td * (0.503109514e+02f + td * (0.188369801e+01f +
+         td * (0.420547422e-01f + td * (0.614396778e-03f + td * (0.602780717e-05f +
+         td * (0.387940929e-07f + td * (0.149436277e-09f + td * 0.262655803e-12f)))))));
+  }
+  float cap = 0.15f * p;
+  es = cap < es ? cap : es;
+  return float(kEp2) * (es / (p - es));
+}
+
 // p = pai**(cp/R) * p00 (Main/mod_moloch.F90:349).  cp/R evaluates to 3.5
 // exactly in IEEE double (cpd = 3.5*rgas), so pai**3.5 = pai^3 * sqrt(pai):
 // three multiplies and a square root instead of pow, equal to a few ulp.
 static_assert(kCpovr == 3.5, "cp/R must be 3.5 for the pai^3*sqrt(pai) form");
 MLC_HD inline double exner_to_pressure(double pai) {
   return pai * pai * pai * sqrt(pai) * kP00;
+}
+MLC_HD inline float exner_to_pressure_f(float pai) {
+  return pai * pai * pai * sqrtf(pai) * float(kP00);
 }
 
 // G(zeta) of Share/mod_zita.F90:105-115.

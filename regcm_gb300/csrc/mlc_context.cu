@@ -128,9 +128,10 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
   if (f64) {
     s.fmz_d = reinterpret_cast<const double *>(s.fmz);
     s.fmzf_d = reinterpret_cast<const double *>(s.fmzf);
+    s.cfz = nullptr;
   } else {
-    s.fmz_d = cv.take<double>(F);
-    s.fmzf_d = cv.take<double>(F1);
+    s.fmz_d = s.fmzf_d = nullptr;
+    s.cfz = cv.take<double>(F1);
   }
   s.zrfmu = cv.take<R>(F); s.zrfmd = cv.take<R>(F);
   s.zeta = cv.take<double>(F); s.dz = cv.take<double>(F);
@@ -589,8 +590,13 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
   MLC_CHK(put3<R>(x, g, s->fmz, W(a.fmz), jx - 1, iy - 1, kz, 0));
   MLC_CHK(put3<R>(x, g, s->fmzf, W(a.fmzf), jx - 1, iy - 1, kz + 1, 0));
   if (sizeof(R) != sizeof(double)) {
-    MLC_CHK(put3<double>(x, g, s->fmz, W(a.fmz_d), jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<double>(x, g, s->fmzf, W(a.fmzf_d), jx - 1, iy - 1, kz + 1, 0));
+    // the hydrostatic factor of the mixed solve, cp*fmzf*dtrdz, in FP64
+    const double dtrdz = c.dtsound * (1.0 / s->zita[kz - 1]);
+    const size_t n = (size_t)(jx - 1) * (iy - 1) * (kz + 1);
+    std::vector<double> cf(n);
+    for (size_t e = 0; e < n; ++e) cf[e] = kCpd * s->fmzf[e] * dtrdz;
+    MLC_CHK(put3<double>(x, g, cf.data(), W(a.cfz), jx - 1, iy - 1, kz + 1, 0));
+    MLC_TRY(cudaStreamSynchronize(x->stream));
   }
   MLC_CHK(put3<R>(x, g, s->rfmzu, W(a.rfmzu), jx, iy - 1, kz, 0));
   MLC_CHK(put3<R>(x, g, s->rfmzv, W(a.rfmzv), jx - 1, iy, kz, 0));

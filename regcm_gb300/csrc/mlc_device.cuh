@@ -42,7 +42,8 @@ struct Scal {
 template <class R>
 struct Stat {
   const R *fmz, *fmzf, *rfmzu, *rfmzv;   // 3-D
-  const double *fmz_d, *fmzf_d;          // FP64 copies for the vertical solve
+  const double *fmz_d, *fmzf_d;          // FP64 fmz, fmzf for the solve of an FP64 member
+  const double *cfz;                     // cp*fmzf*dtsound*rdzita for the solve of a mixed member
   const R *zrfmu, *zrfmd;                // 3-D: (dtrdz*fmz)/fmzf(k), /fmzf(k+1)
   const double *zeta, *dz;               // 3-D, FP64 (surface pressure, budget)
   const R *hx, *hy;                      // 2-D

@@ -36,11 +36,21 @@ __global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff) {
   if (j > g.jx - 1 || i > g.iy - 1) return;
   const bool inner = j >= 2 && j <= g.jx - 2 && i >= 2 && i <= g.iy - 2;
   const size_t ij = g.at2(j, i), F = g.field3();
+  const bool mixed = sizeof(R) == sizeof(float);
   for (int k = 1; k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * g.PS;
-    const R tv = R(st.tetav[o] * st.pai[o]);
+    const double pk = st.pai[o];
+    const R tv = R(st.tetav[o] * pk);
     st.tvirt[o] = tv;
-    if (inner) st.t[o] = tv / qfactor(st.qx, o, F, c.ipptls);
+    const R qf = qfactor(st.qx, o, F, c.ipptls);
+    if (inner) st.t[o] = tv / qf;
+    if (mixed) {
+      // what status_update needs to carry theta_v over as a ratio
+      // (t_end = tvirt/qf also at the ring, where t itself is not refreshed)
+      D.wz[0][o] = qf;
+      D.wz[1][o] = inner ? st.t[o] : tv / qf;
+      D.wz_d[0][o] = pk;
+    }
   }
 }
 
@@ -257,10 +267,11 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
       st.vx[o] = a;
     }
   }
-  // pressure (FP64 Exner reconstruction)
+  // pressure (FP64 Exner reconstruction; FP32 for the FP32 field of a mixed member)
   for (int k = 1; k <= kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
-    st.p[o] = (R)exner_to_pressure(st.pai[o]);
+    if constexpr (sizeof(R) == sizeof(float)) st.p[o] = exner_to_pressure_f(float(st.pai[o]));
+    else st.p[o] = (R)exner_to_pressure(st.pai[o]);
   }
   if (inner) {
     // tvirt at kz-1, kz before the clamps: from the boundary's temp_to_tvirt,
@@ -295,12 +306,29 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
       }
     }
     const R tk = st.t[o];
-    const R tv = tk * qfactor(st.qx, o, F, ipp);
+    const R qf = qfactor(st.qx, o, F, ipp);
+    const R tv = tk * qf;
     st.tvirt[o] = tv;
-    st.tetav[o] = (double)tv / st.pai[o];
     const R pk = st.p[o];
     st.rho[o] = pk / (R(kRgas) * tk);
-    st.qsat[o] = (R)pfwsat((double)tk, (double)pk);
+    if constexpr (sizeof(R) == sizeof(float)) {
+      // theta_v = t*qf/pai as a ratio of the value carried in FP64:
+      //   theta_v' = theta_v * (t/t_end) * (qf/qf_end) * (pai_end/pai),
+      // t_end, qf_end, pai_end as end_tvirt left them.  Where none changed
+      // (the interior) theta_v keeps every FP64 digit; elsewhere the ratio's
+      // FP32 rounding falls on the change, not on theta_v.
+      const float qf0 = D.wz[0][o], t0 = D.wz[1][o];
+      const double p0 = D.wz_d[0][o], p1 = st.pai[o];
+      const float rt = (tk - t0) / t0;
+      const float rq = (qf - qf0) / qf0;
+      const float rp = p0 != p1 ? float(p0 - p1) / float(p1) : 0.f;
+      const float eps = rt + rq + rp + rt * rq + (rt + rq + rt * rq) * rp;
+      if (eps != 0.f) st.tetav[o] = fma(st.tetav[o], (double)eps, st.tetav[o]);
+      st.qsat[o] = pfwsat_f(tk, pk);
+    } else {
+      st.tetav[o] = (double)tv / st.pai[o];
+      st.qsat[o] = (R)pfwsat((double)tk, (double)pk);
+    }
   }
 }
 
@@ -347,25 +375,15 @@ __global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int adv
 // block pass then adds the partials in block order, so the result does not
 // depend on scheduling and a domain gives the same bits alone or in a batch.
 constexpr int kRedThreads = 256;
+constexpr int kRedWarps = kRedThreads / 32;
 constexpr int kNPart = 7;  // dry, dryadv, qmass, qadv, ps max, ps min, non-finite flag
 
-__device__ double block_sum(double x, double *sh) {
-  const int t = threadIdx.x;
-  sh[t] = x;
-  __syncthreads();
-  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
-    if (t < s) sh[t] = sh[t] + sh[t + s];
-    __syncthreads();
-  }
-  double r = sh[0];
-  __syncthreads();
-  return r;
-}
-
+// One warp per row (i, k): lanes stride along j, the rows of a block go to its
+// warps in turn; warp sums by shuffles, then the warps' sums in warp order.
 template <class R>
 __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__restrict__ doms,
                                                                 int uvoff, int advoff) {
-  __shared__ double sh[kRedThreads];
+  __shared__ double sh[kRedWarps][kNPart];
   const Dom<R> &D = doms[blockIdx.y];
   if (!D.active) return;
   if ((int)blockIdx.x >= D.red_blocks) return;
@@ -378,23 +396,36 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   const double dx = c.dx, dt = c.dt, dxsq = dx * dx;
   const size_t F = g.field3();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double dry = 0, dadv = 0, qm = 0, qadv = 0, pmax = -INFINITY, pmin = INFINITY, bad = 0;
   const int nrows = (iy - 1) * kz;  // rows (i in ice, k)
   const int r0 = blockIdx.x * rows_per_block;
   const bool budget = c.debug_level > 0;
-  for (int r = r0; r < min(r0 + rows_per_block, nrows); ++r) {
+  for (int r = r0 + warp; r < min(r0 + rows_per_block, nrows); r += kRedWarps) {
     const int i = r % (iy - 1) + 1, k = r / (iy - 1) + 1;
     const size_t ko = (size_t)(k - 1) * g.PS;
     if (budget && i >= 2 && i <= iy - 2) {
-      for (int j = 2 + threadIdx.x; j <= jx - 2; j += kRedThreads) {
-        const size_t o = g.at2(j, i) + ko;
-        const double dzr = (double)sa.dz[o];
-        const double rh = (double)st.rho[o];
-        dry += dxsq * dzr * rh;
-        for (int n = 0; n < g.nqx; ++n) qm += (double)st.qx[o + (size_t)n * F] * dxsq * dzr * rh;
+      if constexpr (sizeof(R) == sizeof(float)) {
+        // FP32 fields: FP32 point products, FP64 sums, dx^2 applied once below
+        for (int j = 2 + lane; j <= jx - 2; j += 32) {
+          const size_t o = g.at2(j, i) + ko;
+          const float dr = float(sa.dz[o]) * float(st.rho[o]);
+          float qs = 0.f;
+          for (int n = 0; n < g.nqx; ++n) qs += float(st.qx[o + (size_t)n * F]);
+          dry += (double)dr;
+          qm += (double)(dr * qs);
+        }
+      } else {
+        for (int j = 2 + lane; j <= jx - 2; j += 32) {
+          const size_t o = g.at2(j, i) + ko;
+          const double dzr = (double)sa.dz[o];
+          const double rh = (double)st.rho[o];
+          dry += dxsq * dzr * rh;
+          for (int n = 0; n < g.nqx; ++n) qm += (double)st.qx[o + (size_t)n * F] * dxsq * dzr * rh;
+        }
       }
     }
-    if (budget && threadIdx.x == 0) {
+    if (budget && lane == 0) {
       // west and east columns over i in ice (Main/mod_massck.F90:85-100)
       const size_t ow = g.at2(1, i) + ko, oe = g.at2(jx - 1, i) + ko;
       const double uw = (double)st.u[g.at2(1, i) + ko], ue = (double)st.u[g.at2(jx, i) + ko];
@@ -411,7 +442,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
       // south (v at ide1) and north (v at ide2) rows, j in jci (:101-116)
       const int iv = (i == 1) ? 1 : iy;
       const bool south = (i == 1);
-      for (int j = 2 + threadIdx.x; j <= jx - 2; j += kRedThreads) {
+      for (int j = 2 + lane; j <= jx - 2; j += 32) {
         const size_t o = g.at2(j, i) + ko;
         const double vv = (double)st.v[g.at2(j, iv) + ko];
         const double dzr = (double)sa.dz[o], rh = (double)st.rho[o];
@@ -424,36 +455,39 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
       }
     }
     if (k == 1 && i >= 2 && i <= iy - 2) {
-      for (int j = 2 + threadIdx.x; j <= jx - 2; j += kRedThreads) {
+      for (int j = 2 + lane; j <= jx - 2; j += 32) {
         const double x = st.ps[g.at2(j, i)];
         if (!isfinite(x)) bad = 1;
         else { pmax = fmax(pmax, x); pmin = fmin(pmin, x); }
       }
     }
   }
-  dry = block_sum(dry, sh);
-  dadv = block_sum(dadv, sh);
-  qm = block_sum(qm, sh);
-  qadv = block_sum(qadv, sh);
-  bad = block_sum(bad, sh);
-  sh[threadIdx.x] = pmax;
-  __syncthreads();
-  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
-    __syncthreads();
+  if constexpr (sizeof(R) == sizeof(float)) {
+    dry *= dxsq;
+    qm *= dxsq;
   }
-  pmax = sh[0];
-  __syncthreads();
-  sh[threadIdx.x] = pmin;
-  __syncthreads();
-  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
-    __syncthreads();
+  for (int off = 16; off > 0; off >>= 1) {
+    dry += __shfl_down_sync(0xffffffffu, dry, off);
+    dadv += __shfl_down_sync(0xffffffffu, dadv, off);
+    qm += __shfl_down_sync(0xffffffffu, qm, off);
+    qadv += __shfl_down_sync(0xffffffffu, qadv, off);
+    bad += __shfl_down_sync(0xffffffffu, bad, off);
+    pmax = fmax(pmax, __shfl_down_sync(0xffffffffu, pmax, off));
+    pmin = fmin(pmin, __shfl_down_sync(0xffffffffu, pmin, off));
   }
-  pmin = sh[0];
+  if (lane == 0) {
+    sh[warp][0] = dry; sh[warp][1] = dadv; sh[warp][2] = qm; sh[warp][3] = qadv;
+    sh[warp][4] = pmax; sh[warp][5] = pmin; sh[warp][6] = bad;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
+    double a[kNPart] = {0, 0, 0, 0, -INFINITY, INFINITY, 0};
+    for (int w = 0; w < kRedWarps; ++w) {
+      a[0] += sh[w][0]; a[1] += sh[w][1]; a[2] += sh[w][2]; a[3] += sh[w][3];
+      a[4] = fmax(a[4], sh[w][4]); a[5] = fmin(a[5], sh[w][5]); a[6] += sh[w][6];
+    }
     double *p = part + (size_t)blockIdx.x * kNPart;
-    p[0] = dry; p[1] = dadv; p[2] = qm; p[3] = qadv; p[4] = pmax; p[5] = pmin; p[6] = bad;
+    for (int q = 0; q < kNPart; ++q) p[q] = a[q];
   }
 }
 
@@ -521,9 +555,12 @@ inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
 }  // namespace
 
 int reduce_rows_per_block(const Geom &g) {
+  // about 4 blocks per SM for a large domain, at least 4 rows per warp
   const int nrows = (g.iy - 1) * g.kz;
   const int target = 152 * 4;
-  return (nrows + target - 1) / target;
+  int rpb = (nrows + target - 1) / target;
+  rpb = (rpb + kRedWarps - 1) / kRedWarps * kRedWarps;
+  return rpb < 4 * kRedWarps ? 4 * kRedWarps : rpb;
 }
 
 int reduce_blocks(const Geom &g) {

@@ -49,6 +49,9 @@ __global__ void k_sound_prep(const Dom<R> *__restrict__ doms, int advoff) {
   for (int k = 2; k <= g.kz; ++k) {
     double hi = tetav[g.at(j, i, k)];
     tetavf[g.at(j, i, k)] = 0.5 * (lo + hi);
+    // mixed member: theta_v(k-1) - theta_v(k) for the substeps' solves (the
+    // scratch wz[2] is free until the advection of this round)
+    if (sizeof(R) == sizeof(float)) D.wz[2][g.at(j, i, k)] = R(lo - hi);
     lo = hi;
   }
 }
@@ -239,7 +242,6 @@ __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff,
   R *__restrict__ s = D.s;
   R *__restrict__ w = D.w;
   double *__restrict__ pai = D.pai[adv];
-  const double *__restrict__ tetav = D.tetav[adv];
   double *__restrict__ tetavf = D.tetavf;
   extern __shared__ float msm[];
   const int nth = blockDim.x * blockDim.y;
@@ -255,7 +257,6 @@ __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff,
   const double dts_d = c.dtsound;
   const double dtrdz_d = dts_d * c.rdzita;
   const float dtrdz = float(dtrdz_d);
-  const float zcs2 = float((dtrdz_d * dtrdz_d) * kRdrcv);
   const float rdrcv = float(kRdrcv);
   const double gdts = kGrav * dts_d;
   const size_t ij = g.at2(j, i);
@@ -279,36 +280,36 @@ __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff,
     sk = skp1;
   }
 
+  // zrd = cp*tvf*fmzf*dtrdz = tvf*cfz (FP64); zcs2*zrom1w = rdrcv*dtrdz*zrd
+  const float rdt = rdrcv * dtrdz;
+  const float *__restrict__ dtet = D.wz[2];  // theta_v(k-1) - theta_v(k), sound_prep
   float wnext = float(w[ij + (size_t)kz * PS]);
   float wkp1 = 0.f;
   double pai_k = pai[ij + (size_t)(kz - 1) * PS];
-  double tet_k = tetav[ij + (size_t)(kz - 1) * PS];
   float pk_f = float(pai_k);
   float fmz_k = float(sa.fmz[ij + (size_t)(kz - 1) * PS]);
   for (int k = kz; k >= 2; --k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     const double pai_m = pai[o - PS];
-    const double tet_m = tetav[o - PS];
     const float fmz_m = float(sa.fmz[o - PS]);
-    const double fmzf = sa.fmzf_d[o];
     const float wold = float(w[o]);
-    const float corr = wold * float(fmzf) * dtrdz * float(tet_m - tet_k);
+    const float corr = wold * float(sa.fmzf[o]) * dtrdz * dtet[o];
     const double tvf = tetavf[o] - (double)corr;
     tetavf[o] = tvf;
-    const double zrom1w = kCpd * tvf * fmzf;
-    float zwexpl = wold + float(-(zrom1w * dtrdz_d * (pai_m - pai_k)) - gdts);
-    const float zr = float(zrom1w);
+    const double zrd = tvf * sa.cfz[o];
+    float zwexpl = wold + float(fma(-zrd, pai_m - pai_k, -gdts));
+    const float zr = float(zrd);
     const float pm_f = float(pai_m);
-    zwexpl = zwexpl + rdrcv * zr * dtrdz * (pm_f * COL(zf, k - 1) - pk_f * COL(zf, k));
+    zwexpl = zwexpl + rdrcv * zr * (pm_f * COL(zf, k - 1) - pk_f * COL(zf, k));
     const float ff = float(sa.ffilt[k - 1]);
-    const float zu = zcs2 * fmz_m * zr * pm_f + ff;
-    const float zd = zcs2 * fmz_k * zr * pk_f + ff;
+    const float zu = rdt * fmz_m * zr * pm_f + ff;
+    const float zd = rdt * fmz_k * zr * pk_f + ff;
     const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
     wnext = zrapp * (zwexpl + zd * wnext);
     wkp1 = zrapp * zu;
     COL(wp, k) = wnext;
     COL(wk, k) = wkp1;
-    pai_k = pai_m; tet_k = tet_m; pk_f = pm_f; fmz_k = fmz_m;
+    pai_k = pai_m; pk_f = pm_f; fmz_k = fmz_m;
   }
   float wprev = float(w[ij]);
   COL(wp, 1) = wprev;
