@@ -249,7 +249,8 @@ size_t mlc_member_footprint(const mlc_dims *dims, const mlc_params *params);
 
 /* Launch shapes picked by mlc_autotune, and the per-step device time of the
  * tuned kernels against the fixed 32x8 configuration (column kernels and
- * horizontal WAF tiles 32x8; solve and vertical WAF 32x2). */
+ * horizontal WAF tiles 32x8; vertical WAF blocks of 32 columns x 8 level
+ * threads; solve 32x2). */
 typedef struct mlc_tune_report {
   int32_t col_x, col_y;      /* column kernels                        */
   int32_t solve_x, solve_y;  /* implicit w-Exner solve                */

@@ -123,7 +123,7 @@ __device__ __forceinline__ void field_t(const Dom<R> &D, int set, int f, int adv
 }
 
 template <class R>
-__global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+__global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
@@ -134,12 +134,15 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
   R *__restrict__ ux = D.ux[adv];
   R *__restrict__ vx = D.vx[adv];
   R *__restrict__ wx = D.wx[adv];
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const Pt q_ = point_of(tiles_j, 1, 1);
+  const int j = q_.j, k0 = q_.k;
+  if (k0 > g.kz) return;
+  const int i = q_.i;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   if (j > jx - 1 || i > iy - 1) return;
   const size_t ij = g.at2(j, i), PS = g.PS, S = (size_t)g.P;
-  for (int k = 1; k <= kz; ++k) {
+#pragma unroll
+  for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     // uvstagtouvx :1535-1549
     R a;
@@ -160,16 +163,20 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
   }
 }
 
-// Two vertical WAF passes for one column of one field (:858-922).  R is the
-// type of the winds and metric, T the type of the advected field and of the
-// arithmetic (T = R except for the FP64 Exner field of a mixed domain).
+// Two vertical WAF passes for the columns of one field (:858-922).  A block
+// holds blockDim.x consecutive columns (j) of one row i with their levels in
+// shared memory, laid out [level][column]; its blockDim.y thread rows share
+// the levels.  Within a pass every interface flux depends only on the pass
+// input and every cell update only on its two fluxes, so each pass is two
+// level-parallel phases.  R is the type of the winds and metric, T that of
+// the advected field and of the arithmetic.
 template <class R, class T>
 __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set, int advoff) {
   extern __shared__ unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
-  const int nth = blockDim.x * blockDim.y;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  // grid: x = field x tiles along j, y = tiles along i, z = member
+  const int CX = blockDim.x, KT = blockDim.y;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  // grid: x = field x column tiles along j, y = row i, z = member
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const int tiles_j = gridDim.x / nf;
@@ -178,10 +185,17 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   if (set == 0 && f >= n_table_r(D)) return;  // a member with fewer species
   const Geom g = D.g;
   const int kz = g.kz;
-  T *col = smem;                                 // field column, levels 1..kz
-  T *flx = smem + (size_t)(kz + 2) * nth;        // wfw, interfaces 1..kz+1
-  T *sc = smem + (size_t)2 * (kz + 2) * nth;     // s, levels 1..kz+1
-#define COL(a, k) a[(size_t)(k) * nth + tid]
+  const int i = blockIdx.y + 1;
+  if (i > g.iy - 1 || bj * CX + 1 > g.jx - 1) return;
+  const int j = bj * CX + tx + 1;
+  const bool on = j <= g.jx - 1;
+  const size_t L = (size_t)(kz + 2) * CX;
+  T *col = smem;          // field, levels 1..kz
+  T *flx = smem + L;      // wfw, interfaces 1..kz+1
+  T *sc = smem + 2 * L;   // s, levels 1..kz+1
+  T *zu = smem + 3 * L;   // dtrdz*fmz/fmzf(k)
+  T *zd = smem + 4 * L;   // dtrdz*fmz/fmzf(k+1)
+#define A(a, k) a[(size_t)(k) * CX + tx]
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const R *__restrict__ s = D.s;
@@ -190,44 +204,54 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   T *outp, *dst;
   field_t<R, T>(D, set, f, adv, src, outp, dst);
   (void)outp;
-  const int j = bj * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (j > g.jx - 1 || i > g.iy - 1) return;
-  const size_t ij = g.at2(j, i), PS = g.PS;
-  const T dtrdz = T(0.5) * (T(c.dtstepa) * T(c.rdzita));
+  const size_t ij = on ? g.at2(j, i) : 0, PS = g.PS;
+  const T dtrdz = T(0.5) * (pick<T>(c.dtstepa, c.dtstepaf) * pick<T>(c.rdzita, c.rdzitaf));
 
-  for (int k = 1; k <= kz; ++k) COL(col, k) = src[ij + (size_t)(k - 1) * PS];
-  for (int k = 1; k <= kz + 1; ++k) COL(sc, k) = T(s[ij + (size_t)(k - 1) * PS]);
-  for (int pass = 0; pass < 2; ++pass) {
-    COL(flx, 1) = T(0);
-    COL(flx, kz + 1) = T(0);
-    for (int k = 1; k <= kz - 1; ++k) {
-      const T skp = COL(sc, k + 1);
-      const T zamu = skp * dtrdz;
-      T is;
-      int k1, k1p1;
-      if (zamu >= T(0)) {
-        is = T(1); k1 = k + 1; k1p1 = k1 + 1;
-        if (k1p1 > kz) k1p1 = kz;
-      } else {
-        is = T(-1); k1 = k - 1; k1p1 = k;
-        if (k1 < 1) k1 = 1;
-      }
-      COL(flx, k + 1) = waf_flux<T>(T(0.5) * skp, is, zamu, COL(col, k + 1), COL(col, k),
-                                    COL(col, k1) - COL(col, k1p1));
-    }
-    for (int k = 1; k <= kz; ++k) {
+  if (on)
+    for (int k = 1 + ty; k <= kz + 1; k += KT) {
       const size_t o = ij + (size_t)(k - 1) * PS;
-      const T zrfmu = T(sa.zrfmu[o]);
-      const T zrfmd = T(sa.zrfmd[o]);
-      const T pk = COL(col, k);
-      const T zdv = (COL(sc, k) * zrfmu - COL(sc, k + 1) * zrfmd) * pk;
-      COL(col, k) = pk - COL(flx, k) * zrfmu + COL(flx, k + 1) * zrfmd + zdv;
+      A(sc, k) = T(s[o]);
+      if (k <= kz) {
+        A(col, k) = src[o];
+        A(zu, k) = T(sa.zrfmu[o]);
+        A(zd, k) = T(sa.zrfmd[o]);
+      }
     }
+  if (ty == 0) {
+    A(flx, 1) = T(0);
+    A(flx, kz + 1) = T(0);
   }
-
-  for (int k = 1; k <= kz; ++k) dst[ij + (size_t)(k - 1) * PS] = COL(col, k);
-#undef COL
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    if (on)
+      for (int k = 1 + ty; k <= kz - 1; k += KT) {
+        const T skp = A(sc, k + 1);
+        const T zamu = skp * dtrdz;
+        T is;
+        int k1, k1p1;
+        if (zamu >= T(0)) {
+          is = T(1); k1 = k + 1; k1p1 = k1 + 1;
+          if (k1p1 > kz) k1p1 = kz;
+        } else {
+          is = T(-1); k1 = k - 1; k1p1 = k;
+          if (k1 < 1) k1 = 1;
+        }
+        A(flx, k + 1) = waf_flux<T>(T(0.5) * skp, is, zamu, A(col, k + 1), A(col, k),
+                                    A(col, k1) - A(col, k1p1));
+      }
+    __syncthreads();
+    if (on)
+      for (int k = 1 + ty; k <= kz; k += KT) {
+        const T zrfmu = A(zu, k), zrfmd = A(zd, k);
+        const T pk = A(col, k);
+        const T zdv = (A(sc, k) * zrfmu - A(sc, k + 1) * zrfmd) * pk;
+        A(col, k) = pk - A(flx, k) * zrfmu + A(flx, k + 1) * zrfmd + zdv;
+      }
+    __syncthreads();
+  }
+  if (on)
+    for (int k = 1 + ty; k <= kz; k += KT) dst[ij + (size_t)(k - 1) * PS] = A(col, k);
+#undef A
 }
 
 // Meridional then zonal WAF for one tile (:984-1038; ROTLLR :926-983).
@@ -269,8 +293,8 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
   T *out = out0 + ko;
   const R *uk = u + ko;
   const R *vk = v + ko;
-  const T dta = T(c.dtstepa);
-  const T dtrdx = dta * T(c.rdx), dtrdy = dta * T(c.rdx);
+  const T dta = pick<T>(c.dtstepa, c.dtstepaf);
+  const T dtrdx = dta * pick<T>(c.rdx, c.rdxf), dtrdy = dta * pick<T>(c.rdx, c.rdxf);
   const bool rot = c.lrotllr != 0;
   const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
 
@@ -386,25 +410,24 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
 // Species that are not advected (ipptls = 0: qx(iqfrst:nqx)) keep their
 // values when the advected fields move to the other half of their pairs.
 template <class R>
-__global__ void k_species_copy(const Dom<R> *__restrict__ doms, int advoff) {
+__global__ void k_species_copy(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (D.c.ipptls > 0 || j > g.jx - 1 || i > g.iy - 1) return;
+  const Pt q = point_of(tiles_j, 1, 1);
+  if (D.c.ipptls > 0 || q.j > g.jx - 1 || q.i > g.iy - 1 || q.k > g.kz) return;
   const int adv = (D.clk->adv_role + advoff) & 1;
-  const size_t F = g.field3(), ij = g.at2(j, i);
-  for (int n = 1; n < g.nqx; ++n)
-    for (int k = 1; k <= g.kz; ++k) {
-      const size_t o = ij + (size_t)(k - 1) * g.PS + (size_t)n * F;
-      D.qx[adv ^ 1][o] = D.qx[adv][o];
-    }
+  const size_t F = g.field3();
+#pragma unroll
+  for (int k = q.k; k < q.k + kPtLevels && k <= g.kz; ++k) {
+    const size_t o = g.at(q.j, q.i, k);
+    for (int n = 1; n < g.nqx; ++n) D.qx[adv ^ 1][o + (size_t)n * F] = D.qx[adv][o + (size_t)n * F];
+  }
 }
 
 // :809-825
 template <class R>
-__global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff) {
+__global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active || !D.c.curvature) return;
   const Geom g = D.g;
@@ -413,21 +436,24 @@ __global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff) {
   const int adv = (D.clk->adv_role + advoff) & 1;
   R *__restrict__ ux = D.ux[adv];
   R *__restrict__ vx = D.vx[adv];
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const Pt q_ = point_of(tiles_j, 2, 2);
+  const int j = q_.j, k0 = q_.k;
+  if (k0 > g.kz) return;
+  const int i = q_.i;
   if (j > g.jx - 2 || i > g.iy - 2) return;
   const size_t ij = g.at2(j, i);
-  const R dta = R(c.dtstepa);
+  const R dta = pick<R>(c.dtstepa, c.dtstepaf);
   R tanx, tany;
   if (c.lrotllr) {
     const double dlat = kDegrad * 0.5 * (sa.rlat[i - 1] + sa.rlat[i]);
     tanx = R(sin(dlat)) * sa.msfx[ij] * R(kRearthRad);
     tany = tanx;
   } else {
-    tanx = (sa.msfu[ij - 1] - sa.msfu[ij]) * R(c.rdx);
-    tany = (sa.msfv[ij - (size_t)g.P] - sa.msfv[ij]) * R(c.rdx);
+    tanx = (sa.msfu[ij - 1] - sa.msfu[ij]) * pick<R>(c.rdx, c.rdxf);
+    tany = (sa.msfv[ij - (size_t)g.P] - sa.msfv[ij]) * pick<R>(c.rdx, c.rdxf);
   }
-  for (int k = 1; k <= g.kz; ++k) {
+#pragma unroll
+  for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * g.PS;
     R a = ux[o];
     const R b = vx[o];
@@ -439,7 +465,7 @@ __global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff) {
 
 // uvxtouvstag :1477-1522 and htozstag :1461-1475
 template <class R>
-__global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+__global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
@@ -450,15 +476,18 @@ __global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advof
   R *__restrict__ u = D.u[uv];
   R *__restrict__ v = D.v[uv];
   R *__restrict__ w = D.w;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const Pt q_ = point_of(tiles_j, 1, 1);
+  const int j = q_.j, k0 = q_.k;
+  if (k0 > g.kz) return;
+  const int i = q_.i;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   if (j > jx || i > iy) return;
   const size_t ij = g.at2(j, i), PS = g.PS, S = (size_t)g.P;
   const bool do_u = (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2);
   const bool do_v = (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 1);
   const bool do_w = (j <= jx - 1 && i <= iy - 1);
-  for (int k = 1; k <= kz; ++k) {
+#pragma unroll
+  for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     if (do_u) {
       R a;
@@ -505,8 +534,8 @@ __global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advof
 template <class R>
 __global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff) {
   extern __shared__ float vsm[];
-  const int nth = blockDim.x * blockDim.y;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int CX = blockDim.x, KT = blockDim.y;
+  const int tx = threadIdx.x, ty = threadIdx.y;
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const int tiles_j = gridDim.x / 2;
@@ -514,81 +543,96 @@ __global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff) 
   const int bj = blockIdx.x - f * tiles_j;
   const Geom g = D.g;
   const int kz = g.kz;
+  const int i = blockIdx.y + 1;
+  if (i > g.iy - 1 || bj * CX + 1 > g.jx - 1) return;
+  const int j = bj * CX + tx + 1;
+  const bool on = j <= g.jx - 1;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const int adv = (D.clk->adv_role + advoff) & 1;
-  const double *__restrict__ src = f == 0 ? D.tetav[adv] : D.pai[adv];
-  double *__restrict__ dst = D.wz_d[f];
+  const size_t F = g.field3();
+  const DF src(f == 0 ? D.tetav[adv] : D.pai[adv], F);
+  const DF dst(D.wz_d[f], F);
   const R *__restrict__ s = D.s;
-  const int j = bj * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (j > g.jx - 1 || i > g.iy - 1) return;
-#define DZ(k) vsm[(size_t)(k) * nth + tid]                  // v(k+1) - v(k), k = 1..kz-1
-#define E(k) vsm[(size_t)(kz + 1 + (k)) * nth + tid]        // increment, k = 1..kz
-  const size_t ij = g.at2(j, i), PS = g.PS;
-  const float dtrdz = 0.5f * (float(c.dtstepa) * float(c.rdzita));
-  double vlo = src[ij];
-  const double v1 = vlo;
-  for (int k = 1; k <= kz - 1; ++k) {
-    const double vhi = src[ij + (size_t)k * PS];
-    DZ(k) = float(vhi - vlo);
-    vlo = vhi;
-  }
-  const double vtop = vlo;
-  for (int k = 1; k <= kz; ++k) E(k) = 0.f;
-  // FP32 parts of the bottom and top cells, and their FP64 constant parts
-  float eb32 = 0.f, et32 = 0.f;
-  double hb = 0.0, ht = 0.0;
-  for (int pass = 0; pass < 2; ++pass) {
-    float fb = 0.f;                    // flux below cell k, relative to cell k
-    float e_km1 = 0.f, e_k = E(1), e_kp1 = kz >= 2 ? E(2) : 0.f;
-    float sk = float(s[ij]);
-    for (int k = 1; k <= kz; ++k) {
+  const size_t L = (size_t)(kz + 2) * CX;
+  float *dzs = vsm;           // v(k+1) - v(k), k = 1..kz-1
+  float *e = vsm + L;         // increment of the pass input, k = 1..kz
+  float *flo = vsm + 2 * L;   // flux at k+1 relative to cell k, k = 1..kz-1
+  float *sc = vsm + 3 * L;    // s, levels 1..kz+1
+  float *zu = vsm + 4 * L;
+  float *zd = vsm + 5 * L;
+#define A(a, k) a[(size_t)(k) * CX + tx]
+  const size_t ij = on ? g.at2(j, i) : 0, PS = g.PS;
+  const float dtrdz = 0.5f * (c.dtstepaf * c.rdzitaf);
+  if (on)
+    for (int k = 1 + ty; k <= kz + 1; k += KT) {
       const size_t o = ij + (size_t)(k - 1) * PS;
-      const float e_kp2 = k + 2 <= kz ? E(k + 2) : 0.f;
-      const float skp = float(s[o + PS]);
-      float fa = 0.f, fup = 0.f;       // flux above (relative to k), same moved to k+1
-      if (k <= kz - 1) {
+      A(sc, k) = float(s[o]);
+      if (k <= kz) {
+        A(e, k) = 0.f;
+        A(zu, k) = float(sa.zrfmu[o]);
+        A(zd, k) = float(sa.zrfmd[o]);
+        if (k <= kz - 1) A(dzs, k) = df_diff(src.ld(o + PS), src.ld(o));
+      }
+    }
+  __syncthreads();
+  // the threads owning the bottom and top cells keep their FP32 parts and
+  // double-float constant parts in registers over both passes
+  float eb32 = 0.f, et32 = 0.f;
+  F2 hb{0.f, 0.f}, ht{0.f, 0.f};
+  for (int pass = 0; pass < 2; ++pass) {
+    if (on)
+      for (int k = 1 + ty; k <= kz - 1; k += KT) {
+        const float skp = A(sc, k + 1);
         const float zamu = skp * dtrdz;
-        const float dzk = DZ(k);
+        const float ek = A(e, k), ekp1 = A(e, k + 1);
         float is, num;
         if (zamu >= 0.f) {
           is = 1.f;
-          num = k + 2 <= kz ? (e_kp1 - e_kp2) - DZ(k + 1) : 0.f;
+          num = k + 2 <= kz ? (ekp1 - A(e, k + 2)) - A(dzs, k + 1) : 0.f;
         } else {
           is = -1.f;
-          num = k >= 2 ? (e_km1 - e_k) - DZ(k - 1) : 0.f;
+          num = k >= 2 ? (A(e, k - 1) - ek) - A(dzs, k - 1) : 0.f;
         }
-        fa = waf_flux<float>(0.5f * skp, is, zamu, dzk + e_kp1, e_k, num);
-        fup = fa - skp * dzk;
+        A(flo, k) = waf_flux<float>(0.5f * skp, is, zamu, A(dzs, k) + ekp1, ek, num);
       }
-      const float zrfmu = float(sa.zrfmu[o]), zrfmd = float(sa.zrfmd[o]);
-      const float upd = -fb * zrfmu + fa * zrfmd + (sk * zrfmu - skp * zrfmd) * e_k;
-      float en;
-      if (k == 1 || k == kz) {
-        // constant part: k = kz has no flux through kz+1, k = 1 none through 1
-        const double kap = k == kz ? -(double)skp * (double)zrfmd : (double)sk * (double)zrfmu;
-        const double vk = k == kz ? vtop : v1;
-        if (k == kz) { et32 += upd; ht += vk * kap; en = et32 + float(ht); }
-        else { eb32 += upd; hb += vk * kap; en = eb32 + float(hb); }
-      } else {
-        en = e_k + upd;
+    __syncthreads();
+    if (on)
+      for (int k = 1 + ty; k <= kz; k += KT) {
+        const float sk = A(sc, k), skp = A(sc, k + 1);
+        const float zrfmu = A(zu, k), zrfmd = A(zd, k);
+        const float ek = A(e, k);
+        // flux below, moved to cell k; flux above, relative to cell k
+        const float fb = k >= 2 ? A(flo, k - 1) - sk * A(dzs, k - 1) : 0.f;
+        const float fa = k <= kz - 1 ? A(flo, k) : 0.f;
+        const float upd = -fb * zrfmu + fa * zrfmd + (sk * zrfmu - skp * zrfmd) * ek;
+        float en;
+        if (k == kz) {
+          // no flux through kz+1: constant part -v*s(kz+1)*zrfmd, exact product
+          et32 += upd;
+          ht = df_add(ht, df_mul(src.ld(ij + (size_t)(kz - 1) * PS), two_prod(-skp, zrfmd)));
+          en = et32 + df_f(ht);
+        } else if (k == 1) {
+          // no flux through level 1: constant part v*s(1)*zrfmu (s(1) = 0 inside)
+          eb32 += upd;
+          hb = df_add(hb, df_mul(src.ld(ij), two_prod(sk, zrfmu)));
+          en = eb32 + df_f(hb);
+        } else {
+          en = ek + upd;
+        }
+        A(e, k) = en;
       }
-      E(k) = en;                       // old E(k) lives on in e_km1 below
-      e_km1 = e_k; e_k = e_kp1; e_kp1 = e_kp2;
-      fb = fup;
-      sk = skp;
+    __syncthreads();
+  }
+  if (on)
+    for (int k = 1 + ty; k <= kz; k += KT) {
+      F2 d;
+      if (k == kz) d = df_add_f(ht, et32);
+      else if (k == 1) d = df_add_f(hb, eb32);
+      else d = F2{A(e, k), 0.f};
+      dst.st(ij + (size_t)(k - 1) * PS, d);
     }
-  }
-  for (int k = 1; k <= kz; ++k) {
-    double d;
-    if (k == kz) d = (double)et32 + ht;
-    else if (k == 1) d = (double)eb32 + hb;
-    else d = (double)E(k);
-    dst[ij + (size_t)(k - 1) * PS] = d;
-  }
-#undef DZ
-#undef E
+#undef A
 }
 
 // Meridional then zonal WAF of one tile (:984-1038; ROTLLR :926-983) in
@@ -599,7 +643,8 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal_inc(const Dom<R> *_
                                                                 int tiles_j, int uvoff,
                                                                 int advoff) {
   constexpr int WJ = kTJ + 4;          // columns J0-2 .. J0+TJ+1
-  __shared__ double pp_s[kTI + 4][WJ];  // rows I0-2 .. I0+TI+1
+  __shared__ float pph_s[kTI + 4][WJ];  // rows I0-2 .. I0+TI+1: pp as hi + lo
+  __shared__ float ppl_s[kTI + 4][WJ];
   __shared__ float dz_s[kTI + 4][WJ];   // vertical increment
   __shared__ float dy_s[kTI + 3][WJ];   // pp(i+1) - pp(i), rows I0-2 .. I0+TI
   __shared__ float fy_s[kTI + 1][WJ];   // meridional flux at i, relative to pp(i-1)
@@ -621,38 +666,42 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal_inc(const Dom<R> *_
   if (J0 > jx - 1 || I0 > iy - 1) return;
   const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
   const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
-  const double *__restrict__ pp = (f == 0 ? D.tetav[adv] : D.pai[adv]) + ko;
-  double *__restrict__ out = (f == 0 ? D.tetav[adv ^ 1] : D.pai[adv ^ 1]) + ko;
-  const double *__restrict__ dzg = D.wz_d[f] + ko;
+  const size_t F = g.field3();
+  const DF pp(f == 0 ? D.tetav[adv] : D.pai[adv], F);
+  const DF out(f == 0 ? D.tetav[adv ^ 1] : D.pai[adv ^ 1], F);
+  const DF dzg(D.wz_d[f], F);
   const R *__restrict__ uk = D.u[uv] + ko;
   const R *__restrict__ vk = D.v[uv] + ko;
   const int tid = threadIdx.y * kTJ + threadIdx.x;
   const int nth = kTJ * kTI;
-  const float dta = float(c.dtstepa);
-  const float dtrdx = dta * float(c.rdx), dtrdy = dta * float(c.rdx);
+  const float dta = c.dtstepaf;
+  const float dtrdx = dta * c.rdxf, dtrdy = dta * c.rdxf;
   const bool rot = c.lrotllr != 0;
   const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
 
   for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
     const int rr = e / WJ, cc = e % WJ;
     const int i = I0 - 2 + rr, j = J0 - 2 + cc;
-    double x = 0.0, z = 0.0;
+    F2 x{0.f, 0.f};
+    float z = 0.f;
     if (i >= 1 && i <= iy - 1 && j >= 1 && j <= jx - 1) {
-      const size_t ij = g.at2(j, i);
-      x = pp[ij];
-      z = dzg[ij];
+      const size_t ij = g.at2(j, i) + ko;
+      x = pp.ld(ij);
+      z = df_f(dzg.ld(ij));
     }
-    pp_s[rr][cc] = x;
-    dz_s[rr][cc] = float(z);
+    pph_s[rr][cc] = x.hi;
+    ppl_s[rr][cc] = x.lo;
+    dz_s[rr][cc] = z;
   }
   __syncthreads();
   for (int e = tid; e < (kTI + 3) * WJ; e += nth) {
     const int rr = e / WJ, cc = e % WJ;
-    dy_s[rr][cc] = float(pp_s[rr + 1][cc] - pp_s[rr][cc]);
+    dy_s[rr][cc] = (pph_s[rr + 1][cc] - pph_s[rr][cc]) + (ppl_s[rr + 1][cc] - ppl_s[rr][cc]);
   }
   for (int e = tid; e < kTI * (kTJ + 3); e += nth) {
     const int rr = e / (kTJ + 3), cc = e % (kTJ + 3);
-    dx_s[rr][cc] = float(pp_s[rr + 2][cc + 1] - pp_s[rr + 2][cc]);
+    dx_s[rr][cc] = (pph_s[rr + 2][cc + 1] - pph_s[rr + 2][cc]) +
+                   (ppl_s[rr + 2][cc + 1] - ppl_s[rr + 2][cc]);
   }
   __syncthreads();
   // meridional fluxes at interface rows i = I0 .. I0+TI, relative to pp(i-1)
@@ -702,8 +751,7 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal_inc(const Dom<R> *_
         const float rs = float(sa.rmv[ij]), rn = float(sa.rmv[ijN]);
         hy = mx2 * (fs * zrfms - fn * zrfmn);
         if (rs != 1.f || rn != 1.f)
-          hy += float(pp_s[rr + 2][cc] *
-                      (double)(mx2 * (vs * zrfms * (1.f - rs) - vn * zrfmn * (1.f - rn))));
+          hy += pph_s[rr + 2][cc] * (mx2 * (vs * zrfms * (1.f - rs) - vn * zrfmn * (1.f - rn)));
       }
     }
     hy_s[rr][cc] = hy;
@@ -738,8 +786,8 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal_inc(const Dom<R> *_
     const int i = I0 + rr, j = J0 + cc;
     if (i <= iy - 1 && j <= jx - 1) {
       const size_t ij = g.at2(j, i);
-      const double ppk = pp_s[rr + 2][cc + 2];
-      double x = ppk;
+      const F2 ppk{pph_s[rr + 2][cc + 2], ppl_s[rr + 2][cc + 2]};
+      F2 x = ppk;
       if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
         const float fz = float(sa.fmz[ko + ij]);
         const float uw = float(uk[ij]), ue = float(uk[ij + 1]);
@@ -758,17 +806,21 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal_inc(const Dom<R> *_
           const float rw = float(sa.rmu[ij]), re = float(sa.rmu[ij + 1]);
           hx = mx2 * (fw * zrfmw - fe * zrfme);
           if (rw != 1.f || re != 1.f)
-            hx += float(ppk * (double)(mx2 * (uw * zrfmw * (1.f - rw) - ue * zrfme * (1.f - re))));
+            hx += ppk.hi * (mx2 * (uw * zrfmw * (1.f - rw) - ue * zrfme * (1.f - re)));
         }
-        x = ppk + dzg[ij] + (double)(hy_s[rr][cc + 2] + hx);
+        x = df_add_f(df_add(ppk, dzg.ld(ij + ko)), hy_s[rr][cc + 2] + hx);
       }
-      out[ij] = x;
+      out.st(ij + ko, x);
     }
   }
 }
 
-inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
-  return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y), (unsigned)nmem);
+// grid of a point kernel over nj x ni points per level
+inline dim3 pt_grid(const LaunchGeom &L, int nj, int ni, int &tiles_j) {
+  tiles_j = (nj + L.col_x - 1) / L.col_x;
+  const int ti = (ni + L.col_y - 1) / L.col_y;
+  return dim3((unsigned)(tiles_j * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
+              (unsigned)L.nmem);
 }
 
 }  // namespace
@@ -776,16 +828,19 @@ inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
 template <class R>
 void Launch<R>::adv_prep(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_adv_prep<R><<<grid2(L.jx - 1, L.iy - 1, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+  k_adv_prep<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
 }
 
 template <class R, class T>
 void launch_vertical(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int advoff,
                      cudaStream_t s) {
+  // vert_x columns along j per block, vert_y threads along the levels
   const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
-  const size_t smem = (size_t)3 * (L.kz + 2) * b.x * b.y * sizeof(T);
-  dim3 grd = grid2(L.jx - 1, L.iy - 1, b, L.nmem);
-  grd.x *= (unsigned)nf;
+  const size_t smem = (size_t)5 * (L.kz + 2) * b.x * sizeof(T);
+  const dim3 grd((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * nf), (unsigned)(L.iy - 1),
+                 (unsigned)L.nmem);
   k_adv_vertical<R, T><<<grd, b, smem, s>>>(d, nf, set, advoff);
 }
 
@@ -811,9 +866,9 @@ void launch_horizontal(const LaunchGeom &L, const Dom<R> *d, int nf, int set, in
 template <class R>
 void launch_vertical_inc(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
-  const size_t smem = (size_t)2 * (L.kz + 2) * b.x * b.y * sizeof(float);
-  dim3 grd = grid2(L.jx - 1, L.iy - 1, b, L.nmem);
-  grd.x *= 2u;
+  const size_t smem = (size_t)6 * (L.kz + 2) * b.x * sizeof(float);
+  const dim3 grd((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * 2), (unsigned)(L.iy - 1),
+                 (unsigned)L.nmem);
   k_adv_vertical_inc<R><<<grd, b, smem, s>>>(d, advoff);
 }
 
@@ -854,19 +909,25 @@ void Launch<R>::adv_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, 
 template <class R>
 void Launch<R>::adv_species_copy(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_species_copy<R><<<grid2(L.jx - 1, L.iy - 1, b, L.nmem), b, 0, s>>>(d, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+  k_species_copy<R><<<grd, b, 0, s>>>(d, advoff, tj);
 }
 
 template <class R>
 void Launch<R>::adv_curvature(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_adv_curvature<R><<<grid2(L.jx - 3, L.iy - 3, b, L.nmem), b, 0, s>>>(d, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 3, L.iy - 3, tj);
+  k_adv_curvature<R><<<grd, b, 0, s>>>(d, advoff, tj);
 }
 
 template <class R>
 void Launch<R>::adv_back(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_adv_back<R><<<grid2(L.jx, L.iy, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
+  k_adv_back<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
 }
 
 template <class R>

@@ -99,6 +99,15 @@ Scal make_scal(const mlc_params &p) {
   c.nspgx = p.nspgx;
   c.nztop = p.mo_top_nudge ? p.nztop : 0;
   c.debug_level = p.debug_level;
+  c.dxf = float(c.dx); c.rdxf = float(c.rdx); c.dtsecf = float(c.dtsec);
+  c.dtstepaf = float(c.dtstepa); c.dtsoundf = float(c.dtsound);
+  const double gdts = kGrav * c.dtsound;
+  c.gdts_hi = float(gdts);
+  c.gdts_lo = float(gdts - (double)c.gdts_hi);
+  c.dtrdxs = c.dtsound * c.rdx;
+  c.dxrdt = c.dx / c.dtsound;
+  c.dtrdxsf = c.dtsoundf * c.rdxf;
+  c.dxrdtf = c.dxf / c.dtsoundf;
   return c;
 }
 
@@ -143,6 +152,22 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
   s.tnudge = cv.take<double>(d.kz); s.ffilt = cv.take<double>(d.kz); s.gzitakh = cv.take<double>(d.kz);
   s.xkdamp = cv.take<double>(d.kz); s.xknu = cv.take<double>(d.kz); s.gzitak = cv.take<double>(d.kz + 1);
   s.rlat = cv.take<double>(d.iy);
+  if (f64) {
+    s.gzitak_r = reinterpret_cast<const R *>(s.gzitak);
+    s.gzitakh_r = reinterpret_cast<const R *>(s.gzitakh);
+    s.xkdamp_r = reinterpret_cast<const R *>(s.xkdamp);
+    s.xknu_r = reinterpret_cast<const R *>(s.xknu);
+    s.ffilt_r = reinterpret_cast<const R *>(s.ffilt);
+    s.tnudge_r = reinterpret_cast<const R *>(s.tnudge);
+    s.hefc_r = reinterpret_cast<const R *>(s.hefc);
+    s.fcx_r = reinterpret_cast<const R *>(s.fcx);
+    s.dz_r = reinterpret_cast<const R *>(s.dz);
+  } else {
+    s.gzitak_r = cv.take<R>(d.kz + 1); s.gzitakh_r = cv.take<R>(d.kz);
+    s.xkdamp_r = cv.take<R>(d.kz); s.xknu_r = cv.take<R>(d.kz); s.ffilt_r = cv.take<R>(d.kz);
+    s.tnudge_r = cv.take<R>(d.kz); s.hefc_r = cv.take<R>((size_t)p.nspgx * d.kz);
+    s.fcx_r = cv.take<R>(p.nspgx); s.dz_r = cv.take<R>(F);
+  }
   Bdy<R> &b = D.bd;
   for (int h = 0; h < 2; ++h) {
     b.xtb[h] = cv.take<R>(F); b.xqb[h] = cv.take<R>(F); b.xpaib[h] = cv.take<double>(F);
@@ -443,7 +468,7 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
     REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); nl += 2;
     REC("bdy_relax", K::bdy_relax(L, d, uvo, ao, s)); ++nl;
   }
-  REC("end_cross", K::end_cross(L, d, uvo, ao, s)); ++nl;
+  REC("end_cross", K::end_cross(L, d, uvo, ao, s)); nl += 2;
   REC("end_uvstag", K::end_uvstag(L, d, uvo, ao, s)); ++nl;
   REC("end_reduce", K::end_reduce(L, d, uvo, ao, s)); nl += 2;
   return nl;
@@ -533,6 +558,24 @@ int put3(mlc_ctx *x, const Geom &g, const double *h, R *dst, int nj, int ni, int
   return MLC_OK;
 }
 
+// The same for a double-float field of a mixed member (planes of nplane
+// elements: hi, then lo); an FP64 member takes the plain copy.
+template <class R>
+int put3x(mlc_ctx *x, const Geom &g, const double *h, double *dst, int nj, int ni, int nk,
+          size_t soff, size_t nplane) {
+  if (sizeof(R) == sizeof(double)) return put3<double>(x, g, h, dst, nj, ni, nk, soff);
+  if (!h) return MLC_OK;
+  const size_t n = (size_t)nj * ni * nk;
+  if (soff + n > x->staging_elems) return MLC_ERR_INVALID;
+  MLC_TRY(cudaMemcpyAsync(x->staging + soff, h, n * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+  Launch<R>::unpack3_df(x->staging + soff, dst, g, nj, ni, nk, nplane, x->stream);
+  return MLC_OK;
+}
+
+template <class R>
+int get3x(mlc_ctx *x, const Geom &g, const double *src, double *h, int nj, int ni, int nk,
+          size_t soff, size_t nplane);
+
 template <class R>
 int get3(mlc_ctx *x, const Geom &g, const R *src, double *h, int nj, int ni, int nk, size_t soff) {
   if (!h) return MLC_OK;
@@ -541,6 +584,28 @@ int get3(mlc_ctx *x, const Geom &g, const R *src, double *h, int nj, int ni, int
   Launch<R>::pack3(src, x->staging + soff, g, nj, ni, nk, x->stream);
   MLC_TRY(cudaMemcpyAsync(h, x->staging + soff, n * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
   return MLC_OK;
+}
+
+template <class R>
+int get3x(mlc_ctx *x, const Geom &g, const double *src, double *h, int nj, int ni, int nk,
+          size_t soff, size_t nplane) {
+  if (sizeof(R) == sizeof(double)) return get3<double>(x, g, src, h, nj, ni, nk, soff);
+  if (!h) return MLC_OK;
+  const size_t n = (size_t)nj * ni * nk;
+  if (soff + n > x->staging_elems) return MLC_ERR_INVALID;
+  Launch<R>::pack3_df(src, x->staging + soff, g, nj, ni, nk, nplane, x->stream);
+  MLC_TRY(cudaMemcpyAsync(h, x->staging + soff, n * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
+  return MLC_OK;
+}
+
+// A 1-D array in the field type (mixed members keep FP32 copies).
+template <class R>
+int put1r(mlc_ctx *x, const double *h, const R *dst, size_t n) {
+  if (sizeof(R) == sizeof(double)) return MLC_OK;  // aliases the FP64 array
+  std::vector<R> tmp(n);
+  for (size_t e = 0; e < n; ++e) tmp[e] = (R)h[e];
+  MLC_TRY(cudaMemcpyAsync(W(dst), tmp.data(), n * sizeof(R), cudaMemcpyHostToDevice, x->stream));
+  return cuda_status(cudaStreamSynchronize(x->stream));
 }
 
 // 2-D padded copy of a small host array (built on the host, then one copy).
@@ -586,6 +651,7 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
     for (size_t e = 0; e < nd; ++e)
       if (b[e] > p.nspgx || b[e] == 0 || b[e] < -1) return MLC_ERR_INVALID;
   c.rdzita = 1.0 / s->zita[kz - 1];
+  c.rdzitaf = float(c.rdzita);
   // 3-D metric: one field at a time through the staging buffer
   MLC_CHK(put3<R>(x, g, s->fmz, W(a.fmz), jx - 1, iy - 1, kz, 0));
   MLC_CHK(put3<R>(x, g, s->fmzf, W(a.fmzf), jx - 1, iy - 1, kz + 1, 0));
@@ -595,13 +661,14 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
     const size_t n = (size_t)(jx - 1) * (iy - 1) * (kz + 1);
     std::vector<double> cf(n);
     for (size_t e = 0; e < n; ++e) cf[e] = kCpd * s->fmzf[e] * dtrdz;
-    MLC_CHK(put3<double>(x, g, cf.data(), W(a.cfz), jx - 1, iy - 1, kz + 1, 0));
+    MLC_CHK(put3x<R>(x, g, cf.data(), W(a.cfz), jx - 1, iy - 1, kz + 1, 0, g.PS * (size_t)(kz + 1)));
     MLC_TRY(cudaStreamSynchronize(x->stream));
   }
   MLC_CHK(put3<R>(x, g, s->rfmzu, W(a.rfmzu), jx, iy - 1, kz, 0));
   MLC_CHK(put3<R>(x, g, s->rfmzv, W(a.rfmzv), jx - 1, iy, kz, 0));
   MLC_CHK(put3<double>(x, g, s->zeta, W(a.zeta), jx - 1, iy - 1, kz, 0));
   MLC_CHK(put3<double>(x, g, s->dz, W(a.dz), jx - 1, iy - 1, kz, 0));
+  if (sizeof(R) != sizeof(double)) MLC_CHK(put3<R>(x, g, s->dz, W(a.dz_r), jx - 1, iy - 1, kz, 0));
   // vertical WAF ratios (dtrdz*fmz)/fmzf, Main/mod_moloch.F90:888-889
   {
     const double mo_dzita = s->zita[kz - 1];
@@ -661,17 +728,26 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
   std::vector<double> v1(kz + 1);
   for (int k = 1; k <= kz + 1; ++k) v1[k - 1] = gzita(s->zita[k - 1], p.mo_ztop, p.mo_a0);
   MLC_CHK(put1(x, v1.data(), a.gzitak, kz + 1));
+  MLC_CHK(put1r<R>(x, v1.data(), a.gzitak_r, kz + 1));
   for (int k = 1; k <= kz; ++k) v1[k - 1] = gzita(s->zitah[k - 1], p.mo_ztop, p.mo_a0);
   MLC_CHK(put1(x, v1.data(), a.gzitakh, kz));
+  MLC_CHK(put1r<R>(x, v1.data(), a.gzitakh_r, kz));
   for (int k = 1; k <= kz; ++k)
     v1[k - 1] = kNuMax * kDdamp * (1.0 / (k + 1.0) - 1.0 / (kz + 2.0));
   MLC_CHK(put1(x, v1.data(), a.xkdamp, kz));
+  MLC_CHK(put1r<R>(x, v1.data(), a.xkdamp_r, kz));
   for (int k = 1; k <= kz; ++k)
     v1[k - 1] = kNuMax * (0.55 + 0.45 * ((double)(kz - k + 1) - 1.0) / ((double)kz - 1.0));
   MLC_CHK(put1(x, v1.data(), a.xknu, kz));
+  MLC_CHK(put1r<R>(x, v1.data(), a.xknu_r, kz));
   MLC_CHK(put1(x, s->ffilt, a.ffilt, kz));
-  if (s->tnudge) MLC_CHK(put1(x, s->tnudge, a.tnudge, kz));
-  else MLC_TRY(cudaMemsetAsync(W(a.tnudge), 0, kz * sizeof(double), x->stream));
+  MLC_CHK(put1r<R>(x, s->ffilt, a.ffilt_r, kz));
+  {
+    std::vector<double> tn(kz, 0.0);
+    if (s->tnudge) tn.assign(s->tnudge, s->tnudge + kz);
+    MLC_CHK(put1(x, tn.data(), a.tnudge, kz));
+    MLC_CHK(put1r<R>(x, tn.data(), a.tnudge_r, kz));
+  }
   // Levels nudged at the top: the member's own nztop, the last level with a
   // non-zero tnudge (bdyin sets tnudge > 0 exactly on levels 1..nztop,
   // Main/mod_bdycod.F90:507-537).  A level with tnudge = 0 would be left
@@ -682,7 +758,11 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
     for (int k = 1; k <= kz; ++k)
       if (s->tnudge[k - 1] != 0.0) c.nztop = k;
   MLC_CHK(put1(x, s->hefc, a.hefc, (size_t)p.nspgx * kz));
-  if (s->fcx) MLC_CHK(put1(x, s->fcx, a.fcx, p.nspgx));
+  MLC_CHK(put1r<R>(x, s->hefc, a.hefc_r, (size_t)p.nspgx * kz));
+  if (s->fcx) {
+    MLC_CHK(put1(x, s->fcx, a.fcx, p.nspgx));
+    MLC_CHK(put1r<R>(x, s->fcx, a.fcx_r, p.nspgx));
+  }
   if (s->rlat) MLC_CHK(put1(x, s->rlat, a.rlat, iy));
   MLC_TRY(cudaStreamSynchronize(x->stream));
   return MLC_OK;
@@ -703,8 +783,8 @@ int upload_state_impl(mlc_ctx *x, int slot, const mlc_state_ptrs *h) {
   MLC_CHK(put3<R>(x, g, h->u, st.u, jx, iy - 1, kz, adv((size_t)jx * (iy - 1) * kz)));
   MLC_CHK(put3<R>(x, g, h->v, st.v, jx - 1, iy, kz, adv((size_t)(jx - 1) * iy * kz)));
   MLC_CHK(put3<R>(x, g, h->w, st.w, jx - 1, iy - 1, kz + 1, adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
-  MLC_CHK(put3<double>(x, g, h->pai, st.pai, jx - 1, iy - 1, kz, adv(c3)));
-  MLC_CHK(put3<double>(x, g, h->tetav, st.tetav, jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(put3x<R>(x, g, h->pai, st.pai, jx - 1, iy - 1, kz, adv(c3), g.field3()));
+  MLC_CHK(put3x<R>(x, g, h->tetav, st.tetav, jx - 1, iy - 1, kz, adv(c3), g.field3()));
   R *f3[] = {st.t, st.tvirt, st.ux, st.vx, st.p, st.rho, st.qsat};
   const double *h3[] = {h->t, h->tvirt, h->ux, h->vx, h->p, h->rho, h->qsat};
   for (int q = 0; q < 7; ++q) MLC_CHK(put3<R>(x, g, h3[q], f3[q], jx - 1, iy - 1, kz, adv(c3)));
@@ -737,8 +817,8 @@ int download_state_impl(mlc_ctx *x, int slot, const mlc_state_ptrs *h) {
   MLC_CHK(get3<R>(x, g, st.u, h->u, jx, iy - 1, kz, adv((size_t)jx * (iy - 1) * kz)));
   MLC_CHK(get3<R>(x, g, st.v, h->v, jx - 1, iy, kz, adv((size_t)(jx - 1) * iy * kz)));
   MLC_CHK(get3<R>(x, g, st.w, h->w, jx - 1, iy - 1, kz + 1, adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
-  MLC_CHK(get3<double>(x, g, st.pai, h->pai, jx - 1, iy - 1, kz, adv(c3)));
-  MLC_CHK(get3<double>(x, g, st.tetav, h->tetav, jx - 1, iy - 1, kz, adv(c3)));
+  MLC_CHK(get3x<R>(x, g, st.pai, h->pai, jx - 1, iy - 1, kz, adv(c3), g.field3()));
+  MLC_CHK(get3x<R>(x, g, st.tetav, h->tetav, jx - 1, iy - 1, kz, adv(c3), g.field3()));
   const R *f3[] = {st.t, st.tvirt, st.ux, st.vx, st.p, st.rho, st.qsat};
   double *h3[] = {h->t, h->tvirt, h->ux, h->vx, h->p, h->rho, h->qsat};
   for (int q = 0; q < 7; ++q) MLC_CHK(get3<R>(x, g, f3[q], h3[q], jx - 1, iy - 1, kz, adv(c3)));
@@ -773,7 +853,7 @@ int set_boundary_impl(mlc_ctx *x, Member &mb, const mlc_bdy_ptrs *b) {
   for (int s = 0; s < 2; ++s) {
     MLC_CHK(put3<R>(x, g, b->xtb[s], W(a.xtb[s]), jx - 1, iy - 1, kz, 0));
     MLC_CHK(put3<R>(x, g, b->xqb[s], W(a.xqb[s]), jx - 1, iy - 1, kz, 0));
-    MLC_CHK(put3<double>(x, g, b->xpaib[s], W(a.xpaib[s]), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3x<R>(x, g, b->xpaib[s], W(a.xpaib[s]), jx - 1, iy - 1, kz, 0, F));
     if (p.present_qc) MLC_CHK(put3<R>(x, g, b->xlb[s], W(a.xlb[s]), jx - 1, iy - 1, kz, 0));
     if (p.present_qi) MLC_CHK(put3<R>(x, g, b->xib[s], W(a.xib[s]), jx - 1, iy - 1, kz, 0));
     MLC_CHK(put3<R>(x, g, b->dub[s], W(a.dub[s]), jx, iy - 1, kz, 0));
@@ -822,7 +902,7 @@ int create_common(const mlc_params *params, int capacity, size_t budget, mlc_ctx
   LaunchGeom &L = x->key.L;
   L.col_x = 32; L.col_y = 4;
   L.solve_x = 32; L.solve_y = 2;
-  L.vert_x = 32; L.vert_y = 2;
+  L.vert_x = 32; L.vert_y = 8;
   L.htile = 0;
   cudaError_t e = cudaGetDevice(&x->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking);
@@ -1145,7 +1225,7 @@ namespace {
 
 const int kColCand[][2] = {{32, 4}, {32, 8}, {64, 2}, {64, 4}, {128, 1}, {16, 8}};
 const int kSolveCand[][2] = {{32, 2}, {32, 1}, {64, 1}, {32, 4}, {16, 4}};
-const int kVertCand[][2] = {{32, 2}, {32, 1}, {64, 1}, {32, 4}, {16, 4}};
+const int kVertCand[][2] = {{32, 8}, {32, 4}, {64, 4}, {32, 16}, {64, 8}};
 constexpr int kNCol = 6, kNSolve = 5, kNVert = 5, kNTile = 4;
 
 int group_of(const char *name) {
@@ -1159,8 +1239,8 @@ int group_of(const char *name) {
 bool shapes_fit(const LaunchGeom &L) {
   const size_t col3 = (size_t)3 * (L.kz + 2) * sizeof(double);
   if (col3 * L.solve_x * L.solve_y > 200 * 1024) return false;
-  if (col3 * L.vert_x * L.vert_y > 200 * 1024) return false;
-  return L.col_x * L.col_y <= 1024;
+  if ((size_t)6 * (L.kz + 2) * L.vert_x * sizeof(double) > 200 * 1024) return false;
+  return L.col_x * L.col_y <= 1024 && L.vert_x * L.vert_y <= 1024;
 }
 
 // Per-group device time (ms) of `steps` eager steps with the shapes in x->key.L.
@@ -1239,7 +1319,7 @@ int autotune_impl(mlc_ctx *x, int steps, mlc_tune_report *rep) {
     for (int q = 0; q < 4; ++q)
       if (ms[q] < best[q]) { best[q] = ms[q]; pick[q] = idx[q]; }
   }
-  // the fixed configuration: 32 x 8 columns and tiles, 32 x 2 solve/vertical
+  // the fixed configuration: 32 x 8 columns, tiles and vertical blocks, 32 x 2 solve
   LaunchGeom fixed = base;
   set_shapes(fixed, 1, 0, 0, 0);
   double msf[4] = {0, 0, 0, 0}, mst[4] = {0, 0, 0, 0};

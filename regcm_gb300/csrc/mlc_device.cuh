@@ -29,9 +29,14 @@ struct Geom {
   __host__ __device__ size_t field3() const { return PS * (size_t)kz; }
 };
 
-// Scalars of one domain (all derived on the host once, in FP64).
+// Scalars of one domain (all derived on the host once, in FP64; the f-suffixed
+// copies are the same values rounded to FP32 once, for the FP32 kernels).
 struct Scal {
   double dx, rdx, dtsec, dt, dtstepa, dtsound, rdzita, dtbdys, rtb;
+  float dxf, rdxf, dtsecf, dtstepaf, dtsoundf, rdzitaf;
+  float gdts_hi, gdts_lo;   // g*dtsound as a double-float
+  double dtrdxs, dxrdt;     // dtsound*rdx, dx/dtsound (acoustic substep)
+  float dtrdxsf, dxrdtf;
   int nadv, nsound, divdamp, divfilter, top_nudge, apply_bdy, lrotllr, ipptls;
   int present_qc, present_qi, nspgx, nztop, debug_level;
   int hb_cr, hb_ud, hb_vd;  // relaxation zone non-empty (ba%havebound)
@@ -54,6 +59,8 @@ struct Stat {
   const double *tnudge, *ffilt, *gzitakh, *xkdamp, *xknu;      // (kz), 1-based via [k-1]
   const double *gzitak;    // (kz+1)
   const double *rlat;      // (iy)
+  // the 1-D arrays, hefc, fcx and dz in the field type (aliases for FP64)
+  const R *gzitak_r, *gzitakh_r, *xkdamp_r, *xknu_r, *ffilt_r, *tnudge_r, *hefc_r, *fcx_r, *dz_r;
 };
 
 // Prognostic and diagnostic state.
@@ -129,6 +136,88 @@ struct Dom {
   int red_blocks, rows_per_block;
   int active;            // 0: an empty slot, every block returns at once
 };
+
+// A per-domain constant in the kernel's field type: the FP64 value for an
+// FP64 member, its FP32 copy for a mixed one (no conversion on the device).
+template <class R>
+__device__ __forceinline__ R pick(double d, float f) {
+  if constexpr (sizeof(R) == sizeof(double)) return d;
+  else return f;
+}
+
+// ---- double-float values of a mixed member ----------------------------------
+// theta_v, Exner, theta_v at half levels, the vertical increments of the
+// increment-form advection, cp*fmzf*dtrdz and the boundary Exner values of a
+// mixed member are kept as unevaluated sums hi + lo of two floats (about 48
+// significant bits) in two planes of the field's 8-byte-per-element
+// allocation: hi in elements [0, n), lo in [n, 2n) of the float view.
+// Arithmetic on them uses error-free transformations - TwoSum (Knuth, The Art
+// of Computer Programming vol. 2, 4.2.2), Fast2Sum (Dekker 1971) and
+// TwoProduct with a fused multiply-add - so the FP32 path runs no FP64
+// instruction.  The code relies on IEEE FP32 addition (no fast-math).
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ F2 fast_two_sum(float a, float b) {  // needs |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ F2 two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ F2 df_add(F2 a, F2 b) {
+  const F2 s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ F2 df_add_f(F2 a, float b) {
+  const F2 s = two_sum(a.hi, b);
+  return fast_two_sum(s.hi, s.lo + a.lo);
+}
+__device__ __forceinline__ F2 df_mul(F2 a, F2 b) {
+  const F2 p = two_prod(a.hi, b.hi);
+  return fast_two_sum(p.hi, p.lo + (a.hi * b.lo + a.lo * b.hi));
+}
+__device__ __forceinline__ F2 df_mul_f(F2 a, float b) {
+  const F2 p = two_prod(a.hi, b);
+  return fast_two_sum(p.hi, fmaf(a.lo, b, p.lo));
+}
+// a - b rounded to FP32 (the hi difference is exact for values within 2x)
+__device__ __forceinline__ float df_diff(F2 a, F2 b) { return (a.hi - b.hi) + (a.lo - b.lo); }
+__device__ __forceinline__ float df_f(F2 a) { return a.hi + a.lo; }
+
+// Planes of n double-float elements over an 8-byte-per-element allocation.
+struct DF {
+  float *p;
+  size_t n;
+  __device__ __forceinline__ DF(const double *a, size_t n_)
+      : p(reinterpret_cast<float *>(const_cast<double *>(a))), n(n_) {}
+  __device__ __forceinline__ F2 ld(size_t o) const { return {p[o], p[o + n]}; }
+  __device__ __forceinline__ void st(size_t o, F2 v) const { p[o] = v.hi; p[o + n] = v.lo; }
+  __device__ __forceinline__ float hi(size_t o) const { return p[o]; }
+};
+
+// Point kernels run one thread per grid point (j, i, k): blocks of
+// (blockDim.x, blockDim.y) points along (j, i); grid x = the tiles along j
+// times the tiles along i, y = the level, z = the member.  j0, i0 are the
+// first j and i the kernel covers.
+struct Pt {
+  int j, i, k;
+};
+// Levels one thread of a point kernel runs (its per-thread setup - the
+// member's descriptor, roles and 2-D metric - is shared by them); grid y
+// counts chunks of this many levels and Pt::k is the chunk's first level.
+constexpr int kPtLevels = 4;
+__device__ __forceinline__ Pt point_of(int tiles_j, int j0, int i0) {
+  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  return {bj * (int)blockDim.x + (int)threadIdx.x + j0, bi * (int)blockDim.y + (int)threadIdx.y + i0,
+          (int)blockIdx.y * kPtLevels + 1};
+}
 
 // The state with the roles the launch works on.
 template <class R>

@@ -25,31 +25,38 @@ __device__ __forceinline__ R qfactor(const R *qx, size_t o, size_t F, int ipptls
 
 // dynamical_core :1121-1123 and tvirt_to_temp :1629-1648
 template <class R>
-__global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff) {
+__global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
   const Scal &c = D.c;
   const State<R> st = state_of(D, 0, (D.clk->adv_role + advoff) & 1);
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const Pt q_ = point_of(tiles_j, 1, 1);
+  const int j = q_.j, k0 = q_.k;
+  if (k0 > g.kz) return;
+  const int i = q_.i;
   if (j > g.jx - 1 || i > g.iy - 1) return;
   const bool inner = j >= 2 && j <= g.jx - 2 && i >= 2 && i <= g.iy - 2;
   const size_t ij = g.at2(j, i), F = g.field3();
-  const bool mixed = sizeof(R) == sizeof(float);
-  for (int k = 1; k <= g.kz; ++k) {
+#pragma unroll
+  for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * g.PS;
-    const double pk = st.pai[o];
-    const R tv = R(st.tetav[o] * pk);
-    st.tvirt[o] = tv;
     const R qf = qfactor(st.qx, o, F, c.ipptls);
-    if (inner) st.t[o] = tv / qf;
-    if (mixed) {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      const DF th(st.tetav, F), pa(st.pai, F);
+      const F2 pk = pa.ld(o);
+      const R tv = df_f(df_mul(th.ld(o), pk));
+      st.tvirt[o] = tv;
+      if (inner) st.t[o] = tv / qf;
       // what status_update needs to carry theta_v over as a ratio
       // (t_end = tvirt/qf also at the ring, where t itself is not refreshed)
       D.wz[0][o] = qf;
       D.wz[1][o] = inner ? st.t[o] : tv / qf;
-      D.wz_d[0][o] = pk;
+      DF(D.wz_d[0], F).st(o, pk);
+    } else {
+      const R tv = R(st.tetav[o] * st.pai[o]);
+      st.tvirt[o] = tv;
+      if (inner) st.t[o] = tv / qf;
     }
   }
 }
@@ -78,6 +85,17 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
   const double cx0 = 1.0 - cx1;
   const R rx0 = R(x0), rx1 = R(x1);
   const size_t PS = g.PS, F = g.field3(), ko = (size_t)(k - 1) * PS;
+  // Exner at a ring point: x0*b0 + x1*b1 (a mixed member: b0 + x1*(b1 - b0)
+  // in double-float)
+  auto set_pai_ring = [&](size_t ob) {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      const DF b0(bd.xpaib[0], F), b1(bd.xpaib[1], F);
+      const F2 a = b0.ld(ob);
+      DF(st.pai, F).st(ob, df_add_f(a, float(x1) * df_diff(b1.ld(ob), a)));
+    } else {
+      st.pai[ob] = x0 * bd.xpaib[0][ob] + x1 * bd.xpaib[1][ob];
+    }
+  };
   auto blend = [&](const R *const *b, size_t o) { return rx0 * b[0][o] + rx1 * b[1][o]; };
   const int nqx = g.nqx;
   if (phase == 0) {
@@ -93,7 +111,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     const R un = blend(bd.dub, od);
     st.u[od] = un;
     st.t[ob] = blend(bd.xtb, ob);
-    st.pai[ob] = x0 * bd.xpaib[0][ob] + x1 * bd.xpaib[1][ob];
+    set_pai_ring(ob);
     st.qx[ob] = blend(bd.xqb, ob);
     if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
     if (c.present_qi && c.ipptls > 1) st.qx[ob + 2 * F] = blend(bd.xib, ob);
@@ -122,7 +140,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     const R vn = blend(bd.dvb, od);
     st.v[od] = vn;
     st.t[ob] = blend(bd.xtb, ob);
-    st.pai[ob] = x0 * bd.xpaib[0][ob] + x1 * bd.xpaib[1][ob];
+    set_pai_ring(ob);
     st.qx[ob] = blend(bd.xqb, ob);
     if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
     if (c.present_qi && c.ipptls > 1) st.qx[ob + 2 * F] = blend(bd.xib, ob);
@@ -144,7 +162,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
 // (boundary, Main/mod_moloch.F90:478-497), per point; the clock has already
 // moved by dtsec.
 template <class R>
-__global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+__global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
@@ -153,8 +171,10 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const Bdy<R> &bd = D.bd;
   const Clock *clk = D.clk;
   const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const Pt q_ = point_of(tiles_j, 2, 2);
+  const int j = q_.j, k0 = q_.k;
+  if (k0 > g.kz) return;
+  const int i = q_.i;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   if (j > jx - 1 || i > iy - 1) return;
   const double xb = clk->xbctime + c.dtsec;
@@ -175,20 +195,24 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const int ibv = vp ? sa.ibnd_vd[ij] : -1;
   auto blend = [&](const R *const *b, size_t o) { return rx0 * b[0][o] + rx1 * b[1][o]; };
   auto relax = [&](R f, R fext, int ib, int k) {
-    const R xf = R(sa.hefc[(size_t)(ib - 1) + (size_t)(k - 1) * nsp]);
+    const R xf = sa.hefc_r[(size_t)(ib - 1) + (size_t)(k - 1) * nsp];
     return (R(1) - xf) * f + xf * fext;
   };
-  if (cr && c.top_nudge) {
-    const size_t o = ij + PS;  // level 2
-    const R xf = R(wrtau * c.dtsec);
-    const R w2 = st.w[o];
-    const R fext = R(0) * w2;
-    st.w[o] = (R(1) - xf) * w2 + xf * fext;
-  }
-  for (int k = 1; k <= kz; ++k) {
+  const R xfn0 = pick<R>(trtau * c.dtsec, float(trtau * c.dtsec));
+#pragma unroll
+  for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
+    if (k == 2 && cr && c.top_nudge) {
+      const size_t o2 = ij + PS;  // level 2 (w sponge, before the level's relaxation)
+      const R xf = R(wrtau * c.dtsec);
+      const R w2 = st.w[o2];
+      const R fext = R(0) * w2;
+      st.w[o2] = (R(1) - xf) * w2 + xf * fext;
+    }
     const size_t o = ij + (size_t)(k - 1) * PS;
     const bool nud = c.top_nudge && k <= c.nztop;
-    const R xfn = nud ? R(sa.tnudge[k - 1] * trtau * c.dtsec) : R(0);
+    R xfn;
+    if constexpr (sizeof(R) == sizeof(float)) xfn = nud ? sa.tnudge_r[k - 1] * xfn0 : R(0);
+    else xfn = nud ? R(sa.tnudge[k - 1] * trtau * c.dtsec) : R(0);
     if (up) {
       R f = st.u[o];
       if (nud) f = (R(1) - xfn) * f + xfn * blend(bd.dub, o);
@@ -209,7 +233,13 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
       st.t[o] = f;
     }
     if (ibc <= 0) continue;
-    {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      // (1 - xf)*pai + xf*(b0 + x1*(b1 - b0)) as pai + xf*((b0 - pai) + x1*(b1 - b0))
+      const float xf = sa.hefc_r[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
+      const DF pa(st.pai, F), b0(bd.xpaib[0], F), b1(bd.xpaib[1], F);
+      const F2 p = pa.ld(o), a = b0.ld(o);
+      pa.st(o, df_add_f(p, xf * (df_diff(a, p) + float(x1) * df_diff(b1.ld(o), a))));
+    } else {
       const double xf = sa.hefc[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
       const double fext = x0 * bd.xpaib[0][o] + x1 * bd.xpaib[1][o];
       st.pai[o] = (1.0 - xf) * st.pai[o] + xf * fext;
@@ -217,7 +247,7 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
     st.qx[o] = relax(st.qx[o], blend(bd.xqb, o), ibc, k);
     {
       // morelax_fraction with frac = 0 (:3962-3993)
-      const R xf = R(sa.hefc[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp]);
+      const R xf = sa.hefc_r[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
       const R f = st.w[o];
       st.w[o] = (R(1) - xf) * f + xf * f * R(0);
     }
@@ -225,36 +255,77 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
     if (c.ipptls > 1 && c.present_qi) st.qx[o + 2 * F] = relax(st.qx[o + 2 * F], blend(bd.xib, o), ibc, k);
     for (int n = 0; n < g.ntr; ++n) {
       const size_t on = o + (size_t)n * F;
-      const R xf = R(sa.fcx[ibc - 1]);
+      const R xf = sa.fcx_r[ibc - 1];
       const R fext = R(cx0) * bd.chib[0][on] + R(cx1) * bd.chib[1][on];
       st.trac[on] = (R(1) - xf) * st.trac[on] + xf * fext;
     }
   }
 }
 
-// Cross-point work after the boundary: uvstagtouvx and temp_to_tvirt of
-// boundary (:520-523), p (:348-352), extrapolate_surface_pressure
-// (:1592-1606), then status_update (:1403-1443): q clamps, tvirt, tetav,
-// rho, qsat.  rho and qsat of :348-352 are recomputed from the same t and p
-// by status_update, so they are computed once, after it.
+// extrapolate_surface_pressure (:1592-1606) per interior column, from t
+// and q at the two lowest levels before status_update clamps q, and p at the
+// lowest level (the same expression k_end_cross stores).
 template <class R>
-__global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+__global__ void k_end_ps(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
-  if (j > jx - 1 || i > iy - 1) return;
+  if (j > jx - 2 || i > iy - 2) return;
+  const size_t ij = g.at2(j, i), PS = g.PS, F = g.field3();
+  const int ipp = c.ipptls;
+  // tvirt at kz-1, kz before the clamps: from the boundary's temp_to_tvirt,
+  // or tetav*pai of dynamical_core when the boundary is off
+  const size_t o1 = ij + (size_t)(kz - 2) * PS, o2 = ij + (size_t)(kz - 1) * PS;
+  double tv1, tv2;
+  if (c.apply_bdy) {
+    tv1 = (double)(st.t[o1] * qfactor(st.qx, o1, F, ipp));
+    tv2 = (double)(st.t[o2] * qfactor(st.qx, o2, F, ipp));
+  } else {
+    tv1 = (double)st.tvirt[o1];
+    tv2 = (double)st.tvirt[o2];
+  }
+  R p2;
+  if constexpr (sizeof(R) == sizeof(float)) p2 = exner_to_pressure_f(df_f(DF(st.pai, F).ld(o2)));
+  else p2 = (R)exner_to_pressure(st.pai[o2]);
+  const double z1 = sa.zeta[o1], z2 = sa.zeta[o2];
+  double lrt = (tv1 - tv2) / (z1 - z2);
+  if (lrt < -kGovcp) lrt = -kGovcp;
+  else if (lrt > -0.005) lrt = 0.65 * lrt - 0.35 * kLrate;
+  const double tv = tv2 - lrt * 0.5 * z2;
+  st.ps[ij] = (double)p2 * exp(kGovr * z2 / tv);
+}
+
+// Cross-point work after the boundary, per point: uvstagtouvx and
+// temp_to_tvirt of boundary (:520-523), p (:348-352), then status_update
+// (:1403-1443): q clamps, tvirt, tetav, rho, qsat (the surface pressure is
+// k_end_ps's, launched first).  rho and qsat of :348-352 are recomputed from the same t and p
+// by status_update, so they are computed once, after it.
+template <class R>
+__global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
+  const Pt q_ = point_of(tiles_j, 1, 1);
+  const int j = q_.j, i = q_.i;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  if (j > jx - 1 || i > iy - 1 || q_.k > kz) return;
   const size_t ij = g.at2(j, i), PS = g.PS, F = g.field3(), S = (size_t)g.P;
   const bool inner = j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2;
   const int ipp = c.ipptls;
+#pragma unroll
+  for (int k = q_.k; k < q_.k + kPtLevels && k <= kz; ++k) {
+  const size_t o = ij + (size_t)(k - 1) * PS;
   if (c.apply_bdy) {
-    for (int k = 1; k <= kz; ++k) {
-      const size_t o = ij + (size_t)(k - 1) * PS;
+    {
       const R *u = st.u, *v = st.v;
       R a;
       if (j == 1) a = R(0.5) * (u[o] + u[o + 1]);
@@ -268,33 +339,12 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
     }
   }
   // pressure (FP64 Exner reconstruction; FP32 for the FP32 field of a mixed member)
-  for (int k = 1; k <= kz; ++k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    if constexpr (sizeof(R) == sizeof(float)) st.p[o] = exner_to_pressure_f(float(st.pai[o]));
+  {
+    if constexpr (sizeof(R) == sizeof(float)) st.p[o] = exner_to_pressure_f(df_f(DF(st.pai, F).ld(o)));
     else st.p[o] = (R)exner_to_pressure(st.pai[o]);
   }
-  if (inner) {
-    // tvirt at kz-1, kz before the clamps: from the boundary's temp_to_tvirt,
-    // or tetav*pai of dynamical_core when the boundary is off
-    const size_t o1 = ij + (size_t)(kz - 2) * PS, o2 = ij + (size_t)(kz - 1) * PS;
-    double tv1, tv2;
-    if (c.apply_bdy) {
-      tv1 = (double)(st.t[o1] * qfactor(st.qx, o1, F, ipp));
-      tv2 = (double)(st.t[o2] * qfactor(st.qx, o2, F, ipp));
-    } else {
-      tv1 = (double)st.tvirt[o1];
-      tv2 = (double)st.tvirt[o2];
-    }
-    const double z1 = sa.zeta[o1], z2 = sa.zeta[o2];
-    double lrt = (tv1 - tv2) / (z1 - z2);
-    if (lrt < -kGovcp) lrt = -kGovcp;
-    else if (lrt > -0.005) lrt = 0.65 * lrt - 0.35 * kLrate;
-    const double tv = tv2 - lrt * 0.5 * z2;
-    st.ps[g.at2(j, i)] = (double)st.p[o2] * exp(kGovr * z2 / tv);
-  }
   // status_update
-  for (int k = 1; k <= kz; ++k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
+  {
     if (inner) {
       for (int n = 0; n < g.nqx; ++n) {
         const size_t on = o + (size_t)n * F;
@@ -318,23 +368,28 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
       // (the interior) theta_v keeps every FP64 digit; elsewhere the ratio's
       // FP32 rounding falls on the change, not on theta_v.
       const float qf0 = D.wz[0][o], t0 = D.wz[1][o];
-      const double p0 = D.wz_d[0][o], p1 = st.pai[o];
+      const F2 p0 = DF(D.wz_d[0], F).ld(o), p1 = DF(st.pai, F).ld(o);
       const float rt = (tk - t0) / t0;
       const float rq = (qf - qf0) / qf0;
-      const float rp = p0 != p1 ? float(p0 - p1) / float(p1) : 0.f;
+      const float rp = (p0.hi != p1.hi || p0.lo != p1.lo) ? df_diff(p0, p1) / p1.hi : 0.f;
       const float eps = rt + rq + rp + rt * rq + (rt + rq + rt * rq) * rp;
-      if (eps != 0.f) st.tetav[o] = fma(st.tetav[o], (double)eps, st.tetav[o]);
+      if (eps != 0.f) {
+        const DF th(st.tetav, F);
+        const F2 t = th.ld(o);
+        th.st(o, df_add(t, df_mul_f(t, eps)));
+      }
       st.qsat[o] = pfwsat_f(tk, pk);
     } else {
       st.tetav[o] = (double)tv / st.pai[o];
       st.qsat[o] = (R)pfwsat((double)tk, (double)pk);
     }
   }
+  }
 }
 
 // uvxtouvstag at the end of status_update (:1440)
 template <class R>
-__global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+__global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
@@ -343,15 +398,18 @@ __global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int adv
   const R *__restrict__ vx = D.vx[adv];
   R *__restrict__ u = D.u[uv];
   R *__restrict__ v = D.v[uv];
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const Pt q_ = point_of(tiles_j, 1, 1);
+  const int j = q_.j, k0 = q_.k;
+  if (k0 > g.kz) return;
+  const int i = q_.i;
   const int jx = g.jx, iy = g.iy;
   if (j > jx || i > iy) return;
   const size_t ij = g.at2(j, i), PS = g.PS, S = (size_t)g.P;
   const bool do_u = (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2);
   const bool do_v = (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 1);
   if (!do_u && !do_v) return;
-  for (int k = 1; k <= g.kz; ++k) {
+#pragma unroll
+  for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     if (do_u) {
       R a;
@@ -398,6 +456,8 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
   const size_t F = g.field3();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double dry = 0, dadv = 0, qm = 0, qadv = 0, pmax = -INFINITY, pmin = INFINITY, bad = 0;
+  F2 dry2{0.f, 0.f}, qm2{0.f, 0.f}, dadv2{0.f, 0.f}, qadv2{0.f, 0.f};
+  bool lanes_used = false;  // lanes other than 0 hold boundary-flux or ps partials
   const int nrows = (iy - 1) * kz;  // rows (i in ice, k)
   const int r0 = blockIdx.x * rows_per_block;
   const bool budget = c.debug_level > 0;
@@ -406,14 +466,15 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
     const size_t ko = (size_t)(k - 1) * g.PS;
     if (budget && i >= 2 && i <= iy - 2) {
       if constexpr (sizeof(R) == sizeof(float)) {
-        // FP32 fields: FP32 point products, FP64 sums, dx^2 applied once below
+        // FP32 fields: FP32 point products, compensated FP32 sums (double-
+        // float), dx^2 applied once below
         for (int j = 2 + lane; j <= jx - 2; j += 32) {
           const size_t o = g.at2(j, i) + ko;
-          const float dr = float(sa.dz[o]) * float(st.rho[o]);
+          const float dr = sa.dz_r[o] * st.rho[o];
           float qs = 0.f;
-          for (int n = 0; n < g.nqx; ++n) qs += float(st.qx[o + (size_t)n * F]);
-          dry += (double)dr;
-          qm += (double)(dr * qs);
+          for (int n = 0; n < g.nqx; ++n) qs += st.qx[o + (size_t)n * F];
+          dry2 = df_add_f(dry2, dr);
+          qm2 = df_add_f(qm2, dr * qs);
         }
       } else {
         for (int j = 2 + lane; j <= jx - 2; j += 32) {
@@ -425,7 +486,22 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
         }
       }
     }
-    if (budget && lane == 0) {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      if (budget && lane == 0) {
+        // west and east columns (FP32 products, double-float sums)
+        const size_t ow = g.at2(1, i) + ko, oe = g.at2(jx - 1, i) + ko;
+        const float dtdx = float(dt * dx);
+        const float fw = st.u[g.at2(1, i) + ko] * dtdx * sa.dz_r[ow] * st.rho[ow];
+        const float fe = st.u[g.at2(jx, i) + ko] * dtdx * sa.dz_r[oe] * st.rho[oe];
+        dadv2 = df_add_f(df_add_f(dadv2, fw), -fe);
+        float qw = 0.f, qe = 0.f;
+        for (int n = 0; n < g.nqx; ++n) {
+          qw += st.qx[ow + (size_t)n * F];
+          qe += st.qx[oe + (size_t)n * F];
+        }
+        qadv2 = df_add_f(df_add_f(qadv2, qw * fw), -(qe * fe));
+      }
+    } else if (budget && lane == 0) {
       // west and east columns over i in ice (Main/mod_massck.F90:85-100)
       const size_t ow = g.at2(1, i) + ko, oe = g.at2(jx - 1, i) + ko;
       const double uw = (double)st.u[g.at2(1, i) + ko], ue = (double)st.u[g.at2(jx, i) + ko];
@@ -439,6 +515,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
       }
     }
     if (budget && (i == 1 || i == iy - 1)) {
+      lanes_used = true;
       // south (v at ide1) and north (v at ide2) rows, j in jci (:101-116)
       const int iv = (i == 1) ? 1 : iy;
       const bool south = (i == 1);
@@ -455,6 +532,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
       }
     }
     if (k == 1 && i >= 2 && i <= iy - 2) {
+      lanes_used = true;
       for (int j = 2 + lane; j <= jx - 2; j += 32) {
         const double x = st.ps[g.at2(j, i)];
         if (!isfinite(x)) bad = 1;
@@ -462,18 +540,35 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
       }
     }
   }
+  const unsigned full = 0xffffffffu;
   if constexpr (sizeof(R) == sizeof(float)) {
-    dry *= dxsq;
-    qm *= dxsq;
+    // warp sums of the double-float partials in FP32, then dx^2 in FP64 once
+    for (int off = 16; off > 0; off >>= 1) {
+      dry2 = df_add(dry2, F2{__shfl_down_sync(full, dry2.hi, off), __shfl_down_sync(full, dry2.lo, off)});
+      qm2 = df_add(qm2, F2{__shfl_down_sync(full, qm2.hi, off), __shfl_down_sync(full, qm2.lo, off)});
+    }
+    if (lane == 0) {
+      dry = ((double)dry2.hi + (double)dry2.lo) * dxsq;
+      qm = ((double)qm2.hi + (double)qm2.lo) * dxsq;
+      dadv += (double)dadv2.hi + (double)dadv2.lo;
+      qadv += (double)qadv2.hi + (double)qadv2.lo;
+    }
+  } else {
+    for (int off = 16; off > 0; off >>= 1) {
+      dry += __shfl_down_sync(full, dry, off);
+      qm += __shfl_down_sync(full, qm, off);
+    }
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    dry += __shfl_down_sync(0xffffffffu, dry, off);
-    dadv += __shfl_down_sync(0xffffffffu, dadv, off);
-    qm += __shfl_down_sync(0xffffffffu, qm, off);
-    qadv += __shfl_down_sync(0xffffffffu, qadv, off);
-    bad += __shfl_down_sync(0xffffffffu, bad, off);
-    pmax = fmax(pmax, __shfl_down_sync(0xffffffffu, pmax, off));
-    pmin = fmin(pmin, __shfl_down_sync(0xffffffffu, pmin, off));
+  // the boundary fluxes and ps extrema live in lane 0 unless the warp had a
+  // south/north row or the surface row
+  if (__any_sync(full, lanes_used)) {
+    for (int off = 16; off > 0; off >>= 1) {
+      dadv += __shfl_down_sync(full, dadv, off);
+      qadv += __shfl_down_sync(full, qadv, off);
+      bad += __shfl_down_sync(full, bad, off);
+      pmax = fmax(pmax, __shfl_down_sync(full, pmax, off));
+      pmin = fmin(pmin, __shfl_down_sync(full, pmin, off));
+    }
   }
   if (lane == 0) {
     sh[warp][0] = dry; sh[warp][1] = dadv; sh[warp][2] = qm; sh[warp][3] = qadv;
@@ -548,8 +643,46 @@ __global__ void k_pack3(const R *__restrict__ src, double *__restrict__ dst, Geo
   }
 }
 
+// hi = fl(x), lo = fl(x - hi): x to ~48 bits as two floats
+__global__ void k_unpack3_df(const double *__restrict__ src, float *__restrict__ dst, Geom g, int nj,
+                             int ni, int nk, size_t nplane) {
+  const size_t n = (size_t)nj * ni * nk;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e % nj);
+    const size_t r = e / nj;
+    const int i = (int)(r % ni);
+    const int k = (int)(r / ni);
+    const size_t o = (size_t)j + (size_t)i * g.P + (size_t)k * g.PS;
+    const double x = src[e];
+    const float hi = (float)x;
+    dst[o] = hi;
+    dst[o + nplane] = (float)(x - (double)hi);
+  }
+}
+
+__global__ void k_pack3_df(const float *__restrict__ src, double *__restrict__ dst, Geom g, int nj,
+                           int ni, int nk, size_t nplane) {
+  const size_t n = (size_t)nj * ni * nk;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e % nj);
+    const size_t r = e / nj;
+    const int i = (int)(r % ni);
+    const int k = (int)(r / ni);
+    const size_t o = (size_t)j + (size_t)i * g.P + (size_t)k * g.PS;
+    dst[e] = (double)src[o] + (double)src[o + nplane];
+  }
+}
+
 inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
   return dim3((unsigned)((nj + b.x - 1) / b.x), (unsigned)((ni + b.y - 1) / b.y), (unsigned)nmem);
+}
+
+// grid of a point kernel over nj x ni points per level
+inline dim3 pt_grid(const LaunchGeom &L, int nj, int ni, int &tiles_j) {
+  tiles_j = (nj + L.col_x - 1) / L.col_x;
+  const int ti = (ni + L.col_y - 1) / L.col_y;
+  return dim3((unsigned)(tiles_j * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
+              (unsigned)L.nmem);
 }
 
 }  // namespace
@@ -572,7 +705,9 @@ int reduce_blocks(const Geom &g) {
 template <class R>
 void Launch<R>::end_tvirt(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_end_tvirt<R><<<grid2(L.jx - 1, L.iy - 1, b, L.nmem), b, 0, s>>>(d, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+  k_end_tvirt<R><<<grd, b, 0, s>>>(d, advoff, tj);
 }
 
 template <class R>
@@ -586,19 +721,26 @@ void Launch<R>::bdy_ring(const LaunchGeom &L, const Dom<R> *d, int uvoff, int ad
 template <class R>
 void Launch<R>::bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_bdy_relax<R><<<grid2(L.jx - 2, L.iy - 2, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 2, L.iy - 2, tj);
+  k_bdy_relax<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
 }
 
 template <class R>
 void Launch<R>::end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_end_cross<R><<<grid2(L.jx - 1, L.iy - 1, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
+  k_end_ps<R><<<grid2(L.jx - 3, L.iy - 3, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+  k_end_cross<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
 }
 
 template <class R>
 void Launch<R>::end_uvstag(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_end_uvstag<R><<<grid2(L.jx, L.iy, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
+  k_end_uvstag<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
 }
 
 template <class R>
@@ -617,6 +759,18 @@ void Launch<R>::unpack3(const double *src, R *dst, const Geom &g, int nj, int ni
 template <class R>
 void Launch<R>::pack3(const R *src, double *dst, const Geom &g, int nj, int ni, int nk, cudaStream_t s) {
   k_pack3<R><<<152 * 8, 256, 0, s>>>(src, dst, g, nj, ni, nk);
+}
+
+template <class R>
+void Launch<R>::unpack3_df(const double *src, double *dst, const Geom &g, int nj, int ni, int nk,
+                           size_t nplane, cudaStream_t s) {
+  k_unpack3_df<<<152 * 8, 256, 0, s>>>(src, reinterpret_cast<float *>(dst), g, nj, ni, nk, nplane);
+}
+
+template <class R>
+void Launch<R>::pack3_df(const double *src, double *dst, const Geom &g, int nj, int ni, int nk,
+                         size_t nplane, cudaStream_t s) {
+  k_pack3_df<<<152 * 8, 256, 0, s>>>(reinterpret_cast<const float *>(src), dst, g, nj, ni, nk, nplane);
 }
 
 template struct Launch<double>;

@@ -58,6 +58,11 @@ template <class R> struct Launch {
                       cudaStream_t s);
   static void pack3(const R *src, double *dst, const Geom &g, int nj, int ni, int nk,
                     cudaStream_t s);
+  // double-float planes (hi, lo) of nplane elements each
+  static void unpack3_df(const double *src, double *dst, const Geom &g, int nj, int ni, int nk,
+                         size_t nplane, cudaStream_t s);
+  static void pack3_df(const double *src, double *dst, const Geom &g, int nj, int ni, int nk,
+                       size_t nplane, cudaStream_t s);
 };
 
 // Reduction blocks and rows per block the mass budget uses for a geometry.

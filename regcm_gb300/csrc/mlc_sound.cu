@@ -34,34 +34,42 @@ __device__ __forceinline__ double relax_weight(const int32_t *ibnd, const double
 }
 
 template <class R>
-__global__ void k_sound_prep(const Dom<R> *__restrict__ doms, int advoff) {
+__global__ void k_sound_prep(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
+  const Pt q = point_of(tiles_j, 1, 1);
+  if (q.j > g.jx - 1 || q.i > g.iy - 1 || q.k > g.kz) return;
   const int adv = (D.clk->adv_role + advoff) & 1;
   const double *__restrict__ tetav = D.tetav[adv];
   double *__restrict__ tetavf = D.tetavf;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (j > g.jx - 1 || i > g.iy - 1) return;
-  // Main/mod_moloch.F90:564-566
-  double lo = tetav[g.at(j, i, 1)];
-  for (int k = 2; k <= g.kz; ++k) {
-    double hi = tetav[g.at(j, i, k)];
-    tetavf[g.at(j, i, k)] = 0.5 * (lo + hi);
-    // mixed member: theta_v(k-1) - theta_v(k) for the substeps' solves (the
-    // scratch wz[2] is free until the advection of this round)
-    if (sizeof(R) == sizeof(float)) D.wz[2][g.at(j, i, k)] = R(lo - hi);
-    lo = hi;
+  // Main/mod_moloch.F90:564-566, levels 2..kz
+#pragma unroll
+  for (int k = q.k < 2 ? 2 : q.k; k < q.k + kPtLevels && k <= g.kz; ++k) {
+    const size_t o = g.at(q.j, q.i, k), om = o - g.PS;
+    if constexpr (sizeof(R) == sizeof(float)) {
+      // double-float theta_v; also theta_v(k-1) - theta_v(k) for the substeps'
+      // solves (the scratch wz[2] is free until the advection of this round)
+      const DF th(tetav, g.field3()), tf(tetavf, g.PS * (size_t)(g.kz + 1));
+      const F2 lo = th.ld(om), hi = th.ld(o);
+      const F2 sm = df_add(lo, hi);
+      tf.st(o, F2{0.5f * sm.hi, 0.5f * sm.lo});
+      D.wz[2][o] = df_diff(lo, hi);
+    } else {
+      tetavf[o] = 0.5 * (tetav[om] + tetav[o]);
+    }
   }
 }
 
 // Main/mod_moloch.F90:582-618
 template <class R>
-__global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff) {
+__global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
+  const Pt q = point_of(tiles_j, 1, 1);
+  const int j = q.j, i = q.i, kz = g.kz;
+  if (j > g.jx - 1 || i > g.iy - 1 || q.k > kz) return;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const int uv = (D.clk->uv_role + uvoff) & 1;
@@ -70,12 +78,7 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff) {
   R *__restrict__ zdiv2 = D.zdiv2;
   R *__restrict__ s = D.s;
   R *__restrict__ w = D.w;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (j > g.jx - 1 || i > g.iy - 1) return;
-  const int kz = g.kz;
-  const R dts = R(c.dtsound);
-  const R dtrdx = dts * R(c.rdx), dtrdy = dts * R(c.rdx);
+  const R dtrdx = pick<R>(c.dtrdxs, c.dtrdxsf), dtrdy = dtrdx;
   const size_t ij = g.at2(j, i), ijE = g.at2(j + 1, i), ijN = g.at2(j, i + 1);
   const bool interior = (j >= 2 && j <= g.jx - 2 && i >= 2 && i <= g.iy - 2);
   const R rmu0 = sa.rmu[ij], rmu1 = sa.rmu[ijE], rmv0 = sa.rmv[ij], rmv1 = sa.rmv[ijN];
@@ -84,34 +87,36 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff) {
   if (interior) {
     hx0 = sa.hx[ij]; hx1 = sa.hx[ijE]; hy0 = sa.hy[ij]; hy1 = sa.hy[ijN];
   }
-  R um = 0, up = 0, vm = 0, vp = 0;  // level k-1 values
-  for (int k = 1; k <= kz; ++k) {
-    const size_t o = (size_t)(k - 1) * g.PS;
-    const R u0 = u[ij + o], u1 = u[ijE + o], v0 = v[ij + o], v1 = v[ijN + o];
-    R zum, zup;
-    if (c.lrotllr) {
-      zum = dtrdx * u0 * sa.rfmzu[ij + o];
-      zup = dtrdx * u1 * sa.rfmzu[ijE + o];
-    } else {
-      zum = dtrdx * u0 * sa.rfmzu[ij + o] * rmu0;
-      zup = dtrdx * u1 * sa.rfmzu[ijE + o] * rmu1;
-    }
-    const R zvm = dtrdy * v0 * sa.rfmzv[ij + o] * rmv0;
-    const R zvp = dtrdy * v1 * sa.rfmzv[ijN + o] * rmv1;
-    zdiv2[ij + o] = sa.fmz[ij + o] * mfac * ((zup - zum) + (zvp - zvm));
-    if (interior && k >= 2) {
-      const R zuh = (u0 + um) * hx0 + (u1 + up) * hx1;
-      const R zvh = (v0 + vm) * hy0 + (v1 + vp) * hy1;
-      s[ij + o] = -(R(0.25) * (zuh + zvh) * R(sa.gzitak[k - 1]));
-    }
-    if (interior && k == kz) {
-      const R zuh = u0 * hx0 + u1 * hx1;
-      const R zvh = v0 * hy0 + v1 * hy1;
-      const R skp1 = -(R(0.5) * (zuh + zvh));
-      s[ij + (size_t)kz * g.PS] = skp1;
-      w[ij + (size_t)kz * g.PS] = -skp1;
-    }
-    um = u0; up = u1; vm = v0; vp = v1;
+#pragma unroll
+  for (int k = q.k; k < q.k + kPtLevels && k <= kz; ++k) {
+  const size_t o = (size_t)(k - 1) * g.PS;
+  const R u0 = u[ij + o], u1 = u[ijE + o], v0 = v[ij + o], v1 = v[ijN + o];
+  R zum, zup;
+  if (c.lrotllr) {
+    zum = dtrdx * u0 * sa.rfmzu[ij + o];
+    zup = dtrdx * u1 * sa.rfmzu[ijE + o];
+  } else {
+    zum = dtrdx * u0 * sa.rfmzu[ij + o] * rmu0;
+    zup = dtrdx * u1 * sa.rfmzu[ijE + o] * rmu1;
+  }
+  const R zvm = dtrdy * v0 * sa.rfmzv[ij + o] * rmv0;
+  const R zvp = dtrdy * v1 * sa.rfmzv[ijN + o] * rmv1;
+  zdiv2[ij + o] = sa.fmz[ij + o] * mfac * ((zup - zum) + (zvp - zvm));
+  if (!interior) continue;
+  if (k >= 2) {
+    const size_t om = o - g.PS;  // level k-1
+    const R um = u[ij + om], up = u[ijE + om], vm = v[ij + om], vp = v[ijN + om];
+    const R zuh = (u0 + um) * hx0 + (u1 + up) * hx1;
+    const R zvh = (v0 + vm) * hy0 + (v1 + vp) * hy1;
+    s[ij + o] = -(R(0.25) * (zuh + zvh) * sa.gzitak_r[k - 1]);
+  }
+  if (k == kz) {
+    const R zuh = u0 * hx0 + u1 * hx1;
+    const R zvh = v0 * hy0 + v1 * hy1;
+    const R skp1 = -(R(0.5) * (zuh + zvh));
+    s[ij + (size_t)kz * g.PS] = skp1;
+    w[ij + (size_t)kz * g.PS] = -skp1;
+  }
   }
 }
 
@@ -152,6 +157,7 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
 
   // filtered divergence plus the vertical part (:531-543, :627-630)
   double sk = (double)s[ij];  // s(1) = 0 in the interior
+  #pragma unroll 4
   for (int k = 1; k <= kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     double z = (double)zraw[o];
@@ -173,6 +179,7 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
   double pai_k = (double)pai[ij + (size_t)(kz - 1) * PS];
   double tet_k = tetav[ij + (size_t)(kz - 1) * PS];
   double fmz_k = sa.fmz_d[ij + (size_t)(kz - 1) * PS];
+  #pragma unroll 4
   for (int k = kz; k >= 2; --k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     const double pai_m = (double)pai[o - PS];
@@ -198,6 +205,7 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
   // back substitution k = 2..kz (:660-664)
   double wprev = (double)w[ij];  // w(1) = 0
   COL(wp, 1) = wprev;
+  #pragma unroll 4
   for (int k = 2; k <= kz; ++k) {
     wprev = COL(wp, k) + COL(wk, k) * wprev;
     COL(wp, k) = wprev;
@@ -205,6 +213,7 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
   }
   COL(wp, kz + 1) = (double)w[ij + (size_t)kz * PS];
   // Exner function (:668-671)
+  #pragma unroll 4
   for (int k = 1; k <= kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     const double pk = pai[o];
@@ -213,6 +222,7 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
   }
   if (last) {
     // complete s (:728-734)
+    #pragma unroll 4
     for (int k = 2; k <= kz; ++k) {
       const size_t o = ij + (size_t)(k - 1) * PS;
       s[o] = (R)((COL(wp, k) + (double)s[o]) * sa.fmzf_d[o]);
@@ -223,13 +233,13 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
 #undef COL
 }
 
-// The solve of a mixed member (same equations as k_sound_solve).  FP64 is
-// kept where rounding is amplified: theta_v at half levels, the hydrostatic
-// balance -cp*theta_v*fmzf*dtrdz*(pai(k-1) - pai(k)) - g*dts of the w
-// equation (two terms of ~g*dts whose difference drives w), and the Exner
-// update, formed as pai - pai*increment.  The divergence filter, the
-// elimination coefficients, the recurrence and the back substitution are
-// O(1)-conditioned and run in FP32.
+// The solve of a mixed member (same equations as k_sound_solve), in FP32
+// only.  Where rounding is amplified the values are double-floats: theta_v at
+// half levels, the hydrostatic balance -cp*theta_v*fmzf*dtrdz*(pai(k-1) -
+// pai(k)) - g*dts of the w equation (two terms of ~g*dts whose difference
+// drives w), and the Exner update pai - pai*increment.  The divergence
+// filter, the elimination coefficients, the recurrence and the back
+// substitution are O(1)-conditioned and run in plain FP32.
 template <class R>
 __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
   const Dom<R> &D = doms[blockIdx.z];
@@ -241,8 +251,6 @@ __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff,
   const R *__restrict__ zraw = D.zdiv2;
   R *__restrict__ s = D.s;
   R *__restrict__ w = D.w;
-  double *__restrict__ pai = D.pai[adv];
-  double *__restrict__ tetavf = D.tetavf;
   extern __shared__ float msm[];
   const int nth = blockDim.x * blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
@@ -254,54 +262,58 @@ __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff,
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (j > g.jx - 2 || i > g.iy - 2) return;
-  const double dts_d = c.dtsound;
-  const double dtrdz_d = dts_d * c.rdzita;
-  const float dtrdz = float(dtrdz_d);
+  const size_t PS = g.PS, F1 = PS * (size_t)(kz + 1);
+  const DF pai(D.pai[adv], g.field3()), tvf_a(D.tetavf, F1), cfz(sa.cfz, F1);
+  const float dtrdz = c.dtsoundf * c.rdzitaf;
   const float rdrcv = float(kRdrcv);
-  const double gdts = kGrav * dts_d;
+  const float rdt = rdrcv * dtrdz;
+  const F2 ngdts{-c.gdts_hi, -c.gdts_lo};
   const size_t ij = g.at2(j, i);
-  const size_t PS = g.PS;
   const size_t P = (size_t)g.P;
   const int32_t ib = sa.ibnd_cr[ij];
+  const int nsp = c.nspgx;
 
   float sk = float(s[ij]);
+  #pragma unroll 4
   for (int k = 1; k <= kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     float z = float(zraw[o]);
     if (c.divfilter) {
       const float lap = (float(zraw[o - 1]) + float(zraw[o + 1]) + float(zraw[o - P]) +
                          float(zraw[o + P]) - 4.f * z);
-      z = z + float(sa.xknu[k - 1]) * lap;
+      z = z + sa.xknu_r[k - 1] * lap;
     }
     const float skp1 = float(s[o + PS]);
-    const float bw = ib > 0 ? float(1.0 - sa.hefc[(size_t)(ib - 1) + (size_t)(k - 1) * c.nspgx]) : 1.f;
+    const float bw = ib > 0 ? 1.f - sa.hefc_r[(size_t)(ib - 1) + (size_t)(k - 1) * nsp] : 1.f;
     z = z + bw * dtrdz * float(sa.fmz[o]) * (sk - skp1);
     COL(zf, k) = z;
     sk = skp1;
   }
 
-  // zrd = cp*tvf*fmzf*dtrdz = tvf*cfz (FP64); zcs2*zrom1w = rdrcv*dtrdz*zrd
-  const float rdt = rdrcv * dtrdz;
+  // zrd = cp*tvf*fmzf*dtrdz = tvf*cfz; zcs2*zrom1w = rdrcv*dtrdz*zrd
   const float *__restrict__ dtet = D.wz[2];  // theta_v(k-1) - theta_v(k), sound_prep
   float wnext = float(w[ij + (size_t)kz * PS]);
   float wkp1 = 0.f;
-  double pai_k = pai[ij + (size_t)(kz - 1) * PS];
-  float pk_f = float(pai_k);
+  F2 pai_k = pai.ld(ij + (size_t)(kz - 1) * PS);
+  float pk_f = df_f(pai_k);
   float fmz_k = float(sa.fmz[ij + (size_t)(kz - 1) * PS]);
+  #pragma unroll 4
   for (int k = kz; k >= 2; --k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
-    const double pai_m = pai[o - PS];
+    const F2 pai_m = pai.ld(o - PS);
     const float fmz_m = float(sa.fmz[o - PS]);
     const float wold = float(w[o]);
     const float corr = wold * float(sa.fmzf[o]) * dtrdz * dtet[o];
-    const double tvf = tetavf[o] - (double)corr;
-    tetavf[o] = tvf;
-    const double zrd = tvf * sa.cfz[o];
-    float zwexpl = wold + float(fma(-zrd, pai_m - pai_k, -gdts));
-    const float zr = float(zrd);
-    const float pm_f = float(pai_m);
+    const F2 tvf = df_add_f(tvf_a.ld(o), -corr);
+    tvf_a.st(o, tvf);
+    const F2 zrd = df_mul(tvf, cfz.ld(o));
+    const F2 dp = two_sum(pai_m.hi - pai_k.hi, pai_m.lo - pai_k.lo);  // hi difference exact
+    const F2 bal = df_add(ngdts, df_mul(F2{-zrd.hi, -zrd.lo}, dp));
+    float zwexpl = wold + df_f(bal);
+    const float zr = df_f(zrd);
+    const float pm_f = df_f(pai_m);
     zwexpl = zwexpl + rdrcv * zr * (pm_f * COL(zf, k - 1) - pk_f * COL(zf, k));
-    const float ff = float(sa.ffilt[k - 1]);
+    const float ff = sa.ffilt_r[k - 1];
     const float zu = rdt * fmz_m * zr * pm_f + ff;
     const float zd = rdt * fmz_k * zr * pk_f + ff;
     const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
@@ -313,19 +325,23 @@ __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff,
   }
   float wprev = float(w[ij]);
   COL(wp, 1) = wprev;
+  #pragma unroll 4
   for (int k = 2; k <= kz; ++k) {
     wprev = COL(wp, k) + COL(wk, k) * wprev;
     COL(wp, k) = wprev;
     w[ij + (size_t)(k - 1) * PS] = (R)wprev;
   }
   COL(wp, kz + 1) = float(w[ij + (size_t)kz * PS]);
+  #pragma unroll 4
   for (int k = 1; k <= kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
-    const double pk = pai[o];
+    const F2 pk = pai.ld(o);
     const float inc = rdrcv * (COL(zf, k) + (dtrdz * float(sa.fmz[o]) * (COL(wp, k) - COL(wp, k + 1))));
-    pai[o] = fma(-pk, (double)inc, pk);
+    const F2 d = df_mul_f(pk, inc);
+    pai.st(o, df_add(pk, F2{-d.hi, -d.lo}));
   }
   if (last) {
+    #pragma unroll 4
     for (int k = 2; k <= kz; ++k) {
       const size_t o = ij + (size_t)(k - 1) * PS;
       s[o] = (R)((COL(wp, k) + float(s[o])) * float(sa.fmzf[o]));
@@ -338,7 +354,8 @@ __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff,
 
 // Main/mod_moloch.F90:677-721 with divergence_damping :738-765 folded in
 template <class R>
-__global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+__global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int advoff,
+                                 int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
@@ -353,12 +370,35 @@ __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int
   const R *__restrict__ zraw = D.zdiv2;
   const double *__restrict__ pai = D.pai[adv];
   const double *__restrict__ tetav = D.tetav[adv];
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (j > g.jx || i > g.iy) return;
-  const R dts = R(c.dtsound);
-  const R dtrdx = dts * R(c.rdx), dtrdy = dts * R(c.rdx);
-  const R dxrdt = R(c.dx) / dts;
+  const Pt q = point_of(tiles_j, 1, 1);
+  const int j = q.j, i = q.i;
+  if (j > g.jx || i > g.iy || q.k > g.kz) return;
+  constexpr bool mixed = sizeof(R) == sizeof(float);
+  const R dts = pick<R>(c.dtsound, c.dtsoundf);
+  const R dtrdx = pick<R>(c.dtrdxs, c.dtrdxsf), dtrdy = dtrdx;
+  const R dxrdt = pick<R>(c.dxrdt, c.dxrdtf);
+  const size_t F = g.field3();
+  // mixed member: theta_v and Exner are double-floats (hi, lo planes)
+  const float *__restrict__ th_f = reinterpret_cast<const float *>(tetav);
+  const float *__restrict__ pa_f = reinterpret_cast<const float *>(pai);
+  // relaxation weight 1 - hefc(ib, k) (Main/mod_bdycod.F90:4033-4047)
+  auto bweight = [&](const int32_t *ibnd, size_t ij0, int k) -> R {
+    if constexpr (mixed) {
+      const int ib = ibnd[ij0];
+      return ib > 0 ? 1.f - sa.hefc_r[(size_t)(ib - 1) + (size_t)(k - 1) * c.nspgx] : 1.f;
+    } else {
+      return R(relax_weight(ibnd, sa.hefc, c.nspgx, ij0, k));
+    }
+  };
+  // theta_v(a) + theta_v(b) and pai(a) - pai(b) in the field type
+  auto tsum = [&](size_t a, size_t b) -> R {
+    if constexpr (mixed) return (th_f[a] + th_f[b]) + (th_f[a + F] + th_f[b + F]);
+    else return R(tetav[a] + tetav[b]);
+  };
+  auto pdif = [&](size_t a, size_t b) -> R {
+    if constexpr (mixed) return (pa_f[a] - pa_f[b]) + (pa_f[a + F] - pa_f[b + F]);
+    else return R(pai[a] - pai[b]);
+  };
   const R zfz = R(kGrav) * dts;
   const R halfcp = R(0.5) * R(kCpd);
   const size_t ij = g.at2(j, i);
@@ -381,20 +421,21 @@ __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int
     cor_v = sa.corv[ij];
   }
   const size_t W = 1, S = (size_t)g.P;
-  for (int k = 1; k <= g.kz; ++k) {
+#pragma unroll
+  for (int k = q.k; k < q.k + kPtLevels && k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
-    const R gk = R(sa.gzitakh[k - 1]);
+    const R gk = sa.gzitakh_r[k - 1];
     if (has_u) {
       R un = u_in[o];
       if (upd_u) {
         if (c.divdamp) {
-          const R xdam = dxrdt * R(sa.xkdamp[k - 1]) * mu;
+          const R xdam = dxrdt * sa.xkdamp_r[k - 1] * mu;
           un = un + xdam * (zraw[o] - zraw[o - W]);
         }
-        const R zrom1u = halfcp * R(tetav[o - W] + tetav[o]);
+        const R zrom1u = halfcp * tsum(o - W, o);
         const R zcor1u = cor_u * dts * v_in[o];
-        const R bw = R(relax_weight(sa.ibnd_ud, sa.hefc, c.nspgx, ij, k));
-        un = un + bw * (zcor1u - zfz * hxk * gk - zcx * zrom1u * R(pai[o] - pai[o - W]));
+        const R bw = bweight(sa.ibnd_ud, ij, k);
+        un = un + bw * (zcor1u - zfz * hxk * gk - zcx * zrom1u * pdif(o, o - W));
       }
       u_out[o] = un;
     }
@@ -402,13 +443,13 @@ __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int
       R vn = v_in[o];
       if (upd_v) {
         if (c.divdamp) {
-          const R xdam = c.lrotllr ? dxrdt * R(sa.xkdamp[k - 1]) : dxrdt * R(sa.xkdamp[k - 1]) * mv;
+          const R xdam = c.lrotllr ? dxrdt * sa.xkdamp_r[k - 1] : dxrdt * sa.xkdamp_r[k - 1] * mv;
           vn = vn + xdam * (zraw[o] - zraw[o - S]);
         }
-        const R zrom1v = halfcp * R(tetav[o - S] + tetav[o]);
+        const R zrom1v = halfcp * tsum(o - S, o);
         const R zcor1v = cor_v * dts * u_in[o];
-        const R bw = R(relax_weight(sa.ibnd_vd, sa.hefc, c.nspgx, ij, k));
-        vn = vn + bw * (-zcor1v - zfz * hyk * gk - zcy * zrom1v * R(pai[o] - pai[o - S]));
+        const R bw = bweight(sa.ibnd_vd, ij, k);
+        vn = vn + bw * (-zcor1v - zfz * hyk * gk - zcy * zrom1v * pdif(o, o - S));
       }
       v_out[o] = vn;
     }
@@ -416,21 +457,27 @@ __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int
 }
 
 inline dim3 col_block(const LaunchGeom &L) { return dim3((unsigned)L.col_x, (unsigned)L.col_y); }
-inline dim3 col_grid(const LaunchGeom &L, int nj, int ni) {
-  return dim3((unsigned)((nj + L.col_x - 1) / L.col_x), (unsigned)((ni + L.col_y - 1) / L.col_y),
+// grid of a point kernel over nj x ni points per level
+inline dim3 pt_grid(const LaunchGeom &L, int nj, int ni, int &tiles_j) {
+  tiles_j = (nj + L.col_x - 1) / L.col_x;
+  const int ti = (ni + L.col_y - 1) / L.col_y;
+  return dim3((unsigned)(tiles_j * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
               (unsigned)L.nmem);
 }
-
 }  // namespace
 
 template <class R>
 void Launch<R>::sound_prep(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
-  k_sound_prep<R><<<col_grid(L, L.jx - 1, L.iy - 1), col_block(L), 0, s>>>(d, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+  k_sound_prep<R><<<grd, col_block(L), 0, s>>>(d, advoff, tj);
 }
 
 template <class R>
 void Launch<R>::sound_div(const LaunchGeom &L, const Dom<R> *d, int uvoff, cudaStream_t s) {
-  k_sound_div<R><<<col_grid(L, L.jx - 1, L.iy - 1), col_block(L), 0, s>>>(d, uvoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+  k_sound_div<R><<<grd, col_block(L), 0, s>>>(d, uvoff, tj);
 }
 
 template <class R>
@@ -450,7 +497,9 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
 template <class R>
 void Launch<R>::sound_momentum(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                                cudaStream_t s) {
-  k_sound_momentum<R><<<col_grid(L, L.jx, L.iy), col_block(L), 0, s>>>(d, uvoff, advoff);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
+  k_sound_momentum<R><<<grd, col_block(L), 0, s>>>(d, uvoff, advoff, tj);
 }
 
 template <class R>
