@@ -254,155 +254,211 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
 #undef A
 }
 
-// Meridional then zonal WAF for one tile (:984-1038; ROTLLR :926-983).
-template <class R, class T, int kTJ, int kTI>
+// Meridional then zonal WAF for one tile at one level, every field of the R
+// table (:984-1038; ROTLLR :926-983).  The winds, Courant numbers and metric
+// coefficients of the tile are formed once, in shared memory, and then each
+// field in turn is staged with a 2-point halo, its meridional fluxes and the
+// intermediate p0 are built on a 2-column halo, then its zonal fluxes and
+// the result, so each field is read and written once.  The result goes to
+// the field's other buffer because the halo columns of a tile still need its
+// old values.  Per field the expressions are the reference's, operand for
+// operand; only the field-independent factors are computed once.
+template <class R, int kTJ, int kTI>
 __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__restrict__ doms,
-                                                            int nf, int tiles_j, int set,
-                                                            int uvoff, int advoff) {
-  constexpr int WJ = kTJ + 4;  // columns J0-2 .. J0+TJ+1
-  __shared__ T wz_s[kTI + 4][WJ];      // rows I0-2 .. I0+TI+1
-  __shared__ T zpby_s[kTI + 1][WJ];    // rows I0 .. I0+TI
-  __shared__ T p0_s[kTI][WJ];          // rows I0 .. I0+TI-1
-  __shared__ T zpbw_s[kTI][kTJ + 1];   // columns J0 .. J0+TJ
-  // grid: x = tiles along j and i, y = field x level, z = member
+                                                            int tiles_j, int uvoff, int advoff) {
+  using T = R;
+  constexpr int WJ = kTJ + 4;            // columns J0-2 .. J0+TJ+1
+  __shared__ T wz_s[kTI + 4][WJ];        // rows I0-2 .. I0+TI+1
+  __shared__ T zpby_s[kTI + 1][WJ];      // rows I0 .. I0+TI
+  __shared__ T p0_s[kTI][WJ];            // rows I0 .. I0+TI-1
+  __shared__ T zpbw_s[kTI][kTJ + 1];     // columns J0 .. J0+TJ
+  // field-independent factors of the tile
+  __shared__ T vy_s[kTI + 1][WJ], zmy_s[kTI + 1][WJ];   // v, Courant number at rows I0..I0+TI
+  __shared__ T zs_s[kTI][WJ], zn_s[kTI][WJ], dvy_s[kTI][WJ], m2_s[kTI][WJ];
+  __shared__ T ux_s[kTI][kTJ + 1], zmx_s[kTI][kTJ + 1];  // u, Courant number at columns J0..J0+TJ
+  __shared__ T zw_s[kTI][kTJ], ze_s[kTI][kTJ], dvx_s[kTI][kTJ];
+  // grid: x = tiles along j and i, y = level, z = member
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
-  const int f = blockIdx.y % nf;
-  if (set == 0 && f >= n_table_r(D)) return;
-  const int k = blockIdx.y / nf + 1;
+  const int k = blockIdx.y + 1;
   const int bj = blockIdx.x % tiles_j, bi = blockIdx.x / tiles_j;
   const Geom g = D.g;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   if (k > kz) return;
-  const int J0c = bj * kTJ + 1, I0c = bi * kTI + 1;
-  if (J0c > jx - 1 || I0c > iy - 1) return;
+  const int J0 = bj * kTJ + 1, I0 = bi * kTI + 1;
+  if (J0 > jx - 1 || I0 > iy - 1) return;
   const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
-  const R *__restrict__ u = D.u[uv];
-  const R *__restrict__ v = D.v[uv];
-  const T *cur0;
-  T *out0, *wz0;
-  field_t<R, T>(D, set, f, adv, cur0, out0, wz0);
-  const int J0 = J0c, I0 = I0c;
   const int tid = threadIdx.y * kTJ + threadIdx.x;
   const int nth = kTJ * kTI;
   const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
-  const T *pp = cur0 + ko;
-  const T *wz = wz0 + ko;
-  T *out = out0 + ko;
-  const R *uk = u + ko;
-  const R *vk = v + ko;
+  const R *__restrict__ uk = D.u[uv] + ko;
+  const R *__restrict__ vk = D.v[uv] + ko;
   const T dta = pick<T>(c.dtstepa, c.dtstepaf);
   const T dtrdx = dta * pick<T>(c.rdx, c.rdxf), dtrdy = dta * pick<T>(c.rdx, c.rdxf);
   const bool rot = c.lrotllr != 0;
   const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
+  const int nf = n_table_r(D);
 
-  // stage wz (cross points only; others are never read for valid outputs)
-  for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
-    const int rr = e / WJ, cc = e % WJ;
-    const int i = I0 - 2 + rr, j = J0 - 2 + cc;
-    T x = T(0);
-    if (i >= 1 && i <= iy - 1 && j >= 1 && j <= jx - 1) x = wz[g.at2(j, i)];
-    wz_s[rr][cc] = x;
-  }
-  __syncthreads();
-  // meridional fluxes zpby(j,i): j in jce, i in ici1..ice2
+  // ---- field-independent factors ----
   for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
     const int rr = e / WJ, cc = e % WJ;
     const int i = I0 + rr, j = J0 - 2 + cc;
-    T x = T(0);
+    T vv = T(0), zamu = T(0);
     if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 1) {
       const size_t ij = g.at2(j, i);
-      const T vv = T(vk[ij]);
-      const T zamu = rot ? vv * dtrdy : vv * T(sa.msfv[ij]) * dtrdy;
-      T is;
-      int ih;
-      if (zamu > T(0)) { is = T(1); ih = i - 1; }
-      else { is = T(-1); ih = min(i + 1, imax); }
-      const int ihm1 = max(ih - 1, imin);
-      // shared-memory row of global row i is i - (I0 - 2)
-      const int b = 2 - I0;
-      x = waf_flux<T>(T(0.5) * vv, is, zamu, wz_s[i - 1 + b][cc], wz_s[i + b][cc],
-                      wz_s[ih + b][cc] - wz_s[ihm1 + b][cc]);
+      vv = T(vk[ij]);
+      zamu = rot ? vv * dtrdy : vv * T(sa.msfv[ij]) * dtrdy;
     }
-    zpby_s[rr][cc] = x;
+    vy_s[rr][cc] = vv;
+    zmy_s[rr][cc] = zamu;
   }
-  __syncthreads();
-  // p0(j,i): j in jce, i in ici
   for (int e = tid; e < kTI * WJ; e += nth) {
     const int rr = e / WJ, cc = e % WJ;
     const int i = I0 + rr, j = J0 - 2 + cc;
-    T x = T(0);
+    T zs = T(0), zn = T(0), dv = T(0), m2 = T(1);
     if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
       const size_t ij = g.at2(j, i), ijN = ij + (size_t)g.P;
       const T fz = T(sa.fmz[ko + ij]);
-      const T ppk = pp[ij];
-      const T wzk = wz_s[rr + 2][cc];
       if (rot) {
         const T zhxvtn = dtrdy * T(sa.rmv[ijN]) * T(sa.msfx[ij]);
         const T zhxvts = dtrdy * T(sa.rmv[ij]) * T(sa.msfx[ij]);
-        const T zrfmn = zhxvtn * fz * T(sa.rfmzv[ko + ijN]);
-        const T zrfms = zhxvts * fz * T(sa.rfmzv[ko + ij]);
-        const T zdv = (T(vk[ijN]) * zrfmn - T(vk[ij]) * zrfms) * ppk;
-        x = wzk + (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
+        zn = zhxvtn * fz * T(sa.rfmzv[ko + ijN]);
+        zs = zhxvts * fz * T(sa.rfmzv[ko + ij]);
+        dv = T(vk[ijN]) * zn - T(vk[ij]) * zs;
       } else {
         // rfmzu as in the reference (Main/mod_moloch.F90:1000-1001)
-        const T zrfmn = dtrdy * fz * T(sa.rfmzu[ko + ijN]);
-        const T zrfms = dtrdy * fz * T(sa.rfmzu[ko + ij]);
-        const T zdv = (T(vk[ijN]) * T(sa.rmv[ijN]) * zrfmn - T(vk[ij]) * T(sa.rmv[ij]) * zrfms) * ppk;
-        x = wzk + T(sa.mx2[ij]) * (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
+        zn = dtrdy * fz * T(sa.rfmzu[ko + ijN]);
+        zs = dtrdy * fz * T(sa.rfmzu[ko + ij]);
+        dv = T(vk[ijN]) * T(sa.rmv[ijN]) * zn - T(vk[ij]) * T(sa.rmv[ij]) * zs;
+        m2 = T(sa.mx2[ij]);
       }
     }
-    p0_s[rr][cc] = x;
+    zs_s[rr][cc] = zs; zn_s[rr][cc] = zn; dvy_s[rr][cc] = dv; m2_s[rr][cc] = m2;
   }
-  __syncthreads();
-  // zonal fluxes zpbw(j,i): j in jci1..jce2, i in ici
   for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
     const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
     const int i = I0 + rr, j = J0 + cc;
-    T x = T(0);
+    T uu = T(0), zamu = T(0);
     if (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
       const size_t ij = g.at2(j, i);
-      const T uu = T(uk[ij]);
-      const T zamu = uu * T(sa.msfu[ij]) * dtrdx;
-      T is;
-      int jh;
-      if (zamu > T(0)) { is = T(1); jh = j - 1; }
-      else { is = T(-1); jh = min(j + 1, jmax); }
-      const int jhm1 = max(jh - 1, jmin);
-      const int b = 2 - J0;  // p0_s column of global column j is j - (J0 - 2)
-      x = waf_flux<T>(T(0.5) * uu, is, zamu, p0_s[rr][j - 1 + b], p0_s[rr][j + b],
-                      p0_s[rr][jh + b] - p0_s[rr][jhm1 + b]);
+      uu = T(uk[ij]);
+      zamu = uu * T(sa.msfu[ij]) * dtrdx;
     }
-    zpbw_s[rr][cc] = x;
+    ux_s[rr][cc] = uu;
+    zmx_s[rr][cc] = zamu;
   }
-  __syncthreads();
-  // result on the tile: interior update, ring copied
   {
     const int rr = threadIdx.y, cc = threadIdx.x;
     const int i = I0 + rr, j = J0 + cc;
-    if (i <= iy - 1 && j <= jx - 1) {
+    T zw = T(0), ze = T(0), dv = T(0);
+    if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
       const size_t ij = g.at2(j, i);
-      const T ppk = pp[ij];
-      T x = ppk;
-      if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
-        const T fz = T(sa.fmz[ko + ij]);
-        const T p0k = p0_s[rr][cc + 2];
-        if (rot) {
-          const T zcostx = dtrdx * T(sa.msfx[ij]);
-          const T zrfmw = zcostx * fz * T(sa.rfmzu[ko + ij]);
-          const T zrfme = zcostx * fz * T(sa.rfmzu[ko + ij + 1]);
-          const T zdv = (T(uk[ij + 1]) * zrfme - T(uk[ij]) * zrfmw) * ppk;
-          x = p0k + zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv;
-        } else {
-          const T zrfmw = dtrdx * fz * T(sa.rfmzu[ko + ij]);
-          const T zrfme = dtrdx * fz * T(sa.rfmzu[ko + ij + 1]);
-          const T zdv = (T(uk[ij + 1]) * T(sa.rmu[ij + 1]) * zrfme - T(uk[ij]) * T(sa.rmu[ij]) * zrfmw) * ppk;
-          x = p0k + T(sa.mx2[ij]) * (zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv);
-        }
+      const T fz = T(sa.fmz[ko + ij]);
+      if (rot) {
+        const T zcostx = dtrdx * T(sa.msfx[ij]);
+        zw = zcostx * fz * T(sa.rfmzu[ko + ij]);
+        ze = zcostx * fz * T(sa.rfmzu[ko + ij + 1]);
+        dv = T(uk[ij + 1]) * ze - T(uk[ij]) * zw;
+      } else {
+        zw = dtrdx * fz * T(sa.rfmzu[ko + ij]);
+        ze = dtrdx * fz * T(sa.rfmzu[ko + ij + 1]);
+        dv = T(uk[ij + 1]) * T(sa.rmu[ij + 1]) * ze - T(uk[ij]) * T(sa.rmu[ij]) * zw;
       }
-      out[ij] = x;
+    }
+    zw_s[rr][cc] = zw; ze_s[rr][cc] = ze; dvx_s[rr][cc] = dv;
+  }
+
+  for (int f = 0; f < nf; ++f) {
+    const T *cur0;
+    T *out0, *wz0;
+    field_t<R, T>(D, 0, f, adv, cur0, out0, wz0);
+    const T *pp = cur0 + ko;
+    const T *wz = wz0 + ko;
+    T *out = out0 + ko;
+    // stage wz (cross points only; others are never read for valid outputs)
+    for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
+      const int rr = e / WJ, cc = e % WJ;
+      const int i = I0 - 2 + rr, j = J0 - 2 + cc;
+      T x = T(0);
+      if (i >= 1 && i <= iy - 1 && j >= 1 && j <= jx - 1) x = wz[g.at2(j, i)];
+      wz_s[rr][cc] = x;
+    }
+    __syncthreads();  // also orders the factors above before their first use
+    // meridional fluxes zpby(j,i): j in jce, i in ici1..ice2
+    for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
+      const int rr = e / WJ, cc = e % WJ;
+      const int i = I0 + rr, j = J0 - 2 + cc;
+      T x = T(0);
+      if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 1) {
+        const T vv = vy_s[rr][cc];
+        const T zamu = zmy_s[rr][cc];
+        T is;
+        int ih;
+        if (zamu > T(0)) { is = T(1); ih = i - 1; }
+        else { is = T(-1); ih = min(i + 1, imax); }
+        const int ihm1 = max(ih - 1, imin);
+        const int b = 2 - I0;  // shared-memory row of global row i is i + b
+        x = waf_flux<T>(T(0.5) * vv, is, zamu, wz_s[i - 1 + b][cc], wz_s[i + b][cc],
+                        wz_s[ih + b][cc] - wz_s[ihm1 + b][cc]);
+      }
+      zpby_s[rr][cc] = x;
+    }
+    __syncthreads();
+    // p0(j,i): j in jce, i in ici
+    for (int e = tid; e < kTI * WJ; e += nth) {
+      const int rr = e / WJ, cc = e % WJ;
+      const int i = I0 + rr, j = J0 - 2 + cc;
+      T x = T(0);
+      if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
+        const T ppk = pp[g.at2(j, i)];
+        const T wzk = wz_s[rr + 2][cc];
+        const T zdv = dvy_s[rr][cc] * ppk;
+        const T zrfms = zs_s[rr][cc], zrfmn = zn_s[rr][cc];
+        if (rot) x = wzk + (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
+        else x = wzk + m2_s[rr][cc] * (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
+      }
+      p0_s[rr][cc] = x;
+    }
+    __syncthreads();
+    // zonal fluxes zpbw(j,i): j in jci1..jce2, i in ici
+    for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
+      const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
+      const int i = I0 + rr, j = J0 + cc;
+      T x = T(0);
+      if (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
+        const T uu = ux_s[rr][cc];
+        const T zamu = zmx_s[rr][cc];
+        T is;
+        int jh;
+        if (zamu > T(0)) { is = T(1); jh = j - 1; }
+        else { is = T(-1); jh = min(j + 1, jmax); }
+        const int jhm1 = max(jh - 1, jmin);
+        const int b = 2 - J0;  // p0_s column of global column j is j + b
+        x = waf_flux<T>(T(0.5) * uu, is, zamu, p0_s[rr][j - 1 + b], p0_s[rr][j + b],
+                        p0_s[rr][jh + b] - p0_s[rr][jhm1 + b]);
+      }
+      zpbw_s[rr][cc] = x;
+    }
+    __syncthreads();
+    // result on the tile: interior update, ring copied
+    {
+      const int rr = threadIdx.y, cc = threadIdx.x;
+      const int i = I0 + rr, j = J0 + cc;
+      if (i <= iy - 1 && j <= jx - 1) {
+        const size_t ij = g.at2(j, i);
+        const T ppk = pp[ij];
+        T x = ppk;
+        if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
+          const T p0k = p0_s[rr][cc + 2];
+          const T zrfmw = zw_s[rr][cc], zrfme = ze_s[rr][cc];
+          const T zdv = dvx_s[rr][cc] * ppk;
+          if (rot) x = p0k + zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv;
+          else x = p0k + m2_s[rr][cc + 2] * (zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv);
+        }
+        out[ij] = x;
+      }
     }
   }
 }
@@ -844,22 +900,20 @@ void launch_vertical(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int 
   k_adv_vertical<R, T><<<grd, b, smem, s>>>(d, nf, set, advoff);
 }
 
-template <class R, class T, int TJ, int TI>
-void launch_tile(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int uvoff, int advoff,
-                 cudaStream_t s) {
+template <class R, int TJ, int TI>
+void launch_tile(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const int tj = (L.jx - 1 + TJ - 1) / TJ, ti = (L.iy - 1 + TI - 1) / TI;
-  const dim3 grd((unsigned)(tj * ti), (unsigned)(nf * L.kz), (unsigned)L.nmem);
-  k_adv_horizontal<R, T, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(d, nf, tj, set, uvoff, advoff);
+  const dim3 grd((unsigned)(tj * ti), (unsigned)L.kz, (unsigned)L.nmem);
+  k_adv_horizontal<R, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(d, tj, uvoff, advoff);
 }
 
-template <class R, class T>
-void launch_horizontal(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int uvoff,
-                       int advoff, cudaStream_t s) {
+template <class R>
+void launch_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   switch (L.htile) {
-    case 1: launch_tile<R, T, 32, 4>(L, d, nf, set, uvoff, advoff, s); break;
-    case 2: launch_tile<R, T, 64, 4>(L, d, nf, set, uvoff, advoff, s); break;
-    case 3: launch_tile<R, T, 16, 8>(L, d, nf, set, uvoff, advoff, s); break;
-    default: launch_tile<R, T, 32, 8>(L, d, nf, set, uvoff, advoff, s); break;
+    case 1: launch_tile<R, 32, 4>(L, d, uvoff, advoff, s); break;
+    case 2: launch_tile<R, 64, 4>(L, d, uvoff, advoff, s); break;
+    case 3: launch_tile<R, 16, 8>(L, d, uvoff, advoff, s); break;
+    default: launch_tile<R, 32, 8>(L, d, uvoff, advoff, s); break;
   }
 }
 
@@ -901,7 +955,7 @@ void Launch<R>::adv_vertical(const LaunchGeom &L, const Dom<R> *d, int advoff, c
 template <class R>
 void Launch<R>::adv_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                                cudaStream_t s) {
-  launch_horizontal<R, R>(L, d, L.nadv_r, 0, uvoff, advoff, s);
+  launch_horizontal<R>(L, d, uvoff, advoff, s);
   if constexpr (sizeof(R) == sizeof(float))
     if (L.nadv_d) launch_horizontal_inc<R>(L, d, uvoff, advoff, s);
 }
