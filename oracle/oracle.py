@@ -67,6 +67,10 @@ class Oracle:
             assert self.lib.orc_set_boundary(self.h, C.byref(self._bp), case.xbctime,
                                              case.params.dtbdys) == 0
 
+    def set_boundary(self, bdy_ptrs, xbctime: float, dtbdys: float):
+        self._bp = bdy_ptrs
+        assert self.lib.orc_set_boundary(self.h, C.byref(bdy_ptrs), xbctime, dtbdys) == 0
+
     def step(self, n=1):
         d = abi.mlc_diag()
         st = self.lib.orc_step(self.h, n, C.byref(d))
