@@ -42,24 +42,32 @@ template <> struct FlowEps<float> {
 // (local_flow_param, Main/mod_moloch.F90:1571-1590; the flux lines
 // :877-883, :986-993, :1017-1024).  In every use den = c - a, so
 //   (1+phi)*a + (1-phi)*c = (a + c) - phi*den,
-//   phi*den = is*den + (zamu - is)*B,   B = b*den,
-// and B is 0, 2*num, den, num or 2*den as r falls in (-inf,0], (0,1/2),
-// [1/2,1], (1,2) or [2,inf): the division num/den is never formed.  The
-// result equals the reference's to rounding (b is continuous in r, so the
-// region tests need no exact ties), at a third of the FP64 instructions.
+//   phi*den = is*den + (zamu - is)*B,   B = b*den.
+// With d = |den| > 0 and q = num*sign(den) (so r = q/d), multiplying the
+// limiter by d > 0 gives
+//   B = sign(den) * max(0, min(2d, max(q, min(2q, d)))),
+// whose candidates 0, q, 2q, d, 2d are exact: B is one of 0, 2*num, den, num,
+// 2*den exactly, the value of b*den in each region of r, ties included.  No
+// division.  FP32 takes the branch-free clamp; FP64 tests the regions of r in
+// turn (0, 1/2, 1, 2), which usually stops early - on GB300 each FP64 min, max
+// or compare is an instruction of the 1/64-rate FP64 pipe.  Both give the same
+// B, and the flux equals the reference's to rounding.
 template <class T>
 __device__ __forceinline__ T waf_flux(T hvel, T is, T zamu, T a, T c, T num) {
   const T den = c - a;
-  const T aden = fabs(den);
+  const T d = fabs(den);
+  const T q = den < T(0) ? -num : num;
   T B;
-  if (aden < FlowEps<T>::den()) {
+  if (d < FlowEps<T>::den()) {
     B = fabs(num) < FlowEps<T>::num() ? den : T(0);  // r = 1 or r = 0
+  } else if constexpr (sizeof(T) == sizeof(float)) {
+    const T bd = fmax(T(0), fmin(d + d, fmax(q, fmin(q + q, d))));
+    B = den < T(0) ? -bd : bd;
   } else {
-    const T q = den < T(0) ? -num : num;  // r = q / |den|
     if (q <= T(0)) B = T(0);
-    else if (q < T(0.5) * aden) B = num + num;
-    else if (q <= aden) B = den;
-    else if (q < T(2) * aden) B = num;
+    else if (q < T(0.5) * d) B = num + num;
+    else if (q <= d) B = den;
+    else if (q < T(2) * d) B = num;
     else B = den + den;
   }
   return hvel * ((a + c) - (is * den + (zamu - is) * B));

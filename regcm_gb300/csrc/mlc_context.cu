@@ -449,7 +449,7 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
     for (int n = 0; n < nsound; ++n) {
       const int uvoff = r * nsound + n;
       REC("sound_div", K::sound_div(L, d, uvoff, s)); ++nl;
-      REC("sound_solve", K::sound_solve(L, d, uvoff, r, n == nsound - 1, s)); ++nl;
+      REC("sound_solve", K::sound_solve(L, d, uvoff, r, n == nsound - 1, s)); nl += x->mixed ? 3 : 1;
       REC("sound_momentum", K::sound_momentum(L, d, uvoff, r, s)); ++nl;
     }
     // ---- advection (Main/mod_moloch.F90:767-1042) ----

@@ -234,48 +234,53 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
 }
 
 // The solve of a mixed member (same equations as k_sound_solve), in FP32
-// only.  Where rounding is amplified the values are double-floats: theta_v at
-// half levels, the hydrostatic balance -cp*theta_v*fmzf*dtrdz*(pai(k-1) -
+// only, split at the recurrence so that only the Thomas recurrence runs column
+// by column.  Where rounding is amplified the values are double-floats: theta_v
+// at half levels, the hydrostatic balance -cp*theta_v*fmzf*dtrdz*(pai(k-1) -
 // pai(k)) - g*dts of the w equation (two terms of ~g*dts whose difference
-// drives w), and the Exner update pai - pai*increment.  The divergence
-// filter, the elimination coefficients, the recurrence and the back
-// substitution are O(1)-conditioned and run in plain FP32.
+// drives w), and the Exner update pai - pai*increment.  The divergence filter,
+// the elimination coefficients (O(1)-conditioned), the recurrence and the back
+// substitution run in plain FP32.  Scratch (free during the acoustic
+// loop): wz[2] theta_v(k-1) - theta_v(k) from sound_prep; the FP32 planes of
+// wz_d[0] hold zf and the explicit w, those of wz_d[1] the coefficients zu
+// and zd (zu is overwritten by the elimination multipliers).
 template <class R>
-__global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
+struct SolveScratch {
+  float *zf, *zw, *zu, *zd;
+  __device__ __forceinline__ SolveScratch(const Dom<R> &D, size_t F)
+      : zf(reinterpret_cast<float *>(D.wz_d[0])), zw(zf + F),
+        zu(reinterpret_cast<float *>(D.wz_d[1])), zd(zu + F) {}
+};
+
+// Level-parallel part 1: the filtered divergence zf and, per level 2..kz,
+// theta_v at the half level, the explicit w and the coefficients zu, zd.
+template <class R>
+__global__ void k_solve_coef(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
+  const Pt q = point_of(tiles_j, 2, 2);
+  const int j = q.j, i = q.i, kz = g.kz;
+  if (j > g.jx - 2 || i > g.iy - 2 || q.k > kz) return;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const int adv = (D.clk->adv_role + advoff) & 1;
   const R *__restrict__ zraw = D.zdiv2;
-  R *__restrict__ s = D.s;
-  R *__restrict__ w = D.w;
-  extern __shared__ float msm[];
-  const int nth = blockDim.x * blockDim.y;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  const int kz = g.kz;
-  float *zf = msm;
-  float *wp = msm + (size_t)(kz + 2) * nth;
-  float *wk = msm + (size_t)2 * (kz + 2) * nth;
-#define COL(a, k) a[(size_t)(k) * nth + tid]
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  if (j > g.jx - 2 || i > g.iy - 2) return;
-  const size_t PS = g.PS, F1 = PS * (size_t)(kz + 1);
-  const DF pai(D.pai[adv], g.field3()), tvf_a(D.tetavf, F1), cfz(sa.cfz, F1);
+  const R *__restrict__ s = D.s;
+  const R *__restrict__ w = D.w;
+  const size_t PS = g.PS, F = g.field3(), F1 = PS * (size_t)(kz + 1);
+  const DF pai(D.pai[adv], F), tvf_a(D.tetavf, F1), cfz(sa.cfz, F1);
+  const SolveScratch<R> sc(D, F);
+  const float *__restrict__ dtet = D.wz[2];
   const float dtrdz = c.dtsoundf * c.rdzitaf;
   const float rdrcv = float(kRdrcv);
   const float rdt = rdrcv * dtrdz;
   const F2 ngdts{-c.gdts_hi, -c.gdts_lo};
-  const size_t ij = g.at2(j, i);
-  const size_t P = (size_t)g.P;
+  const size_t ij = g.at2(j, i), P = (size_t)g.P;
   const int32_t ib = sa.ibnd_cr[ij];
   const int nsp = c.nspgx;
-
-  float sk = float(s[ij]);
-  #pragma unroll 4
-  for (int k = 1; k <= kz; ++k) {
+  // divergence_diffusion plus the vertical divergence (:531-543, :627-630)
+  auto zf_at = [&](int k) -> float {
     const size_t o = ij + (size_t)(k - 1) * PS;
     float z = float(zraw[o]);
     if (c.divfilter) {
@@ -283,73 +288,106 @@ __global__ void k_sound_solve_mixed(const Dom<R> *__restrict__ doms, int advoff,
                          float(zraw[o + P]) - 4.f * z);
       z = z + sa.xknu_r[k - 1] * lap;
     }
-    const float skp1 = float(s[o + PS]);
     const float bw = ib > 0 ? 1.f - sa.hefc_r[(size_t)(ib - 1) + (size_t)(k - 1) * nsp] : 1.f;
-    z = z + bw * dtrdz * float(sa.fmz[o]) * (sk - skp1);
-    COL(zf, k) = z;
-    sk = skp1;
+    return z + bw * dtrdz * float(sa.fmz[o]) * (float(s[o]) - float(s[o + PS]));
+  };
+  float zf_m = q.k >= 2 ? zf_at(q.k - 1) : 0.f;
+#pragma unroll
+  for (int k = q.k; k < q.k + kPtLevels && k <= kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    const float zfk = zf_at(k);
+    sc.zf[o] = zfk;
+    if (k >= 2) {
+      const F2 pai_m = pai.ld(o - PS), pai_k = pai.ld(o);
+      const float wold = float(w[o]);
+      const float corr = wold * float(sa.fmzf[o]) * dtrdz * dtet[o];
+      const F2 tvf = df_add_f(tvf_a.ld(o), -corr);
+      tvf_a.st(o, tvf);
+      const F2 zrd = df_mul(tvf, cfz.ld(o));
+      const F2 dp = two_sum(pai_m.hi - pai_k.hi, pai_m.lo - pai_k.lo);  // hi difference exact
+      const F2 bal = df_add(ngdts, df_mul(F2{-zrd.hi, -zrd.lo}, dp));
+      const float zr = df_f(zrd), pm = df_f(pai_m), pk = df_f(pai_k);
+      float zw = wold + df_f(bal);
+      zw = zw + rdrcv * zr * (pm * zf_m - pk * zfk);
+      const float ff = sa.ffilt_r[k - 1];
+      sc.zw[o] = zw;
+      sc.zu[o] = rdt * float(sa.fmz[o - PS]) * zr * pm + ff;
+      sc.zd[o] = rdt * float(sa.fmz[o]) * zr * pk + ff;
+    }
+    zf_m = zfk;
   }
+}
 
-  // zrd = cp*tvf*fmzf*dtrdz = tvf*cfz; zcs2*zrom1w = rdrcv*dtrdz*zrd
-  const float *__restrict__ dtet = D.wz[2];  // theta_v(k-1) - theta_v(k), sound_prep
+// Part 2, per column: elimination k = kz..2 (:634-656) and back substitution
+// (:660-664); the new w replaces the old one, the multipliers replace zu.
+template <class R>
+__global__ void k_solve_sweep(const Dom<R> *__restrict__ doms) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (j > g.jx - 2 || i > g.iy - 2) return;
+  const int kz = g.kz;
+  const size_t PS = g.PS, F = g.field3();
+  const SolveScratch<R> sc(D, F);
+  R *__restrict__ w = D.w;
+  const size_t ij = g.at2(j, i);
   float wnext = float(w[ij + (size_t)kz * PS]);
   float wkp1 = 0.f;
-  F2 pai_k = pai.ld(ij + (size_t)(kz - 1) * PS);
-  float pk_f = df_f(pai_k);
-  float fmz_k = float(sa.fmz[ij + (size_t)(kz - 1) * PS]);
-  #pragma unroll 4
+#pragma unroll 4
   for (int k = kz; k >= 2; --k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
-    const F2 pai_m = pai.ld(o - PS);
-    const float fmz_m = float(sa.fmz[o - PS]);
-    const float wold = float(w[o]);
-    const float corr = wold * float(sa.fmzf[o]) * dtrdz * dtet[o];
-    const F2 tvf = df_add_f(tvf_a.ld(o), -corr);
-    tvf_a.st(o, tvf);
-    const F2 zrd = df_mul(tvf, cfz.ld(o));
-    const F2 dp = two_sum(pai_m.hi - pai_k.hi, pai_m.lo - pai_k.lo);  // hi difference exact
-    const F2 bal = df_add(ngdts, df_mul(F2{-zrd.hi, -zrd.lo}, dp));
-    float zwexpl = wold + df_f(bal);
-    const float zr = df_f(zrd);
-    const float pm_f = df_f(pai_m);
-    zwexpl = zwexpl + rdrcv * zr * (pm_f * COL(zf, k - 1) - pk_f * COL(zf, k));
-    const float ff = sa.ffilt_r[k - 1];
-    const float zu = rdt * fmz_m * zr * pm_f + ff;
-    const float zd = rdt * fmz_k * zr * pk_f + ff;
+    const float zu = sc.zu[o], zd = sc.zd[o];
     const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
-    wnext = zrapp * (zwexpl + zd * wnext);
+    wnext = zrapp * (sc.zw[o] + zd * wnext);
     wkp1 = zrapp * zu;
-    COL(wp, k) = wnext;
-    COL(wk, k) = wkp1;
-    pai_k = pai_m; pk_f = pm_f; fmz_k = fmz_m;
+    w[o] = (R)wnext;
+    sc.zu[o] = wkp1;
   }
   float wprev = float(w[ij]);
-  COL(wp, 1) = wprev;
-  #pragma unroll 4
+#pragma unroll 4
   for (int k = 2; k <= kz; ++k) {
-    wprev = COL(wp, k) + COL(wk, k) * wprev;
-    COL(wp, k) = wprev;
-    w[ij + (size_t)(k - 1) * PS] = (R)wprev;
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    wprev = float(w[o]) + sc.zu[o] * wprev;
+    w[o] = (R)wprev;
   }
-  COL(wp, kz + 1) = float(w[ij + (size_t)kz * PS]);
-  #pragma unroll 4
-  for (int k = 1; k <= kz; ++k) {
+}
+
+// Part 3, level-parallel: the Exner update (:668-671) and, after the last
+// substep, the completed s (:728-734).
+template <class R>
+__global__ void k_solve_exner(const Dom<R> *__restrict__ doms, int advoff, int last, int tiles_j) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const Pt q = point_of(tiles_j, 2, 2);
+  const int j = q.j, i = q.i, kz = g.kz;
+  if (j > g.jx - 2 || i > g.iy - 2 || q.k > kz) return;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const size_t PS = g.PS, F = g.field3();
+  const DF pai(D.pai[adv], F);
+  const SolveScratch<R> sc(D, F);
+  const R *__restrict__ w = D.w;
+  R *__restrict__ s = D.s;
+  const float dtrdz = c.dtsoundf * c.rdzitaf;
+  const float rdrcv = float(kRdrcv);
+  const size_t ij = g.at2(j, i);
+#pragma unroll
+  for (int k = q.k; k < q.k + kPtLevels && k <= kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
     const F2 pk = pai.ld(o);
-    const float inc = rdrcv * (COL(zf, k) + (dtrdz * float(sa.fmz[o]) * (COL(wp, k) - COL(wp, k + 1))));
+    const float inc = rdrcv * (sc.zf[o] + (dtrdz * float(sa.fmz[o]) * (float(w[o]) - float(w[o + PS]))));
     const F2 d = df_mul_f(pk, inc);
     pai.st(o, df_add(pk, F2{-d.hi, -d.lo}));
+    if (last && k >= 2) s[o] = (R)((float(w[o]) + float(s[o])) * float(sa.fmzf[o]));
   }
-  if (last) {
-    #pragma unroll 4
-    for (int k = 2; k <= kz; ++k) {
-      const size_t o = ij + (size_t)(k - 1) * PS;
-      s[o] = (R)((COL(wp, k) + float(s[o])) * float(sa.fmzf[o]));
-    }
+  if (last && q.k == 1) {
     s[ij] = R(0);
     s[ij + (size_t)kz * PS] = R(0);
   }
-#undef COL
 }
 
 // Main/mod_moloch.F90:677-721 with divergence_damping :738-765 folded in
@@ -488,10 +526,16 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
   const dim3 grd((unsigned)((L.jx - 3 + blk.x - 1) / blk.x), (unsigned)((L.iy - 3 + blk.y - 1) / blk.y),
                  (unsigned)L.nmem);
   const size_t cols = (size_t)3 * (L.kz + 2) * blk.x * blk.y;
-  if constexpr (sizeof(R) == sizeof(float))
-    k_sound_solve_mixed<R><<<grd, blk, cols * sizeof(float), s>>>(d, advoff, last ? 1 : 0);
-  else
+  if constexpr (sizeof(R) == sizeof(float)) {
+    // coefficients and Exner update level-parallel, the recurrence per column
+    int tj;
+    const dim3 pg = pt_grid(L, L.jx - 3, L.iy - 3, tj);
+    k_solve_coef<R><<<pg, col_block(L), 0, s>>>(d, advoff, tj);
+    k_solve_sweep<R><<<grd, blk, 0, s>>>(d);
+    k_solve_exner<R><<<pg, col_block(L), 0, s>>>(d, advoff, last ? 1 : 0, tj);
+  } else {
     k_sound_solve<R><<<grd, blk, cols * sizeof(double), s>>>(d, advoff, last ? 1 : 0);
+  }
 }
 
 template <class R>
@@ -505,8 +549,7 @@ void Launch<R>::sound_momentum(const LaunchGeom &L, const Dom<R> *d, int uvoff, 
 template <class R>
 cudaError_t Launch<R>::configure_sound() {
   if constexpr (sizeof(R) == sizeof(float))
-    return cudaFuncSetAttribute(k_sound_solve_mixed<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                200 * 1024);
+    return cudaSuccess;  // the mixed solve uses no dynamic shared memory
   else
     return cudaFuncSetAttribute(k_sound_solve<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 200 * 1024);

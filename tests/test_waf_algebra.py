@@ -25,23 +25,45 @@ def ref_flux(hvel, is_, zamu, a, c, num):
 
 
 def new_flux(hvel, is_, zamu, a, c, num):
+    """The kernels' form: B = sign(den) * max(0, min(2d, max(q, min(2q, d))))
+    with d = |den|, q = num*sign(den); no division, no branch on r."""
     den = c - a
+    d = abs(den)
+    q = -num if den < 0 else num
+    bd = max(0.0, min(d + d, max(q, min(q + q, d))))
+    B = -bd if den < 0 else bd
+    if d < 1.0e-30:
+        B = den if abs(num) < float(np.float32(1.0e-30)) else 0.0
+    return hvel * ((a + c) - (is_ * den + (zamu - is_) * B))
+
+
+def branch_b(num, den):
+    """B = b*den by region of r = num/den (the earlier form, kept as a check)."""
     aden = abs(den)
     if aden < 1.0e-30:
-        B = den if abs(num) < float(np.float32(1.0e-30)) else 0.0
-    else:
+        return den if abs(num) < float(np.float32(1.0e-30)) else 0.0
+    q = -num if den < 0 else num
+    if q <= 0:
+        return 0.0
+    if q < 0.5 * aden:
+        return num + num
+    if q <= aden:
+        return den
+    if q < 2.0 * aden:
+        return num
+    return den + den
+
+
+def test_clamp_limiter_equals_region_form_exactly():
+    rng = np.random.default_rng(3)
+    for _ in range(20000):
+        den = rng.normal() * 10 ** rng.uniform(-3, 3)
+        num = den * rng.choice([-1.0, 0.0, 0.25, 0.5, 0.75, 1.0, 1.5, 2.0, 3.0, rng.uniform(-3, 3)])
+        d = abs(den)
         q = -num if den < 0 else num
-        if q <= 0:
-            B = 0.0
-        elif q < 0.5 * aden:
-            B = num + num
-        elif q <= aden:
-            B = den
-        elif q < 2.0 * aden:
-            B = num
-        else:
-            B = den + den
-    return hvel * ((a + c) - (is_ * den + (zamu - is_) * B))
+        bd = max(0.0, min(d + d, max(q, min(q + q, d))))
+        B = -bd if den < 0 else bd
+        assert B == branch_b(num, den), (num, den)
 
 
 def test_division_free_flux_matches_reference():
