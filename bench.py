@@ -142,6 +142,13 @@ def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None
     return None if by is None else float(by)
 
 
+# DRAM bytes per point of a launch, measured by ncu on a smaller case of the same
+# kernel and precision (profiles/adv_horizontal_fp64_moist256_full.md: 715.5 MB
+# for 2.69 M points of the moist recipe, 10 advected fields); scaled to the
+# bench case by its points.  Keyed by (kernel, precision, advected fields).
+MEASURED_TRAFFIC_PER_POINT = {("adv_horizontal", "fp64", 10): 715.5e6 / (256 * 256 * 41)}
+
+
 def n_adv_fields(case) -> int:
     p, d = case.params, case.dims
     return 6 + (d.nqx - 1 if p.ipptls > 0 else 0) + d.ntr
@@ -287,6 +294,11 @@ def run_ours(args, rank, world):
         "share_of_step": kms / total_k,
         "traffic": None,
     }
+    tpp = MEASURED_TRAFFIC_PER_POINT.get((dom_name, args.precision, nf))
+    if tpp:
+        roofline["traffic"] = tpp * case.points
+        roofline["traffic_source"] = "ncu on 256x256x41, scaled by points"
+
     if bytes_per:
         ach = bytes_per / (kms / nl / 1000.0) / 1e9
         roofline.update({"achieved": ach, "frac": ach / hbm_peak, "algorithmic_bytes": bytes_per})
