@@ -262,6 +262,55 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
 #undef A
 }
 
+// ---- TMA tile loads and mbarriers (inline PTX, sm_90+) ----------------------
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// orders this thread's earlier generic-proxy accesses of shared memory before
+// a following async-proxy (TMA) write to it
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// one tiled copy of the box at (x, y, z) of the tensor map into shared memory
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+// gives up after a bounded number of polls (a copy that never lands must not
+// hang the GPU); the caller records the fault
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
+  for (int it = 0; it < (1 << 18); ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+template <int TJ, int TI>
+constexpr int tile_shape_index() {
+  return (TJ == 32 && TI == 8) ? 0 : (TJ == 32 && TI == 4) ? 1 : (TJ == 64 && TI == 4) ? 2 : 3;
+}
+
 // Meridional then zonal WAF for one tile at one level, every field of the R
 // table (:984-1038; ROTLLR :926-983).  The winds, Courant numbers and metric
 // coefficients of the tile are formed once, in shared memory, and then each
@@ -276,7 +325,14 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
                                                             int tiles_j, int uvoff, int advoff) {
   using T = R;
   constexpr int WJ = kTJ + 4;            // columns J0-2 .. J0+TJ+1
-  __shared__ T wz_s[kTI + 4][WJ];        // rows I0-2 .. I0+TI+1
+  // halo tiles of two fields (TMA destinations, double-buffered): rows
+  // I0-2 .. I0+TI+1; column J0-2+cc of the kernel sits at cc + OFF, the copy
+  // starting OFF columns further left so that it starts on 16 bytes
+  constexpr int OFF = sizeof(T) == sizeof(float) ? 2 : 0;
+  constexpr int BW = WJ + 2 * OFF;
+  constexpr unsigned kBox = (unsigned)((kTI + 4) * BW * sizeof(T));
+  __shared__ __align__(128) T wzt[2][kTI + 4][BW];
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ T zpby_s[kTI + 1][WJ];      // rows I0 .. I0+TI
   __shared__ T p0_s[kTI][WJ];            // rows I0 .. I0+TI-1
   __shared__ T zpbw_s[kTI][kTJ + 1];     // columns J0 .. J0+TJ
@@ -308,8 +364,26 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
   const bool rot = c.lrotllr != 0;
   const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
   const int nf = n_table_r(D);
+  const char *tmaps = static_cast<const char *>(D.tmap) +
+                      (size_t)tile_shape_index<kTJ, kTI>() * kMaxFields * kTmapBytes;
+  auto issue = [&](int fld, int b) {  // one thread: the halo tile of field fld into buffer b
+    fence_proxy_async();
+    mbar_expect_tx(&mbar[b], kBox);
+    tma_load_3d(&wzt[b][0][0], tmaps + (size_t)fld * kTmapBytes, J0 - 3 - OFF, I0 - 3, k - 1,
+                &mbar[b]);
+  };
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    issue(0, 0);
+    if (nf > 1) issue(1, 1);
+  }
 
-  // ---- field-independent factors ----
+  // ---- field-independent factors (while the first tiles land) ----
   for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
     const int rr = e / WJ, cc = e % WJ;
     const int i = I0 + rr, j = J0 - 2 + cc;
@@ -385,15 +459,20 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
     const T *pp = cur0 + ko;
     const T *wz = wz0 + ko;
     T *out = out0 + ko;
-    // stage wz (cross points only; others are never read for valid outputs)
-    for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
-      const int rr = e / WJ, cc = e % WJ;
-      const int i = I0 - 2 + rr, j = J0 - 2 + cc;
-      T x = T(0);
-      if (i >= 1 && i <= iy - 1 && j >= 1 && j <= jx - 1) x = wz[g.at2(j, i)];
-      wz_s[rr][cc] = x;
+    (void)wz;
+    // the field's halo tile (zero outside the cross points)
+    const int b = f & 1;
+    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((f >> 1) & 1));
+    if (__syncthreads_or(!landed)) {  // also orders the factors above before their use
+      if (tid == 0) {
+        atomicOr(&D.clk->fault, 1);
+        // let copies still in flight land before the shared memory is released
+        mbar_wait_bounded(&mbar[b], (unsigned)((f >> 1) & 1));
+        if (f + 1 < nf) mbar_wait_bounded(&mbar[b ^ 1], (unsigned)(((f + 1) >> 1) & 1));
+      }
+      return;
     }
-    __syncthreads();  // also orders the factors above before their first use
+    T (*wz_s)[BW] = wzt[b];
     // meridional fluxes zpby(j,i): j in jce, i in ici1..ice2
     for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
       const int rr = e / WJ, cc = e % WJ;
@@ -407,9 +486,9 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
         if (zamu > T(0)) { is = T(1); ih = i - 1; }
         else { is = T(-1); ih = min(i + 1, imax); }
         const int ihm1 = max(ih - 1, imin);
-        const int b = 2 - I0;  // shared-memory row of global row i is i + b
-        x = waf_flux<T>(T(0.5) * vv, is, zamu, wz_s[i - 1 + b][cc], wz_s[i + b][cc],
-                        wz_s[ih + b][cc] - wz_s[ihm1 + b][cc]);
+        const int bo = 2 - I0;  // shared-memory row of global row i is i + bo
+        x = waf_flux<T>(T(0.5) * vv, is, zamu, wz_s[i - 1 + bo][cc + OFF], wz_s[i + bo][cc + OFF],
+                        wz_s[ih + bo][cc + OFF] - wz_s[ihm1 + bo][cc + OFF]);
       }
       zpby_s[rr][cc] = x;
     }
@@ -421,7 +500,7 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
       T x = T(0);
       if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
         const T ppk = pp[g.at2(j, i)];
-        const T wzk = wz_s[rr + 2][cc];
+        const T wzk = wz_s[rr + 2][cc + OFF];
         const T zdv = dvy_s[rr][cc] * ppk;
         const T zrfms = zs_s[rr][cc], zrfmn = zn_s[rr][cc];
         if (rot) x = wzk + (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
@@ -430,6 +509,8 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
       p0_s[rr][cc] = x;
     }
     __syncthreads();
+    // buffer b is read for the last time above: fetch the field after next
+    if (tid == 0 && f + 2 < nf) issue(f + 2, b);
     // zonal fluxes zpbw(j,i): j in jci1..jce2, i in ici
     for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
       const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
@@ -443,9 +524,9 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
         if (zamu > T(0)) { is = T(1); jh = j - 1; }
         else { is = T(-1); jh = min(j + 1, jmax); }
         const int jhm1 = max(jh - 1, jmin);
-        const int b = 2 - J0;  // p0_s column of global column j is j + b
-        x = waf_flux<T>(T(0.5) * uu, is, zamu, p0_s[rr][j - 1 + b], p0_s[rr][j + b],
-                        p0_s[rr][jh + b] - p0_s[rr][jhm1 + b]);
+        const int bo = 2 - J0;  // p0_s column of global column j is j + bo
+        x = waf_flux<T>(T(0.5) * uu, is, zamu, p0_s[rr][j - 1 + bo], p0_s[rr][j + bo],
+                        p0_s[rr][jh + bo] - p0_s[rr][jhm1 + bo]);
       }
       zpbw_s[rr][cc] = x;
     }

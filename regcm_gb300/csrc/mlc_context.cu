@@ -22,6 +22,9 @@
 #include <new>
 #include <vector>
 
+#include <cuda.h>          // CUtensorMap and its enums (the encoder is fetched at run time)
+#include <cudaTypedefs.h>
+
 #include "../../include/moloch_gb300.h"
 #include "mlc_kernels.cuh"
 
@@ -180,6 +183,7 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
   D.red_blocks = reduce_blocks(g);
   D.rows_per_block = reduce_rows_per_block(g);
   D.partials = cv.take<double>((size_t)D.red_blocks * 8);
+  D.tmap = cv.take<char>((size_t)kTileShapes * kMaxFields * kTmapBytes);
 }
 
 template <class R>
@@ -308,6 +312,62 @@ int ensure_staging(mlc_ctx *x, const mlc_dims &d) {
   return MLC_OK;
 }
 
+// ---- TMA tensor maps of the wz fields --------------------------------------
+// The horizontal WAF loads each field's halo tile (rows I0-2 .. I0+TI+1,
+// columns J0-2 .. J0+TJ+1 at one level) with one tiled TMA copy.  The map's
+// extents are the cross points (jx-1, iy-1, kz), so everything outside them
+// reads as zero, as the kernel needs.  A copy must start on a 16-byte
+// boundary: FP32 tiles start 4 columns left of J0 (x = TJ*bj - 4) and are
+// TJ+8 wide, FP64 tiles 2 columns left (x = TJ*bj - 2) and TJ+4 wide; both
+// widths are multiples of 16 bytes and x*element size is a multiple of 16.
+const int kTileJ[kTileShapes] = {32, 32, 64, 16};
+const int kTileI[kTileShapes] = {8, 4, 4, 8};
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+template <class R>
+int encode_tmaps(mlc_ctx *x, const Member &m, const Dom<R> &D) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return MLC_ERR_CUDA;
+  const Geom &g = m.g;
+  const int nf = n_table_r(m.dims, x->prm, sizeof(R) == sizeof(double));
+  std::vector<CUtensorMap> maps((size_t)kTileShapes * kMaxFields);
+  std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+  const size_t es = sizeof(R);
+  const cuuint64_t dims[3] = {(cuuint64_t)(g.jx - 1), (cuuint64_t)(g.iy - 1), (cuuint64_t)g.kz};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.P * es, (cuuint64_t)g.PS * es};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  for (int t = 0; t < kTileShapes; ++t) {
+    const cuuint32_t box[3] = {(cuuint32_t)(kTileJ[t] + (es == 4 ? 8 : 4)), (cuuint32_t)(kTileI[t] + 4), 1};
+    for (int f = 0; f < nf; ++f) {
+      const CUresult r = enc(&maps[(size_t)t * kMaxFields + f],
+                             es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                             3, const_cast<R *>(D.wz[f]), dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return MLC_ERR_CUDA;
+    }
+  }
+  MLC_TRY(cudaMemcpyAsync(const_cast<void *>(D.tmap), maps.data(), maps.size() * sizeof(CUtensorMap),
+                          cudaMemcpyHostToDevice, x->stream));
+  return cuda_status(cudaStreamSynchronize(x->stream));
+}
+
 // Give slot `slot` a member of extents d: allocate and zero its arena, reset
 // its clock and diagnostics.  Every array starts at zero: s and w at the ring
 // stay zero, as the reference's reset_tendencies and init_moloch leave them.
@@ -333,6 +393,13 @@ int add_member(mlc_ctx *x, int slot, const mlc_dims &d) {
   MLC_TRY(cudaMemsetAsync(x->clks + slot, 0, sizeof(Clock), x->stream));
   MLC_TRY(cudaMemsetAsync(x->diags + slot, 0, sizeof(DiagDev), x->stream));
   MLC_TRY(cudaStreamSynchronize(x->stream));
+  {
+    const int st = x->mixed ? encode_tmaps<float>(x, m, m.df) : encode_tmaps<double>(x, m, m.dd);
+    if (st != MLC_OK) {
+      cudaFreeAsync(m.raw, x->stream);
+      return st;
+    }
+  }
   m.used = true;
   x->mem[slot] = m;
   x->in_use += m.bytes;
@@ -548,9 +615,30 @@ Clock get_clock(mlc_ctx *x, int slot, int *st) {
 // device layout through the staging buffer at element offset `soff`.  One
 // stream orders every copy and (un)pack, so consecutive fields may reuse the
 // same staging slice.
+// An FP64 array goes straight between the packed host array and the padded
+// device layout in one pitched copy (rows of nj, ni rows of a plane on the
+// host, iy on the device); a conversion to FP32 goes through the staging buffer.
+cudaMemcpy3DParms pitched(const Geom &g, const double *host, double *dev, int nj, int ni, int nk,
+                          bool to_device) {
+  cudaMemcpy3DParms c{};
+  cudaPitchedPtr hp = make_cudaPitchedPtr(const_cast<double *>(host), (size_t)nj * sizeof(double),
+                                          (size_t)nj, (size_t)ni);
+  cudaPitchedPtr dp = make_cudaPitchedPtr(dev, (size_t)g.P * sizeof(double), (size_t)g.P, (size_t)g.iy);
+  c.srcPtr = to_device ? hp : dp;
+  c.dstPtr = to_device ? dp : hp;
+  c.extent = make_cudaExtent((size_t)nj * sizeof(double), (size_t)ni, (size_t)nk);
+  c.kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  return c;
+}
+
 template <class R>
 int put3(mlc_ctx *x, const Geom &g, const double *h, R *dst, int nj, int ni, int nk, size_t soff) {
   if (!h) return MLC_OK;
+  if constexpr (sizeof(R) == sizeof(double)) {
+    const cudaMemcpy3DParms c = pitched(g, h, reinterpret_cast<double *>(dst), nj, ni, nk, true);
+    MLC_TRY(cudaMemcpy3DAsync(&c, x->stream));
+    return MLC_OK;
+  }
   const size_t n = (size_t)nj * ni * nk;
   if (soff + n > x->staging_elems) return MLC_ERR_INVALID;
   MLC_TRY(cudaMemcpyAsync(x->staging + soff, h, n * sizeof(double), cudaMemcpyHostToDevice, x->stream));
@@ -579,6 +667,12 @@ int get3x(mlc_ctx *x, const Geom &g, const double *src, double *h, int nj, int n
 template <class R>
 int get3(mlc_ctx *x, const Geom &g, const R *src, double *h, int nj, int ni, int nk, size_t soff) {
   if (!h) return MLC_OK;
+  if constexpr (sizeof(R) == sizeof(double)) {
+    const cudaMemcpy3DParms c =
+        pitched(g, h, reinterpret_cast<double *>(const_cast<R *>(src)), nj, ni, nk, false);
+    MLC_TRY(cudaMemcpy3DAsync(&c, x->stream));
+    return MLC_OK;
+  }
   const size_t n = (size_t)nj * ni * nk;
   if (soff + n > x->staging_elems) return MLC_ERR_INVALID;
   Launch<R>::pack3(src, x->staging + soff, g, nj, ni, nk, x->stream);
@@ -963,10 +1057,11 @@ int fetch_diags(mlc_ctx *x, int nsteps, mlc_diag *out) {
   MLC_TRY(cudaMemcpyAsync(dd.data(), x->diags, n * sizeof(DiagDev), cudaMemcpyDeviceToHost, x->stream));
   MLC_TRY(cudaMemcpyAsync(ck.data(), x->clks, n * sizeof(Clock), cudaMemcpyDeviceToHost, x->stream));
   MLC_TRY(cudaStreamSynchronize(x->stream));
-  bool bad = false;
+  bool bad = false, fault = false;
   for (size_t m = 0; m < n; ++m) {
     const bool used = x->mem[m].used;
     if (used && ck[m].nonfinite) bad = true;
+    if (used && ck[m].fault) fault = true;
     if (!out) continue;
     std::memset(&out[m], 0, sizeof(out[m]));
     if (!used) continue;
@@ -979,6 +1074,10 @@ int fetch_diags(mlc_ctx *x, int nsteps, mlc_diag *out) {
     out[m].qmass = dd[m].qmass;
     out[m].qadv = dd[m].qadv;
     out[m].xbctime = ck[m].xbctime;
+  }
+  if (fault) {
+    g_last_error = "a bounded device wait gave up (TMA tile load)";
+    return MLC_ERR_CUDA;
   }
   return bad ? MLC_ERR_NONFINITE : MLC_OK;
 }

@@ -103,7 +103,7 @@ struct Clock {
   int step;          // steps completed since the last reset
   int uv_role;       // half of the u/v pairs holding the state at step start
   int adv_role;      // half of the advected-field pairs holding the state
-  int pad;
+  int fault;         // sticky: a bounded device wait gave up (1 = TMA tile load)
 };
 
 // Mass budget and ps extrema of the last step (FP64).
@@ -135,7 +135,12 @@ struct Dom {
   double *partials;
   int red_blocks, rows_per_block;
   int active;            // 0: an empty slot, every block returns at once
+  // TMA tensor maps (CUtensorMap, 128 B each, 64-B aligned) of the wz fields,
+  // [horizontal tile shape][field], for the horizontal WAF's halo tiles
+  const void *tmap;
 };
+constexpr int kTileShapes = 4;   // horizontal WAF tiles 32x8, 32x4, 64x4, 16x8
+constexpr int kTmapBytes = 128;
 
 // A per-domain constant in the kernel's field type: the FP64 value for an
 // FP64 member, its FP32 copy for a mixed one (no conversion on the device).
