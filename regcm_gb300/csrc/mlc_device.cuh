@@ -192,6 +192,21 @@ __device__ __forceinline__ F2 df_mul_f(F2 a, float b) {
   const F2 p = two_prod(a.hi, b);
   return fast_two_sum(p.hi, fmaf(a.lo, b, p.lo));
 }
+// a / b for a double-float a and an FP32 b: one correction of the FP32 quotient
+// with the exact remainder (a - q*b by TwoProduct)
+__device__ __forceinline__ F2 df_div_f(F2 a, float b) {
+  const float q1 = a.hi / b;
+  const F2 p = two_prod(q1, b);
+  const float r = ((a.hi - p.hi) - p.lo) + a.lo;
+  return fast_two_sum(q1, r / b);
+}
+// a / b for double-floats, the same way
+__device__ __forceinline__ F2 df_div(F2 a, F2 b) {
+  const float q1 = a.hi / b.hi;
+  const F2 p = df_mul(F2{q1, 0.f}, b);
+  const float r = ((a.hi - p.hi) - p.lo) + a.lo;
+  return fast_two_sum(q1, r / b.hi);
+}
 // a - b rounded to FP32 (the hi difference is exact for values within 2x)
 __device__ __forceinline__ float df_diff(F2 a, F2 b) { return (a.hi - b.hi) + (a.lo - b.lo); }
 __device__ __forceinline__ float df_f(F2 a) { return a.hi + a.lo; }

@@ -43,16 +43,19 @@ __global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff, int til
     const size_t o = ij + (size_t)(k - 1) * g.PS;
     const R qf = qfactor(st.qx, o, F, c.ipptls);
     if constexpr (sizeof(R) == sizeof(float)) {
+      // t as a double-float through the step end: hi in t, lo in wz[1] (the
+      // scratch is free until the next advection); status_update rebuilds
+      // theta_v = t*qf/pai from it, so t's FP32 rounding never reaches theta_v
       const DF th(st.tetav, F), pa(st.pai, F);
-      const F2 pk = pa.ld(o);
-      const R tv = df_f(df_mul(th.ld(o), pk));
-      st.tvirt[o] = tv;
-      if (inner) st.t[o] = tv / qf;
-      // what status_update needs to carry theta_v over as a ratio
-      // (t_end = tvirt/qf also at the ring, where t itself is not refreshed)
-      D.wz[0][o] = qf;
-      D.wz[1][o] = inner ? st.t[o] : tv / qf;
-      DF(D.wz_d[0], F).st(o, pk);
+      const F2 tv = df_mul(th.ld(o), pa.ld(o));
+      st.tvirt[o] = df_f(tv);
+      if (inner) {
+        const F2 t = df_div_f(tv, qf);
+        st.t[o] = t.hi;
+        D.wz[1][o] = t.lo;
+      } else {
+        D.wz[1][o] = 0.f;  // the ring keeps its t (bdyval sets it)
+      }
     } else {
       const R tv = R(st.tetav[o] * st.pai[o]);
       st.tvirt[o] = tv;
@@ -111,6 +114,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     const R un = blend(bd.dub, od);
     st.u[od] = un;
     st.t[ob] = blend(bd.xtb, ob);
+    if constexpr (sizeof(R) == sizeof(float)) D.wz[1][ob] = 0.f;
     set_pai_ring(ob);
     st.qx[ob] = blend(bd.xqb, ob);
     if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
@@ -140,6 +144,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     const R vn = blend(bd.dvb, od);
     st.v[od] = vn;
     st.t[ob] = blend(bd.xtb, ob);
+    if constexpr (sizeof(R) == sizeof(float)) D.wz[1][ob] = 0.f;
     set_pai_ring(ob);
     st.qx[ob] = blend(bd.xqb, ob);
     if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
@@ -226,7 +231,18 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
       st.v[o] = f;
     }
     if (!cr) continue;
-    {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      // (1-x)*t + x*b as t + x*(b - t) on the double-float t
+      F2 f{st.t[o], D.wz[1][o]};
+      const float bt = blend(bd.xtb, o);
+      if (nud) f = df_add_f(f, xfn * ((bt - f.hi) - f.lo));
+      if (ibc > 0) {
+        const float xf = sa.hefc_r[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
+        f = df_add_f(f, xf * ((bt - f.hi) - f.lo));
+      }
+      st.t[o] = f.hi;
+      D.wz[1][o] = f.lo;
+    } else {
       R f = st.t[o];
       if (nud) f = (R(1) - xfn) * f + xfn * blend(bd.xtb, o);
       if (ibc > 0) f = relax(f, blend(bd.xtb, o), ibc, k);
@@ -362,22 +378,10 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
     const R pk = st.p[o];
     st.rho[o] = pk / (R(kRgas) * tk);
     if constexpr (sizeof(R) == sizeof(float)) {
-      // theta_v = t*qf/pai as a ratio of the value carried in FP64:
-      //   theta_v' = theta_v * (t/t_end) * (qf/qf_end) * (pai_end/pai),
-      // t_end, qf_end, pai_end as end_tvirt left them.  Where none changed
-      // (the interior) theta_v keeps every FP64 digit; elsewhere the ratio's
-      // FP32 rounding falls on the change, not on theta_v.
-      const float qf0 = D.wz[0][o], t0 = D.wz[1][o];
-      const F2 p0 = DF(D.wz_d[0], F).ld(o), p1 = DF(st.pai, F).ld(o);
-      const float rt = (tk - t0) / t0;
-      const float rq = (qf - qf0) / qf0;
-      const float rp = (p0.hi != p1.hi || p0.lo != p1.lo) ? df_diff(p0, p1) / p1.hi : 0.f;
-      const float eps = rt + rq + rp + rt * rq + (rt + rq + rt * rq) * rp;
-      if (eps != 0.f) {
-        const DF th(st.tetav, F);
-        const F2 t = th.ld(o);
-        th.st(o, df_add(t, df_mul_f(t, eps)));
-      }
+      // theta_v = tvirt/pai from the double-float t (Main/mod_moloch.F90:1403-1443):
+      // where nothing relaxed t, t*qf/pai gives back theta_v to ~1e-14
+      const F2 t2{tk, D.wz[1][o]};
+      DF(st.tetav, F).st(o, df_div(df_mul_f(t2, qf), DF(st.pai, F).ld(o)));
       st.qsat[o] = pfwsat_f(tk, pk);
     } else {
       st.tetav[o] = (double)tv / st.pai[o];

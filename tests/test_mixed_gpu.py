@@ -1,11 +1,11 @@
-"""Mixed precision (FP32 fields and horizontal stencils; FP64 Exner function
-and theta_v, vertical implicit solve, pressure reconstruction and mass sums)
-against the FP64 CPU oracle after 100 steps.
+"""Mixed precision (FP32 fields and horizontal stencils; theta_v, Exner, the
+vertical implicit solve's hydrostatic balance, the Exner update, temperature
+through the step end and the mass sums carried to FP64 accuracy as
+double-floats) against the FP64 CPU oracle after 100 steps.
 
-theta_v, u, v and tracers stay within the specified 1e-4 relative L2.  w does
-not: with u and v stored in FP32 (about 1e-6 m/s), the horizontal divergence
-loses about three digits to cancellation and the implicit w follows it, so w
-sits near 3-5e-4.  The test holds w to 1e-3 and records that gap."""
+theta_v, u, v, w, qv and tracers stay within the specified 1e-4 relative L2
+(measured: w 2.4e-5 dry, 7.6e-5 moist; theta_v 1.7e-8 / 1.3e-7; v 2.0e-6 /
+1.3e-5), Exner within 1e-8."""
 from __future__ import annotations
 
 import numpy as np
@@ -43,14 +43,13 @@ def run_mixed_vs_oracle(make, nsteps):
 ])
 def test_mixed_hundred_steps(name, make):
     got, ref, dm, do = run_mixed_vs_oracle(make, 100)
-    err = {n: rel_l2(got[n], ref[n]) for n in ("tetav", "u", "v")}
+    err = {n: rel_l2(got[n], ref[n]) for n in ("tetav", "u", "v", "w")}
     if "trac" in ref:
         err["trac"] = rel_l2(got["trac"], ref["trac"])
+    err["qv"] = rel_l2(got["qx"][..., 0], ref["qx"][..., 0])
     bad = {k: v for k, v in err.items() if not v <= 1e-4}
     assert not bad, f"{name}: {err}"
-    assert rel_l2(got["w"], ref["w"]) <= 1e-3
-    # moisture and the thermodynamic diagnostics stay close too
-    assert rel_l2(got["qx"][..., 0], ref["qx"][..., 0]) <= 1e-4
-    assert rel_l2(got["pai"], ref["pai"]) <= 1e-7
+    assert rel_l2(got["pai"], ref["pai"]) <= 1e-8
+    assert rel_l2(got["tetav"], ref["tetav"]) <= 1e-6
     # FP64 mass sums of the FP32 state: the dry-air mass agrees to FP32 rounding
     assert abs(dm.drymass - do.drymass) <= 1e-6 * abs(do.drymass)
