@@ -115,29 +115,33 @@ def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None
     Counts follow the fusion contract 'each kernel reads its inputs and writes
     its outputs once'; 2-D and 1-D arrays are ignored.  Per point (cross
     point x level) of the launch's domain, with R the field type (wbytes) and
-    D = FP64 (the Exner function and theta_v are FP64 in both precisions,
-    and the solve reads FP64 copies of fmz, fmzf):
-      sound_div       u, v, rfmzu, rfmzv, fmz -> zdiv2, s               7 R
-      sound_solve     zdiv2, s, w -> w                                  4 R
-                      pai, tetav, tetavf, fmz, fmzf -> pai, tetavf      7 D
-      sound_momentum  u, v, zdiv2 -> u, v                               5 R
-                      pai, tetav                                        2 D
-      adv_vertical    per field: field -> wz (2); shared s, zrfmu, zrfmd
-      adv_horizontal  per field: field, wz -> out (3); shared u, v, fmz, rfmzu
-    where theta_v and Exner are the FP64 fields.
+    D = 8 bytes (the Exner function and theta_v: FP64, or a double-float pair
+    of FP32 planes in a mixed member; the FP64 solve also reads fmz, fmzf):
+      sound_div           u, v, rfmzu, rfmzv, fmz -> zdiv2, s               7 R
+      sound_solve         zdiv2, s, w -> w                                  4 R
+                          pai, tetav, tetavf, fmz, fmzf -> pai, tetavf      7 D
+      sound_momentum      u, v, zdiv2 -> u, v                               5 R
+                          pai, tetav                                        2 D
+      adv_vertical        per field of type R: field -> wz (2 R); shared s, zrfmu, zrfmd (3 R)
+      adv_horizontal      per field of type R: field, wz -> out (3 R); shared u, v, fmz, rfmzu (4 R)
+      adv_vertical_inc    theta_v, Exner of a mixed member: field -> increment (2 D each); 3 R shared
+      adv_horizontal_inc  the same two: field, increment -> out (3 D each); 4 R shared
+    In an FP64 member every advected field is of type R.
     """
     d = case.dims
     pts = (d.jx - 1) * (d.iy - 1) * d.kz
     inner = (d.jx - 3) * (d.iy - 3) * d.kz
     r, w = wbytes, 8
-    nd = 2                       # theta_v, Exner
-    nr = nadv_fields - nd        # fields of type R
+    nd = 2 if wbytes == 4 else 0     # double-float fields of a mixed member
+    nr = nadv_fields - nd            # fields of type R
     by = {
         "sound_div": 7 * r * pts,
         "sound_solve": (4 * r + 7 * w) * inner,
         "sound_momentum": (5 * r + 2 * w) * pts,
-        "adv_vertical": ((2 * nr + 3) * r + 2 * nd * w) * pts,
-        "adv_horizontal": ((3 * nr + 4) * r + 3 * nd * w) * pts,
+        "adv_vertical": (2 * nr + 3) * r * pts,
+        "adv_horizontal": (3 * nr + 4) * r * pts,
+        "adv_vertical_inc": (2 * nd * w + 3 * r) * pts if nd else None,
+        "adv_horizontal_inc": (3 * nd * w + 4 * r) * pts if nd else None,
     }.get(name)
     return None if by is None else float(by)
 

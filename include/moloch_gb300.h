@@ -249,13 +249,15 @@ size_t mlc_member_footprint(const mlc_dims *dims, const mlc_params *params);
 
 /* Launch shapes picked by mlc_autotune, and the per-step device time of the
  * tuned kernels against the fixed 32x8 configuration (column kernels and
- * horizontal WAF tiles 32x8; vertical WAF blocks of 32 columns x 8 level
- * threads; solve 32x2). */
+ * horizontal WAF tiles 32x8; vertical WAF blocks of 32 x 8 columns, one
+ * thread per column; solve 32x2). */
 typedef struct mlc_tune_report {
   int32_t col_x, col_y;      /* column kernels                        */
   int32_t solve_x, solve_y;  /* implicit w-Exner solve                */
   int32_t vert_x, vert_y;    /* vertical WAF passes                   */
-  int32_t htile;             /* horizontal WAF tile: 0 32x8, 1 32x4, 2 64x4, 3 16x8 */
+  int32_t htile;             /* horizontal WAF tile, columns x rows:
+                                FP32 0 32x8, 1 64x8, 2 128x8, 3 128x4;
+                                FP64 0 32x8, 1 64x8, 2 64x4, 3 32x4   */
   double  ms_fixed;          /* tuned kernel groups, fixed shapes [ms/step] */
   double  ms_tuned;          /* the same groups, picked shapes [ms/step]    */
 } mlc_tune_report;
@@ -265,6 +267,12 @@ typedef struct mlc_tune_report {
  * kernel group, and re-record the step graphs.  No counterpart in the
  * reference. */
 int mlc_autotune(mlc_ctx *ctx, int steps_per_trial, mlc_tune_report *rep);
+
+/* Apply launch shapes, e.g. a report saved from mlc_autotune on the same
+ * workload (its ms fields are ignored).  Each shape must be one of the
+ * autotuner's candidates, else MLC_ERR_INVALID and nothing changes.  Results
+ * do not depend on the shapes. */
+int mlc_set_launch_shapes(mlc_ctx *ctx, const mlc_tune_report *shapes);
 
 /* Device bytes one domain of these extents holds (for admission control). */
 size_t mlc_footprint_bytes(const mlc_dims *dims, int precision);

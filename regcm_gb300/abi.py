@@ -156,6 +156,7 @@ def _declare(lib):
         "mlc_launches_per_step": (C.c_int, [C.c_void_p]),
         "mlc_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
         "mlc_autotune": (C.c_int, [C.c_void_p, C.c_int, P(mlc_tune_report)]),
+        "mlc_set_launch_shapes": (C.c_int, [C.c_void_p, P(mlc_tune_report)]),
         "mlc_create_multi": (C.c_int, [P(mlc_dims), P(mlc_params), C.c_int, P(C.c_void_p)]),
         "mlc_create_pool": (C.c_int, [P(mlc_params), C.c_int, C.c_size_t, P(C.c_void_p)]),
         "mlc_pool_add": (C.c_int, [C.c_void_p, P(mlc_dims), P(C.c_int)]),

@@ -19,6 +19,8 @@
 // Operand order follows the reference expression by expression.  The ratios
 // dtrdz*fmz/fmzf of the vertical passes are per-domain constants read from
 // arrays computed once with the same expression.
+#include <type_traits>
+
 #include "mlc_kernels.cuh"
 
 namespace mlc {
@@ -50,21 +52,27 @@ template <> struct FlowEps<float> {
 // 2*den exactly, the value of b*den in each region of r, ties included.  No
 // division.  FP32 takes the branch-free clamp; FP64 tests the regions of r in
 // turn (0, 1/2, 1, 2), which usually stops early - on GB300 each FP64 min, max
-// or compare is an instruction of the 1/64-rate FP64 pipe.  Both give the same
-// B, and the flux equals the reference's to rounding.
+// or compare is an instruction of the 1/64-rate FP64 pipe - and keeps the
+// reference's guard of denominators below minden exactly.
 template <class T>
 __device__ __forceinline__ T waf_flux(T hvel, T is, T zamu, T a, T c, T num) {
   const T den = c - a;
-  const T d = fabs(den);
-  const T q = den < T(0) ? -num : num;
   T B;
-  if (d < FlowEps<T>::den()) {
-    B = fabs(num) < FlowEps<T>::num() ? den : T(0);  // r = 1 or r = 0
-  } else if constexpr (sizeof(T) == sizeof(float)) {
-    const T bd = fmax(T(0), fmin(d + d, fmax(q, fmin(q + q, d))));
-    B = den < T(0) ? -bd : bd;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    // FP32: the branch-free clamp, signs moved by bit operations; the guard
+    // of tiny denominators is left out - it changes B only where
+    // |den| < 1e-15, by less than 2|den|, far below FP32 rounding of the
+    // flux
+    const unsigned sg = __float_as_uint(den) & 0x80000000u;
+    const float q = __uint_as_float(__float_as_uint(num) ^ sg);
+    const float d = fabsf(den);
+    const float bd = fmaxf(0.f, fminf(d + d, fmaxf(q, fminf(q + q, d))));
+    B = __uint_as_float(__float_as_uint(bd) ^ sg);
   } else {
-    if (q <= T(0)) B = T(0);
+    const T d = fabs(den);
+    const T q = den < T(0) ? -num : num;
+    if (d < FlowEps<T>::den()) B = fabs(num) < FlowEps<T>::num() ? den : T(0);  // r = 1 or r = 0
+    else if (q <= T(0)) B = T(0);
     else if (q < T(0.5) * d) B = num + num;
     else if (q <= d) B = den;
     else if (q < T(2) * d) B = num;
@@ -171,95 +179,128 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
   }
 }
 
-// Two vertical WAF passes for the columns of one field (:858-922).  A block
-// holds blockDim.x consecutive columns (j) of one row i with their levels in
-// shared memory, laid out [level][column]; its blockDim.y thread rows share
-// the levels.  Within a pass every interface flux depends only on the pass
-// input and every cell update only on its two fluxes, so each pass is two
-// level-parallel phases.  R is the type of the winds and metric, T that of
-// the advected field and of the arithmetic.
+// Two vertical WAF passes (do_vadvtwice, :858-922), one thread per column
+// and field, streaming the levels upward through registers.  Pass 1's flux
+// at interface k+1 needs the input at levels k-1..k+2 and its update at k the
+// fluxes at k and k+1; pass 2 needs pass 1's output at m-1..m+2, so it runs
+// two levels behind pass 1 in the same loop.  Every value is loaded once and
+// the column never touches shared memory.  R is the type of the winds and
+// metric, T that of the advected field and of the arithmetic.  Fluxes and
+// updates are the reference's expressions, operand for operand.
+template <class T>
+__device__ __forceinline__ T vflux(T dtrdz, T skp, T cm1, T ck, T cp1, T cp2, int k, int kz) {
+  // interface k+1 between levels k and k+1; the upwind difference col(k1) -
+  // col(k1p1) with the reference's clamps k1p1 = min(k+2, kz), k1 = max(k-1, 1)
+  const T zamu = skp * dtrdz;
+  T is, num;
+  if (zamu >= T(0)) {
+    is = T(1);
+    num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
+  } else {
+    is = T(-1);
+    num = k >= 2 ? cm1 - ck : ck - ck;
+  }
+  return waf_flux<T>(T(0.5) * skp, is, zamu, cp1, ck, num);
+}
+template <class T>
+__device__ __forceinline__ T vupdate(T pk, T fb, T fa, T sk, T skp, T zu, T zd) {
+  const T zdv = (sk * zu - skp * zd) * pk;
+  return pk - fb * zu + fa * zd + zdv;
+}
+
+// grid: x = column tiles along j times the fields (field fastest, so the
+// blocks reading one column's s and metric run together), y = row tiles,
+// z = member; block (vert_x, vert_y) columns along (j, i)
 template <class R, class T>
 __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set, int advoff) {
-  extern __shared__ unsigned char smem_raw[];
-  T *smem = reinterpret_cast<T *>(smem_raw);
-  const int CX = blockDim.x, KT = blockDim.y;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  // grid: x = field x column tiles along j, y = row i, z = member
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
-  const int tiles_j = gridDim.x / nf;
-  const int f = blockIdx.x / tiles_j;
-  const int bj = blockIdx.x - f * tiles_j;
+  const int f = (int)(blockIdx.x % (unsigned)nf);
+  const int bj = (int)(blockIdx.x / (unsigned)nf);
   if (set == 0 && f >= n_table_r(D)) return;  // a member with fewer species
   const Geom g = D.g;
   const int kz = g.kz;
-  const int i = blockIdx.y + 1;
-  if (i > g.iy - 1 || bj * CX + 1 > g.jx - 1) return;
-  const int j = bj * CX + tx + 1;
-  const bool on = j <= g.jx - 1;
-  const size_t L = (size_t)(kz + 2) * CX;
-  T *col = smem;          // field, levels 1..kz
-  T *flx = smem + L;      // wfw, interfaces 1..kz+1
-  T *sc = smem + 2 * L;   // s, levels 1..kz+1
-  T *zu = smem + 3 * L;   // dtrdz*fmz/fmzf(k)
-  T *zd = smem + 4 * L;   // dtrdz*fmz/fmzf(k+1)
-#define A(a, k) a[(size_t)(k) * CX + tx]
+  const int j = bj * (int)blockDim.x + (int)threadIdx.x + 1;
+  const int i = (int)blockIdx.y * (int)blockDim.y + (int)threadIdx.y + 1;
+  if (j > g.jx - 1 || i > g.iy - 1) return;
   const Scal &c = D.c;
-  const Stat<R> &sa = D.sa;
-  const R *__restrict__ s = D.s;
   const int adv = (D.clk->adv_role + advoff) & 1;
   const T *src;
   T *outp, *dst;
   field_t<R, T>(D, set, f, adv, src, outp, dst);
   (void)outp;
-  const size_t ij = on ? g.at2(j, i) : 0, PS = g.PS;
+  const size_t ij = g.at2(j, i);
+  src += ij;
+  dst += ij;
+  const R *__restrict__ sp = D.s + ij;
+  const R *__restrict__ zup = D.sa.zrfmu + ij;
+  const R *__restrict__ zdp = D.sa.zrfmd + ij;
+  const unsigned PS = (unsigned)g.PS;  // a domain's fields stay below 2^31 elements
   const T dtrdz = T(0.5) * (pick<T>(c.dtstepa, c.dtstepaf) * pick<T>(c.rdzita, c.rdzitaf));
 
-  if (on)
-    for (int k = 1 + ty; k <= kz + 1; k += KT) {
-      const size_t o = ij + (size_t)(k - 1) * PS;
-      A(sc, k) = T(s[o]);
-      if (k <= kz) {
-        A(col, k) = src[o];
-        A(zu, k) = T(sa.zrfmu[o]);
-        A(zd, k) = T(sa.zrfmd[o]);
-      }
+  // windows: pass-1 input at k-1..k+2, pass-1 output at k-3..k-1, s at
+  // k-2..k+1, metric at k-2..k-1, the pass-1 flux at interface k and the
+  // pass-2 flux at interface k-2
+  T c0m1 = T(0), c0k = src[0], c0p1 = src[PS];
+  T c1m3 = T(0), c1m2 = T(0), c1m1 = T(0);
+  T sm2 = T(0), sm1 = T(0), sk = T(sp[0]);
+  T zum2 = T(0), zdm2 = T(0), zum1 = T(0), zdm1 = T(0);
+  T f1k = T(0), f2m = T(0);
+  // the next level's loads, issued one level ahead
+  T n_s = T(sp[PS]), n_c = src[2 * PS], n_zu = T(zup[0]), n_zd = T(zdp[0]);
+  // level k; every bound check is known to hold inside the column
+  // (4 <= k <= kz-3), so the interior steps carry none
+  auto step = [&](int k, auto interior) {
+    constexpr bool I = decltype(interior)::value;
+    const unsigned o = (unsigned)(k - 1) * PS;
+    const T skp1 = n_s, c0p2 = (I || k + 2 <= kz) ? n_c : T(0), zuk = n_zu, zdk = n_zd;
+    if (I || k < kz) {
+      n_s = T(sp[o + 2 * PS]);
+      n_zu = T(zup[o + PS]);
+      n_zd = T(zdp[o + PS]);
+      if (I || k + 3 <= kz) n_c = src[o + 3 * PS];
     }
-  if (ty == 0) {
-    A(flx, 1) = T(0);
-    A(flx, kz + 1) = T(0);
-  }
-  __syncthreads();
-  for (int pass = 0; pass < 2; ++pass) {
-    if (on)
-      for (int k = 1 + ty; k <= kz - 1; k += KT) {
-        const T skp = A(sc, k + 1);
-        const T zamu = skp * dtrdz;
-        T is;
-        int k1, k1p1;
-        if (zamu >= T(0)) {
-          is = T(1); k1 = k + 1; k1p1 = k1 + 1;
-          if (k1p1 > kz) k1p1 = kz;
-        } else {
-          is = T(-1); k1 = k - 1; k1p1 = k;
-          if (k1 < 1) k1 = 1;
-        }
-        A(flx, k + 1) = waf_flux<T>(T(0.5) * skp, is, zamu, A(col, k + 1), A(col, k),
-                                    A(col, k1) - A(col, k1p1));
+    T f1kp;
+    if (I) {
+      const T zamu = skp1 * dtrdz;
+      const bool up = zamu >= T(0);
+      f1kp = waf_flux<T>(T(0.5) * skp1, up ? T(1) : T(-1), zamu, c0p1, c0k,
+                         up ? c0p1 - c0p2 : c0m1 - c0k);
+    } else {
+      f1kp = k <= kz - 1 ? vflux<T>(dtrdz, skp1, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
+    }
+    const T c1k = vupdate<T>(c0k, f1k, f1kp, sk, skp1, zuk, zdk);
+    if (I || k >= 3) {  // pass 2 at level m = k-2
+      T f2n;
+      if (I) {
+        const T zamu = sm1 * dtrdz;
+        const bool up = zamu >= T(0);
+        f2n = waf_flux<T>(T(0.5) * sm1, up ? T(1) : T(-1), zamu, c1m1, c1m2,
+                          up ? c1m1 - c1k : c1m3 - c1m2);
+      } else {
+        f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1k, k - 2, kz);
       }
-    __syncthreads();
-    if (on)
-      for (int k = 1 + ty; k <= kz; k += KT) {
-        const T zrfmu = A(zu, k), zrfmd = A(zd, k);
-        const T pk = A(col, k);
-        const T zdv = (A(sc, k) * zrfmu - A(sc, k + 1) * zrfmd) * pk;
-        A(col, k) = pk - A(flx, k) * zrfmu + A(flx, k + 1) * zrfmd + zdv;
-      }
-    __syncthreads();
-  }
-  if (on)
-    for (int k = 1 + ty; k <= kz; k += KT) dst[ij + (size_t)(k - 1) * PS] = A(col, k);
-#undef A
+      dst[o - 2 * PS] = vupdate<T>(c1m2, f2m, f2n, sm2, sm1, zum2, zdm2);
+      f2m = f2n;
+    }
+    c0m1 = c0k; c0k = c0p1; c0p1 = c0p2;
+    c1m3 = c1m2; c1m2 = c1m1; c1m1 = c1k;
+    sm2 = sm1; sm1 = sk; sk = skp1;
+    zum2 = zum1; zdm2 = zdm1; zum1 = zuk; zdm1 = zdk;
+    f1k = f1kp;
+  };
+  using edge = std::integral_constant<bool, false>;
+  using mid = std::integral_constant<bool, true>;
+  const int k1 = min(3, kz), k2 = max(4, kz - 2);
+  for (int k = 1; k <= k1; ++k) step(k, edge{});
+#pragma unroll 4
+  for (int k = 4; k < k2; ++k) step(k, mid{});
+  for (int k = k2; k <= kz; ++k) step(k, edge{});
+  // pass 2 at levels kz-1 (flux through interface kz) and kz (none above)
+  const unsigned ot = (unsigned)(kz - 1) * PS;
+  const T f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
+  dst[ot - PS] = vupdate<T>(c1m2, f2m, f2n, sm2, sm1, zum2, zdm2);
+  dst[ot] = vupdate<T>(c1m1, f2n, T(0), sm1, sk, zum1, zdm1);
 }
 
 // ---- TMA tile loads and mbarriers (inline PTX, sm_90+) ----------------------
@@ -306,76 +347,140 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
   return false;
 }
 
-template <int TJ, int TI>
-constexpr int tile_shape_index() {
-  return (TJ == 32 && TI == 8) ? 0 : (TJ == 32 && TI == 4) ? 1 : (TJ == 64 && TI == 4) ? 2 : 3;
+// ---- lane vectors ---------------------------------------------------------
+template <int B> struct VecOf;
+template <> struct VecOf<4> { using t = unsigned; };
+template <> struct VecOf<8> { using t = uint2; };
+template <> struct VecOf<16> { using t = uint4; };
+
+// v consecutive elements at p, which is aligned to min(v * sizeof(T), 16)
+template <class T, int V>
+__device__ __forceinline__ void ld_vec(T (&x)[V], const T *p) {
+  constexpr int B = V * (int)sizeof(T);
+  if constexpr (B <= 16) {
+    const typename VecOf<B>::t w = *reinterpret_cast<const typename VecOf<B>::t *>(p);
+    memcpy(x, &w, B);
+  } else {
+#pragma unroll
+    for (int h = 0; h < B / 16; ++h) {
+      const uint4 w = reinterpret_cast<const uint4 *>(p)[h];
+      memcpy(reinterpret_cast<char *>(x) + 16 * h, &w, 16);
+    }
+  }
+}
+template <class T, int V>
+__device__ __forceinline__ void st_vec(T *p, const T (&x)[V]) {
+  constexpr int B = V * (int)sizeof(T);
+  if constexpr (B <= 16) {
+    typename VecOf<B>::t w;
+    memcpy(&w, x, B);
+    *reinterpret_cast<typename VecOf<B>::t *>(p) = w;
+  } else {
+#pragma unroll
+    for (int h = 0; h < B / 16; ++h) {
+      uint4 w;
+      memcpy(&w, reinterpret_cast<const char *>(x) + 16 * h, 16);
+      reinterpret_cast<uint4 *>(p)[h] = w;
+    }
+  }
+}
+// the lane's v elements of row r (1-based) of a plane, or zeros
+template <class T, int V>
+__device__ __forceinline__ void ld_row(T (&x)[V], const T *plane, int e0, int r, unsigned P, bool ok) {
+  if (ok) {
+    ld_vec<T, V>(x, plane + (unsigned)e0 + (unsigned)(r - 1) * P);
+  } else {
+#pragma unroll
+    for (int q = 0; q < V; ++q) x[q] = T(0);
+  }
+}
+// element q+1 of the lane's columns: the lane's own, or the next lane's first
+template <class T, int V>
+__device__ __forceinline__ void next_col(T (&e)[V], const T (&x)[V]) {
+#pragma unroll
+  for (int q = 0; q + 1 < V; ++q) e[q] = x[q + 1];
+  e[V - 1] = __shfl_down_sync(0xffffffffu, x[0], 1);
 }
 
-// Meridional then zonal WAF for one tile at one level, every field of the R
-// table (:984-1038; ROTLLR :926-983).  The winds, Courant numbers and metric
-// coefficients of the tile are formed once, in shared memory, and then each
-// field in turn is staged with a 2-point halo, its meridional fluxes and the
-// intermediate p0 are built on a 2-column halo, then its zonal fluxes and
-// the result, so each field is read and written once.  The result goes to
-// the field's other buffer because the halo columns of a tile still need its
-// old values.  Per field the expressions are the reference's, operand for
-// operand; only the field-independent factors are computed once.
-template <class R, int kTJ, int kTI>
-__global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__restrict__ doms,
-                                                            int tiles_j, int uvoff, int advoff) {
+// Meridional then zonal WAF at one level for a tile of nw rows, every field
+// of the R table (:984-1038; ROTLLR :926-983).  Warp w owns row I0+w; lane l
+// owns v consecutive columns of it.  The winds, Courant numbers and metric
+// coefficients of the lane's points are formed once, in registers, and then
+// for each field in turn: its halo tile (rows I0-2 .. I0+nw+1, landed by TMA,
+// double-buffered) gives the meridional fluxes of the warp's row, shared
+// with the row above through shared memory (the last warp also forms the
+// flux of row I0+nw); the intermediate p0 follows; the zonal fluxes take
+// their neighbours' p0 from the adjacent lanes by shuffles, and the result
+// goes to the field's other buffer (the halo of other tiles still needs the
+// old values).  A warp's range is 32*v columns, of which it writes the
+// middle 32*v - 4 (a column's zonal update needs p0 two columns either
+// side); tiles overlap by four columns.  Per field the expressions are the
+// reference's, operand for operand.
+template <class R, int V, int NW>
+__global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__restrict__ doms,
+                                                           int tiles_j, int uvoff, int advoff) {
   using T = R;
-  constexpr int WJ = kTJ + 4;            // columns J0-2 .. J0+TJ+1
-  // halo tiles of two fields (TMA destinations, double-buffered): rows
-  // I0-2 .. I0+TI+1; column J0-2+cc of the kernel sits at cc + OFF, the copy
-  // starting OFF columns further left so that it starts on 16 bytes
-  constexpr int OFF = sizeof(T) == sizeof(float) ? 2 : 0;
-  constexpr int BW = WJ + 2 * OFF;
-  constexpr unsigned kBox = (unsigned)((kTI + 4) * BW * sizeof(T));
-  __shared__ __align__(128) T wzt[2][kTI + 4][BW];
+  constexpr int W = 32 * V;       // columns of a warp's range
+  constexpr int S = W - 4;        // columns it writes: range columns 2 .. W-3
+  constexpr int OB0 = hshape_ob0(V);
+  constexpr int OFF = hshape_off((int)sizeof(T), V);
+  constexpr int BW = W + 2 * OFF;  // halo tile row: range column c sits at c + OFF
+  constexpr unsigned kBox = (unsigned)((NW + 4) * BW * sizeof(T));
+  constexpr unsigned kBuf = (kBox + 127u) / 128u * 128u;
+  constexpr int shape = (sizeof(T) == 4) ? (V == 1 ? 0 : V == 2 ? 1 : NW == 8 ? 2 : 3)
+                                         : (V == 1 ? (NW == 8 ? 0 : 3) : (NW == 8 ? 1 : 2));
+  static_assert(hshape((int)sizeof(T), shape).v == V && hshape((int)sizeof(T), shape).nw == NW,
+                "tile shape table");
+  __shared__ __align__(128) unsigned char wzraw[2][kBuf];  // TMA destinations
+  __shared__ __align__(16) T zp_s[2][NW + 1][W];           // meridional fluxes, rows I0 .. I0+NW
   __shared__ __align__(8) uint64_t mbar[2];
-  __shared__ T zpby_s[kTI + 1][WJ];      // rows I0 .. I0+TI
-  __shared__ T p0_s[kTI][WJ];            // rows I0 .. I0+TI-1
-  __shared__ T zpbw_s[kTI][kTJ + 1];     // columns J0 .. J0+TJ
-  // field-independent factors of the tile
-  __shared__ T vy_s[kTI + 1][WJ], zmy_s[kTI + 1][WJ];   // v, Courant number at rows I0..I0+TI
-  __shared__ T zs_s[kTI][WJ], zn_s[kTI][WJ], dvy_s[kTI][WJ], m2_s[kTI][WJ];
-  __shared__ T ux_s[kTI][kTJ + 1], zmx_s[kTI][kTJ + 1];  // u, Courant number at columns J0..J0+TJ
-  __shared__ T zw_s[kTI][kTJ], ze_s[kTI][kTJ], dvx_s[kTI][kTJ];
+  __shared__ const T *cur_s[kMaxFields];                   // each field's current and other half
+  __shared__ T *out_s[kMaxFields];
   // grid: x = tiles along j and i, y = level, z = member
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const int k = blockIdx.y + 1;
-  const int bj = blockIdx.x % tiles_j, bi = blockIdx.x / tiles_j;
   const Geom g = D.g;
+  const int jx = g.jx, iy = g.iy;
+  if (k > g.kz) return;
+  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int ob = bj * S + OB0;  // column offset (j - 1) of the range's first column
+  const int I0 = bi * NW + 1;
+  if (ob + 3 > jx - 1 || I0 > iy - 1) return;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
-  const int jx = g.jx, iy = g.iy, kz = g.kz;
-  if (k > kz) return;
-  const int J0 = bj * kTJ + 1, I0 = bi * kTI + 1;
-  if (J0 > jx - 1 || I0 > iy - 1) return;
   const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
-  const int tid = threadIdx.y * kTJ + threadIdx.x;
-  const int nth = kTJ * kTI;
-  const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
-  const R *__restrict__ uk = D.u[uv] + ko;
-  const R *__restrict__ vk = D.v[uv] + ko;
+  const int lane = (int)(threadIdx.x & 31u), wp = (int)(threadIdx.x >> 5);
+  const int tid = (int)threadIdx.x;
+  const int i = I0 + wp;
+  const int e0 = ob + V * lane;                  // column offset of the lane's first column
+  const bool inrow = e0 >= 0 && e0 + V <= g.P;   // the lane's columns lie inside a row
+  const unsigned P = (unsigned)g.P;
+  const unsigned ko = (unsigned)(k - 1) * (unsigned)g.PS;  // a field stays below 2^31 elements
+  const T *__restrict__ uk = D.u[uv] + ko;
+  const T *__restrict__ vk = D.v[uv] + ko;
   const T dta = pick<T>(c.dtstepa, c.dtstepaf);
   const T dtrdx = dta * pick<T>(c.rdx, c.rdxf), dtrdy = dta * pick<T>(c.rdx, c.rdxf);
   const bool rot = c.lrotllr != 0;
-  const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
   const int nf = n_table_r(D);
-  const char *tmaps = static_cast<const char *>(D.tmap) +
-                      (size_t)tile_shape_index<kTJ, kTI>() * kMaxFields * kTmapBytes;
+  const char *tmaps = static_cast<const char *>(D.tmap) + (size_t)shape * kMaxFields * kTmapBytes;
+  auto tile = [&](int b) { return reinterpret_cast<T(*)[BW]>(wzraw[b]); };
   auto issue = [&](int fld, int b) {  // one thread: the halo tile of field fld into buffer b
     fence_proxy_async();
     mbar_expect_tx(&mbar[b], kBox);
-    tma_load_3d(&wzt[b][0][0], tmaps + (size_t)fld * kTmapBytes, J0 - 3 - OFF, I0 - 3, k - 1,
-                &mbar[b]);
+    tma_load_3d(wzraw[b], tmaps + (size_t)fld * kTmapBytes, ob - OFF, I0 - 3, k - 1, &mbar[b]);
   };
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     fence_mbar_init();
+  }
+  if (tid < nf) {
+    const T *cur0;
+    T *out0, *wz0;
+    field_t<R, T>(D, 0, tid, adv, cur0, out0, wz0);
+    cur_s[tid] = cur0 + ko;
+    out_s[tid] = out0 + ko;
   }
   __syncthreads();
   if (tid == 0) {
@@ -383,87 +488,166 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
     if (nf > 1) issue(1, 1);
   }
 
-  // ---- field-independent factors (while the first tiles land) ----
-  for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
-    const int rr = e / WJ, cc = e % WJ;
-    const int i = I0 + rr, j = J0 - 2 + cc;
-    T vv = T(0), zamu = T(0);
-    if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 1) {
-      const size_t ij = g.at2(j, i);
-      vv = T(vk[ij]);
-      zamu = rot ? vv * dtrdy : vv * T(sa.msfv[ij]) * dtrdy;
+  // ---- the lane's coefficients (while the first tiles land) ----
+  int jq[V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) jq[q] = e0 + q + 1;
+  const bool rowM = i >= 2 && i <= iy - 1;  // meridional flux rows
+  const bool rowP = i >= 2 && i <= iy - 2;  // p0, zonal flux and update rows
+  const bool okM = inrow && rowM, okP = inrow && rowP;
+  T vv[V], zmy[V], vve[V], zmye[V];
+  bool mv[V], me[V];  // meridional flux defined at the column (row i, row I0+NW)
+  {
+    T a[V], b[V];
+    ld_row<T, V>(a, vk, e0, i, P, okM);
+    ld_row<T, V>(b, sa.msfv, e0, i, P, okM && !rot);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const bool ok = okM && jq[q] >= 1 && jq[q] <= jx - 1;
+      mv[q] = ok;
+      vv[q] = ok ? a[q] : T(0);
+      zmy[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
     }
-    vy_s[rr][cc] = vv;
-    zmy_s[rr][cc] = zamu;
+    // the last warp also forms the fluxes of row I0+NW
+    const int ie = I0 + NW;
+    const bool okE = wp == NW - 1 && inrow && ie >= 2 && ie <= iy - 1;
+    ld_row<T, V>(a, vk, e0, ie, P, okE);
+    ld_row<T, V>(b, sa.msfv, e0, ie, P, okE && !rot);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const bool ok = okE && jq[q] >= 1 && jq[q] <= jx - 1;
+      me[q] = ok;
+      vve[q] = ok ? a[q] : T(0);
+      zmye[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
+    }
   }
-  for (int e = tid; e < kTI * WJ; e += nth) {
-    const int rr = e / WJ, cc = e % WJ;
-    const int i = I0 + rr, j = J0 - 2 + cc;
-    T zs = T(0), zn = T(0), dv = T(0), m2 = T(1);
-    if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
-      const size_t ij = g.at2(j, i), ijN = ij + (size_t)g.P;
-      const T fz = T(sa.fmz[ko + ij]);
+  T zs[V], zn[V], dvy[V], m2[V], uu[V], zmx[V], zw[V], ze[V], dvx[V];
+  bool pv[V], xv[V], rv[V];  // p0, zonal flux, interior update defined at the column
+  {
+    T fz[V], vi[V], vn[V], ri[V], rn[V], fi[V], fn[V], mf[V], ui[V], rmui[V], msu[V];
+    ld_row<T, V>(fz, sa.fmz + ko, e0, i, P, okP);
+    ld_row<T, V>(vi, vk, e0, i, P, okP);
+    ld_row<T, V>(vn, vk, e0, i + 1, P, okP);
+    ld_row<T, V>(ri, sa.rmv, e0, i, P, okP);
+    ld_row<T, V>(rn, sa.rmv, e0, i + 1, P, okP);
+    ld_row<T, V>(fi, (rot ? sa.rfmzv : sa.rfmzu) + ko, e0, i, P, okP);
+    ld_row<T, V>(fn, (rot ? sa.rfmzv : sa.rfmzu) + ko, e0, i + 1, P, okP);
+    ld_row<T, V>(mf, rot ? sa.msfx : sa.mx2, e0, i, P, okP);
+    ld_row<T, V>(ui, uk, e0, i, P, okP);
+    ld_row<T, V>(rmui, sa.rmu, e0, i, P, okP && !rot);
+    ld_row<T, V>(msu, sa.msfu, e0, i, P, okP);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const int j = jq[q];
+      pv[q] = okP && j >= 1 && j <= jx - 1;
+      xv[q] = okP && j >= 2 && j <= jx - 1;
+      rv[q] = okP && j >= 2 && j <= jx - 2;
       if (rot) {
-        const T zhxvtn = dtrdy * T(sa.rmv[ijN]) * T(sa.msfx[ij]);
-        const T zhxvts = dtrdy * T(sa.rmv[ij]) * T(sa.msfx[ij]);
-        zn = zhxvtn * fz * T(sa.rfmzv[ko + ijN]);
-        zs = zhxvts * fz * T(sa.rfmzv[ko + ij]);
-        dv = T(vk[ijN]) * zn - T(vk[ij]) * zs;
+        const T zhxvtn = dtrdy * rn[q] * mf[q];
+        const T zhxvts = dtrdy * ri[q] * mf[q];
+        zn[q] = zhxvtn * fz[q] * fn[q];
+        zs[q] = zhxvts * fz[q] * fi[q];
+        dvy[q] = vn[q] * zn[q] - vi[q] * zs[q];
+        m2[q] = T(1);
       } else {
         // rfmzu as in the reference (Main/mod_moloch.F90:1000-1001)
-        zn = dtrdy * fz * T(sa.rfmzu[ko + ijN]);
-        zs = dtrdy * fz * T(sa.rfmzu[ko + ij]);
-        dv = T(vk[ijN]) * T(sa.rmv[ijN]) * zn - T(vk[ij]) * T(sa.rmv[ij]) * zs;
-        m2 = T(sa.mx2[ij]);
+        zn[q] = dtrdy * fz[q] * fn[q];
+        zs[q] = dtrdy * fz[q] * fi[q];
+        dvy[q] = vn[q] * rn[q] * zn[q] - vi[q] * ri[q] * zs[q];
+        m2[q] = mf[q];
       }
+      uu[q] = xv[q] ? ui[q] : T(0);
+      zmx[q] = xv[q] ? ui[q] * msu[q] * dtrdx : T(0);
     }
-    zs_s[rr][cc] = zs; zn_s[rr][cc] = zn; dvy_s[rr][cc] = dv; m2_s[rr][cc] = m2;
-  }
-  for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
-    const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
-    const int i = I0 + rr, j = J0 + cc;
-    T uu = T(0), zamu = T(0);
-    if (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
-      const size_t ij = g.at2(j, i);
-      uu = T(uk[ij]);
-      zamu = uu * T(sa.msfu[ij]) * dtrdx;
-    }
-    ux_s[rr][cc] = uu;
-    zmx_s[rr][cc] = zamu;
-  }
-  {
-    const int rr = threadIdx.y, cc = threadIdx.x;
-    const int i = I0 + rr, j = J0 + cc;
-    T zw = T(0), ze = T(0), dv = T(0);
-    if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
-      const size_t ij = g.at2(j, i);
-      const T fz = T(sa.fmz[ko + ij]);
+    // the zonal update also needs u, rfmzu and rmu one column east
+    T fzu[V], fze[V], ue[V], rme[V];
+    ld_row<T, V>(fzu, sa.rfmzu + ko, e0, i, P, okP);
+    next_col<T, V>(fze, fzu);
+    next_col<T, V>(ue, ui);
+    next_col<T, V>(rme, rmui);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
       if (rot) {
-        const T zcostx = dtrdx * T(sa.msfx[ij]);
-        zw = zcostx * fz * T(sa.rfmzu[ko + ij]);
-        ze = zcostx * fz * T(sa.rfmzu[ko + ij + 1]);
-        dv = T(uk[ij + 1]) * ze - T(uk[ij]) * zw;
+        const T zcostx = dtrdx * mf[q];
+        zw[q] = zcostx * fz[q] * fzu[q];
+        ze[q] = zcostx * fz[q] * fze[q];
+        dvx[q] = ue[q] * ze[q] - ui[q] * zw[q];
       } else {
-        zw = dtrdx * fz * T(sa.rfmzu[ko + ij]);
-        ze = dtrdx * fz * T(sa.rfmzu[ko + ij + 1]);
-        dv = T(uk[ij + 1]) * T(sa.rmu[ij + 1]) * ze - T(uk[ij]) * T(sa.rmu[ij]) * zw;
+        zw[q] = dtrdx * fz[q] * fzu[q];
+        ze[q] = dtrdx * fz[q] * fze[q];
+        dvx[q] = ue[q] * rme[q] * ze[q] - ui[q] * rmui[q] * zw[q];
       }
     }
-    zw_s[rr][cc] = zw; ze_s[rr][cc] = ze; dvx_s[rr][cc] = dv;
   }
+  // rows of the halo tile (global row r at tile row r - I0 + 2) the upwind
+  // differences use, with the reference's clamps ih = min(i+1, imax),
+  // ihm1 = max(ih-1, imin)
+  auto mrows = [&](int r, int &ta, int &tb, int &tc) {
+    ta = max(r - 2, 1) - I0 + 2;
+    const int rb = min(r + 1, iy - 1);
+    tb = rb - I0 + 2;
+    tc = max(rb - 1, 1) - I0 + 2;
+  };
+  int tA, tB, tC, eA, eB, eC;
+  mrows(i, tA, tB, tC);
+  mrows(I0 + NW, eA, eB, eC);
+  // columns the lane may write: range columns 2 .. W-3 inside the domain
+  bool wv[V];
+  bool wall = true;
+#pragma unroll
+  for (int q = 0; q < V; ++q) {
+    const int cc = V * lane + q;
+    wv[q] = inrow && i <= iy - 1 && cc >= 2 && cc <= W - 3 && jq[q] >= 1 && jq[q] <= jx - 1;
+    wall = wall && wv[q];
+  }
+  const bool rowin = inrow && i <= iy - 1;
 
   for (int f = 0; f < nf; ++f) {
-    const T *cur0;
-    T *out0, *wz0;
-    field_t<R, T>(D, 0, f, adv, cur0, out0, wz0);
-    const T *pp = cur0 + ko;
-    const T *wz = wz0 + ko;
-    T *out = out0 + ko;
-    (void)wz;
-    // the field's halo tile (zero outside the cross points)
+    const T *pp = cur_s[f];
+    T *out = out_s[f];
+    // the field's old values at the lane's points, in flight during the
+    // meridional pass
+    T ppk[V];
+    ld_row<T, V>(ppk, pp, e0, i, P, rowin);
     const int b = f & 1;
     const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((f >> 1) & 1));
-    if (__syncthreads_or(!landed)) {  // also orders the factors above before their use
+    T(*wt)[BW] = tile(b);
+    T(*zp)[W] = zp_s[b];
+    // meridional fluxes zpby(j,i): j in jce, i in ici1..ice2
+    T wzi[V];
+    {
+      T wa[V], wA[V], wB[V], wC[V], x[V];
+      ld_vec<T, V>(wa, &wt[i - I0 + 1][OFF + V * lane]);
+      ld_vec<T, V>(wzi, &wt[i - I0 + 2][OFF + V * lane]);
+      ld_vec<T, V>(wA, &wt[tA][OFF + V * lane]);
+      ld_vec<T, V>(wB, &wt[tB][OFF + V * lane]);
+      ld_vec<T, V>(wC, &wt[tC][OFF + V * lane]);
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        const bool up = zmy[q] > T(0);
+        const T y = waf_flux<T>(T(0.5) * vv[q], up ? T(1) : T(-1), zmy[q], wa[q], wzi[q],
+                                up ? wa[q] - wA[q] : wB[q] - wC[q]);
+        x[q] = mv[q] ? y : T(0);  // zero outside the flux points
+      }
+      st_vec<T, V>(&zp[wp][V * lane], x);
+      if (wp == NW - 1) {
+        T xa[V], xc[V];
+        ld_vec<T, V>(xa, &wt[NW + 1][OFF + V * lane]);
+        ld_vec<T, V>(xc, &wt[NW + 2][OFF + V * lane]);
+        ld_vec<T, V>(wA, &wt[eA][OFF + V * lane]);
+        ld_vec<T, V>(wB, &wt[eB][OFF + V * lane]);
+        ld_vec<T, V>(wC, &wt[eC][OFF + V * lane]);
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          const bool up = zmye[q] > T(0);
+          const T y = waf_flux<T>(T(0.5) * vve[q], up ? T(1) : T(-1), zmye[q], xa[q], xc[q],
+                                  up ? xa[q] - wA[q] : wB[q] - wC[q]);
+          x[q] = me[q] ? y : T(0);
+        }
+        st_vec<T, V>(&zp[NW][V * lane], x);
+      }
+    }
+    if (__syncthreads_or(!landed)) {
       if (tid == 0) {
         atomicOr(&D.clk->fault, 1);
         // let copies still in flight land before the shared memory is released
@@ -472,82 +656,62 @@ __global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal(const Dom<R> *__res
       }
       return;
     }
-    T (*wz_s)[BW] = wzt[b];
-    // meridional fluxes zpby(j,i): j in jce, i in ici1..ice2
-    for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
-      const int rr = e / WJ, cc = e % WJ;
-      const int i = I0 + rr, j = J0 - 2 + cc;
-      T x = T(0);
-      if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 1) {
-        const T vv = vy_s[rr][cc];
-        const T zamu = zmy_s[rr][cc];
-        T is;
-        int ih;
-        if (zamu > T(0)) { is = T(1); ih = i - 1; }
-        else { is = T(-1); ih = min(i + 1, imax); }
-        const int ihm1 = max(ih - 1, imin);
-        const int bo = 2 - I0;  // shared-memory row of global row i is i + bo
-        x = waf_flux<T>(T(0.5) * vv, is, zamu, wz_s[i - 1 + bo][cc + OFF], wz_s[i + bo][cc + OFF],
-                        wz_s[ih + bo][cc + OFF] - wz_s[ihm1 + bo][cc + OFF]);
-      }
-      zpby_s[rr][cc] = x;
-    }
-    __syncthreads();
-    // p0(j,i): j in jce, i in ici
-    for (int e = tid; e < kTI * WJ; e += nth) {
-      const int rr = e / WJ, cc = e % WJ;
-      const int i = I0 + rr, j = J0 - 2 + cc;
-      T x = T(0);
-      if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
-        const T ppk = pp[g.at2(j, i)];
-        const T wzk = wz_s[rr + 2][cc + OFF];
-        const T zdv = dvy_s[rr][cc] * ppk;
-        const T zrfms = zs_s[rr][cc], zrfmn = zn_s[rr][cc];
-        if (rot) x = wzk + (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
-        else x = wzk + m2_s[rr][cc] * (zpby_s[rr][cc] * zrfms - zpby_s[rr + 1][cc] * zrfmn + zdv);
-      }
-      p0_s[rr][cc] = x;
-    }
-    __syncthreads();
     // buffer b is read for the last time above: fetch the field after next
     if (tid == 0 && f + 2 < nf) issue(f + 2, b);
-    // zonal fluxes zpbw(j,i): j in jci1..jce2, i in ici
-    for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
-      const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
-      const int i = I0 + rr, j = J0 + cc;
-      T x = T(0);
-      if (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
-        const T uu = ux_s[rr][cc];
-        const T zamu = zmx_s[rr][cc];
-        T is;
-        int jh;
-        if (zamu > T(0)) { is = T(1); jh = j - 1; }
-        else { is = T(-1); jh = min(j + 1, jmax); }
-        const int jhm1 = max(jh - 1, jmin);
-        const int bo = 2 - J0;  // p0_s column of global column j is j + bo
-        x = waf_flux<T>(T(0.5) * uu, is, zamu, p0_s[rr][j - 1 + bo], p0_s[rr][j + bo],
-                        p0_s[rr][jh + bo] - p0_s[rr][jhm1 + bo]);
-      }
-      zpbw_s[rr][cc] = x;
-    }
-    __syncthreads();
-    // result on the tile: interior update, ring copied
+    // p0(j,i): j in jce, i in ici
+    T p0[V];
     {
-      const int rr = threadIdx.y, cc = threadIdx.x;
-      const int i = I0 + rr, j = J0 + cc;
-      if (i <= iy - 1 && j <= jx - 1) {
-        const size_t ij = g.at2(j, i);
-        const T ppk = pp[ij];
-        T x = ppk;
-        if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
-          const T p0k = p0_s[rr][cc + 2];
-          const T zrfmw = zw_s[rr][cc], zrfme = ze_s[rr][cc];
-          const T zdv = dvx_s[rr][cc] * ppk;
-          if (rot) x = p0k + zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv;
-          else x = p0k + m2_s[rr][cc + 2] * (zpbw_s[rr][cc] * zrfmw - zpbw_s[rr][cc + 1] * zrfme + zdv);
-        }
-        out[ij] = x;
+      T ys[V], yn[V];
+      ld_vec<T, V>(ys, &zp[wp][V * lane]);
+      ld_vec<T, V>(yn, &zp[wp + 1][V * lane]);
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        const T zdv = dvy[q] * ppk[q];
+        T x;
+        if (rot) x = wzi[q] + (ys[q] * zs[q] - yn[q] * zn[q] + zdv);
+        else x = wzi[q] + m2[q] * (ys[q] * zs[q] - yn[q] * zn[q] + zdv);
+        p0[q] = pv[q] ? x : T(0);
       }
+    }
+    // zonal fluxes zpbw(j,i): j in jci1..jce2, i in ici; p0 at range
+    // columns c-2 .. c+1 (the lane's own, two from the lane to the west, one
+    // from the lane to the east)
+    T pw2, pw1, pe1;
+    pw2 = __shfl_up_sync(0xffffffffu, V >= 2 ? p0[V >= 2 ? V - 2 : 0] : p0[0], V >= 2 ? 1 : 2);
+    pw1 = __shfl_up_sync(0xffffffffu, p0[V - 1], 1);
+    pe1 = __shfl_down_sync(0xffffffffu, p0[0], 1);
+    auto p0at = [&](int q) -> T {  // p0 of lane column q, q in -2 .. V
+      return q == -2 ? pw2 : q == -1 ? pw1 : q == V ? pe1 : p0[q < 0 ? 0 : q >= V ? V - 1 : q];
+    };
+    T zx[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const int j = jq[q];
+      const bool up = zmx[q] > T(0);
+      const T a = p0at(q - 1), cq = p0at(q);
+      // jhm1 = max(j-2, jmin) upwind; jh = min(j+1, jmax) downwind
+      const T num = up ? a - (j == 2 ? a : p0at(q - 2)) : (j == jx - 1 ? cq - a : p0at(q + 1) - cq);
+      const T x = waf_flux<T>(T(0.5) * uu[q], up ? T(1) : T(-1), zmx[q], a, cq, num);
+      zx[q] = xv[q] ? x : T(0);
+    }
+    T zxe[V];
+    next_col<T, V>(zxe, zx);
+    // result: interior update, ring copied
+    T res[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const T zdv = dvx[q] * ppk[q];
+      T x;
+      if (rot) x = p0[q] + zx[q] * zw[q] - zxe[q] * ze[q] + zdv;
+      else x = p0[q] + m2[q] * (zx[q] * zw[q] - zxe[q] * ze[q] + zdv);
+      res[q] = rv[q] ? x : ppk[q];
+    }
+    if (wall) {
+      st_vec<T, V>(out + (unsigned)e0 + (unsigned)(i - 1) * P, res);
+    } else if (rowin) {
+#pragma unroll
+      for (int q = 0; q < V; ++q)
+        if (wv[q]) out[(unsigned)(e0 + q) + (unsigned)(i - 1) * P] = res[q];
     }
   }
 }
@@ -674,288 +838,431 @@ __global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advof
 // per interface, relative to the cell below (south, west) of it, and moved to
 // the other cell's reference by -2*hvel*(its value - the first cell's).
 
-// Both vertical passes (Main/mod_moloch.F90:858-922).  Writes the increment
-// dz = (field after the passes) - field, in FP64.
-template <class R>
-__global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff) {
-  extern __shared__ float vsm[];
-  const int CX = blockDim.x, KT = blockDim.y;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const Dom<R> &D = doms[blockIdx.z];
-  if (!D.active) return;
-  const int tiles_j = gridDim.x / 2;
-  const int f = blockIdx.x / tiles_j;
-  const int bj = blockIdx.x - f * tiles_j;
-  const Geom g = D.g;
-  const int kz = g.kz;
-  const int i = blockIdx.y + 1;
-  if (i > g.iy - 1 || bj * CX + 1 > g.jx - 1) return;
-  const int j = bj * CX + tx + 1;
-  const bool on = j <= g.jx - 1;
-  const Scal &c = D.c;
-  const Stat<R> &sa = D.sa;
-  const int adv = (D.clk->adv_role + advoff) & 1;
-  const size_t F = g.field3();
-  const DF src(f == 0 ? D.tetav[adv] : D.pai[adv], F);
-  const DF dst(D.wz_d[f], F);
-  const R *__restrict__ s = D.s;
-  const size_t L = (size_t)(kz + 2) * CX;
-  float *dzs = vsm;           // v(k+1) - v(k), k = 1..kz-1
-  float *e = vsm + L;         // increment of the pass input, k = 1..kz
-  float *flo = vsm + 2 * L;   // flux at k+1 relative to cell k, k = 1..kz-1
-  float *sc = vsm + 3 * L;    // s, levels 1..kz+1
-  float *zu = vsm + 4 * L;
-  float *zd = vsm + 5 * L;
-#define A(a, k) a[(size_t)(k) * CX + tx]
-  const size_t ij = on ? g.at2(j, i) : 0, PS = g.PS;
-  const float dtrdz = 0.5f * (c.dtstepaf * c.rdzitaf);
-  if (on)
-    for (int k = 1 + ty; k <= kz + 1; k += KT) {
-      const size_t o = ij + (size_t)(k - 1) * PS;
-      A(sc, k) = float(s[o]);
-      if (k <= kz) {
-        A(e, k) = 0.f;
-        A(zu, k) = float(sa.zrfmu[o]);
-        A(zd, k) = float(sa.zrfmd[o]);
-        if (k <= kz - 1) A(dzs, k) = df_diff(src.ld(o + PS), src.ld(o));
-      }
-    }
-  __syncthreads();
-  // the threads owning the bottom and top cells keep their FP32 parts and
-  // double-float constant parts in registers over both passes
-  float eb32 = 0.f, et32 = 0.f;
-  F2 hb{0.f, 0.f}, ht{0.f, 0.f};
-  for (int pass = 0; pass < 2; ++pass) {
-    if (on)
-      for (int k = 1 + ty; k <= kz - 1; k += KT) {
-        const float skp = A(sc, k + 1);
-        const float zamu = skp * dtrdz;
-        const float ek = A(e, k), ekp1 = A(e, k + 1);
-        float is, num;
-        if (zamu >= 0.f) {
-          is = 1.f;
-          num = k + 2 <= kz ? (ekp1 - A(e, k + 2)) - A(dzs, k + 1) : 0.f;
-        } else {
-          is = -1.f;
-          num = k >= 2 ? (A(e, k - 1) - ek) - A(dzs, k - 1) : 0.f;
-        }
-        A(flo, k) = waf_flux<float>(0.5f * skp, is, zamu, A(dzs, k) + ekp1, ek, num);
-      }
-    __syncthreads();
-    if (on)
-      for (int k = 1 + ty; k <= kz; k += KT) {
-        const float sk = A(sc, k), skp = A(sc, k + 1);
-        const float zrfmu = A(zu, k), zrfmd = A(zd, k);
-        const float ek = A(e, k);
-        // flux below, moved to cell k; flux above, relative to cell k
-        const float fb = k >= 2 ? A(flo, k - 1) - sk * A(dzs, k - 1) : 0.f;
-        const float fa = k <= kz - 1 ? A(flo, k) : 0.f;
-        const float upd = -fb * zrfmu + fa * zrfmd + (sk * zrfmu - skp * zrfmd) * ek;
-        float en;
-        if (k == kz) {
-          // no flux through kz+1: constant part -v*s(kz+1)*zrfmd, exact product
-          et32 += upd;
-          ht = df_add(ht, df_mul(src.ld(ij + (size_t)(kz - 1) * PS), two_prod(-skp, zrfmd)));
-          en = et32 + df_f(ht);
-        } else if (k == 1) {
-          // no flux through level 1: constant part v*s(1)*zrfmu (s(1) = 0 inside)
-          eb32 += upd;
-          hb = df_add(hb, df_mul(src.ld(ij), two_prod(sk, zrfmu)));
-          en = eb32 + df_f(hb);
-        } else {
-          en = ek + upd;
-        }
-        A(e, k) = en;
-      }
-    __syncthreads();
+// Both vertical passes (Main/mod_moloch.F90:858-922) in increment form, one
+// thread per column, streaming the levels upward like k_adv_vertical with
+// pass 2 two levels behind pass 1.  e is the pass input's increment over the
+// field (zero for pass 1), dzs(k) = field(k+1) - field(k).  The flux through
+// interface k+1 is formed relative to cell k and moved to cell k+1 by
+// -s(k+1)*dzs(k).  Writes the increment dz = (field after the passes) -
+// field, as a double-float: the bottom and top cells carry a double-float
+// constant part (no flux through levels 1 and kz+1, where s need not vanish).
+__device__ __forceinline__ float vflux_inc(float dtrdz, float skp, float em1, float ek, float ekp1,
+                                           float ekp2, float dzm1, float dzk, float dzp1, int k,
+                                           int kz) {
+  const float zamu = skp * dtrdz;
+  float is, num;
+  if (zamu >= 0.f) {
+    is = 1.f;
+    num = k + 2 <= kz ? (ekp1 - ekp2) - dzp1 : 0.f;
+  } else {
+    is = -1.f;
+    num = k >= 2 ? (em1 - ek) - dzm1 : 0.f;
   }
-  if (on)
-    for (int k = 1 + ty; k <= kz; k += KT) {
-      F2 d;
-      if (k == kz) d = df_add_f(ht, et32);
-      else if (k == 1) d = df_add_f(hb, eb32);
-      else d = F2{A(e, k), 0.f};
-      dst.st(ij + (size_t)(k - 1) * PS, d);
-    }
-#undef A
+  return waf_flux<float>(0.5f * skp, is, zamu, dzk + ekp1, ek, num);
+}
+// the cell update without the bottom/top constant parts; flb is the flux
+// through interface k (relative to cell k-1), fla the flux through k+1
+__device__ __forceinline__ float vupdate_inc(float ek, float flb, float fla, float sk, float skp,
+                                             float zu, float zd, float dzm1, int k, int kz) {
+  const float fb = k >= 2 ? flb - sk * dzm1 : 0.f;
+  const float fa = k <= kz - 1 ? fla : 0.f;
+  return -fb * zu + fa * zd + (sk * zu - skp * zd) * ek;
 }
 
-// Meridional then zonal WAF of one tile (:984-1038; ROTLLR :926-983) in
-// increment form.  pp is the field at the start of the advection step, dz
-// its vertical increment; out = pp + dz + (meridional + zonal increments).
-template <class R, int kTJ, int kTI>
-__global__ void __launch_bounds__(kTJ *kTI) k_adv_horizontal_inc(const Dom<R> *__restrict__ doms,
-                                                                int tiles_j, int uvoff,
-                                                                int advoff) {
-  constexpr int WJ = kTJ + 4;          // columns J0-2 .. J0+TJ+1
-  __shared__ float pph_s[kTI + 4][WJ];  // rows I0-2 .. I0+TI+1: pp as hi + lo
-  __shared__ float ppl_s[kTI + 4][WJ];
-  __shared__ float dz_s[kTI + 4][WJ];   // vertical increment
-  __shared__ float dy_s[kTI + 3][WJ];   // pp(i+1) - pp(i), rows I0-2 .. I0+TI
-  __shared__ float fy_s[kTI + 1][WJ];   // meridional flux at i, relative to pp(i-1)
-  __shared__ float ey_s[kTI][WJ];       // p0 - pp, rows I0 .. I0+TI-1
-  __shared__ float hy_s[kTI][WJ];       // meridional increment alone
-  __shared__ float dx_s[kTI][kTJ + 3];  // pp(j+1) - pp(j), columns J0-2 .. J0+TJ
-  __shared__ float fx_s[kTI][kTJ + 1];  // zonal flux at j, relative to pp(j-1)
+template <class R>
+__global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
-  const int f = blockIdx.y & 1;
-  const int k = (blockIdx.y >> 1) + 1;
-  const int bj = blockIdx.x % tiles_j, bi = blockIdx.x / tiles_j;
+  const int f = (int)(blockIdx.x & 1u);
+  const int bj = (int)(blockIdx.x >> 1);
   const Geom g = D.g;
+  const int kz = g.kz;
+  const int j = bj * (int)blockDim.x + (int)threadIdx.x + 1;
+  const int i = (int)blockIdx.y * (int)blockDim.y + (int)threadIdx.y + 1;
+  if (j > g.jx - 1 || i > g.iy - 1) return;
+  const Scal &c = D.c;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const size_t F = g.field3();
+  const size_t ij = g.at2(j, i);
+  // double-float planes: offsets count floats of the hi plane
+  const DF src0(f == 0 ? D.tetav[adv] : D.pai[adv], F);
+  const DF dst0(D.wz_d[f], F);
+  const DF src{src0.p + ij, F};
+  const DF dst{dst0.p + ij, F};
+  const R *__restrict__ sp = D.s + ij;
+  const R *__restrict__ zup = D.sa.zrfmu + ij;
+  const R *__restrict__ zdp = D.sa.zrfmd + ij;
+  const unsigned PS = (unsigned)g.PS;
+  const float dtrdz = 0.5f * (c.dtstepaf * c.rdzitaf);
+
+  // the bottom cell's and top cell's FP32 parts and double-float constant parts
+  float eb32 = 0.f, et32 = 0.f;
+  F2 hb{0.f, 0.f}, ht{0.f, 0.f};
+  const F2 src1 = src.ld(0);
+  // windows: field at k+1, dzs at k-3..k, pass-1 output at k-3..k-1, s at
+  // k-2..k+1, metric at k-2..k-1, pass-1 flux at k (relative to k-1), pass-2
+  // flux at k-2
+  F2 xp1 = src.ld(PS);
+  float dm3 = 0.f, dm2 = 0.f, dm1 = 0.f, dk = df_diff(xp1, src1);
+  float e1m3 = 0.f, e1m2 = 0.f, e1m1 = 0.f;
+  float sm2 = 0.f, sm1 = 0.f, sk = float(sp[0]);
+  float zum2 = 0.f, zdm2 = 0.f, zum1 = 0.f, zdm1 = 0.f;
+  float f1k = 0.f, f2m = 0.f;
+  unsigned o = 0;
+  F2 n_x = src.ld(2 * PS);
+  float n_s = float(sp[PS]), n_zu = float(zup[0]), n_zd = float(zdp[0]);
+  for (int k = 1; k <= kz; ++k, o += PS) {
+    const float skp1 = n_s, zuk = n_zu, zdk = n_zd;
+    const F2 xp2 = n_x;  // field at k+2 (k+2 <= kz)
+    if (k < kz) {
+      n_s = float(sp[o + 2 * PS]);
+      n_zu = float(zup[o + PS]);
+      n_zd = float(zdp[o + PS]);
+      if (k + 3 <= kz) n_x = src.ld(o + 3 * PS);
+    }
+    const float dp1 = k + 2 <= kz ? df_diff(xp2, xp1) : 0.f;  // dzs(k+1)
+    // pass 1 (input increment zero)
+    const float f1kp = k <= kz - 1 ? vflux_inc(dtrdz, skp1, 0.f, 0.f, 0.f, 0.f, dm1, dk, dp1, k, kz) : 0.f;
+    const float u1 = vupdate_inc(0.f, f1k, f1kp, sk, skp1, zuk, zdk, dm1, k, kz);
+    float e1k;
+    if (k == kz) {
+      et32 += u1;
+      ht = df_add(ht, df_mul(src.ld(o), two_prod(-skp1, zdk)));
+      e1k = et32 + df_f(ht);
+    } else if (k == 1) {
+      eb32 += u1;
+      hb = df_add(hb, df_mul(src1, two_prod(sk, zuk)));
+      e1k = eb32 + df_f(hb);
+    } else {
+      e1k = 0.f + u1;
+    }
+    if (k >= 3) {  // pass 2 at level m = k-2
+      const int m = k - 2;
+      const float f2n = vflux_inc(dtrdz, sm1, e1m3, e1m2, e1m1, e1k, dm3, dm2, dm1, m, kz);
+      const float u2 = vupdate_inc(e1m2, f2m, f2n, sm2, sm1, zum2, zdm2, dm3, m, kz);
+      F2 d;
+      if (m == 1) {
+        eb32 += u2;
+        hb = df_add(hb, df_mul(src1, two_prod(sm2, zum2)));
+        d = df_add_f(hb, eb32);
+      } else {
+        d = F2{e1m2 + u2, 0.f};
+      }
+      dst.st(o - 2 * PS, d);
+      f2m = f2n;
+    }
+    dm3 = dm2; dm2 = dm1; dm1 = dk; dk = dp1;
+    xp1 = xp2;
+    e1m3 = e1m2; e1m2 = e1m1; e1m1 = e1k;
+    sm2 = sm1; sm1 = sk; sk = skp1;
+    zum2 = zum1; zdm2 = zdm1; zum1 = zuk; zdm1 = zdk;
+    f1k = f1kp;
+  }
+  // pass 2 at levels kz-1 and kz; dm3 = dzs(kz-2), dm2 = dzs(kz-1) now
+  const unsigned ot = (unsigned)(kz - 1) * PS;
+  const float f2n = vflux_inc(dtrdz, sm1, e1m3, e1m2, e1m1, 0.f, dm3, dm2, dm1, kz - 1, kz);
+  const float u2 = vupdate_inc(e1m2, f2m, f2n, sm2, sm1, zum2, zdm2, dm3, kz - 1, kz);
+  dst.st(ot - PS, F2{e1m2 + u2, 0.f});
+  const float ut = vupdate_inc(e1m1, f2n, 0.f, sm1, sk, zum1, zdm1, dm2, kz, kz);
+  et32 += ut;
+  ht = df_add(ht, df_mul(src.ld(ot), two_prod(-sk, zdm1)));
+  dst.st(ot, df_add_f(ht, et32));
+}
+
+// Meridional then zonal WAF (:984-1038; ROTLLR :926-983) in increment form
+// for theta_v and Exner of a mixed member, at one level for a tile of nw rows,
+// with the lane geometry of k_adv_horizontal: warp w owns row I0+w, lane l
+// owns v consecutive columns, coefficients in registers, the meridional
+// fluxes shared between rows through shared memory and the zonal neighbours
+// taken from adjacent lanes.  pp is the field at the start of the advection
+// step (double-float), dz its vertical increment; out = pp + dz + (meridional
+// + zonal increments).  Fluxes are formed relative to the cell south (west)
+// of the interface, from FP32 increments and neighbour differences.
+template <class R, int V, int NW>
+__global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__restrict__ doms,
+                                                               int tiles_j, int uvoff,
+                                                               int advoff) {
+  constexpr int W = 32 * V, S = W - 4;
+  constexpr int OB0 = hshape_ob0(V);
+  __shared__ __align__(16) float fy_s[2][NW + 1][W];  // meridional fluxes, rows I0 .. I0+NW
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const int k = blockIdx.y + 1;
+  const Geom g = D.g;
+  const int jx = g.jx, iy = g.iy;
+  if (k > g.kz) return;
+  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int ob = bj * S + OB0;
+  const int I0 = bi * NW + 1;
+  if (ob + 3 > jx - 1 || I0 > iy - 1) return;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
-  const int jx = g.jx, iy = g.iy, kz = g.kz;
-  if (k > kz) return;
-  const int J0 = bj * kTJ + 1, I0 = bi * kTI + 1;
-  if (J0 > jx - 1 || I0 > iy - 1) return;
   const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
-  const size_t PS = g.PS, ko = (size_t)(k - 1) * PS;
+  const int lane = (int)(threadIdx.x & 31u), wp = (int)(threadIdx.x >> 5);
+  const int i = I0 + wp;
+  const int e0 = ob + V * lane;
+  const bool inrow = e0 >= 0 && e0 + V <= g.P;
+  const unsigned P = (unsigned)g.P;
+  const unsigned ko = (unsigned)(k - 1) * (unsigned)g.PS;
   const size_t F = g.field3();
-  const DF pp(f == 0 ? D.tetav[adv] : D.pai[adv], F);
-  const DF out(f == 0 ? D.tetav[adv ^ 1] : D.pai[adv ^ 1], F);
-  const DF dzg(D.wz_d[f], F);
-  const R *__restrict__ uk = D.u[uv] + ko;
-  const R *__restrict__ vk = D.v[uv] + ko;
-  const int tid = threadIdx.y * kTJ + threadIdx.x;
-  const int nth = kTJ * kTI;
+  const float *__restrict__ uk = D.u[uv] + ko;
+  const float *__restrict__ vk = D.v[uv] + ko;
   const float dta = c.dtstepaf;
   const float dtrdx = dta * c.rdxf, dtrdy = dta * c.rdxf;
   const bool rot = c.lrotllr != 0;
-  const int imin = 1, imax = iy - 1, jmin = 1, jmax = jx - 1;
+  using T = float;
 
-  for (int e = tid; e < (kTI + 4) * WJ; e += nth) {
-    const int rr = e / WJ, cc = e % WJ;
-    const int i = I0 - 2 + rr, j = J0 - 2 + cc;
-    F2 x{0.f, 0.f};
-    float z = 0.f;
-    if (i >= 1 && i <= iy - 1 && j >= 1 && j <= jx - 1) {
-      const size_t ij = g.at2(j, i) + ko;
-      x = pp.ld(ij);
-      z = df_f(dzg.ld(ij));
+  int jq[V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) jq[q] = e0 + q + 1;
+  const bool rowM = i >= 2 && i <= iy - 1;
+  const bool rowP = i >= 2 && i <= iy - 2;
+  const bool okM = inrow && rowM, okP = inrow && rowP;
+  const int ie = I0 + NW;
+  const bool okE = wp == NW - 1 && inrow && ie >= 2 && ie <= iy - 1;
+  // ---- coefficients ----
+  T vv[V], zmy[V], vve[V], zmye[V];
+  bool mv[V], me[V];
+  {
+    T a[V], b[V];
+    ld_row<T, V>(a, vk, e0, i, P, okM);
+    ld_row<T, V>(b, sa.msfv, e0, i, P, okM && !rot);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const bool ok = okM && jq[q] >= 1 && jq[q] <= jx - 1;
+      mv[q] = ok;
+      vv[q] = ok ? a[q] : T(0);
+      zmy[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
     }
-    pph_s[rr][cc] = x.hi;
-    ppl_s[rr][cc] = x.lo;
-    dz_s[rr][cc] = z;
-  }
-  __syncthreads();
-  for (int e = tid; e < (kTI + 3) * WJ; e += nth) {
-    const int rr = e / WJ, cc = e % WJ;
-    dy_s[rr][cc] = (pph_s[rr + 1][cc] - pph_s[rr][cc]) + (ppl_s[rr + 1][cc] - ppl_s[rr][cc]);
-  }
-  for (int e = tid; e < kTI * (kTJ + 3); e += nth) {
-    const int rr = e / (kTJ + 3), cc = e % (kTJ + 3);
-    dx_s[rr][cc] = (pph_s[rr + 2][cc + 1] - pph_s[rr + 2][cc]) +
-                   (ppl_s[rr + 2][cc + 1] - ppl_s[rr + 2][cc]);
-  }
-  __syncthreads();
-  // meridional fluxes at interface rows i = I0 .. I0+TI, relative to pp(i-1)
-  for (int e = tid; e < (kTI + 1) * WJ; e += nth) {
-    const int rr = e / WJ, cc = e % WJ;
-    const int i = I0 + rr, j = J0 - 2 + cc;
-    float x = 0.f;
-    if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 1) {
-      const size_t ij = g.at2(j, i);
-      const float vv = float(vk[ij]);
-      const float zamu = rot ? vv * dtrdy : vv * float(sa.msfv[ij]) * dtrdy;
-      float is;
-      int ih;
-      if (zamu > 0.f) { is = 1.f; ih = i - 1; }
-      else { is = -1.f; ih = min(i + 1, imax); }
-      const int ihm1 = max(ih - 1, imin);
-      const int b = 2 - I0;  // tile row of global row i is i + b
-      const float dpp = ih != ihm1 ? dy_s[ihm1 + b][cc] : 0.f;
-      const float num = (dz_s[ih + b][cc] - dz_s[ihm1 + b][cc]) + dpp;
-      x = waf_flux<float>(0.5f * vv, is, zamu, dz_s[i - 1 + b][cc],
-                          dz_s[i + b][cc] + dy_s[i - 1 + b][cc], num);
+    ld_row<T, V>(a, vk, e0, ie, P, okE);
+    ld_row<T, V>(b, sa.msfv, e0, ie, P, okE && !rot);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const bool ok = okE && jq[q] >= 1 && jq[q] <= jx - 1;
+      me[q] = ok;
+      vve[q] = ok ? a[q] : T(0);
+      zmye[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
     }
-    fy_s[rr][cc] = x;
   }
-  __syncthreads();
-  // p0 - pp on rows I0 .. I0+TI-1
-  for (int e = tid; e < kTI * WJ; e += nth) {
-    const int rr = e / WJ, cc = e % WJ;
-    const int i = I0 + rr, j = J0 - 2 + cc;
-    float hy = 0.f;
-    if (j >= 1 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
-      const size_t ij = g.at2(j, i), ijN = ij + (size_t)g.P;
-      const float fz = float(sa.fmz[ko + ij]);
-      const float vs = float(vk[ij]), vn = float(vk[ijN]);
-      const float fs = fy_s[rr][cc] - vs * dy_s[rr + 1][cc];  // moved to pp(i)
-      const float fn = fy_s[rr + 1][cc];
+  T zs[V], zn[V], vsv[V], cy[V], m2[V], uu[V], zmx[V], zw[V], ze[V], uwv[V], cx[V];
+  bool pv[V], xv[V], rv[V], cyf[V], cxf[V];
+  {
+    T fz[V], vi[V], vn[V], ri[V], rn[V], fi[V], fn[V], mf[V], ui[V], rmui[V], msu[V];
+    ld_row<T, V>(fz, sa.fmz + ko, e0, i, P, okP);
+    ld_row<T, V>(vi, vk, e0, i, P, okP);
+    ld_row<T, V>(vn, vk, e0, i + 1, P, okP);
+    ld_row<T, V>(ri, sa.rmv, e0, i, P, okP);
+    ld_row<T, V>(rn, sa.rmv, e0, i + 1, P, okP);
+    ld_row<T, V>(fi, (rot ? sa.rfmzv : sa.rfmzu) + ko, e0, i, P, okP);
+    ld_row<T, V>(fn, (rot ? sa.rfmzv : sa.rfmzu) + ko, e0, i + 1, P, okP);
+    ld_row<T, V>(mf, rot ? sa.msfx : sa.mx2, e0, i, P, okP);
+    ld_row<T, V>(ui, uk, e0, i, P, okP);
+    ld_row<T, V>(rmui, sa.rmu, e0, i, P, okP && !rot);
+    ld_row<T, V>(msu, sa.msfu, e0, i, P, okP);
+    T fzu[V], fze[V], ue[V], rme[V];
+    ld_row<T, V>(fzu, sa.rfmzu + ko, e0, i, P, okP);
+    next_col<T, V>(fze, fzu);
+    next_col<T, V>(ue, ui);
+    next_col<T, V>(rme, rmui);
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const int j = jq[q];
+      pv[q] = okP && j >= 1 && j <= jx - 1;
+      xv[q] = okP && j >= 2 && j <= jx - 1;
+      rv[q] = okP && j >= 2 && j <= jx - 2;
+      vsv[q] = vi[q];
+      uwv[q] = ui[q];
       if (rot) {
-        const float zhxvtn = dtrdy * float(sa.rmv[ijN]) * float(sa.msfx[ij]);
-        const float zhxvts = dtrdy * float(sa.rmv[ij]) * float(sa.msfx[ij]);
-        const float zrfmn = zhxvtn * fz * float(sa.rfmzv[ko + ijN]);
-        const float zrfms = zhxvts * fz * float(sa.rfmzv[ko + ij]);
-        hy = fs * zrfms - fn * zrfmn;
+        const T zhxvtn = dtrdy * rn[q] * mf[q];
+        const T zhxvts = dtrdy * ri[q] * mf[q];
+        zn[q] = zhxvtn * fz[q] * fn[q];
+        zs[q] = zhxvts * fz[q] * fi[q];
+        m2[q] = T(1);
+        cyf[q] = false;
+        cy[q] = T(0);
+        const T zcostx = dtrdx * mf[q];
+        zw[q] = zcostx * fz[q] * fzu[q];
+        ze[q] = zcostx * fz[q] * fze[q];
+        cxf[q] = false;
+        cx[q] = T(0);
       } else {
-        const float zrfmn = dtrdy * fz * float(sa.rfmzu[ko + ijN]);
-        const float zrfms = dtrdy * fz * float(sa.rfmzu[ko + ij]);
-        const float mx2 = float(sa.mx2[ij]);
-        const float rs = float(sa.rmv[ij]), rn = float(sa.rmv[ijN]);
-        hy = mx2 * (fs * zrfms - fn * zrfmn);
-        if (rs != 1.f || rn != 1.f)
-          hy += pph_s[rr + 2][cc] * (mx2 * (vs * zrfms * (1.f - rs) - vn * zrfmn * (1.f - rn)));
+        zn[q] = dtrdy * fz[q] * fn[q];
+        zs[q] = dtrdy * fz[q] * fi[q];
+        m2[q] = mf[q];
+        // the map-factor terms a constant field does not cancel
+        cyf[q] = ri[q] != 1.f || rn[q] != 1.f;
+        cy[q] = mf[q] * (vi[q] * zs[q] * (1.f - ri[q]) - vn[q] * zn[q] * (1.f - rn[q]));
+        zw[q] = dtrdx * fz[q] * fzu[q];
+        ze[q] = dtrdx * fz[q] * fze[q];
+        cxf[q] = rmui[q] != 1.f || rme[q] != 1.f;
+        cx[q] = mf[q] * (ui[q] * zw[q] * (1.f - rmui[q]) - ue[q] * ze[q] * (1.f - rme[q]));
+      }
+      uu[q] = xv[q] ? ui[q] : T(0);
+      zmx[q] = xv[q] ? ui[q] * msu[q] * dtrdx : T(0);
+    }
+  }
+  const bool rowin = inrow && i <= iy - 1;
+  bool wv[V];
+  bool wall = true;
+#pragma unroll
+  for (int q = 0; q < V; ++q) {
+    const int cc = V * lane + q;
+    wv[q] = rowin && cc >= 2 && cc <= W - 3 && jq[q] >= 1 && jq[q] <= jx - 1;
+    wall = wall && wv[q];
+  }
+  // a row r of a double-float plane pair (hi, lo), zero outside rows 1 .. iy-1
+  auto ld_pair = [&](T(&h)[V], T(&l)[V], const float *hi, int r) {
+    const bool ok = inrow && r >= 1 && r <= iy - 1;
+    ld_row<T, V>(h, hi + ko, e0, r, P, ok);
+    ld_row<T, V>(l, hi + F + ko, e0, r, P, ok);
+  };
+  // the meridional flux through the south face of row r (relative to pp(r-1))
+  // from dz and pp differences of rows r-2 .. r+1; the reference's clamps
+  // ih = min(r+1, imax), ihm1 = max(ih-1, imin)
+  auto mflux = [&](T (&x)[V], const T (&vvr)[V], const T (&zm)[V], const bool (&ok)[V], int r,
+                   const T (&zm2)[V], const T (&zm1)[V], const T (&z0)[V], const T (&zp1)[V],
+                   const T (&dym2)[V], const T (&dym1)[V], const T (&dy0)[V]) {
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const bool up = zm[q] > 0.f;
+      float num;
+      if (up) num = r >= 3 ? (zm1[q] - zm2[q]) + dym2[q] : (zm1[q] - zm1[q]) + 0.f;
+      else num = r <= iy - 2 ? (zp1[q] - z0[q]) + dy0[q] : (z0[q] - zm1[q]) + dym1[q];
+      const float y = waf_flux<float>(0.5f * vvr[q], up ? 1.f : -1.f, zm[q], zm1[q], z0[q] + dym1[q], num);
+      x[q] = ok[q] ? y : 0.f;
+    }
+  };
+
+  for (int f = 0; f < 2; ++f) {
+    const float *pph = reinterpret_cast<const float *>(f == 0 ? D.tetav[adv] : D.pai[adv]);
+    float *outh = reinterpret_cast<float *>(f == 0 ? D.tetav[adv ^ 1] : D.pai[adv ^ 1]);
+    const float *dzh = reinterpret_cast<const float *>(D.wz_d[f]);
+    float (*fy)[W] = fy_s[f];
+    // rows i-2 .. i+1 of pp (hi, lo) and dz (rounded to FP32)
+    T ph[4][V], pl[4][V], zz[4][V], dzi_h[V], dzi_l[V];
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr) {
+      ld_pair(ph[rr], pl[rr], pph, i - 2 + rr);
+      T zh[V], zl[V];
+      ld_pair(zh, zl, dzh, i - 2 + rr);
+#pragma unroll
+      for (int q = 0; q < V; ++q) zz[rr][q] = zh[q] + zl[q];
+      if (rr == 2) {
+#pragma unroll
+        for (int q = 0; q < V; ++q) { dzi_h[q] = zh[q]; dzi_l[q] = zl[q]; }
       }
     }
-    hy_s[rr][cc] = hy;
-    ey_s[rr][cc] = dz_s[rr + 2][cc] + hy;
-  }
-  __syncthreads();
-  // zonal fluxes at interface columns j = J0 .. J0+TJ, relative to pp(j-1)
-  for (int e = tid; e < kTI * (kTJ + 1); e += nth) {
-    const int rr = e / (kTJ + 1), cc = e % (kTJ + 1);
-    const int i = I0 + rr, j = J0 + cc;
-    float x = 0.f;
-    if (j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2) {
-      const size_t ij = g.at2(j, i);
-      const float uu = float(uk[ij]);
-      const float zamu = uu * float(sa.msfu[ij]) * dtrdx;
-      float is;
-      int jh;
-      if (zamu > 0.f) { is = 1.f; jh = j - 1; }
-      else { is = -1.f; jh = min(j + 1, jmax); }
-      const int jhm1 = max(jh - 1, jmin);
-      const int b = 2 - J0;  // ey_s / dx_s column of global column j is j + b
-      const float dpp = jh != jhm1 ? dx_s[rr][jhm1 + b] : 0.f;
-      const float num = (ey_s[rr][jh + b] - ey_s[rr][jhm1 + b]) + dpp;
-      x = waf_flux<float>(0.5f * uu, is, zamu, ey_s[rr][j - 1 + b],
-                          ey_s[rr][j + b] + dx_s[rr][j - 1 + b], num);
+    // dy(r) = pp(r+1) - pp(r) for r = i-2, i-1, i
+    T dy[3][V];
+#pragma unroll
+    for (int rr = 0; rr < 3; ++rr)
+#pragma unroll
+      for (int q = 0; q < V; ++q)
+        dy[rr][q] = (ph[rr + 1][q] - ph[rr][q]) + (pl[rr + 1][q] - pl[rr][q]);
+    {
+      T x[V];
+      mflux(x, vv, zmy, mv, i, zz[0], zz[1], zz[2], zz[3], dy[0], dy[1], dy[2]);
+      st_vec<T, V>(&fy[wp][V * lane], x);
     }
-    fx_s[rr][cc] = x;
-  }
-  __syncthreads();
-  {
-    const int rr = threadIdx.y, cc = threadIdx.x;
-    const int i = I0 + rr, j = J0 + cc;
-    if (i <= iy - 1 && j <= jx - 1) {
-      const size_t ij = g.at2(j, i);
-      const F2 ppk{pph_s[rr + 2][cc + 2], ppl_s[rr + 2][cc + 2]};
+    if (wp == NW - 1) {  // the flux of row I0+NW: rows ie-2 .. ie+1 = i-1 .. i+2
+      T h4[V], l4[V], zh[V], zl[V], z4[V], dy3[V];
+      ld_pair(h4, l4, pph, i + 2);
+      ld_pair(zh, zl, dzh, i + 2);
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        z4[q] = zh[q] + zl[q];
+        dy3[q] = (h4[q] - ph[3][q]) + (l4[q] - pl[3][q]);
+      }
+      T x[V];
+      mflux(x, vve, zmye, me, ie, zz[1], zz[2], zz[3], z4, dy[1], dy[2], dy3);
+      st_vec<T, V>(&fy[NW][V * lane], x);
+    }
+    __syncthreads();
+    // p0 - pp: ey = dz + hy, hy the meridional increment
+    T hy[V], ey[V];
+    {
+      T ys[V], yn[V];
+      ld_vec<T, V>(ys, &fy[wp][V * lane]);
+      ld_vec<T, V>(yn, &fy[wp + 1][V * lane]);
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        const float fs = ys[q] - vsv[q] * dy[1][q];  // moved to pp(i)
+        const float fn = yn[q];
+        float h = m2[q] * (fs * zs[q] - fn * zn[q]);
+        if (rot) h = fs * zs[q] - fn * zn[q];
+        else if (cyf[q]) h += ph[2][q] * cy[q];
+        hy[q] = pv[q] ? h : 0.f;
+        ey[q] = zz[2][q] + hy[q];
+      }
+    }
+    // dx(j) = pp(j+1) - pp(j) at row i for the lane's columns; the east
+    // neighbour's pp from the next lane
+    T dx[V], dxw2, dxw1;
+    {
+      T eh[V], el[V];
+      next_col<T, V>(eh, ph[2]);
+      next_col<T, V>(el, pl[2]);
+#pragma unroll
+      for (int q = 0; q < V; ++q) dx[q] = (eh[q] - ph[2][q]) + (el[q] - pl[2][q]);
+      dxw2 = __shfl_up_sync(0xffffffffu, dx[V >= 2 ? V - 2 : 0], V >= 2 ? 1 : 2);
+      dxw1 = __shfl_up_sync(0xffffffffu, dx[V - 1], 1);
+    }
+    const float ew2 = __shfl_up_sync(0xffffffffu, ey[V >= 2 ? V - 2 : 0], V >= 2 ? 1 : 2);
+    const float ew1 = __shfl_up_sync(0xffffffffu, ey[V - 1], 1);
+    const float ee1 = __shfl_down_sync(0xffffffffu, ey[0], 1);
+    auto eyat = [&](int q) -> float {
+      return q == -2 ? ew2 : q == -1 ? ew1 : q == V ? ee1 : ey[q < 0 ? 0 : q >= V ? V - 1 : q];
+    };
+    auto dxat = [&](int q) -> float {
+      return q == -2 ? dxw2 : q == -1 ? dxw1 : dx[q < 0 ? 0 : q >= V ? V - 1 : q];
+    };
+    // zonal fluxes at the lane's columns, relative to pp(j-1)
+    T fx[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const int j = jq[q];
+      const bool up = zmx[q] > 0.f;
+      const float a = eyat(q - 1), cq = eyat(q);
+      float num;
+      if (up) num = j >= 3 ? (a - eyat(q - 2)) + dxat(q - 2) : (a - a) + 0.f;
+      else num = j <= jx - 2 ? (eyat(q + 1) - cq) + dxat(q) : (cq - a) + dxat(q - 1);
+      const float y = waf_flux<float>(0.5f * uu[q], up ? 1.f : -1.f, zmx[q], a, cq + dxat(q - 1), num);
+      fx[q] = xv[q] ? y : 0.f;
+    }
+    T fxe[V];
+    next_col<T, V>(fxe, fx);
+    // result
+    T rh[V], rl[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const F2 ppk{ph[2][q], pl[2][q]};
       F2 x = ppk;
-      if (j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2) {
-        const float fz = float(sa.fmz[ko + ij]);
-        const float uw = float(uk[ij]), ue = float(uk[ij + 1]);
-        const float fw = fx_s[rr][cc] - uw * dx_s[rr][cc + 1];  // moved to pp(j)
-        const float fe = fx_s[rr][cc + 1];
+      if (rv[q]) {
+        const float fw = fx[q] - uwv[q] * dxat(q - 1);  // moved to pp(j)
+        const float fe = fxe[q];
         float hx;
         if (rot) {
-          const float zcostx = dtrdx * float(sa.msfx[ij]);
-          const float zrfmw = zcostx * fz * float(sa.rfmzu[ko + ij]);
-          const float zrfme = zcostx * fz * float(sa.rfmzu[ko + ij + 1]);
-          hx = fw * zrfmw - fe * zrfme;
+          hx = fw * zw[q] - fe * ze[q];
         } else {
-          const float zrfmw = dtrdx * fz * float(sa.rfmzu[ko + ij]);
-          const float zrfme = dtrdx * fz * float(sa.rfmzu[ko + ij + 1]);
-          const float mx2 = float(sa.mx2[ij]);
-          const float rw = float(sa.rmu[ij]), re = float(sa.rmu[ij + 1]);
-          hx = mx2 * (fw * zrfmw - fe * zrfme);
-          if (rw != 1.f || re != 1.f)
-            hx += ppk.hi * (mx2 * (uw * zrfmw * (1.f - rw) - ue * zrfme * (1.f - re)));
+          hx = m2[q] * (fw * zw[q] - fe * ze[q]);
+          if (cxf[q]) hx += ppk.hi * cx[q];
         }
-        x = df_add_f(df_add(ppk, dzg.ld(ij + ko)), hy_s[rr][cc + 2] + hx);
+        x = df_add_f(df_add(ppk, F2{dzi_h[q], dzi_l[q]}), hy[q] + hx);
       }
-      out.st(ij + ko, x);
+      rh[q] = x.hi;
+      rl[q] = x.lo;
+    }
+    float *oh = outh + ko + (unsigned)(i - 1) * P;
+    if (wall) {
+      st_vec<T, V>(oh + (unsigned)e0, rh);
+      st_vec<T, V>(oh + F + (unsigned)e0, rl);
+    } else if (rowin) {
+#pragma unroll
+      for (int q = 0; q < V; ++q)
+        if (wv[q]) {
+          oh[(unsigned)(e0 + q)] = rh[q];
+          oh[F + (unsigned)(e0 + q)] = rl[q];
+        }
     }
   }
 }
@@ -981,72 +1288,82 @@ void Launch<R>::adv_prep(const LaunchGeom &L, const Dom<R> *d, int uvoff, int ad
 template <class R, class T>
 void launch_vertical(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int advoff,
                      cudaStream_t s) {
-  // vert_x columns along j per block, vert_y threads along the levels
+  // one thread per column: blocks of vert_x x vert_y columns along (j, i)
   const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
-  const size_t smem = (size_t)5 * (L.kz + 2) * b.x * sizeof(T);
-  const dim3 grd((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * nf), (unsigned)(L.iy - 1),
-                 (unsigned)L.nmem);
-  k_adv_vertical<R, T><<<grd, b, smem, s>>>(d, nf, set, advoff);
+  const dim3 grd((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * nf),
+                 (unsigned)((L.iy - 1 + L.vert_y - 1) / L.vert_y), (unsigned)L.nmem);
+  k_adv_vertical<R, T><<<grd, b, 0, s>>>(d, nf, set, advoff);
 }
 
-template <class R, int TJ, int TI>
+template <class R, int V, int NW>
 void launch_tile(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
-  const int tj = (L.jx - 1 + TJ - 1) / TJ, ti = (L.iy - 1 + TI - 1) / TI;
+  // tiles along j: tile bj writes j = bj*S + ob0 + 3 .. bj*S + ob0 + S + 2
+  constexpr int S = 32 * V - 4;
+  const int tj = (L.jx - 3 - hshape_ob0(V) + S - 1) / S, ti = (L.iy - 1 + NW - 1) / NW;
   const dim3 grd((unsigned)(tj * ti), (unsigned)L.kz, (unsigned)L.nmem);
-  k_adv_horizontal<R, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(d, tj, uvoff, advoff);
+  k_adv_horizontal<R, V, NW><<<grd, 32 * NW, 0, s>>>(d, tj, uvoff, advoff);
 }
 
 template <class R>
 void launch_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+  constexpr int eb = (int)sizeof(R);
   switch (L.htile) {
-    case 1: launch_tile<R, 32, 4>(L, d, uvoff, advoff, s); break;
-    case 2: launch_tile<R, 64, 4>(L, d, uvoff, advoff, s); break;
-    case 3: launch_tile<R, 16, 8>(L, d, uvoff, advoff, s); break;
-    default: launch_tile<R, 32, 8>(L, d, uvoff, advoff, s); break;
+    case 1: launch_tile<R, hshape(eb, 1).v, hshape(eb, 1).nw>(L, d, uvoff, advoff, s); break;
+    case 2: launch_tile<R, hshape(eb, 2).v, hshape(eb, 2).nw>(L, d, uvoff, advoff, s); break;
+    case 3: launch_tile<R, hshape(eb, 3).v, hshape(eb, 3).nw>(L, d, uvoff, advoff, s); break;
+    default: launch_tile<R, hshape(eb, 0).v, hshape(eb, 0).nw>(L, d, uvoff, advoff, s); break;
   }
 }
 
 template <class R>
 void launch_vertical_inc(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
-  const size_t smem = (size_t)6 * (L.kz + 2) * b.x * sizeof(float);
-  const dim3 grd((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * 2), (unsigned)(L.iy - 1),
-                 (unsigned)L.nmem);
-  k_adv_vertical_inc<R><<<grd, b, smem, s>>>(d, advoff);
+  const dim3 grd((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * 2),
+                 (unsigned)((L.iy - 1 + L.vert_y - 1) / L.vert_y), (unsigned)L.nmem);
+  k_adv_vertical_inc<R><<<grd, b, 0, s>>>(d, advoff);
 }
 
-template <class R, int TJ, int TI>
+template <class R, int V, int NW>
 void launch_tile_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
-  const int tj = (L.jx - 1 + TJ - 1) / TJ, ti = (L.iy - 1 + TI - 1) / TI;
-  const dim3 grd((unsigned)(tj * ti), (unsigned)(2 * L.kz), (unsigned)L.nmem);
-  k_adv_horizontal_inc<R, TJ, TI><<<grd, dim3(TJ, TI), 0, s>>>(d, tj, uvoff, advoff);
+  constexpr int S = 32 * V - 4;
+  const int tj = (L.jx - 3 - hshape_ob0(V) + S - 1) / S, ti = (L.iy - 1 + NW - 1) / NW;
+  const dim3 grd((unsigned)(tj * ti), (unsigned)L.kz, (unsigned)L.nmem);
+  k_adv_horizontal_inc<R, V, NW><<<grd, 32 * NW, 0, s>>>(d, tj, uvoff, advoff);
 }
 
+// the increment form keeps two planes per field: lanes of at most 2 columns
 template <class R>
 void launch_horizontal_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                            cudaStream_t s) {
   switch (L.htile) {
-    case 1: launch_tile_inc<R, 32, 4>(L, d, uvoff, advoff, s); break;
-    case 2: launch_tile_inc<R, 64, 4>(L, d, uvoff, advoff, s); break;
-    case 3: launch_tile_inc<R, 16, 8>(L, d, uvoff, advoff, s); break;
-    default: launch_tile_inc<R, 32, 8>(L, d, uvoff, advoff, s); break;
+    case 1:
+    case 2: launch_tile_inc<R, 2, 8>(L, d, uvoff, advoff, s); break;
+    case 3: launch_tile_inc<R, 2, 4>(L, d, uvoff, advoff, s); break;
+    default: launch_tile_inc<R, 1, 8>(L, d, uvoff, advoff, s); break;
   }
 }
 
-// The FP64 fields of a mixed member (L.nadv_d = 2) use the increment form.
 template <class R>
 void Launch<R>::adv_vertical(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   launch_vertical<R, R>(L, d, L.nadv_r, 0, advoff, s);
-  if constexpr (sizeof(R) == sizeof(float))
-    if (L.nadv_d) launch_vertical_inc<R>(L, d, advoff, s);
 }
 
 template <class R>
 void Launch<R>::adv_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                                cudaStream_t s) {
   launch_horizontal<R>(L, d, uvoff, advoff, s);
-  if constexpr (sizeof(R) == sizeof(float))
-    if (L.nadv_d) launch_horizontal_inc<R>(L, d, uvoff, advoff, s);
+}
+
+// The FP64 fields of a mixed member (L.nadv_d = 2) use the increment form.
+template <class R>
+void Launch<R>::adv_vertical_inc(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
+  if constexpr (sizeof(R) == sizeof(float)) launch_vertical_inc<R>(L, d, advoff, s);
+}
+
+template <class R>
+void Launch<R>::adv_horizontal_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                                   cudaStream_t s) {
+  if constexpr (sizeof(R) == sizeof(float)) launch_horizontal_inc<R>(L, d, uvoff, advoff, s);
 }
 
 template <class R>
@@ -1075,13 +1392,7 @@ void Launch<R>::adv_back(const LaunchGeom &L, const Dom<R> *d, int uvoff, int ad
 
 template <class R>
 cudaError_t Launch<R>::configure_advect() {
-  cudaError_t e = cudaFuncSetAttribute(k_adv_vertical<R, R>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  if constexpr (sizeof(R) == sizeof(float))
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_adv_vertical_inc<R>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  return e;
+  return cudaSuccess;
 }
 
 template struct Launch<double>;

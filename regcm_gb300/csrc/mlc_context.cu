@@ -320,8 +320,6 @@ int ensure_staging(mlc_ctx *x, const mlc_dims &d) {
 // boundary: FP32 tiles start 4 columns left of J0 (x = TJ*bj - 4) and are
 // TJ+8 wide, FP64 tiles 2 columns left (x = TJ*bj - 2) and TJ+4 wide; both
 // widths are multiples of 16 bytes and x*element size is a multiple of 16.
-const int kTileJ[kTileShapes] = {32, 32, 64, 16};
-const int kTileI[kTileShapes] = {8, 4, 4, 8};
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -353,7 +351,8 @@ int encode_tmaps(mlc_ctx *x, const Member &m, const Dom<R> &D) {
   const cuuint64_t strides[2] = {(cuuint64_t)g.P * es, (cuuint64_t)g.PS * es};
   const cuuint32_t estr[3] = {1, 1, 1};
   for (int t = 0; t < kTileShapes; ++t) {
-    const cuuint32_t box[3] = {(cuuint32_t)(kTileJ[t] + (es == 4 ? 8 : 4)), (cuuint32_t)(kTileI[t] + 4), 1};
+    const HShape h = hshape((int)es, t);
+    const cuuint32_t box[3] = {(cuuint32_t)(32 * h.v + 2 * hshape_off((int)es, h.v)), (cuuint32_t)(h.nw + 4), 1};
     for (int f = 0; f < nf; ++f) {
       const CUresult r = enc(&maps[(size_t)t * kMaxFields + f],
                              es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
@@ -508,7 +507,6 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
   const Dom<R> *d = static_cast<const Dom<R> *>(x->table);
   cudaStream_t s = x->stream;
   const int nadv = x->prm.mo_nadv, nsound = x->prm.mo_nsound;
-  const int nv = L.nadv_d ? 2 : 1;  // FP64 theta_v/Exner launches of a mixed step
   int nl = 0;
   for (int r = 0; r < nadv; ++r) {
     // ---- sound (Main/mod_moloch.F90:531-765) ----
@@ -522,8 +520,10 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
     // ---- advection (Main/mod_moloch.F90:767-1042) ----
     const int uvo = (r + 1) * nsound;
     REC("adv_prep", K::adv_prep(L, d, uvo, r, s)); ++nl;
-    REC("adv_vertical", K::adv_vertical(L, d, r, s)); nl += nv;
-    REC("adv_horizontal", K::adv_horizontal(L, d, uvo, r, s)); nl += nv;
+    REC("adv_vertical", K::adv_vertical(L, d, r, s)); ++nl;
+    if (L.nadv_d) { REC("adv_vertical_inc", K::adv_vertical_inc(L, d, r, s)); ++nl; }
+    REC("adv_horizontal", K::adv_horizontal(L, d, uvo, r, s)); ++nl;
+    if (L.nadv_d) { REC("adv_horizontal_inc", K::adv_horizontal_inc(L, d, uvo, r, s)); ++nl; }
     if (x->key.any_copy) { REC("adv_species_copy", K::adv_species_copy(L, d, r, s)); ++nl; }
     if (x->key.any_curv) { REC("adv_curvature", K::adv_curvature(L, d, r + 1, s)); ++nl; }
     REC("adv_back", K::adv_back(L, d, uvo, r + 1, s)); ++nl;
@@ -996,8 +996,8 @@ int create_common(const mlc_params *params, int capacity, size_t budget, mlc_ctx
   LaunchGeom &L = x->key.L;
   L.col_x = 32; L.col_y = 4;
   L.solve_x = 32; L.solve_y = 2;
-  L.vert_x = 32; L.vert_y = 8;
-  L.htile = 0;
+  L.vert_x = 32; L.vert_y = 4;
+  L.htile = 1;  // 64x8 tiles; the autotuner's fixed configuration is 32x8
   cudaError_t e = cudaGetDevice(&x->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) {
@@ -1324,13 +1324,13 @@ namespace {
 
 const int kColCand[][2] = {{32, 4}, {32, 8}, {64, 2}, {64, 4}, {128, 1}, {16, 8}};
 const int kSolveCand[][2] = {{32, 2}, {32, 1}, {64, 1}, {32, 4}, {16, 4}};
-const int kVertCand[][2] = {{32, 8}, {32, 4}, {64, 4}, {32, 16}, {64, 8}};
+const int kVertCand[][2] = {{32, 4}, {32, 8}, {64, 2}, {32, 2}, {128, 1}};
 constexpr int kNCol = 6, kNSolve = 5, kNVert = 5, kNTile = 4;
 
 int group_of(const char *name) {
   if (!std::strcmp(name, "sound_solve")) return 1;
-  if (!std::strcmp(name, "adv_vertical")) return 2;
-  if (!std::strcmp(name, "adv_horizontal")) return 3;
+  if (!std::strcmp(name, "adv_vertical") || !std::strcmp(name, "adv_vertical_inc")) return 2;
+  if (!std::strcmp(name, "adv_horizontal") || !std::strcmp(name, "adv_horizontal_inc")) return 3;
   if (!std::strcmp(name, "bdy_ring") || !std::strcmp(name, "end_reduce")) return -1;
   return 0;  // column kernels
 }
@@ -1338,7 +1338,6 @@ int group_of(const char *name) {
 bool shapes_fit(const LaunchGeom &L) {
   const size_t col3 = (size_t)3 * (L.kz + 2) * sizeof(double);
   if (col3 * L.solve_x * L.solve_y > 200 * 1024) return false;
-  if ((size_t)6 * (L.kz + 2) * L.vert_x * sizeof(double) > 200 * 1024) return false;
   return L.col_x * L.col_y <= 1024 && L.vert_x * L.vert_y <= 1024;
 }
 
@@ -1420,7 +1419,7 @@ int autotune_impl(mlc_ctx *x, int steps, mlc_tune_report *rep) {
   }
   // the fixed configuration: 32 x 8 columns, tiles and vertical blocks, 32 x 2 solve
   LaunchGeom fixed = base;
-  set_shapes(fixed, 1, 0, 0, 0);
+  set_shapes(fixed, 1, 0, 1, 0);
   double msf[4] = {0, 0, 0, 0}, mst[4] = {0, 0, 0, 0};
   if (st == MLC_OK) {
     x->key.L = fixed;
@@ -1462,6 +1461,24 @@ int mlc_autotune(mlc_ctx *x, int steps, mlc_tune_report *rep) {
   if (!x || steps < 1) return MLC_ERR_INVALID;
   if (!ready(x)) return MLC_ERR_STATE;
   return x->mixed ? autotune_impl<float>(x, steps, rep) : autotune_impl<double>(x, steps, rep);
+}
+
+int mlc_set_launch_shapes(mlc_ctx *x, const mlc_tune_report *r) {
+  if (!x || !r) return MLC_ERR_INVALID;
+  auto find = [](const int (*cand)[2], int n, int a, int b) {
+    for (int q = 0; q < n; ++q)
+      if (cand[q][0] == a && cand[q][1] == b) return q;
+    return -1;
+  };
+  const int col = find(kColCand, kNCol, r->col_x, r->col_y);
+  const int solve = find(kSolveCand, kNSolve, r->solve_x, r->solve_y);
+  const int vert = find(kVertCand, kNVert, r->vert_x, r->vert_y);
+  if (col < 0 || solve < 0 || vert < 0 || r->htile < 0 || r->htile >= kNTile) return MLC_ERR_INVALID;
+  LaunchGeom L = x->key.L;
+  set_shapes(L, col, solve, vert, r->htile);
+  if (!shapes_fit(L)) return MLC_ERR_INVALID;
+  x->key.L = L;  // the graph is recorded again at the next step
+  return MLC_OK;
 }
 
 const char *mlc_last_error(void) { return g_last_error; }

@@ -139,8 +139,33 @@ struct Dom {
   // [horizontal tile shape][field], for the horizontal WAF's halo tiles
   const void *tmap;
 };
-constexpr int kTileShapes = 4;   // horizontal WAF tiles 32x8, 32x4, 64x4, 16x8
+constexpr int kTileShapes = 4;
 constexpr int kTmapBytes = 128;
+
+// Tile shapes of the horizontal WAF (LaunchGeom::htile).  A warp is one row
+// of 32*v columns, lane l holding columns v*l .. v*l+v-1; a block is nw rows.
+// Every warp computes its whole range and writes all but two columns at each
+// end (the zonal fluxes of a column need the intermediate field two columns
+// either side), so consecutive tiles overlap by four columns.
+//   FP32: 0 = 32x8, 1 = 64x8, 2 = 128x8, 3 = 128x4
+//   FP64: 0 = 32x8, 1 = 64x8, 2 = 64x4,  3 = 32x4
+struct HShape {
+  int v, nw;
+};
+__host__ __device__ constexpr HShape hshape(int elem_bytes, int idx) {
+  return elem_bytes == 4
+             ? (idx == 1 ? HShape{2, 8} : idx == 2 ? HShape{4, 8} : idx == 3 ? HShape{4, 4} : HShape{1, 8})
+             : (idx == 1 ? HShape{2, 8} : idx == 2 ? HShape{2, 4} : idx == 3 ? HShape{1, 4} : HShape{1, 8});
+}
+// Column offset (j - 1) of the first tile's first column: at most -2, so the
+// first written column is j <= 1, and a multiple of v (aligned lane vectors).
+__host__ __device__ constexpr int hshape_ob0(int v) { return -(v > 2 ? v : 2); }
+// Columns the halo tile's TMA box starts left of the warp range, so that the
+// copy starts on 16 bytes (tile offsets step by 32*v - 4, a multiple of 16
+// bytes); the box is 32*v + 2*off columns by nw + 4 rows.
+__host__ __device__ constexpr int hshape_off(int elem_bytes, int v) {
+  return ((hshape_ob0(v) % (16 / elem_bytes)) + 16 / elem_bytes) % (16 / elem_bytes);
+}
 
 // A per-domain constant in the kernel's field type: the FP64 value for an
 // FP64 member, its FP32 copy for a mixed one (no conversion on the device).
@@ -217,6 +242,7 @@ struct DF {
   size_t n;
   __device__ __forceinline__ DF(const double *a, size_t n_)
       : p(reinterpret_cast<float *>(const_cast<double *>(a))), n(n_) {}
+  __device__ __forceinline__ DF(float *p_, size_t n_) : p(p_), n(n_) {}
   __device__ __forceinline__ F2 ld(size_t o) const { return {p[o], p[o + n]}; }
   __device__ __forceinline__ void st(size_t o, F2 v) const { p[o] = v.hi; p[o + n] = v.lo; }
   __device__ __forceinline__ float hi(size_t o) const { return p[o]; }

@@ -20,7 +20,7 @@ struct LaunchGeom {
   int col_x, col_y;      // column kernels
   int solve_x, solve_y;  // sound_solve
   int vert_x, vert_y;    // adv_vertical
-  int htile;             // adv_horizontal tile: 0 32x8, 1 32x4, 2 64x4, 3 16x8
+  int htile;             // adv_horizontal tile shape (hshape)
   int nadv_r;            // advected fields of type R per member
   int nadv_d;            // advected FP64 fields per member (mixed: theta_v, Exner)
   int red_blocks;        // reduction blocks of the largest member
@@ -42,6 +42,10 @@ template <class R> struct Launch {
   static void adv_vertical(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
   static void adv_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                              cudaStream_t s);
+  // theta_v and Exner of a mixed member (double-float, increment form)
+  static void adv_vertical_inc(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
+  static void adv_horizontal_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                                 cudaStream_t s);
   static void adv_species_copy(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
   static void adv_curvature(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
   static void adv_back(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);

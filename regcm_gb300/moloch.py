@@ -70,6 +70,13 @@ class MolochDomain:
     def set_graphs(self, on: bool):
         abi.check(self.lib.mlc_set_graphs(self._ctx, 1 if on else 0), "mlc_set_graphs")
 
+    def autotune(self, steps_per_trial: int = 2) -> dict:
+        return _autotune(self.lib, self._ctx, steps_per_trial)
+
+    def set_launch_shapes(self, shapes: dict):
+        """Apply launch shapes (a dict as autotune returns; ms fields ignored)."""
+        _set_launch_shapes(self.lib, self._ctx, shapes)
+
     def close(self):
         if self._ctx:
             self.lib.mlc_destroy(self._ctx)
@@ -86,6 +93,25 @@ class MolochDomain:
             self.close()
         except Exception:
             pass
+
+
+def _autotune(lib, ctx, steps_per_trial):
+    rep = abi.mlc_tune_report()
+    abi.check(lib.mlc_autotune(ctx, steps_per_trial, C.byref(rep)), "autotune")
+    return rep.as_dict()
+
+
+# the fixed configuration the autotuner compares against
+DEFAULT_SHAPES = {"col_x": 32, "col_y": 4, "solve_x": 32, "solve_y": 2, "vert_x": 32, "vert_y": 4,
+                  "htile": 0}
+
+
+def _set_launch_shapes(lib, ctx, shapes):
+    rep = abi.mlc_tune_report()
+    for n, _ in rep._fields_:
+        if not n.startswith("ms_"):
+            setattr(rep, n, shapes.get(n, DEFAULT_SHAPES[n]))
+    abi.check(lib.mlc_set_launch_shapes(ctx, C.byref(rep)), "mlc_set_launch_shapes")
 
 
 _SHARED_PARAMS = ("dtsec", "dx", "mo_ztop", "mo_h", "mo_a0", "mo_nadv", "mo_nsound",
@@ -196,9 +222,11 @@ class MolochBatch:
         return self.lib.mlc_launches_per_step(self._ctx)
 
     def autotune(self, steps_per_trial: int = 2) -> dict:
-        rep = abi.mlc_tune_report()
-        abi.check(self.lib.mlc_autotune(self._ctx, steps_per_trial, C.byref(rep)), "autotune")
-        return rep.as_dict()
+        return _autotune(self.lib, self._ctx, steps_per_trial)
+
+    def set_launch_shapes(self, shapes: dict):
+        """Apply launch shapes (a dict as autotune returns; ms fields ignored)."""
+        _set_launch_shapes(self.lib, self._ctx, shapes)
 
     def close(self):
         if self._ctx:

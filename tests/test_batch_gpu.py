@@ -69,4 +69,7 @@ def test_autotune_keeps_state_and_results():
         b = plain.cases[m].empty_state()
         plain.download(m, plain.cases[m].state_ptrs_of(b))
         for n in a:
-            assert np.array_equal(a[n], b[n]), (m, n)
+            # the tuned tile shapes may round FP32 fields differently at a
+            # few points (tests/test_shapes_gpu.py); the state must be kept
+            d = np.abs(a[n] - b[n]).max()
+            assert d <= 2e-5 * np.abs(b[n]).max(), (m, n, d)

@@ -53,3 +53,36 @@ def test_mixed_hundred_steps(name, make):
     assert rel_l2(got["tetav"], ref["tetav"]) <= 1e-6
     # FP64 mass sums of the FP32 state: the dry-air mass agrees to FP32 rounding
     assert abs(dm.drymass - do.drymass) <= 1e-6 * abs(do.drymass)
+
+
+# Largest pointwise difference from the FP64 oracle after one step, relative
+# to the field's largest value (measured on these members: u 4e-7, v 4.1e-5
+# where v is small, w 4.2e-6, theta_v 1.2e-7, Exner 1.1e-8, qv 2.5e-7).  An
+# indexing error at a tile edge shows as differences of order the increments.
+ONE_STEP_MAX = {"u": 2e-6, "v": 2e-4, "w": 2e-5, "tetav": 1e-6, "pai": 1e-7, "qx": 2e-6}
+
+
+@pytest.mark.parametrize("htile", [0, 1, 2, 3])
+def test_mixed_one_step_pointwise(htile):
+    from regcm_gb300.moloch import DEFAULT_SHAPES, MolochBatch
+
+    def members(prec):
+        return ([cs.config3_member(m, scale=0.25, precision=prec) for m in (0, 2)] +
+                [cs.config3_member(6, scale=1.0, precision=prec)])
+
+    cases = members(abi.MLC_PREC_MIXED)
+    b = MolochBatch(cases)
+    b.set_launch_shapes(dict(DEFAULT_SHAPES, htile=htile))
+    b.step(1)
+    for m, (c, cf) in enumerate(zip(cases, members(abi.MLC_PREC_FP64))):
+        got = c.empty_state()
+        b.download(m, c.state_ptrs_of(got))
+        orc = Oracle(cf)
+        st, _ = orc.step(1)
+        assert st == 0
+        ref = orc.state()
+        orc.close()
+        for n, tol in ONE_STEP_MAX.items():
+            d = np.abs(got[n] - ref[n]).max() / np.abs(ref[n]).max()
+            assert d <= tol, (htile, m, n, d)
+    b.close()
