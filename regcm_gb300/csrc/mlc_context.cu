@@ -211,6 +211,9 @@ int validate_dims(const mlc_dims *d, const mlc_params *p) {
   // With these bounds (and at most kMaxSlots members) every grid dimension of
   // every launch stays within CUDA's limits (y and z below 65536).
   if (d->jx > kMaxExtent || d->iy > kMaxExtent) return MLC_ERR_TOO_LARGE;
+  // kernels index within one 3-D field with 32-bit offsets
+  if ((size_t)(d->jx + 32) * (size_t)d->iy * (size_t)(d->kz + 1) >= ((size_t)1 << 31))
+    return MLC_ERR_TOO_LARGE;
   if (d->nqx < 2 || d->nqx > 10 || d->ntr < 0 || d->ntr > 8) return MLC_ERR_INVALID;
   if (p->ipptls == 2 && d->nqx < 5) return MLC_ERR_INVALID;
   if (n_table_r(*d, *p, true) > kMaxFields) return MLC_ERR_UNSUPPORTED;
@@ -514,7 +517,7 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
     for (int n = 0; n < nsound; ++n) {
       const int uvoff = r * nsound + n;
       REC("sound_div", K::sound_div(L, d, uvoff, s)); ++nl;
-      REC("sound_solve", K::sound_solve(L, d, uvoff, r, n == nsound - 1, s)); nl += x->mixed ? 3 : 1;
+      REC("sound_solve", K::sound_solve(L, d, uvoff, r, n == nsound - 1, s)); ++nl;
       REC("sound_momentum", K::sound_momentum(L, d, uvoff, r, s)); ++nl;
     }
     // ---- advection (Main/mod_moloch.F90:767-1042) ----

@@ -234,159 +234,181 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
 }
 
 // The solve of a mixed member (same equations as k_sound_solve), in FP32
-// only, split at the recurrence so that only the Thomas recurrence runs column
-// by column.  Where rounding is amplified the values are double-floats: theta_v
-// at half levels, the hydrostatic balance -cp*theta_v*fmzf*dtrdz*(pai(k-1) -
-// pai(k)) - g*dts of the w equation (two terms of ~g*dts whose difference
-// drives w), and the Exner update pai - pai*increment.  The divergence filter,
-// the elimination coefficients (O(1)-conditioned), the recurrence and the back
-// substitution run in plain FP32.  Scratch (free during the acoustic
-// loop): wz[2] theta_v(k-1) - theta_v(k) from sound_prep; the FP32 planes of
-// wz_d[0] hold zf and the explicit w, those of wz_d[1] the coefficients zu
-// and zd (zu is overwritten by the elimination multipliers).
+// only, one thread per column.  Where rounding is amplified the values are
+// double-floats: theta_v at half levels, the hydrostatic balance
+// -cp*theta_v*fmzf*dtrdz*(pai(k-1) - pai(k)) - g*dts of the w equation (two
+// terms of ~g*dts whose difference drives w), and the Exner update
+// pai - pai*increment.  The divergence filter, the elimination coefficients
+// (O(1)-conditioned), the recurrence and the back substitution run in plain
+// FP32.  The downward pass forms each level's coefficients and eliminates at
+// once; the upward pass substitutes back and updates Exner (and, after the
+// last substep, s) a level behind.  Between the passes the column's
+// eliminated w stays in w, its multipliers and filtered divergence in the
+// FP32 planes of wz_d[1] and wz_d[0] (free during the acoustic loop; a
+// column's two passes follow each other closely, so these round trips stay in
+// L2).  wz[2] holds theta_v(k-1) - theta_v(k) from sound_prep.
 template <class R>
-struct SolveScratch {
-  float *zf, *zw, *zu, *zd;
-  __device__ __forceinline__ SolveScratch(const Dom<R> &D, size_t F)
-      : zf(reinterpret_cast<float *>(D.wz_d[0])), zw(zf + F),
-        zu(reinterpret_cast<float *>(D.wz_d[1])), zd(zu + F) {}
-};
-
-// Level-parallel part 1: the filtered divergence zf and, per level 2..kz,
-// theta_v at the half level, the explicit w and the coefficients zu, zd.
-template <class R>
-__global__ void k_solve_coef(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
+__global__ void k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
-  const Pt q = point_of(tiles_j, 2, 2);
-  const int j = q.j, i = q.i, kz = g.kz;
-  if (j > g.jx - 2 || i > g.iy - 2 || q.k > kz) return;
+  const int j = (int)(blockIdx.x * blockDim.x + threadIdx.x) + 2;
+  const int i = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
+  if (j > g.jx - 2 || i > g.iy - 2) return;
+  const int kz = g.kz;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const int adv = (D.clk->adv_role + advoff) & 1;
-  const R *__restrict__ zraw = D.zdiv2;
-  const R *__restrict__ s = D.s;
-  const R *__restrict__ w = D.w;
-  const size_t PS = g.PS, F = g.field3(), F1 = PS * (size_t)(kz + 1);
-  const DF pai(D.pai[adv], F), tvf_a(D.tetavf, F1), cfz(sa.cfz, F1);
-  const SolveScratch<R> sc(D, F);
-  const float *__restrict__ dtet = D.wz[2];
+  const size_t F = g.field3(), F1 = g.PS * (size_t)(kz + 1);
+  const size_t ij = g.at2(j, i);
+  // offsets from the column's own point, signed (the divergence filter reads
+  // the neighbours at level 1 below the column's offset); every plane is a
+  // separate array, so loads of the next level may pass this level's stores
+  const int PS = (int)g.PS, P = g.P;
+  float *__restrict__ pai_h = reinterpret_cast<float *>(D.pai[adv]) + ij;
+  float *__restrict__ pai_l = pai_h + F;
+  float *__restrict__ tvf_h = reinterpret_cast<float *>(D.tetavf) + ij;
+  float *__restrict__ tvf_l = tvf_h + F1;
+  const float *__restrict__ cfz_h = reinterpret_cast<const float *>(sa.cfz) + ij;
+  const float *__restrict__ cfz_l = cfz_h + F1;
+  float *__restrict__ zfs = reinterpret_cast<float *>(D.wz_d[0]) + ij;
+  float *__restrict__ mul = reinterpret_cast<float *>(D.wz_d[1]) + ij;
+  const float *__restrict__ zraw = D.zdiv2 + ij;
+  const float *__restrict__ dtet = D.wz[2] + ij;
+  const float *__restrict__ fmz = sa.fmz + ij;
+  const float *__restrict__ fmzf = sa.fmzf + ij;
+  float *__restrict__ s = D.s + ij;
+  float *__restrict__ w = D.w + ij;
   const float dtrdz = c.dtsoundf * c.rdzitaf;
   const float rdrcv = float(kRdrcv);
   const float rdt = rdrcv * dtrdz;
   const F2 ngdts{-c.gdts_hi, -c.gdts_lo};
-  const size_t ij = g.at2(j, i), P = (size_t)g.P;
   const int32_t ib = sa.ibnd_cr[ij];
   const int nsp = c.nspgx;
-  // divergence_diffusion plus the vertical divergence (:531-543, :627-630)
-  auto zf_at = [&](int k) -> float {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    float z = float(zraw[o]);
-    if (c.divfilter) {
-      const float lap = (float(zraw[o - 1]) + float(zraw[o + 1]) + float(zraw[o - P]) +
-                         float(zraw[o + P]) - 4.f * z);
-      z = z + sa.xknu_r[k - 1] * lap;
-    }
-    const float bw = ib > 0 ? 1.f - sa.hefc_r[(size_t)(ib - 1) + (size_t)(k - 1) * nsp] : 1.f;
-    return z + bw * dtrdz * float(sa.fmz[o]) * (float(s[o]) - float(s[o + PS]));
+  const bool filt = c.divfilter != 0;
+
+  // per level m: the raw divergence with its filter stencil, s, fmz and
+  // Exner (the cell below the interface of level m+1) ...
+  struct LvA {
+    float z, lap, s, fmz;
+    F2 pai;
   };
-  float zf_m = q.k >= 2 ? zf_at(q.k - 1) : 0.f;
-#pragma unroll
-  for (int k = q.k; k < q.k + kPtLevels && k <= kz; ++k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    const float zfk = zf_at(k);
-    sc.zf[o] = zfk;
-    if (k >= 2) {
-      const F2 pai_m = pai.ld(o - PS), pai_k = pai.ld(o);
-      const float wold = float(w[o]);
-      const float corr = wold * float(sa.fmzf[o]) * dtrdz * dtet[o];
-      const F2 tvf = df_add_f(tvf_a.ld(o), -corr);
-      tvf_a.st(o, tvf);
-      const F2 zrd = df_mul(tvf, cfz.ld(o));
-      const F2 dp = two_sum(pai_m.hi - pai_k.hi, pai_m.lo - pai_k.lo);  // hi difference exact
-      const F2 bal = df_add(ngdts, df_mul(F2{-zrd.hi, -zrd.lo}, dp));
-      const float zr = df_f(zrd), pm = df_f(pai_m), pk = df_f(pai_k);
-      float zw = wold + df_f(bal);
-      zw = zw + rdrcv * zr * (pm * zf_m - pk * zfk);
-      const float ff = sa.ffilt_r[k - 1];
-      sc.zw[o] = zw;
-      sc.zu[o] = rdt * float(sa.fmz[o - PS]) * zr * pm + ff;
-      sc.zd[o] = rdt * float(sa.fmz[o]) * zr * pk + ff;
-    }
-    zf_m = zfk;
-  }
-}
+  auto loadA = [&](int m) {
+    const int o = (m - 1) * PS;
+    LvA a;
+    a.z = zraw[o];
+    a.lap = filt ? (zraw[o - 1] + zraw[o + 1] + zraw[o - P] + zraw[o + P] - 4.f * a.z) : 0.f;
+    a.s = s[o];
+    a.fmz = fmz[o];
+    a.pai = F2{pai_h[o], pai_l[o]};
+    return a;
+  };
+  // ... and what the w equation of level m reads at its own interface
+  struct LvB {
+    float w, fmzf, dtet;
+    F2 tvf, cfz;
+  };
+  auto loadB = [&](int m) {
+    const int o = (m - 1) * PS;
+    LvB b;
+    b.w = w[o];
+    b.fmzf = fmzf[o];
+    b.dtet = dtet[o];
+    b.tvf = F2{tvf_h[o], tvf_l[o]};
+    b.cfz = F2{cfz_h[o], cfz_l[o]};
+    return b;
+  };
+  // divergence_diffusion plus the vertical divergence (:531-543, :627-630)
+  auto zf_of = [&](int m, const LvA &a, float s_above) {
+    float z = a.z;
+    if (filt) z = z + sa.xknu_r[m - 1] * a.lap;
+    const float bw = ib > 0 ? 1.f - sa.hefc_r[(size_t)(ib - 1) + (size_t)(m - 1) * nsp] : 1.f;
+    return z + bw * dtrdz * a.fmz * (a.s - s_above);
+  };
 
-// Part 2, per column: elimination k = kz..2 (:634-656) and back substitution
-// (:660-664); the new w replaces the old one, the multipliers replace zu.
-template <class R>
-__global__ void k_solve_sweep(const Dom<R> *__restrict__ doms) {
-  const Dom<R> &D = doms[blockIdx.z];
-  if (!D.active) return;
-  const Geom g = D.g;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  if (j > g.jx - 2 || i > g.iy - 2) return;
-  const int kz = g.kz;
-  const size_t PS = g.PS, F = g.field3();
-  const SolveScratch<R> sc(D, F);
-  R *__restrict__ w = D.w;
-  const size_t ij = g.at2(j, i);
-  float wnext = float(w[ij + (size_t)kz * PS]);
+  // downward: coefficients of level k and elimination k = kz..2 (:634-656)
+  float wnext = w[kz * PS];  // w(kz+1) = -s(kz+1)
   float wkp1 = 0.f;
-#pragma unroll 4
+  LvA ak = loadA(kz);         // level k
+  float zfk = zf_of(kz, ak, s[kz * PS]);
+  LvA am = loadA(kz - 1);     // level k-1
+  LvB bk = loadB(kz);         // level k
   for (int k = kz; k >= 2; --k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    const float zu = sc.zu[o], zd = sc.zd[o];
+    const int o = (k - 1) * PS;
+    // next level's loads, in flight during this level
+    LvA an{};
+    LvB bn{};
+    if (k >= 3) {
+      an = loadA(k - 2);
+      bn = loadB(k - 1);
+    }
+    const float zf_m = zf_of(k - 1, am, ak.s);
+    zfs[o] = zfk;
+    const F2 pai_m = am.pai, pai_k = ak.pai;
+    const float wold = bk.w;
+    const float corr = wold * bk.fmzf * dtrdz * bk.dtet;
+    const F2 tvf = df_add_f(bk.tvf, -corr);
+    tvf_h[o] = tvf.hi;
+    tvf_l[o] = tvf.lo;
+    const F2 zrd = df_mul(tvf, bk.cfz);
+    const F2 dp = two_sum(pai_m.hi - pai_k.hi, pai_m.lo - pai_k.lo);  // hi difference exact
+    const F2 bal = df_add(ngdts, df_mul(F2{-zrd.hi, -zrd.lo}, dp));
+    const float zr = df_f(zrd), pm = df_f(pai_m), pk = df_f(pai_k);
+    float zw = wold + df_f(bal);
+    zw = zw + rdrcv * zr * (pm * zf_m - pk * zfk);
+    const float ff = sa.ffilt_r[k - 1];
+    const float zu = rdt * am.fmz * zr * pm + ff;
+    const float zd = rdt * ak.fmz * zr * pk + ff;
     const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
-    wnext = zrapp * (sc.zw[o] + zd * wnext);
+    wnext = zrapp * (zw + zd * wnext);
     wkp1 = zrapp * zu;
-    w[o] = (R)wnext;
-    sc.zu[o] = wkp1;
+    w[o] = wnext;
+    mul[o] = wkp1;
+    zfk = zf_m;
+    ak = am;
+    am = an;
+    bk = bn;
   }
-  float wprev = float(w[ij]);
-#pragma unroll 4
-  for (int k = 2; k <= kz; ++k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    wprev = float(w[o]) + sc.zu[o] * wprev;
-    w[o] = (R)wprev;
-  }
-}
-
-// Part 3, level-parallel: the Exner update (:668-671) and, after the last
-// substep, the completed s (:728-734).
-template <class R>
-__global__ void k_solve_exner(const Dom<R> *__restrict__ doms, int advoff, int last, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
-  if (!D.active) return;
-  const Geom g = D.g;
-  const Pt q = point_of(tiles_j, 2, 2);
-  const int j = q.j, i = q.i, kz = g.kz;
-  if (j > g.jx - 2 || i > g.iy - 2 || q.k > kz) return;
-  const Scal &c = D.c;
-  const Stat<R> &sa = D.sa;
-  const int adv = (D.clk->adv_role + advoff) & 1;
-  const size_t PS = g.PS, F = g.field3();
-  const DF pai(D.pai[adv], F);
-  const SolveScratch<R> sc(D, F);
-  const R *__restrict__ w = D.w;
-  R *__restrict__ s = D.s;
-  const float dtrdz = c.dtsoundf * c.rdzitaf;
-  const float rdrcv = float(kRdrcv);
-  const size_t ij = g.at2(j, i);
-#pragma unroll
-  for (int k = q.k; k < q.k + kPtLevels && k <= kz; ++k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    const F2 pk = pai.ld(o);
-    const float inc = rdrcv * (sc.zf[o] + (dtrdz * float(sa.fmz[o]) * (float(w[o]) - float(w[o + PS]))));
+  zfs[0] = zfk;  // level 1
+  // upward: back substitution k = 2..kz (:660-664), the Exner function
+  // (:668-671) and s (:728-734) of level k-1 once w(k) is known
+  auto exner = [&](int m, float wm, float wmp, F2 pk, float zf, float fz, float sm, float fzf) {
+    const int o = (m - 1) * PS;
+    const float inc = rdrcv * (zf + (dtrdz * fz * (wm - wmp)));
     const F2 d = df_mul_f(pk, inc);
-    pai.st(o, df_add(pk, F2{-d.hi, -d.lo}));
-    if (last && k >= 2) s[o] = (R)((float(w[o]) + float(s[o])) * float(sa.fmzf[o]));
+    const F2 pn = df_add(pk, F2{-d.hi, -d.lo});
+    pai_h[o] = pn.hi;
+    pai_l[o] = pn.lo;
+    if (last && m >= 2) s[o] = (wm + sm) * fzf;
+  };
+  float wprev = w[0];  // w(1) = 0
+  // level m's Exner inputs, loaded a level ahead
+  F2 ep = F2{pai_h[0], pai_l[0]};
+  float ezf = zfs[0], efz = fmz[0], es = s[0], efzf = fmzf[0];
+  float nw = w[PS], nmul = mul[PS];
+  for (int k = 2; k <= kz; ++k) {
+    const int o = (k - 1) * PS;
+    const float wel = nw, mk = nmul;
+    const F2 cp = ep;
+    const float czf = ezf, cfz_ = efz, cs = es, cfzf = efzf;
+    if (k < kz) {
+      nw = w[o + PS];
+      nmul = mul[o + PS];
+    }
+    ep = F2{pai_h[o], pai_l[o]};
+    ezf = zfs[o];
+    efz = fmz[o];
+    es = s[o];
+    efzf = fmzf[o];
+    const float wk = wel + mk * wprev;
+    w[o] = wk;
+    exner(k - 1, wprev, wk, cp, czf, cfz_, cs, cfzf);
+    wprev = wk;
   }
-  if (last && q.k == 1) {
-    s[ij] = R(0);
-    s[ij + (size_t)kz * PS] = R(0);
+  exner(kz, wprev, w[kz * PS], ep, ezf, efz, es, efzf);
+  if (last) {
+    s[0] = 0.f;
+    s[kz * PS] = 0.f;
   }
 }
 
@@ -527,12 +549,7 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
                  (unsigned)L.nmem);
   const size_t cols = (size_t)3 * (L.kz + 2) * blk.x * blk.y;
   if constexpr (sizeof(R) == sizeof(float)) {
-    // coefficients and Exner update level-parallel, the recurrence per column
-    int tj;
-    const dim3 pg = pt_grid(L, L.jx - 3, L.iy - 3, tj);
-    k_solve_coef<R><<<pg, col_block(L), 0, s>>>(d, advoff, tj);
-    k_solve_sweep<R><<<grd, blk, 0, s>>>(d);
-    k_solve_exner<R><<<pg, col_block(L), 0, s>>>(d, advoff, last ? 1 : 0, tj);
+    k_solve_mixed<R><<<grd, blk, 0, s>>>(d, advoff, last ? 1 : 0);
   } else {
     k_sound_solve<R><<<grd, blk, cols * sizeof(double), s>>>(d, advoff, last ? 1 : 0);
   }
