@@ -181,7 +181,6 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
     b.xpsb[h] = cv.take<double>(P2);
   }
   D.red_blocks = reduce_blocks(g);
-  D.rows_per_block = reduce_rows_per_block(g);
   D.partials = cv.take<double>((size_t)D.red_blocks * 8);
   D.tmap = cv.take<char>((size_t)kTileShapes * kMaxFields * kTmapBytes);
 }

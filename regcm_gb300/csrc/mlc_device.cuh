@@ -133,7 +133,7 @@ struct Dom {
   Clock *clk;
   DiagDev *diag;
   double *partials;
-  int red_blocks, rows_per_block;
+  int red_blocks;
   int active;            // 0: an empty slot, every block returns at once
   // TMA tensor maps (CUtensorMap, 128 B each, 64-B aligned) of the wz fields,
   // [horizontal tile shape][field], for the horizontal WAF's halo tiles

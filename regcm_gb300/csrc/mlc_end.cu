@@ -10,6 +10,8 @@
 // the reference advances it by dtsec (Main/mod_bdycod.F90:2653) before
 // motopnudge and morelax blend again, so those read xbctime + dtsec; the
 // final reduction kernel stores the advanced clock.
+#include <algorithm>
+
 #include "mlc_kernels.cuh"
 
 namespace mlc {
@@ -180,7 +182,7 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const int j = q_.j, k0 = q_.k;
   if (k0 > g.kz) return;
   const int i = q_.i;
-  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  const int jx = g.jx, iy = g.iy;
   if (j > jx - 1 || i > iy - 1) return;
   const double xb = clk->xbctime + c.dtsec;
   const double x1 = (xb + c.dt) * c.rtb;
@@ -440,140 +442,165 @@ constexpr int kRedThreads = 256;
 constexpr int kRedWarps = kRedThreads / 32;
 constexpr int kNPart = 7;  // dry, dryadv, qmass, qadv, ps max, ps min, non-finite flag
 
-// One warp per row (i, k): lanes stride along j, the rows of a block go to its
-// warps in turn; warp sums by shuffles, then the warps' sums in warp order.
+// dz of the member's field type (the FP32 copy for a mixed member)
+template <class R>
+__device__ __forceinline__ const R *pick_dz(const Stat<R> &sa) {
+  if constexpr (sizeof(R) == sizeof(float)) return sa.dz_r;
+  else return sa.dz;
+}
+// 16 bytes at p (16-byte aligned) as V elements
+template <class R, int V>
+__device__ __forceinline__ void ld_vec16(R (&x)[V], const R *p) {
+  const uint4 w = *reinterpret_cast<const uint4 *>(p);
+  memcpy(x, &w, 16);
+}
+
+// Partial sums of the mass budget (Main/mod_massck.F90:57-369) and the ps
+// extrema of one member, per block.  The interior sums run over the member's
+// 3-D arrays as flat vectors of 16 bytes (every row starts on 128 bytes, so a
+// vector never straddles a row); a grid-stride loop over the vectors keeps
+// many loads in flight.  The species of a point are summed before they are
+// weighted by its dry mass dx^2*dz*rho.  FP32 members form the point products
+// in FP32, add each vector's in FP32 and accumulate them as double-floats;
+// dx^2 is applied once per thread.  The lateral fluxes and the ps extrema
+// are grid-stride loops over their own items.  Sums are in a fixed order for
+// a given member, whatever else the launch holds.
 template <class R>
 __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__restrict__ doms,
                                                                 int uvoff, int advoff) {
   __shared__ double sh[kRedWarps][kNPart];
   const Dom<R> &D = doms[blockIdx.y];
   if (!D.active) return;
-  if ((int)blockIdx.x >= D.red_blocks) return;
+  const int nb = D.red_blocks;
+  if ((int)blockIdx.x >= nb) return;
   const Geom g = D.g;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
-  double *part = D.partials;
-  const int rows_per_block = D.rows_per_block;
-  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  const int jx = g.jx, iy = g.iy, kz = g.kz, nqx = g.nqx;
   const double dx = c.dx, dt = c.dt, dxsq = dx * dx;
   const size_t F = g.field3();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned gt = blockIdx.x * kRedThreads + threadIdx.x;  // this thread's first item
+  const unsigned gs = (unsigned)nb * kRedThreads;              // stride
   double dry = 0, dadv = 0, qm = 0, qadv = 0, pmax = -INFINITY, pmin = INFINITY, bad = 0;
-  F2 dry2{0.f, 0.f}, qm2{0.f, 0.f}, dadv2{0.f, 0.f}, qadv2{0.f, 0.f};
-  bool lanes_used = false;  // lanes other than 0 hold boundary-flux or ps partials
-  const int nrows = (iy - 1) * kz;  // rows (i in ice, k)
-  const int r0 = blockIdx.x * rows_per_block;
   const bool budget = c.debug_level > 0;
-  for (int r = r0 + warp; r < min(r0 + rows_per_block, nrows); r += kRedWarps) {
-    const int i = r % (iy - 1) + 1, k = r / (iy - 1) + 1;
-    const size_t ko = (size_t)(k - 1) * g.PS;
-    if (budget && i >= 2 && i <= iy - 2) {
+  if (budget) {
+    constexpr int V = 16 / (int)sizeof(R);
+    const unsigned nvec = (unsigned)(g.PS * (size_t)kz) / V;  // below 2^31 / V
+    const unsigned P = (unsigned)g.P;
+    const R *__restrict__ dzp = pick_dz<R>(sa);
+    F2 dry2{0.f, 0.f}, qm2{0.f, 0.f};
+    for (unsigned v = gt; v < nvec; v += gs) {
+      const unsigned base = v * V;
+      const unsigned r = base / P;               // (i-1) + (k-1)*iy
+      const int c0 = (int)(base - r * P);        // j-1 of the vector's first element
+      const int i = (int)(r % (unsigned)iy) + 1;
+      if (i < 2 || i > iy - 2 || c0 + 1 > jx - 2) continue;
+      R dz[V], rh[V], qs[V], q1[V];
+      ld_vec16<R, V>(dz, dzp + base);
+      ld_vec16<R, V>(rh, st.rho + base);
+      ld_vec16<R, V>(qs, st.qx + base);
+      for (int n = 1; n < nqx; ++n) {
+        ld_vec16<R, V>(q1, st.qx + base + (size_t)n * F);
+#pragma unroll
+        for (int q = 0; q < V; ++q) qs[q] += q1[q];
+      }
       if constexpr (sizeof(R) == sizeof(float)) {
-        // FP32 fields: FP32 point products, compensated FP32 sums (double-
-        // float), dx^2 applied once below
-        for (int j = 2 + lane; j <= jx - 2; j += 32) {
-          const size_t o = g.at2(j, i) + ko;
-          const float dr = sa.dz_r[o] * st.rho[o];
-          float qs = 0.f;
-          for (int n = 0; n < g.nqx; ++n) qs += st.qx[o + (size_t)n * F];
-          dry2 = df_add_f(dry2, dr);
-          qm2 = df_add_f(qm2, dr * qs);
+        float sd = 0.f, sq = 0.f;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          const int j = c0 + q + 1;
+          const float dr = (j >= 2 && j <= jx - 2) ? dz[q] * rh[q] : 0.f;
+          sd += dr;
+          sq += dr * qs[q];
         }
+        dry2 = df_add_f(dry2, sd);
+        qm2 = df_add_f(qm2, sq);
       } else {
-        for (int j = 2 + lane; j <= jx - 2; j += 32) {
-          const size_t o = g.at2(j, i) + ko;
-          const double dzr = (double)sa.dz[o];
-          const double rh = (double)st.rho[o];
-          dry += dxsq * dzr * rh;
-          for (int n = 0; n < g.nqx; ++n) qm += (double)st.qx[o + (size_t)n * F] * dxsq * dzr * rh;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          const int j = c0 + q + 1;
+          if (j >= 2 && j <= jx - 2) {
+            const double wpt = dxsq * (double)dz[q] * (double)rh[q];
+            dry += wpt;
+            qm += (double)qs[q] * wpt;
+          }
         }
       }
     }
     if constexpr (sizeof(R) == sizeof(float)) {
-      if (budget && lane == 0) {
-        // west and east columns (FP32 products, double-float sums)
-        const size_t ow = g.at2(1, i) + ko, oe = g.at2(jx - 1, i) + ko;
+      dry = ((double)dry2.hi + (double)dry2.lo) * dxsq;
+      qm = ((double)qm2.hi + (double)qm2.lo) * dxsq;
+    }
+    // west and east columns over i in ice = 1 .. iy-1 (:85-100)
+    const unsigned nwe = (unsigned)((iy - 1) * kz);
+    for (unsigned e = gt; e < nwe; e += gs) {
+      const int i = (int)(e % (unsigned)(iy - 1)) + 1, k = (int)(e / (unsigned)(iy - 1)) + 1;
+      const size_t ko = (size_t)(k - 1) * g.PS;
+      const size_t ow = g.at2(1, i) + ko, oe = g.at2(jx - 1, i) + ko;
+      if constexpr (sizeof(R) == sizeof(float)) {
+        // FP32 products, summed in FP64
         const float dtdx = float(dt * dx);
         const float fw = st.u[g.at2(1, i) + ko] * dtdx * sa.dz_r[ow] * st.rho[ow];
         const float fe = st.u[g.at2(jx, i) + ko] * dtdx * sa.dz_r[oe] * st.rho[oe];
-        dadv2 = df_add_f(df_add_f(dadv2, fw), -fe);
         float qw = 0.f, qe = 0.f;
-        for (int n = 0; n < g.nqx; ++n) {
+        for (int n = 0; n < nqx; ++n) {
           qw += st.qx[ow + (size_t)n * F];
           qe += st.qx[oe + (size_t)n * F];
         }
-        qadv2 = df_add_f(df_add_f(qadv2, qw * fw), -(qe * fe));
-      }
-    } else if (budget && lane == 0) {
-      // west and east columns over i in ice (Main/mod_massck.F90:85-100)
-      const size_t ow = g.at2(1, i) + ko, oe = g.at2(jx - 1, i) + ko;
-      const double uw = (double)st.u[g.at2(1, i) + ko], ue = (double)st.u[g.at2(jx, i) + ko];
-      const double dzw = (double)sa.dz[ow], rw = (double)st.rho[ow];
-      const double dze = (double)sa.dz[oe], re = (double)st.rho[oe];
-      dadv += uw * dt * dx * dzw * rw;
-      dadv -= ue * dt * dx * dze * re;
-      for (int n = 0; n < g.nqx; ++n) {
-        qadv += (double)st.qx[ow + (size_t)n * F] * uw * dt * dx * dzw * rw;
-        qadv -= (double)st.qx[oe + (size_t)n * F] * ue * dt * dx * dze * re;
-      }
-    }
-    if (budget && (i == 1 || i == iy - 1)) {
-      lanes_used = true;
-      // south (v at ide1) and north (v at ide2) rows, j in jci (:101-116)
-      const int iv = (i == 1) ? 1 : iy;
-      const bool south = (i == 1);
-      for (int j = 2 + lane; j <= jx - 2; j += 32) {
-        const size_t o = g.at2(j, i) + ko;
-        const double vv = (double)st.v[g.at2(j, iv) + ko];
-        const double dzr = (double)sa.dz[o], rh = (double)st.rho[o];
-        const double fl = vv * dt * dx * dzr * rh;
-        dadv = south ? dadv + fl : dadv - fl;
-        for (int n = 0; n < g.nqx; ++n) {
-          const double q = (double)st.qx[o + (size_t)n * F] * vv * dt * dx * dzr * rh;
-          qadv = south ? qadv + q : qadv - q;
+        dadv += (double)fw - (double)fe;
+        qadv += (double)(qw * fw) - (double)(qe * fe);
+      } else {
+        const double uw = (double)st.u[g.at2(1, i) + ko], ue = (double)st.u[g.at2(jx, i) + ko];
+        const double dzw = (double)sa.dz[ow], rw = (double)st.rho[ow];
+        const double dze = (double)sa.dz[oe], re = (double)st.rho[oe];
+        dadv += uw * dt * dx * dzw * rw;
+        dadv -= ue * dt * dx * dze * re;
+        for (int n = 0; n < nqx; ++n) {
+          qadv += (double)st.qx[ow + (size_t)n * F] * uw * dt * dx * dzw * rw;
+          qadv -= (double)st.qx[oe + (size_t)n * F] * ue * dt * dx * dze * re;
         }
       }
     }
-    if (k == 1 && i >= 2 && i <= iy - 2) {
-      lanes_used = true;
-      for (int j = 2 + lane; j <= jx - 2; j += 32) {
-        const double x = st.ps[g.at2(j, i)];
-        if (!isfinite(x)) bad = 1;
-        else { pmax = fmax(pmax, x); pmin = fmin(pmin, x); }
+    // south (v at ide1) and north (v at ide2) rows, j in jci (:101-116)
+    const unsigned nsn = (unsigned)(2 * kz * (jx - 3));
+    for (unsigned e = gt; e < nsn; e += gs) {
+      const int j = (int)(e % (unsigned)(jx - 3)) + 2;
+      const unsigned rest = e / (unsigned)(jx - 3);
+      const bool south = (rest & 1u) == 0;
+      const int k = (int)(rest >> 1) + 1;
+      const int i = south ? 1 : iy - 1, iv = south ? 1 : iy;
+      const size_t ko = (size_t)(k - 1) * g.PS;
+      const size_t o = g.at2(j, i) + ko;
+      const double vv = (double)st.v[g.at2(j, iv) + ko];
+      const double dzr = (double)sa.dz[o], rh = (double)st.rho[o];
+      const double fl = vv * dt * dx * dzr * rh;
+      dadv = south ? dadv + fl : dadv - fl;
+      for (int n = 0; n < nqx; ++n) {
+        const double q = (double)st.qx[o + (size_t)n * F] * vv * dt * dx * dzr * rh;
+        qadv = south ? qadv + q : qadv - q;
       }
     }
   }
+  // ps extrema over the interior
+  const unsigned nps = (unsigned)((iy - 3) * (jx - 3));
+  for (unsigned e = gt; e < nps; e += gs) {
+    const int j = (int)(e % (unsigned)(jx - 3)) + 2, i = (int)(e / (unsigned)(jx - 3)) + 2;
+    const double x = st.ps[g.at2(j, i)];
+    if (!isfinite(x)) bad = 1;
+    else { pmax = fmax(pmax, x); pmin = fmin(pmin, x); }
+  }
   const unsigned full = 0xffffffffu;
-  if constexpr (sizeof(R) == sizeof(float)) {
-    // warp sums of the double-float partials in FP32, then dx^2 in FP64 once
-    for (int off = 16; off > 0; off >>= 1) {
-      dry2 = df_add(dry2, F2{__shfl_down_sync(full, dry2.hi, off), __shfl_down_sync(full, dry2.lo, off)});
-      qm2 = df_add(qm2, F2{__shfl_down_sync(full, qm2.hi, off), __shfl_down_sync(full, qm2.lo, off)});
-    }
-    if (lane == 0) {
-      dry = ((double)dry2.hi + (double)dry2.lo) * dxsq;
-      qm = ((double)qm2.hi + (double)qm2.lo) * dxsq;
-      dadv += (double)dadv2.hi + (double)dadv2.lo;
-      qadv += (double)qadv2.hi + (double)qadv2.lo;
-    }
-  } else {
-    for (int off = 16; off > 0; off >>= 1) {
-      dry += __shfl_down_sync(full, dry, off);
-      qm += __shfl_down_sync(full, qm, off);
-    }
+  for (int off = 16; off > 0; off >>= 1) {
+    dry += __shfl_down_sync(full, dry, off);
+    qm += __shfl_down_sync(full, qm, off);
+    dadv += __shfl_down_sync(full, dadv, off);
+    qadv += __shfl_down_sync(full, qadv, off);
+    bad += __shfl_down_sync(full, bad, off);
+    pmax = fmax(pmax, __shfl_down_sync(full, pmax, off));
+    pmin = fmin(pmin, __shfl_down_sync(full, pmin, off));
   }
-  // the boundary fluxes and ps extrema live in lane 0 unless the warp had a
-  // south/north row or the surface row
-  if (__any_sync(full, lanes_used)) {
-    for (int off = 16; off > 0; off >>= 1) {
-      dadv += __shfl_down_sync(full, dadv, off);
-      qadv += __shfl_down_sync(full, qadv, off);
-      bad += __shfl_down_sync(full, bad, off);
-      pmax = fmax(pmax, __shfl_down_sync(full, pmax, off));
-      pmin = fmin(pmin, __shfl_down_sync(full, pmin, off));
-    }
-  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) {
     sh[warp][0] = dry; sh[warp][1] = dadv; sh[warp][2] = qm; sh[warp][3] = qadv;
     sh[warp][4] = pmax; sh[warp][5] = pmin; sh[warp][6] = bad;
@@ -585,39 +612,46 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
       a[0] += sh[w][0]; a[1] += sh[w][1]; a[2] += sh[w][2]; a[3] += sh[w][3];
       a[4] = fmax(a[4], sh[w][4]); a[5] = fmin(a[5], sh[w][5]); a[6] += sh[w][6];
     }
-    double *p = part + (size_t)blockIdx.x * kNPart;
+    double *p = D.partials + (size_t)blockIdx.x * kNPart;
     for (int q = 0; q < kNPart; ++q) p[q] = a[q];
   }
 }
 
-// Per member: add the partials in block order, store the diagnostics, then
-// advance the boundary clock and the buffer roles to the next step's.
+// Per member: add the partials (lanes stride over the blocks, then a fixed
+// shuffle tree), store the diagnostics, then advance the boundary clock and
+// the buffer roles to the next step's.
 template <class R>
 __global__ void k_reduce_final(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
-  if (threadIdx.x != 0) return;
   const Dom<R> &D = doms[blockIdx.x];
   if (!D.active) return;
   const double *part = D.partials;
   const int nblocks = D.red_blocks;
-  DiagDev *diag = D.diag;
-  Clock *clk = D.clk;
-  const double dtsec = D.c.dtsec;
-  const int apply_bdy = D.c.apply_bdy;
-  double a[4] = {0, 0, 0, 0}, pmax = -INFINITY, pmin = INFINITY;
-  bool bad = false;
-  for (int b = 0; b < nblocks; ++b) {
+  const int lane = threadIdx.x;
+  double a[4] = {0, 0, 0, 0}, pmax = -INFINITY, pmin = INFINITY, bad = 0;
+  for (int b = lane; b < nblocks; b += 32) {
     const double *p = part + (size_t)b * kNPart;
     for (int q = 0; q < 4; ++q) a[q] += p[q];
     pmax = fmax(pmax, p[4]);
     pmin = fmin(pmin, p[5]);
-    if (p[6] != 0.0) bad = true;
+    bad += p[6];
   }
+  const unsigned full = 0xffffffffu;
+  for (int off = 16; off > 0; off >>= 1) {
+    for (int q = 0; q < 4; ++q) a[q] += __shfl_down_sync(full, a[q], off);
+    pmax = fmax(pmax, __shfl_down_sync(full, pmax, off));
+    pmin = fmin(pmin, __shfl_down_sync(full, pmin, off));
+    bad += __shfl_down_sync(full, bad, off);
+  }
+  if (lane != 0) return;
+  DiagDev *diag = D.diag;
+  Clock *clk = D.clk;
+  const bool isbad = bad != 0.0;
   diag->drymass = a[0]; diag->dryadv = a[1]; diag->qmass = a[2]; diag->qadv = a[3];
-  diag->ps_max = bad ? NAN : pmax;
-  diag->ps_min = bad ? NAN : pmin;
-  diag->nonfinite = bad ? 1 : 0;
-  if (bad && !clk->nonfinite) { clk->nonfinite = 1; clk->bad_step = clk->step; }
-  if (apply_bdy) clk->xbctime = clk->xbctime + dtsec;
+  diag->ps_max = isbad ? NAN : pmax;
+  diag->ps_min = isbad ? NAN : pmin;
+  diag->nonfinite = isbad ? 1 : 0;
+  if (isbad && !clk->nonfinite) { clk->nonfinite = 1; clk->bad_step = clk->step; }
+  if (D.c.apply_bdy) clk->xbctime = clk->xbctime + D.c.dtsec;
   clk->step = clk->step + 1;
   clk->uv_role = (clk->uv_role + uvoff) & 1;
   clk->adv_role = (clk->adv_role + advoff) & 1;
@@ -691,19 +725,12 @@ inline dim3 pt_grid(const LaunchGeom &L, int nj, int ni, int &tiles_j) {
 
 }  // namespace
 
-int reduce_rows_per_block(const Geom &g) {
-  // about 4 blocks per SM for a large domain, at least 4 rows per warp
-  const int nrows = (g.iy - 1) * g.kz;
-  const int target = 152 * 4;
-  int rpb = (nrows + target - 1) / target;
-  rpb = (rpb + kRedWarps - 1) / kRedWarps * kRedWarps;
-  return rpb < 4 * kRedWarps ? 4 * kRedWarps : rpb;
-}
-
+// some 16 elements per thread, at most 4 blocks per SM
 int reduce_blocks(const Geom &g) {
-  const int nrows = (g.iy - 1) * g.kz;
-  const int rpb = reduce_rows_per_block(g);
-  return (nrows + rpb - 1) / rpb;
+  const size_t n = g.PS * (size_t)g.kz;
+  const size_t per_block = (size_t)kRedThreads * 16;
+  const size_t nb = (n + per_block - 1) / per_block;
+  return (int)std::min<size_t>(std::max<size_t>(nb, 1), 152 * 4);
 }
 
 template <class R>

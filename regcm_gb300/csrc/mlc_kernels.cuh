@@ -69,8 +69,7 @@ template <class R> struct Launch {
                        size_t nplane, cudaStream_t s);
 };
 
-// Reduction blocks and rows per block the mass budget uses for a geometry.
+// Reduction blocks the mass budget uses for a geometry.
 int reduce_blocks(const Geom &g);
-int reduce_rows_per_block(const Geom &g);
 
 }  // namespace mlc
