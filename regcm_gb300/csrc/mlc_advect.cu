@@ -34,10 +34,6 @@ template <> struct FlowEps<double> {
   static __device__ __forceinline__ double den() { return 1.0e-30; }
   static __device__ __forceinline__ double num() { return (double)1.0e-30f; }
 };
-template <> struct FlowEps<float> {
-  static __device__ __forceinline__ float den() { return 1.0e-15f; }
-  static __device__ __forceinline__ float num() { return 1.0e-15f; }
-};
 
 // WAF flux  hvel*((1+phi)*a + (1-phi)*c)  with  phi = is + zamu*b - is*b  and
 // the limiter  b = max(0, min(2, max(r, min(2r, 1))))  of  r = num/den
@@ -463,7 +459,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
   const T dtrdx = dta * pick<T>(c.rdx, c.rdxf), dtrdy = dta * pick<T>(c.rdx, c.rdxf);
   const bool rot = c.lrotllr != 0;
   const int nf = n_table_r(D);
-  const char *tmaps = static_cast<const char *>(D.tmap) + (size_t)shape * kMaxFields * kTmapBytes;
+  const char *tmaps = static_cast<const char *>(D.tmap) + (size_t)shape * kTmapSlots * kTmapBytes;
   auto tile = [&](int b) { return reinterpret_cast<T(*)[BW]>(wzraw[b]); };
   auto issue = [&](int fld, int b) {  // one thread: the halo tile of field fld into buffer b
     fence_proxy_async();
@@ -984,7 +980,17 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
                                                                int advoff) {
   constexpr int W = 32 * V, S = W - 4;
   constexpr int OB0 = hshape_ob0(V);
+  constexpr int OFF = hshape_off(4, V);
+  constexpr int BW = W + 2 * OFF;  // tile row: range column c sits at c + OFF
+  constexpr unsigned kBox = (unsigned)((NW + 4) * BW * 4);
+  constexpr unsigned kBuf = (kBox + 127u) / 128u * 128u;
+  constexpr int shape = V == 1 ? 0 : NW == 8 ? 1 : 3;
+  static_assert(hshape_inc(shape).v == V && hshape_inc(shape).nw == NW, "tile shape table");
+  // per field: the halo tiles (rows I0-2 .. I0+NW+1) of pp hi, pp lo, dz hi,
+  // dz lo, landed by TMA, all issued at the start
+  __shared__ __align__(128) unsigned char tiles[2][4][kBuf];
   __shared__ __align__(16) float fy_s[2][NW + 1][W];  // meridional fluxes, rows I0 .. I0+NW
+  __shared__ __align__(8) uint64_t mbar[2];
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const int k = blockIdx.y + 1;
@@ -1011,6 +1017,23 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
   const float dtrdx = dta * c.rdxf, dtrdy = dta * c.rdxf;
   const bool rot = c.lrotllr != 0;
   using T = float;
+  const int tid = (int)threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const char *tm = static_cast<const char *>(D.tmap) + ((size_t)shape * kTmapSlots + kMaxFields) * kTmapBytes;
+    for (int f = 0; f < 2; ++f) {
+      mbar_expect_tx(&mbar[f], 4u * kBox);
+      const int pslot = 4 * f + 2 * adv, dslot = 8 + 2 * f;
+      const int slot[4] = {pslot, pslot + 1, dslot, dslot + 1};
+      for (int q = 0; q < 4; ++q)
+        tma_load_3d(tiles[f][q], tm + (size_t)slot[q] * kTmapBytes, ob - OFF, I0 - 3, k - 1, &mbar[f]);
+    }
+  }
 
   int jq[V];
 #pragma unroll
@@ -1110,12 +1133,6 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
     wv[q] = rowin && cc >= 2 && cc <= W - 3 && jq[q] >= 1 && jq[q] <= jx - 1;
     wall = wall && wv[q];
   }
-  // a row r of a double-float plane pair (hi, lo), zero outside rows 1 .. iy-1
-  auto ld_pair = [&](T(&h)[V], T(&l)[V], const float *hi, int r) {
-    const bool ok = inrow && r >= 1 && r <= iy - 1;
-    ld_row<T, V>(h, hi + ko, e0, r, P, ok);
-    ld_row<T, V>(l, hi + F + ko, e0, r, P, ok);
-  };
   // the meridional flux through the south face of row r (relative to pp(r-1))
   // from dz and pp differences of rows r-2 .. r+1; the reference's clamps
   // ih = min(r+1, imax), ihm1 = max(ih-1, imin)
@@ -1134,17 +1151,24 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
   };
 
   for (int f = 0; f < 2; ++f) {
-    const float *pph = reinterpret_cast<const float *>(f == 0 ? D.tetav[adv] : D.pai[adv]);
     float *outh = reinterpret_cast<float *>(f == 0 ? D.tetav[adv ^ 1] : D.pai[adv ^ 1]);
-    const float *dzh = reinterpret_cast<const float *>(D.wz_d[f]);
     float (*fy)[W] = fy_s[f];
-    // rows i-2 .. i+1 of pp (hi, lo) and dz (rounded to FP32)
+    const bool landed = mbar_wait_bounded(&mbar[f], 0u);
+    const float(*tph)[BW] = reinterpret_cast<const float(*)[BW]>(tiles[f][0]);
+    const float(*tpl)[BW] = reinterpret_cast<const float(*)[BW]>(tiles[f][1]);
+    const float(*tzh)[BW] = reinterpret_cast<const float(*)[BW]>(tiles[f][2]);
+    const float(*tzl)[BW] = reinterpret_cast<const float(*)[BW]>(tiles[f][3]);
+    const int cl = OFF + V * lane;
+    // rows i-2 .. i+1 (tile rows wp .. wp+3) of pp (hi, lo) and dz (rounded
+    // to FP32); zero outside the cross points
     T ph[4][V], pl[4][V], zz[4][V], dzi_h[V], dzi_l[V];
 #pragma unroll
     for (int rr = 0; rr < 4; ++rr) {
-      ld_pair(ph[rr], pl[rr], pph, i - 2 + rr);
+      ld_vec<T, V>(ph[rr], &tph[wp + rr][cl]);
+      ld_vec<T, V>(pl[rr], &tpl[wp + rr][cl]);
       T zh[V], zl[V];
-      ld_pair(zh, zl, dzh, i - 2 + rr);
+      ld_vec<T, V>(zh, &tzh[wp + rr][cl]);
+      ld_vec<T, V>(zl, &tzl[wp + rr][cl]);
 #pragma unroll
       for (int q = 0; q < V; ++q) zz[rr][q] = zh[q] + zl[q];
       if (rr == 2) {
@@ -1166,8 +1190,10 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
     }
     if (wp == NW - 1) {  // the flux of row I0+NW: rows ie-2 .. ie+1 = i-1 .. i+2
       T h4[V], l4[V], zh[V], zl[V], z4[V], dy3[V];
-      ld_pair(h4, l4, pph, i + 2);
-      ld_pair(zh, zl, dzh, i + 2);
+      ld_vec<T, V>(h4, &tph[NW + 3][cl]);
+      ld_vec<T, V>(l4, &tpl[NW + 3][cl]);
+      ld_vec<T, V>(zh, &tzh[NW + 3][cl]);
+      ld_vec<T, V>(zl, &tzl[NW + 3][cl]);
 #pragma unroll
       for (int q = 0; q < V; ++q) {
         z4[q] = zh[q] + zl[q];
@@ -1177,7 +1203,15 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
       mflux(x, vve, zmye, me, ie, zz[1], zz[2], zz[3], z4, dy[1], dy[2], dy3);
       st_vec<T, V>(&fy[NW][V * lane], x);
     }
-    __syncthreads();
+    if (__syncthreads_or(!landed)) {
+      if (tid == 0) {
+        atomicOr(&D.clk->fault, 1);
+        // let copies still in flight land before the shared memory is released
+        mbar_wait_bounded(&mbar[f], 0u);
+        if (f == 0) mbar_wait_bounded(&mbar[1], 0u);
+      }
+      return;
+    }
     // p0 - pp: ey = dz + hy, hy the meridional increment
     T hy[V], ey[V];
     {

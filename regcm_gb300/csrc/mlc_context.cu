@@ -182,7 +182,7 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
   }
   D.red_blocks = reduce_blocks(g);
   D.partials = cv.take<double>((size_t)D.red_blocks * 8);
-  D.tmap = cv.take<char>((size_t)kTileShapes * kMaxFields * kTmapBytes);
+  D.tmap = cv.take<char>((size_t)kTileShapes * kTmapSlots * kTmapBytes);
 }
 
 template <class R>
@@ -314,14 +314,16 @@ int ensure_staging(mlc_ctx *x, const mlc_dims &d) {
   return MLC_OK;
 }
 
-// ---- TMA tensor maps of the wz fields --------------------------------------
-// The horizontal WAF loads each field's halo tile (rows I0-2 .. I0+TI+1,
-// columns J0-2 .. J0+TJ+1 at one level) with one tiled TMA copy.  The map's
-// extents are the cross points (jx-1, iy-1, kz), so everything outside them
-// reads as zero, as the kernel needs.  A copy must start on a 16-byte
-// boundary: FP32 tiles start 4 columns left of J0 (x = TJ*bj - 4) and are
-// TJ+8 wide, FP64 tiles 2 columns left (x = TJ*bj - 2) and TJ+4 wide; both
-// widths are multiples of 16 bytes and x*element size is a multiple of 16.
+// ---- TMA tensor maps ---------------------------------------------------------
+// The horizontal WAF loads each field's halo tile (rows I0-2 .. I0+nw+1, the
+// warp range's 32*v columns at one level; hshape) with one tiled TMA copy,
+// and the increment form the planes of theta_v, Exner and their vertical
+// increments the same way.  The map's extents are the cross points (jx-1,
+// iy-1, kz), so everything outside them reads as zero, as the kernels need.
+// A copy must start on a 16-byte boundary: tile offsets step by 32*v - 4
+// columns, a multiple of 16 bytes, and the first tile starts hshape_off
+// columns left of its range so that its x times the element size is a
+// multiple of 16; every box row is a multiple of 16 bytes.
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -346,22 +348,35 @@ int encode_tmaps(mlc_ctx *x, const Member &m, const Dom<R> &D) {
   if (!enc) return MLC_ERR_CUDA;
   const Geom &g = m.g;
   const int nf = n_table_r(m.dims, x->prm, sizeof(R) == sizeof(double));
-  std::vector<CUtensorMap> maps((size_t)kTileShapes * kMaxFields);
+  std::vector<CUtensorMap> maps((size_t)kTileShapes * kTmapSlots);
   std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
   const size_t es = sizeof(R);
   const cuuint64_t dims[3] = {(cuuint64_t)(g.jx - 1), (cuuint64_t)(g.iy - 1), (cuuint64_t)g.kz};
-  const cuuint64_t strides[2] = {(cuuint64_t)g.P * es, (cuuint64_t)g.PS * es};
   const cuuint32_t estr[3] = {1, 1, 1};
+  auto encode = [&](CUtensorMap *mp, const void *base, size_t ebytes, HShape h) {
+    const cuuint64_t strides[2] = {(cuuint64_t)g.P * ebytes, (cuuint64_t)g.PS * ebytes};
+    const cuuint32_t box[3] = {(cuuint32_t)(32 * h.v + 2 * hshape_off((int)ebytes, h.v)),
+                               (cuuint32_t)(h.nw + 4), 1};
+    return enc(mp, ebytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+               const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  const size_t F = g.field3();
   for (int t = 0; t < kTileShapes; ++t) {
-    const HShape h = hshape((int)es, t);
-    const cuuint32_t box[3] = {(cuuint32_t)(32 * h.v + 2 * hshape_off((int)es, h.v)), (cuuint32_t)(h.nw + 4), 1};
-    for (int f = 0; f < nf; ++f) {
-      const CUresult r = enc(&maps[(size_t)t * kMaxFields + f],
-                             es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
-                             3, const_cast<R *>(D.wz[f]), dims, strides, box, estr,
-                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r != CUDA_SUCCESS) return MLC_ERR_CUDA;
+    CUtensorMap *row = &maps[(size_t)t * kTmapSlots];
+    for (int f = 0; f < nf; ++f)
+      if (!encode(&row[f], D.wz[f], es, hshape((int)es, t))) return MLC_ERR_CUDA;
+    if (x->mixed) {
+      // double-float planes: hi at the allocation's start, lo F floats on
+      const HShape hi = hshape_inc(t);
+      const double *src[6] = {D.tetav[0], D.tetav[1], D.pai[0], D.pai[1], D.wz_d[0], D.wz_d[1]};
+      for (int q = 0; q < 6; ++q) {
+        const float *h = reinterpret_cast<const float *>(src[q]);
+        if (!encode(&row[kMaxFields + 2 * q], h, 4, hi) ||
+            !encode(&row[kMaxFields + 2 * q + 1], h + F, 4, hi))
+          return MLC_ERR_CUDA;
+      }
     }
   }
   MLC_TRY(cudaMemcpyAsync(const_cast<void *>(D.tmap), maps.data(), maps.size() * sizeof(CUtensorMap),

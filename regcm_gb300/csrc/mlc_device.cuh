@@ -141,6 +141,14 @@ struct Dom {
 };
 constexpr int kTileShapes = 4;
 constexpr int kTmapBytes = 128;
+// Tensor maps per tile shape: the kMaxFields wz fields of the R table, then
+// the planes the increment form of a mixed member reads: theta_v and Exner
+// of both buffer halves (hi, lo) and their vertical increments (hi, lo)
+//   kMaxFields + 0..3  theta_v[0].hi, theta_v[0].lo, theta_v[1].hi, theta_v[1].lo
+//   kMaxFields + 4..7  Exner[0].hi, ..., Exner[1].lo
+//   kMaxFields + 8..11 increment of theta_v (hi, lo), of Exner (hi, lo)
+constexpr int kIncMaps = 12;
+constexpr int kTmapSlots = kMaxFields + kIncMaps;
 
 // Tile shapes of the horizontal WAF (LaunchGeom::htile).  A warp is one row
 // of 32*v columns, lane l holding columns v*l .. v*l+v-1; a block is nw rows.
@@ -156,6 +164,11 @@ __host__ __device__ constexpr HShape hshape(int elem_bytes, int idx) {
   return elem_bytes == 4
              ? (idx == 1 ? HShape{2, 8} : idx == 2 ? HShape{4, 8} : idx == 3 ? HShape{4, 4} : HShape{1, 8})
              : (idx == 1 ? HShape{2, 8} : idx == 2 ? HShape{2, 4} : idx == 3 ? HShape{1, 4} : HShape{1, 8});
+}
+// Tile shapes of the increment-form WAF (two planes per field: lanes of at
+// most two columns): LaunchGeom::htile 0 = 32x8, 1 and 2 = 64x8, 3 = 64x4.
+__host__ __device__ constexpr HShape hshape_inc(int idx) {
+  return idx == 0 ? HShape{1, 8} : idx == 3 ? HShape{2, 4} : HShape{2, 8};
 }
 // Column offset (j - 1) of the first tile's first column: at most -2, so the
 // first written column is j <= 1, and a multiple of v (aligned lane vectors).
