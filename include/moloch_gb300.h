@@ -256,8 +256,7 @@ typedef struct mlc_tune_report {
   int32_t solve_x, solve_y;  /* implicit w-Exner solve                */
   int32_t vert_x, vert_y;    /* vertical WAF passes                   */
   int32_t htile;             /* horizontal WAF tile, columns x rows:
-                                FP32 0 32x8, 1 64x8, 2 128x8, 3 128x4;
-                                FP64 0 32x8, 1 64x8, 2 64x4, 3 32x4   */
+                                0 32x8, 1 64x8, 2 64x4, 3 32x4        */
   double  ms_fixed;          /* tuned kernel groups, fixed shapes [ms/step] */
   double  ms_tuned;          /* the same groups, picked shapes [ms/step]    */
 } mlc_tune_report;

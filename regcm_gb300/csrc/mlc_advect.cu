@@ -423,8 +423,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
   constexpr int BW = W + 2 * OFF;  // halo tile row: range column c sits at c + OFF
   constexpr unsigned kBox = (unsigned)((NW + 4) * BW * sizeof(T));
   constexpr unsigned kBuf = (kBox + 127u) / 128u * 128u;
-  constexpr int shape = (sizeof(T) == 4) ? (V == 1 ? 0 : V == 2 ? 1 : NW == 8 ? 2 : 3)
-                                         : (V == 1 ? (NW == 8 ? 0 : 3) : (NW == 8 ? 1 : 2));
+  constexpr int shape = V == 1 ? (NW == 8 ? 0 : 3) : (NW == 8 ? 1 : 2);
   static_assert(hshape((int)sizeof(T), shape).v == V && hshape((int)sizeof(T), shape).nw == NW,
                 "tile shape table");
   __shared__ __align__(128) unsigned char wzraw[2][kBuf];  // TMA destinations
@@ -984,7 +983,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
   constexpr int BW = W + 2 * OFF;  // tile row: range column c sits at c + OFF
   constexpr unsigned kBox = (unsigned)((NW + 4) * BW * 4);
   constexpr unsigned kBuf = (kBox + 127u) / 128u * 128u;
-  constexpr int shape = V == 1 ? 0 : NW == 8 ? 1 : 3;
+  constexpr int shape = V == 1 ? 0 : 1;
   static_assert(hshape_inc(shape).v == V && hshape_inc(shape).nw == NW, "tile shape table");
   // per field: the halo tiles (rows I0-2 .. I0+NW+1) of pp hi, pp lo, dz hi,
   // dz lo, landed by TMA, all issued at the start
@@ -1365,16 +1364,11 @@ void launch_tile_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff
   k_adv_horizontal_inc<R, V, NW><<<grd, 32 * NW, 0, s>>>(d, tj, uvoff, advoff);
 }
 
-// the increment form keeps two planes per field: lanes of at most 2 columns
 template <class R>
 void launch_horizontal_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                            cudaStream_t s) {
-  switch (L.htile) {
-    case 1:
-    case 2: launch_tile_inc<R, 2, 8>(L, d, uvoff, advoff, s); break;
-    case 3: launch_tile_inc<R, 2, 4>(L, d, uvoff, advoff, s); break;
-    default: launch_tile_inc<R, 1, 8>(L, d, uvoff, advoff, s); break;
-  }
+  if (hshape_inc(L.htile).v == 2) launch_tile_inc<R, 2, hshape_inc(1).nw>(L, d, uvoff, advoff, s);
+  else launch_tile_inc<R, 1, hshape_inc(0).nw>(L, d, uvoff, advoff, s);
 }
 
 template <class R>

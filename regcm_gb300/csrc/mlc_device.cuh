@@ -155,20 +155,18 @@ constexpr int kTmapSlots = kMaxFields + kIncMaps;
 // Every warp computes its whole range and writes all but two columns at each
 // end (the zonal fluxes of a column need the intermediate field two columns
 // either side), so consecutive tiles overlap by four columns.
-//   FP32: 0 = 32x8, 1 = 64x8, 2 = 128x8, 3 = 128x4
-//   FP64: 0 = 32x8, 1 = 64x8, 2 = 64x4,  3 = 32x4
+//   0 = 32x8, 1 = 64x8, 2 = 64x4, 3 = 32x4 (columns x rows)
 struct HShape {
   int v, nw;
 };
 __host__ __device__ constexpr HShape hshape(int elem_bytes, int idx) {
-  return elem_bytes == 4
-             ? (idx == 1 ? HShape{2, 8} : idx == 2 ? HShape{4, 8} : idx == 3 ? HShape{4, 4} : HShape{1, 8})
-             : (idx == 1 ? HShape{2, 8} : idx == 2 ? HShape{2, 4} : idx == 3 ? HShape{1, 4} : HShape{1, 8});
+  return (void)elem_bytes,
+         idx == 1 ? HShape{2, 8} : idx == 2 ? HShape{2, 4} : idx == 3 ? HShape{1, 4} : HShape{1, 8};
 }
-// Tile shapes of the increment-form WAF (two planes per field: lanes of at
-// most two columns): LaunchGeom::htile 0 = 32x8, 1 and 2 = 64x8, 3 = 64x4.
+// The increment-form WAF (theta_v and Exner of a mixed member, two planes per
+// field) runs the same lanes in blocks of four rows.
 __host__ __device__ constexpr HShape hshape_inc(int idx) {
-  return idx == 0 ? HShape{1, 8} : idx == 3 ? HShape{2, 4} : HShape{2, 8};
+  return HShape{hshape(4, idx).v, 4};
 }
 // Column offset (j - 1) of the first tile's first column: at most -2, so the
 // first written column is j <= 1, and a multiple of v (aligned lane vectors).

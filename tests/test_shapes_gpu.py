@@ -34,8 +34,8 @@ SHAPES = [dict(DEFAULT_SHAPES, htile=h) for h in (1, 2, 3)] + [
 
 
 def members(prec):
-    # 30x55, 24x71 and 56x25 points at scale 0.25; 224x100 (two 128-column
-    # tiles and more) at scale 1
+    # 30x55, 24x71 and 56x25 points at scale 0.25; 224x100 (four 64-column
+    # tiles, eight 32-column tiles) at scale 1
     return ([cs.config3_member(m, scale=0.25, precision=prec) for m in (0, 2)] +
             [cs.config3_member(6, scale=1.0, precision=prec)])
 
