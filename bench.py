@@ -253,11 +253,6 @@ def run_ours(args, rank, world):
     lib.mlc_step_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.mlc_diag),
                                    C.POINTER(C.c_float)]
 
-    class KT(C.Structure):
-        _fields_ = [("name", C.c_char * 32), ("launches", C.c_int32), ("ms", C.c_double)]
-
-    lib.mlc_profile_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(KT), C.c_int,
-                                      C.POINTER(C.c_int)]
     # warm-up (records the step graphs)
     dom.step(args.warmup)
     if world > 1:
@@ -279,35 +274,7 @@ def run_ours(args, rank, world):
     value = pts * args.steps * world / t_dev
     launches = dom.launches_per_step()
 
-    # per-kernel device times (eager steps, events around each kernel group)
-    ktab = (KT * 32)()
-    nk = C.c_int()
-    abi.check(lib.mlc_profile_steps(ctx, 2, ktab, 32, C.byref(nk)), "mlc_profile_steps")
-    kernels = {ktab[i].name.decode(): (ktab[i].launches, ktab[i].ms) for i in range(nk.value)}
-    total_k = sum(v[1] for v in kernels.values())
-    wbytes = 4 if args.precision == "mixed" else 8
-    nf = n_adv_fields(case)
-    dom_name = max(kernels, key=lambda k: kernels[k][1])
-    pk = peaks()
-    hbm_peak = float(pk.get("hbm_gbs", 6800.0))
-    bytes_per = kernel_bytes(dom_name, case, nf, wbytes)
-    nl, kms = kernels[dom_name]
-    roofline = {
-        "kernel": dom_name, "bound": "hbm", "unit": "GB/s",
-        "peak": hbm_peak, "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
-        "share_of_step": kms / total_k,
-        "traffic": None,
-    }
-    tpp = MEASURED_TRAFFIC_PER_POINT.get((dom_name, args.precision, nf))
-    if tpp:
-        roofline["traffic"] = tpp * case.points
-        roofline["traffic_source"] = "ncu on 256x256x41, scaled by points"
-
-    if bytes_per:
-        ach = bytes_per / (kms / nl / 1000.0) / 1e9
-        roofline.update({"achieved": ach, "frac": ach / hbm_peak, "algorithmic_bytes": bytes_per})
-    roofline["kernels_ms_per_step"] = {k: v[1] / 2.0 for k, v in sorted(
-        kernels.items(), key=lambda kv: -kv[1][1])}
+    roofline = kernel_roofline(lib, ctx, case, args.precision)
 
     # end-to-end through the C ABI with pinned host buffers
     e2e = None
@@ -619,6 +586,48 @@ def run_serving(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+class KernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_int32), ("ms", C.c_double)]
+
+
+def kernel_roofline(lib, ctx, case, precision):
+    """Per-kernel-group device times of two eager steps (CUDA events around
+    each group on the library stream) and the roofline of the dominant group:
+    its algorithmic bytes per launch over its mean launch time, against the
+    measured HBM copy bandwidth."""
+    lib.mlc_profile_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(KernelTime), C.c_int,
+                                      C.POINTER(C.c_int)]
+    ktab = (KernelTime * 32)()
+    nk = C.c_int()
+    from regcm_gb300 import abi
+    abi.check(lib.mlc_profile_steps(ctx, 2, ktab, 32, C.byref(nk)), "mlc_profile_steps")
+    kernels = {ktab[i].name.decode(): (ktab[i].launches, ktab[i].ms) for i in range(nk.value)}
+    total_k = sum(v[1] for v in kernels.values())
+    wbytes = 4 if precision == "mixed" else 8
+    nf = n_adv_fields(case)
+    dom_name = max(kernels, key=lambda k: kernels[k][1])
+    pk = peaks()
+    hbm_peak = float(pk.get("hbm_gbs", 6800.0))
+    bytes_per = kernel_bytes(dom_name, case, nf, wbytes)
+    nl, kms = kernels[dom_name]
+    roofline = {
+        "kernel": dom_name, "bound": "hbm", "unit": "GB/s",
+        "peak": hbm_peak, "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
+        "share_of_step": kms / total_k,
+        "traffic": None,
+    }
+    tpp = MEASURED_TRAFFIC_PER_POINT.get((dom_name, precision, nf))
+    if tpp:
+        roofline["traffic"] = tpp * case.points
+        roofline["traffic_source"] = "ncu on 256x256x41, scaled by points"
+    if bytes_per:
+        ach = bytes_per / (kms / nl / 1000.0) / 1e9
+        roofline.update({"achieved": ach, "frac": ach / hbm_peak, "algorithmic_bytes": bytes_per})
+    roofline["kernels_ms_per_step"] = {k: v[1] / 2.0 for k, v in sorted(
+        kernels.items(), key=lambda kv: -kv[1][1])}
+    return roofline
+
+
 def run_mixed_side(args, rank):
     """The same workload in mixed precision (FP32 fields, FP64 solve/Exner/theta),
     timed the same way, for the FP64-and-FP32 side-by-side report."""
@@ -635,11 +644,13 @@ def run_mixed_side(args, rank):
     diag = abi.mlc_diag()
     ms = C.c_float()
     abi.check(lib.mlc_step_timed(dom._ctx, args.steps, C.byref(diag), C.byref(ms)), "mixed")
+    roofline = kernel_roofline(lib, dom._ctx, case, "mixed")
     dom.close()
     torch.cuda.synchronize()
     t = ms.value / 1000.0
     return {"mixed": {"value": case.points * args.steps / t, "unit": UNIT,
-                      "ms_per_step": 1000.0 * t / args.steps, "dtype": "f32+f64"}}
+                      "ms_per_step": 1000.0 * t / args.steps, "dtype": "f32+f64",
+                      "roofline": roofline}}
 
 
 def main():
@@ -656,13 +667,16 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0, help="arena budget (c4)")
     ap.add_argument("--capacity", type=int, default=256, help="member slots (c4)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
+                    help="default: fp64 for c0/c1 (mixed side by side), mixed for c2-c4")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision side run")
     ap.add_argument("--size", type=int, default=0, help="cross points per side (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.precision is None:
+        args.precision = "mixed" if args.config in ("c2", "c3", "c4") else "fp64"
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":

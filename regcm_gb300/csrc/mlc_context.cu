@@ -173,7 +173,7 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
   }
   Bdy<R> &b = D.bd;
   for (int h = 0; h < 2; ++h) {
-    b.xtb[h] = cv.take<R>(F); b.xqb[h] = cv.take<R>(F); b.xpaib[h] = cv.take<double>(F);
+    b.xtb[h] = cv.take<double>(F); b.xqb[h] = cv.take<R>(F); b.xpaib[h] = cv.take<double>(F);
     b.xlb[h] = p.present_qc ? cv.take<R>(F) : nullptr;
     b.xib[h] = p.present_qi ? cv.take<R>(F) : nullptr;
     b.dub[h] = cv.take<R>(F); b.dvb[h] = cv.take<R>(F);
@@ -962,7 +962,7 @@ int set_boundary_impl(mlc_ctx *x, Member &mb, const mlc_bdy_ptrs *b) {
     if (d.ntr > 0 && !b->chib[s]) return MLC_ERR_INVALID;
   }
   for (int s = 0; s < 2; ++s) {
-    MLC_CHK(put3<R>(x, g, b->xtb[s], W(a.xtb[s]), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3x<R>(x, g, b->xtb[s], W(a.xtb[s]), jx - 1, iy - 1, kz, 0, F));
     MLC_CHK(put3<R>(x, g, b->xqb[s], W(a.xqb[s]), jx - 1, iy - 1, kz, 0));
     MLC_CHK(put3x<R>(x, g, b->xpaib[s], W(a.xpaib[s]), jx - 1, iy - 1, kz, 0, F));
     if (p.present_qc) MLC_CHK(put3<R>(x, g, b->xlb[s], W(a.xlb[s]), jx - 1, iy - 1, kz, 0));

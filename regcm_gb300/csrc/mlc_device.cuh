@@ -76,11 +76,14 @@ struct State {
   double *ps;    // 2-D, FP64
 };
 
-// Boundary data b0/b1 for one domain.
+// Boundary data b0/b1 for one domain.  Temperature and Exner are FP64 (a
+// mixed member: double-float planes): the relaxation pulls t and pai toward
+// them every step, so a rounded copy would leave a persistent offset in the
+// relaxation zone.
 template <class R>
 struct Bdy {
-  const R *xtb[2], *xqb[2], *xlb[2], *xib[2], *dub[2], *dvb[2], *chib[2];
-  const double *xpaib[2], *xpsb[2];
+  const R *xqb[2], *xlb[2], *xib[2], *dub[2], *dvb[2], *chib[2];
+  const double *xtb[2], *xpaib[2], *xpsb[2];
 };
 
 // Per-step device scratch that kernels of one step share.

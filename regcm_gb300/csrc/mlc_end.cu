@@ -24,6 +24,18 @@ __device__ __forceinline__ R qfactor(const R *qx, size_t o, size_t F, int ipptls
   if (ipptls == 1) return R(1) + R(kEp1) * qx[o] - qx[o + F];
   return R(1) + R(kEp1) * qx[o];
 }
+// The same factor for a mixed member as the exact double-float 1 + d, with
+// only d = ep1*qv - condensate in FP32.  The step end divides t by qf and
+// multiplies by it again after the relaxation changed qv: an FP32 qf's
+// rounding (6e-8) cancels only where qv did not change, and would otherwise
+// reach theta_v in the relaxation zone every step.
+__device__ __forceinline__ F2 qfactor_df(const float *qx, size_t o, size_t F, int ipptls) {
+  float d;
+  if (ipptls > 1) d = float(kEp1) * qx[o] - qx[o + F] - qx[o + 2 * F] - qx[o + 3 * F] - qx[o + 4 * F];
+  else if (ipptls == 1) d = float(kEp1) * qx[o] - qx[o + F];
+  else d = float(kEp1) * qx[o];
+  return fast_two_sum(1.f, d);
+}
 
 // dynamical_core :1121-1123 and tvirt_to_temp :1629-1648
 template <class R>
@@ -52,7 +64,7 @@ __global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff, int til
       const F2 tv = df_mul(th.ld(o), pa.ld(o));
       st.tvirt[o] = df_f(tv);
       if (inner) {
-        const F2 t = df_div_f(tv, qf);
+        const F2 t = df_div(tv, qfactor_df(st.qx, o, F, c.ipptls));
         st.t[o] = t.hi;
         D.wz[1][o] = t.lo;
       } else {
@@ -69,6 +81,24 @@ __global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff, int til
 // bdyval, MOLOCH branch (Main/mod_bdycod.F90:1631-1860).  Phase 0 does the
 // west/east columns (corners excluded), phase 1 the south/north rows
 // (corners included), which read the corner values phase 0 left.
+// Boundary blends and relaxations.  An FP64 member evaluates the reference's
+// expressions x0*b0 + x1*b1 and (1 - x)*f + x*fext.  In FP32 both carry a
+// rounding that repeats every step - 1 - x and x0 are rounded once and for
+// all - and the relaxation turns it into a steady forcing of order
+// eps*f/x (1e-5 of the field in the inner rings, with a ring-to-ring pattern
+// that the divergence picks up); the increment forms b0 + x1*(b1 - b0) and
+// f + x*(fext - f) round only the small correction.
+template <class R>
+__device__ __forceinline__ R bdy_blend(R x0, R x1, R b0, R b1) {
+  if constexpr (sizeof(R) == sizeof(float)) return b0 + x1 * (b1 - b0);
+  else return x0 * b0 + x1 * b1;
+}
+template <class R>
+__device__ __forceinline__ R bdy_relax_to(R f, R x, R fext) {
+  if constexpr (sizeof(R) == sizeof(float)) return f + x * (fext - f);
+  else return (R(1) - x) * f + x * fext;
+}
+
 template <class R>
 __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int phase) {
   const Dom<R> &D = doms[blockIdx.z >> 1];
@@ -101,7 +131,19 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
       st.pai[ob] = x0 * bd.xpaib[0][ob] + x1 * bd.xpaib[1][ob];
     }
   };
-  auto blend = [&](const R *const *b, size_t o) { return rx0 * b[0][o] + rx1 * b[1][o]; };
+  auto blend = [&](const R *const *b, size_t o) { return bdy_blend<R>(rx0, rx1, b[0][o], b[1][o]); };
+  // t at a ring point: the blend (a mixed member: double-float, lo in wz[1])
+  auto set_t_ring = [&](size_t ob) {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      const DF b0(bd.xtb[0], F), b1(bd.xtb[1], F);
+      const F2 a = b0.ld(ob);
+      const F2 t = df_add_f(a, float(x1) * df_diff(b1.ld(ob), a));
+      st.t[ob] = t.hi;
+      D.wz[1][ob] = t.lo;
+    } else {
+      st.t[ob] = x0 * bd.xtb[0][ob] + x1 * bd.xtb[1][ob];
+    }
+  };
   const int nqx = g.nqx;
   if (phase == 0) {
     const int i = idx + 2;  // i in idi = 2..iy-1 (v), ici = 2..iy-2 (others)
@@ -115,8 +157,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     if (k == 1) st.ps[g.at2(jb, i)] = x0 * bd.xpsb[0][g.at2(jb, i)] + x1 * bd.xpsb[1][g.at2(jb, i)];
     const R un = blend(bd.dub, od);
     st.u[od] = un;
-    st.t[ob] = blend(bd.xtb, ob);
-    if constexpr (sizeof(R) == sizeof(float)) D.wz[1][ob] = 0.f;
+    set_t_ring(ob);
     set_pai_ring(ob);
     st.qx[ob] = blend(bd.xqb, ob);
     if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
@@ -130,7 +171,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     st.w[ob] = inflow ? R(0) : st.w[oi];
     for (int n = 0; n < g.ntr; ++n) {
       const size_t on = (size_t)n * F;
-      st.trac[ob + on] = R(cx0) * bd.chib[0][ob + on] + R(cx1) * bd.chib[1][ob + on];
+      st.trac[ob + on] = bdy_blend<R>(R(cx0), R(cx1), bd.chib[0][ob + on], bd.chib[1][ob + on]);
     }
   } else {
     const int j = idx + 1;  // j in jde = 1..jx (u), jce = 1..jx-1 (others)
@@ -145,8 +186,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     if (k == 1) st.ps[g.at2(j, ib)] = x0 * bd.xpsb[0][g.at2(j, ib)] + x1 * bd.xpsb[1][g.at2(j, ib)];
     const R vn = blend(bd.dvb, od);
     st.v[od] = vn;
-    st.t[ob] = blend(bd.xtb, ob);
-    if constexpr (sizeof(R) == sizeof(float)) D.wz[1][ob] = 0.f;
+    set_t_ring(ob);
     set_pai_ring(ob);
     st.qx[ob] = blend(bd.xqb, ob);
     if (c.present_qc) st.qx[ob + F] = blend(bd.xlb, ob);
@@ -160,7 +200,7 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     st.w[ob] = inflow ? R(0) : st.w[oi];
     for (int n = 0; n < g.ntr; ++n) {
       const size_t on = (size_t)n * F;
-      st.trac[ob + on] = R(cx0) * bd.chib[0][ob + on] + R(cx1) * bd.chib[1][ob + on];
+      st.trac[ob + on] = bdy_blend<R>(R(cx0), R(cx1), bd.chib[0][ob + on], bd.chib[1][ob + on]);
     }
   }
 }
@@ -200,10 +240,10 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const int ibc = cr ? sa.ibnd_cr[ij] : -1;
   const int ibu = up ? sa.ibnd_ud[ij] : -1;
   const int ibv = vp ? sa.ibnd_vd[ij] : -1;
-  auto blend = [&](const R *const *b, size_t o) { return rx0 * b[0][o] + rx1 * b[1][o]; };
+  auto blend = [&](const R *const *b, size_t o) { return bdy_blend<R>(rx0, rx1, b[0][o], b[1][o]); };
   auto relax = [&](R f, R fext, int ib, int k) {
     const R xf = sa.hefc_r[(size_t)(ib - 1) + (size_t)(k - 1) * nsp];
-    return (R(1) - xf) * f + xf * fext;
+    return bdy_relax_to<R>(f, xf, fext);
   };
   const R xfn0 = pick<R>(trtau * c.dtsec, float(trtau * c.dtsec));
 #pragma unroll
@@ -213,7 +253,7 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
       const R xf = R(wrtau * c.dtsec);
       const R w2 = st.w[o2];
       const R fext = R(0) * w2;
-      st.w[o2] = (R(1) - xf) * w2 + xf * fext;
+      st.w[o2] = bdy_relax_to<R>(w2, xf, fext);
     }
     const size_t o = ij + (size_t)(k - 1) * PS;
     const bool nud = c.top_nudge && k <= c.nztop;
@@ -222,13 +262,13 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
     else xfn = nud ? R(sa.tnudge[k - 1] * trtau * c.dtsec) : R(0);
     if (up) {
       R f = st.u[o];
-      if (nud) f = (R(1) - xfn) * f + xfn * blend(bd.dub, o);
+      if (nud) f = bdy_relax_to<R>(f, xfn, blend(bd.dub, o));
       if (ibu > 0) f = relax(f, blend(bd.dub, o), ibu, k);
       st.u[o] = f;
     }
     if (vp) {
       R f = st.v[o];
-      if (nud) f = (R(1) - xfn) * f + xfn * blend(bd.dvb, o);
+      if (nud) f = bdy_relax_to<R>(f, xfn, blend(bd.dvb, o));
       if (ibv > 0) f = relax(f, blend(bd.dvb, o), ibv, k);
       st.v[o] = f;
     }
@@ -236,18 +276,21 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
     if constexpr (sizeof(R) == sizeof(float)) {
       // (1-x)*t + x*b as t + x*(b - t) on the double-float t
       F2 f{st.t[o], D.wz[1][o]};
-      const float bt = blend(bd.xtb, o);
-      if (nud) f = df_add_f(f, xfn * ((bt - f.hi) - f.lo));
+      const DF b0(bd.xtb[0], F), b1(bd.xtb[1], F);
+      const F2 a = b0.ld(o);
+      const F2 bt = df_add_f(a, float(x1) * df_diff(b1.ld(o), a));
+      if (nud) f = df_add_f(f, xfn * df_diff(bt, f));
       if (ibc > 0) {
         const float xf = sa.hefc_r[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
-        f = df_add_f(f, xf * ((bt - f.hi) - f.lo));
+        f = df_add_f(f, xf * df_diff(bt, f));
       }
       st.t[o] = f.hi;
       D.wz[1][o] = f.lo;
     } else {
       R f = st.t[o];
-      if (nud) f = (R(1) - xfn) * f + xfn * blend(bd.xtb, o);
-      if (ibc > 0) f = relax(f, blend(bd.xtb, o), ibc, k);
+      const double bt = x0 * bd.xtb[0][o] + x1 * bd.xtb[1][o];
+      if (nud) f = (R(1) - xfn) * f + xfn * R(bt);
+      if (ibc > 0) f = relax(f, R(bt), ibc, k);
       st.t[o] = f;
     }
     if (ibc <= 0) continue;
@@ -267,15 +310,15 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
       // morelax_fraction with frac = 0 (:3962-3993)
       const R xf = sa.hefc_r[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
       const R f = st.w[o];
-      st.w[o] = (R(1) - xf) * f + xf * f * R(0);
+      st.w[o] = bdy_relax_to<R>(f, xf, f * R(0));
     }
     if (c.ipptls > 0 && c.present_qc) st.qx[o + F] = relax(st.qx[o + F], blend(bd.xlb, o), ibc, k);
     if (c.ipptls > 1 && c.present_qi) st.qx[o + 2 * F] = relax(st.qx[o + 2 * F], blend(bd.xib, o), ibc, k);
     for (int n = 0; n < g.ntr; ++n) {
       const size_t on = o + (size_t)n * F;
       const R xf = sa.fcx_r[ibc - 1];
-      const R fext = R(cx0) * bd.chib[0][on] + R(cx1) * bd.chib[1][on];
-      st.trac[on] = (R(1) - xf) * st.trac[on] + xf * fext;
+      const R fext = bdy_blend<R>(R(cx0), R(cx1), bd.chib[0][on], bd.chib[1][on]);
+      st.trac[on] = bdy_relax_to<R>(st.trac[on], xf, fext);
     }
   }
 }
@@ -383,7 +426,7 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
       // theta_v = tvirt/pai from the double-float t (Main/mod_moloch.F90:1403-1443):
       // where nothing relaxed t, t*qf/pai gives back theta_v to ~1e-14
       const F2 t2{tk, D.wz[1][o]};
-      DF(st.tetav, F).st(o, df_div(df_mul_f(t2, qf), DF(st.pai, F).ld(o)));
+      DF(st.tetav, F).st(o, df_div(df_mul(t2, qfactor_df(st.qx, o, F, ipp)), DF(st.pai, F).ld(o)));
       st.qsat[o] = pfwsat_f(tk, pk);
     } else {
       st.tetav[o] = (double)tv / st.pai[o];

@@ -1,11 +1,13 @@
 """Mixed precision (FP32 fields and horizontal stencils; theta_v, Exner, the
 vertical implicit solve's hydrostatic balance, the Exner update, temperature
-through the step end and the mass sums carried to FP64 accuracy as
+and the virtual-temperature factor through the step end, the temperature and
+Exner boundary data and the mass sums carried to FP64 accuracy as
 double-floats) against the FP64 CPU oracle after 100 steps.
 
-theta_v, u, v, w, qv and tracers stay within the specified 1e-4 relative L2
-(measured: w 2.4e-5 dry, 7.6e-5 moist; theta_v 1.7e-8 / 1.3e-7; v 2.0e-6 /
-1.3e-5), Exner within 1e-8."""
+The scope asks for 1e-4 relative L2 on theta_v, u, v, w, qv and tracers;
+the test holds them to 3e-5 (measured, dry 48^2 / moist 64^2: w 8.2e-6 /
+2.4e-6, v 1.1e-6 / 2.9e-6, u 3.5e-7 / 3.1e-7, qv 4.9e-7 / 2.0e-7),
+theta_v to 2e-8 (1.4e-9 / 1.8e-9) and Exner to 5e-9 (3.6e-10 / 5.7e-10)."""
 from __future__ import annotations
 
 import numpy as np
@@ -47,10 +49,10 @@ def test_mixed_hundred_steps(name, make):
     if "trac" in ref:
         err["trac"] = rel_l2(got["trac"], ref["trac"])
     err["qv"] = rel_l2(got["qx"][..., 0], ref["qx"][..., 0])
-    bad = {k: v for k, v in err.items() if not v <= 1e-4}
+    bad = {k: v for k, v in err.items() if not v <= 3e-5}
     assert not bad, f"{name}: {err}"
-    assert rel_l2(got["pai"], ref["pai"]) <= 1e-8
-    assert rel_l2(got["tetav"], ref["tetav"]) <= 1e-6
+    assert rel_l2(got["pai"], ref["pai"]) <= 5e-9
+    assert rel_l2(got["tetav"], ref["tetav"]) <= 2e-8
     # FP64 mass sums of the FP32 state: the dry-air mass agrees to FP32 rounding
     assert abs(dm.drymass - do.drymass) <= 1e-6 * abs(do.drymass)
 
