@@ -247,8 +247,11 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
 // FP32 planes of wz_d[1] and wz_d[0] (free during the acoustic loop; a
 // column's two passes follow each other closely, so these round trips stay in
 // L2).  wz[2] holds theta_v(k-1) - theta_v(k) from sound_prep.
+// At most 128 threads a block, five blocks an SM: about 100 registers a
+// thread, so that more columns' loads are in flight (the kernel waits on
+// memory; measured 14 % faster than the unconstrained 111 registers)
 template <class R>
-__global__ void k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
+__global__ void __launch_bounds__(128, 5) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
