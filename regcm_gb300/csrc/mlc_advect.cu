@@ -65,13 +65,24 @@ __device__ __forceinline__ T waf_flux(T hvel, T is, T zamu, T a, T c, T num) {
     const float bd = fmaxf(0.f, fminf(d + d, fmaxf(q, fminf(q + q, d))));
     B = __uint_as_float(__float_as_uint(bd) ^ sg);
   } else {
-    const T d = fabs(den);
-    const T q = den < T(0) ? -num : num;
-    if (d < FlowEps<T>::den()) B = fabs(num) < FlowEps<T>::num() ? den : T(0);  // r = 1 or r = 0
-    else if (q <= T(0)) B = T(0);
-    else if (q < T(0.5) * d) B = num + num;
-    else if (q <= d) B = den;
-    else if (q < T(2) * d) B = num;
+    // FP64: the region tests on the integer pipe.  Non-negative doubles order
+    // like their bit patterns read as integers, and for a normal d (d >= minden
+    // here) d/2 and 2d are d's pattern -/+ 2^52; q = sign(den)*num by a sign-bit
+    // XOR.  The tests are the comparisons above exactly (a NaN num fails every
+    // comparison and takes the last region in both forms); only the flux itself
+    // uses the FP64 pipe.
+    const long long bden = __double_as_longlong(den), bnum = __double_as_longlong(num);
+    const long long mag = 0x7fffffffffffffffLL, one_exp = 1LL << 52;
+    const long long ad = bden & mag;                    // |den|
+    const long long bq = bnum ^ (bden & ~mag);          // q, as a signed pattern
+    const long long eden = __double_as_longlong(FlowEps<T>::den());
+    const long long enum_ = __double_as_longlong(FlowEps<T>::num());
+    if (ad < eden) B = (bnum & mag) < enum_ ? den : T(0);  // r = 1 or r = 0
+    else if ((bnum & mag) > 0x7ff0000000000000LL) B = den + den;  // num is NaN
+    else if (bq <= 0) B = T(0);                          // q <= 0 (and -0)
+    else if (bq < ad - one_exp) B = num + num;           // q < d/2
+    else if (bq <= ad) B = den;                          // q <= d
+    else if (bq < ad + one_exp) B = num;                 // q < 2d
     else B = den + den;
   }
   return hvel * ((a + c) - (is * den + (zamu - is) * B));
@@ -261,7 +272,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
       const T zamu = skp1 * dtrdz;
       const bool up = zamu >= T(0);
       f1kp = waf_flux<T>(T(0.5) * skp1, up ? T(1) : T(-1), zamu, c0p1, c0k,
-                         up ? c0p1 - c0p2 : c0m1 - c0k);
+                         (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
     } else {
       f1kp = k <= kz - 1 ? vflux<T>(dtrdz, skp1, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
     }
@@ -272,7 +283,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
         const T zamu = sm1 * dtrdz;
         const bool up = zamu >= T(0);
         f2n = waf_flux<T>(T(0.5) * sm1, up ? T(1) : T(-1), zamu, c1m1, c1m2,
-                          up ? c1m1 - c1k : c1m3 - c1m2);
+                          (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
       } else {
         f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1k, k - 2, kz);
       }
@@ -500,7 +511,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     for (int q = 0; q < V; ++q) {
       const bool ok = okM && jq[q] >= 1 && jq[q] <= jx - 1;
       mv[q] = ok;
-      vv[q] = ok ? a[q] : T(0);
+      vv[q] = ok ? T(0.5) * a[q] : T(0);  // the flux's hvel = v/2 (exact)
       zmy[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
     }
     // the last warp also forms the fluxes of row I0+NW
@@ -512,7 +523,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     for (int q = 0; q < V; ++q) {
       const bool ok = okE && jq[q] >= 1 && jq[q] <= jx - 1;
       me[q] = ok;
-      vve[q] = ok ? a[q] : T(0);
+      vve[q] = ok ? T(0.5) * a[q] : T(0);
       zmye[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
     }
   }
@@ -551,7 +562,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
         dvy[q] = vn[q] * rn[q] * zn[q] - vi[q] * ri[q] * zs[q];
         m2[q] = mf[q];
       }
-      uu[q] = xv[q] ? ui[q] : T(0);
+      uu[q] = xv[q] ? T(0.5) * ui[q] : T(0);  // hvel = u/2 (exact)
       zmx[q] = xv[q] ? ui[q] * msu[q] * dtrdx : T(0);
     }
     // the zonal update also needs u, rfmzu and rmu one column east
@@ -620,8 +631,8 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 #pragma unroll
       for (int q = 0; q < V; ++q) {
         const bool up = zmy[q] > T(0);
-        const T y = waf_flux<T>(T(0.5) * vv[q], up ? T(1) : T(-1), zmy[q], wa[q], wzi[q],
-                                up ? wa[q] - wA[q] : wB[q] - wC[q]);
+        const T y = waf_flux<T>(vv[q], up ? T(1) : T(-1), zmy[q], wa[q], wzi[q],
+                                (up ? wa[q] : wB[q]) - (up ? wA[q] : wC[q]));
         x[q] = mv[q] ? y : T(0);  // zero outside the flux points
       }
       st_vec<T, V>(&zp[wp][V * lane], x);
@@ -635,8 +646,8 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 #pragma unroll
         for (int q = 0; q < V; ++q) {
           const bool up = zmye[q] > T(0);
-          const T y = waf_flux<T>(T(0.5) * vve[q], up ? T(1) : T(-1), zmye[q], xa[q], xc[q],
-                                  up ? xa[q] - wA[q] : wB[q] - wC[q]);
+          const T y = waf_flux<T>(vve[q], up ? T(1) : T(-1), zmye[q], xa[q], xc[q],
+                                  (up ? xa[q] : wB[q]) - (up ? wA[q] : wC[q]));
           x[q] = me[q] ? y : T(0);
         }
         st_vec<T, V>(&zp[NW][V * lane], x);
@@ -685,8 +696,10 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       const bool up = zmx[q] > T(0);
       const T a = p0at(q - 1), cq = p0at(q);
       // jhm1 = max(j-2, jmin) upwind; jh = min(j+1, jmax) downwind
-      const T num = up ? a - (j == 2 ? a : p0at(q - 2)) : (j == jx - 1 ? cq - a : p0at(q + 1) - cq);
-      const T x = waf_flux<T>(T(0.5) * uu[q], up ? T(1) : T(-1), zmx[q], a, cq, num);
+      // upwind a - p0(jhm1), downwind p0(jh) - p0(jh-1): one subtraction of selected operands
+      const T n1 = up ? a : (j == jx - 1 ? cq : p0at(q + 1));
+      const T n2 = up ? (j == 2 ? a : p0at(q - 2)) : (j == jx - 1 ? a : cq);
+      const T x = waf_flux<T>(uu[q], up ? T(1) : T(-1), zmx[q], a, cq, n1 - n2);
       zx[q] = xv[q] ? x : T(0);
     }
     T zxe[V];
