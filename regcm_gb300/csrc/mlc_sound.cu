@@ -519,6 +519,293 @@ __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int
   }
 }
 
+// 16 bytes at p (16-byte aligned) as 4 floats / 4 ints
+__device__ __forceinline__ void ld4(float (&x)[4], const float *p) {
+  const float4 v = *reinterpret_cast<const float4 *>(p);
+  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ void ld4i(int (&x)[4], const int32_t *p) {
+  const int4 v = *reinterpret_cast<const int4 *>(p);
+  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+// x[q] at q = -1..3: the lane's own elements, the one west of them read singly
+struct West4 {
+  float w, x[4];
+  __device__ __forceinline__ float at(int q) const { return q < 0 ? w : x[q]; }
+};
+
+// The divergence and s of a mixed member (the same equations as
+// k_sound_div) with lanes of four consecutive columns: 16-byte loads at the
+// lane's points and the row north of them, the east neighbour of the last
+// element read singly, the level below carried from the previous level.
+template <class R>
+__global__ void __launch_bounds__(128) k_sound_div_v4(const Dom<R> *__restrict__ doms, int uvoff,
+                                                      int tiles_j) {
+  static_assert(sizeof(R) == sizeof(float), "FP32 fields");
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int e0 = (bj * 32 + (int)threadIdx.x) * 4;
+  const int i = bi * (int)blockDim.y + (int)threadIdx.y + 1;
+  const int k0 = (int)blockIdx.y * kPtLevels + 1;
+  if (e0 + 1 > jx - 1 || i > iy - 1 || k0 > kz) return;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int uv = (D.clk->uv_role + uvoff) & 1;
+  const float *__restrict__ u = D.u[uv];
+  const float *__restrict__ v = D.v[uv];
+  float *__restrict__ zdiv2 = D.zdiv2;
+  float *__restrict__ sv = D.s;
+  float *__restrict__ w = D.w;
+  const float dtrdx = c.dtrdxsf, dtrdy = dtrdx;
+  const unsigned P = (unsigned)g.P, PS = (unsigned)g.PS;
+  const unsigned ij = (unsigned)e0 + (unsigned)(i - 1) * P;
+  const bool east = e0 + 4 <= jx - 1;  // element 3 has an east neighbour to read
+  bool has[4], inner[4];
+  bool all = true;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = e0 + q + 1;
+    has[q] = j <= jx - 1;
+    inner[q] = j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2;
+    all = all && has[q];
+  }
+  const bool any_inner = inner[0] || inner[1] || inner[2] || inner[3];
+  auto next4 = [&](float (&e)[4], const float (&x)[4], const float *arr, unsigned o) {
+    e[0] = x[1]; e[1] = x[2]; e[2] = x[3];
+    e[3] = east ? arr[o + 4] : 0.f;
+  };
+  float rmu0[4], rmu1[4], rmv0[4], rmv1[4], mfac[4], hx0[4], hx1[4], hy0[4], hy1[4];
+  ld4(rmu0, sa.rmu + ij);
+  next4(rmu1, rmu0, sa.rmu, ij);
+  ld4(rmv0, sa.rmv + ij);
+  ld4(rmv1, sa.rmv + ij + P);
+  ld4(mfac, (c.lrotllr ? sa.msfx : sa.mx2) + ij);
+  ld4(hx0, sa.hx + ij);
+  next4(hx1, hx0, sa.hx, ij);
+  ld4(hy0, sa.hy + ij);
+  ld4(hy1, sa.hy + ij + P);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (!inner[q]) hx0[q] = hx1[q] = hy0[q] = hy1[q] = 0.f;
+  // the winds of the level below (for s)
+  float um[4], upm[4], vm[4], vpm[4];
+  if (k0 >= 2 && any_inner) {
+    const unsigned om = ij + (unsigned)(k0 - 2) * PS;
+    ld4(um, u + om);
+    next4(upm, um, u, om);
+    ld4(vm, v + om);
+    ld4(vpm, v + om + P);
+  }
+  for (int k = k0; k < k0 + kPtLevels && k <= kz; ++k) {
+    const unsigned o = ij + (unsigned)(k - 1) * PS;
+    float u0[4], u1[4], v0[4], v1[4], fu0[4], fu1[4], fv0[4], fv1[4], fz[4], zd[4];
+    ld4(u0, u + o);
+    next4(u1, u0, u, o);
+    ld4(v0, v + o);
+    ld4(v1, v + o + P);
+    ld4(fu0, sa.rfmzu + o);
+    next4(fu1, fu0, sa.rfmzu, o);
+    ld4(fv0, sa.rfmzv + o);
+    ld4(fv1, sa.rfmzv + o + P);
+    ld4(fz, sa.fmz + o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float zum, zup;
+      if (c.lrotllr) {
+        zum = dtrdx * u0[q] * fu0[q];
+        zup = dtrdx * u1[q] * fu1[q];
+      } else {
+        zum = dtrdx * u0[q] * fu0[q] * rmu0[q];
+        zup = dtrdx * u1[q] * fu1[q] * rmu1[q];
+      }
+      const float zvm = dtrdy * v0[q] * fv0[q] * rmv0[q];
+      const float zvp = dtrdy * v1[q] * fv1[q] * rmv1[q];
+      zd[q] = fz[q] * mfac[q] * ((zup - zum) + (zvp - zvm));
+    }
+    if (all) {
+      *reinterpret_cast<float4 *>(zdiv2 + o) = make_float4(zd[0], zd[1], zd[2], zd[3]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (has[q]) zdiv2[o + q] = zd[q];
+    }
+    if (any_inner) {
+      if (k >= 2) {
+        const float gk = sa.gzitak_r[k - 1];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (inner[q]) {
+            const float zuh = (u0[q] + um[q]) * hx0[q] + (u1[q] + upm[q]) * hx1[q];
+            const float zvh = (v0[q] + vm[q]) * hy0[q] + (v1[q] + vpm[q]) * hy1[q];
+            sv[o + q] = -(0.25f * (zuh + zvh) * gk);
+          }
+      }
+      if (k == kz) {
+        const unsigned ot = ij + (unsigned)kz * PS;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (inner[q]) {
+            const float zuh = u0[q] * hx0[q] + u1[q] * hx1[q];
+            const float zvh = v0[q] * hy0[q] + v1[q] * hy1[q];
+            const float skp1 = -(0.5f * (zuh + zvh));
+            sv[ot + q] = skp1;
+            w[ot + q] = -skp1;
+          }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        um[q] = u0[q]; upm[q] = u1[q]; vm[q] = v0[q]; vpm[q] = v1[q];
+      }
+    }
+  }
+}
+
+// The momentum update of a mixed member (the same equations as
+// k_sound_momentum) with lanes of four consecutive columns: 16-byte loads of
+// every field at the lane's points and the row south of them; the west
+// neighbours are the lane's own elements but for the first, read singly.  A
+// block is 32 lanes x 4 rows; grid x = 128-column tiles times row tiles, y =
+// level chunks, z = member.
+template <class R>
+__global__ void __launch_bounds__(128) k_sound_momentum_v4(const Dom<R> *__restrict__ doms,
+                                                           int uvoff, int advoff, int tiles_j) {
+  static_assert(sizeof(R) == sizeof(float), "FP32 fields");
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int e0 = (bj * 32 + (int)threadIdx.x) * 4;  // j-1 of the lane's first column
+  const int i = bi * (int)blockDim.y + (int)threadIdx.y + 1;
+  const int k0 = (int)blockIdx.y * kPtLevels + 1;
+  if (e0 + 1 > jx || i > iy || k0 > kz) return;
+  const Scal &c = D.c;
+  const Stat<R> &sa = D.sa;
+  const int uv = (D.clk->uv_role + uvoff) & 1;
+  const int adv = (D.clk->adv_role + advoff) & 1;
+  const float *__restrict__ u_in = D.u[uv];
+  const float *__restrict__ v_in = D.v[uv];
+  float *__restrict__ u_out = D.u[uv ^ 1];
+  float *__restrict__ v_out = D.v[uv ^ 1];
+  const float *__restrict__ zraw = D.zdiv2;
+  const size_t F = g.field3();
+  const float *__restrict__ th_h = reinterpret_cast<const float *>(D.tetav[adv]);
+  const float *__restrict__ th_l = th_h + F;
+  const float *__restrict__ pa_h = reinterpret_cast<const float *>(D.pai[adv]);
+  const float *__restrict__ pa_l = pa_h + F;
+  const float dts = c.dtsoundf, dtrdx = c.dtrdxsf, dtrdy = dtrdx, dxrdt = c.dxrdtf;
+  const float zfz = float(kGrav) * dts;
+  const float halfcp = 0.5f * float(kCpd);
+  const unsigned P = (unsigned)g.P;
+  const unsigned ij = (unsigned)e0 + (unsigned)(i - 1) * P;
+  const bool west = e0 >= 1, south = i >= 2;
+  bool upd_u[4], upd_v[4], has_u[4], has_v[4];
+  bool all_u = true, all_v = true;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = e0 + q + 1;
+    has_u[q] = i <= iy - 1 && j <= jx;
+    has_v[q] = j <= jx - 1;
+    upd_u[q] = j >= 2 && j <= jx - 1 && i >= 2 && i <= iy - 2;
+    upd_v[q] = j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 1;
+    all_u = all_u && has_u[q];
+    all_v = all_v && has_v[q];
+  }
+  // 2-D coefficients of the lane's columns (zero where nothing is updated)
+  float mu[4], hx4[4], cu4[4], mv[4], hy4[4], cv4[4];
+  int ibu[4], ibv[4];
+  ld4(mu, sa.msfu + ij);
+  ld4(hx4, sa.hx + ij);
+  ld4(cu4, sa.coru + ij);
+  ld4(mv, sa.msfv + ij);
+  ld4(hy4, sa.hy + ij);
+  ld4(cv4, sa.corv + ij);
+  ld4i(ibu, sa.ibnd_ud + ij);
+  ld4i(ibv, sa.ibnd_vd + ij);
+  const int nsp = c.nspgx;
+  for (int k = k0; k < k0 + kPtLevels && k <= kz; ++k) {
+    const unsigned o = ij + (unsigned)(k - 1) * (unsigned)g.PS;
+    float un[4], vn[4], uo[4], vo[4];
+    ld4(uo, u_in + o);
+    ld4(vo, v_in + o);
+    West4 zr, th, tl, ph, pl;
+    ld4(zr.x, zraw + o);
+    ld4(th.x, th_h + o);
+    ld4(tl.x, th_l + o);
+    ld4(ph.x, pa_h + o);
+    ld4(pl.x, pa_l + o);
+    zr.w = th.w = tl.w = ph.w = pl.w = 0.f;
+    if (west) {
+      zr.w = zraw[o - 1];
+      th.w = th_h[o - 1];
+      tl.w = th_l[o - 1];
+      ph.w = pa_h[o - 1];
+      pl.w = pa_l[o - 1];
+    }
+    float zs[4] = {0.f, 0.f, 0.f, 0.f}, ts[4] = {0.f, 0.f, 0.f, 0.f}, tsl[4] = {0.f, 0.f, 0.f, 0.f};
+    float ps[4] = {0.f, 0.f, 0.f, 0.f}, psl[4] = {0.f, 0.f, 0.f, 0.f};
+    if (south) {
+      ld4(zs, zraw + o - P);
+      ld4(ts, th_h + o - P);
+      ld4(tsl, th_l + o - P);
+      ld4(ps, pa_h + o - P);
+      ld4(psl, pa_l + o - P);
+    }
+    const float gk = sa.gzitakh_r[k - 1];
+    const float xk = sa.xkdamp_r[k - 1];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float a = uo[q];
+      if (upd_u[q]) {
+        if (c.divdamp) {
+          const float xdam = dxrdt * xk * mu[q];
+          a = a + xdam * (zr.x[q] - zr.at(q - 1));
+        }
+        const float zrom1u = halfcp * ((th.at(q - 1) + th.x[q]) + (tl.at(q - 1) + tl.x[q]));
+        const float zcor1u = cu4[q] * dts * vo[q];
+        const int ib = ibu[q];
+        const float bw = ib > 0 ? 1.f - sa.hefc_r[(size_t)(ib - 1) + (size_t)(k - 1) * nsp] : 1.f;
+        const float zcx = dtrdx * mu[q];
+        const float pd = (ph.x[q] - ph.at(q - 1)) + (pl.x[q] - pl.at(q - 1));
+        a = a + bw * (zcor1u - zfz * hx4[q] * gk - zcx * zrom1u * pd);
+      }
+      un[q] = a;
+      float b = vo[q];
+      if (upd_v[q]) {
+        if (c.divdamp) {
+          const float xdam = c.lrotllr ? dxrdt * xk : dxrdt * xk * mv[q];
+          b = b + xdam * (zr.x[q] - zs[q]);
+        }
+        const float zrom1v = halfcp * ((ts[q] + th.x[q]) + (tsl[q] + tl.x[q]));
+        const float zcor1v = cv4[q] * dts * uo[q];
+        const int ib = ibv[q];
+        const float bw = ib > 0 ? 1.f - sa.hefc_r[(size_t)(ib - 1) + (size_t)(k - 1) * nsp] : 1.f;
+        const float zcy = c.lrotllr ? dtrdy : dtrdy * mv[q];
+        const float pd = (ph.x[q] - ps[q]) + (pl.x[q] - psl[q]);
+        b = b + bw * (-zcor1v - zfz * hy4[q] * gk - zcy * zrom1v * pd);
+      }
+      vn[q] = b;
+    }
+    if (all_u) {
+      *reinterpret_cast<float4 *>(u_out + o) = make_float4(un[0], un[1], un[2], un[3]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (has_u[q]) u_out[o + q] = un[q];
+    }
+    if (all_v) {
+      *reinterpret_cast<float4 *>(v_out + o) = make_float4(vn[0], vn[1], vn[2], vn[3]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (has_v[q]) v_out[o + q] = vn[q];
+    }
+  }
+}
+
 inline dim3 col_block(const LaunchGeom &L) { return dim3((unsigned)L.col_x, (unsigned)L.col_y); }
 // grid of a point kernel over nj x ni points per level
 inline dim3 pt_grid(const LaunchGeom &L, int nj, int ni, int &tiles_j) {
@@ -538,9 +825,15 @@ void Launch<R>::sound_prep(const LaunchGeom &L, const Dom<R> *d, int advoff, cud
 
 template <class R>
 void Launch<R>::sound_div(const LaunchGeom &L, const Dom<R> *d, int uvoff, cudaStream_t s) {
-  int tj;
-  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-  k_sound_div<R><<<grd, col_block(L), 0, s>>>(d, uvoff, tj);
+  if constexpr (sizeof(R) == sizeof(float)) {
+    const int tj = (L.jx - 1 + 127) / 128, ti = (L.iy - 1 + 3) / 4;
+    const dim3 grd((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels), (unsigned)L.nmem);
+    k_sound_div_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, tj);
+  } else {
+    int tj;
+    const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+    k_sound_div<R><<<grd, col_block(L), 0, s>>>(d, uvoff, tj);
+  }
 }
 
 template <class R>
@@ -561,9 +854,16 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
 template <class R>
 void Launch<R>::sound_momentum(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                                cudaStream_t s) {
-  int tj;
-  const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
-  k_sound_momentum<R><<<grd, col_block(L), 0, s>>>(d, uvoff, advoff, tj);
+  if constexpr (sizeof(R) == sizeof(float)) {
+    // lanes of four columns: 128 columns by 4 rows a block
+    const int tj = (L.jx + 127) / 128, ti = (L.iy + 3) / 4;
+    const dim3 grd((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels), (unsigned)L.nmem);
+    k_sound_momentum_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, advoff, tj);
+  } else {
+    int tj;
+    const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
+    k_sound_momentum<R><<<grd, col_block(L), 0, s>>>(d, uvoff, advoff, tj);
+  }
 }
 
 template <class R>
