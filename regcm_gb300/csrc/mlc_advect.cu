@@ -434,12 +434,13 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
   constexpr int BW = W + 2 * OFF;  // halo tile row: range column c sits at c + OFF
   constexpr unsigned kBox = (unsigned)((NW + 4) * BW * sizeof(T));
   constexpr unsigned kBuf = (kBox + 127u) / 128u * 128u;
+  constexpr int kStages = 4;  // halo tiles in flight: the next three fields land while one is used
   constexpr int shape = V == 1 ? (NW == 8 ? 0 : 3) : (NW == 8 ? 1 : 2);
   static_assert(hshape((int)sizeof(T), shape).v == V && hshape((int)sizeof(T), shape).nw == NW,
                 "tile shape table");
-  __shared__ __align__(128) unsigned char wzraw[2][kBuf];  // TMA destinations
+  __shared__ __align__(128) unsigned char wzraw[kStages][kBuf];  // TMA destinations
   __shared__ __align__(16) T zp_s[2][NW + 1][W];           // meridional fluxes, rows I0 .. I0+NW
-  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ __align__(8) uint64_t mbar[kStages];
   __shared__ const T *cur_s[kMaxFields];                   // each field's current and other half
   __shared__ T *out_s[kMaxFields];
   // grid: x = tiles along j and i, y = level, z = member
@@ -477,8 +478,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     tma_load_3d(wzraw[b], tmaps + (size_t)fld * kTmapBytes, ob - OFF, I0 - 3, k - 1, &mbar[b]);
   };
   if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    for (int q = 0; q < kStages; ++q) mbar_init(&mbar[q], 1);
     fence_mbar_init();
   }
   if (tid < nf) {
@@ -489,10 +489,8 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     out_s[tid] = out0 + ko;
   }
   __syncthreads();
-  if (tid == 0) {
-    issue(0, 0);
-    if (nf > 1) issue(1, 1);
-  }
+  if (tid == 0)
+    for (int q = 0; q < kStages && q < nf; ++q) issue(q, q);
 
   // ---- the lane's coefficients (while the first tiles land) ----
   int jq[V];
@@ -615,10 +613,10 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     // meridional pass
     T ppk[V];
     ld_row<T, V>(ppk, pp, e0, i, P, rowin);
-    const int b = f & 1;
-    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((f >> 1) & 1));
+    const int b = f % kStages;
+    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((f / kStages) & 1));
     T(*wt)[BW] = tile(b);
-    T(*zp)[W] = zp_s[b];
+    T(*zp)[W] = zp_s[f & 1];
     // meridional fluxes zpby(j,i): j in jce, i in ici1..ice2
     T wzi[V];
     {
@@ -657,13 +655,13 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       if (tid == 0) {
         atomicOr(&D.clk->fault, 1);
         // let copies still in flight land before the shared memory is released
-        mbar_wait_bounded(&mbar[b], (unsigned)((f >> 1) & 1));
-        if (f + 1 < nf) mbar_wait_bounded(&mbar[b ^ 1], (unsigned)(((f + 1) >> 1) & 1));
+        for (int g2 = f; g2 < f + kStages && g2 < nf; ++g2)
+          mbar_wait_bounded(&mbar[g2 % kStages], (unsigned)((g2 / kStages) & 1));
       }
       return;
     }
-    // buffer b is read for the last time above: fetch the field after next
-    if (tid == 0 && f + 2 < nf) issue(f + 2, b);
+    // buffer b is read for the last time above: fetch the field kStages on
+    if (tid == 0 && f + kStages < nf) issue(f + kStages, b);
     // p0(j,i): j in jce, i in ici
     T p0[V];
     {
