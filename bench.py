@@ -153,6 +153,15 @@ def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None
 # bench case by its points.  Keyed by (kernel group, precision, advected fields).
 MEASURED_TRAFFIC_PER_POINT = {("adv_horizontal", "fp64", 10): 733.6e6 / (256 * 256 * 41),
                               ("sound_solve", "mixed", 10): 182.0e6 / (256 * 256 * 41)}
+# What limits the dominant kernel when it is not HBM, from the same ncu captures.
+MEASURED_LIMITER = {
+    ("adv_horizontal", "fp64"): {
+        "pipe": "fp64", "active": 0.837,
+        "source": "ncu sm__inst_executed_pipe_fp64, profiles/adv_horizontal_fp64_moist256_full.md"},
+    ("sound_solve", "mixed"): {
+        "stall": "long scoreboard (memory latency)", "warps_active": 0.20,
+        "source": "ncu, profiles/kernels_mixed_moist256_full.md"},
+}
 
 
 def n_adv_fields(case) -> int:
@@ -622,6 +631,9 @@ def kernel_roofline(lib, ctx, case, precision):
     if tpp:
         roofline["traffic"] = tpp * case.points
         roofline["traffic_source"] = "ncu on 256x256x41, scaled by points"
+    lim = MEASURED_LIMITER.get((dom_name, precision))
+    if lim:
+        roofline["limiter"] = lim
     if bytes_per:
         ach = bytes_per / (kms / nl / 1000.0) / 1e9
         roofline.update({"achieved": ach, "frac": ach / hbm_peak, "algorithmic_bytes": bytes_per})

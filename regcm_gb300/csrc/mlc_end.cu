@@ -436,6 +436,167 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
   }
 }
 
+// 16 bytes at p (16-byte aligned) as 4 floats; a float4 store
+__device__ __forceinline__ void ld4f(float (&x)[4], const float *p) {
+  const float4 v = *reinterpret_cast<const float4 *>(p);
+  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ void st4f(float *p, const float (&x)[4]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(x[0], x[1], x[2], x[3]);
+}
+
+// k_end_cross of a mixed member with lanes of four consecutive columns
+// (16-byte loads and stores; the same expressions): ux, vx, p, the
+// status_update clamps, tvirt, rho, theta_v (double-float) and qsat.  A block
+// is 32 lanes x 4 rows; grid x = 128-column tiles times row tiles, y = level
+// chunks, z = member.
+template <class R>
+__global__ void __launch_bounds__(128) k_end_cross_v4(const Dom<R> *__restrict__ doms, int uvoff,
+                                                      int advoff, int tiles_j) {
+  static_assert(sizeof(R) == sizeof(float), "FP32 fields");
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const int jx = g.jx, iy = g.iy, kz = g.kz;
+  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int e0 = (bj * 32 + (int)threadIdx.x) * 4;
+  const int i = bi * (int)blockDim.y + (int)threadIdx.y + 1;
+  const int k0 = (int)blockIdx.y * kPtLevels + 1;
+  if (e0 + 1 > jx - 1 || i > iy - 1 || k0 > kz) return;
+  const Scal &c = D.c;
+  const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
+  const float *__restrict__ u = st.u;
+  const float *__restrict__ v = st.v;
+  float *__restrict__ ux = st.ux;
+  float *__restrict__ vx = st.vx;
+  float *__restrict__ pp = st.p;
+  float *__restrict__ tt = st.t;
+  float *__restrict__ tvir = st.tvirt;
+  float *__restrict__ rho = st.rho;
+  float *__restrict__ qsat = st.qsat;
+  float *__restrict__ qx = st.qx;
+  float *__restrict__ trac = st.trac;
+  const float *__restrict__ tlo = D.wz[1];
+  const size_t F = g.field3();
+  float *__restrict__ pa_h = reinterpret_cast<float *>(st.pai);
+  float *__restrict__ th_h = reinterpret_cast<float *>(st.tetav);
+  const unsigned P = (unsigned)g.P, PS = (unsigned)g.PS;
+  const unsigned ij = (unsigned)e0 + (unsigned)(i - 1) * P;
+  const int ipp = c.ipptls;
+  bool has[4], inner[4];
+  bool all = true;
+  int nvalid = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = e0 + q + 1;
+    has[q] = j <= jx - 1;
+    inner[q] = j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2;
+    all = all && has[q];
+    nvalid += has[q] ? 1 : 0;
+  }
+  const bool any_inner = inner[0] || inner[1] || inner[2] || inner[3];
+  auto store = [&](float *dst, const float (&x)[4]) {
+    if (all) {
+      st4f(dst, x);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (has[q]) dst[q] = x[q];
+    }
+  };
+  for (int k = k0; k < k0 + kPtLevels && k <= kz; ++k) {
+    const unsigned o = ij + (unsigned)(k - 1) * PS;
+    if (c.apply_bdy) {
+      // u at j-1 .. j+2 and v at rows i-1 .. i+2 (:1535-1566)
+      float uc[4], ue1 = 0.f, ue2 = 0.f, uw = 0.f;
+      ld4f(uc, u + o);
+      if (e0 >= 1) uw = u[o - 1];
+      if (nvalid == 4) ue1 = u[o + 4];          // j+1 of the last column (<= jx)
+      if (e0 + 4 <= jx - 2) ue2 = u[o + 5];     // j+2 of the last column
+      const float un[6] = {uw, uc[0], uc[1], uc[2], uc[3], ue1};  // u at j-1 .. j+4 of column 0
+      float a[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = e0 + q + 1;
+        const float u0 = un[q + 1], u1 = un[q + 2], um = un[q];
+        const float u2 = q < 3 ? un[q + 3] : ue2;
+        if (j == 1) a[q] = 0.5f * (u0 + u1);
+        else if (j == jx - 1) a[q] = 0.5f * (u1 + u0);
+        else a[q] = 0.5625f * (u1 + u0) - 0.0625f * (u2 + um);
+      }
+      store(ux + o, a);
+      float vc[4], vn[4], vs[4] = {0.f, 0.f, 0.f, 0.f}, vnn[4] = {0.f, 0.f, 0.f, 0.f};
+      ld4f(vc, v + o);
+      ld4f(vn, v + o + P);
+      if (i >= 2 && i <= iy - 2) {
+        ld4f(vs, v + o - P);
+        ld4f(vnn, v + o + 2 * P);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (i == 1) a[q] = 0.5f * (vc[q] + vn[q]);
+        else if (i == iy - 1) a[q] = 0.5f * (vn[q] + vc[q]);
+        else a[q] = 0.5625f * (vn[q] + vc[q]) - 0.0625f * (vnn[q] + vs[q]);
+      }
+      store(vx + o, a);
+    }
+    // pressure (FP32 of the double-float Exner)
+    float ph[4], pl[4], pk[4];
+    ld4f(ph, pa_h + o);
+    ld4f(pl, pa_h + F + o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) pk[q] = exner_to_pressure_f(ph[q] + pl[q]);
+    store(pp + o, pk);
+    // status_update: species clamps at inner points
+    if (any_inner) {
+      for (int n = 0; n < g.nqx; ++n) {
+        float x[4];
+        ld4f(x, qx + o + (size_t)n * F);
+        bool ch = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (inner[q] && x[q] < float(qx_check(n))) {
+            x[q] = float(qx_zero(n));
+            ch = true;
+          }
+        if (ch) store(qx + o + (size_t)n * F, x);
+      }
+      for (int n = 0; n < g.ntr; ++n) {
+        float x[4];
+        ld4f(x, trac + o + (size_t)n * F);
+        bool ch = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (inner[q] && x[q] < 0.f) {
+            x[q] = 0.f;
+            ch = true;
+          }
+        if (ch) store(trac + o + (size_t)n * F, x);
+      }
+    }
+    float tk[4], tl[4], tv[4], rh[4], th_o[4], tl_o[4], qs[4];
+    ld4f(tk, tt + o);
+    ld4f(tl, tlo + o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const size_t oq = o + q;
+      const float qf = qfactor(qx, oq, F, ipp);
+      tv[q] = tk[q] * qf;
+      rh[q] = pk[q] / (float(kRgas) * tk[q]);
+      // theta_v = tvirt/pai from the double-float t (Main/mod_moloch.F90:1403-1443)
+      const F2 th2 = df_div(df_mul(F2{tk[q], tl[q]}, qfactor_df(qx, oq, F, ipp)), F2{ph[q], pl[q]});
+      th_o[q] = th2.hi;
+      tl_o[q] = th2.lo;
+      qs[q] = pfwsat_f(tk[q], pk[q]);
+    }
+    store(tvir + o, tv);
+    store(rho + o, rh);
+    store(th_h + o, th_o);
+    store(th_h + F + o, tl_o);
+    store(qsat + o, qs);
+  }
+}
+
 // uvxtouvstag at the end of status_update (:1440)
 template <class R>
 __global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
@@ -804,9 +965,15 @@ template <class R>
 void Launch<R>::end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   k_end_ps<R><<<grid2(L.jx - 3, L.iy - 3, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
-  int tj;
-  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-  k_end_cross<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  if constexpr (sizeof(R) == sizeof(float)) {
+    const int tj = (L.jx - 1 + 127) / 128, ti = (L.iy - 1 + 3) / 4;
+    const dim3 grd((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels), (unsigned)L.nmem);
+    k_end_cross_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, advoff, tj);
+  } else {
+    int tj;
+    const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+    k_end_cross<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  }
 }
 
 template <class R>
