@@ -260,19 +260,20 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
     R xfn;
     if constexpr (sizeof(R) == sizeof(float)) xfn = nud ? sa.tnudge_r[k - 1] * xfn0 : R(0);
     else xfn = nud ? R(sa.tnudge[k - 1] * trtau * c.dtsec) : R(0);
-    if (up) {
+    // only nudged levels and the relaxation zone change anything
+    if (up && (nud || ibu > 0)) {
       R f = st.u[o];
       if (nud) f = bdy_relax_to<R>(f, xfn, blend(bd.dub, o));
       if (ibu > 0) f = relax(f, blend(bd.dub, o), ibu, k);
       st.u[o] = f;
     }
-    if (vp) {
+    if (vp && (nud || ibv > 0)) {
       R f = st.v[o];
       if (nud) f = bdy_relax_to<R>(f, xfn, blend(bd.dvb, o));
       if (ibv > 0) f = relax(f, blend(bd.dvb, o), ibv, k);
       st.v[o] = f;
     }
-    if (!cr) continue;
+    if (!cr || (!nud && ibc <= 0)) continue;
     if constexpr (sizeof(R) == sizeof(float)) {
       // (1-x)*t + x*b as t + x*(b - t) on the double-float t
       F2 f{st.t[o], D.wz[1][o]};
