@@ -88,3 +88,46 @@ def test_mixed_one_step_pointwise(htile):
             d = np.abs(got[n] - ref[n]).max() / np.abs(ref[n]).max()
             assert d <= tol, (htile, m, n, d)
     b.close()
+
+
+def _variants(prec):
+    def small_dry(**kw):
+        return cs.build(24, 22, 12, dx=12000.0, dt=60.0, nsound=3, moist=False, seed=3,
+                        hills=[(12 * 12000.0, 11 * 12000.0, 600.0)], wind=10.0, theta_noise=0.3,
+                        tracer=True, name="small_dry", precision=prec, **kw)
+
+    def small_moist(**kw):
+        return cs.build(40, 38, 14, dx=3000.0, dt=20.0, nsound=4, moist=True, seed=4,
+                        hills=[(20 * 3000.0, 18 * 3000.0, 1200.0), (8 * 3000.0, 30 * 3000.0, 400.0)],
+                        jet=True, theta_noise=0.2, name="small_moist", precision=prec, **kw)
+
+    return {
+        "dry_tracer": small_dry,
+        "moist": small_moist,
+        "rotllr": lambda: small_dry(lrotllr=True),
+        "rotllr_moist": lambda: small_moist(lrotllr=True),
+        "no_bdy": lambda: small_dry(apply_bdy=False),
+        "nadv2": lambda: cs.build(24, 22, 12, dx=12000.0, dt=60.0, nsound=2, nadv=2, moist=False,
+                                  seed=7, wind=15.0, tracer=True, name="nadv2", precision=prec),
+        "moist_nsound5": lambda: cs.build(40, 36, 10, dx=3000.0, dt=20.0, nsound=5, moist=True,
+                                          seed=9, jet=True, name="moist5", precision=prec),
+    }
+
+
+@pytest.mark.parametrize("name", list(_variants(abi.MLC_PREC_FP64)))
+def test_mixed_variants_one_step(name):
+    """Every model option the FP64 parity tests cover (rotated pole, boundary
+    off, two advection rounds, five substeps), in mixed precision, against the
+    FP64 oracle point by point after one step: differences of FP32 rounding
+    size, far below those of a wrong index or branch (~1e-3 of the field)."""
+    got, ref, _, _ = run_mixed_vs_oracle(lambda p: _variants(p)[name](), 1)
+    vel = max(np.abs(ref["u"]).max(), np.abs(ref["v"]).max())
+    bounds = {"tetav": (np.abs(ref["tetav"]).max(), 1e-6), "pai": (np.abs(ref["pai"]).max(), 1e-7),
+              "u": (vel, 1e-5), "v": (vel, 1e-5), "w": (max(np.abs(ref["w"]).max(), 1e-3), 1e-4)}
+    if "qx" in ref:
+        bounds["qx"] = (np.abs(ref["qx"][..., 0]).max(), 1e-5)
+    if "trac" in ref:
+        bounds["trac"] = (np.abs(ref["trac"]).max(), 1e-5)
+    for n, (scale, tol) in bounds.items():
+        d = np.abs(got[n] - ref[n]).max() / scale
+        assert d <= tol, (name, n, d)
