@@ -77,7 +77,7 @@ typedef struct mlc_params {
   int32_t mo_divdamp;     /* divergence damping on/off           [mo_divdamp]   */
   int32_t mo_divfilter;   /* divergence filter on/off            [mo_divfilter] */
   int32_t mo_top_nudge;   /* top nudging on/off                  [mo_top_nudge] */
-  int32_t mo_spectral_nudge; /* spectral nudging: must be 0 (not built)   */
+  int32_t mo_spectral_nudge; /* spectral nudging on/off          [mo_spectral_nudge] */
   int32_t do_apply_bdy;   /* lateral boundary relaxation on/off [do_apply_bdy] */
   int32_t lrotllr;        /* ROTLLR projection branch            [iproj]   */
   int32_t ipptls;         /* microphysics class: 0,1,2           [ipptls]  */
@@ -88,6 +88,7 @@ typedef struct mlc_params {
   int32_t nztop;          /* levels nudged at the top            [nztop]   */
   int32_t debug_level;    /* > 0: mass budget every step         [debug_level] */
   int32_t precision;      /* MLC_PREC_FP64 or MLC_PREC_MIXED               */
+  double  dtrad;          /* spectral nudging interval [s] (radiation step) [dtrad] */
 } mlc_params;
 
 /* Time-invariant fields (host pointers, read once by mlc_bind_static).
@@ -115,6 +116,8 @@ typedef struct mlc_static_ptrs {
   const int32_t *ibnd_cr;             /* (jx,iy) zone index, cross points   */
   const int32_t *ibnd_ud;             /* (jx,iy) zone index, u points       */
   const int32_t *ibnd_vd;             /* (jx,iy) zone index, v points       */
+  const double  *cnudge;              /* (kz) spectral nudging weights (read
+                                         only when mo_spectral_nudge)       */
 } mlc_static_ptrs;
 
 /* Prognostic and diagnostic state (mo_atm fields, sfs%psa). */

@@ -54,6 +54,11 @@ int mlc_setup_relaxation(const mlc_dims *d, mlc_params *p, const double *zeta,
                          double *hefc, double *fcx, double *tnudge,
                          double *ffilt, double *gmeanz);
 
+/* The level weights of spectral nudging (lowpass_init, Main/mod_bdycod.F90:
+ * 3890-3894): cnudge(k) = dtrad/dtbdys * min((gmeanz(k)/mo_h)^2, 1), from the
+ * domain-mean level heights gmeanz (kz) of mlc_setup_relaxation. */
+int mlc_setup_spectral(const mlc_params *p, int kz, const double *gmeanz, double *cnudge);
+
 /* setup_boundaries (Main/mod_atm_interface.F90:384-545), one-process,
  * non-band domain: ibnd (jx, iy) = relaxation-zone index (>= 2) or -1.
  * ldotx/ldoty select dot (1) or cross (0) staggering in x and y:

@@ -55,6 +55,11 @@ struct Oracle {
   bool hb_cr = false, hb_ud = false, hb_vd = false;
   F3 bdywtu, bdywtv, bdywtw;
   double mo_dzita = 0, rdzita = 0, dtstepa = 0, dtsound = 0;
+  // spectral nudging (Main/mod_bdycod.F90:3844-3960)
+  int km = 0, lm = 0;
+  F2<double> bvx, bvy, sx, sy, zn1;
+  std::vector<double> cnudge;  // 1-based
+  double tspectral = 0;
 
   // ---- state ----
   F3 u, v, w, pai, tetav, t, tvirt, ux, vx, p, rho, qsat;
@@ -89,6 +94,10 @@ struct Oracle {
   void morelax_fraction(int j1, int j2, int i1, int i2, const F2<int32_t> &ibnd, bool hb,
                         F3 &f, double frac);
   void morelax_chiten();
+  void lowpass_init();
+  void lowpass_filter(int j1, int j2, int i1, int i2, int jj1, int jj2, int ii1, int ii2, F2<double> &f);
+  void mospectral_nudge(int j1, int j2, int i1, int i2, int jj1, int jj2, int ii1, int ii2, F3 &f,
+                        const F3 *bnd);
   void status_update(double dtinc);
   void massck(mlc_diag *dg);
   void uvstagtouvx();
@@ -225,6 +234,12 @@ int Oracle::bind_static(const mlc_static_ptrs *st) {
     zitah[k] = st->zitah[k - 1];
     ffilt[k] = st->ffilt[k - 1];
     tnudge[k] = st->tnudge ? st->tnudge[k - 1] : 0.0;
+  }
+  cnudge.assign(kz + 1, 0.0);
+  if (prm.mo_spectral_nudge) {
+    if (!st->cnudge) return MLC_ERR_INVALID;
+    for (int k = 1; k <= kz; ++k) cnudge[k] = st->cnudge[k - 1];
+    lowpass_init();
   }
   std::memcpy(hefc.d.data(), st->hefc, hefc.d.size() * sizeof(double));
   for (int n = 1; n <= prm.nspgx; ++n) fcx[n] = st->fcx ? st->fcx[n - 1] : 0.0;
@@ -763,7 +778,71 @@ void Oracle::tvirt_to_temp() {
       for (int j = jci1; j <= jci2; ++j) t(j, i, k) = tvirt(j, i, k) / qfac(qx, prm.ipptls, j, i, k);
 }
 
-// Main/mod_moloch.F90:448-529 (spectral nudging and diagnostics left out)
+// Main/mod_bdycod.F90:3844-3896 (serial: njcross = jx-1, nicross = iy-1,
+// ds in km); cnudge comes with the static fields.
+void Oracle::lowpass_init() {
+  const double ds = dx / 1000.0;
+  const int njcross = jx - 1, nicross = iy - 1;
+  km = std::max((int)std::lround((njcross * ds) / 1500.0), 1);
+  lm = std::max((int)std::lround((nicross * ds) / 750.0), 1);
+  const double dxa = mathpi / (double)(njcross - 1);
+  const double dya = mathpi / (double)(nicross - 1);
+  std::vector<double> px(2 * km + 1), py(2 * lm + 1);
+  for (int k = 1; k <= 2 * km; ++k) px[k] = std::exp(-std::pow((double)k / (double)km, 2));
+  for (int l = 1; l <= 2 * lm; ++l) py[l] = std::exp(-std::pow((double)l / (double)lm, 2));
+  bvx.init(jde1, jde2, 1, 2 * km);
+  bvy.init(ide1, ide2, 1, 2 * lm);
+  sx.init(ide1, ide2, 1, 2 * km);
+  sy.init(jde1, jde2, 1, 2 * lm);
+  zn1.init(jde1, jde2, ide1, ide2);
+  const int jxm1 = jx - 1, iym1 = iy - 1;
+  for (int k = 1; k <= 2 * km; ++k)
+    for (int j = jde1; j <= jde2; ++j)
+      bvx(j, k) = std::sqrt(2.0 / (double)jxm1 * px[k]) * std::sin(k * (j - 2) * dxa);
+  for (int l = 1; l <= 2 * lm; ++l)
+    for (int i = ide1; i <= ide2; ++i)
+      bvy(i, l) = std::sqrt(2.0 / (double)iym1 * py[l]) * std::sin(l * (i - 2) * dya);
+}
+
+// Main/mod_bdycod.F90:3898-3938 (row_reduce/column_reduce: one process)
+void Oracle::lowpass_filter(int j1, int j2, int i1, int i2, int jj1, int jj2, int ii1, int ii2,
+                            F2<double> &f) {
+  for (int k = 1; k <= 2 * km; ++k)
+    for (int i = i1; i <= i2; ++i) {
+      sx(i, k) = 0.0;
+      for (int j = jj1; j <= jj2; ++j) sx(i, k) = sx(i, k) + f(j, i) * bvx(j, k);
+    }
+  std::fill(f.d.begin(), f.d.end(), 0.0);
+  for (int k = 1; k <= 2 * km; ++k)
+    for (int i = i1; i <= i2; ++i)
+      for (int j = j1; j <= j2; ++j) f(j, i) = f(j, i) + sx(i, k) * bvx(j, k);
+  for (int l = 1; l <= 2 * lm; ++l)
+    for (int j = j1; j <= j2; ++j) {
+      sy(j, l) = 0.0;
+      for (int i = ii1; i <= ii2; ++i) sy(j, l) = sy(j, l) + f(j, i) * bvy(i, l);
+    }
+  std::fill(f.d.begin(), f.d.end(), 0.0);
+  for (int l = 1; l <= 2 * lm; ++l)
+    for (int i = i1; i <= i2; ++i)
+      for (int j = j1; j <= j2; ++j) f(j, i) = f(j, i) + sy(j, l) * bvy(i, l);
+}
+
+// Main/mod_bdycod.F90:3940-3960
+void Oracle::mospectral_nudge(int j1, int j2, int i1, int i2, int jj1, int jj2, int ii1, int ii2,
+                              F3 &f, const F3 *bnd) {
+  const double x1 = (xbctime + dt) * rtb;
+  const double x0 = 1.0 - x1;
+  for (int k = 1; k <= kz; ++k) {
+    for (int i = i1; i <= i2; ++i)
+      for (int j = j1; j <= j2; ++j)
+        zn1(j, i) = (x0 * bnd[0](j, i, k) + x1 * bnd[1](j, i, k)) - f(j, i, k);
+    lowpass_filter(j1, j2, i1, i2, jj1, jj2, ii1, ii2, zn1);
+    for (int i = ii1; i <= ii2; ++i)
+      for (int j = jj1; j <= jj2; ++j) f(j, i, k) = f(j, i, k) + cnudge[k] * zn1(j, i);
+  }
+}
+
+// Main/mod_moloch.F90:448-529 (diagnostics left out)
 void Oracle::boundary() {
   bdyval();
   if (prm.mo_top_nudge) motopnudge(0.0, dtsec);
@@ -779,6 +858,16 @@ void Oracle::boundary() {
       morelax_external(jci1, jci2, ici1, ici2, ibnd_cr, hb_cr, qx[2], xib);
   }
   if (ntr > 0) morelax_chiten();
+  if (prm.mo_spectral_nudge) {
+    // Main/mod_moloch.F90:499-506; the temperature call sums its x
+    // projection over jci1..jci1 only, as the reference passes it
+    tspectral = tspectral + dtsec;
+    if ((int)std::fmod(tspectral, prm.dtrad) == 0) {
+      mospectral_nudge(jce1, jce2, ice1, ice2, jci1, jci1, ici1, ici2, t, xtb);
+      mospectral_nudge(jde1, jde2, ice1, ice2, jdi1, jdi2, ici1, ici2, u, dub);
+      mospectral_nudge(jce1, jce2, ide1, ide2, jci1, jci2, idi1, idi2, v, dvb);
+    }
+  }
   uvstagtouvx();
   temp_to_tvirt();
   for (int k = 1; k <= kz; ++k)

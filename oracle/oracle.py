@@ -44,6 +44,7 @@ def load():
         lib.orc_setup_relaxation.argtypes = [P(abi.mlc_dims), P(abi.mlc_params), dp, dp, dp, dp,
                                              dp, P(C.c_int)]
         lib.orc_setup_boundaries.argtypes = [C.c_int] * 6 + [P(C.c_int32)]
+        lib.orc_setup_spectral.argtypes = [P(abi.mlc_params), C.c_int, dp, dp]
         lib.orc_paicompute.argtypes = [P(abi.mlc_dims)] + [dp] * 5 + [C.c_double, dp]
         _lib = lib
     return _lib

@@ -202,6 +202,17 @@ int orc_setup_relaxation(const mlc_dims *d, const mlc_params *p, const double *z
   return 0;
 }
 
+// lowpass_init's level weights (Main/mod_bdycod.F90:3890-3894).
+int orc_setup_spectral(const mlc_params *p, int kz, const double *gmeanz, double *cnudge) {
+  const double rtb = 1.0 / p->dtbdys;
+  const double cn0 = p->dtrad * rtb;
+  for (int k = 1; k <= kz; ++k) {
+    const double r = gmeanz[k - 1] / p->mo_h;  // x**2 is x*x in Fortran
+    cnudge[k - 1] = cn0 * std::min(r * r, 1.0);
+  }
+  return 0;
+}
+
 // setup_boundaries, one process, non-band: ibnd (jx, iy).
 int orc_setup_boundaries(int jx, int iy, int ldotx, int ldoty, int nspgx, int nspgd, int32_t *out) {
   F2<int32_t> ibnd(1, jx, 1, iy, -1);

@@ -55,7 +55,7 @@ class mlc_params(C.Structure):
                 ("do_apply_bdy", C.c_int32), ("lrotllr", C.c_int32),
                 ("ipptls", C.c_int32), ("present_qc", C.c_int32), ("present_qi", C.c_int32),
                 ("nspgx", C.c_int32), ("nspgd", C.c_int32), ("nztop", C.c_int32),
-                ("debug_level", C.c_int32), ("precision", C.c_int32)]
+                ("debug_level", C.c_int32), ("precision", C.c_int32), ("dtrad", C.c_double)]
 
 
 STATIC_FIELDS = ["msfu", "msfv", "msfx", "ulat", "vlat", "rlat", "hx", "hy", "fmz", "fmzf",
@@ -64,8 +64,13 @@ STATIC_FIELDS = ["msfu", "msfv", "msfx", "ulat", "vlat", "rlat", "hx", "hy", "fm
 IBND_FIELDS = ["ibnd_cr", "ibnd_ud", "ibnd_vd"]
 
 
+# read only when mo_spectral_nudge is set
+SPECTRAL_FIELDS = ["cnudge"]
+
+
 class mlc_static_ptrs(C.Structure):
-    _fields_ = [(n, _dp) for n in STATIC_FIELDS] + [(n, _ip) for n in IBND_FIELDS]
+    _fields_ = ([(n, _dp) for n in STATIC_FIELDS] + [(n, _ip) for n in IBND_FIELDS] +
+                [(n, _dp) for n in SPECTRAL_FIELDS])
 
 
 STATE_FIELDS = ["u", "v", "w", "pai", "tetav", "t", "tvirt", "ux", "vx", "p", "rho", "qsat",
@@ -143,6 +148,7 @@ def _declare(lib):
         "mlc_setup_relaxation": (C.c_int, [P(mlc_dims), P(mlc_params), _dp, _dp, _dp, _dp, _dp,
                                            _dp]),
         "mlc_setup_boundaries": (C.c_int, [C.c_int] * 6 + [_ip]),
+        "mlc_setup_spectral": (C.c_int, [P(mlc_params), C.c_int, _dp, _dp]),
         "mlc_paicompute": (C.c_int, [P(mlc_dims), P(mlc_params)] + [_dp] * 7),
         "mlc_pfwsat": (C.c_int, [C.c_size_t, _dp, _dp, _dp]),
         "mlc_create_batch": (C.c_int, [P(mlc_dims), P(mlc_params), C.c_int, P(C.c_void_p)]),

@@ -103,7 +103,7 @@ class Case:
     # -- pointer structs (arrays stay owned by this object) ---------------
     def static_ptrs(self) -> abi.mlc_static_ptrs:
         s = abi.mlc_static_ptrs()
-        for n in abi.STATIC_FIELDS:
+        for n in abi.STATIC_FIELDS + abi.SPECTRAL_FIELDS:
             setattr(s, n, abi.dptr(self.static.get(n)))
         for n in abi.IBND_FIELDS:
             setattr(s, n, abi.iptr(self.static[n]))
@@ -145,7 +145,7 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
           moist: bool = False, seed: int = 0, hills=None, wind=10.0, jet: bool = False,
           theta_noise: float = 0.1, tracer: bool = False, precision: int = abi.MLC_PREC_FP64,
           name: str = "case", debug_level: int = 1, lrotllr: bool = False,
-          apply_bdy: bool = True) -> Case:
+          apply_bdy: bool = True, spectral: bool = False, dtrad: float = 1800.0) -> Case:
     """Build one synthetic domain of nx x ny cross points and kz levels."""
     lib = abi.load()
     jx, iy = nx + 1, ny + 1
@@ -157,7 +157,8 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
     p.mo_ztop, p.mo_h, p.mo_a0 = 25000.0, 8000.0, 0.0
     p.mo_nadv, p.mo_nsound = nadv, nsound
     p.mo_divdamp = p.mo_divfilter = p.mo_top_nudge = 1
-    p.mo_spectral_nudge = 0
+    p.mo_spectral_nudge = 1 if spectral else 0
+    p.dtrad = float(dtrad)
     p.do_apply_bdy = 1 if apply_bdy else 0
     p.lrotllr = 1 if lrotllr else 0
     p.ipptls = 2 if moist else 0
@@ -222,6 +223,10 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
         st[n] = np.zeros((jx, iy), dtype=np.int32, order="F")
         abi.check(lib.mlc_setup_boundaries(jx, iy, lx, ly, p.nspgx, p.nspgd, abi.iptr(st[n])),
                   "mlc_setup_boundaries")
+    if spectral:
+        st["cnudge"] = _f((kz,))
+        abi.check(lib.mlc_setup_spectral(C.byref(p), kz, abi.dptr(st["gmeanz"]),
+                                         abi.dptr(st["cnudge"])), "mlc_setup_spectral")
 
     # ---- atmosphere on cross points ----
     rng_n = 0

@@ -79,6 +79,16 @@ Geom make_geom(const mlc_dims &d, int elem_bytes) {
   return g;
 }
 
+// Sine modes of spectral nudging (lowpass_init, Main/mod_bdycod.F90:3852-3853;
+// one process: njcross = jx-1, nicross = iy-1, ds in km): 2*km in x, 2*lm in y.
+void spectral_modes(const mlc_dims &d, const mlc_params &p, int &km2, int &lm2) {
+  const double ds = p.dx / 1000.0;
+  const long km = std::lround(((double)(d.jx - 1) * ds) / 1500.0);
+  const long lm = std::lround(((double)(d.iy - 1) * ds) / 750.0);
+  km2 = 2 * (int)std::max(km, 1L);
+  lm2 = 2 * (int)std::max(lm, 1L);
+}
+
 Scal make_scal(const mlc_params &p) {
   Scal c{};
   c.dx = p.dx;
@@ -111,6 +121,8 @@ Scal make_scal(const mlc_params &p) {
   c.dxrdt = c.dx / c.dtsound;
   c.dtrdxsf = c.dtsoundf * c.rdxf;
   c.dxrdtf = c.dxf / c.dtsoundf;
+  c.spectral = p.mo_spectral_nudge;
+  c.dtrad = p.dtrad;
   return c;
 }
 
@@ -180,6 +192,17 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
     b.chib[h] = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;
     b.xpsb[h] = cv.take<double>(P2);
   }
+  if (p.mo_spectral_nudge) {
+    int km2, lm2;
+    spectral_modes(d, p, km2, lm2);
+    s.bvx = cv.take<R>((size_t)km2 * d.jx);
+    s.bvy = cv.take<R>((size_t)lm2 * d.iy);
+    s.cnudge = cv.take<R>(d.kz);
+    D.spec = cv.take<R>((size_t)3 * d.kz * d.iy * km2);
+  } else {
+    s.bvx = s.bvy = s.cnudge = nullptr;
+    D.spec = nullptr;
+  }
   D.red_blocks = reduce_blocks(g);
   D.partials = cv.take<double>((size_t)D.red_blocks * 8);
   D.tmap = cv.take<char>((size_t)kTileShapes * kTmapSlots * kTmapBytes);
@@ -199,7 +222,7 @@ int validate_params(const mlc_params *p) {
     return MLC_ERR_INVALID;
   if (!(p->dtbdys > 0) || p->nspgx < 3 || p->nspgd < 3) return MLC_ERR_INVALID;
   if (p->ipptls < 0 || p->ipptls > 2) return MLC_ERR_UNSUPPORTED;
-  if (p->mo_spectral_nudge) return MLC_ERR_UNSUPPORTED;
+  if (p->mo_spectral_nudge && !(p->dtrad > 0)) return MLC_ERR_INVALID;
   if (p->precision != MLC_PREC_FP64 && p->precision != MLC_PREC_MIXED) return MLC_ERR_INVALID;
   return MLC_OK;
 }
@@ -218,6 +241,11 @@ int validate_dims(const mlc_dims *d, const mlc_params *p) {
   if (n_table_r(*d, *p, true) > kMaxFields) return MLC_ERR_UNSUPPORTED;
   // the tracer relaxation assumes disjoint south/north and west/east bands
   if (d->ntr > 0 && (d->jx - 1 < 2 * p->nspgx || d->iy - 1 < 2 * p->nspgx)) return MLC_ERR_UNSUPPORTED;
+  if (p->mo_spectral_nudge) {
+    int km2, lm2;
+    spectral_modes(*d, *p, km2, lm2);
+    if (km2 > kMaxModes || lm2 > kMaxModes) return MLC_ERR_UNSUPPORTED;
+  }
   return MLC_OK;
 }
 
@@ -393,6 +421,7 @@ int add_member(mlc_ctx *x, int slot, const mlc_dims &d) {
   m.dims = d;
   m.g = make_geom(d, x->mixed ? 4 : 8);
   m.c = make_scal(x->prm);
+  if (x->prm.mo_spectral_nudge) spectral_modes(d, x->prm, m.c.km2, m.c.lm2);
   m.bytes = x->mixed ? arena_bytes<float>(d, x->prm) : arena_bytes<double>(d, x->prm);
   if (x->budget && x->in_use + m.bytes > x->budget) return MLC_ERR_BUDGET;
   MLC_CHK(ensure_staging(x, d));
@@ -551,6 +580,7 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
   if (x->prm.do_apply_bdy) {
     REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); nl += 2;
     REC("bdy_relax", K::bdy_relax(L, d, uvo, ao, s)); ++nl;
+    if (x->prm.mo_spectral_nudge) { REC("bdy_spectral", K::bdy_spectral(L, d, uvo, ao, s)); nl += 3; }
   }
   REC("end_cross", K::end_cross(L, d, uvo, ao, s)); nl += 2;
   REC("end_uvstag", K::end_uvstag(L, d, uvo, ao, s)); ++nl;
@@ -707,6 +737,16 @@ int get3x(mlc_ctx *x, const Geom &g, const double *src, double *h, int nj, int n
   Launch<R>::pack3_df(src, x->staging + soff, g, nj, ni, nk, nplane, x->stream);
   MLC_TRY(cudaMemcpyAsync(h, x->staging + soff, n * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
   return MLC_OK;
+}
+
+// A 1-D array of the field type that has no FP64 twin (written in both
+// precisions).
+template <class R>
+int put1_as(mlc_ctx *x, const double *h, const R *dst, size_t n) {
+  std::vector<R> tmp(n);
+  for (size_t e = 0; e < n; ++e) tmp[e] = (R)h[e];
+  MLC_TRY(cudaMemcpyAsync(W(dst), tmp.data(), n * sizeof(R), cudaMemcpyHostToDevice, x->stream));
+  return cuda_status(cudaStreamSynchronize(x->stream));
 }
 
 // A 1-D array in the field type (mixed members keep FP32 copies).
@@ -875,6 +915,28 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
     MLC_CHK(put1r<R>(x, s->fcx, a.fcx_r, p.nspgx));
   }
   if (s->rlat) MLC_CHK(put1(x, s->rlat, a.rlat, iy));
+  if (p.mo_spectral_nudge) {
+    // lowpass_init (Main/mod_bdycod.F90:3844-3896, one process: njcross =
+    // jx-1, nicross = iy-1) in FP64, rows of the modes k = 1..2km over
+    // j = 1..jx (jde) and l = 1..2lm over i = 1..iy (ide)
+    if (!s->cnudge) return MLC_ERR_INVALID;
+    const int km2 = c.km2, lm2 = c.lm2;
+    const double dxa = kPi / (double)(jx - 2), dya = kPi / (double)(iy - 2);
+    std::vector<double> bx((size_t)km2 * jx), by((size_t)lm2 * iy);
+    for (int m = 1; m <= km2; ++m) {
+      const double r = (double)m / (double)(km2 / 2);
+      const double amp = std::sqrt(2.0 / (double)(jx - 1) * std::exp(-(r * r)));
+      for (int j = 1; j <= jx; ++j) bx[(size_t)(m - 1) * jx + (j - 1)] = amp * std::sin(m * (j - 2) * dxa);
+    }
+    for (int l = 1; l <= lm2; ++l) {
+      const double r = (double)l / (double)(lm2 / 2);
+      const double amp = std::sqrt(2.0 / (double)(iy - 1) * std::exp(-(r * r)));
+      for (int i = 1; i <= iy; ++i) by[(size_t)(l - 1) * iy + (i - 1)] = amp * std::sin(l * (i - 2) * dya);
+    }
+    MLC_CHK(put1_as<R>(x, bx.data(), a.bvx, bx.size()));
+    MLC_CHK(put1_as<R>(x, by.data(), a.bvy, by.size()));
+    MLC_CHK(put1_as<R>(x, s->cnudge, a.cnudge, kz));
+  }
   MLC_TRY(cudaStreamSynchronize(x->stream));
   return MLC_OK;
 }
@@ -1118,7 +1180,8 @@ void mlc_default_params(mlc_params *p) {
   p->mo_divdamp = 1;
   p->mo_divfilter = 1;
   p->mo_top_nudge = 1;
-  p->mo_spectral_nudge = 0;  // built path: spectral nudging off
+  p->mo_spectral_nudge = 0;
+  p->dtrad = 1800.0;  // Main/mod_params.F90:1229-1230
   p->do_apply_bdy = 1;
   p->lrotllr = 0;
   p->ipptls = 1;

@@ -41,7 +41,12 @@ struct Scal {
   int present_qc, present_qi, nspgx, nztop, debug_level;
   int hb_cr, hb_ud, hb_vd;  // relaxation zone non-empty (ba%havebound)
   int curvature;            // curvature terms are not identically zero
+  int spectral;             // spectral nudging on
+  int km2, lm2;             // sine modes in x and y (2*km, 2*lm)
+  double dtrad;             // spectral nudging interval
 };
+// sine modes of spectral nudging per direction, at most
+constexpr int kMaxModes = 32;
 
 // Time-invariant device arrays.  Metric arrays use the field type R.
 template <class R>
@@ -61,6 +66,9 @@ struct Stat {
   const double *rlat;      // (iy)
   // the 1-D arrays, hefc, fcx and dz in the field type (aliases for FP64)
   const R *gzitak_r, *gzitakh_r, *xkdamp_r, *xknu_r, *ffilt_r, *tnudge_r, *hefc_r, *fcx_r, *dz_r;
+  // spectral nudging: sine bases bvx (km2 rows of jx) and bvy (lm2 rows of
+  // iy), the level weights cnudge (kz)
+  const R *bvx, *bvy, *cnudge;
 };
 
 // Prognostic and diagnostic state.
@@ -107,6 +115,7 @@ struct Clock {
   int uv_role;       // half of the u/v pairs holding the state at step start
   int adv_role;      // half of the advected-field pairs holding the state
   int fault;         // sticky: a bounded device wait gave up (1 = TMA tile load)
+  double tspectral;  // seconds of boundary updates, for the spectral nudging interval
 };
 
 // Mass budget and ps extrema of the last step (FP64).
@@ -136,6 +145,7 @@ struct Dom {
   Clock *clk;
   DiagDev *diag;
   double *partials;
+  R *spec;               // spectral nudging: per field and level, iy rows of km2 coefficients
   int red_blocks;
   int active;            // 0: an empty slot, every block returns at once
   // TMA tensor maps (CUtensorMap, 128 B each, 64-B aligned) of the wz fields,

@@ -324,6 +324,173 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   }
 }
 
+// ---- spectral nudging (Main/mod_bdycod.F90:3898-3960, called from
+// Main/mod_moloch.F90:499-506 after the relaxation) ----
+// The reference projects the departure d = blend(b0,b1) - f of t, u and v
+// onto km2 sine modes in x (sums over the field's interior columns jj), back
+// to the grid, onto lm2 modes in y (sums over its interior rows ii) and back,
+// and adds cnudge(k) times the result on jj x ii.  Only d on jj x ii enters,
+// and the four passes factor into
+//   sx(i,m) = sum_{j in jj} d(j,i) bvx(j,m)                 (k_spec_rows)
+//   C(m,l)  = sum_{i in ii} sx(i,m) bvy(i,l)                (k_spec_modes)
+//   G(i,m)  = sum_l C(m,l) bvy(i,l)                          (k_spec_modes)
+//   f(j,i) += cnudge(k) sum_m bvx(j,m) G(i,m)                (k_spec_apply)
+// per field, level and member.  Ranges: t jj = jci1..jci1 (the reference's
+// call passes jci1 as both bounds), ii = ici; u jdi x ici; v jci x idi.
+// The kernels run every step and return at once unless the interval is due.
+
+// the step's boundary update is a spectral nudging step: tspectral + dtsec
+// (the reference's tspectral after its increment) is a multiple of dtrad
+__device__ __forceinline__ bool spectral_due(const Scal &c, const Clock *clk) {
+  return c.spectral && (int)fmod(clk->tspectral + c.dtsec, c.dtrad) == 0;
+}
+struct SpecRange {
+  int jj1, jj2, ii1, ii2;
+};
+__device__ __forceinline__ SpecRange spec_range(int f, const Geom &g) {
+  if (f == 0) return {2, 2, 2, g.iy - 2};
+  if (f == 1) return {2, g.jx - 1, 2, g.iy - 2};
+  return {2, g.jx - 2, 2, g.iy - 1};
+}
+
+// Departure of field f (0 t, 1 u, 2 v) from the blended boundary data at o.
+template <class R>
+__device__ __forceinline__ R spec_departure(const Dom<R> &D, const State<R> &st, int f, size_t o,
+                                            double x0, double x1) {
+  const Bdy<R> &bd = D.bd;
+  if (f == 0) {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      const size_t F = D.g.field3();
+      const DF b0(bd.xtb[0], F), b1(bd.xtb[1], F);
+      const F2 a = b0.ld(o);
+      const F2 bt = df_add_f(a, float(x1) * df_diff(b1.ld(o), a));
+      return df_diff(bt, F2{st.t[o], D.wz[1][o]});
+    } else {
+      return (x0 * bd.xtb[0][o] + x1 * bd.xtb[1][o]) - st.t[o];
+    }
+  }
+  const R *const *b = f == 1 ? bd.dub : bd.dvb;
+  const R cur = f == 1 ? st.u[o] : st.v[o];
+  return bdy_blend<R>(R(x0), R(x1), b[0][o], b[1][o]) - cur;
+}
+
+// sx(i, m) of one row: a warp per row i, lanes over j; grid (rows/8,
+// kz*3, members), 256 threads.
+template <class R>
+__global__ void __launch_bounds__(256) k_spec_rows(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Scal &c = D.c;
+  const Clock *clk = D.clk;
+  if (!spectral_due(c, clk)) return;
+  const Geom g = D.g;
+  const int k = (int)blockIdx.y / 3 + 1, f = (int)blockIdx.y % 3;
+  if (k > g.kz) return;
+  const SpecRange r = spec_range(f, g);
+  const int lane = (int)threadIdx.x & 31;
+  const int i = r.ii1 + (int)blockIdx.x * 8 + ((int)threadIdx.x >> 5);
+  if (i > r.ii2) return;
+  const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
+  const double x1 = (clk->xbctime + c.dtsec + c.dt) * c.rtb, x0 = 1.0 - x1;
+  const int km2 = c.km2;
+  const R *bvx = D.sa.bvx;
+  R acc[kMaxModes];
+#pragma unroll
+  for (int m = 0; m < kMaxModes; ++m) acc[m] = R(0);
+  const size_t row = g.at2(1, i) + (size_t)(k - 1) * g.PS;
+  for (int j = r.jj1 + lane; j <= r.jj2; j += 32) {
+    const R dv = spec_departure(D, st, f, row + (size_t)(j - 1), x0, x1);
+#pragma unroll
+    for (int m = 0; m < kMaxModes; ++m)
+      if (m < km2) acc[m] += dv * bvx[(size_t)m * g.jx + (j - 1)];
+  }
+  R mine = R(0);
+#pragma unroll
+  for (int m = 0; m < kMaxModes; ++m) {
+    if (m < km2) {
+      R v = acc[m];
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+      if (lane == m) mine = v;
+    }
+  }
+  if (lane < km2)
+    D.spec[((size_t)(f * g.kz + k - 1) * g.iy + (size_t)(i - 1)) * km2 + lane] = mine;
+}
+
+// C(m, l) in shared memory, then G(i, m) over sx in place; one block of 256
+// threads per field, level and member.
+template <class R>
+__global__ void __launch_bounds__(256) k_spec_modes(const Dom<R> *__restrict__ doms) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Scal &c = D.c;
+  if (!spectral_due(c, D.clk)) return;
+  const Geom g = D.g;
+  const int k = (int)blockIdx.y / 3 + 1, f = (int)blockIdx.y % 3;
+  if (k > g.kz) return;
+  const SpecRange r = spec_range(f, g);
+  const int km2 = c.km2, lm2 = c.lm2, ni = r.ii2 - r.ii1 + 1;
+  const R *bvy = D.sa.bvy;
+  R *sx = D.spec + (size_t)(f * g.kz + k - 1) * g.iy * km2;
+  __shared__ R cm[kMaxModes * kMaxModes];
+  for (int p = (int)threadIdx.x; p < km2 * lm2; p += (int)blockDim.x) {
+    const int m = p / lm2, l = p % lm2;
+    R a = R(0);
+    for (int i = r.ii1; i <= r.ii2; ++i) a += sx[(size_t)(i - 1) * km2 + m] * bvy[(size_t)l * g.iy + (i - 1)];
+    cm[p] = a;
+  }
+  __syncthreads();
+  for (int p = (int)threadIdx.x; p < ni * km2; p += (int)blockDim.x) {
+    const int i = r.ii1 + p / km2, m = p % km2;
+    R a = R(0);
+    for (int l = 0; l < lm2; ++l) a += cm[m * lm2 + l] * bvy[(size_t)l * g.iy + (i - 1)];
+    sx[(size_t)(i - 1) * km2 + m] = a;
+  }
+}
+
+// f(j,i,k) += cnudge(k) sum_m bvx(j,m) G(i,m) for t, u and v at one point
+// (j, i from 2), kPtLevels levels per thread.
+template <class R>
+__global__ void k_spec_apply(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Scal &c = D.c;
+  const Clock *clk = D.clk;
+  if (!spectral_due(c, clk)) return;
+  const Geom g = D.g;
+  const Pt q_ = point_of(tiles_j, 2, 2);
+  const int j = q_.j, i = q_.i, k0 = q_.k;
+  if (k0 > g.kz || j > g.jx - 1 || i > g.iy - 1) return;
+  const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
+  const int km2 = c.km2;
+  const R *bvx = D.sa.bvx + (j - 1);
+  const size_t ij = g.at2(j, i);
+  auto proj = [&](int f, int k) {
+    const R *gg = D.spec + ((size_t)(f * g.kz + k - 1) * g.iy + (size_t)(i - 1)) * km2;
+    R a = R(0);
+    for (int m = 0; m < km2; ++m) a += bvx[(size_t)m * g.jx] * gg[m];
+    return a;
+  };
+  const bool tp = j == 2 && i <= g.iy - 2, up = i <= g.iy - 2, vp = j <= g.jx - 2;
+#pragma unroll
+  for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * g.PS;
+    const R cn = D.sa.cnudge[k - 1];
+    if (tp) {
+      if constexpr (sizeof(R) == sizeof(float)) {
+        const F2 t = df_add_f(F2{st.t[o], D.wz[1][o]}, cn * proj(0, k));
+        st.t[o] = t.hi;
+        D.wz[1][o] = t.lo;
+      } else {
+        st.t[o] = st.t[o] + cn * proj(0, k);
+      }
+    }
+    if (up) st.u[o] = st.u[o] + cn * proj(1, k);
+    if (vp) st.v[o] = st.v[o] + cn * proj(2, k);
+  }
+}
+
 // extrapolate_surface_pressure (:1592-1606) per interior column, from t
 // and q at the two lowest levels before status_update clamps q, and p at the
 // lowest level (the same expression k_end_cross stores).
@@ -857,6 +1024,7 @@ __global__ void k_reduce_final(const Dom<R> *__restrict__ doms, int uvoff, int a
   diag->nonfinite = isbad ? 1 : 0;
   if (isbad && !clk->nonfinite) { clk->nonfinite = 1; clk->bad_step = clk->step; }
   if (D.c.apply_bdy) clk->xbctime = clk->xbctime + D.c.dtsec;
+  if (D.c.apply_bdy && D.c.spectral) clk->tspectral = clk->tspectral + D.c.dtsec;
   clk->step = clk->step + 1;
   clk->uv_role = (clk->uv_role + uvoff) & 1;
   clk->adv_role = (clk->adv_role + advoff) & 1;
@@ -960,6 +1128,18 @@ void Launch<R>::bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int a
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 2, L.iy - 2, tj);
   k_bdy_relax<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+}
+
+template <class R>
+void Launch<R>::bdy_spectral(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
+                             cudaStream_t s) {
+  const unsigned fk = (unsigned)(L.kz * 3);
+  k_spec_rows<R><<<dim3((unsigned)((L.iy + 7) / 8), fk, (unsigned)L.nmem), 256, 0, s>>>(d, uvoff, advoff);
+  k_spec_modes<R><<<dim3(1, fk, (unsigned)L.nmem), 256, 0, s>>>(d);
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 2, L.iy - 2, tj);
+  k_spec_apply<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
 }
 
 template <class R>

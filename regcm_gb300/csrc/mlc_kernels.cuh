@@ -53,6 +53,7 @@ template <class R> struct Launch {
   static void end_tvirt(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
   static void bdy_ring(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  static void bdy_spectral(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void end_uvstag(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void end_reduce(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,

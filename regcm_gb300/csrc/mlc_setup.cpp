@@ -209,6 +209,18 @@ int mlc_relax_coefficients(int np, double gmmin, double gmmax, double *coeff) {
   return MLC_OK;
 }
 
+int mlc_setup_spectral(const mlc_params *p, int kz, const double *gmeanz, double *cnudge) {
+  if (!p || !gmeanz || !cnudge || kz < 1 || p->dtbdys <= 0.0 || p->mo_h <= 0.0)
+    return MLC_ERR_INVALID;
+  const double cn0 = p->dtrad * (1.0 / p->dtbdys);
+  for (int k = 0; k < kz; ++k) {
+    const double r = gmeanz[k] / p->mo_h;
+    const double r2 = r * r;
+    cnudge[k] = cn0 * (r2 < 1.0 ? r2 : 1.0);
+  }
+  return MLC_OK;
+}
+
 int mlc_setup_relaxation(const mlc_dims *d, mlc_params *p, const double *zeta, double *hefc,
                          double *fcx, double *tnudge, double *ffilt, double *gmeanz_out) {
   if (!d || !p || !zeta || !hefc) return MLC_ERR_INVALID;

@@ -44,12 +44,14 @@ module mod_moloch_gb300
     integer(c_int32_t) :: mo_top_nudge, mo_spectral_nudge, do_apply_bdy
     integer(c_int32_t) :: lrotllr, ipptls, present_qc, present_qi
     integer(c_int32_t) :: nspgx, nspgd, nztop, debug_level, precision
+    real(c_double) :: dtrad
   end type mlc_params
 
   type, bind(c) :: mlc_static_ptrs
     type(c_ptr) :: msfu, msfv, msfx, ulat, vlat, rlat, hx, hy
     type(c_ptr) :: fmz, fmzf, rfmzu, rfmzv, zeta, dz, zita, zitah
     type(c_ptr) :: ffilt, hefc, fcx, tnudge, ibnd_cr, ibnd_ud, ibnd_vd
+    type(c_ptr) :: cnudge
   end type mlc_static_ptrs
 
   type, bind(c) :: mlc_state_ptrs
@@ -118,6 +120,13 @@ module mod_moloch_gb300
       type(mlc_params), intent(inout) :: p
       type(c_ptr), value :: zeta, hefc, fcx, tnudge, ffilt, gmeanz
     end function
+    integer(c_int) function mlc_setup_spectral(p, kz, gmeanz, cnudge) &
+        bind(c, name='mlc_setup_spectral')
+      import :: c_int, c_ptr, mlc_params
+      type(mlc_params), intent(in) :: p
+      integer(c_int), value :: kz
+      type(c_ptr), value :: gmeanz, cnudge
+    end function
   end interface
 
   type(c_ptr), save :: ctx = c_null_ptr
@@ -129,6 +138,7 @@ module mod_moloch_gb300
   ! the library's restatement of setup_bdycon/init builds them here
   real(c_double), allocatable, target, save :: hefc_l(:,:), fcx_l(:)
   real(c_double), allocatable, target, save :: tnudge_l(:), ffilt_l(:), gmeanz_l(:)
+  real(c_double), allocatable, target, save :: cnudge_l(:)
 
   contains
 
@@ -161,6 +171,7 @@ module mod_moloch_gb300
     prm%mo_divfilter = merge(1, 0, mo_divfilter)
     prm%mo_top_nudge = merge(1, 0, mo_top_nudge)
     prm%mo_spectral_nudge = merge(1, 0, mo_spectral_nudge)
+    prm%dtrad = dtrad
     prm%do_apply_bdy = 1
     prm%lrotllr = merge(1, 0, iproj == 'ROTLLR')
     prm%ipptls = ipptls
@@ -180,6 +191,12 @@ module mod_moloch_gb300
     call check(mlc_setup_relaxation(dims, prm, c_loc(mo_atm%zeta), c_loc(hefc_l), &
                c_loc(fcx_l), c_loc(tnudge_l), c_loc(ffilt_l), c_loc(gmeanz_l)), &
                'init_moloch(relaxation)')
+    allocate(cnudge_l(kz))
+    cnudge_l = 0.0_c_double
+    if ( mo_spectral_nudge ) then
+      call check(mlc_setup_spectral(prm, int(kz, c_int), c_loc(gmeanz_l), c_loc(cnudge_l)), &
+                 'init_moloch(spectral)')
+    end if
     call check(mlc_create(dims, prm, ctx), 'init_moloch(create)')
     allocate(ibcr(jde1:jde2,ide1:ide2), ibud(jde1:jde2,ide1:ide2), &
              ibvd(jde1:jde2,ide1:ide2))
@@ -209,6 +226,7 @@ module mod_moloch_gb300
     s%ibnd_cr = c_loc(ibcr)
     s%ibnd_ud = c_loc(ibud)
     s%ibnd_vd = c_loc(ibvd)
+    s%cnudge = c_loc(cnudge_l)
     call check(mlc_bind_static(ctx, s), 'init_moloch(static)')
     call upload( )
     b%xtb(1) = c_loc(xtb%b0)

@@ -52,13 +52,15 @@ def test_create_rejects_bad_input_before_touching_the_device():
     p = abi.mlc_params()
     lib.mlc_default_params(C.byref(p))
     ctx = C.c_void_p()
-    # too few levels / spectral nudging requested / no output pointer
+    # too few levels / spectral nudging without an interval / no output pointer
     assert lib.mlc_create(C.byref(abi.mlc_dims(65, 65, 2, 2, 0)), C.byref(p), C.byref(ctx)) == \
         abi.MLC_ERR_INVALID
     p.mo_spectral_nudge = 1
+    p.dtrad = 0.0
     assert lib.mlc_create(C.byref(abi.mlc_dims(65, 65, 30, 2, 0)), C.byref(p), C.byref(ctx)) == \
-        abi.MLC_ERR_UNSUPPORTED
+        abi.MLC_ERR_INVALID
     p.mo_spectral_nudge = 0
+    p.dtrad = 1800.0
     p.ipptls = 2
     assert lib.mlc_create(C.byref(abi.mlc_dims(65, 65, 30, 2, 0)), C.byref(p), C.byref(ctx)) == \
         abi.MLC_ERR_INVALID  # ipptls 2 needs qv..qs

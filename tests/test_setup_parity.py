@@ -99,6 +99,12 @@ def test_metric_relaxation_pai(moist, lrot):
     assert np.array_equal(fcx, st["fcx"])
     assert np.array_equal(tn, st["tnudge"]) and np.array_equal(ff, st["ffilt"])
     assert nz.value == p.nztop
+    # spectral nudging weights from the level-mean heights
+    cn_lib, cn_orc = np.zeros(kz), np.zeros(kz)
+    assert abi.load().mlc_setup_spectral(C.byref(p), kz, abi.dptr(st["gmeanz"]), abi.dptr(cn_lib)) == 0
+    ol.orc_setup_spectral(C.byref(p), kz, abi.dptr(st["gmeanz"]), abi.dptr(cn_orc))
+    assert np.array_equal(cn_lib, cn_orc)
+    assert np.all(cn_lib >= 0) and cn_lib.max() <= p.dtrad / p.dtbdys
     # paicompute on the case's own inputs
     t = c.bdy["xtb"][0]
     qv = c.bdy["xqb"][0]
