@@ -194,9 +194,10 @@ int mlc_set_boundary(mlc_ctx *ctx, const mlc_bdy_ptrs *b, double xbctime,
                      double dtbdys);
 
 /* moloch (Main/mod_moloch.F90:312-446) nsteps times: dynamical core,
- * boundary relaxation, diagnostics, status update, mass budget (when
- * debug_level > 0) and the NaN/Inf check on ps.  Physics is not part of
- * this path: tendencies are zero.  out (optional) receives the diagnostics
+ * boundary relaxation, diagnostics, mkslice's edits of the state, status
+ * update, mass budget (when debug_level > 0) and the NaN/Inf check on ps.
+ * Physics is not part of this path: tendencies are zero (the split step
+ * below takes them).  out (optional) receives the diagnostics
  * of the last step.  Returns MLC_ERR_NONFINITE when ps is not finite. */
 int mlc_step(mlc_ctx *ctx, int nsteps, mlc_diag *out);
 
@@ -234,6 +235,32 @@ int mlc_member_set_boundary(mlc_ctx *ctx, int m, const mlc_bdy_ptrs *b, double x
 /* nsteps steps of every active member; out (optional) receives one entry per
  * slot (steps_done = 0 for empty slots). */
 int mlc_step_batch(mlc_ctx *ctx, int nsteps, mlc_diag *out);
+
+/* ---- physics coupling: the step split at the physics
+ * (Main/mod_moloch.F90:354-376).  mlc_step_dynamics runs every active
+ * member through the dynamical core, the boundary, p/rho/qsat, the surface
+ * pressure and the edits mkslice makes to the state (Main/mod_slice.F90:
+ * 110-147: the qx and tracer floors); the state is then the one the physics
+ * reads (mlc_member_download_state returns it).  The physics' tendencies go
+ * in with mlc_member_set_tendencies; mlc_step_finish applies status_update
+ * (:1403-1443) with them, the mass budget and the ps check, and ends the
+ * step (out, optional: one entry per slot).  Tendencies are zero at every
+ * step's start (reset_tendencies :1044-1083): a member without
+ * set_tendencies gets zero, NULL arrays are zero, and mlc_step equals
+ * mlc_step_dynamics + mlc_step_finish with no tendencies.  While a step is
+ * open, calls that step, upload, bind, add or remove members or change
+ * launch shapes return MLC_ERR_STATE; download_state and set_tendencies are
+ * accepted.  Split steps launch their kernels one by one (no graph). */
+typedef struct mlc_tend_ptrs {
+  const double *tten;    /* (jx-3,iy-3,kz) temperature tendency on jci x ici [K/s]  */
+  const double *uten;    /* (jx-3,iy-3,kz) zonal wind (cross points) [m/s^2]        */
+  const double *vten;    /* (jx-3,iy-3,kz) meridional wind (cross points) [m/s^2]   */
+  const double *qxten;   /* (jx-3,iy-3,kz,nqx) water species [kg/kg/s]              */
+  const double *chiten;  /* (jx-3,iy-3,kz,ntr) tracers                              */
+} mlc_tend_ptrs;
+int mlc_step_dynamics(mlc_ctx *ctx);
+int mlc_member_set_tendencies(mlc_ctx *ctx, int m, const mlc_tend_ptrs *t);
+int mlc_step_finish(mlc_ctx *ctx, mlc_diag *out);
 
 /* Serving pool: a context of `capacity` empty slots whose members join and
  * leave between steps (continuous batching).  A join allocates the member's

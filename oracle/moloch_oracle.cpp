@@ -4,7 +4,8 @@
 // in the reference's order of operations, for checking the GPU library.  It
 // follows (all paths relative to the RegCM source tree):
 //   Main/mod_moloch.F90:201-308   init_moloch
-//   Main/mod_moloch.F90:312-446   moloch (physics, mkslice and zenitm left out)
+//   Main/mod_moloch.F90:312-446   moloch (physics and zenitm left out; of mkslice,
+//                                 Main/mod_slice.F90:110-147, its edits of the state)
 //   Main/mod_moloch.F90:448-529   boundary
 //   Main/mod_moloch.F90:531-765   divergence_diffusion, sound, divergence_damping
 //   Main/mod_moloch.F90:767-1042  advection, wafone
@@ -72,6 +73,11 @@ struct Oracle {
   std::vector<F3> chib[2];
   double xbctime = 0, dtbdys = 1, rtb = 1;
 
+  // ---- physics tendencies (jci x ici, Main/mod_atm_interface.F90:606-617) ----
+  F3 tten, uten, vten;
+  std::vector<F3> qxten, chiten;
+  bool step_open = false;
+
   // ---- work ----
   F3 s, wwkw, tetavf, zdiv2, laplacian, wz, p0, wfw, wx, zpby, zpbw, ud, vd;
 
@@ -79,6 +85,9 @@ struct Oracle {
   int bind_static(const mlc_static_ptrs *st);
   void init_moloch();
   void moloch(mlc_diag *dg);
+  void moloch_dynamics();
+  void moloch_finish(mlc_diag *dg);
+  void mkslice();
   void reset_tendencies();
   void dynamical_core(double dta, double dts);
   void sound(double dts);
@@ -192,6 +201,11 @@ int Oracle::create(const mlc_dims *d, const mlc_params *pp) {
   qx.assign(nqx, F3()); for (auto &f : qx) f.init(jce1, jce2, ice1, ice2, 1, kz);
   trac.assign(ntr, F3()); for (auto &f : trac) f.init(jce1, jce2, ice1, ice2, 1, kz);
   ps.init(jce1, jce2, ice1, ice2);
+  tten.init(jci1, jci2, ici1, ici2, 1, kz);
+  uten.init(jci1, jci2, ici1, ici2, 1, kz);
+  vten.init(jci1, jci2, ici1, ici2, 1, kz);
+  qxten.assign(nqx, F3()); for (auto &f : qxten) f.init(jci1, jci2, ici1, ici2, 1, kz);
+  chiten.assign(ntr, F3()); for (auto &f : chiten) f.init(jci1, jci2, ici1, ici2, 1, kz);
 
   for (int b = 0; b < 2; ++b) {
     for (F3 *f : {&xtb[b], &xqb[b], &xpaib[b], &xlb[b], &xib[b]})
@@ -297,8 +311,16 @@ void Oracle::init_moloch() {
 }
 
 // ---------------------------------------------------------------- step ----
-// Main/mod_moloch.F90:312-446
+// Main/mod_moloch.F90:312-446, as its two halves around the physics: the
+// dynamics through mkslice's edits of the state (:312-357), then
+// status_update with the tendencies the physics left, the mass check and
+// the ps check (:376-422).
 void Oracle::moloch(mlc_diag *dg) {
+  moloch_dynamics();
+  moloch_finish(dg);
+}
+
+void Oracle::moloch_dynamics() {
   reset_tendencies();
   dynamical_core(dtstepa, dtsound);
   if (prm.do_apply_bdy) boundary();
@@ -312,6 +334,10 @@ void Oracle::moloch(mlc_diag *dg) {
         qsat(j, i, k) = pfwsat(t(j, i, k), p(j, i, k));
       }
   extrapolate_surface_pressure();
+  mkslice();
+}
+
+void Oracle::moloch_finish(mlc_diag *dg) {
   status_update(dtsec);
   if (prm.debug_level > 0) massck(dg);
   // :407-422 -- any non-finite ps is reported (the reference tests max/min)
@@ -327,8 +353,13 @@ void Oracle::moloch(mlc_diag *dg) {
   if (dg) { dg->ps_max = mx; dg->ps_min = mn; dg->nonfinite = bad; dg->xbctime = xbctime; }
 }
 
-// Main/mod_moloch.F90:1044-1083 (tendency arrays are zero on this path)
+// Main/mod_moloch.F90:1044-1083
 void Oracle::reset_tendencies() {
+  std::fill(tten.d.begin(), tten.d.end(), 0.0);
+  std::fill(uten.d.begin(), uten.d.end(), 0.0);
+  std::fill(vten.d.begin(), vten.d.end(), 0.0);
+  for (auto &f : qxten) std::fill(f.d.begin(), f.d.end(), 0.0);
+  for (auto &f : chiten) std::fill(f.d.begin(), f.d.end(), 0.0);
   std::fill(s.d.begin(), s.d.end(), 0.0);
   for (int k = 1; k <= kz; ++k)
     for (int i = ici1; i <= ici2; ++i)
@@ -1068,9 +1099,10 @@ void Oracle::morelax_chiten() {
         }
 }
 
-// Main/mod_moloch.F90:1403-1443 with zero tendencies (t, ux, vx, qx and
-// trac + dt*0 leave their operands unchanged)
-void Oracle::status_update(double) {
+// Main/mod_slice.F90:110-147 (idynamic = 3): the edits mkslice makes to the
+// MOLOCH state through its atms pointers (qxb3d => qx, chib3d => trac).  The
+// fields it derives for the physics (pf3d, th3d, rhb3d, ...) are not state.
+void Oracle::mkslice() {
   for (int n = 0; n < nqx; ++n)
     for (int k = 1; k <= kz; ++k)
       for (int i = ici1; i <= ici2; ++i)
@@ -1080,7 +1112,32 @@ void Oracle::status_update(double) {
     for (int k = 1; k <= kz; ++k)
       for (int i = ici1; i <= ici2; ++i)
         for (int j = jci1; j <= jci2; ++j)
+          if (trac[n](j, i, k) < 1.0e-50) trac[n](j, i, k) = 0.0;
+}
+
+// Main/mod_moloch.F90:1403-1443 (TKE is out of scope)
+void Oracle::status_update(double dtinc) {
+  for (int k = 1; k <= kz; ++k)
+    for (int i = ici1; i <= ici2; ++i)
+      for (int j = jci1; j <= jci2; ++j) {
+        t(j, i, k) = t(j, i, k) + dtinc * tten(j, i, k);
+        ux(j, i, k) = ux(j, i, k) + dtinc * uten(j, i, k);
+        vx(j, i, k) = vx(j, i, k) + dtinc * vten(j, i, k);
+      }
+  for (int n = 0; n < nqx; ++n)
+    for (int k = 1; k <= kz; ++k)
+      for (int i = ici1; i <= ici2; ++i)
+        for (int j = jci1; j <= jci2; ++j) {
+          qx[n](j, i, k) = qx[n](j, i, k) + dtinc * qxten[n](j, i, k);
+          if (qx[n](j, i, k) < qxcheckval[n]) qx[n](j, i, k) = qxzeroval[n];
+        }
+  for (int n = 0; n < ntr; ++n)
+    for (int k = 1; k <= kz; ++k)
+      for (int i = ici1; i <= ici2; ++i)
+        for (int j = jci1; j <= jci2; ++j) {
+          trac[n](j, i, k) = trac[n](j, i, k) + dtinc * chiten[n](j, i, k);
           if (trac[n](j, i, k) < 0.0) trac[n](j, i, k) = 0.0;
+        }
   temp_to_tvirt();
 #pragma omp parallel for
   for (int k = 1; k <= kz; ++k)
@@ -1204,13 +1261,49 @@ int orc_set_boundary(void *h, const mlc_bdy_ptrs *b, double xbctime, double dtbd
 
 int orc_step(void *h, int nsteps, mlc_diag *dg) {
   Oracle &o = *static_cast<Oracle *>(h);
-  if (!o.have_static || !o.have_state || (o.prm.do_apply_bdy && !o.have_bdy)) return MLC_ERR_STATE;
+  if (!o.have_static || !o.have_state || (o.prm.do_apply_bdy && !o.have_bdy) || o.step_open)
+    return MLC_ERR_STATE;
   mlc_diag tmp{};
   for (int n = 0; n < nsteps; ++n) {
     o.moloch(&tmp);
     tmp.steps_done = n + 1;
     if (tmp.nonfinite) break;
   }
+  tmp.xbctime = o.xbctime;
+  if (dg) *dg = tmp;
+  return tmp.nonfinite ? MLC_ERR_NONFINITE : MLC_OK;
+}
+
+// The step split around the physics: the dynamics through mkslice, then
+// (after orc_set_tendencies) status_update, mass check and ps check.
+int orc_step_dynamics(void *h) {
+  Oracle &o = *static_cast<Oracle *>(h);
+  if (!o.have_static || !o.have_state || (o.prm.do_apply_bdy && !o.have_bdy) || o.step_open)
+    return MLC_ERR_STATE;
+  o.moloch_dynamics();
+  o.step_open = true;
+  return MLC_OK;
+}
+
+int orc_set_tendencies(void *h, const mlc_tend_ptrs *tp) {
+  Oracle &o = *static_cast<Oracle *>(h);
+  if (!o.step_open || !tp) return MLC_ERR_STATE;
+  const size_t n3 = o.tten.d.size();
+  if (tp->tten) o.tten.load(tp->tten);
+  if (tp->uten) o.uten.load(tp->uten);
+  if (tp->vten) o.vten.load(tp->vten);
+  if (tp->qxten) for (int n = 0; n < o.nqx; ++n) o.qxten[n].load(tp->qxten + n * n3);
+  if (tp->chiten) for (int n = 0; n < o.ntr; ++n) o.chiten[n].load(tp->chiten + n * n3);
+  return MLC_OK;
+}
+
+int orc_step_finish(void *h, mlc_diag *dg) {
+  Oracle &o = *static_cast<Oracle *>(h);
+  if (!o.step_open) return MLC_ERR_STATE;
+  mlc_diag tmp{};
+  o.moloch_finish(&tmp);
+  o.step_open = false;
+  tmp.steps_done = 1;
   tmp.xbctime = o.xbctime;
   if (dg) *dg = tmp;
   return tmp.nonfinite ? MLC_ERR_NONFINITE : MLC_OK;

@@ -36,6 +36,9 @@ def load():
         lib.orc_get_state.argtypes = [C.c_void_p, P(abi.mlc_state_ptrs)]
         lib.orc_set_boundary.argtypes = [C.c_void_p, P(abi.mlc_bdy_ptrs), C.c_double, C.c_double]
         lib.orc_step.argtypes = [C.c_void_p, C.c_int, P(abi.mlc_diag)]
+        lib.orc_step_dynamics.argtypes = [C.c_void_p]
+        lib.orc_set_tendencies.argtypes = [C.c_void_p, P(abi.mlc_tend_ptrs)]
+        lib.orc_step_finish.argtypes = [C.c_void_p, P(abi.mlc_diag)]
         lib.orc_sound_only.argtypes = [C.c_void_p]
         lib.orc_get_work.argtypes = [C.c_void_p, C.c_int, dp]
         lib.orc_setup_levels.argtypes = [C.c_int, C.c_double, dp, dp]
@@ -75,6 +78,17 @@ class Oracle:
     def step(self, n=1):
         d = abi.mlc_diag()
         st = self.lib.orc_step(self.h, n, C.byref(d))
+        return st, d
+
+    def step_dynamics(self):
+        return self.lib.orc_step_dynamics(self.h)
+
+    def set_tendencies(self, tend_ptrs):
+        return self.lib.orc_set_tendencies(self.h, C.byref(tend_ptrs))
+
+    def step_finish(self):
+        d = abi.mlc_diag()
+        st = self.lib.orc_step_finish(self.h, C.byref(d))
         return st, d
 
     def sound_only(self):

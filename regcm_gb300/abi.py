@@ -88,6 +88,14 @@ class mlc_bdy_ptrs(C.Structure):
     _fields_ = [(n, _dp * 2) for n in BDY_FIELDS]
 
 
+# physics tendencies on the interior jci x ici, (jx-3, iy-3, kz[, n])
+TEND_FIELDS = ["tten", "uten", "vten", "qxten", "chiten"]
+
+
+class mlc_tend_ptrs(C.Structure):
+    _fields_ = [(n, _dp) for n in TEND_FIELDS]
+
+
 class mlc_tune_report(C.Structure):
     _fields_ = [("col_x", C.c_int32), ("col_y", C.c_int32), ("solve_x", C.c_int32),
                 ("solve_y", C.c_int32), ("vert_x", C.c_int32), ("vert_y", C.c_int32),
@@ -169,6 +177,9 @@ def _declare(lib):
         "mlc_pool_remove": (C.c_int, [C.c_void_p, C.c_int]),
         "mlc_pool_bytes": (C.c_size_t, [C.c_void_p]),
         "mlc_member_footprint": (C.c_size_t, [P(mlc_dims), P(mlc_params)]),
+        "mlc_step_dynamics": (C.c_int, [C.c_void_p]),
+        "mlc_member_set_tendencies": (C.c_int, [C.c_void_p, C.c_int, P(mlc_tend_ptrs)]),
+        "mlc_step_finish": (C.c_int, [C.c_void_p, P(mlc_diag)]),
     }
     for name, (res, args) in sigs.items():
         try:

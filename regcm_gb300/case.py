@@ -127,6 +127,38 @@ class Case:
             setattr(b, n, arr)
         return b
 
+    def tendencies(self, seed: int = 0) -> dict:
+        """Synthetic physics tendencies on the interior jci x ici, Fortran
+        arrays (jx-3, iy-3, kz[, n]) as mo_atm%tten/uten/vten/qxten/chiten:
+        heating and wind forcing of a few K/day and m/s/h, small species
+        sources, and at one point in twenty a sink of 1.5 times the initial
+        amount per step, which drives q below its floor there."""
+        d = self.dims
+        rng = np.random.default_rng(seed)
+        shp = (d.jx - 3, d.iy - 3, d.kz)
+        f = lambda a: np.asfortranarray(a, dtype=np.float64)
+        out = {"tten": f(rng.normal(0.0, 1e-4, shp)), "uten": f(rng.normal(0.0, 3e-4, shp)),
+               "vten": f(rng.normal(0.0, 3e-4, shp))}
+        dt = self.params.dtsec
+
+        def species(q0, scale):
+            ten = rng.normal(0.0, scale, q0.shape)
+            sink = rng.random(q0.shape) < 0.05
+            ten[sink] = -1.5 * q0[sink] / dt - scale
+            return f(ten)
+
+        out["qxten"] = species(self.state["qx"][1:-1, 1:-1], 1e-9)
+        if d.ntr:
+            out["chiten"] = species(self.state["trac"][1:-1, 1:-1], 1e-7)
+        return out
+
+    @staticmethod
+    def tend_ptrs_of(tend: dict) -> abi.mlc_tend_ptrs:
+        t = abi.mlc_tend_ptrs()
+        for n in abi.TEND_FIELDS:
+            setattr(t, n, abi.dptr(tend.get(n)))
+        return t
+
     def empty_state(self) -> dict:
         """Arrays shaped like the state, for downloads."""
         return {k: np.zeros_like(v, order="F") for k, v in self.state.items()}

@@ -280,6 +280,11 @@ struct Member {
   Dom<double> dd{};      // descriptor of an FP64 member
   Dom<float> df{};       // descriptor of a mixed member
   bool have_static = false, have_state = false, have_bdy = false;
+  // physics tendencies (allocated at the first mlc_member_set_tendencies;
+  // live only between that call and the end of the open step)
+  void *tend_raw = nullptr;
+  size_t tend_bytes = 0;
+  bool tend_live = false;
 };
 
 template <class R> Dom<R> &dom_of(Member &m);
@@ -316,6 +321,7 @@ struct mlc_ctx {
   bool graph_valid = false;
   bool use_graphs = true;
   int launches_per_step = 0;
+  bool step_open = false;      // between mlc_step_dynamics and mlc_step_finish
 };
 
 namespace {
@@ -456,7 +462,8 @@ int remove_member(mlc_ctx *x, int slot) {
   Member &m = x->mem[slot];
   // stream order puts the release after every step already enqueued
   MLC_TRY(cudaFreeAsync(m.raw, x->stream));
-  x->in_use -= m.bytes;
+  if (m.tend_raw) MLC_TRY(cudaFreeAsync(m.tend_raw, x->stream));
+  x->in_use -= m.bytes + m.tend_bytes;
   m = Member{};
   x->table_dirty = true;
   return MLC_OK;
@@ -486,6 +493,7 @@ int refresh(mlc_ctx *x) {
     D.clk = x->clks + slot;
     D.diag = x->diags + slot;
     D.active = 1;
+    D.tend = m.tend_live ? static_cast<const R *>(m.tend_raw) : nullptr;
     t.push_back(D);
     L.jx = std::max(L.jx, m.g.jx);
     L.iy = std::max(L.iy, m.g.iy);
@@ -545,16 +553,19 @@ struct Recorder {
 // member on the context stream; returns the number of kernels launched.
 // The offsets count the acoustic substeps (uvoff) and advection rounds
 // (advoff) since the step began; with the roles in each member's clock they
-// name the buffers every launch works on.
+// name the buffers every launch works on.  phase: kStepAll the whole step;
+// kStepDynamics up to mkslice (:312-357), kStepFinish from status_update
+// (:376-446) to the end, the two halves around the physics.
+constexpr int kStepAll = 0, kStepDynamics = 1, kStepFinish = 2;
 template <class R>
-int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
+int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr, int phase = kStepAll) {
   using K = Launch<R>;
   const LaunchGeom &L = x->key.L;
   const Dom<R> *d = static_cast<const Dom<R> *>(x->table);
   cudaStream_t s = x->stream;
   const int nadv = x->prm.mo_nadv, nsound = x->prm.mo_nsound;
   int nl = 0;
-  for (int r = 0; r < nadv; ++r) {
+  for (int r = 0; r < nadv && phase != kStepFinish; ++r) {
     // ---- sound (Main/mod_moloch.F90:531-765) ----
     REC("sound_prep", K::sound_prep(L, d, r, s)); ++nl;
     for (int n = 0; n < nsound; ++n) {
@@ -576,13 +587,22 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr) {
   }
   // ---- step end (Main/mod_moloch.F90:340-446) ----
   const int uvo = nadv * nsound, ao = nadv;
-  REC("end_tvirt", K::end_tvirt(L, d, ao, s)); ++nl;
-  if (x->prm.do_apply_bdy) {
-    REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); nl += 2;
-    REC("bdy_relax", K::bdy_relax(L, d, uvo, ao, s)); ++nl;
-    if (x->prm.mo_spectral_nudge) { REC("bdy_spectral", K::bdy_spectral(L, d, uvo, ao, s)); nl += 3; }
+  if (phase != kStepFinish) {
+    REC("end_tvirt", K::end_tvirt(L, d, ao, s)); ++nl;
+    if (x->prm.do_apply_bdy) {
+      REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); nl += 2;
+      REC("bdy_relax", K::bdy_relax(L, d, uvo, ao, s)); ++nl;
+      if (x->prm.mo_spectral_nudge) { REC("bdy_spectral", K::bdy_spectral(L, d, uvo, ao, s)); nl += 3; }
+    }
   }
-  REC("end_cross", K::end_cross(L, d, uvo, ao, s)); nl += 2;
+  if (phase == kStepAll) {
+    REC("end_cross", K::end_cross(L, d, uvo, ao, s)); nl += 2;
+  } else if (phase == kStepDynamics) {
+    REC("end_mkslice", K::end_cross_split(L, d, uvo, ao, false, s)); nl += 2;
+    return nl;
+  } else {
+    REC("end_status", K::end_cross_split(L, d, uvo, ao, true, s)); ++nl;
+  }
   REC("end_uvstag", K::end_uvstag(L, d, uvo, ao, s)); ++nl;
   REC("end_reduce", K::end_reduce(L, d, uvo, ao, s)); nl += 2;
   return nl;
@@ -981,7 +1001,11 @@ int download_state_impl(mlc_ctx *x, int slot, const mlc_state_ptrs *h) {
   int cst;
   const Clock ck = get_clock(x, slot, &cst);
   MLC_CHK(cst);
-  const State<R> st = state_of(dom_of<R>(mb), ck.uv_role, ck.adv_role);
+  // inside an open step the roles advance only at its end: the current
+  // halves are those the step's last kernels work on
+  const int uvo = x->step_open ? x->prm.mo_nadv * x->prm.mo_nsound : 0;
+  const int ao = x->step_open ? x->prm.mo_nadv : 0;
+  const State<R> st = state_of(dom_of<R>(mb), (ck.uv_role + uvo) & 1, (ck.adv_role + ao) & 1);
   const Geom &g = mb.g;
   const int jx = mb.dims.jx, iy = mb.dims.iy, kz = mb.dims.kz;
   size_t off = 0;
@@ -1043,8 +1067,10 @@ void release(mlc_ctx *x) {
   if (!x) return;
   if (x->stream) cudaStreamSynchronize(x->stream);
   if (x->graph) cudaGraphExecDestroy(x->graph);
-  for (Member &m : x->mem)
+  for (Member &m : x->mem) {
     if (m.raw) cudaFreeAsync(m.raw, x->stream);
+    if (m.tend_raw) cudaFreeAsync(m.tend_raw, x->stream);
+  }
   if (x->staging) cudaFreeAsync(x->staging, x->stream);
   if (x->stream) cudaStreamSynchronize(x->stream);
   if (x->clks) cudaFree(x->clks);
@@ -1163,6 +1189,43 @@ int fetch_diags(mlc_ctx *x, int nsteps, mlc_diag *out) {
 
 }  // namespace
 
+namespace {
+
+template <class R>
+int set_tendencies_impl(mlc_ctx *x, Member &mb, const mlc_tend_ptrs *t) {
+  const Geom &g = mb.g;
+  const int nf = 3 + mb.dims.nqx + mb.dims.ntr;
+  const size_t F = g.field3();
+  if (!mb.tend_raw) {
+    const size_t bytes = (size_t)nf * F * sizeof(R);
+    if (x->budget && x->in_use + bytes > x->budget) return MLC_ERR_BUDGET;
+    cudaError_t e = cudaMallocFromPoolAsync(&mb.tend_raw, bytes, x->pool, x->stream);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      mb.tend_raw = nullptr;
+      return MLC_ERR_NOMEM;
+    }
+    mb.tend_bytes = bytes;
+    x->in_use += bytes;
+  }
+  R *base = static_cast<R *>(mb.tend_raw);
+  // NULL arrays leave zero, as reset_tendencies does at every step's start
+  MLC_TRY(cudaMemsetAsync(base, 0, (size_t)nf * F * sizeof(R), x->stream));
+  const int nj = mb.dims.jx - 3, ni = mb.dims.iy - 3, kz = mb.dims.kz;
+  const size_t n3 = (size_t)nj * ni * kz;
+  const size_t at22 = g.at2(2, 2);
+  const double *h[3] = {t->tten, t->uten, t->vten};
+  for (int f = 0; f < 3; ++f) MLC_CHK(put3<R>(x, g, h[f], base + (size_t)f * F + at22, nj, ni, kz, 0));
+  for (int n = 0; n < mb.dims.nqx && t->qxten; ++n)
+    MLC_CHK(put3<R>(x, g, t->qxten + n * n3, base + (size_t)(3 + n) * F + at22, nj, ni, kz, 0));
+  for (int n = 0; n < mb.dims.ntr && t->chiten; ++n)
+    MLC_CHK(put3<R>(x, g, t->chiten + n * n3, base + (size_t)(3 + mb.dims.nqx + n) * F + at22, nj, ni,
+                    kz, 0));
+  return cuda_status(cudaStreamSynchronize(x->stream));
+}
+
+}  // namespace
+
 extern "C" {
 
 void mlc_default_params(mlc_params *p) {
@@ -1245,6 +1308,7 @@ int mlc_create_pool(const mlc_params *params, int capacity, size_t budget_bytes,
 
 int mlc_pool_add(mlc_ctx *x, const mlc_dims *dims, int *slot) {
   if (!x || !dims || !slot) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   *slot = -1;
   for (size_t m = 0; m < x->mem.size(); ++m)
     if (!x->mem[m].used) {
@@ -1257,6 +1321,7 @@ int mlc_pool_add(mlc_ctx *x, const mlc_dims *dims, int *slot) {
 
 int mlc_pool_remove(mlc_ctx *x, int slot) {
   if (!member_ok(x, slot)) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   return remove_member(x, slot);
 }
 
@@ -1264,6 +1329,7 @@ size_t mlc_pool_bytes(const mlc_ctx *x) { return x ? x->in_use : 0; }
 
 int mlc_member_bind_static(mlc_ctx *x, int m, const mlc_static_ptrs *s) {
   if (!member_ok(x, m) || !s) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   if (!s->zita) return MLC_ERR_INVALID;
   Member &mb = x->mem[m];
   const int st = x->mixed ? bind_static_impl<float>(x, mb, s) : bind_static_impl<double>(x, mb, s);
@@ -1276,6 +1342,7 @@ int mlc_bind_static(mlc_ctx *x, const mlc_static_ptrs *s) { return mlc_member_bi
 
 int mlc_member_upload_state(mlc_ctx *x, int m, const mlc_state_ptrs *h) {
   if (!member_ok(x, m) || !h) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   const int st = x->mixed ? upload_state_impl<float>(x, m, h) : upload_state_impl<double>(x, m, h);
   if (st == MLC_OK) x->mem[m].have_state = true;
   return st;
@@ -1297,6 +1364,7 @@ int mlc_download_state(mlc_ctx *x, const mlc_state_ptrs *h) {
 int mlc_member_set_boundary(mlc_ctx *x, int m, const mlc_bdy_ptrs *b, double xbctime,
                             double dtbdys) {
   if (!member_ok(x, m) || !b || !(dtbdys > 0)) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   Member &mb = x->mem[m];
   MLC_CHK(x->mixed ? set_boundary_impl<float>(x, mb, b) : set_boundary_impl<double>(x, mb, b));
   int cst;
@@ -1318,6 +1386,7 @@ int mlc_set_boundary(mlc_ctx *x, const mlc_bdy_ptrs *b, double xbctime, double d
 
 int mlc_step_batch(mlc_ctx *x, int nsteps, mlc_diag *out) {
   if (!x || nsteps < 0) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   if (!ready(x)) return MLC_ERR_STATE;
   MLC_CHK(step_any(x, nsteps));
   return fetch_diags(x, nsteps, out);
@@ -1331,6 +1400,51 @@ int mlc_step(mlc_ctx *x, int nsteps, mlc_diag *out) {
   return st;
 }
 
+// ---- the step split at the physics (Main/mod_moloch.F90:354-376) ----------
+
+int mlc_step_dynamics(mlc_ctx *x) {
+  if (!x) return MLC_ERR_INVALID;
+  if (x->step_open || !ready(x)) return MLC_ERR_STATE;
+  MLC_CHK(x->mixed ? refresh<float>(x) : refresh<double>(x));
+  if (x->key.L.nmem == 0) return MLC_OK;
+  if (x->mixed) enqueue_step<float>(x, nullptr, kStepDynamics);
+  else enqueue_step<double>(x, nullptr, kStepDynamics);
+  MLC_TRY(cudaGetLastError());
+  x->step_open = true;
+  return MLC_OK;
+}
+
+int mlc_member_set_tendencies(mlc_ctx *x, int m, const mlc_tend_ptrs *t) {
+  if (!member_ok(x, m) || !t) return MLC_ERR_INVALID;
+  if (!x->step_open) return MLC_ERR_STATE;
+  Member &mb = x->mem[m];
+  const int st = x->mixed ? set_tendencies_impl<float>(x, mb, t) : set_tendencies_impl<double>(x, mb, t);
+  if (st != MLC_OK) return st;
+  mb.tend_live = true;
+  x->table_dirty = true;
+  return MLC_OK;
+}
+
+int mlc_step_finish(mlc_ctx *x, mlc_diag *out) {
+  if (!x) return MLC_ERR_INVALID;
+  if (!x->step_open) return MLC_ERR_STATE;
+  MLC_CHK(x->mixed ? refresh<float>(x) : refresh<double>(x));
+  if (x->key.L.nmem > 0) {
+    if (x->mixed) enqueue_step<float>(x, nullptr, kStepFinish);
+    else enqueue_step<double>(x, nullptr, kStepFinish);
+    MLC_TRY(cudaGetLastError());
+  }
+  x->step_open = false;
+  // reset_tendencies: the next step starts from zero tendencies
+  bool any = false;
+  for (Member &m : x->mem) {
+    any = any || m.tend_live;
+    m.tend_live = false;
+  }
+  if (any) x->table_dirty = true;
+  return fetch_diags(x, 1, out);
+}
+
 int mlc_members(const mlc_ctx *x) { return x ? (int)x->mem.size() : 0; }
 
 void mlc_destroy(mlc_ctx *x) { release(x); }
@@ -1339,6 +1453,7 @@ void mlc_destroy(mlc_ctx *x) { release(x); }
 // context stream (bracketing exactly the step launches).
 int mlc_step_timed(mlc_ctx *x, int nsteps, mlc_diag *out, float *ms) {
   if (!x || !ms || nsteps < 0) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   if (!ready(x)) return MLC_ERR_STATE;
   // descriptor upload and graph recording happen before the timed region
   MLC_CHK(step_any(x, 0));
@@ -1367,6 +1482,7 @@ int mlc_step_timed(mlc_ctx *x, int nsteps, mlc_diag *out, float *ms) {
 // launch group on the context stream).  Fills up to max_out entries.
 int mlc_profile_steps(mlc_ctx *x, int nsteps, mlc_kernel_time *out, int max_out, int *n_out) {
   if (!x || !out || !n_out) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   if (!ready(x)) return MLC_ERR_STATE;
   MLC_CHK(step_any(x, 0));
   Recorder rec;
@@ -1539,12 +1655,14 @@ extern "C" {
 
 int mlc_autotune(mlc_ctx *x, int steps, mlc_tune_report *rep) {
   if (!x || steps < 1) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   if (!ready(x)) return MLC_ERR_STATE;
   return x->mixed ? autotune_impl<float>(x, steps, rep) : autotune_impl<double>(x, steps, rep);
 }
 
 int mlc_set_launch_shapes(mlc_ctx *x, const mlc_tune_report *r) {
   if (!x || !r) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
   auto find = [](const int (*cand)[2], int n, int a, int b) {
     for (int q = 0; q < n; ++q)
       if (cand[q][0] == a && cand[q][1] == b) return q;

@@ -146,6 +146,9 @@ struct Dom {
   DiagDev *diag;
   double *partials;
   R *spec;               // spectral nudging: per field and level, iy rows of km2 coefficients
+  // physics tendencies of the open step (null: zero), fields of the state's
+  // layout: tten, uten, vten, then nqx qxten, then ntr chiten
+  const R *tend;
   int red_blocks;
   int active;            // 0: an empty slot, every block returns at once
   // TMA tensor maps (CUtensorMap, 128 B each, 64-B aligned) of the wz fields,

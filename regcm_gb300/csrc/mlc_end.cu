@@ -531,11 +531,18 @@ __global__ void k_end_ps(const Dom<R> *__restrict__ doms, int uvoff, int advoff)
 }
 
 // Cross-point work after the boundary, per point: uvstagtouvx and
-// temp_to_tvirt of boundary (:520-523), p (:348-352), then status_update
-// (:1403-1443): q clamps, tvirt, tetav, rho, qsat (the surface pressure is
-// k_end_ps's, launched first).  rho and qsat of :348-352 are recomputed from the same t and p
-// by status_update, so they are computed once, after it.
-template <class R>
+// temp_to_tvirt of boundary (:520-523), p (:348-352), the edits mkslice
+// makes to the state (Main/mod_slice.F90:136-147: qx and tracer floors),
+// then status_update (:1403-1443): tendencies, q clamps, tvirt, tetav, rho,
+// qsat (the surface pressure is k_end_ps's, launched first).
+//   kEndAll   the whole sequence with zero tendencies (mlc_step).  rho and
+//             qsat of :348-352, and tvirt and tetav of the boundary, are
+//             recomputed from the same inputs by status_update, so they are
+//             computed once, after it.
+//   kEndPre   up to mkslice: the state the physics reads.
+//   kEndPost  status_update with the member's tendencies (Dom::tend).
+constexpr int kEndAll = 0, kEndPre = 1, kEndPost = 2;
+template <class R, int PH>
 __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
@@ -553,7 +560,7 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
 #pragma unroll
   for (int k = q_.k; k < q_.k + kPtLevels && k <= kz; ++k) {
   const size_t o = ij + (size_t)(k - 1) * PS;
-  if (c.apply_bdy) {
+  if (PH != kEndPost && c.apply_bdy) {
     {
       const R *u = st.u, *v = st.v;
       R a;
@@ -568,12 +575,26 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
     }
   }
   // pressure (FP64 Exner reconstruction; FP32 for the FP32 field of a mixed member)
-  {
+  if (PH != kEndPost) {
     if constexpr (sizeof(R) == sizeof(float)) st.p[o] = exner_to_pressure_f(df_f(DF(st.pai, F).ld(o)));
     else st.p[o] = (R)exner_to_pressure(st.pai[o]);
   }
-  // status_update
-  {
+  if (PH == kEndPre) {
+    // the state at mkslice: tvirt and theta_v of the boundary (before the
+    // floors), rho and qsat of :348-352, then mkslice's floors
+    const R tk = st.t[o], pk = st.p[o];
+    if (c.apply_bdy) {
+      st.tvirt[o] = tk * qfactor(st.qx, o, F, ipp);
+      if constexpr (sizeof(R) == sizeof(float)) {
+        const F2 t2{tk, D.wz[1][o]};
+        DF(st.tetav, F).st(o, df_div(df_mul(t2, qfactor_df(st.qx, o, F, ipp)), DF(st.pai, F).ld(o)));
+      } else {
+        st.tetav[o] = (double)st.tvirt[o] / st.pai[o];
+      }
+    }
+    st.rho[o] = pk / (R(kRgas) * tk);
+    if constexpr (sizeof(R) == sizeof(float)) st.qsat[o] = pfwsat_f(tk, pk);
+    else st.qsat[o] = (R)pfwsat((double)tk, (double)pk);
     if (inner) {
       for (int n = 0; n < g.nqx; ++n) {
         const size_t on = o + (size_t)n * F;
@@ -581,7 +602,45 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
       }
       for (int n = 0; n < g.ntr; ++n) {
         const size_t on = o + (size_t)n * F;
-        if (st.trac[on] < R(0)) st.trac[on] = R(0);
+        if (st.trac[on] < R(1.0e-50)) st.trac[on] = R(0);
+      }
+    }
+    continue;
+  }
+  // status_update
+  {
+    const R *ten = PH == kEndPost ? D.tend : nullptr;
+    if (inner) {
+      if (ten) {
+        // t, ux, vx += dtsec * tendency (a mixed member's t is a double-float)
+        if constexpr (sizeof(R) == sizeof(float)) {
+          const F2 t2 = df_add_f(F2{st.t[o], D.wz[1][o]}, c.dtsecf * ten[o]);
+          st.t[o] = t2.hi;
+          D.wz[1][o] = t2.lo;
+          st.ux[o] = st.ux[o] + c.dtsecf * ten[o + F];
+          st.vx[o] = st.vx[o] + c.dtsecf * ten[o + 2 * F];
+        } else {
+          st.t[o] = st.t[o] + c.dtsec * ten[o];
+          st.ux[o] = st.ux[o] + c.dtsec * ten[o + F];
+          st.vx[o] = st.vx[o] + c.dtsec * ten[o + 2 * F];
+        }
+      }
+      const R dts = pick<R>(c.dtsec, c.dtsecf);
+      for (int n = 0; n < g.nqx; ++n) {
+        const size_t on = o + (size_t)n * F;
+        R q = st.qx[on];
+        if (PH == kEndAll && q < R(qx_check(n))) q = R(qx_zero(n));  // mkslice
+        if (ten) q = q + dts * ten[o + (size_t)(3 + n) * F];
+        if (q < R(qx_check(n))) q = R(qx_zero(n));
+        st.qx[on] = q;
+      }
+      for (int n = 0; n < g.ntr; ++n) {
+        const size_t on = o + (size_t)n * F;
+        R q = st.trac[on];
+        if (PH == kEndAll && q < R(1.0e-50)) q = R(0);  // mkslice
+        if (ten) q = q + dts * ten[o + (size_t)(3 + g.nqx + n) * F];
+        if (q < R(0)) q = R(0);
+        st.trac[on] = q;
       }
     }
     const R tk = st.t[o];
@@ -715,7 +774,9 @@ __global__ void __launch_bounds__(128) k_end_cross_v4(const Dom<R> *__restrict__
 #pragma unroll
     for (int q = 0; q < 4; ++q) pk[q] = exner_to_pressure_f(ph[q] + pl[q]);
     store(pp + o, pk);
-    // status_update: species clamps at inner points
+    // mkslice's floors, then status_update's (zero tendencies): at inner
+    // points qx below its check value becomes its zero value, and a tracer
+    // below 1e-50 becomes 0 (in FP32 every value below 1e-50 is <= 0)
     if (any_inner) {
       for (int n = 0; n < g.nqx; ++n) {
         float x[4];
@@ -735,7 +796,7 @@ __global__ void __launch_bounds__(128) k_end_cross_v4(const Dom<R> *__restrict__
         bool ch = false;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-          if (inner[q] && x[q] < 0.f) {
+          if (inner[q] && x[q] <= 0.f) {
             x[q] = 0.f;
             ch = true;
           }
@@ -1153,7 +1214,21 @@ void Launch<R>::end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int a
   } else {
     int tj;
     const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-    k_end_cross<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+    k_end_cross<R, kEndAll><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  }
+}
+
+template <class R>
+void Launch<R>::end_cross_split(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, bool post,
+                                cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+  if (post) {
+    k_end_cross<R, kEndPost><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  } else {
+    k_end_ps<R><<<grid2(L.jx - 3, L.iy - 3, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
+    k_end_cross<R, kEndPre><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
   }
 }
 

@@ -55,6 +55,10 @@ template <class R> struct Launch {
   static void bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void bdy_spectral(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  // the step split at the physics: k_end_ps and the cross-point work up to
+  // mkslice (post = false), or status_update with the tendencies (post = true)
+  static void end_cross_split(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, bool post,
+                              cudaStream_t s);
   static void end_uvstag(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void end_reduce(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                          cudaStream_t s);

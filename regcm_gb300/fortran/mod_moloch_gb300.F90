@@ -11,8 +11,14 @@
 ! include/moloch_gb300.h; a negative status becomes fatal(), as the
 ! reference's own error paths do.
 !
-! Physics still runs on the host between steps: moloch uploads the
-! prognostic state, advances one step on the GPU and downloads the state.
+! Physics still runs on the host, inside the step as in the reference:
+! moloch uploads the prognostic state, runs the dynamics half of the step on
+! the GPU (through mkslice's edits of the state), downloads the state for
+! mkslice and the physics on the host, hands their tendencies back and lets
+! the GPU finish the step (status_update, mass check), then downloads the
+! state.  physical_parametrizations is a private procedure of
+! Main/mod_moloch.F90 (:1143-1401); the maintainer makes it public (or
+! moves it to its own module) for this call.
 ! Builds with real(rkx) = real(rk8) (the FP64 build); MLC_PREC_MIXED keeps
 ! the same host arrays and converts on the device.
 !
@@ -27,6 +33,7 @@ module mod_moloch_gb300
   use mod_atm_interface
   use mod_bdycod
   use mod_zita
+  use mod_slice, only : mkslice
 
   implicit none
 
@@ -63,6 +70,10 @@ module mod_moloch_gb300
     type(c_ptr) :: xtb(2), xqb(2), xpaib(2), xlb(2), xib(2)
     type(c_ptr) :: dub(2), dvb(2), xpsb(2), chib(2)
   end type mlc_bdy_ptrs
+
+  type, bind(c) :: mlc_tend_ptrs
+    type(c_ptr) :: tten, uten, vten, qxten, chiten
+  end type mlc_tend_ptrs
 
   type, bind(c) :: mlc_diag
     real(c_double) :: ps_max, ps_min
@@ -107,6 +118,22 @@ module mod_moloch_gb300
       import :: mlc_diag, c_int, c_ptr
       type(c_ptr), value :: ctx
       integer(c_int), value :: n
+      type(mlc_diag), intent(out) :: diag
+    end function
+    integer(c_int) function mlc_step_dynamics(ctx) bind(c, name='mlc_step_dynamics')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function mlc_member_set_tendencies(ctx, m, t) &
+        bind(c, name='mlc_member_set_tendencies')
+      import :: mlc_tend_ptrs, c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: m
+      type(mlc_tend_ptrs), intent(in) :: t
+    end function
+    integer(c_int) function mlc_step_finish(ctx, diag) bind(c, name='mlc_step_finish')
+      import :: mlc_diag, c_int, c_ptr
+      type(c_ptr), value :: ctx
       type(mlc_diag), intent(out) :: diag
     end function
     type(c_ptr) function mlc_strerror(st) bind(c, name='mlc_strerror')
@@ -281,19 +308,38 @@ module mod_moloch_gb300
     st%ps = c_loc(sfs%psa)
   end subroutine state_ptrs
 
-  ! replaces Main/mod_moloch.F90:312-446 for the dynamics; physics stays on
-  ! the host and sees the state the GPU step leaves
+  ! replaces Main/mod_moloch.F90:312-446: the GPU runs the dynamics half
+  ! (:312-357) and status_update onwards (:376-446); mkslice and the physics
+  ! (:357-370) run on the host in between
   subroutine moloch
     type(mlc_state_ptrs) :: st
+    type(mlc_tend_ptrs) :: tp
     type(mlc_diag) :: dg
     integer(c_int) :: ist
     call state_ptrs(st)
     call check(mlc_upload_state(ctx, st), 'moloch(upload)')
-    ist = mlc_step(ctx, 1_c_int, dg)
+    call check(mlc_step_dynamics(ctx), 'moloch(dynamics)')
+    call check(mlc_download_state(ctx, st), 'moloch(download)')
+    ! reset_tendencies (:1044-1083) for the host's arrays
+    mo_atm%tten = d_zero
+    mo_atm%uten = d_zero
+    mo_atm%vten = d_zero
+    mo_atm%qxten = d_zero
+    call mkslice
+    if ( do_phys .and. moloch_realcase ) then
+      call physical_parametrizations
+    end if
+    tp%tten = c_loc(mo_atm%tten)
+    tp%uten = c_loc(mo_atm%uten)
+    tp%vten = c_loc(mo_atm%vten)
+    tp%qxten = c_loc(mo_atm%qxten)
+    tp%chiten = c_null_ptr
+    call check(mlc_member_set_tendencies(ctx, 0_c_int, tp), 'moloch(tendencies)')
+    ist = mlc_step_finish(ctx, dg)
     if ( ist == -6 ) then
       call fatal(__FILE__,__LINE__,'CFL VIOLATION')
     end if
-    call check(ist, 'moloch(step)')
+    call check(ist, 'moloch(status_update)')
     call check(mlc_download_state(ctx, st), 'moloch(download)')
     xbctime = real(dg%xbctime,rkx)
   end subroutine moloch

@@ -64,6 +64,25 @@ class MolochDomain:
     def download(self, state_ptrs: abi.mlc_state_ptrs):
         abi.check(self.lib.mlc_download_state(self._ctx, C.byref(state_ptrs)), "download")
 
+    # -- the step split at the physics (Main/mod_moloch.F90:354-376) --------
+    def step_dynamics(self):
+        """Dynamics, boundary and mkslice's edits: the state the physics reads."""
+        abi.check(self.lib.mlc_step_dynamics(self._ctx), "moloch(dynamics)")
+
+    def set_tendencies(self, tend_ptrs: abi.mlc_tend_ptrs):
+        """The physics' tendencies for the open step (NULL fields are zero)."""
+        abi.check(self.lib.mlc_member_set_tendencies(self._ctx, 0, C.byref(tend_ptrs)),
+                  "physics tendencies")
+
+    def step_finish(self) -> abi.mlc_diag:
+        """status_update with the tendencies, mass budget and ps check."""
+        d = abi.mlc_diag()
+        st = self.lib.mlc_step_finish(self._ctx, C.byref(d))
+        if st == abi.MLC_ERR_NONFINITE:
+            raise CFLViolation(st, "moloch")
+        abi.check(st, "moloch(status_update)")
+        return d
+
     def launches_per_step(self) -> int:
         return self.lib.mlc_launches_per_step(self._ctx)
 
@@ -211,6 +230,21 @@ class MolochBatch:
     def download(self, m: int, state_ptrs: abi.mlc_state_ptrs):
         abi.check(self.lib.mlc_member_download_state(self._ctx, m, C.byref(state_ptrs)),
                   "download")
+
+    def step_dynamics(self):
+        abi.check(self.lib.mlc_step_dynamics(self._ctx), "moloch(dynamics)")
+
+    def set_tendencies(self, m: int, tend_ptrs: abi.mlc_tend_ptrs):
+        abi.check(self.lib.mlc_member_set_tendencies(self._ctx, m, C.byref(tend_ptrs)),
+                  "physics tendencies")
+
+    def step_finish(self):
+        diags = (abi.mlc_diag * self.nmem)()
+        st = self.lib.mlc_step_finish(self._ctx, diags)
+        if st == abi.MLC_ERR_NONFINITE:
+            raise CFLViolation(st, "moloch(batch)")
+        abi.check(st, "moloch(status_update)")
+        return list(diags)
 
     def upload(self, m: int, state_ptrs: abi.mlc_state_ptrs):
         abi.check(self.lib.mlc_member_upload_state(self._ctx, m, C.byref(state_ptrs)), "upload")
