@@ -28,6 +28,7 @@
 // OpenMP (results do not depend on the thread count); reductions are serial.
 #include "oracle_common.h"
 #include "../include/moloch_gb300.h"
+#include "../include/moloch_gb300_restart.h"
 
 #include <algorithm>
 #include <cstdio>
@@ -1307,6 +1308,45 @@ int orc_step_finish(void *h, mlc_diag *dg) {
   tmp.xbctime = o.xbctime;
   if (dg) *dg = tmp;
   return tmp.nonfinite ? MLC_ERR_NONFINITE : MLC_OK;
+}
+
+// The restart state of Main/mod_init.F90:421-450 (copies from the SAV
+// fields) and :941-960 (p, qs, rho, tvirt with qv only, tetav), loop by loop
+// over jce x ice; ux and vx stay zero as getmem leaves them.
+int orc_restart_state(const mlc_dims *d, const mlc_sav_fields *f, const mlc_state_ptrs *st) {
+  const size_t jx = d->jx, iy = d->iy, kz = d->kz;
+  const size_t nj = jx - 1, ni = iy - 1;
+  std::memcpy(st->u, f->u, jx * ni * kz * sizeof(double));
+  std::memcpy(st->v, f->v, nj * iy * kz * sizeof(double));
+  std::memcpy(st->w, f->w, nj * ni * (kz + 1) * sizeof(double));
+  std::memcpy(st->t, f->t, nj * ni * kz * sizeof(double));
+  std::memcpy(st->pai, f->pai, nj * ni * kz * sizeof(double));
+  std::memcpy(st->qx, f->qx, nj * ni * kz * d->nqx * sizeof(double));
+  if (d->ntr > 0) std::memcpy(st->trac, f->trac, nj * ni * kz * d->ntr * sizeof(double));
+  std::memcpy(st->ps, f->ps, nj * ni * sizeof(double));
+  for (size_t k = 0; k < kz; ++k)
+    for (size_t i = 0; i < ni; ++i)
+      for (size_t j = 0; j < nj; ++j) {
+        const size_t e = j + nj * (i + ni * k);
+        st->p[e] = std::pow(st->pai[e], orc::cpovr) * orc::p00;
+      }
+  for (size_t k = 0; k < kz; ++k)
+    for (size_t i = 0; i < ni; ++i)
+      for (size_t j = 0; j < nj; ++j) {
+        const size_t e = j + nj * (i + ni * k);
+        st->qsat[e] = orc::pfwsat(st->t[e], st->p[e]);
+        st->rho[e] = st->p[e] / (orc::rgas * st->t[e]);
+      }
+  for (size_t k = 0; k < kz; ++k)
+    for (size_t i = 0; i < ni; ++i)
+      for (size_t j = 0; j < nj; ++j) {
+        const size_t e = j + nj * (i + ni * k);
+        st->tvirt[e] = st->t[e] * (1.0 + orc::ep1 * st->qx[e]);
+        st->tetav[e] = st->tvirt[e] / st->pai[e];
+      }
+  std::memset(st->ux, 0, nj * ni * kz * sizeof(double));
+  std::memset(st->vx, 0, nj * ni * kz * sizeof(double));
+  return MLC_OK;
 }
 
 // One call of sound(dtsound) alone, for substep-level parity tests.

@@ -39,6 +39,7 @@ def load():
         lib.orc_step_dynamics.argtypes = [C.c_void_p]
         lib.orc_set_tendencies.argtypes = [C.c_void_p, P(abi.mlc_tend_ptrs)]
         lib.orc_step_finish.argtypes = [C.c_void_p, P(abi.mlc_diag)]
+        lib.orc_restart_state.argtypes = [P(abi.mlc_dims), P(abi.mlc_sav_fields), P(abi.mlc_state_ptrs)]
         lib.orc_sound_only.argtypes = [C.c_void_p]
         lib.orc_get_work.argtypes = [C.c_void_p, C.c_int, dp]
         lib.orc_setup_levels.argtypes = [C.c_int, C.c_double, dp, dp]

@@ -96,6 +96,14 @@ class mlc_tend_ptrs(C.Structure):
     _fields_ = [(n, _dp) for n in TEND_FIELDS]
 
 
+# the MOLOCH variables of a SAV restart file
+SAV_FIELDS = ["u", "v", "w", "t", "pai", "qx", "ps", "trac"]
+
+
+class mlc_sav_fields(C.Structure):
+    _fields_ = [(n, _dp) for n in SAV_FIELDS]
+
+
 class mlc_tune_report(C.Structure):
     _fields_ = [("col_x", C.c_int32), ("col_y", C.c_int32), ("solve_x", C.c_int32),
                 ("solve_y", C.c_int32), ("vert_x", C.c_int32), ("vert_y", C.c_int32),
@@ -177,6 +185,13 @@ def _declare(lib):
         "mlc_pool_remove": (C.c_int, [C.c_void_p, C.c_int]),
         "mlc_pool_bytes": (C.c_size_t, [C.c_void_p]),
         "mlc_member_footprint": (C.c_size_t, [P(mlc_dims), P(mlc_params)]),
+        "mlc_sav_write": (C.c_int, [C.c_char_p, P(mlc_dims), P(mlc_sav_fields), C.c_char_p,
+                                    C.c_char_p]),
+        "mlc_sav_read": (C.c_int, [C.c_char_p, P(mlc_dims), P(mlc_sav_fields), C.c_char_p,
+                                   C.c_size_t]),
+        "mlc_sav_restart_state": (C.c_int, [P(mlc_dims), P(mlc_sav_fields), P(mlc_state_ptrs)]),
+        "mlc_member_write_sav": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_char_p, C.c_char_p]),
+        "mlc_member_read_sav": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p]),
         "mlc_step_dynamics": (C.c_int, [C.c_void_p]),
         "mlc_member_set_tendencies": (C.c_int, [C.c_void_p, C.c_int, P(mlc_tend_ptrs)]),
         "mlc_step_finish": (C.c_int, [C.c_void_p, P(mlc_diag)]),

@@ -152,6 +152,21 @@ class Case:
             out["chiten"] = species(self.state["trac"][1:-1, 1:-1], 1e-7)
         return out
 
+    def empty_sav(self) -> dict:
+        """Arrays for the MOLOCH variables of a SAV file."""
+        out = {n: np.zeros_like(self.state[n], order="F")
+               for n in ("u", "v", "w", "t", "pai", "qx", "ps")}
+        if self.dims.ntr:
+            out["trac"] = np.zeros_like(self.state["trac"], order="F")
+        return out
+
+    @staticmethod
+    def sav_ptrs_of(sav: dict) -> abi.mlc_sav_fields:
+        f = abi.mlc_sav_fields()
+        for n in abi.SAV_FIELDS:
+            setattr(f, n, abi.dptr(sav.get(n)))
+        return f
+
     @staticmethod
     def tend_ptrs_of(tend: dict) -> abi.mlc_tend_ptrs:
         t = abi.mlc_tend_ptrs()

@@ -26,6 +26,7 @@
 #include <cudaTypedefs.h>
 
 #include "../../include/moloch_gb300.h"
+#include "../../include/moloch_gb300_restart.h"
 #include "mlc_kernels.cuh"
 
 using namespace mlc;
@@ -1443,6 +1444,46 @@ int mlc_step_finish(mlc_ctx *x, mlc_diag *out) {
   }
   if (any) x->table_dirty = true;
   return fetch_diags(x, 1, out);
+}
+
+// ---- SAV restart files (Main/mod_savefile.F90, Main/mod_init.F90:421-450,941-966)
+
+int mlc_member_write_sav(mlc_ctx *x, int m, const char *path, const char *idatex,
+                         const char *calendar) {
+  if (!member_ok(x, m) || !path) return MLC_ERR_INVALID;
+  const mlc_dims d = x->mem[m].dims;
+  const size_t jx = d.jx, iy = d.iy, kz = d.kz, c3 = (jx - 1) * (iy - 1) * kz;
+  std::vector<double> u(jx * (iy - 1) * kz), v((jx - 1) * iy * kz), w((jx - 1) * (iy - 1) * (kz + 1));
+  std::vector<double> t(c3), pai(c3), qx(c3 * d.nqx), ps((jx - 1) * (iy - 1)), trac(c3 * d.ntr);
+  mlc_state_ptrs sp{};
+  sp.u = u.data(); sp.v = v.data(); sp.w = w.data(); sp.t = t.data(); sp.pai = pai.data();
+  sp.qx = qx.data(); sp.ps = ps.data(); sp.trac = d.ntr ? trac.data() : nullptr;
+  MLC_CHK(mlc_member_download_state(x, m, &sp));
+  mlc_sav_fields f{u.data(), v.data(), w.data(), t.data(), pai.data(), qx.data(), ps.data(),
+                   d.ntr ? trac.data() : nullptr};
+  return mlc_sav_write(path, &d, &f, idatex, calendar);
+}
+
+int mlc_member_read_sav(mlc_ctx *x, int m, const char *path) {
+  if (!member_ok(x, m) || !path) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
+  const mlc_dims d = x->mem[m].dims;
+  const size_t jx = d.jx, iy = d.iy, kz = d.kz, c3 = (jx - 1) * (iy - 1) * kz;
+  std::vector<double> u(jx * (iy - 1) * kz), v((jx - 1) * iy * kz), w((jx - 1) * (iy - 1) * (kz + 1));
+  std::vector<double> t(c3), pai(c3), qx(c3 * d.nqx), ps((jx - 1) * (iy - 1)), trac(c3 * d.ntr);
+  mlc_sav_fields f{u.data(), v.data(), w.data(), t.data(), pai.data(), qx.data(), ps.data(),
+                   d.ntr ? trac.data() : nullptr};
+  MLC_CHK(mlc_sav_read(path, &d, &f, nullptr, 0));
+  std::vector<double> su(u.size()), sv(v.size()), sw(w.size()), s3[9];
+  for (auto &a : s3) a.resize(c3);
+  std::vector<double> sq(qx.size()), sps(ps.size()), str(trac.size());
+  mlc_state_ptrs sp{};
+  sp.u = su.data(); sp.v = sv.data(); sp.w = sw.data(); sp.pai = s3[0].data(); sp.tetav = s3[1].data();
+  sp.t = s3[2].data(); sp.tvirt = s3[3].data(); sp.ux = s3[4].data(); sp.vx = s3[5].data();
+  sp.p = s3[6].data(); sp.rho = s3[7].data(); sp.qsat = s3[8].data(); sp.qx = sq.data();
+  sp.ps = sps.data(); sp.trac = d.ntr ? str.data() : nullptr;
+  MLC_CHK(mlc_sav_restart_state(&d, &f, &sp));
+  return mlc_member_upload_state(x, m, &sp);
 }
 
 int mlc_members(const mlc_ctx *x) { return x ? (int)x->mem.size() : 0; }

@@ -64,6 +64,17 @@ class MolochDomain:
     def download(self, state_ptrs: abi.mlc_state_ptrs):
         abi.check(self.lib.mlc_download_state(self._ctx, C.byref(state_ptrs)), "download")
 
+    # -- SAV restart files (Main/mod_savefile.F90, Main/mod_init.F90) ------
+    def write_sav(self, path: str, idatex: str | None = None, calendar: str | None = None):
+        """Snapshot the device state into the MOLOCH variables of a SAV file."""
+        enc = lambda x: None if x is None else x.encode()
+        abi.check(self.lib.mlc_member_write_sav(self._ctx, 0, str(path).encode(), enc(idatex),
+                                                enc(calendar)), "write_savefile")
+
+    def read_sav(self, path: str):
+        """Restart the device state from a SAV file (read_savefile + init)."""
+        abi.check(self.lib.mlc_member_read_sav(self._ctx, 0, str(path).encode()), "read_savefile")
+
     # -- the step split at the physics (Main/mod_moloch.F90:354-376) --------
     def step_dynamics(self):
         """Dynamics, boundary and mkslice's edits: the state the physics reads."""
