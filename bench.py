@@ -152,15 +152,15 @@ def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None
 # profiles/kernels_mixed_moist256_full.md, k_solve_mixed 182.0 MB); scaled to the
 # bench case by its points.  Keyed by (kernel group, precision, advected fields).
 MEASURED_TRAFFIC_PER_POINT = {("adv_horizontal", "fp64", 10): 733.6e6 / (256 * 256 * 41),
-                              ("sound_solve", "mixed", 10): 182.0e6 / (256 * 256 * 41)}
+                              ("sound_solve", "mixed", 10): 204.0e6 / (256 * 256 * 41)}
 # What limits the dominant kernel when it is not HBM, from the same ncu captures.
 MEASURED_LIMITER = {
     ("adv_horizontal", "fp64"): {
         "pipe": "fp64", "active": 0.837,
         "source": "ncu sm__inst_executed_pipe_fp64, profiles/adv_horizontal_fp64_moist256_full.md"},
     ("sound_solve", "mixed"): {
-        "stall": "long scoreboard (memory latency)", "warps_active": 0.20,
-        "source": "ncu, profiles/kernels_mixed_moist256_full.md"},
+        "stall": "block barrier (one a level, freeing a copy stage)", "warps_active": 0.21,
+        "source": "ncu, profiles/solve_mixed_bulk_moist256_full.md"},
 }
 
 

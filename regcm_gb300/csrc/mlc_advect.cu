@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "mlc_kernels.cuh"
+#include "mlc_tma.cuh"
 
 namespace mlc {
 
@@ -308,50 +309,6 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   const T f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
   dst[ot - PS] = vupdate<T>(c1m2, f2m, f2n, sm2, sm1, zum2, zdm2);
   dst[ot] = vupdate<T>(c1m1, f2n, T(0), sm1, sk, zum1, zdm1);
-}
-
-// ---- TMA tile loads and mbarriers (inline PTX, sm_90+) ----------------------
-__device__ __forceinline__ unsigned smem_u32(const void *p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-// orders this thread's earlier generic-proxy accesses of shared memory before
-// a following async-proxy (TMA) write to it
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-// one tiled copy of the box at (x, y, z) of the tensor map into shared memory
-__device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z,
-                                            uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
-  return ok != 0;
-}
-// gives up after a bounded number of polls (a copy that never lands must not
-// hang the GPU); the caller records the fault
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
-  for (int it = 0; it < (1 << 18); ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
 }
 
 // ---- lane vectors ---------------------------------------------------------

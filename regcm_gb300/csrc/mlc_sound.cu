@@ -21,6 +21,7 @@
 // weight bdywt recomputed from ibnd and hefc instead of read from an array
 // (the same value, Main/mod_bdycod.F90:4033-4047).
 #include "mlc_kernels.cuh"
+#include "mlc_tma.cuh"
 
 namespace mlc {
 
@@ -233,6 +234,11 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
 #undef COL
 }
 
+constexpr int kSvStages = 4;   // levels in flight ahead of the one being solved
+constexpr int kSvW = 128;            // columns of a block (one row segment)
+constexpr int kSvZW = kSvW + 8;      // raw divergence rows with a 4-column halo each side
+constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
+
 // The solve of a mixed member (same equations as k_sound_solve), in FP32
 // only, one thread per column.  Where rounding is amplified the values are
 // double-floats: theta_v at half levels, the hydrostatic balance
@@ -244,139 +250,214 @@ __global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int l
 // once; the upward pass substitutes back and updates Exner (and, after the
 // last substep, s) a level behind.  Between the passes the column's
 // eliminated w stays in w, its multipliers and filtered divergence in the
-// FP32 planes of wz_d[1] and wz_d[0] (free during the acoustic loop; a
-// column's two passes follow each other closely, so these round trips stay in
-// L2).  wz[2] holds theta_v(k-1) - theta_v(k) from sound_prep.
-// At most 128 threads a block, five blocks an SM: about 100 registers a
-// thread, so that more columns' loads are in flight (the kernel waits on
-// memory; measured 14 % faster than the unconstrained 111 registers)
+// FP32 planes of wz_d[1] and wz_d[0] (free during the acoustic loop).
+// wz[2] holds theta_v(k-1) - theta_v(k) from sound_prep.
+//
+// The inputs stream through shared memory: a block is 128 consecutive
+// columns of one row, and the copy engine brings each level's planes as
+// 512-byte row segments (untiled bulk copies, 16-byte aligned: the segment
+// starts at a multiple of 128 columns, the raw divergence's halo of 4
+// columns keeps that alignment) kSvStages levels ahead of the level being
+// solved, so the per-level chain of dependent arithmetic never waits on
+// memory.  The copies of one level (11 planes and 1 or 3 divergence rows)
+// complete on one mbarrier; a stage is refilled after every thread has read
+// it (one block barrier a level).  The upward pass reads back w, the
+// multipliers and the filtered divergence the threads stored in the
+// downward pass, after a proxy fence.  (Measured on the 512x512x41 step:
+// 0.73 ms of solves a step against 0.95 for the same thread-per-column
+// kernel with register prefetch of one level.)
 template <class R>
-__global__ void __launch_bounds__(128, 5) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
+__global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
+  constexpr int NS = kSvStages;
+  extern __shared__ __align__(16) float sv_smem[];
+  __shared__ __align__(8) uint64_t mbar[NS];
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
-  const int j = (int)(blockIdx.x * blockDim.x + threadIdx.x) + 2;
-  const int i = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
-  if (j > g.jx - 2 || i > g.iy - 2) return;
+  const int t = (int)threadIdx.x;
+  const int x0 = (int)blockIdx.x * kSvW;          // first column (0-based j-1) of the block
+  const int i = (int)blockIdx.y + 2;
+  if (x0 + 1 > g.jx - 2 || i > g.iy - 2) return;  // uniform over the block
+  const int j = x0 + t + 1;
+  const bool act = j >= 2 && j <= g.jx - 2;
   const int kz = g.kz;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const int adv = (D.clk->adv_role + advoff) & 1;
   const size_t F = g.field3(), F1 = g.PS * (size_t)(kz + 1);
-  const size_t ij = g.at2(j, i);
-  // offsets from the column's own point, signed (the divergence filter reads
-  // the neighbours at level 1 below the column's offset); every plane is a
-  // separate array, so loads of the next level may pass this level's stores
   const int PS = (int)g.PS, P = g.P;
-  float *__restrict__ pai_h = reinterpret_cast<float *>(D.pai[adv]) + ij;
+  const size_t r0 = g.at2(1, i);                  // row i, column 1
+  // row bases (column 1 of row i, level 1)
+  float *__restrict__ pai_h = reinterpret_cast<float *>(D.pai[adv]) + r0;
   float *__restrict__ pai_l = pai_h + F;
-  float *__restrict__ tvf_h = reinterpret_cast<float *>(D.tetavf) + ij;
+  float *__restrict__ tvf_h = reinterpret_cast<float *>(D.tetavf) + r0;
   float *__restrict__ tvf_l = tvf_h + F1;
-  const float *__restrict__ cfz_h = reinterpret_cast<const float *>(sa.cfz) + ij;
+  const float *__restrict__ cfz_h = reinterpret_cast<const float *>(sa.cfz) + r0;
   const float *__restrict__ cfz_l = cfz_h + F1;
-  float *__restrict__ zfs = reinterpret_cast<float *>(D.wz_d[0]) + ij;
-  float *__restrict__ mul = reinterpret_cast<float *>(D.wz_d[1]) + ij;
-  const float *__restrict__ zraw = D.zdiv2 + ij;
-  const float *__restrict__ dtet = D.wz[2] + ij;
-  const float *__restrict__ fmz = sa.fmz + ij;
-  const float *__restrict__ fmzf = sa.fmzf + ij;
-  float *__restrict__ s = D.s + ij;
-  float *__restrict__ w = D.w + ij;
+  float *__restrict__ zfs = reinterpret_cast<float *>(D.wz_d[0]) + r0;
+  float *__restrict__ mul = reinterpret_cast<float *>(D.wz_d[1]) + r0;
+  const float *__restrict__ zraw = D.zdiv2 + r0;
+  const float *__restrict__ dtet = D.wz[2] + r0;
+  const float *__restrict__ fmz = sa.fmz + r0;
+  const float *__restrict__ fmzf = sa.fmzf + r0;
+  float *__restrict__ s = D.s + r0;
+  float *__restrict__ w = D.w + r0;
   const float dtrdz = c.dtsoundf * c.rdzitaf;
   const float rdrcv = float(kRdrcv);
   const float rdt = rdrcv * dtrdz;
   const F2 ngdts{-c.gdts_hi, -c.gdts_lo};
-  const int32_t ib = sa.ibnd_cr[ij];
+  const int ij_off = j - 1;                       // this thread's column offset in a row
+  const int32_t ib = act ? sa.ibnd_cr[r0 + ij_off] : 0;
   const int nsp = c.nspgx;
   const bool filt = c.divfilter != 0;
+  // copy extents: the block's columns, and the raw divergence with its halo
+  const int xe = min(x0 + kSvW, P);
+  const int zs = x0 >= 4 ? x0 - 4 : 0, ze = min(x0 + kSvW + 4, P);
+  const unsigned wb = (unsigned)(xe - x0) * 4u, zb = (unsigned)(ze - zs) * 4u;
+  const int zc = x0 + t - zs;                     // this column in a halo row
+  auto stage = [&](int b) { return sv_smem + (size_t)b * kSvStage; };
+  // stage layout: zraw rows i, i-1, i+1 (kSvZW each), then 11 fields of kSvW
+  auto fld = [&](float *st, int f) { return st + 3 * kSvZW + f * kSvW; };
+  const int nd = kz - 1;                          // down units: m = kz-1 .. 1
+  // down unit u: A(m) = zraw, s, fmz, pai at level m; B(m+1) = w, fmzf,
+  // dtet, tvf, cfz at interface m+1 (m = kz-1-u)
+  auto issue_down = [&](int u, int b) {
+    const int m = kz - 1 - u;
+    float *st = stage(b);
+    uint64_t *bar = &mbar[b];
+    fence_proxy_async();
+    mbar_expect_tx(bar, (filt ? 3u : 1u) * zb + 11u * wb);
+    const int o = (m - 1) * PS, ob = m * PS;
+    bulk_load(st, zraw + o + zs, zb, bar);
+    if (filt) {
+      bulk_load(st + kSvZW, zraw + o - P + zs, zb, bar);
+      bulk_load(st + 2 * kSvZW, zraw + o + P + zs, zb, bar);
+    }
+    bulk_load(fld(st, 0), s + o + x0, wb, bar);
+    bulk_load(fld(st, 1), fmz + o + x0, wb, bar);
+    bulk_load(fld(st, 2), pai_h + o + x0, wb, bar);
+    bulk_load(fld(st, 3), pai_l + o + x0, wb, bar);
+    bulk_load(fld(st, 4), w + ob + x0, wb, bar);
+    bulk_load(fld(st, 5), fmzf + ob + x0, wb, bar);
+    bulk_load(fld(st, 6), dtet + ob + x0, wb, bar);
+    bulk_load(fld(st, 7), tvf_h + ob + x0, wb, bar);
+    bulk_load(fld(st, 8), tvf_l + ob + x0, wb, bar);
+    bulk_load(fld(st, 9), cfz_h + ob + x0, wb, bar);
+    bulk_load(fld(st, 10), cfz_l + ob + x0, wb, bar);
+  };
+  // up unit v (m = v + 2): w(m), mul(m) (m <= kz), and pai, zfs, fmz, s,
+  // fmzf at level m-1
+  auto issue_up = [&](int v, int b) {
+    const int m = v + 2;
+    float *st = stage(b);
+    uint64_t *bar = &mbar[b];
+    fence_proxy_async();
+    mbar_expect_tx(bar, (m <= kz ? 8u : 7u) * wb);
+    const int o = (m - 1) * PS, op = (m - 2) * PS;
+    bulk_load(fld(st, 0), w + o + x0, wb, bar);
+    if (m <= kz) bulk_load(fld(st, 1), mul + o + x0, wb, bar);
+    bulk_load(fld(st, 2), pai_h + op + x0, wb, bar);
+    bulk_load(fld(st, 3), pai_l + op + x0, wb, bar);
+    bulk_load(fld(st, 4), zfs + op + x0, wb, bar);
+    bulk_load(fld(st, 5), fmz + op + x0, wb, bar);
+    bulk_load(fld(st, 6), s + op + x0, wb, bar);
+    bulk_load(fld(st, 7), fmzf + op + x0, wb, bar);
+  };
+  // a failed wait (a copy that never landed): record it, let the copies in
+  // flight land (bounded) and leave
+  auto bail = [&](int gnext, int gend) {
+    if (t == 0) {
+      atomicOr(&D.clk->fault, 1);
+      for (int q = gnext; q < gend && q < gnext + NS; ++q) mbar_wait_bounded(&mbar[q % NS], (unsigned)((q / NS) & 1));
+    }
+  };
+  if (t == 0) {
+    for (int q = 0; q < NS; ++q) mbar_init(&mbar[q], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (t == 0)
+    for (int u = 0; u < NS && u < nd; ++u) issue_down(u, u);
 
-  // per level m: the raw divergence with its filter stencil, s, fmz and
-  // Exner (the cell below the interface of level m+1) ...
   struct LvA {
     float z, lap, s, fmz;
     F2 pai;
   };
-  auto loadA = [&](int m) {
-    const int o = (m - 1) * PS;
-    LvA a;
-    a.z = zraw[o];
-    a.lap = filt ? (zraw[o - 1] + zraw[o + 1] + zraw[o - P] + zraw[o + P] - 4.f * a.z) : 0.f;
-    a.s = s[o];
-    a.fmz = fmz[o];
-    a.pai = F2{pai_h[o], pai_l[o]};
-    return a;
-  };
-  // ... and what the w equation of level m reads at its own interface
-  struct LvB {
-    float w, fmzf, dtet;
-    F2 tvf, cfz;
-  };
-  auto loadB = [&](int m) {
-    const int o = (m - 1) * PS;
-    LvB b;
-    b.w = w[o];
-    b.fmzf = fmzf[o];
-    b.dtet = dtet[o];
-    b.tvf = F2{tvf_h[o], tvf_l[o]};
-    b.cfz = F2{cfz_h[o], cfz_l[o]};
-    return b;
-  };
-  // divergence_diffusion plus the vertical divergence (:531-543, :627-630)
   auto zf_of = [&](int m, const LvA &a, float s_above) {
     float z = a.z;
     if (filt) z = z + sa.xknu_r[m - 1] * a.lap;
     const float bw = ib > 0 ? 1.f - sa.hefc_r[(size_t)(ib - 1) + (size_t)(m - 1) * nsp] : 1.f;
     return z + bw * dtrdz * a.fmz * (a.s - s_above);
   };
-
-  // downward: coefficients of level k and elimination k = kz..2 (:634-656)
-  float wnext = w[kz * PS];  // w(kz+1) = -s(kz+1)
-  float wkp1 = 0.f;
-  LvA ak = loadA(kz);         // level k
-  float zfk = zf_of(kz, ak, s[kz * PS]);
-  LvA am = loadA(kz - 1);     // level k-1
-  LvB bk = loadB(kz);         // level k
-  for (int k = kz; k >= 2; --k) {
-    const int o = (k - 1) * PS;
-    // next level's loads, in flight during this level
-    LvA an{};
-    LvB bn{};
-    if (k >= 3) {
-      an = loadA(k - 2);
-      bn = loadB(k - 1);
-    }
-    const float zf_m = zf_of(k - 1, am, ak.s);
-    zfs[o] = zfk;
-    const F2 pai_m = am.pai, pai_k = ak.pai;
-    const float wold = bk.w;
-    const float corr = wold * bk.fmzf * dtrdz * bk.dtet;
-    const F2 tvf = df_add_f(bk.tvf, -corr);
-    tvf_h[o] = tvf.hi;
-    tvf_l[o] = tvf.lo;
-    const F2 zrd = df_mul(tvf, bk.cfz);
-    const F2 dp = two_sum(pai_m.hi - pai_k.hi, pai_m.lo - pai_k.lo);  // hi difference exact
-    const F2 bal = df_add(ngdts, df_mul(F2{-zrd.hi, -zrd.lo}, dp));
-    const float zr = df_f(zrd), pm = df_f(pai_m), pk = df_f(pai_k);
-    float zw = wold + df_f(bal);
-    zw = zw + rdrcv * zr * (pm * zf_m - pk * zfk);
-    const float ff = sa.ffilt_r[k - 1];
-    const float zu = rdt * am.fmz * zr * pm + ff;
-    const float zd = rdt * ak.fmz * zr * pk + ff;
-    const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
-    wnext = zrapp * (zw + zd * wnext);
-    wkp1 = zrapp * zu;
-    w[o] = wnext;
-    mul[o] = wkp1;
-    zfk = zf_m;
-    ak = am;
-    am = an;
-    bk = bn;
+  // level kz and the interface below it straight from memory (once)
+  LvA ak{};
+  float wnext = 0.f, zfk = 0.f;
+  if (act) {
+    const int o = (kz - 1) * PS + ij_off;
+    ak.z = zraw[o];
+    ak.lap = filt ? (zraw[o - 1] + zraw[o + 1] + zraw[o - P] + zraw[o + P] - 4.f * ak.z) : 0.f;
+    ak.s = s[o];
+    ak.fmz = fmz[o];
+    ak.pai = F2{pai_h[o], pai_l[o]};
+    wnext = w[kz * PS + ij_off];
+    zfk = zf_of(kz, ak, s[kz * PS + ij_off]);
   }
-  zfs[0] = zfk;  // level 1
-  // upward: back substitution k = 2..kz (:660-664), the Exner function
-  // (:668-671) and s (:728-734) of level k-1 once w(k) is known
+  float wkp1 = 0.f;
+  for (int u = 0; u < nd; ++u) {
+    const int k = kz - u, m = k - 1;
+    const int b = u % NS;
+    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((u / NS) & 1));
+    const float *st = stage(b);
+    if (act) {
+      const int o = (k - 1) * PS + ij_off;
+      LvA am;
+      am.z = st[zc];
+      am.lap = filt ? (st[zc - 1] + st[zc + 1] + st[kSvZW + zc] + st[2 * kSvZW + zc] - 4.f * am.z) : 0.f;
+      const float *f0 = st + 3 * kSvZW + t;
+      am.s = f0[0];
+      am.fmz = f0[kSvW];
+      am.pai = F2{f0[2 * kSvW], f0[3 * kSvW]};
+      const float wold = f0[4 * kSvW], bfmzf = f0[5 * kSvW], bdtet = f0[6 * kSvW];
+      const F2 btvf{f0[7 * kSvW], f0[8 * kSvW]}, bcfz{f0[9 * kSvW], f0[10 * kSvW]};
+      const float zf_m = zf_of(m, am, ak.s);
+      zfs[o] = zfk;
+      const F2 pai_m = am.pai, pai_k = ak.pai;
+      const float corr = wold * bfmzf * dtrdz * bdtet;
+      const F2 tvf = df_add_f(btvf, -corr);
+      tvf_h[o] = tvf.hi;
+      tvf_l[o] = tvf.lo;
+      const F2 zrd = df_mul(tvf, bcfz);
+      const F2 dp = two_sum(pai_m.hi - pai_k.hi, pai_m.lo - pai_k.lo);
+      const F2 bal = df_add(ngdts, df_mul(F2{-zrd.hi, -zrd.lo}, dp));
+      const float zr = df_f(zrd), pm = df_f(pai_m), pk = df_f(pai_k);
+      float zw = wold + df_f(bal);
+      zw = zw + rdrcv * zr * (pm * zf_m - pk * zfk);
+      const float ff = sa.ffilt_r[k - 1];
+      const float zu = rdt * am.fmz * zr * pm + ff;
+      const float zd = rdt * ak.fmz * zr * pk + ff;
+      const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
+      wnext = zrapp * (zw + zd * wnext);
+      wkp1 = zrapp * zu;
+      w[o] = wnext;
+      mul[o] = wkp1;
+      zfk = zf_m;
+      ak = am;
+    }
+    if (__syncthreads_or(!landed)) {
+      bail(u + 1, nd);
+      return;
+    }
+    if (t == 0 && u + NS < nd) issue_down(u + NS, b);
+  }
+  if (act) zfs[ij_off] = zfk;  // level 1
+  // this thread's stores of w, mul and zfs are read back by the copy engine
+  fence_proxy_async_global();
+  __syncthreads();
+  const int nu = kz;  // up units: m = 2 .. kz+1
+  if (t == 0)
+    for (int v = 0; v < NS && v < nu; ++v) issue_up(v, (nd + v) % NS);
   auto exner = [&](int m, float wm, float wmp, F2 pk, float zf, float fz, float sm, float fzf) {
-    const int o = (m - 1) * PS;
+    const int o = (m - 1) * PS + ij_off;
     const float inc = rdrcv * (zf + (dtrdz * fz * (wm - wmp)));
     const F2 d = df_mul_f(pk, inc);
     const F2 pn = df_add(pk, F2{-d.hi, -d.lo});
@@ -384,37 +465,36 @@ __global__ void __launch_bounds__(128, 5) k_solve_mixed(const Dom<R> *__restrict
     pai_l[o] = pn.lo;
     if (last && m >= 2) s[o] = (wm + sm) * fzf;
   };
-  float wprev = w[0];  // w(1) = 0
-  // level m's Exner inputs, loaded a level ahead
-  F2 ep = F2{pai_h[0], pai_l[0]};
-  float ezf = zfs[0], efz = fmz[0], es = s[0], efzf = fmzf[0];
-  float nw = w[PS], nmul = mul[PS];
-  for (int k = 2; k <= kz; ++k) {
-    const int o = (k - 1) * PS;
-    const float wel = nw, mk = nmul;
-    const F2 cp = ep;
-    const float czf = ezf, cfz_ = efz, cs = es, cfzf = efzf;
-    if (k < kz) {
-      nw = w[o + PS];
-      nmul = mul[o + PS];
+  float wprev = act ? w[ij_off] : 0.f;  // w(1) = 0
+  for (int v = 0; v < nu; ++v) {
+    const int k = v + 2, gu = nd + v;
+    const int b = gu % NS;
+    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((gu / NS) & 1));
+    if (act) {
+      const float *f0 = stage(b) + 3 * kSvZW + t;
+      const float wel = f0[0];
+      const F2 cp{f0[2 * kSvW], f0[3 * kSvW]};
+      const float czf = f0[4 * kSvW], cfz_ = f0[5 * kSvW], cs = f0[6 * kSvW], cfzf = f0[7 * kSvW];
+      if (k <= kz) {
+        const float wk = wel + f0[kSvW] * wprev;
+        w[(k - 1) * PS + ij_off] = wk;
+        exner(k - 1, wprev, wk, cp, czf, cfz_, cs, cfzf);
+        wprev = wk;
+      } else {
+        exner(kz, wprev, wel, cp, czf, cfz_, cs, cfzf);
+      }
     }
-    ep = F2{pai_h[o], pai_l[o]};
-    ezf = zfs[o];
-    efz = fmz[o];
-    es = s[o];
-    efzf = fmzf[o];
-    const float wk = wel + mk * wprev;
-    w[o] = wk;
-    exner(k - 1, wprev, wk, cp, czf, cfz_, cs, cfzf);
-    wprev = wk;
+    if (__syncthreads_or(!landed)) {
+      bail(gu + 1, nd + nu);
+      return;
+    }
+    if (t == 0 && v + NS < nu) issue_up(v + NS, b);
   }
-  exner(kz, wprev, w[kz * PS], ep, ezf, efz, es, efzf);
-  if (last) {
-    s[0] = 0.f;
-    s[kz * PS] = 0.f;
+  if (last && act) {
+    s[ij_off] = 0.f;
+    s[kz * PS + ij_off] = 0.f;
   }
 }
-
 // Main/mod_moloch.F90:677-721 with divergence_damping :738-765 folded in
 template <class R>
 __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int advoff,
@@ -845,7 +925,10 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
                  (unsigned)L.nmem);
   const size_t cols = (size_t)3 * (L.kz + 2) * blk.x * blk.y;
   if constexpr (sizeof(R) == sizeof(float)) {
-    k_solve_mixed<R><<<grd, blk, 0, s>>>(d, advoff, last ? 1 : 0);
+    // one block per 128-column row segment (the solve shape applies to FP64)
+    const int tj = (L.jx - 1 + kSvW - 1) / kSvW;
+    k_solve_mixed<R><<<dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem), kSvW,
+                       (size_t)kSvStages * kSvStage * sizeof(float), s>>>(d, advoff, last ? 1 : 0);
   } else {
     k_sound_solve<R><<<grd, blk, cols * sizeof(double), s>>>(d, advoff, last ? 1 : 0);
   }
