@@ -178,11 +178,12 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
     s.hefc_r = reinterpret_cast<const R *>(s.hefc);
     s.fcx_r = reinterpret_cast<const R *>(s.fcx);
     s.dz_r = reinterpret_cast<const R *>(s.dz);
+    s.dz_lo = nullptr;
   } else {
     s.gzitak_r = cv.take<R>(d.kz + 1); s.gzitakh_r = cv.take<R>(d.kz);
     s.xkdamp_r = cv.take<R>(d.kz); s.xknu_r = cv.take<R>(d.kz); s.ffilt_r = cv.take<R>(d.kz);
     s.tnudge_r = cv.take<R>(d.kz); s.hefc_r = cv.take<R>((size_t)p.nspgx * d.kz);
-    s.fcx_r = cv.take<R>(p.nspgx); s.dz_r = cv.take<R>(F);
+    s.fcx_r = cv.take<R>(p.nspgx); s.dz_r = cv.take<R>(F); s.dz_lo = cv.take<R>(F);
   }
   Bdy<R> &b = D.bd;
   for (int h = 0; h < 2; ++h) {
@@ -840,7 +841,15 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
   MLC_CHK(put3<R>(x, g, s->rfmzv, W(a.rfmzv), jx - 1, iy, kz, 0));
   MLC_CHK(put3<double>(x, g, s->zeta, W(a.zeta), jx - 1, iy - 1, kz, 0));
   MLC_CHK(put3<double>(x, g, s->dz, W(a.dz), jx - 1, iy - 1, kz, 0));
-  if (sizeof(R) != sizeof(double)) MLC_CHK(put3<R>(x, g, s->dz, W(a.dz_r), jx - 1, iy - 1, kz, 0));
+  if (sizeof(R) != sizeof(double)) {
+    MLC_CHK(put3<R>(x, g, s->dz, W(a.dz_r), jx - 1, iy - 1, kz, 0));
+    // the remainder dz - (float)dz, so that {dz_r, dz_lo} carries dz to FP64 accuracy
+    const size_t n = (size_t)(jx - 1) * (iy - 1) * kz;
+    std::vector<double> lo(n);
+    for (size_t e = 0; e < n; ++e) lo[e] = s->dz[e] - (double)(float)s->dz[e];
+    MLC_CHK(put3<R>(x, g, lo.data(), W(a.dz_lo), jx - 1, iy - 1, kz, 0));
+    MLC_TRY(cudaStreamSynchronize(x->stream));
+  }
   // vertical WAF ratios (dtrdz*fmz)/fmzf, Main/mod_moloch.F90:888-889
   {
     const double mo_dzita = s->zita[kz - 1];

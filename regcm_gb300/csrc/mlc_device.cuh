@@ -66,6 +66,9 @@ struct Stat {
   const double *rlat;      // (iy)
   // the 1-D arrays, hefc, fcx and dz in the field type (aliases for FP64)
   const R *gzitak_r, *gzitakh_r, *xkdamp_r, *xknu_r, *ffilt_r, *tnudge_r, *hefc_r, *fcx_r, *dz_r;
+  // a mixed member's dz - dz_r (dz as the double-float {dz_r, dz_lo}, for the
+  // mass budget); null for an FP64 member
+  const R *dz_lo;
   // spectral nudging: sine bases bvx (km2 rows of jx) and bvy (lm2 rows of
   // iy), the level weights cnudge (kz)
   const R *bvx, *bvy, *cnudge;

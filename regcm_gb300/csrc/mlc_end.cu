@@ -542,6 +542,7 @@ __global__ void k_end_ps(const Dom<R> *__restrict__ doms, int uvoff, int advoff)
 //   kEndPre   up to mkslice: the state the physics reads.
 //   kEndPost  status_update with the member's tendencies (Dom::tend).
 constexpr int kEndAll = 0, kEndPre = 1, kEndPost = 2;
+constexpr double kTracFloor = 1.0e-50;  // mkslice's tracer floor (Main/mod_slice.F90:141-147)
 template <class R, int PH>
 __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
   const Dom<R> &D = doms[blockIdx.z];
@@ -602,7 +603,7 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
       }
       for (int n = 0; n < g.ntr; ++n) {
         const size_t on = o + (size_t)n * F;
-        if (st.trac[on] < R(1.0e-50)) st.trac[on] = R(0);
+        if ((double)st.trac[on] < kTracFloor) st.trac[on] = R(0);
       }
     }
     continue;
@@ -637,7 +638,7 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
       for (int n = 0; n < g.ntr; ++n) {
         const size_t on = o + (size_t)n * F;
         R q = st.trac[on];
-        if (PH == kEndAll && q < R(1.0e-50)) q = R(0);  // mkslice
+        if (PH == kEndAll && (double)q < kTracFloor) q = R(0);  // mkslice
         if (ten) q = q + dts * ten[o + (size_t)(3 + g.nqx + n) * F];
         if (q < R(0)) q = R(0);
         st.trac[on] = q;
@@ -932,24 +933,32 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
       R dz[V], rh[V], qs[V], q1[V];
       ld_vec16<R, V>(dz, dzp + base);
       ld_vec16<R, V>(rh, st.rho + base);
-      ld_vec16<R, V>(qs, st.qx + base);
-      for (int n = 1; n < nqx; ++n) {
-        ld_vec16<R, V>(q1, st.qx + base + (size_t)n * F);
-#pragma unroll
-        for (int q = 0; q < V; ++q) qs[q] += q1[q];
-      }
       if constexpr (sizeof(R) == sizeof(float)) {
-        float sd = 0.f, sq = 0.f;
+        // FP32 state, FP64-accurate sums: dz as the double-float {dz_r,
+        // dz_lo}, dz*rho and each species' share as double-float products,
+        // double-float running sums (about 1e-14 relative against the FP64
+        // sums of the same FP32 state)
+        R dzl[V];
+        ld_vec16<R, V>(dzl, sa.dz_lo + base);
+        F2 dr[V];
 #pragma unroll
         for (int q = 0; q < V; ++q) {
           const int j = c0 + q + 1;
-          const float dr = (j >= 2 && j <= jx - 2) ? dz[q] * rh[q] : 0.f;
-          sd += dr;
-          sq += dr * qs[q];
+          dr[q] = (j >= 2 && j <= jx - 2) ? df_mul_f(F2{dz[q], dzl[q]}, rh[q]) : F2{0.f, 0.f};
+          dry2 = df_add(dry2, dr[q]);
         }
-        dry2 = df_add_f(dry2, sd);
-        qm2 = df_add_f(qm2, sq);
+        for (int n = 0; n < nqx; ++n) {
+          ld_vec16<R, V>(q1, st.qx + base + (size_t)n * F);
+#pragma unroll
+          for (int q = 0; q < V; ++q) qm2 = df_add(qm2, df_mul_f(dr[q], q1[q]));
+        }
       } else {
+        ld_vec16<R, V>(qs, st.qx + base);
+        for (int n = 1; n < nqx; ++n) {
+          ld_vec16<R, V>(q1, st.qx + base + (size_t)n * F);
+#pragma unroll
+          for (int q = 0; q < V; ++q) qs[q] += q1[q];
+        }
 #pragma unroll
         for (int q = 0; q < V; ++q) {
           const int j = c0 + q + 1;
@@ -971,19 +980,9 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
       const int i = (int)(e % (unsigned)(iy - 1)) + 1, k = (int)(e / (unsigned)(iy - 1)) + 1;
       const size_t ko = (size_t)(k - 1) * g.PS;
       const size_t ow = g.at2(1, i) + ko, oe = g.at2(jx - 1, i) + ko;
-      if constexpr (sizeof(R) == sizeof(float)) {
-        // FP32 products, summed in FP64
-        const float dtdx = float(dt * dx);
-        const float fw = st.u[g.at2(1, i) + ko] * dtdx * sa.dz_r[ow] * st.rho[ow];
-        const float fe = st.u[g.at2(jx, i) + ko] * dtdx * sa.dz_r[oe] * st.rho[oe];
-        float qw = 0.f, qe = 0.f;
-        for (int n = 0; n < nqx; ++n) {
-          qw += st.qx[ow + (size_t)n * F];
-          qe += st.qx[oe + (size_t)n * F];
-        }
-        dadv += (double)fw - (double)fe;
-        qadv += (double)(qw * fw) - (double)(qe * fe);
-      } else {
+      {
+        // FP64 products of the state's values in both precisions (a few
+        // thousand terms: the budget stays FP64-accurate for a mixed member)
         const double uw = (double)st.u[g.at2(1, i) + ko], ue = (double)st.u[g.at2(jx, i) + ko];
         const double dzw = (double)sa.dz[ow], rw = (double)st.rho[ow];
         const double dze = (double)sa.dz[oe], re = (double)st.rho[oe];
