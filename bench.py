@@ -149,7 +149,7 @@ def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None
 # DRAM bytes per point of a launch, measured by ncu on a smaller case of the same
 # kernel and precision (moist 256x256x41, 10 advected fields:
 # profiles/adv_horizontal_fp64_moist256_full.md, 733.6 MB;
-# profiles/kernels_mixed_moist256_full.md, k_solve_mixed 182.0 MB); scaled to the
+# profiles/solve_mixed_bulk_moist256_full.md, k_solve_mixed 204.0 MB); scaled to the
 # bench case by its points.  Keyed by (kernel group, precision, advected fields).
 MEASURED_TRAFFIC_PER_POINT = {("adv_horizontal", "fp64", 10): 733.6e6 / (256 * 256 * 41),
                               ("sound_solve", "mixed", 10): 204.0e6 / (256 * 256 * 41)}

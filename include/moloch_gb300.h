@@ -283,7 +283,9 @@ size_t mlc_member_footprint(const mlc_dims *dims, const mlc_params *params);
  * thread per column; solve 32x2). */
 typedef struct mlc_tune_report {
   int32_t col_x, col_y;      /* column kernels                        */
-  int32_t solve_x, solve_y;  /* implicit w-Exner solve                */
+  int32_t solve_x, solve_y;  /* accepted for compatibility and reported;
+                                the solves run on 128-column row
+                                segments whatever these say            */
   int32_t vert_x, vert_y;    /* vertical WAF passes                   */
   int32_t htile;             /* horizontal WAF tile, columns x rows:
                                 0 32x8, 1 64x8, 2 64x4, 3 32x4        */

@@ -1582,8 +1582,6 @@ int group_of(const char *name) {
 }
 
 bool shapes_fit(const LaunchGeom &L) {
-  const size_t col3 = (size_t)3 * (L.kz + 2) * sizeof(double);
-  if (col3 * L.solve_x * L.solve_y > 200 * 1024) return false;
   return L.col_x * L.col_y <= 1024 && L.vert_x * L.vert_y <= 1024;
 }
 

@@ -18,7 +18,7 @@ namespace mlc {
 struct LaunchGeom {
   int jx, iy, kz, nmem;
   int col_x, col_y;      // column kernels
-  int solve_x, solve_y;  // sound_solve
+  int solve_x, solve_y;  // kept in the tune report; the solves use fixed 128-column blocks
   int vert_x, vert_y;    // adv_vertical
   int htile;             // adv_horizontal tile shape (hshape)
   int nadv_r;            // advected fields of type R per member

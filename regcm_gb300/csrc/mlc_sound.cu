@@ -121,119 +121,214 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tile
   }
 }
 
-// Main/mod_moloch.F90:531-543,627-671,728-734.  The column of one thread is
-// kept in shared memory laid out [level][thread] (consecutive threads hit
-// consecutive banks).  The recurrence runs in FP64 for either field type.
+// The implicit w-Exner solve of an FP64 member (Main/mod_moloch.F90:627-671,
+// s :728-734): per interior column the filtered divergence plus its vertical
+// part, the Thomas elimination k = kz..2, back substitution, the Exner
+// update and (after the last substep) s.  Same structure as the mixed solve
+// below: a block is one 128-column row segment, one thread per column, the
+// downward pass forms each level's coefficients and eliminates at once, the
+// upward pass substitutes back and updates Exner a level behind; every
+// level's planes arrive in shared memory as 1 KB row segments by bulk copies
+// kDvStages levels ahead (the raw divergence with a 2-column halo).  Between
+// the passes the eliminated w stays in w, the multipliers and the filtered
+// divergence in the scratch planes wz[1] and wz[0] (free during the acoustic
+// loop).  The per-level expressions are the reference's, in its order.
+// (Measured on the 512x512x41 step: 3.99 ms of solves a step against 5.68
+// for a column-in-shared-memory form, whose 66 KB a block left 6 warps an SM.)
+constexpr int kDvStages = 3;
+constexpr int kDvW = 128;
+constexpr int kDvZW = kDvW + 4;                   // raw divergence row, 2-column halo each side
+constexpr int kDvStage = 3 * kDvZW + 7 * kDvW;   // doubles of one stage
 template <class R>
-__global__ void k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last) {
+__global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last) {
+  static_assert(sizeof(R) == sizeof(double), "FP64 member");
+  constexpr int NS = kDvStages;
+  extern __shared__ __align__(16) double dv_smem[];
+  __shared__ __align__(8) uint64_t mbar[NS];
   const Dom<R> &D = doms[blockIdx.z];
   if (!D.active) return;
   const Geom g = D.g;
+  const int t = (int)threadIdx.x;
+  const int x0 = (int)blockIdx.x * kDvW;
+  const int i = (int)blockIdx.y + 2;
+  if (x0 + 1 > g.jx - 2 || i > g.iy - 2) return;  // uniform over the block
+  const int j = x0 + t + 1;
+  const bool act = j >= 2 && j <= g.jx - 2;
+  const int kz = g.kz;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const int adv = (D.clk->adv_role + advoff) & 1;
-  const R *__restrict__ zraw = D.zdiv2;
-  R *__restrict__ s = D.s;
-  R *__restrict__ w = D.w;
-  double *__restrict__ pai = D.pai[adv];
-  const double *__restrict__ tetav = D.tetav[adv];
-  double *__restrict__ tetavf = D.tetavf;
-  extern __shared__ double smem[];
-  const int nth = blockDim.x * blockDim.y;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  const int kz = g.kz;
-  double *zf = smem;                               // (kz+1) levels, index k
-  double *wp = smem + (size_t)(kz + 2) * nth;      // w after elimination, then final
-  double *wk = smem + (size_t)2 * (kz + 2) * nth;  // elimination multipliers
-#define COL(a, k) a[(size_t)(k) * nth + tid]
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  if (j > g.jx - 2 || i > g.iy - 2) return;
+  const int PS = (int)g.PS, P = g.P;
+  const size_t r0 = g.at2(1, i);
+  const double *__restrict__ zraw = D.zdiv2 + r0;
+  double *__restrict__ s = D.s + r0;
+  double *__restrict__ w = D.w + r0;
+  double *__restrict__ pai = D.pai[adv] + r0;
+  const double *__restrict__ tetav = D.tetav[adv] + r0;
+  double *__restrict__ tetavf = D.tetavf + r0;
+  const double *__restrict__ fmz = sa.fmz_d + r0;
+  const double *__restrict__ fmzf = sa.fmzf_d + r0;
+  double *__restrict__ zfs = D.wz[0] + r0;   // free during the acoustic loop
+  double *__restrict__ mul = D.wz[1] + r0;
   const double dts = c.dtsound;
   const double dtrdz = dts * c.rdzita;
   const double zcs2 = (dtrdz * dtrdz) * kRdrcv;
-  const size_t ij = g.at2(j, i);
-  const size_t PS = g.PS;
-  const size_t P = (size_t)g.P;
-
-  // filtered divergence plus the vertical part (:531-543, :627-630)
-  double sk = (double)s[ij];  // s(1) = 0 in the interior
-  #pragma unroll 4
-  for (int k = 1; k <= kz; ++k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    double z = (double)zraw[o];
-    if (c.divfilter) {
-      const double lap = ((double)zraw[o - 1] + (double)zraw[o + 1] + (double)zraw[o - P] +
-                          (double)zraw[o + P] - 4.0 * z);
-      z = z + sa.xknu[k - 1] * lap;
+  const int ij_off = j - 1;
+  const size_t ij = r0 + (size_t)ij_off;
+  const bool filt = c.divfilter != 0;
+  const int xe = min(x0 + kDvW, P);
+  const int zs = x0 >= 2 ? x0 - 2 : 0, ze = min(x0 + kDvW + 2, P);
+  const unsigned wb = (unsigned)(xe - x0) * 8u, zb = (unsigned)(ze - zs) * 8u;
+  const int zc = x0 + t - zs;
+  auto stage = [&](int b) { return dv_smem + (size_t)b * kDvStage; };
+  auto fld = [&](double *st, int f) { return st + 3 * kDvZW + f * kDvW; };
+  const int nd = kz - 1;
+  // down unit u (m = kz-1-u): zraw rows, s, fmz, pai, tetav at m; w, fmzf, tetavf at m+1
+  auto issue_down = [&](int u, int b) {
+    const int m = kz - 1 - u;
+    double *st = stage(b);
+    uint64_t *bar = &mbar[b];
+    fence_proxy_async();
+    mbar_expect_tx(bar, (filt ? 3u : 1u) * zb + 7u * wb);
+    const int o = (m - 1) * PS, ob = m * PS;
+    bulk_load(st, zraw + o + zs, zb, bar);
+    if (filt) {
+      bulk_load(st + kDvZW, zraw + o - P + zs, zb, bar);
+      bulk_load(st + 2 * kDvZW, zraw + o + P + zs, zb, bar);
     }
-    const double skp1 = (double)s[o + PS];
-    const double bw = relax_weight(sa.ibnd_cr, sa.hefc, c.nspgx, ij, k);
-    z = z + bw * dtrdz * sa.fmz_d[o] * (sk - skp1);
-    COL(zf, k) = z;
-    sk = skp1;
-  }
-
-  // elimination k = kz..2 (:634-656); wwkw(kz+1) = 0
-  double wnext = (double)w[ij + (size_t)kz * PS];  // w(kz+1) = -s(kz+1)
-  double wkp1 = 0.0;
-  double pai_k = (double)pai[ij + (size_t)(kz - 1) * PS];
-  double tet_k = tetav[ij + (size_t)(kz - 1) * PS];
-  double fmz_k = sa.fmz_d[ij + (size_t)(kz - 1) * PS];
-  #pragma unroll 4
-  for (int k = kz; k >= 2; --k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    const double pai_m = (double)pai[o - PS];
-    const double tet_m = tetav[o - PS];
-    const double fmz_m = sa.fmz_d[o - PS];
-    const double fmzf = sa.fmzf_d[o];
-    const double wold = (double)w[o];
-    const double tvf = tetavf[o] - wold * fmzf * dtrdz * (tet_m - tet_k);
-    tetavf[o] = tvf;
-    const double zrom1w = kCpd * tvf * fmzf;
-    double zwexpl = wold - zrom1w * dtrdz * (pai_m - pai_k) - kGrav * dts;
-    zwexpl = zwexpl + kRdrcv * zrom1w * dtrdz * (pai_m * COL(zf, k - 1) - pai_k * COL(zf, k));
-    const double ff = sa.ffilt[k - 1];
-    const double zu = zcs2 * fmz_m * zrom1w * pai_m + ff;
-    const double zd = zcs2 * fmz_k * zrom1w * pai_k + ff;
-    const double zrapp = 1.0 / (1.0 + zd + zu - zd * wkp1);
-    wnext = zrapp * (zwexpl + zd * wnext);
-    wkp1 = zrapp * zu;
-    COL(wp, k) = wnext;
-    COL(wk, k) = wkp1;
-    pai_k = pai_m; tet_k = tet_m; fmz_k = fmz_m;
-  }
-  // back substitution k = 2..kz (:660-664)
-  double wprev = (double)w[ij];  // w(1) = 0
-  COL(wp, 1) = wprev;
-  #pragma unroll 4
-  for (int k = 2; k <= kz; ++k) {
-    wprev = COL(wp, k) + COL(wk, k) * wprev;
-    COL(wp, k) = wprev;
-    w[ij + (size_t)(k - 1) * PS] = (R)wprev;
-  }
-  COL(wp, kz + 1) = (double)w[ij + (size_t)kz * PS];
-  // Exner function (:668-671)
-  #pragma unroll 4
-  for (int k = 1; k <= kz; ++k) {
-    const size_t o = ij + (size_t)(k - 1) * PS;
-    const double pk = pai[o];
-    pai[o] = pk * (1.0 - kRdrcv * (COL(zf, k) + (dtrdz * sa.fmz_d[o] *
-                                                 (COL(wp, k) - COL(wp, k + 1)))));
-  }
-  if (last) {
-    // complete s (:728-734)
-    #pragma unroll 4
-    for (int k = 2; k <= kz; ++k) {
-      const size_t o = ij + (size_t)(k - 1) * PS;
-      s[o] = (R)((COL(wp, k) + (double)s[o]) * sa.fmzf_d[o]);
+    bulk_load(fld(st, 0), s + o + x0, wb, bar);
+    bulk_load(fld(st, 1), fmz + o + x0, wb, bar);
+    bulk_load(fld(st, 2), pai + o + x0, wb, bar);
+    bulk_load(fld(st, 3), tetav + o + x0, wb, bar);
+    bulk_load(fld(st, 4), w + ob + x0, wb, bar);
+    bulk_load(fld(st, 5), fmzf + ob + x0, wb, bar);
+    bulk_load(fld(st, 6), tetavf + ob + x0, wb, bar);
+  };
+  // up unit v (m = v + 2): w(m), mul(m) (m <= kz); pai, zfs, fmz, s, fmzf at m-1
+  auto issue_up = [&](int v, int b) {
+    const int m = v + 2;
+    double *st = stage(b);
+    uint64_t *bar = &mbar[b];
+    fence_proxy_async();
+    mbar_expect_tx(bar, (m <= kz ? 7u : 6u) * wb);
+    const int o = (m - 1) * PS, op = (m - 2) * PS;
+    bulk_load(fld(st, 0), w + o + x0, wb, bar);
+    if (m <= kz) bulk_load(fld(st, 1), mul + o + x0, wb, bar);
+    bulk_load(fld(st, 2), pai + op + x0, wb, bar);
+    bulk_load(fld(st, 3), zfs + op + x0, wb, bar);
+    bulk_load(fld(st, 4), fmz + op + x0, wb, bar);
+    bulk_load(fld(st, 5), s + op + x0, wb, bar);
+    bulk_load(fld(st, 6), fmzf + op + x0, wb, bar);
+  };
+  auto bail = [&](int gnext, int gend) {
+    if (t == 0) {
+      atomicOr(&D.clk->fault, 1);
+      for (int q = gnext; q < gend && q < gnext + NS; ++q) mbar_wait_bounded(&mbar[q % NS], (unsigned)((q / NS) & 1));
     }
-    s[ij] = R(0);
-    s[ij + (size_t)kz * PS] = R(0);
+  };
+  if (t == 0) {
+    for (int q = 0; q < NS; ++q) mbar_init(&mbar[q], 1);
+    fence_mbar_init();
   }
-#undef COL
+  __syncthreads();
+  if (t == 0)
+    for (int u = 0; u < NS && u < nd; ++u) issue_down(u, u);
+  // filtered divergence plus the vertical part of level m (:531-543, :627-630)
+  auto zf_of = [&](int m, double z, double lap, double fz, double sm, double sm1) {
+    if (filt) z = z + sa.xknu[m - 1] * lap;
+    const double bw = relax_weight(sa.ibnd_cr, sa.hefc, c.nspgx, ij, m);
+    return z + bw * dtrdz * fz * (sm - sm1);
+  };
+  double wnext = 0.0, wkp1 = 0.0, zfk = 0.0, pai_k = 0.0, tet_k = 0.0, fmz_k = 0.0, s_k = 0.0;
+  if (act) {
+    const int o = (kz - 1) * PS + ij_off;
+    const double z = zraw[o];
+    const double lap = filt ? (zraw[o - 1] + zraw[o + 1] + zraw[o - P] + zraw[o + P] - 4.0 * z) : 0.0;
+    s_k = s[o];
+    fmz_k = fmz[o];
+    zfk = zf_of(kz, z, lap, fmz_k, s_k, s[kz * PS + ij_off]);
+    pai_k = pai[o];
+    tet_k = tetav[o];
+    wnext = w[kz * PS + ij_off];  // w(kz+1) = -s(kz+1)
+  }
+  for (int u = 0; u < nd; ++u) {
+    const int k = kz - u, m = k - 1;
+    const int b = u % NS;
+    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((u / NS) & 1));
+    const double *st = stage(b);
+    if (act) {
+      const int o = (k - 1) * PS + ij_off;
+      const double z = st[zc];
+      const double lap = filt ? (st[zc - 1] + st[zc + 1] + st[kDvZW + zc] + st[2 * kDvZW + zc] - 4.0 * z) : 0.0;
+      const double *f0 = st + 3 * kDvZW + t;
+      const double s_m = f0[0], fmz_m = f0[kDvW], pai_m = f0[2 * kDvW], tet_m = f0[3 * kDvW];
+      const double wold = f0[4 * kDvW], fmzf_k = f0[5 * kDvW], tvf0 = f0[6 * kDvW];
+      const double zf_m = zf_of(m, z, lap, fmz_m, s_m, s_k);
+      zfs[o] = zfk;
+      const double tvf = tvf0 - wold * fmzf_k * dtrdz * (tet_m - tet_k);
+      tetavf[o] = tvf;
+      const double zrom1w = kCpd * tvf * fmzf_k;
+      double zwexpl = wold - zrom1w * dtrdz * (pai_m - pai_k) - kGrav * dts;
+      zwexpl = zwexpl + kRdrcv * zrom1w * dtrdz * (pai_m * zf_m - pai_k * zfk);
+      const double ff = sa.ffilt[k - 1];
+      const double zu = zcs2 * fmz_m * zrom1w * pai_m + ff;
+      const double zd = zcs2 * fmz_k * zrom1w * pai_k + ff;
+      const double zrapp = 1.0 / (1.0 + zd + zu - zd * wkp1);
+      wnext = zrapp * (zwexpl + zd * wnext);
+      wkp1 = zrapp * zu;
+      w[o] = wnext;
+      mul[o] = wkp1;
+      zfk = zf_m;
+      pai_k = pai_m; tet_k = tet_m; fmz_k = fmz_m; s_k = s_m;
+    }
+    if (__syncthreads_or(!landed)) {
+      bail(u + 1, nd);
+      return;
+    }
+    if (t == 0 && u + NS < nd) issue_down(u + NS, b);
+  }
+  if (act) zfs[ij_off] = zfk;  // level 1
+  fence_proxy_async_global();
+  __syncthreads();
+  const int nu = kz;
+  if (t == 0)
+    for (int v = 0; v < NS && v < nu; ++v) issue_up(v, (nd + v) % NS);
+  // Exner (:668-671) of level m once w(m+1) is known, and s (:728-734)
+  auto exner = [&](int m, double wm, double wmp, double pk, double zf, double fz, double sm, double fzf) {
+    const int o = (m - 1) * PS + ij_off;
+    pai[o] = pk * (1.0 - kRdrcv * (zf + (dtrdz * fz * (wm - wmp))));
+    if (last && m >= 2) s[o] = (wm + sm) * fzf;
+  };
+  double wprev = act ? w[ij_off] : 0.0;  // w(1) = 0
+  for (int v = 0; v < nu; ++v) {
+    const int k = v + 2, gu = nd + v;
+    const int b = gu % NS;
+    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((gu / NS) & 1));
+    if (act) {
+      const double *f0 = stage(b) + 3 * kDvZW + t;
+      const double wel = f0[0];
+      const double cp = f0[2 * kDvW], czf = f0[3 * kDvW], cfz_ = f0[4 * kDvW], cs = f0[5 * kDvW],
+                   cfzf = f0[6 * kDvW];
+      if (k <= kz) {
+        const double wk = wel + f0[kDvW] * wprev;
+        w[(k - 1) * PS + ij_off] = wk;
+        exner(k - 1, wprev, wk, cp, czf, cfz_, cs, cfzf);
+        wprev = wk;
+      } else {
+        exner(kz, wprev, wel, cp, czf, cfz_, cs, cfzf);
+      }
+    }
+    if (__syncthreads_or(!landed)) {
+      bail(gu + 1, nd + nu);
+      return;
+    }
+    if (t == 0 && v + NS < nu) issue_up(v + NS, b);
+  }
+  if (last && act) {
+    s[ij_off] = 0.0;
+    s[kz * PS + ij_off] = 0.0;
+  }
 }
-
 constexpr int kSvStages = 4;   // levels in flight ahead of the one being solved
 constexpr int kSvW = 128;            // columns of a block (one row segment)
 constexpr int kSvZW = kSvW + 8;      // raw divergence rows with a 4-column halo each side
@@ -920,17 +1015,16 @@ template <class R>
 void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, bool last,
                             cudaStream_t s) {
   (void)uvoff;
-  const dim3 blk((unsigned)L.solve_x, (unsigned)L.solve_y);
-  const dim3 grd((unsigned)((L.jx - 3 + blk.x - 1) / blk.x), (unsigned)((L.iy - 3 + blk.y - 1) / blk.y),
-                 (unsigned)L.nmem);
-  const size_t cols = (size_t)3 * (L.kz + 2) * blk.x * blk.y;
+  // one block per 128-column row segment in both precisions (the solve
+  // launch shape of LaunchGeom is not used)
   if constexpr (sizeof(R) == sizeof(float)) {
-    // one block per 128-column row segment (the solve shape applies to FP64)
     const int tj = (L.jx - 1 + kSvW - 1) / kSvW;
     k_solve_mixed<R><<<dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem), kSvW,
                        (size_t)kSvStages * kSvStage * sizeof(float), s>>>(d, advoff, last ? 1 : 0);
   } else {
-    k_sound_solve<R><<<grd, blk, cols * sizeof(double), s>>>(d, advoff, last ? 1 : 0);
+    const int tj = (L.jx - 1 + kDvW - 1) / kDvW;
+    k_sound_solve<R><<<dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem), kDvW,
+                       (size_t)kDvStages * kDvStage * sizeof(double), s>>>(d, advoff, last ? 1 : 0);
   }
 }
 
