@@ -36,6 +36,50 @@ template <> struct FlowEps<double> {
   static __device__ __forceinline__ double num() { return (double)1.0e-30f; }
 };
 
+// x0 + m*(a*b - c*d + e*f) of the horizontal updates.  For FP64 the products
+// are fused explicitly (the second and third into fused multiply-adds), so the
+// rounding does not depend on how the compiler contracts the expression in
+// each tile instantiation: the tile shapes give bit-identical FP64 results.
+// FP32 leaves the contraction to the compiler.  rot: m = 1, no product.
+// chain: the rotated-pole form is x0 + a*b - c*d + e*f, left to right (the
+// zonal update), else x0 + (a*b - c*d + e*f) (the meridional one).
+template <class T>
+__device__ __forceinline__ T stencil_update(T x0, T m, bool rot, bool chain, T a, T b, T c, T d, T e,
+                                            T f) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (rot && chain) return __fma_rn(e, f, __fma_rn(-c, d, __fma_rn(a, b, x0)));
+    const T t = __fma_rn(e, f, __fma_rn(-c, d, __dmul_rn(a, b)));
+    return rot ? __dadd_rn(x0, t) : __fma_rn(m, t, x0);
+  } else {
+    const T z = e * f;
+    if (rot && chain) return x0 + a * b - c * d + z;
+    return rot ? x0 + (a * b - c * d + z) : x0 + m * (a * b - c * d + z);
+  }
+}
+
+// The upwind tests zamu >= 0 and zamu > 0.  For FP64 they are made on the
+// bit pattern by the integer pipe (each FP64 compare is an instruction of the
+// 1/64-rate FP64 pipe on GB300), with the comparisons' exact results for
+// -0, infinities and NaN; FP32 compares directly.
+template <class T>
+__device__ __forceinline__ bool nonneg(T x) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    const long long b = __double_as_longlong(x);
+    return (b >= 0 && b <= 0x7ff0000000000000LL) || b == (long long)0x8000000000000000ULL;
+  } else {
+    return x >= T(0);
+  }
+}
+template <class T>
+__device__ __forceinline__ bool positive(T x) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7ff0000000000000LL;
+  } else {
+    return x > T(0);
+  }
+}
+
 // WAF flux  hvel*((1+phi)*a + (1-phi)*c)  with  phi = is + zamu*b - is*b  and
 // the limiter  b = max(0, min(2, max(r, min(2r, 1))))  of  r = num/den
 // (local_flow_param, Main/mod_moloch.F90:1571-1590; the flux lines
@@ -50,9 +94,11 @@ template <> struct FlowEps<double> {
 // division.  FP32 takes the branch-free clamp; FP64 tests the regions of r in
 // turn (0, 1/2, 1, 2), which usually stops early - on GB300 each FP64 min, max
 // or compare is an instruction of the 1/64-rate FP64 pipe - and keeps the
-// reference's guard of denominators below minden exactly.
+// reference's guard of denominators below minden exactly.  is = +1 (up) or
+// -1 enters as a choice of constants and of den's sign (is*den exactly), not
+// as a multiplication.
 template <class T>
-__device__ __forceinline__ T waf_flux(T hvel, T is, T zamu, T a, T c, T num) {
+__device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) {
   const T den = c - a;
   T B;
   if constexpr (sizeof(T) == sizeof(float)) {
@@ -86,7 +132,18 @@ __device__ __forceinline__ T waf_flux(T hvel, T is, T zamu, T a, T c, T num) {
     else if (bq < ad + one_exp) B = num;                 // q < 2d
     else B = den + den;
   }
-  return hvel * ((a + c) - (is * den + (zamu - is) * B));
+  if constexpr (sizeof(T) == sizeof(double)) {
+    // is*den as a choice of den's sign (no FP64 multiply); the fused
+    // multiply-add and the final product are explicit, so that the compiler
+    // cannot fuse them into the caller's arithmetic differently in each tile
+    // instantiation (the tile shapes give bit-identical results)
+    const T sden = up ? den : -den;
+    const T zmi = zamu - (up ? T(1) : T(-1));
+    return __dmul_rn(hvel, (a + c) - __fma_rn(zmi, B, sden));
+  } else {
+    const T is = up ? T(1) : T(-1);
+    return hvel * ((a + c) - (is * den + (zamu - is) * B));
+  }
 }
 
 // The advected fields of a member, in the reference's order (tetav, pai,
@@ -200,15 +257,11 @@ __device__ __forceinline__ T vflux(T dtrdz, T skp, T cm1, T ck, T cp1, T cp2, in
   // interface k+1 between levels k and k+1; the upwind difference col(k1) -
   // col(k1p1) with the reference's clamps k1p1 = min(k+2, kz), k1 = max(k-1, 1)
   const T zamu = skp * dtrdz;
-  T is, num;
-  if (zamu >= T(0)) {
-    is = T(1);
-    num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
-  } else {
-    is = T(-1);
-    num = k >= 2 ? cm1 - ck : ck - ck;
-  }
-  return waf_flux<T>(T(0.5) * skp, is, zamu, cp1, ck, num);
+  const bool up = nonneg(zamu);
+  T num;
+  if (up) num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
+  else num = k >= 2 ? cm1 - ck : ck - ck;
+  return waf_flux<T>(T(0.5) * skp, up, zamu, cp1, ck, num);
 }
 template <class T>
 __device__ __forceinline__ T vupdate(T pk, T fb, T fa, T sk, T skp, T zu, T zd) {
@@ -271,8 +324,8 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     T f1kp;
     if (I) {
       const T zamu = skp1 * dtrdz;
-      const bool up = zamu >= T(0);
-      f1kp = waf_flux<T>(T(0.5) * skp1, up ? T(1) : T(-1), zamu, c0p1, c0k,
+      const bool up = nonneg(zamu);
+      f1kp = waf_flux<T>(T(0.5) * skp1, up, zamu, c0p1, c0k,
                          (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
     } else {
       f1kp = k <= kz - 1 ? vflux<T>(dtrdz, skp1, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
@@ -282,8 +335,8 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
       T f2n;
       if (I) {
         const T zamu = sm1 * dtrdz;
-        const bool up = zamu >= T(0);
-        f2n = waf_flux<T>(T(0.5) * sm1, up ? T(1) : T(-1), zamu, c1m1, c1m2,
+        const bool up = nonneg(zamu);
+        f2n = waf_flux<T>(T(0.5) * sm1, up, zamu, c1m1, c1m2,
                           (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
       } else {
         f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1k, k - 2, kz);
@@ -585,8 +638,8 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       ld_vec<T, V>(wC, &wt[tC][OFF + V * lane]);
 #pragma unroll
       for (int q = 0; q < V; ++q) {
-        const bool up = zmy[q] > T(0);
-        const T y = waf_flux<T>(vv[q], up ? T(1) : T(-1), zmy[q], wa[q], wzi[q],
+        const bool up = positive(zmy[q]);
+        const T y = waf_flux<T>(vv[q], up, zmy[q], wa[q], wzi[q],
                                 (up ? wa[q] : wB[q]) - (up ? wA[q] : wC[q]));
         x[q] = mv[q] ? y : T(0);  // zero outside the flux points
       }
@@ -600,8 +653,8 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
         ld_vec<T, V>(wC, &wt[eC][OFF + V * lane]);
 #pragma unroll
         for (int q = 0; q < V; ++q) {
-          const bool up = zmye[q] > T(0);
-          const T y = waf_flux<T>(vve[q], up ? T(1) : T(-1), zmye[q], xa[q], xc[q],
+          const bool up = positive(zmye[q]);
+          const T y = waf_flux<T>(vve[q], up, zmye[q], xa[q], xc[q],
                                   (up ? xa[q] : wB[q]) - (up ? wA[q] : wC[q]));
           x[q] = me[q] ? y : T(0);
         }
@@ -627,10 +680,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       ld_vec<T, V>(yn, &zp[wp + 1][V * lane]);
 #pragma unroll
       for (int q = 0; q < V; ++q) {
-        const T zdv = dvy[q] * ppk[q];
-        T x;
-        if (rot) x = wzi[q] + (ys[q] * zs[q] - yn[q] * zn[q] + zdv);
-        else x = wzi[q] + m2[q] * (ys[q] * zs[q] - yn[q] * zn[q] + zdv);
+        const T x = stencil_update<T>(wzi[q], m2[q], rot, false, ys[q], zs[q], yn[q], zn[q], dvy[q], ppk[q]);
         p0[q] = pv[q] ? x : T(0);
       }
     }
@@ -648,13 +698,13 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 #pragma unroll
     for (int q = 0; q < V; ++q) {
       const int j = jq[q];
-      const bool up = zmx[q] > T(0);
+      const bool up = positive(zmx[q]);
       const T a = p0at(q - 1), cq = p0at(q);
       // jhm1 = max(j-2, jmin) upwind; jh = min(j+1, jmax) downwind
       // upwind a - p0(jhm1), downwind p0(jh) - p0(jh-1): one subtraction of selected operands
       const T n1 = up ? a : (j == jx - 1 ? cq : p0at(q + 1));
       const T n2 = up ? (j == 2 ? a : p0at(q - 2)) : (j == jx - 1 ? a : cq);
-      const T x = waf_flux<T>(uu[q], up ? T(1) : T(-1), zmx[q], a, cq, n1 - n2);
+      const T x = waf_flux<T>(uu[q], up, zmx[q], a, cq, n1 - n2);
       zx[q] = xv[q] ? x : T(0);
     }
     T zxe[V];
@@ -663,10 +713,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     T res[V];
 #pragma unroll
     for (int q = 0; q < V; ++q) {
-      const T zdv = dvx[q] * ppk[q];
-      T x;
-      if (rot) x = p0[q] + zx[q] * zw[q] - zxe[q] * ze[q] + zdv;
-      else x = p0[q] + m2[q] * (zx[q] * zw[q] - zxe[q] * ze[q] + zdv);
+      const T x = stencil_update<T>(p0[q], m2[q], rot, true, zx[q], zw[q], zxe[q], ze[q], dvx[q], ppk[q]);
       res[q] = rv[q] ? x : ppk[q];
     }
     if (wall) {
@@ -813,15 +860,11 @@ __device__ __forceinline__ float vflux_inc(float dtrdz, float skp, float em1, fl
                                            float ekp2, float dzm1, float dzk, float dzp1, int k,
                                            int kz) {
   const float zamu = skp * dtrdz;
-  float is, num;
-  if (zamu >= 0.f) {
-    is = 1.f;
-    num = k + 2 <= kz ? (ekp1 - ekp2) - dzp1 : 0.f;
-  } else {
-    is = -1.f;
-    num = k >= 2 ? (em1 - ek) - dzm1 : 0.f;
-  }
-  return waf_flux<float>(0.5f * skp, is, zamu, dzk + ekp1, ek, num);
+  const bool up = zamu >= 0.f;
+  float num;
+  if (up) num = k + 2 <= kz ? (ekp1 - ekp2) - dzp1 : 0.f;
+  else num = k >= 2 ? (em1 - ek) - dzm1 : 0.f;
+  return waf_flux<float>(0.5f * skp, up, zamu, dzk + ekp1, ek, num);
 }
 // the cell update without the bottom/top constant parts; flb is the flux
 // through interface k (relative to cell k-1), fla the flux through k+1
@@ -1112,7 +1155,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
       float num;
       if (up) num = r >= 3 ? (zm1[q] - zm2[q]) + dym2[q] : (zm1[q] - zm1[q]) + 0.f;
       else num = r <= iy - 2 ? (zp1[q] - z0[q]) + dy0[q] : (z0[q] - zm1[q]) + dym1[q];
-      const float y = waf_flux<float>(0.5f * vvr[q], up ? 1.f : -1.f, zm[q], zm1[q], z0[q] + dym1[q], num);
+      const float y = waf_flux<float>(0.5f * vvr[q], up, zm[q], zm1[q], z0[q] + dym1[q], num);
       x[q] = ok[q] ? y : 0.f;
     }
   };
@@ -1227,7 +1270,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
       float num;
       if (up) num = j >= 3 ? (a - eyat(q - 2)) + dxat(q - 2) : (a - a) + 0.f;
       else num = j <= jx - 2 ? (eyat(q + 1) - cq) + dxat(q) : (cq - a) + dxat(q - 1);
-      const float y = waf_flux<float>(0.5f * uu[q], up ? 1.f : -1.f, zmx[q], a, cq + dxat(q - 1), num);
+      const float y = waf_flux<float>(0.5f * uu[q], up, zmx[q], a, cq + dxat(q - 1), num);
       fx[q] = xv[q] ? y : 0.f;
     }
     T fxe[V];
