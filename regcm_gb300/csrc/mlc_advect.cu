@@ -241,6 +241,11 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
     else if (k == kz) a = R(0.5) * (w[o + PS] + w[o]);
     else a = R(0.5625) * (w[o + PS] + w[o]) - R(0.0625) * (w[o + 2 * PS] + w[o - PS]);
     wx[o] = a;
+    if constexpr (sizeof(R) == sizeof(double)) {
+      // the vertical WAF update's factor s(k)*zu(k) - s(k+1)*zd(k), once for
+      // all fields (FP64 arithmetic is the FP64 path's bound)
+      D.vdiv[o] = __fma_rn(-D.s[o + PS], D.sa.zrfmd[o], __dmul_rn(D.s[o], D.sa.zrfmu[o]));
+    }
   }
 }
 
@@ -267,6 +272,12 @@ template <class T>
 __device__ __forceinline__ T vupdate(T pk, T fb, T fa, T sk, T skp, T zu, T zd) {
   const T zdv = (sk * zu - skp * zd) * pk;
   return pk - fb * zu + fa * zd + zdv;
+}
+// the same with the factor sk*zu - skp*zd given (FP64: from adv_prep), the
+// products fused explicitly
+template <class T>
+__device__ __forceinline__ T vupdate_f(T pk, T fb, T fa, T dv, T zu, T zd) {
+  return __fma_rn(dv, pk, __fma_rn(fa, zd, __fma_rn(-fb, zu, pk)));
 }
 
 // grid: x = column tiles along j times the fields (field fastest, so the
@@ -307,6 +318,10 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   T sm2 = T(0), sm1 = T(0), sk = T(sp[0]);
   T zum2 = T(0), zdm2 = T(0), zum1 = T(0), zdm1 = T(0);
   T f1k = T(0), f2m = T(0);
+  // FP64 member: the update's divergence factor, precomputed per level
+  constexpr bool kPre = sizeof(R) == sizeof(double) && sizeof(T) == sizeof(double);
+  const double *__restrict__ dvp = kPre ? D.vdiv + ij : nullptr;
+  T dvm2 = T(0), dvm1 = T(0), n_dv = kPre ? T(dvp[0]) : T(0);
   // the next level's loads, issued one level ahead
   T n_s = T(sp[PS]), n_c = src[2 * PS], n_zu = T(zup[0]), n_zd = T(zdp[0]);
   // level k; every bound check is known to hold inside the column
@@ -315,10 +330,12 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     constexpr bool I = decltype(interior)::value;
     const unsigned o = (unsigned)(k - 1) * PS;
     const T skp1 = n_s, c0p2 = (I || k + 2 <= kz) ? n_c : T(0), zuk = n_zu, zdk = n_zd;
+    const T dvk = n_dv;
     if (I || k < kz) {
       n_s = T(sp[o + 2 * PS]);
       n_zu = T(zup[o + PS]);
       n_zd = T(zdp[o + PS]);
+      if constexpr (kPre) n_dv = T(dvp[o + PS]);
       if (I || k + 3 <= kz) n_c = src[o + 3 * PS];
     }
     T f1kp;
@@ -330,7 +347,9 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     } else {
       f1kp = k <= kz - 1 ? vflux<T>(dtrdz, skp1, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
     }
-    const T c1k = vupdate<T>(c0k, f1k, f1kp, sk, skp1, zuk, zdk);
+    T c1k;
+    if constexpr (kPre) c1k = vupdate_f<T>(c0k, f1k, f1kp, dvk, zuk, zdk);
+    else c1k = vupdate<T>(c0k, f1k, f1kp, sk, skp1, zuk, zdk);
     if (I || k >= 3) {  // pass 2 at level m = k-2
       T f2n;
       if (I) {
@@ -341,13 +360,15 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
       } else {
         f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1k, k - 2, kz);
       }
-      dst[o - 2 * PS] = vupdate<T>(c1m2, f2m, f2n, sm2, sm1, zum2, zdm2);
+      if constexpr (kPre) dst[o - 2 * PS] = vupdate_f<T>(c1m2, f2m, f2n, dvm2, zum2, zdm2);
+      else dst[o - 2 * PS] = vupdate<T>(c1m2, f2m, f2n, sm2, sm1, zum2, zdm2);
       f2m = f2n;
     }
     c0m1 = c0k; c0k = c0p1; c0p1 = c0p2;
     c1m3 = c1m2; c1m2 = c1m1; c1m1 = c1k;
     sm2 = sm1; sm1 = sk; sk = skp1;
     zum2 = zum1; zdm2 = zdm1; zum1 = zuk; zdm1 = zdk;
+    dvm2 = dvm1; dvm1 = dvk;
     f1k = f1kp;
   };
   using edge = std::integral_constant<bool, false>;
@@ -360,8 +381,13 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   // pass 2 at levels kz-1 (flux through interface kz) and kz (none above)
   const unsigned ot = (unsigned)(kz - 1) * PS;
   const T f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
-  dst[ot - PS] = vupdate<T>(c1m2, f2m, f2n, sm2, sm1, zum2, zdm2);
-  dst[ot] = vupdate<T>(c1m1, f2n, T(0), sm1, sk, zum1, zdm1);
+  if constexpr (kPre) {
+    dst[ot - PS] = vupdate_f<T>(c1m2, f2m, f2n, dvm2, zum2, zdm2);
+    dst[ot] = vupdate_f<T>(c1m1, f2n, T(0), dvm1, zum1, zdm1);
+  } else {
+    dst[ot - PS] = vupdate<T>(c1m2, f2m, f2n, sm2, sm1, zum2, zdm2);
+    dst[ot] = vupdate<T>(c1m1, f2n, T(0), sm1, sk, zum1, zdm1);
+  }
 }
 
 // ---- lane vectors ---------------------------------------------------------

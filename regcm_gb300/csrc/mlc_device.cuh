@@ -149,6 +149,9 @@ struct Dom {
   DiagDev *diag;
   double *partials;
   R *spec;               // spectral nudging: per field and level, iy rows of km2 coefficients
+  // an FP64 member's s(k)*zrfmu(k) - s(k+1)*zrfmd(k) of the advection round
+  // (the vertical WAF update's divergence factor, the same for every field)
+  double *vdiv;
   // physics tendencies of the open step (null: zero), fields of the state's
   // layout: tten, uten, vten, then nqx qxten, then ntr chiten
   const R *tend;
