@@ -504,9 +504,35 @@ def run_uneven(args, rank, world):
         for n in ("tetav", "u", "v", "w"):
             errs[n].append(rel_l2(got[n], ref[n]))
         errs["qv"].append(rel_l2(got["qx"][..., 0], ref["qx"][..., 0]))
+    # per-kernel-group times of one eager step (after the state comparison:
+    # profiling advances the members) and the dominant group's roofline,
+    # its algorithmic bytes summed over the uneven members
+    KT = KernelTime
+    lib.mlc_profile_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(KT), C.c_int, C.POINTER(C.c_int)]
+    ktab = (KT * 32)()
+    nk = C.c_int()
+    abi.check(lib.mlc_profile_steps(batch._ctx, 1, ktab, 32, C.byref(nk)), "profile")
+    kernels = {ktab[i].name.decode(): (ktab[i].launches, ktab[i].ms) for i in range(nk.value)}
     batch.close()
     if rank != 0:
         return
+    import types
+    wbytes = 4 if prec == abi.MLC_PREC_MIXED else 8
+    dom_name = max(kernels, key=lambda k: kernels[k][1])
+    nl, kms = kernels[dom_name]
+    pk = peaks()
+    hbm_peak = float(pk.get("hbm_gbs", 6800.0))
+    roofline = {"kernel": dom_name, "bound": "hbm", "unit": "GB/s", "peak": hbm_peak,
+                "peak_source": "measured" if "hbm_gbs" in pk else "fallback", "traffic": None,
+                "share_of_step": kms / sum(v[1] for v in kernels.values()),
+                "kernels_ms_per_step": {k: v[1] for k, v in sorted(kernels.items(),
+                                                                     key=lambda kv: -kv[1][1])}}
+    per = [kernel_bytes(dom_name, types.SimpleNamespace(dims=dm, params=params),
+                        n_adv_fields(types.SimpleNamespace(dims=dm, params=params)), wbytes)
+           for dm in dims]
+    if all(b is not None for b in per):
+        ach = sum(per) / (kms / nl / 1000.0) / 1e9
+        roofline.update({"achieved": ach, "frac": ach / hbm_peak, "algorithmic_bytes": sum(per)})
     plain = plain_gp / plain_t
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -518,7 +544,7 @@ def run_uneven(args, rank, world):
                    "members": nmem, "points_total": sum(pts), "points_min": min(pts),
                    "points_max": max(pts), "precision": args.precision,
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2"},
-        "gpu_launches": launches * args.steps,
+        "roofline": roofline, "gpu_launches": launches * args.steps,
         "side_by_side": {"plain_fp64_one_domain_at_a_time": {"value": plain, "unit": UNIT,
                                                              "sample_domains": len(sample)},
                          "ratio_to_plain_fp64": value / world / plain, "autotune": tune},
