@@ -170,6 +170,14 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
   s.xkdamp = cv.take<double>(d.kz); s.xknu = cv.take<double>(d.kz); s.gzitak = cv.take<double>(d.kz + 1);
   s.rlat = cv.take<double>(d.iy);
   if (f64) {
+    s.dv_cu = cv.take<double>(F); s.dv_cv = cv.take<double>(F); s.dv_cf = cv.take<double>(F);
+    s.mo_du = cv.take<double>(F); s.mo_dv = cv.take<double>(F);
+    s.mo_gu = cv.take<double>(F); s.mo_gv = cv.take<double>(F);
+    s.mo_cu = cv.take<double>(P2); s.mo_cv = cv.take<double>(P2);
+  } else {
+    s.dv_cu = s.dv_cv = s.dv_cf = s.mo_du = s.mo_dv = s.mo_gu = s.mo_gv = s.mo_cu = s.mo_cv = nullptr;
+  }
+  if (f64) {
     s.gzitak_r = reinterpret_cast<const R *>(s.gzitak);
     s.gzitakh_r = reinterpret_cast<const R *>(s.gzitakh);
     s.xkdamp_r = reinterpret_cast<const R *>(s.xkdamp);
@@ -946,6 +954,72 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
     MLC_CHK(put1r<R>(x, s->fcx, a.fcx_r, p.nspgx));
   }
   if (s->rlat) MLC_CHK(put1(x, s->rlat, a.rlat, iy));
+  if (sizeof(R) == sizeof(double)) {
+    // the acoustic substep's constant factors, in the kernels' operand order
+    // (the same products the kernels formed every substep)
+    const bool rot = p.lrotllr != 0;
+    const double dtrdx = c.dtrdxs, dtrdy = c.dtrdxs, dxrdt = c.dxrdt, dts = c.dtsound;
+    const double zfz = kGrav * dts;
+    std::vector<double> xkd(kz), gkh(kz);
+    for (int k = 1; k <= kz; ++k) {
+      xkd[k - 1] = kNuMax * kDdamp * (1.0 / (k + 1.0) - 1.0 / (kz + 2.0));
+      gkh[k - 1] = gzita(s->zitah[k - 1], p.mo_ztop, p.mo_a0);
+    }
+    const size_t nu = (size_t)jx * (iy - 1), nv = (size_t)(jx - 1) * iy, nc = (size_t)(jx - 1) * (iy - 1);
+    std::vector<double> fu(nu * kz), fv(nv * kz), fc(nc * kz), gu(nu * kz), gv(nv * kz);
+    std::vector<double> cu(nu), cvv(nv);
+    for (int k = 0; k < kz; ++k)
+      for (int i = 0; i < iy - 1; ++i)
+        for (int j = 0; j < jx; ++j) {
+          const size_t e = (size_t)j + (size_t)i * jx, e3 = e + nu * k;
+          const double rmu = 1.0 / s->msfu[e];
+          fu[e3] = rot ? dtrdx * s->rfmzu[e3] : dtrdx * s->rfmzu[e3] * rmu;
+          gu[e3] = zfz * s->hx[e] * gkh[k];
+        }
+    for (int k = 0; k < kz; ++k)
+      for (int i = 0; i < iy; ++i)
+        for (int j = 0; j < jx - 1; ++j) {
+          const size_t e2 = (size_t)j + (size_t)i * jx;          // msfv (jx, iy)
+          const size_t e = (size_t)j + (size_t)i * (jx - 1), e3 = e + nv * k;
+          const double rmv = 1.0 / s->msfv[e2];
+          fv[e3] = dtrdy * s->rfmzv[e3] * rmv;
+          gv[e3] = zfz * s->hy[e] * gkh[k];
+        }
+    for (int k = 0; k < kz; ++k)
+      for (int i = 0; i < iy - 1; ++i)
+        for (int j = 0; j < jx - 1; ++j) {
+          const size_t e2 = (size_t)j + (size_t)i * jx;
+          const size_t e3 = (size_t)j + (size_t)i * (jx - 1) + nc * k;
+          const double mfac = rot ? s->msfx[e2] : s->msfx[e2] * s->msfx[e2];
+          fc[e3] = s->fmz[e3] * mfac;
+        }
+    MLC_CHK(put3<double>(x, g, fu.data(), W(a.dv_cu), jx, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, g, fv.data(), W(a.dv_cv), jx - 1, iy, kz, 0));
+    MLC_CHK(put3<double>(x, g, fc.data(), W(a.dv_cf), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, g, gu.data(), W(a.mo_gu), jx, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, g, gv.data(), W(a.mo_gv), jx - 1, iy, kz, 0));
+    MLC_TRY(cudaStreamSynchronize(x->stream));
+    for (int k = 0; k < kz; ++k)
+      for (int i = 0; i < iy - 1; ++i)
+        for (int j = 0; j < jx; ++j) {
+          const size_t e = (size_t)j + (size_t)i * jx;
+          fu[e + nu * k] = dxrdt * xkd[k] * s->msfu[e];
+        }
+    for (int k = 0; k < kz; ++k)
+      for (int i = 0; i < iy; ++i)
+        for (int j = 0; j < jx - 1; ++j) {
+          const size_t e2 = (size_t)j + (size_t)i * jx;
+          const size_t e = (size_t)j + (size_t)i * (jx - 1);
+          fv[e + nv * k] = rot ? dxrdt * xkd[k] : dxrdt * xkd[k] * s->msfv[e2];
+        }
+    for (size_t e = 0; e < nu; ++e) cu[e] = kOmega2 * std::sin(s->ulat[e] * kDegrad) * dts;
+    for (size_t e = 0; e < nv; ++e) cvv[e] = kOmega2 * std::sin(s->vlat[e] * kDegrad) * dts;
+    MLC_CHK(put3<double>(x, g, fu.data(), W(a.mo_du), jx, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, g, fv.data(), W(a.mo_dv), jx - 1, iy, kz, 0));
+    MLC_CHK(put3<double>(x, g, cu.data(), W(a.mo_cu), jx, iy - 1, 1, 0));
+    MLC_CHK(put3<double>(x, g, cvv.data(), W(a.mo_cv), jx - 1, iy, 1, 0));
+    MLC_TRY(cudaStreamSynchronize(x->stream));
+  }
   if (p.mo_spectral_nudge) {
     // lowpass_init (Main/mod_bdycod.F90:3844-3896, one process: njcross =
     // jx-1, nicross = iy-1) in FP64, rows of the modes k = 1..2km over

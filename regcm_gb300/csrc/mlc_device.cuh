@@ -69,6 +69,14 @@ struct Stat {
   // a mixed member's dz - dz_r (dz as the double-float {dz_r, dz_lo}, for the
   // mass budget); null for an FP64 member
   const R *dz_lo;
+  // an FP64 member's constant factors of the acoustic substep, formed once at
+  // bind time in the kernels' own operand order (null for a mixed member):
+  //   sound_div: dtrdx*rfmzu*rmu (u points; rotated: dtrdx*rfmzu),
+  //              dtrdy*rfmzv*rmv (v points), fmz*mfac (cross points)
+  //   sound_momentum: dxrdt*xkdamp(k)*msfu and dxrdt*xkdamp(k)*msfv
+  //              (rotated: dxrdt*xkdamp(k)), g*dts*hx*gzitakh(k) and
+  //              g*dts*hy*gzitakh(k) (3-D), coru*dts and corv*dts (2-D)
+  const double *dv_cu, *dv_cv, *dv_cf, *mo_du, *mo_dv, *mo_gu, *mo_gv, *mo_cu, *mo_cv;
   // spectral nudging: sine bases bvx (km2 rows of jx) and bvy (lm2 rows of
   // iy), the level weights cnudge (kz)
   const R *bvx, *bvy, *cnudge;

@@ -92,6 +92,13 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tile
   for (int k = q.k; k < q.k + kPtLevels && k <= kz; ++k) {
   const size_t o = (size_t)(k - 1) * g.PS;
   const R u0 = u[ij + o], u1 = u[ijE + o], v0 = v[ij + o], v1 = v[ijN + o];
+  if constexpr (sizeof(R) == sizeof(double)) {
+    // the constant factors formed at bind time: u*(dtrdx*rfmzu*rmu) for
+    // dtrdx*u*rfmzu*rmu (one FP64 product a flux instead of three)
+    const R zum = u0 * sa.dv_cu[ij + o], zup = u1 * sa.dv_cu[ijE + o];
+    const R zvm = v0 * sa.dv_cv[ij + o], zvp = v1 * sa.dv_cv[ijN + o];
+    zdiv2[ij + o] = sa.dv_cf[ij + o] * ((zup - zum) + (zvp - zvm));
+  } else {
   R zum, zup;
   if (c.lrotllr) {
     zum = dtrdx * u0 * sa.rfmzu[ij + o];
@@ -103,6 +110,7 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tile
   const R zvm = dtrdy * v0 * sa.rfmzv[ij + o] * rmv0;
   const R zvp = dtrdy * v1 * sa.rfmzv[ijN + o] * rmv1;
   zdiv2[ij + o] = sa.fmz[ij + o] * mfac * ((zup - zum) + (zvp - zvm));
+  }
   if (!interior) continue;
   if (k >= 2) {
     const size_t om = o - g.PS;  // level k-1
@@ -666,14 +674,25 @@ __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int
     if (has_u) {
       R un = u_in[o];
       if (upd_u) {
+        // FP64: the constant products dxrdt*xkdamp*msfu, g*dts*hx*gzitakh and
+        // coru*dts come from bind time (same operands, same order)
         if (c.divdamp) {
-          const R xdam = dxrdt * sa.xkdamp_r[k - 1] * mu;
+          R xdam;
+          if constexpr (mixed) xdam = dxrdt * sa.xkdamp_r[k - 1] * mu;
+          else xdam = sa.mo_du[o];
           un = un + xdam * (zraw[o] - zraw[o - W]);
         }
         const R zrom1u = halfcp * tsum(o - W, o);
-        const R zcor1u = cor_u * dts * v_in[o];
+        R zcor1u, zg;
+        if constexpr (mixed) {
+          zcor1u = cor_u * dts * v_in[o];
+          zg = zfz * hxk * gk;
+        } else {
+          zcor1u = sa.mo_cu[ij] * v_in[o];
+          zg = sa.mo_gu[o];
+        }
         const R bw = bweight(sa.ibnd_ud, ij, k);
-        un = un + bw * (zcor1u - zfz * hxk * gk - zcx * zrom1u * pdif(o, o - W));
+        un = un + bw * (zcor1u - zg - zcx * zrom1u * pdif(o, o - W));
       }
       u_out[o] = un;
     }
@@ -681,13 +700,22 @@ __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int
       R vn = v_in[o];
       if (upd_v) {
         if (c.divdamp) {
-          const R xdam = c.lrotllr ? dxrdt * sa.xkdamp_r[k - 1] : dxrdt * sa.xkdamp_r[k - 1] * mv;
+          R xdam;
+          if constexpr (mixed) xdam = c.lrotllr ? dxrdt * sa.xkdamp_r[k - 1] : dxrdt * sa.xkdamp_r[k - 1] * mv;
+          else xdam = sa.mo_dv[o];
           vn = vn + xdam * (zraw[o] - zraw[o - S]);
         }
         const R zrom1v = halfcp * tsum(o - S, o);
-        const R zcor1v = cor_v * dts * u_in[o];
+        R zcor1v, zg;
+        if constexpr (mixed) {
+          zcor1v = cor_v * dts * u_in[o];
+          zg = zfz * hyk * gk;
+        } else {
+          zcor1v = sa.mo_cv[ij] * u_in[o];
+          zg = sa.mo_gv[o];
+        }
         const R bw = bweight(sa.ibnd_vd, ij, k);
-        vn = vn + bw * (-zcor1v - zfz * hyk * gk - zcy * zrom1v * pdif(o, o - S));
+        vn = vn + bw * (-zcor1v - zg - zcy * zrom1v * pdif(o, o - S));
       }
       v_out[o] = vn;
     }
