@@ -156,8 +156,8 @@ MEASURED_TRAFFIC_PER_POINT = {("adv_horizontal", "fp64", 10): 733.6e6 / (256 * 2
 # What limits the dominant kernel when it is not HBM, from the same ncu captures.
 MEASURED_LIMITER = {
     ("adv_horizontal", "fp64"): {
-        "pipe": "fp64", "active": 0.837,
-        "source": "ncu sm__inst_executed_pipe_fp64, profiles/adv_horizontal_fp64_moist256_full.md"},
+        "pipe": "fp64", "active": 0.85,
+        "source": "ncu sm__inst_executed_pipe_fp64, profiles/kernels_fp64_mixed_moist256.md"},
     ("sound_solve", "mixed"): {
         "stall": "block barrier (one a level, freeing a copy stage)", "warps_active": 0.21,
         "source": "ncu, profiles/solve_mixed_bulk_moist256_full.md"},
