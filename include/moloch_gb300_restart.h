@@ -58,7 +58,8 @@ int mlc_sav_read(const char *path, const mlc_dims *d, const mlc_sav_fields *f, c
  * before it reads them). */
 int mlc_sav_restart_state(const mlc_dims *d, const mlc_sav_fields *f, const mlc_state_ptrs *st);
 
-/* Snapshot member m of a context (its state on the device) into a SAV file. */
+/* Snapshot member m of a context (its state on the device) into a SAV file;
+ * MLC_ERR_STATE inside a step split at the physics. */
 int mlc_member_write_sav(mlc_ctx *ctx, int m, const char *path, const char *idatex,
                          const char *calendar);
 

@@ -1535,6 +1535,7 @@ int mlc_step_finish(mlc_ctx *x, mlc_diag *out) {
 int mlc_member_write_sav(mlc_ctx *x, int m, const char *path, const char *idatex,
                          const char *calendar) {
   if (!member_ok(x, m) || !path) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;  // a restart holds a whole step's state
   const mlc_dims d = x->mem[m].dims;
   const size_t jx = d.jx, iy = d.iy, kz = d.kz, c3 = (jx - 1) * (iy - 1) * kz;
   std::vector<double> u(jx * (iy - 1) * kz), v((jx - 1) * iy * kz), w((jx - 1) * (iy - 1) * (kz + 1));
