@@ -72,3 +72,42 @@ def test_footprint_grows_with_domain():
     b = lib.mlc_footprint_bytes(C.byref(abi.mlc_dims(513, 513, 41, 5, 0)), abi.MLC_PREC_FP64)
     c = lib.mlc_footprint_bytes(C.byref(abi.mlc_dims(513, 513, 41, 5, 0)), abi.MLC_PREC_MIXED)
     assert 0 < a < b and c < b
+
+
+def test_struct_layouts_match_the_headers(tmp_path):
+    """Every ctypes structure of the bindings has the size and field offsets
+    the C compiler gives the header's structure (guards against drift)."""
+    import ctypes as C
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = [abi.mlc_dims, abi.mlc_params, abi.mlc_static_ptrs, abi.mlc_state_ptrs,
+               abi.mlc_bdy_ptrs, abi.mlc_diag, abi.mlc_tune_report, abi.mlc_tend_ptrs,
+               abi.mlc_sav_fields]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "moloch_gb300.h"',
+             '#include "moloch_gb300_setup.h"', '#include "moloch_gb300_restart.h"',
+             'int main(void) {']
+    for st in structs:
+        n = st.__name__
+        lines.append(f'  printf("{n} size %zu\\n", sizeof({n}));')
+        for f, _ in st._fields_:
+            lines.append(f'  printf("{n} {f} %zu\\n", offsetof({n}, {f}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = Path(__file__).resolve().parent.parent / "include"
+    subprocess.run([cc, "-std=c99", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = {}
+    for line in out.splitlines():
+        a, b, v = line.split()
+        got[(a, b)] = int(v)
+    for st in structs:
+        n = st.__name__
+        assert got[(n, "size")] == C.sizeof(st), n
+        for f, _ in st._fields_:
+            assert got[(n, f)] == getattr(st, f).offset, (n, f)
