@@ -111,3 +111,45 @@ def test_struct_layouts_match_the_headers(tmp_path):
         assert got[(n, "size")] == C.sizeof(st), n
         for f, _ in st._fields_:
             assert got[(n, f)] == getattr(st, f).offset, (n, f)
+
+
+def test_fortran_shim_types_follow_the_headers():
+    """The bind(c) derived types of the Fortran shim list the same fields, in
+    the same order and of matching kinds, as the ctypes structures (the shim
+    is not compiled here: no Fortran compiler)."""
+    import ctypes as C
+
+    src = (Path(__file__).resolve().parent.parent / "regcm_gb300" / "fortran" /
+           "mod_moloch_gb300.F90").read_text()
+    kinds = {"real(c_double)": "d", "integer(c_int32_t)": "i", "type(c_ptr)": "p"}
+    types = {}
+    for m in re.finditer(r"type, bind\(c\) :: (\w+)\n(.*?)end type", src, re.S):
+        fields = []
+        for line in m.group(2).splitlines():
+            line = line.strip()
+            if not line:
+                continue
+            decl, names = line.split("::")
+            k = kinds[decl.strip()]
+            for nm in names.split(","):
+                nm = nm.strip()
+                cnt = 1
+                mm = re.match(r"(\w+)\((\d+)\)", nm)
+                if mm:
+                    nm, cnt = mm.group(1), int(mm.group(2))
+                fields.append((nm, k, cnt))
+        types[m.group(1)] = fields
+
+    def kind_of(t):
+        if isinstance(t, type) and issubclass(t, C.Array):
+            return kind_of(t._type_)[0], t._length_
+        if t is C.c_double:
+            return "d", 1
+        if t in (C.c_int32, C.c_int):
+            return "i", 1
+        return "p", 1
+
+    for st in (abi.mlc_dims, abi.mlc_params, abi.mlc_static_ptrs, abi.mlc_state_ptrs,
+               abi.mlc_bdy_ptrs, abi.mlc_diag, abi.mlc_tend_ptrs):
+        want = [(n,) + kind_of(t) for n, t in st._fields_]
+        assert types[st.__name__] == want, st.__name__
