@@ -1,6 +1,7 @@
 """SAV restart files without a GPU: the netCDF classic writer and reader of
 the library (mlc_sav_write / mlc_sav_read) checked against scipy's
-independent netCDF-3 implementation in both directions, their error paths,
+independent netCDF-3 implementation in both directions (and a CDF-5 file
+written by hand from the format's definition), their error paths,
 and the restart state (Main/mod_init.F90:421-450,941-960) against the
 oracle's restatement.
 """
@@ -137,3 +138,64 @@ def test_restart_state_matches_oracle():
     # the diagnostics follow from t, pai and qv alone
     assert np.allclose(a["tvirt"], sav["t"] * (1 + 0.6077 * sav["qx"][..., 0]), rtol=1e-4)
     assert not np.any(a["ux"]) and not np.any(a["vx"])
+
+
+def _cdf5_bytes(dims, atts, vars_):
+    """A netCDF CDF-5 (64-bit data) file written by hand: header of 64-bit
+    counts and lengths, then each variable's big-endian values at its offset."""
+    import struct
+    u32 = lambda v: struct.pack(">I", v)
+    u64 = lambda v: struct.pack(">Q", v)
+
+    def name(s):
+        b = s.encode()
+        return u64(len(b)) + b + b"\0" * ((4 - len(b) % 4) % 4)
+
+    def header(begins):
+        h = b"CDF\x05" + u64(0)
+        h += u32(10) + u64(len(dims))
+        for n, ln in dims:
+            h += name(n) + u64(ln)
+        h += u32(12) + u64(len(atts))
+        for n, txt in atts:
+            b = txt.encode()
+            h += name(n) + u32(2) + u64(len(b)) + b + b"\0" * ((4 - len(b) % 4) % 4)
+        h += u32(11) + u64(len(vars_))
+        for (n, dimids, data), beg in zip(vars_, begins):
+            h += name(n) + u64(len(dimids)) + b"".join(u64(d) for d in dimids)
+            h += u32(0) + u64(0) + u32(6) + u64(data.size * 8) + u64(beg)
+        return h
+
+    size = len(header([0] * len(vars_)))
+    begins, off = [], size
+    for _, _, data in vars_:
+        begins.append(off)
+        off += data.size * 8
+    out = header(begins)
+    for _, _, data in vars_:
+        out += np.asarray(data, dtype=">f8").tobytes()
+    return out
+
+
+def test_cdf5_file_reads_in_library(tmp_path):
+    """A CDF-5 file (RegCM built with NETCDF_CDF5, or a variable above 4 GiB)
+    reads like the classic formats."""
+    c = small()
+    sav = random_sav(c, seed=2)
+    d = c.dims
+    names = ["jcross", "icross", "jdot", "idot", "khalf", "kfull", "nqx", "ntr"]
+    lens = [d.jx - 1, d.iy - 1, d.jx, d.iy, d.kz, d.kz + 1, d.nqx, d.ntr]
+    did = {n: q for q, n in enumerate(names)}
+    vars_ = []
+    for v, fdims in VARS.items():
+        # Fortran order in memory = netCDF dimensions listed slowest first
+        vars_.append((v, [did[n] for n in reversed(fdims)], sav[KEYS[v]].ravel(order="F")))
+    path = tmp_path / "SAV.cdf5.nc"
+    path.write_bytes(_cdf5_bytes(list(zip(names, lens)), [("idatex", "2001020300")], vars_))
+    got = c.empty_sav()
+    buf = C.create_string_buffer(16)
+    assert abi.load().mlc_sav_read(str(path).encode(), C.byref(d), C.byref(c.sav_ptrs_of(got)),
+                                   buf, 16) == 0
+    assert buf.value == b"2001020300"
+    for n, a in sav.items():
+        assert np.array_equal(got[n], a), n
