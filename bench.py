@@ -13,12 +13,19 @@ Our arm prints one JSON line with
   e2e        the same metric through the C ABI with host buffers: per step
              upload of the prognostic inputs from pinned memory, the step,
              download of the full state,
-  roofline   the dominant kernel's algorithmic bytes / its average launch time
-             against the measured HBM copy bandwidth, plus ncu-style context,
+  roofline   the dominant kernel against what bounds it: in FP64 the FP64
+             pipe (algorithmic FP64 operations per launch / its average launch
+             time, against the FP64 multiply-add rate measured in the same run
+             by mlc_fp64_peak), with its HBM figures beside; in mixed
+             precision HBM (algorithmic bytes / launch time against the
+             measured copy bandwidth),
   cpu_baseline  the CPU oracle (FP64 C++ restatement of the reference, OpenMP
-             on all host cores) timed on a bounded sample of the same domain.
+             on all host cores, and on one core) timed on a bounded sample of
+             the same domain.
 `--impl reference` times that CPU implementation alone (the reference's own
-Fortran cannot be built here: no Fortran compiler, MPI or netCDF).
+Fortran cannot be built here: no Fortran compiler, MPI or netCDF).  Its input
+is built through the oracle's own setup routines, so that arm never loads the
+GPU library.
 
 Multi-GPU: replicas only (each rank advances its own domain; no data-path
 collective); value = all ranks' gp-steps / the slowest rank's time.
@@ -146,22 +153,62 @@ def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None
     return None if by is None else float(by)
 
 
-# DRAM bytes per point of a launch, measured by ncu on a smaller case of the same
-# kernel and precision (moist 256x256x41, 10 advected fields:
-# profiles/adv_horizontal_fp64_moist256_full.md, 733.6 MB;
-# profiles/solve_mixed_bulk_moist256_full.md, k_solve_mixed 204.0 MB); scaled to the
-# bench case by its points.  Keyed by (kernel group, precision, advected fields).
-MEASURED_TRAFFIC_PER_POINT = {("adv_horizontal", "fp64", 10): 733.6e6 / (256 * 256 * 41),
-                              ("sound_solve", "mixed", 10): 204.0e6 / (256 * 256 * 41)}
-# What limits the dominant kernel when it is not HBM, from the same ncu captures.
-MEASURED_LIMITER = {
-    ("adv_horizontal", "fp64"): {
-        "pipe": "fp64", "active": 0.85,
-        "source": "ncu sm__inst_executed_pipe_fp64, profiles/kernels_fp64_mixed_moist256.md"},
-    ("sound_solve", "mixed"): {
-        "stall": "block barrier (one a level, freeing a copy stage)", "warps_active": 0.21,
-        "source": "ncu, profiles/solve_mixed_bulk_moist256_full.md"},
+# DRAM bytes per point of a launch (dram__bytes_read.sum + dram__bytes_write.sum)
+# from one ncu capture of the same kernel and precision on the quarter-size
+# case (moist 256x256x41, 10 advected fields), scaled to the bench case by its
+# points.  These are constants from that capture, not measured by this run:
+# the line prints them with that label and the kernel build they were taken
+# on.  Keyed by (kernel group, precision, advected fields).
+CAPTURED_TRAFFIC_PER_POINT = {
+    ("adv_horizontal", "fp64", 10): (733.6e6 / (256 * 256 * 41), "41cf599"),
+    ("sound_solve", "mixed", 10): (204.0e6 / (256 * 256 * 41), "a05c4c8"),
 }
+# What limits the dominant kernel besides its roofline, from the same captures.
+CAPTURED_LIMITER = {
+    ("adv_horizontal", "fp64"): {
+        "pipe": "fp64", "active": 0.85, "counter": "sm__inst_executed_pipe_fp64"},
+    ("sound_solve", "mixed"): {
+        "stall": "block barrier (one a level, freeing a copy stage)", "warps_active": 0.21},
+}
+
+
+def kernel_fp64_ops(name: str, case, nadv_fields: int) -> float | None:
+    """Algorithmic FP64 operations of one launch of an FP64 member's kernel
+    group: the arithmetic the reference performs for the same results,
+    counted from Main/mod_moloch.F90 with each add, multiply, divide, min
+    and max one operation (a multiply-add is two), and the factors that do
+    not depend on the advected field counted once per point.
+
+      adv_horizontal  (wafone :949-1040, per direction) limiter flux of a
+                      field: 2 differences, r = num/den, 2r, 4 min/max,
+                      zphi (2 products, 2 sums), 1 +- zphi, the two products,
+                      their sum and the product by 0.5 v = 18; update of p0
+                      or pp: zdv's product by pp, the flux terms (2 products,
+                      2 sums), mx2 * (...) and the sum = 7.  Field-independent
+                      per point and direction: zamu (2), 0.5 v (1), zrfmn/s
+                      (4), zdv's factor (5) = 12.  Both directions:
+                      50 F + 24 per point.
+      adv_vertical    (:862-922, do_vadvtwice) per pass and field: the same
+                      flux (18) and update (zdv's product, 2 products, 3
+                      sums = 6); field-independent: zamu (1), 0.5 s (1),
+                      zrfmu/zrfmd (4), zdv's factor (3) = 9.  Two passes:
+                      48 F + 18 per point.
+      sound_solve     (:627-671) per interior point: tetavf (5), zrom1w (2),
+                      zwexpl (13), zu/zd (8), zrapp (5, one divide), w and
+                      wwkw (4), back substitution (2), Exner update (7),
+                      filtered divergence (5-point Laplacian, 7), its
+                      vertical term (5) = 58.
+    """
+    d = case.dims
+    pts = (d.jx - 1) * (d.iy - 1) * d.kz
+    inner = (d.jx - 3) * (d.iy - 3) * d.kz
+    f = nadv_fields
+    ops = {
+        "adv_horizontal": (50 * f + 24) * pts,
+        "adv_vertical": (48 * f + 18) * pts,
+        "sound_solve": 58 * inner,
+    }.get(name)
+    return None if ops is None else float(ops)
 
 
 def n_adv_fields(case) -> int:
@@ -169,17 +216,24 @@ def n_adv_fields(case) -> int:
     return 6 + (d.nqx - 1 if p.ipptls > 0 else 0) + d.ntr
 
 
-def make_case(args, rank=0):
+def make_case(args, rank=0, setup=None):
     from regcm_gb300 import abi
     from regcm_gb300 import case as cs
     prec = abi.MLC_PREC_MIXED if args.precision == "mixed" else abi.MLC_PREC_FP64
     if args.config == "c1":
         n = args.size or 512
-        return cs.config1(nx=n, ny=n, seed=1 + rank, precision=prec)
+        return cs.config1(nx=n, ny=n, seed=1 + rank, precision=prec, setup=setup)
     if args.config == "c0":
         n = args.size or 64
-        return cs.config0(nx=n, ny=n, seed=rank, precision=prec)
+        return cs.config0(nx=n, ny=n, seed=rank, precision=prec, setup=setup)
     raise SystemExit(f"unknown config {args.config}")
+
+
+def config_of(args, world, points):
+    """The workload description both arms print."""
+    return {"workload": workload_name(args), "points_per_domain": points,
+            "precision": args.precision, "parallelism": f"replicas{world}",
+            "l2": "inputs larger than L2 (state > 1 GB)"}
 
 
 def workload_name(args):
@@ -191,9 +245,11 @@ def workload_name(args):
 
 
 # ---- CPU oracle timing -------------------------------------------------------
-def time_oracle(case, steps: int, warmup: int = 1, budget_s: float = 30.0):
-    """gp-steps/s of the CPU oracle on `case` (all host threads)."""
-    from oracle.oracle import Oracle
+def time_oracle(case, steps: int, warmup: int = 1, budget_s: float = 30.0, threads: int = 0):
+    """gp-steps/s of the CPU oracle on `case` (`threads` OpenMP threads; 0 =
+    every host thread this process may use)."""
+    from oracle.oracle import Oracle, set_threads
+    set_threads(threads or cpu_threads())
     o = Oracle(case)
     t0 = time.perf_counter()
     for _ in range(warmup):
@@ -217,18 +273,23 @@ def cpu_threads():
 
 # ---- the reference arm -------------------------------------------------------
 def run_reference(args, rank, world):
+    """The CPU oracle alone on the same workload.  The domain is built by the
+    oracle's restatement of the setup routines (bit-identical to the
+    library's, tests/test_setup_parity.py), so this arm never maps the GPU
+    library."""
     if rank != 0:
         return
-    os.environ.setdefault("OMP_NUM_THREADS", str(cpu_threads()))
-    case = make_case(args)
+    from oracle.oracle import OracleSetup
+    threads = cpu_threads()
+    case = make_case(args, setup=OracleSetup())
     value, n, dt = time_oracle(case, args.steps, warmup=max(1, min(args.warmup, 2)),
-                               budget_s=150.0)
+                               budget_s=150.0, threads=threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": n, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / n,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": workload_name(args), "l2": "inputs larger than L2"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+        "data": "synthetic", "config": config_of(args, world, case.points),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
                          "kind": "port",
                          "sample": f"{n} full steps of the {workload_name(args)} domain "
                                    "(CPU oracle: C++ FP64 restatement of Main/mod_moloch.F90; the "
@@ -326,19 +387,20 @@ def run_ours(args, rank, world):
         return
     cpu = None
     if world == 1 and not args.no_cpu:
-        os.environ.setdefault("OMP_NUM_THREADS", str(cpu_threads()))
-        cv, n, dt = time_oracle(case, steps=5, warmup=1, budget_s=20.0)
-        cpu = {"value": cv, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
-               "kind": "port",
-               "sample": f"{n} full steps of the same domain on the CPU oracle (C++ FP64, OpenMP)"}
+        threads = cpu_threads()
+        cv, n, dt = time_oracle(case, steps=5, warmup=1, budget_s=20.0, threads=threads)
+        c1, n1, dt1 = time_oracle(case, steps=1, warmup=0, budget_s=1.0, threads=1)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} full steps of the same domain on the CPU oracle (C++ FP64, OpenMP)",
+               "single_core": {"value": c1, "unit": UNIT, "cores": 1,
+                               "sample": f"{n1} full step of the same domain, one thread",
+                               "seconds": dt1}}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": workload_name(args), "points_per_domain": pts,
-                   "precision": args.precision, "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2 (state > 1 GB)"},
+        "config": config_of(args, world, pts),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "side_by_side": side,
         "gpu_launches": launches * args.steps, "clocks": clk.summary(),
         "diag": {"ps_min": diag.ps_min, "ps_max": diag.ps_max, "drymass": diag.drymass},
@@ -627,11 +689,30 @@ class KernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int32), ("ms", C.c_double)]
 
 
+_FP64_PEAK = None
+
+
+def fp64_peak(lib) -> float:
+    """FP64 multiply-add throughput of this GPU in FLOP/s, measured once per
+    run by the library's probe (mlc_fp64_peak: independent FMA chains on
+    every SM, best of 5 launches)."""
+    global _FP64_PEAK
+    if _FP64_PEAK is None:
+        v = C.c_double()
+        from regcm_gb300 import abi
+        abi.check(lib.mlc_fp64_peak(5, C.byref(v)), "mlc_fp64_peak")
+        _FP64_PEAK = v.value
+    return _FP64_PEAK
+
+
 def kernel_roofline(lib, ctx, case, precision):
     """Per-kernel-group device times of two eager steps (CUDA events around
-    each group on the library stream) and the roofline of the dominant group:
-    its algorithmic bytes per launch over its mean launch time, against the
-    measured HBM copy bandwidth."""
+    each group on the library stream) and the roofline of the dominant group.
+    Mixed precision: its algorithmic bytes per launch over its mean launch
+    time, against the measured HBM copy bandwidth.  FP64: its algorithmic
+    FP64 operations per launch over the mean launch time, against the FP64
+    rate measured in this run (the FP64 kernels are FP64-pipe bound on
+    GB300); the HBM figures follow in `hbm`."""
     lib.mlc_profile_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(KernelTime), C.c_int,
                                       C.POINTER(C.c_int)]
     ktab = (KernelTime * 32)()
@@ -645,24 +726,41 @@ def kernel_roofline(lib, ctx, case, precision):
     dom_name = max(kernels, key=lambda k: kernels[k][1])
     pk = peaks()
     hbm_peak = float(pk.get("hbm_gbs", 6800.0))
+    hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback"
     bytes_per = kernel_bytes(dom_name, case, nf, wbytes)
     nl, kms = kernels[dom_name]
-    roofline = {
-        "kernel": dom_name, "bound": "hbm", "unit": "GB/s",
-        "peak": hbm_peak, "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
-        "share_of_step": kms / total_k,
-        "traffic": None,
-    }
-    tpp = MEASURED_TRAFFIC_PER_POINT.get((dom_name, precision, nf))
-    if tpp:
-        roofline["traffic"] = tpp * case.points
-        roofline["traffic_source"] = "ncu on 256x256x41, scaled by points"
-    lim = MEASURED_LIMITER.get((dom_name, precision))
-    if lim:
-        roofline["limiter"] = lim
+    t_launch = kms / nl / 1000.0
+    hbm = {"unit": "GB/s", "peak": hbm_peak, "peak_source": hbm_src}
     if bytes_per:
-        ach = bytes_per / (kms / nl / 1000.0) / 1e9
-        roofline.update({"achieved": ach, "frac": ach / hbm_peak, "algorithmic_bytes": bytes_per})
+        ach = bytes_per / t_launch / 1e9
+        hbm.update({"achieved": ach, "frac": ach / hbm_peak, "algorithmic_bytes": bytes_per})
+    traffic = None
+    cap = CAPTURED_TRAFFIC_PER_POINT.get((dom_name, precision, nf))
+    if cap:
+        traffic = cap[0] * case.points
+    ops = kernel_fp64_ops(dom_name, case, nf) if precision == "fp64" else None
+    if ops:
+        peak = fp64_peak(lib) / 1e12
+        ach = ops / t_launch / 1e12
+        roofline = {"kernel": dom_name, "bound": "fp64", "unit": "TFLOP/s", "achieved": ach,
+                    "peak": peak,
+                    "peak_source": "measured in this run (mlc_fp64_peak, FP64 FMA chains)",
+                    "frac": ach / peak, "algorithmic_fp64_ops": ops, "traffic": traffic,
+                    "hbm": hbm}
+    else:
+        roofline = {"kernel": dom_name, "bound": "hbm", "unit": "GB/s", "peak": hbm_peak,
+                    "peak_source": hbm_src, "traffic": traffic}
+        if "achieved" in hbm:
+            roofline.update({"achieved": hbm["achieved"], "frac": hbm["frac"],
+                             "algorithmic_bytes": bytes_per})
+    roofline["share_of_step"] = kms / total_k
+    if cap:
+        roofline["traffic_source"] = (f"constant: ncu DRAM bytes of this kernel on moist "
+                                      f"256x256x41 at build {cap[1]}, scaled by points; "
+                                      "not measured by this run")
+    lim = CAPTURED_LIMITER.get((dom_name, precision))
+    if lim:
+        roofline["limiter"] = dict(lim, source="constant from the same ncu capture")
     roofline["kernels_ms_per_step"] = {k: v[1] / 2.0 for k, v in sorted(
         kernels.items(), key=lambda kv: -kv[1][1])}
     return roofline

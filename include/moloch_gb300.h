@@ -332,6 +332,12 @@ int mlc_launches_per_step(const mlc_ctx *ctx);
 /* Record steps into CUDA graphs (default 1) or launch them one by one (0). */
 int mlc_set_graphs(mlc_ctx *ctx, int on);
 
+/* FP64 throughput of the current device (no counterpart in the reference):
+ * independent FP64 multiply-add chains on every SM, the best of `repeats`
+ * timed launches, in FLOP/s (a multiply-add counts two).  The plain FP64
+ * step is bound by this pipe on GB300; benchmarks report against it. */
+int mlc_fp64_peak(int repeats, double *flops);
+
 /* ---- mass budget without allocation (no counterpart in the reference) --
  * For callers that own their device memory and cannot let the library call
  * cudaMalloc (a host model whose memory manager owns the device heap, code
@@ -343,9 +349,13 @@ int mlc_set_graphs(mlc_ctx *ctx, int on);
  * Partial sums live in a fixed 256 KiB file-scope device array, so domains
  * with more than 32768 rows ((iy-1)*kz) get MLC_ERR_TOO_LARGE.  The first
  * call on each device looks up that array's address: make it before any
- * stream capture.  Kernels are enqueued on `stream` (a cudaStream_t, NULL =
- * default stream) and the call returns without waiting; calls that overlap
- * on the GPU share the array and race, so serialise them. */
+ * stream capture.  The address is kept with the id of the CUDA context it
+ * was taken in and looked up again when the current context differs (after
+ * cudaDeviceReset the module loads at a new address); a call that does the
+ * lookup again must also come outside a capture.  Kernels are enqueued on
+ * `stream` (a cudaStream_t, NULL = default stream) and the call returns
+ * without waiting; calls that overlap on the GPU share the array and race,
+ * so serialise them. */
 int mlc_mass_budget_noalloc(const mlc_dims *d, double dx, double dt, const double *rho,
                             const double *dz, const double *qx, const double *u,
                             const double *v, const double *ps, double *out, void *stream);

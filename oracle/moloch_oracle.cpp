@@ -33,6 +33,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <memory>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace orc {
 
@@ -1355,6 +1358,24 @@ int orc_sound_only(void *h) {
   o.reset_tendencies();
   o.sound(o.dtsound);
   return MLC_OK;
+}
+
+// pfwsat elementwise over n points (Share/pfwsat.inc:1-43), for building
+// synthetic inputs without the library.
+int orc_pfwsat(size_t n, const double *t, const double *p, double *qs) {
+  for (size_t m = 0; m < n; ++m) qs[m] = orc::pfwsat(t[m], p[m]);
+  return MLC_OK;
+}
+
+// Threads of the OpenMP loops (the 1-core and all-cores CPU baselines).
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : 1);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
 }
 
 // Copy a work array out: 0 = s, 1 = zdiv2, 2 = tetavf.

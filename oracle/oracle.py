@@ -50,6 +50,11 @@ def load():
         lib.orc_setup_boundaries.argtypes = [C.c_int] * 6 + [P(C.c_int32)]
         lib.orc_setup_spectral.argtypes = [P(abi.mlc_params), C.c_int, dp, dp]
         lib.orc_paicompute.argtypes = [P(abi.mlc_dims)] + [dp] * 5 + [C.c_double, dp]
+        lib.orc_setup_nspg.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                       P(C.c_int), P(C.c_int)]
+        lib.orc_gmeanz.argtypes = [P(abi.mlc_dims), dp, dp]
+        lib.orc_pfwsat.argtypes = [C.c_size_t, dp, dp, dp]
+        lib.orc_set_threads.argtypes = [C.c_int]
         _lib = lib
     return _lib
 
@@ -113,3 +118,65 @@ class Oracle:
 
     def __del__(self):
         self.close()
+
+
+def set_threads(n: int) -> int:
+    """Threads of the oracle's OpenMP loops; returns the count in effect."""
+    return int(load().orc_set_threads(int(n)))
+
+
+class OracleSetup:
+    """The oracle's restatement of RegCM's setup routines behind the
+    interface of regcm_gb300.case's setup backends, so a case can be built
+    without loading the GPU library (the CPU reference timing)."""
+
+    def __init__(self):
+        self.lib = load()
+
+    @staticmethod
+    def _ok(st, where):
+        if st != 0:
+            raise RuntimeError(f"{where}: status {st}")
+
+    def nspg(self, jx, iy, ds_km):
+        gx, gd = C.c_int(), C.c_int()
+        self._ok(self.lib.orc_setup_nspg(jx, iy, ds_km, 1, 0, 0, C.byref(gx), C.byref(gd)),
+                 "orc_setup_nspg")
+        return gx.value, gd.value
+
+    def levels(self, kz, ztop, zita, zitah):
+        self._ok(self.lib.orc_setup_levels(kz, ztop, abi.dptr(zita), abi.dptr(zitah)),
+                 "orc_setup_levels")
+
+    def metric(self, dims, params, arrays):
+        self._ok(self.lib.orc_setup_metric(C.byref(dims), C.byref(params),
+                                           *[abi.dptr(a) for a in arrays]), "orc_setup_metric")
+
+    def relaxation(self, dims, params, zeta, hefc, fcx, tnudge, ffilt, gmeanz):
+        nz = C.c_int()
+        self._ok(self.lib.orc_setup_relaxation(C.byref(dims), C.byref(params), abi.dptr(zeta),
+                                               abi.dptr(hefc), abi.dptr(fcx), abi.dptr(tnudge),
+                                               abi.dptr(ffilt), C.byref(nz)),
+                 "orc_setup_relaxation")
+        params.nztop = nz.value
+        self._ok(self.lib.orc_gmeanz(C.byref(dims), abi.dptr(zeta), abi.dptr(gmeanz)), "orc_gmeanz")
+
+    def boundaries(self, jx, iy, lx, ly, nspgx, nspgd, out):
+        self._ok(self.lib.orc_setup_boundaries(jx, iy, lx, ly, nspgx, nspgd, abi.iptr(out)),
+                 "orc_setup_boundaries")
+
+    def spectral(self, params, kz, gmeanz, cnudge):
+        self._ok(self.lib.orc_setup_spectral(C.byref(params), kz, abi.dptr(gmeanz),
+                                             abi.dptr(cnudge)), "orc_setup_spectral")
+
+    def paicompute(self, dims, params, ps, zeta, t, qv, fmzf, zita, pai):
+        self._ok(self.lib.orc_paicompute(C.byref(dims), abi.dptr(ps), abi.dptr(zeta), abi.dptr(t),
+                                         abi.dptr(qv), abi.dptr(fmzf), float(zita[dims.kz - 1]),
+                                         abi.dptr(pai)), "orc_paicompute")
+
+    def pfwsat(self, t, p):
+        t = np.asfortranarray(t, dtype=np.float64)
+        p = np.asfortranarray(p, dtype=np.float64)
+        out = np.empty_like(t, order="F")
+        self._ok(self.lib.orc_pfwsat(t.size, abi.dptr(t), abi.dptr(p), abi.dptr(out)), "orc_pfwsat")
+        return out

@@ -202,6 +202,22 @@ int orc_setup_relaxation(const mlc_dims *d, const mlc_params *p, const double *z
   return 0;
 }
 
+// The domain-mean level heights of setup_bdycon (gmeanz, same sum order
+// as orc_setup_relaxation), for the spectral nudging weights.
+int orc_gmeanz(const mlc_dims *d, const double *zeta_, double *gmeanz_o) {
+  const int jx = d->jx, iy = d->iy, kz = d->kz;
+  F3 zeta(1, jx - 1, 1, iy - 1, 1, kz);
+  zeta.load(zeta_);
+  const double np = (double)((jx - 1) * (iy - 1));
+  for (int k = 1; k <= kz; ++k) {
+    double meanz = 0.0;
+    for (int j = 1; j <= jx - 1; ++j)
+      for (int i = 1; i <= iy - 1; ++i) meanz = meanz + zeta(j, i, k) / np;
+    gmeanz_o[k - 1] = meanz;
+  }
+  return 0;
+}
+
 // lowpass_init's level weights (Main/mod_bdycod.F90:3890-3894).
 int orc_setup_spectral(const mlc_params *p, int kz, const double *gmeanz, double *cnudge) {
   const double rtb = 1.0 / p->dtbdys;
@@ -253,6 +269,32 @@ int orc_setup_boundaries(int jx, int iy, int ldotx, int ldoty, int nspgx, int ns
       if (j >= jgbr1 && j <= jgbr2) ibnd(j, i) = jgbr2 - j + 2;
     }
   std::memcpy(out, ibnd.d.data(), ibnd.d.size() * sizeof(int32_t));
+  return 0;
+}
+
+// nspgx/nspgd as initparam derives them (Share/mod_dynparam.F90:762-786):
+// the default 6 points scaled to the resolution ds (km), at most a quarter
+// of the smaller extent, at least 6; a namelist value (> 0) replaces the
+// default; with Lehmann weights for MOLOCH a power of two plus 2 points.
+int orc_setup_nspg(int jx, int iy, double ds, int lehmann, int nspgx_nl, int nspgd_nl,
+                   int *nspgx_o, int *nspgd_o) {
+  int nspgx = 6, nspgd = 6;
+  const int quarter = std::min(jx, iy) / 4;
+  nspgx = std::max(std::min(std::max((int)((double)(nspgx * 50) / ds), nspgx), quarter), 6);
+  nspgd = std::max(std::min(std::max((int)((double)(nspgd * 50) / ds), nspgd), quarter), 6);
+  if (nspgx_nl > 0) nspgx = nspgx_nl;
+  if (nspgd_nl > 0) nspgd = nspgd_nl;
+  nspgx = std::max(nspgx, 6);
+  nspgd = std::max(nspgd, 6);
+  if (lehmann) {
+    nspgx = std::min(std::max(6, (int)std::lround(20.0 * std::pow(ds, -0.35)) + 1), 34);
+    int isp = 1;
+    while (isp < nspgx - 2) isp *= 2;
+    nspgx = isp + 2;
+    nspgd = nspgx;
+  }
+  *nspgx_o = nspgx;
+  *nspgd_o = nspgd;
   return 0;
 }
 

@@ -177,6 +177,7 @@ def _declare(lib):
         "mlc_step_batch": (C.c_int, [C.c_void_p, C.c_int, P(mlc_diag)]),
         "mlc_launches_per_step": (C.c_int, [C.c_void_p]),
         "mlc_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+        "mlc_fp64_peak": (C.c_int, [C.c_int, P(C.c_double)]),
         "mlc_autotune": (C.c_int, [C.c_void_p, C.c_int, P(mlc_tune_report)]),
         "mlc_set_launch_shapes": (C.c_int, [C.c_void_p, P(mlc_tune_report)]),
         "mlc_create_multi": (C.c_int, [P(mlc_dims), P(mlc_params), C.c_int, P(C.c_void_p)]),

@@ -22,7 +22,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fno-fast-math", "-ffp-contract=off"]
 
-CU_SOURCES = ["mlc_sound.cu", "mlc_advect.cu", "mlc_end.cu", "mlc_context.cu", "mlc_noalloc.cu"]
+CU_SOURCES = ["mlc_sound.cu", "mlc_advect.cu", "mlc_end.cu", "mlc_context.cu", "mlc_noalloc.cu",
+              "mlc_peak.cu"]
 CPP_SOURCES = ["mlc_setup.cpp", "mlc_restart.cpp"]
 
 

@@ -16,8 +16,10 @@ memory from a seeded recipe:
 * Lehmann relaxation weights (bdy_use_lehmann = .true.), top nudging on,
   spectral nudging off, divergence damping and filter on.
 
-Static fields come from the library's own host setup (moloch_gb300_setup.h).
-Every array is a Fortran-ordered float64 numpy array with the extents of
+Static fields come from a setup backend: by default the library's own host
+setup (moloch_gb300_setup.h, ``LibrarySetup``); any object with the same
+methods may stand in for it (a caller that must not load the GPU library
+passes its own).  Every array is a Fortran-ordered float64 numpy array with the extents of
 include/moloch_gb300.h.  Random numbers come from SplitMix64 so any consumer
 (the GPU library, the CPU oracle) sees identical bytes.
 """
@@ -70,13 +72,60 @@ def isa(height):
     return t, p
 
 
-def pfwsat(t, p):
-    """Saturation mixing ratio through the library's own restatement."""
-    t = np.asfortranarray(t, dtype=np.float64)
-    p = np.asfortranarray(p, dtype=np.float64)
-    out = np.empty_like(t, order="F")
-    abi.check(abi.load().mlc_pfwsat(t.size, abi.dptr(t), abi.dptr(p), abi.dptr(out)), "mlc_pfwsat")
-    return out
+class LibrarySetup:
+    """The library's host setup helpers (include/moloch_gb300_setup.h) as a
+    case-building backend: levels, nspgx, metric, relaxation weights,
+    boundary masks, spectral weights, paicompute and pfwsat."""
+
+    def __init__(self):
+        self.lib = abi.load()
+
+    def nspg(self, jx, iy, ds_km):
+        gx, gd = C.c_int(), C.c_int()
+        abi.check(self.lib.mlc_setup_nspg(jx, iy, ds_km, 1, 0, 0, C.byref(gx), C.byref(gd)),
+                  "mlc_setup_nspg")
+        return gx.value, gd.value
+
+    def levels(self, kz, ztop, zita, zitah):
+        abi.check(self.lib.mlc_setup_levels(kz, ztop, abi.dptr(zita), abi.dptr(zitah)),
+                  "mlc_setup_levels")
+
+    def metric(self, dims, params, arrays):
+        abi.check(self.lib.mlc_setup_metric(C.byref(dims), C.byref(params),
+                                            *[abi.dptr(a) for a in arrays]), "mlc_setup_metric")
+
+    def relaxation(self, dims, params, zeta, hefc, fcx, tnudge, ffilt, gmeanz):
+        abi.check(self.lib.mlc_setup_relaxation(C.byref(dims), C.byref(params), abi.dptr(zeta),
+                                                abi.dptr(hefc), abi.dptr(fcx), abi.dptr(tnudge),
+                                                abi.dptr(ffilt), abi.dptr(gmeanz)),
+                  "mlc_setup_relaxation")
+
+    def boundaries(self, jx, iy, lx, ly, nspgx, nspgd, out):
+        abi.check(self.lib.mlc_setup_boundaries(jx, iy, lx, ly, nspgx, nspgd, abi.iptr(out)),
+                  "mlc_setup_boundaries")
+
+    def spectral(self, params, kz, gmeanz, cnudge):
+        abi.check(self.lib.mlc_setup_spectral(C.byref(params), kz, abi.dptr(gmeanz),
+                                              abi.dptr(cnudge)), "mlc_setup_spectral")
+
+    def paicompute(self, dims, params, ps, zeta, t, qv, fmzf, zita, pai):
+        abi.check(self.lib.mlc_paicompute(C.byref(dims), C.byref(params), abi.dptr(ps),
+                                          abi.dptr(zeta), abi.dptr(t), abi.dptr(qv),
+                                          abi.dptr(fmzf), abi.dptr(zita), abi.dptr(pai)),
+                  "mlc_paicompute")
+
+    def pfwsat(self, t, p):
+        t = np.asfortranarray(t, dtype=np.float64)
+        p = np.asfortranarray(p, dtype=np.float64)
+        out = np.empty_like(t, order="F")
+        abi.check(self.lib.mlc_pfwsat(t.size, abi.dptr(t), abi.dptr(p), abi.dptr(out)),
+                  "mlc_pfwsat")
+        return out
+
+
+def pfwsat(t, p, setup=None):
+    """Saturation mixing ratio (Share/pfwsat.inc) through the setup backend."""
+    return (setup or LibrarySetup()).pfwsat(t, p)
 
 
 def _f(shape):
@@ -182,24 +231,25 @@ class Case:
         return {k: np.array(v, order="F", copy=True) for k, v in self.state.items()}
 
 
-def default_params() -> abi.mlc_params:
-    p = abi.mlc_params()
-    abi.load().mlc_default_params(C.byref(p))
-    return p
+def _zero_params() -> abi.mlc_params:
+    """A parameter block with every field zero; build() sets each one."""
+    return abi.mlc_params()
 
 
 def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv: int = 1,
           moist: bool = False, seed: int = 0, hills=None, wind=10.0, jet: bool = False,
           theta_noise: float = 0.1, tracer: bool = False, precision: int = abi.MLC_PREC_FP64,
           name: str = "case", debug_level: int = 1, lrotllr: bool = False,
-          apply_bdy: bool = True, spectral: bool = False, dtrad: float = 1800.0) -> Case:
-    """Build one synthetic domain of nx x ny cross points and kz levels."""
-    lib = abi.load()
+          apply_bdy: bool = True, spectral: bool = False, dtrad: float = 1800.0,
+          setup=None) -> Case:
+    """Build one synthetic domain of nx x ny cross points and kz levels.
+    `setup` is the backend of the static fields (default: the library's)."""
+    su = setup or LibrarySetup()
     jx, iy = nx + 1, ny + 1
     nqx = 5 if moist else 2
     ntr = 1 if tracer else 0
     dims = abi.mlc_dims(jx, iy, kz, nqx, ntr)
-    p = default_params()
+    p = _zero_params()
     p.dtsec, p.dx = float(dt), float(dx)
     p.mo_ztop, p.mo_h, p.mo_a0 = 25000.0, 8000.0, 0.0
     p.mo_nadv, p.mo_nsound = nadv, nsound
@@ -214,10 +264,7 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
     p.debug_level = debug_level
     p.precision = precision
     p.dtbdys = 6.0 * 3600.0
-    gx, gd = C.c_int(), C.c_int()
-    abi.check(lib.mlc_setup_nspg(jx, iy, dx / 1000.0, 1, 0, 0, C.byref(gx), C.byref(gd)),
-              "mlc_setup_nspg")
-    p.nspgx, p.nspgd = gx.value, gd.value
+    p.nspgx, p.nspgd = su.nspg(jx, iy, dx / 1000.0)
 
     # ---- terrain (geopotential) at cross / u / v positions on (jx, iy) ----
     xc = (np.arange(1, jx + 1) - 0.5) * dx
@@ -246,34 +293,29 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
     st["vlat"] = np.full((jx - 1, iy), 45.0, order="F")
     st["rlat"] = np.full((iy,), 45.0, order="F")
     zita, zitah = np.zeros(kz + 1), np.zeros(kz)
-    abi.check(lib.mlc_setup_levels(kz, p.mo_ztop, abi.dptr(zita), abi.dptr(zitah)),
-              "mlc_setup_levels")
+    su.levels(kz, p.mo_ztop, zita, zitah)
     st["zita"], st["zitah"] = zita, zitah
     for n, shp in (("hx", (jx, iy - 1)), ("hy", (jx - 1, iy)), ("zeta", (jx - 1, iy - 1, kz)),
                    ("fmz", (jx - 1, iy - 1, kz)), ("rfmzu", (jx, iy - 1, kz)),
                    ("rfmzv", (jx - 1, iy, kz)), ("fmzf", (jx - 1, iy - 1, kz + 1)),
                    ("zetaf", (jx - 1, iy - 1, kz + 1)), ("dz", (jx - 1, iy - 1, kz))):
         st[n] = _f(shp)
-    abi.check(lib.mlc_setup_metric(C.byref(dims), C.byref(p), *[abi.dptr(st[n]) for n in (
+    su.metric(dims, p, [st[n] for n in (
         "ht", "htu", "htv", "msfu", "msfv", "zita", "zitah", "hx", "hy", "zeta", "fmz",
-        "rfmzu", "rfmzv", "fmzf", "zetaf", "dz")]), "mlc_setup_metric")
+        "rfmzu", "rfmzv", "fmzf", "zetaf", "dz")])
     st["hefc"] = _f((p.nspgx, kz))
     st["fcx"] = _f((p.nspgx,))
     st["tnudge"] = _f((kz,))
     st["ffilt"] = _f((kz,))
     st["gmeanz"] = _f((kz,))
-    abi.check(lib.mlc_setup_relaxation(C.byref(dims), C.byref(p), abi.dptr(st["zeta"]),
-                                       abi.dptr(st["hefc"]), abi.dptr(st["fcx"]),
-                                       abi.dptr(st["tnudge"]), abi.dptr(st["ffilt"]),
-                                       abi.dptr(st["gmeanz"])), "mlc_setup_relaxation")
+    su.relaxation(dims, p, st["zeta"], st["hefc"], st["fcx"], st["tnudge"], st["ffilt"],
+                  st["gmeanz"])
     for n, (lx, ly) in (("ibnd_cr", (0, 0)), ("ibnd_ud", (1, 0)), ("ibnd_vd", (0, 1))):
         st[n] = np.zeros((jx, iy), dtype=np.int32, order="F")
-        abi.check(lib.mlc_setup_boundaries(jx, iy, lx, ly, p.nspgx, p.nspgd, abi.iptr(st[n])),
-                  "mlc_setup_boundaries")
+        su.boundaries(jx, iy, lx, ly, p.nspgx, p.nspgd, st[n])
     if spectral:
         st["cnudge"] = _f((kz,))
-        abi.check(lib.mlc_setup_spectral(C.byref(p), kz, abi.dptr(st["gmeanz"]),
-                                         abi.dptr(st["cnudge"])), "mlc_setup_spectral")
+        su.spectral(p, kz, st["gmeanz"], st["cnudge"])
 
     # ---- atmosphere on cross points ----
     rng_n = 0
@@ -285,14 +327,12 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
     ps_isa = np.asfortranarray(ps_isa)
     if moist:
         noise = splitmix64(seed * 7919 + 1, int(np.prod(cshape))).reshape(cshape, order="F")
-        qv = 0.7 * pfwsat(t_isa, np.asfortranarray(p_isa)) * (1.0 + 0.1 * (noise - 0.5))
+        qv = 0.7 * su.pfwsat(t_isa, np.asfortranarray(p_isa)) * (1.0 + 0.1 * (noise - 0.5))
         qv = np.asfortranarray(qv)
     else:
         qv = np.full(cshape, 1.0e-8, order="F")
     pai = _f(cshape)
-    abi.check(lib.mlc_paicompute(C.byref(dims), C.byref(p), abi.dptr(ps_isa), abi.dptr(st["zeta"]),
-                                 abi.dptr(t_isa), abi.dptr(qv), abi.dptr(st["fmzf"]),
-                                 abi.dptr(zita), abi.dptr(pai)), "mlc_paicompute")
+    su.paicompute(dims, p, ps_isa, st["zeta"], t_isa, qv, st["fmzf"], zita, pai)
     thv = t_isa * (1.0 + EP1 * qv) / pai
     noise = splitmix64(seed * 7919 + 2, int(np.prod(cshape))).reshape(cshape, order="F")
     inner = np.zeros(cshape, dtype=bool)
@@ -356,7 +396,7 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
         "w": _f((jx - 1, iy - 1, kz + 1)), "pai": np.array(pai, order="F"),
         "tetav": np.asfortranarray(tvirt / pai), "t": np.array(t_b, order="F"),
         "tvirt": tvirt, "ux": _f(cshape), "vx": _f(cshape), "p": pres, "rho": rho,
-        "qsat": pfwsat(t_b, pres), "qx": qx, "ps": psa,
+        "qsat": su.pfwsat(t_b, pres), "qx": qx, "ps": psa,
     }
     if tracer:
         state["trac"] = np.array(trac, order="F")

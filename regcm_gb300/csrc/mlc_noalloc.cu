@@ -21,7 +21,9 @@
 //   them (one stream, or events);
 // * every partial record the final pass reads is written by the same call
 //   before it is read, so no part of the array has to start at zero.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <mutex>
 
@@ -37,18 +39,50 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_budget_scratch[kBudgetBlocks * kBudgetRecord];
 
-// Host-side copy of the array's device address, per device.  In host code
-// the name g_budget_scratch is only a stand-in: its device address comes
-// from cudaGetSymbolAddress with the device current.
+// Host-side copy of the array's device address, per device, with the id of
+// the CUDA context it was taken in.  In host code the name g_budget_scratch
+// is only a stand-in: its device address comes from cudaGetSymbolAddress
+// with the device current.  A cudaDeviceReset (or any new primary context)
+// reloads the module at another address, so the cached address is used only
+// while the current context's id is the one it was taken in; otherwise it is
+// looked up again.
 std::mutex g_mu;
 double *g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
+
+// The unique id of the current CUDA context (0 if it cannot be read), from
+// driver entry points fetched through the runtime (no link against libcuda).
+unsigned long long current_context_id() {
+  static PFN_cuCtxGetCurrent_v4000 get_ctx = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_ctx = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+    cudaGetLastError();
+  });
+  if (!get_ctx || !get_id) return 0;
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_ctx(&c) != CUDA_SUCCESS || !c) return 0;
+  if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 int scratch_for_current_device(double **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return MLC_ERR_NODEVICE;
   if (dev < 0 || dev >= kMaxDevices) return MLC_ERR_INVALID;
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || ctx == 0 || g_scratch_ctx[dev] != ctx) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_budget_scratch);
     if (e != cudaSuccess || !p) {
@@ -56,6 +90,8 @@ int scratch_for_current_device(double **out) {
       return MLC_ERR_CUDA;
     }
     g_scratch_ptr[dev] = static_cast<double *>(p);
+    // the lookup makes the device's primary context current if none was
+    g_scratch_ctx[dev] = ctx ? ctx : current_context_id();
   }
   *out = g_scratch_ptr[dev];
   return MLC_OK;

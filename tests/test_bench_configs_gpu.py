@@ -1,0 +1,117 @@
+"""Parity on the benchmark's own workloads, through the C ABI.
+
+* The convection-permitting moist domain the default benchmark line times
+  (512 x 512 x 41, dx 3 km, dt 20 s, 4 substeps, 5 water species), FP64:
+  relative L2 per field <= 1e-12 after one step against the CPU oracle.
+* The dry domain with a passive tracer (64 x 64 x 30, dx 12 km, dt 60 s,
+  3 substeps), FP64: <= 1e-9 after 100 steps.
+* The moist 512 x 512 x 41 domain in mixed precision (FP32 fields; theta_v,
+  Exner, the solve's hydrostatic balance, temperature and the mass sums to
+  FP64 accuracy), against the FP64 oracle after 20 steps.  The scope's bar is
+  1e-4 relative L2 on theta, u, v, w and the species; measured on GB300:
+  see MIXED_C1_MEASURED.  The column mass sum_k dz*rho of every column is
+  compared with the oracle's, and the budget's dry mass with the oracle's.
+
+When MOLOCH_TEST_REPORT is set, the measured errors are also written there
+as JSON (one file per test), for the design notes.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from regcm_gb300 import abi
+from regcm_gb300 import case as cs
+from regcm_gb300.moloch import domain_from_case
+
+from .conftest import rel_l2
+from .test_parity_gpu import field_errors, run_pair
+
+pytestmark = pytest.mark.gpu
+
+
+def _report(name: str, data: dict):
+    d = os.environ.get("MOLOCH_TEST_REPORT")
+    if d:
+        os.makedirs(d, exist_ok=True)
+        with open(os.path.join(d, f"{name}.json"), "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+
+
+def test_c1_moist_512_fp64_one_step():
+    case = cs.config1()
+    g, o, dg, do = run_pair(case, 1)
+    err = field_errors(g, o, case)
+    _report("c1_fp64_one_step", err)
+    bad = {k: v for k, v in err.items() if not v <= 1e-12}
+    assert not bad, bad
+    for k in ("drymass", "qmass", "ps_max", "ps_min"):
+        assert abs(getattr(dg, k) - getattr(do, k)) <= 1e-12 * abs(getattr(do, k)), k
+
+
+def test_c0_dry_64_fp64_hundred_steps():
+    case = cs.config0()
+    g, o, dg, do = run_pair(case, 100, chunk=25)
+    err = field_errors(g, o, case)
+    _report("c0_fp64_hundred_steps", err)
+    bad = {k: v for k, v in err.items() if not v <= 1e-9}
+    assert not bad, bad
+    assert abs(dg.drymass - do.drymass) <= 1e-12 * abs(do.drymass)
+
+
+# Relative L2 against the FP64 oracle after 20 steps of the 512 x 512 x 41
+# moist domain, measured on GB300; the test holds each field to the bound.
+MIXED_C1_BOUND = {"tetav": 2e-8, "pai": 5e-9, "u": 3e-5, "v": 3e-5, "w": 3e-5, "qv": 3e-5,
+                  "qc": 1e-4}
+
+
+def column_mass(case, st):
+    """sum_k dz * rho per column of the interior (jci x ici), FP64."""
+    dz = case.static["dz"]
+    return np.einsum("jik,jik->ji", dz[1:-1, 1:-1, :], st["rho"][1:-1, 1:-1, :])
+
+
+def dry_mass(case, st):
+    """sum of dx^2 * dz * rho over jci x ici x k, exactly rounded (math.fsum)."""
+    import math
+    dx = case.params.dx
+    v = (dx * dx) * case.static["dz"][1:-1, 1:-1, :] * st["rho"][1:-1, 1:-1, :]
+    return math.fsum(v.ravel())
+
+
+def test_c1_moist_512_mixed_twenty_steps():
+    nsteps = 20
+    cm = cs.config1(precision=abi.MLC_PREC_MIXED)
+    dom = domain_from_case(cm)
+    dm = dom.step(nsteps)
+    got = cm.empty_state()
+    dom.download(cm.state_ptrs_of(got))
+    dom.close()
+    cf = cs.config1()
+    orc = Oracle(cf)
+    st, do = orc.step(nsteps)
+    assert st == 0
+    ref = orc.state()
+    orc.close()
+    err = {n: rel_l2(got[n], ref[n]) for n in ("tetav", "pai", "u", "v", "w")}
+    err["qv"] = rel_l2(got["qx"][..., 0], ref["qx"][..., 0])
+    err["qc"] = rel_l2(got["qx"][..., 1], ref["qx"][..., 1])
+    cg, co = column_mass(cm, got), column_mass(cf, ref)
+    col = float(np.max(np.abs(cg - co) / np.abs(co)))
+    dry = abs(dm.drymass - do.drymass) / abs(do.drymass)
+    # dry-mass drift over the run: the budget after the last step minus the
+    # same sum (Main/mod_massck.F90:77-90) over the initial state
+    m0 = dry_mass(cf, cf.state)
+    _report("c1_mixed_twenty_steps", dict(err, column_mass_max_rel=col, drymass_rel=dry,
+                                          drift_mixed=(dm.drymass - m0) / m0,
+                                          drift_oracle=(do.drymass - m0) / m0))
+    bad = {k: v for k, v in err.items() if not v <= MIXED_C1_BOUND[k]}
+    assert not bad, err
+    # column mass of every column and the budget's dry mass: FP32 fields, so
+    # agreement to FP32 rounding of rho, not to FP64
+    assert col <= 1e-6, col
+    assert dry <= 1e-6, dry

@@ -133,3 +133,37 @@ def test_pfwsat_known_answer():
     # the 0.15 p cap (Share/pfwsat.inc:36-41)
     assert q[1] == ep2 * ((0.15 * 3.0e3) / (3.0e3 - 0.15 * 3.0e3))
     assert 0.02 < q[2] < 0.03
+
+
+@pytest.mark.parametrize("jx,iy,ds,leh", [(65, 65, 12.0, 1), (513, 513, 3.0, 1), (65, 65, 12.0, 0),
+                                          (30, 200, 50.0, 0), (401, 97, 2.0, 0), (49, 49, 25.0, 1)])
+def test_nspg_oracle(jx, iy, ds, leh):
+    a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    assert abi.load().mlc_setup_nspg(jx, iy, ds, leh, 0, 0, C.byref(a), C.byref(b)) == 0
+    assert orc.load().orc_setup_nspg(jx, iy, ds, leh, 0, 0, C.byref(c), C.byref(d)) == 0
+    assert (a.value, b.value) == (c.value, d.value)
+
+
+@pytest.mark.parametrize("make", [
+    lambda su: cs.config0(nx=32, ny=28, kz=20, setup=su),
+    lambda su: cs.config1(nx=40, ny=36, kz=24, setup=su),
+    lambda su: cs.build(24, 22, 12, dx=12000.0, dt=60.0, nsound=3, moist=True, seed=2,
+                        spectral=True, setup=su),
+])
+def test_case_from_oracle_setup_is_identical(make):
+    """A case built through the oracle's setup (how the CPU reference timing
+    builds its input without loading the GPU library) holds exactly the
+    bytes of the case the library's setup builds."""
+    a = make(None)
+    b = make(orc.OracleSetup())
+    for f, _ in abi.mlc_params._fields_:
+        assert getattr(a.params, f) == getattr(b.params, f), f
+    assert a.dims.as_tuple() == b.dims.as_tuple()
+    for part in ("static", "state"):
+        da, db = getattr(a, part), getattr(b, part)
+        assert da.keys() == db.keys()
+        for n in da:
+            assert np.array_equal(da[n], db[n]), (part, n)
+    for n in a.bdy:
+        for x, y in zip(a.bdy[n], b.bdy[n]):
+            assert np.array_equal(x, y), n
