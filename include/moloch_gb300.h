@@ -80,7 +80,8 @@ typedef struct mlc_params {
   int32_t mo_spectral_nudge; /* spectral nudging on/off          [mo_spectral_nudge] */
   int32_t do_apply_bdy;   /* lateral boundary relaxation on/off [do_apply_bdy] */
   int32_t lrotllr;        /* ROTLLR projection branch            [iproj]   */
-  int32_t ipptls;         /* microphysics class: 0,1,2           [ipptls]  */
+  int32_t ipptls;         /* microphysics class 0-5: nqx 2 (0, 1), 5 (2, 3),
+                             7 (4), 10 (5)                      [ipptls]  */
   int32_t present_qc;     /* boundary data carries qc            [present_qc] */
   int32_t present_qi;     /* boundary data carries qi            [present_qi] */
   int32_t nspgx;          /* relaxation zone width, cross points [nspgx]   */
@@ -89,6 +90,13 @@ typedef struct mlc_params {
   int32_t debug_level;    /* > 0: mass budget every step         [debug_level] */
   int32_t precision;      /* MLC_PREC_FP64 or MLC_PREC_MIXED               */
   double  dtrad;          /* spectral nudging interval [s] (radiation step) [dtrad] */
+  int32_t bdy_use_lehmann; /* relaxation weights: Lehmann's (1) or exponential
+                              nudging (0)                     [bdy_use_lehmann] */
+  int32_t ibltyp;         /* PBL scheme; 2 (UW) carries TKE, advected with
+                             the step                         [ibltyp]  */
+  double  high_nudge;     /* exponential nudging strength at the top,   */
+  double  medium_nudge;   /* near sigma 0.4 and at the surface          */
+  double  low_nudge;      /*          [high_nudge, medium_nudge, low_nudge] */
 } mlc_params;
 
 /* Time-invariant fields (host pointers, read once by mlc_bind_static).
@@ -331,6 +339,22 @@ int mlc_launches_per_step(const mlc_ctx *ctx);
 
 /* Record steps into CUDA graphs (default 1) or launch them one by one (0). */
 int mlc_set_graphs(mlc_ctx *ctx, int on);
+
+/* Test hook of the bounded device waits (no counterpart in the reference).
+ * With polls > 0, every block of the member's horizontal WAF waits, before
+ * it issues any copy, on an mbarrier that nothing completes, gives up after
+ * `polls` polls and records the fault the way a tile copy that never lands
+ * does: the step then returns MLC_ERR_CUDA ("a bounded device wait gave
+ * up") and the member's state is not valid.  Nothing faults or hangs on the
+ * GPU.  0 (the default) turns the hook off. */
+int mlc_member_test_stall(mlc_ctx *ctx, int member, int polls);
+
+/* Mixed precision only (no counterpart in the reference): the implicit
+ * w-Exner solve's Thomas recurrence and back substitution in double-float
+ * arithmetic, about 48 significant bits (1, the default), or in FP32 (0).
+ * The solve's right-hand side (hydrostatic balance) and the Exner update
+ * are double-float either way.  Takes effect at the next step. */
+int mlc_set_solve_precision(mlc_ctx *ctx, int df_recurrence);
 
 /* FP64 throughput of the current device (no counterpart in the reference):
  * independent FP64 multiply-add chains on every SM, the best of `repeats`

@@ -40,16 +40,25 @@ int mlc_setup_metric(const mlc_dims *d, const mlc_params *p,
                      double *rfmzu, double *rfmzv, double *fmzf,
                      double *zetaf, double *dz);
 
+/* exponential_nudging (Main/mpplib/mod_runparams.F90:611-637): the nudging
+ * profile anudge (kz) at the half levels, from the three strengths at the
+ * top, at the first full level with sigma > 0.4 and at the surface, through
+ * RegCM's spline1d (Share/mod_spline.F90:387-459). */
+int mlc_exponential_nudging(int kz, double ztop, double high, double medium, double low,
+                            double *anudge);
+
 /* relax_coefficients (Main/mpplib/mod_runparams.F90:648-702): Lehmann's
  * optimal relaxation weights; np must be 1 or a power of two (<= 32). */
 int mlc_relax_coefficients(int np, double gmmin, double gmmax, double *coeff);
 
 /* The MOLOCH half of setup_bdycon (Main/mod_bdycod.F90:478-560) and the
  * sponge of init (Main/mod_init.F90:1008-1025): hefc (nspgx,kz) with
- * Lehmann weights, fcx (nspgx) for tracers (Main/chemlib/mod_che_bdyco.F90:
- * 1036-1039), the domain-mean level height, nztop and tnudge (kz), ffilt
- * (kz).  zeta is (jx-1,iy-1,kz).  Writes p->nztop.  Only the Lehmann
- * weights are built (bdy_use_lehmann = .true.). */
+ * Lehmann's weights when p->bdy_use_lehmann is set, else the exponential
+ * nudging profile (exponential_nudging, Main/mpplib/mod_runparams.F90:
+ * 611-637, from p->high_nudge, medium_nudge, low_nudge); fcx (nspgx) for
+ * tracers (Main/chemlib/mod_che_bdyco.F90:1036-1039), the domain-mean level
+ * height, nztop and tnudge (kz), ffilt (kz).  zeta is (jx-1,iy-1,kz).
+ * Writes p->nztop. */
 int mlc_setup_relaxation(const mlc_dims *d, mlc_params *p, const double *zeta,
                          double *hefc, double *fcx, double *tnudge,
                          double *ffilt, double *gmeanz);

@@ -53,6 +53,7 @@ def load():
         lib.orc_setup_nspg.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
                                        P(C.c_int), P(C.c_int)]
         lib.orc_gmeanz.argtypes = [P(abi.mlc_dims), dp, dp]
+        lib.orc_exponential_nudging.argtypes = [C.c_int] + [C.c_double] * 4 + [dp]
         lib.orc_pfwsat.argtypes = [C.c_size_t, dp, dp, dp]
         lib.orc_set_threads.argtypes = [C.c_int]
         _lib = lib
@@ -138,10 +139,10 @@ class OracleSetup:
         if st != 0:
             raise RuntimeError(f"{where}: status {st}")
 
-    def nspg(self, jx, iy, ds_km):
+    def nspg(self, jx, iy, ds_km, lehmann=True):
         gx, gd = C.c_int(), C.c_int()
-        self._ok(self.lib.orc_setup_nspg(jx, iy, ds_km, 1, 0, 0, C.byref(gx), C.byref(gd)),
-                 "orc_setup_nspg")
+        self._ok(self.lib.orc_setup_nspg(jx, iy, ds_km, 1 if lehmann else 0, 0, 0,
+                                         C.byref(gx), C.byref(gd)), "orc_setup_nspg")
         return gx.value, gd.value
 
     def levels(self, kz, ztop, zita, zitah):

@@ -15,6 +15,20 @@
 
 namespace orc {
 
+// model_zitaf / model_zitah (Share/mod_zita.F90:54-86), as orc_setup_levels
+static void orc_setup_levels_(int kz, double ztop, double *zitaf_out, double *zitah_out) {
+  std::vector<double> zitaf(kz + 2), zitah(kz + 1);
+  double dz = ztop / (double)kz;
+  zitaf[kz + 1] = 0.0;
+  zitaf[1] = ztop;
+  for (int k = kz; k >= 2; --k) zitaf[k] = zitaf[k + 1] + dz;
+  zitah[kz] = dz * 0.5;
+  zitah[1] = ztop - dz * 0.5;
+  for (int k = kz - 1; k >= 2; --k) zitah[k] = zitah[k + 1] + dz;
+  for (int k = 1; k <= kz + 1; ++k) zitaf_out[k - 1] = zitaf[k];
+  for (int k = 1; k <= kz; ++k) zitah_out[k - 1] = zitah[k];
+}
+
 static double zfz(double ztop, double zh) { return ztop / (std::exp(ztop / zh) - 1.0); }
 static double bzita(double zita, double ztop, double zh) { return zfz(ztop, zh) * (std::exp(zita / zh) - 1.0); }
 static double bzitap(double zita, double ztop, double zh) { return zfz(ztop, zh) * std::exp(zita / zh) / zh; }
@@ -36,6 +50,84 @@ static double md_zeta(double zita, double geopot, double ztop, double zh, double
   return orog * (gzita_(zita, ztop, a0) - 1.0) + bzita(zita, ztop, zh);
 }
 
+// spline1d (Share/mod_spline.F90:387-459), 1-based arrays, y2 updated in
+// place as the Fortran does.
+static void spline1d(int nold, const std::vector<double> &xold, const std::vector<double> &yold,
+                     std::vector<double> &y2, int nnew, const std::vector<double> &xnew,
+                     std::vector<double> &ynew) {
+  const double afac = 6.0, bfac = d_one / afac;
+  std::vector<double> p(nold), q(nold);
+  int noldm1 = nold - 1;
+  double dxl = xold[2] - xold[1];
+  double dxr = xold[3] - xold[2];
+  double dydxl = (yold[2] - yold[1]) / dxl;
+  double dydxr = (yold[3] - yold[2]) / dxr;
+  double rtdxc = 0.5 / (dxl + dxr);
+  p[1] = rtdxc * (bfac * (dydxr - dydxl) - dxl * y2[1]);
+  q[1] = -rtdxc * dxr;
+  if (nold > 3) {
+    for (int k = 3; k <= nold; ++k) {
+      dxl = dxr;
+      dydxl = dydxr;
+      dxr = xold[k + 1] - xold[k];
+      dydxr = (yold[k + 1] - yold[k]) / dxr;
+      double dxc = dxl + dxr;
+      double den = d_one / (dxl * q[k - 2] + dxc + dxc);
+      p[k - 1] = den * (bfac * (dydxr - dydxl) - dxl * p[k - 2]);
+      q[k - 1] = -den * dxr;
+    }
+  }
+  for (int k = noldm1; k >= 2; --k) y2[k] = p[k - 1] + q[k - 1] * y2[k + 1];
+  int k = -1, kold = 0;
+  double ak = 0, bk = 0, ck = 0;
+  for (int k1 = 1; k1 <= nnew; ++k1) {
+    double xk = xnew[k1];
+    if (xk < xold[1]) { ynew[k1] = yold[1]; continue; }
+    if (xk >= xold[nold]) { ynew[k1] = yold[nold]; continue; }
+    for (int k2 = 2; k2 <= nold; ++k2) {
+      if (xold[k2] <= xk) continue;
+      kold = k2 - 1;
+      break;
+    }
+    if (k == kold) {
+      double x = xk - xold[k];
+      double xsq = x * x;
+      ynew[k1] = ak * xsq * x + bk * xsq + ck * x + yold[k];
+      continue;
+    }
+    k = kold;
+    double y2k = y2[k], y2kp1 = y2[k + 1];
+    double dx = xold[k + 1] - xold[k];
+    double rdx = d_one / dx;
+    ak = bfac * rdx * (y2kp1 - y2k);
+    bk = 0.5 * y2k;
+    ck = rdx * (yold[k + 1] - yold[k]) - bfac * dx * (y2kp1 + y2k + y2k);
+    double x = xk - xold[k];
+    double xsq = x * x;
+    ynew[k1] = ak * xsq * x + bk * xsq + ck * x + yold[k];
+  }
+}
+
+// exponential_nudging (Main/mpplib/mod_runparams.F90:611-637) with
+// sigma = sigmazita(zita), hsigma = sigmazita(zitah) (Main/mod_params.F90:
+// 2464-2465, Share/mod_zita.F90:40-45).
+static void exponential_nudging(int kz, double ztop, double high, double medium, double low,
+                                std::vector<double> &nudge) {
+  std::vector<double> zf(kz + 1), zh(kz);
+  orc_setup_levels_(kz, ztop, zf.data(), zh.data());
+  std::vector<double> sigma(kz + 2), hsigma(kz + 1);
+  for (int k = 1; k <= kz + 1; ++k) sigma[k] = 1.0 - zf[k - 1] / ztop;
+  for (int k = 1; k <= kz; ++k) hsigma[k] = 1.0 - zh[k - 1] / ztop;
+  int kw;
+  for (kw = 2; kw <= kz; ++kw)
+    if (sigma[kw] > 0.40) break;
+  std::vector<double> zcin = {0.0, sigma[1], sigma[kw], sigma[kz + 1]};
+  std::vector<double> ncin = {0.0, high, medium, low};
+  std::vector<double> ycin = {0.0, 0.0, 0.0, 0.0};
+  nudge.assign(kz + 1, 0.0);
+  spline1d(3, zcin, ncin, ycin, kz, hsigma, nudge);
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -43,16 +135,15 @@ using namespace orc;
 extern "C" {
 
 int orc_setup_levels(int kz, double ztop, double *zitaf_out, double *zitah_out) {
-  std::vector<double> zitaf(kz + 2), zitah(kz + 1);
-  double dz = ztop / (double)kz;
-  zitaf[kz + 1] = 0.0;
-  zitaf[1] = ztop;
-  for (int k = kz; k >= 2; --k) zitaf[k] = zitaf[k + 1] + dz;
-  zitah[kz] = dz * 0.5;
-  zitah[1] = ztop - dz * 0.5;
-  for (int k = kz - 1; k >= 2; --k) zitah[k] = zitah[k + 1] + dz;
-  for (int k = 1; k <= kz + 1; ++k) zitaf_out[k - 1] = zitaf[k];
-  for (int k = 1; k <= kz; ++k) zitah_out[k - 1] = zitah[k];
+  orc_setup_levels_(kz, ztop, zitaf_out, zitah_out);
+  return 0;
+}
+
+int orc_exponential_nudging(int kz, double ztop, double high, double medium, double low,
+                            double *anudge) {
+  std::vector<double> nudge;
+  exponential_nudging(kz, ztop, high, medium, low, nudge);
+  for (int k = 1; k <= kz; ++k) anudge[k - 1] = nudge[k];
   return 0;
 }
 
@@ -174,12 +265,20 @@ int orc_setup_relaxation(const mlc_dims *d, const mlc_params *p, const double *z
   }
   F2<double> hefc(1, nspgx, 1, kz);
   for (int k = 1; k <= kz; ++k) { hefc(1, k) = 1.0; hefc(nspgx, k) = 0.0; }
-  double cflmax = std::min(0.999, (300.0 * (p->dtsec / (double)p->mo_nadv)) / (2.0 * p->dx));
-  double cflmin = std::max(0.001, (10.0 * (p->dtsec / (double)p->mo_nadv)) / (2.0 * p->dx));
-  std::vector<double> c(nspgx);
-  for (int k = 1; k <= kz; ++k) {
-    orc_relax_coefficients(nspgx - 2, cflmin, cflmax, c.data());
-    for (int n = 2; n <= nspgx - 1; ++n) hefc(n, k) = c[n - 2];
+  if (p->bdy_use_lehmann) {
+    double cflmax = std::min(0.999, (300.0 * (p->dtsec / (double)p->mo_nadv)) / (2.0 * p->dx));
+    double cflmin = std::max(0.001, (10.0 * (p->dtsec / (double)p->mo_nadv)) / (2.0 * p->dx));
+    std::vector<double> c(nspgx);
+    for (int k = 1; k <= kz; ++k) {
+      orc_relax_coefficients(nspgx - 2, cflmin, cflmax, c.data());
+      for (int n = 2; n <= nspgx - 1; ++n) hefc(n, k) = c[n - 2];
+    }
+  } else {
+    // Main/mod_bdycod.F90:538-544
+    std::vector<double> anudge;
+    exponential_nudging(kz, p->mo_ztop, p->high_nudge, p->medium_nudge, p->low_nudge, anudge);
+    for (int k = 1; k <= kz; ++k)
+      for (int n = 2; n <= nspgx - 1; ++n) hefc(n, k) = std::exp(-(double)(n - 1) / anudge[k]);
   }
   std::memcpy(hefc_o, hefc.d.data(), hefc.d.size() * 8);
   fcx_o[0] = 1.0;

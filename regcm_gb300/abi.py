@@ -55,7 +55,9 @@ class mlc_params(C.Structure):
                 ("do_apply_bdy", C.c_int32), ("lrotllr", C.c_int32),
                 ("ipptls", C.c_int32), ("present_qc", C.c_int32), ("present_qi", C.c_int32),
                 ("nspgx", C.c_int32), ("nspgd", C.c_int32), ("nztop", C.c_int32),
-                ("debug_level", C.c_int32), ("precision", C.c_int32), ("dtrad", C.c_double)]
+                ("debug_level", C.c_int32), ("precision", C.c_int32), ("dtrad", C.c_double),
+                ("bdy_use_lehmann", C.c_int32), ("ibltyp", C.c_int32), ("high_nudge", C.c_double),
+                ("medium_nudge", C.c_double), ("low_nudge", C.c_double)]
 
 
 STATIC_FIELDS = ["msfu", "msfv", "msfx", "ulat", "vlat", "rlat", "hx", "hy", "fmz", "fmzf",
@@ -161,6 +163,7 @@ def _declare(lib):
                                      P(C.c_int), P(C.c_int)]),
         "mlc_setup_metric": (C.c_int, [P(mlc_dims), P(mlc_params)] + [_dp] * 16),
         "mlc_relax_coefficients": (C.c_int, [C.c_int, C.c_double, C.c_double, _dp]),
+        "mlc_exponential_nudging": (C.c_int, [C.c_int] + [C.c_double] * 4 + [_dp]),
         "mlc_setup_relaxation": (C.c_int, [P(mlc_dims), P(mlc_params), _dp, _dp, _dp, _dp, _dp,
                                            _dp]),
         "mlc_setup_boundaries": (C.c_int, [C.c_int] * 6 + [_ip]),
@@ -178,6 +181,8 @@ def _declare(lib):
         "mlc_launches_per_step": (C.c_int, [C.c_void_p]),
         "mlc_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
         "mlc_fp64_peak": (C.c_int, [C.c_int, P(C.c_double)]),
+        "mlc_set_solve_precision": (C.c_int, [C.c_void_p, C.c_int]),
+        "mlc_member_test_stall": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
         "mlc_autotune": (C.c_int, [C.c_void_p, C.c_int, P(mlc_tune_report)]),
         "mlc_set_launch_shapes": (C.c_int, [C.c_void_p, P(mlc_tune_report)]),
         "mlc_create_multi": (C.c_int, [P(mlc_dims), P(mlc_params), C.c_int, P(C.c_void_p)]),

@@ -80,10 +80,10 @@ class LibrarySetup:
     def __init__(self):
         self.lib = abi.load()
 
-    def nspg(self, jx, iy, ds_km):
+    def nspg(self, jx, iy, ds_km, lehmann=True):
         gx, gd = C.c_int(), C.c_int()
-        abi.check(self.lib.mlc_setup_nspg(jx, iy, ds_km, 1, 0, 0, C.byref(gx), C.byref(gd)),
-                  "mlc_setup_nspg")
+        abi.check(self.lib.mlc_setup_nspg(jx, iy, ds_km, 1 if lehmann else 0, 0, 0,
+                                          C.byref(gx), C.byref(gd)), "mlc_setup_nspg")
         return gx.value, gd.value
 
     def levels(self, kz, ztop, zita, zitah):
@@ -241,12 +241,18 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
           theta_noise: float = 0.1, tracer: bool = False, precision: int = abi.MLC_PREC_FP64,
           name: str = "case", debug_level: int = 1, lrotllr: bool = False,
           apply_bdy: bool = True, spectral: bool = False, dtrad: float = 1800.0,
-          setup=None) -> Case:
+          lehmann: bool = True, ipptls: int | None = None, setup=None) -> Case:
     """Build one synthetic domain of nx x ny cross points and kz levels.
-    `setup` is the backend of the static fields (default: the library's)."""
+    `lehmann` picks Lehmann's relaxation weights (else exponential nudging
+    with the reference's default strengths 3, 2, 1); `ipptls` the
+    microphysics class of a moist domain (default 2; 3-5 add species that
+    start at zero); `setup` is the backend of the static fields (default:
+    the library's)."""
     su = setup or LibrarySetup()
     jx, iy = nx + 1, ny + 1
-    nqx = 5 if moist else 2
+    if ipptls is None:
+        ipptls = 2 if moist else 0
+    nqx = {0: 2, 1: 2, 2: 5, 3: 5, 4: 7, 5: 10}[ipptls]
     ntr = 1 if tracer else 0
     dims = abi.mlc_dims(jx, iy, kz, nqx, ntr)
     p = _zero_params()
@@ -258,13 +264,16 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
     p.dtrad = float(dtrad)
     p.do_apply_bdy = 1 if apply_bdy else 0
     p.lrotllr = 1 if lrotllr else 0
-    p.ipptls = 2 if moist else 0
+    p.ipptls = ipptls
     p.present_qc = 1 if moist else 0
     p.present_qi = 1 if moist else 0
     p.debug_level = debug_level
     p.precision = precision
     p.dtbdys = 6.0 * 3600.0
-    p.nspgx, p.nspgd = su.nspg(jx, iy, dx / 1000.0)
+    p.bdy_use_lehmann = 1 if lehmann else 0
+    p.ibltyp = 1
+    p.high_nudge, p.medium_nudge, p.low_nudge = 3.0, 2.0, 1.0
+    p.nspgx, p.nspgd = su.nspg(jx, iy, dx / 1000.0, lehmann)
 
     # ---- terrain (geopotential) at cross / u / v positions on (jx, iy) ----
     xc = (np.arange(1, jx + 1) - 0.5) * dx
@@ -365,6 +374,15 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
         qc_b = np.asfortranarray(1.0e-4 * patch)
         qi_b = _f(cshape)
         qx[..., 1] = qc_b
+        # the classes with more species: graupel and hail in the same patch,
+        # number concentrations (ipptls 5) above their floors
+        if ipptls >= 4:
+            qx[..., 5] = 5.0e-5 * patch
+            qx[..., 6] = 2.0e-5 * patch
+        if ipptls == 5:
+            qx[..., 7] = 1.0e10 * (1.0 + patch)
+            qx[..., 8] = 1.0e2 * (1.0 + patch)
+            qx[..., 9] = 1.0e-2 * (1.0 + patch)
     trac = None
     chib = None
     if tracer:

@@ -525,6 +525,14 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     out_s[tid] = out0 + ko;
   }
   __syncthreads();
+  if (D.stall_polls > 0) {
+    // test hook: wait on a barrier that no copy completes (none is issued
+    // yet), give up after the member's poll count and record the fault the
+    // way the tile waits below do; the block leaves with nothing in flight
+    const bool landed = mbar_wait_polls(&mbar[0], 0u, D.stall_polls);
+    if (__syncthreads_or(!landed) && tid == 0) atomicOr(&D.clk->fault, 1);
+    return;
+  }
   if (tid == 0)
     for (int q = 0; q < kStages && q < nf; ++q) issue(q, q);
 

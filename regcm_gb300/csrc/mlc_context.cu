@@ -232,7 +232,7 @@ int validate_params(const mlc_params *p) {
   if (!(p->dtsec > 0) || !(p->dx > 0) || !(p->mo_ztop > 0) || p->mo_nadv < 1 || p->mo_nsound < 1)
     return MLC_ERR_INVALID;
   if (!(p->dtbdys > 0) || p->nspgx < 3 || p->nspgd < 3) return MLC_ERR_INVALID;
-  if (p->ipptls < 0 || p->ipptls > 2) return MLC_ERR_UNSUPPORTED;
+  if (p->ipptls < 0 || p->ipptls > 5) return MLC_ERR_UNSUPPORTED;
   if (p->mo_spectral_nudge && !(p->dtrad > 0)) return MLC_ERR_INVALID;
   if (p->precision != MLC_PREC_FP64 && p->precision != MLC_PREC_MIXED) return MLC_ERR_INVALID;
   return MLC_OK;
@@ -248,7 +248,9 @@ int validate_dims(const mlc_dims *d, const mlc_params *p) {
   if ((size_t)(d->jx + 32) * (size_t)d->iy * (size_t)(d->kz + 1) >= ((size_t)1 << 31))
     return MLC_ERR_TOO_LARGE;
   if (d->nqx < 2 || d->nqx > 10 || d->ntr < 0 || d->ntr > 8) return MLC_ERR_INVALID;
-  if (p->ipptls == 2 && d->nqx < 5) return MLC_ERR_INVALID;
+  // species per microphysics class (Main/mod_params.F90:1724-1736)
+  if (p->ipptls >= 2 && d->nqx != (p->ipptls <= 3 ? 5 : p->ipptls == 4 ? 7 : 10))
+    return MLC_ERR_INVALID;
   if (n_table_r(*d, *p, true) > kMaxFields) return MLC_ERR_UNSUPPORTED;
   // the tracer relaxation assumes disjoint south/north and west/east bands
   if (d->ntr > 0 && (d->jx - 1 < 2 * p->nspgx || d->iy - 1 < 2 * p->nspgx)) return MLC_ERR_UNSUPPORTED;
@@ -296,6 +298,7 @@ struct Member {
   void *tend_raw = nullptr;
   size_t tend_bytes = 0;
   bool tend_live = false;
+  int stall_polls = 0;   // test hook of the bounded waits (mlc_member_test_stall)
 };
 
 template <class R> Dom<R> &dom_of(Member &m);
@@ -504,6 +507,7 @@ int refresh(mlc_ctx *x) {
     D.clk = x->clks + slot;
     D.diag = x->diags + slot;
     D.active = 1;
+    D.stall_polls = m.stall_polls;
     D.tend = m.tend_live ? static_cast<const R *>(m.tend_raw) : nullptr;
     t.push_back(D);
     L.jx = std::max(L.jx, m.g.jx);
@@ -1188,6 +1192,7 @@ int create_common(const mlc_params *params, int capacity, size_t budget, mlc_ctx
   L.solve_x = 32; L.solve_y = 2;
   L.vert_x = 32; L.vert_y = 4;
   L.htile = 1;  // 64x8 tiles; the autotuner's fixed configuration is 32x8
+  L.solve_df = 1;  // the mixed solve's recurrence to FP64 accuracy
   cudaError_t e = cudaGetDevice(&x->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) {
@@ -1340,6 +1345,12 @@ void mlc_default_params(mlc_params *p) {
   p->nztop = 0;
   p->debug_level = 0;
   p->precision = MLC_PREC_FP64;
+  // Share/mod_dynparam.F90:141,150-152 and Main/mod_params.F90 (ibltyp)
+  p->bdy_use_lehmann = 0;
+  p->ibltyp = 1;
+  p->high_nudge = 3.0;
+  p->medium_nudge = 2.0;
+  p->low_nudge = 1.0;
 }
 
 const char *mlc_strerror(int st) {
@@ -1812,6 +1823,21 @@ int mlc_launches_per_step(const mlc_ctx *x) { return x ? x->launches_per_step : 
 int mlc_set_graphs(mlc_ctx *x, int on) {
   if (!x) return MLC_ERR_INVALID;
   x->use_graphs = on != 0;
+  return MLC_OK;
+}
+
+int mlc_member_test_stall(mlc_ctx *x, int m, int polls) {
+  if (!member_ok(x, m) || polls < 0) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
+  x->mem[m].stall_polls = polls;
+  x->table_dirty = true;
+  return MLC_OK;
+}
+
+int mlc_set_solve_precision(mlc_ctx *x, int df_recurrence) {
+  if (!x) return MLC_ERR_INVALID;
+  if (x->step_open) return MLC_ERR_STATE;
+  x->key.L.solve_df = df_recurrence ? 1 : 0;
   return MLC_OK;
 }
 

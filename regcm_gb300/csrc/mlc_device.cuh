@@ -165,6 +165,10 @@ struct Dom {
   const R *tend;
   int red_blocks;
   int active;            // 0: an empty slot, every block returns at once
+  // test hook of the bounded waits (0 = off): the horizontal WAF's blocks
+  // wait this many polls on an mbarrier no copy completes, then record the
+  // fault, as they do for a copy that never lands
+  int stall_polls;
   // TMA tensor maps (CUtensorMap, 128 B each, 64-B aligned) of the wz fields,
   // [horizontal tile shape][field], for the horizontal WAF's halo tiles
   const void *tmap;

@@ -24,6 +24,7 @@ struct LaunchGeom {
   int nadv_r;            // advected fields of type R per member
   int nadv_d;            // advected FP64 fields per member (mixed: theta_v, Exner)
   int red_blocks;        // reduction blocks of the largest member
+  int solve_df;          // mixed solve: recurrence in double-float (1) or FP32 (0)
 };
 
 template <class R> struct Launch {

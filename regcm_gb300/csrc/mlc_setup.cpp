@@ -221,6 +221,53 @@ int mlc_setup_spectral(const mlc_params *p, int kz, const double *gmeanz, double
   return MLC_OK;
 }
 
+int mlc_exponential_nudging(int kz, double ztop, double high, double medium, double low,
+                            double *anudge) {
+  if (kz < 2 || !(ztop > 0.0) || !anudge) return MLC_ERR_INVALID;
+  if (!(high > 0.0) || !(medium > 0.0) || !(low > 0.0)) return MLC_ERR_INVALID;
+  std::vector<double> zita(kz + 1), zitah(kz);
+  mlc_setup_levels(kz, ztop, zita.data(), zitah.data());
+  // sigmazita (Share/mod_zita.F90:40-45) at full and half levels
+  auto sig = [&](double z) { return 1.0 - z / ztop; };
+  // the first full level k in 2..kz with sigma(k) > 0.4, else kz+1
+  int kmid = kz + 1;
+  for (int k = 2; k <= kz; ++k)
+    if (sig(zita[k - 1]) > 0.40) {
+      kmid = k;
+      break;
+    }
+  const double xo[3] = {sig(zita[0]), sig(zita[kmid - 1]), sig(zita[kz])};
+  const double yo[3] = {high, medium, low};
+  // spline1d with three knots and y2 = 0 at both ends: one interior value
+  // y2(2) = p(1), in the routine's own arithmetic (bfac = 1/6)
+  const double bfac = 1.0 / 6.0;
+  const double dxl = xo[1] - xo[0], dxr = xo[2] - xo[1];
+  const double dydxl = (yo[1] - yo[0]) / dxl, dydxr = (yo[2] - yo[1]) / dxr;
+  const double rtdxc = 0.5 / (dxl + dxr);
+  const double y2[3] = {0.0, rtdxc * (bfac * (dydxr - dydxl) - dxl * 0.0) + (-rtdxc * dxr) * 0.0, 0.0};
+  for (int k = 0; k < kz; ++k) {
+    const double xk = sig(zitah[k]);
+    if (xk < xo[0]) {
+      anudge[k] = yo[0];
+      continue;
+    }
+    if (xk >= xo[2]) {
+      anudge[k] = yo[2];
+      continue;
+    }
+    const int q = xo[1] > xk ? 0 : 1;  // interval [xo[q], xo[q+1])
+    const double dx = xo[q + 1] - xo[q];
+    const double rdx = 1.0 / dx;
+    const double ak = bfac * rdx * (y2[q + 1] - y2[q]);
+    const double bk = 0.5 * y2[q];
+    const double ck = rdx * (yo[q + 1] - yo[q]) - bfac * dx * (y2[q + 1] + y2[q] + y2[q]);
+    const double x = xk - xo[q];
+    const double xsq = x * x;
+    anudge[k] = ak * xsq * x + bk * xsq + ck * x + yo[q];
+  }
+  return MLC_OK;
+}
+
 int mlc_setup_relaxation(const mlc_dims *d, mlc_params *p, const double *zeta, double *hefc,
                          double *fcx, double *tnudge, double *ffilt, double *gmeanz_out) {
   if (!d || !p || !zeta || !hefc) return MLC_ERR_INVALID;
@@ -240,6 +287,19 @@ int mlc_setup_relaxation(const mlc_dims *d, mlc_params *p, const double *zeta, d
   for (int k = 0; k < kz; ++k)
     if (gmeanz[k] > kZzTop) ++nztop;
   p->nztop = (p->mo_top_nudge) ? nztop : 0;
+  if (!p->bdy_use_lehmann) {
+    // exponential nudging (Main/mod_bdycod.F90:538-544)
+    std::vector<double> anudge(kz);
+    int st = mlc_exponential_nudging(kz, p->mo_ztop, p->high_nudge, p->medium_nudge,
+                                     p->low_nudge, anudge.data());
+    if (st != MLC_OK) return st;
+    for (int k = 0; k < kz; ++k) {
+      double *col = hefc + (size_t)k * nsp;
+      col[0] = 1.0;
+      col[nsp - 1] = 0.0;
+      for (int n = 2; n <= nsp - 1; ++n) col[n - 1] = std::exp(-(double)(n - 1) / anudge[k]);
+    }
+  } else {
   // Lehmann weights (Main/mod_bdycod.F90:522-537)
   const double dta = p->dtsec / (double)p->mo_nadv;
   double cflmax = (300.0 * dta) / (2.0 * p->dx);
@@ -256,6 +316,7 @@ int mlc_setup_relaxation(const mlc_dims *d, mlc_params *p, const double *zeta, d
     col[0] = 1.0;
     col[nsp - 1] = 0.0;
     for (int n = 0; n < nsp - 2; ++n) col[n + 1] = w[n];
+  }
   }
   if (fcx) {
     fcx[0] = 1.0;

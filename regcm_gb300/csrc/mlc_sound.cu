@@ -369,7 +369,7 @@ constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
 // downward pass, after a proxy fence.  (Measured on the 512x512x41 step:
 // 0.73 ms of solves a step against 0.95 for the same thread-per-column
 // kernel with register prefetch of one level.)
-template <class R>
+template <class R, bool DFR>
 __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
   constexpr int NS = kSvStages;
   extern __shared__ __align__(16) float sv_smem[];
@@ -399,6 +399,10 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
   const float *__restrict__ cfz_l = cfz_h + F1;
   float *__restrict__ zfs = reinterpret_cast<float *>(D.wz_d[0]) + r0;
   float *__restrict__ mul = reinterpret_cast<float *>(D.wz_d[1]) + r0;
+  // DFR: the low parts of the eliminated w and of the multipliers, in the
+  // free lo planes of the same scratch allocations
+  float *__restrict__ w_lo = zfs + F;
+  float *__restrict__ mul_lo = mul + F;
   const float *__restrict__ zraw = D.zdiv2 + r0;
   const float *__restrict__ dtet = D.wz[2] + r0;
   const float *__restrict__ fmz = sa.fmz + r0;
@@ -455,10 +459,14 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
     float *st = stage(b);
     uint64_t *bar = &mbar[b];
     fence_proxy_async();
-    mbar_expect_tx(bar, (m <= kz ? 8u : 7u) * wb);
+    mbar_expect_tx(bar, (m <= kz ? (DFR ? 10u : 8u) : 7u) * wb);
     const int o = (m - 1) * PS, op = (m - 2) * PS;
     bulk_load(fld(st, 0), w + o + x0, wb, bar);
     if (m <= kz) bulk_load(fld(st, 1), mul + o + x0, wb, bar);
+    if (DFR && m <= kz) {
+      bulk_load(fld(st, 8), w_lo + o + x0, wb, bar);
+      bulk_load(fld(st, 9), mul_lo + o + x0, wb, bar);
+    }
     bulk_load(fld(st, 2), pai_h + op + x0, wb, bar);
     bulk_load(fld(st, 3), pai_l + op + x0, wb, bar);
     bulk_load(fld(st, 4), zfs + op + x0, wb, bar);
@@ -506,6 +514,7 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
     zfk = zf_of(kz, ak, s[kz * PS + ij_off]);
   }
   float wkp1 = 0.f;
+  F2 wnextd{wnext, 0.f}, wkp1d{0.f, 0.f};
   for (int u = 0; u < nd; ++u) {
     const int k = kz - u, m = k - 1;
     const int b = u % NS;
@@ -533,16 +542,31 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
       const F2 dp = two_sum(pai_m.hi - pai_k.hi, pai_m.lo - pai_k.lo);
       const F2 bal = df_add(ngdts, df_mul(F2{-zrd.hi, -zrd.lo}, dp));
       const float zr = df_f(zrd), pm = df_f(pai_m), pk = df_f(pai_k);
-      float zw = wold + df_f(bal);
-      zw = zw + rdrcv * zr * (pm * zf_m - pk * zfk);
       const float ff = sa.ffilt_r[k - 1];
       const float zu = rdt * am.fmz * zr * pm + ff;
       const float zd = rdt * ak.fmz * zr * pk + ff;
-      const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
-      wnext = zrapp * (zw + zd * wnext);
-      wkp1 = zrapp * zu;
-      w[o] = wnext;
-      mul[o] = wkp1;
+      if constexpr (DFR) {
+        // the recurrence in double-float: the explicit w keeps the hydrostatic
+        // balance's low part, the pivots and multipliers carry theirs
+        F2 zw = df_add_f(bal, wold);
+        zw = df_add_f(zw, rdrcv * zr * (pm * zf_m - pk * zfk));
+        const F2 den = df_add(two_sum(1.f + zd, zu), df_mul_f(F2{-wkp1d.hi, -wkp1d.lo}, zd));
+        const F2 zrapp = df_div(F2{1.f, 0.f}, den);
+        wnextd = df_mul(zrapp, df_add(zw, df_mul_f(wnextd, zd)));
+        wkp1d = df_mul_f(zrapp, zu);
+        w[o] = wnextd.hi;
+        w_lo[o] = wnextd.lo;
+        mul[o] = wkp1d.hi;
+        mul_lo[o] = wkp1d.lo;
+      } else {
+        float zw = wold + df_f(bal);
+        zw = zw + rdrcv * zr * (pm * zf_m - pk * zfk);
+        const float zrapp = 1.f / (1.f + zd + zu - zd * wkp1);
+        wnext = zrapp * (zw + zd * wnext);
+        wkp1 = zrapp * zu;
+        w[o] = wnext;
+        mul[o] = wkp1;
+      }
       zfk = zf_m;
       ak = am;
     }
@@ -559,9 +583,9 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
   const int nu = kz;  // up units: m = 2 .. kz+1
   if (t == 0)
     for (int v = 0; v < NS && v < nu; ++v) issue_up(v, (nd + v) % NS);
-  auto exner = [&](int m, float wm, float wmp, F2 pk, float zf, float fz, float sm, float fzf) {
+  auto exner = [&](int m, float wm, float dw, F2 pk, float zf, float fz, float sm, float fzf) {
     const int o = (m - 1) * PS + ij_off;
-    const float inc = rdrcv * (zf + (dtrdz * fz * (wm - wmp)));
+    const float inc = rdrcv * (zf + (dtrdz * fz * dw));
     const F2 d = df_mul_f(pk, inc);
     const F2 pn = df_add(pk, F2{-d.hi, -d.lo});
     pai_h[o] = pn.hi;
@@ -569,6 +593,7 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
     if (last && m >= 2) s[o] = (wm + sm) * fzf;
   };
   float wprev = act ? w[ij_off] : 0.f;  // w(1) = 0
+  F2 wprevd{wprev, 0.f};
   for (int v = 0; v < nu; ++v) {
     const int k = v + 2, gu = nd + v;
     const int b = gu % NS;
@@ -578,13 +603,26 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
       const float wel = f0[0];
       const F2 cp{f0[2 * kSvW], f0[3 * kSvW]};
       const float czf = f0[4 * kSvW], cfz_ = f0[5 * kSvW], cs = f0[6 * kSvW], cfzf = f0[7 * kSvW];
-      if (k <= kz) {
-        const float wk = wel + f0[kSvW] * wprev;
-        w[(k - 1) * PS + ij_off] = wk;
-        exner(k - 1, wprev, wk, cp, czf, cfz_, cs, cfzf);
-        wprev = wk;
+      if constexpr (DFR) {
+        if (k <= kz) {
+          const F2 wk = df_add(F2{wel, f0[8 * kSvW]},
+                               df_mul(F2{f0[kSvW], f0[9 * kSvW]}, wprevd));
+          const float wkf = df_f(wk);
+          w[(k - 1) * PS + ij_off] = wkf;
+          exner(k - 1, df_f(wprevd), df_diff(wprevd, wk), cp, czf, cfz_, cs, cfzf);
+          wprevd = wk;
+        } else {
+          exner(kz, df_f(wprevd), df_f(df_add_f(wprevd, -wel)), cp, czf, cfz_, cs, cfzf);
+        }
       } else {
-        exner(kz, wprev, wel, cp, czf, cfz_, cs, cfzf);
+        if (k <= kz) {
+          const float wk = wel + f0[kSvW] * wprev;
+          w[(k - 1) * PS + ij_off] = wk;
+          exner(k - 1, wprev, wprev - wk, cp, czf, cfz_, cs, cfzf);
+          wprev = wk;
+        } else {
+          exner(kz, wprev, wprev - wel, cp, czf, cfz_, cs, cfzf);
+        }
       }
     }
     if (__syncthreads_or(!landed)) {
@@ -1047,8 +1085,12 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
   // launch shape of LaunchGeom is not used)
   if constexpr (sizeof(R) == sizeof(float)) {
     const int tj = (L.jx - 1 + kSvW - 1) / kSvW;
-    k_solve_mixed<R><<<dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem), kSvW,
-                       (size_t)kSvStages * kSvStage * sizeof(float), s>>>(d, advoff, last ? 1 : 0);
+    const dim3 grid((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem);
+    const size_t smem = (size_t)kSvStages * kSvStage * sizeof(float);
+    if (L.solve_df)
+      k_solve_mixed<R, true><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0);
+    else
+      k_solve_mixed<R, false><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0);
   } else {
     const int tj = (L.jx - 1 + kDvW - 1) / kDvW;
     k_sound_solve<R><<<dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem), kDvW,

@@ -45,10 +45,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
 }
 // gives up after a bounded number of polls (a copy that never lands must not
 // hang the GPU); the caller records the fault
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
-  for (int it = 0; it < (1 << 18); ++it)
+__device__ __forceinline__ bool mbar_wait_polls(uint64_t *bar, unsigned parity, int polls) {
+  for (int it = 0; it < polls; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
+  return mbar_wait_polls(bar, parity, 1 << 18);
 }
 
 // orders this thread's earlier generic-proxy stores to global memory before

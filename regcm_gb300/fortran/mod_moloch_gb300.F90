@@ -52,6 +52,8 @@ module mod_moloch_gb300
     integer(c_int32_t) :: lrotllr, ipptls, present_qc, present_qi
     integer(c_int32_t) :: nspgx, nspgd, nztop, debug_level, precision
     real(c_double) :: dtrad
+    integer(c_int32_t) :: bdy_use_lehmann, ibltyp
+    real(c_double) :: high_nudge, medium_nudge, low_nudge
   end type mlc_params
 
   type, bind(c) :: mlc_static_ptrs
@@ -207,6 +209,11 @@ module mod_moloch_gb300
     prm%nspgx = nspgx
     prm%nspgd = nspgd
     prm%debug_level = debug_level
+    prm%bdy_use_lehmann = merge(1, 0, bdy_use_lehmann)
+    prm%ibltyp = ibltyp
+    prm%high_nudge = high_nudge
+    prm%medium_nudge = medium_nudge
+    prm%low_nudge = low_nudge
     ! the context is created in init_moloch, once zeta exists
   end subroutine allocate_moloch
 

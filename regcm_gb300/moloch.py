@@ -100,6 +100,12 @@ class MolochDomain:
     def set_graphs(self, on: bool):
         abi.check(self.lib.mlc_set_graphs(self._ctx, 1 if on else 0), "mlc_set_graphs")
 
+    def set_solve_precision(self, df_recurrence: bool):
+        """Mixed precision: the w-Exner recurrence in double-float (True,
+        the default) or FP32 (False)."""
+        abi.check(self.lib.mlc_set_solve_precision(self._ctx, 1 if df_recurrence else 0),
+                  "mlc_set_solve_precision")
+
     def autotune(self, steps_per_trial: int = 2) -> dict:
         return _autotune(self.lib, self._ctx, steps_per_trial)
 
@@ -262,6 +268,12 @@ class MolochBatch:
 
     def set_graphs(self, on: bool):
         abi.check(self.lib.mlc_set_graphs(self._ctx, 1 if on else 0), "mlc_set_graphs")
+
+    def set_solve_precision(self, df_recurrence: bool):
+        """Mixed precision: the w-Exner recurrence in double-float (True,
+        the default) or FP32 (False)."""
+        abi.check(self.lib.mlc_set_solve_precision(self._ctx, 1 if df_recurrence else 0),
+                  "mlc_set_solve_precision")
 
     def launches_per_step(self) -> int:
         return self.lib.mlc_launches_per_step(self._ctx)

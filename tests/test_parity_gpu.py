@@ -77,6 +77,13 @@ CASES = {
                               seed=7, wind=15.0, tracer=True, name="nadv2"),
     "moist_nsound5": lambda: cs.build(40, 36, 10, dx=3000.0, dt=20.0, nsound=5, moist=True,
                                       seed=9, jet=True, name="moist5"),
+    # exponential relaxation weights (bdy_use_lehmann = .false., the
+    # reference's default) and the microphysics classes with more species
+    "dry_exp_nudging": lambda: small_dry(lehmann=False),
+    "moist_exp_nudging": lambda: small_moist(lehmann=False),
+    "moist_ipptls3": lambda: small_moist(ipptls=3),
+    "moist_ipptls4": lambda: small_moist(ipptls=4),
+    "moist_ipptls5": lambda: small_moist(ipptls=5),
 }
 
 
@@ -95,7 +102,7 @@ def test_one_step(name):
     assert dg.xbctime == do.xbctime
 
 
-@pytest.mark.parametrize("name", ["dry_tracer", "moist"])
+@pytest.mark.parametrize("name", ["dry_tracer", "moist", "moist_exp_nudging", "moist_ipptls5"])
 def test_hundred_steps(name):
     case = CASES[name]()
     g, o, dg, do = run_pair(case, 100, chunk=25)

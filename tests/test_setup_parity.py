@@ -167,3 +167,46 @@ def test_case_from_oracle_setup_is_identical(make):
     for n in a.bdy:
         for x, y in zip(a.bdy[n], b.bdy[n]):
             assert np.array_equal(x, y), n
+
+
+@pytest.mark.parametrize("kz,ztop,hml", [(30, 25000.0, (3.0, 2.0, 1.0)), (41, 25000.0, (3.0, 2.0, 1.0)),
+                                         (18, 30000.0, (5.0, 1.5, 0.5)), (60, 20000.0, (2.0, 2.5, 1.0))])
+def test_exponential_nudging(kz, ztop, hml):
+    lib, ol = abi.load(), orc.load()
+    a, b = np.zeros(kz), np.zeros(kz)
+    assert lib.mlc_exponential_nudging(kz, ztop, *hml, abi.dptr(a)) == 0
+    assert ol.orc_exponential_nudging(kz, ztop, *hml, abi.dptr(b)) == 0
+    assert np.array_equal(a, b)
+    assert np.all(a > 0)
+
+
+def test_exponential_nudging_known_answers():
+    lib = abi.load()
+    # equal strengths: the spline is the constant
+    a = np.zeros(30)
+    assert lib.mlc_exponential_nudging(30, 25000.0, 2.0, 2.0, 2.0, abi.dptr(a)) == 0
+    assert np.all(a == 2.0)
+    # the reference's strengths 3, 2, 1 fall from the top (k = 1) to the surface
+    assert lib.mlc_exponential_nudging(30, 25000.0, 3.0, 2.0, 1.0, abi.dptr(a)) == 0
+    assert np.all(np.diff(a) < 0) and 2.9 < a[0] <= 3.0 and 1.0 <= a[-1] < 1.1
+
+
+@pytest.mark.parametrize("moist", [False, True])
+def test_exponential_relaxation_weights(moist):
+    """hefc with bdy_use_lehmann = .false.: the library's setup equals the
+    oracle's bit for bit, and the weights are exp(-(n-1)/anudge(k))."""
+    c = cs.build(30, 26, 20, dx=12000.0, dt=60.0, nsound=3, moist=moist, seed=6, lehmann=False)
+    d, p, st = c.dims, c.params, c.static
+    assert p.bdy_use_lehmann == 0 and p.nspgx >= 6
+    hefc = np.zeros_like(st["hefc"], order="F")
+    fcx = np.zeros(p.nspgx)
+    tn, ff = np.zeros(d.kz), np.zeros(d.kz)
+    nz = C.c_int()
+    orc.load().orc_setup_relaxation(C.byref(d), C.byref(p), abi.dptr(st["zeta"]), abi.dptr(hefc),
+                                    abi.dptr(fcx), abi.dptr(tn), abi.dptr(ff), C.byref(nz))
+    assert np.array_equal(hefc, st["hefc"])
+    an = np.zeros(d.kz)
+    abi.load().mlc_exponential_nudging(d.kz, p.mo_ztop, 3.0, 2.0, 1.0, abi.dptr(an))
+    n = np.arange(2, p.nspgx)
+    assert np.allclose(st["hefc"][1:-1, :], np.exp(-(n - 1)[:, None] / an[None, :]), rtol=1e-15)
+    assert np.all(st["hefc"][0] == 1.0) and np.all(st["hefc"][-1] == 0.0)
