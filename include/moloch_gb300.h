@@ -145,6 +145,8 @@ typedef struct mlc_state_ptrs {
   double *qx;     /* (jx-1,iy-1,kz,nqx) */
   double *trac;   /* (jx-1,iy-1,kz,ntr), may be NULL when ntr = 0 */
   double *ps;     /* (jx-1,iy-1) surface pressure */
+  double *tke;    /* (jx-1,iy-1,kz+1) turbulent kinetic energy [m2/s2] at
+                     the interfaces; used when ibltyp = 2, else may be NULL */
 } mlc_state_ptrs;
 
 /* Lateral boundary data: index 0 = b0, 1 = b1 (v3dbound%b0/%b1). */
@@ -265,6 +267,7 @@ typedef struct mlc_tend_ptrs {
   const double *vten;    /* (jx-3,iy-3,kz) meridional wind (cross points) [m/s^2]   */
   const double *qxten;   /* (jx-3,iy-3,kz,nqx) water species [kg/kg/s]              */
   const double *chiten;  /* (jx-3,iy-3,kz,ntr) tracers                              */
+  const double *tketen;  /* (jx-3,iy-3,kz+1) TKE (ibltyp = 2) [m2/s3]                */
 } mlc_tend_ptrs;
 int mlc_step_dynamics(mlc_ctx *ctx);
 int mlc_member_set_tendencies(mlc_ctx *ctx, int m, const mlc_tend_ptrs *t);

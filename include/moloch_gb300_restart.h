@@ -37,6 +37,8 @@ typedef struct mlc_sav_fields {
   double *qx;    /* atm_qx  (jx-1,iy-1,kz,nqx)  dims (jcross,icross,khalf,nqx)  */
   double *ps;    /* ps      (jx-1,iy-1)                                         */
   double *trac;  /* trac    (jx-1,iy-1,kz,ntr)  only when ntr > 0 (ichem = 1)   */
+  double *tke;   /* atm_tke (jx-1,iy-1,kz+1)    dims (jcross,icross,kfull);
+                    written and read when not NULL (ibltyp = 2)               */
 } mlc_sav_fields;
 
 /* Write the fields to `path` with the global attributes idatex and

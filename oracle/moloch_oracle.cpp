@@ -70,6 +70,8 @@ struct Oracle {
   F3 u, v, w, pai, tetav, t, tvirt, ux, vx, p, rho, qsat;
   std::vector<F3> qx, trac;
   F2<double> ps;
+  bool use_tke = false;   // ibltyp = 2
+  F3 tke, tkex;           // (jce, ice, 1:kzp1) and its copy at the levels
 
   // ---- boundary ----
   F3 xtb[2], xqb[2], xpaib[2], xlb[2], xib[2], dub[2], dvb[2];
@@ -78,7 +80,7 @@ struct Oracle {
   double xbctime = 0, dtbdys = 1, rtb = 1;
 
   // ---- physics tendencies (jci x ici, Main/mod_atm_interface.F90:606-617) ----
-  F3 tten, uten, vten;
+  F3 tten, uten, vten, tketen;
   std::vector<F3> qxten, chiten;
   bool step_open = false;
 
@@ -210,6 +212,13 @@ int Oracle::create(const mlc_dims *d, const mlc_params *pp) {
   vten.init(jci1, jci2, ici1, ici2, 1, kz);
   qxten.assign(nqx, F3()); for (auto &f : qxten) f.init(jci1, jci2, ici1, ici2, 1, kz);
   chiten.assign(ntr, F3()); for (auto &f : chiten) f.init(jci1, jci2, ici1, ici2, 1, kz);
+  // Main/mod_atm_interface.F90:611-612, Main/mod_moloch.F90:184
+  use_tke = prm.ibltyp == 2;
+  if (use_tke) {
+    tke.init(jce1, jce2, ice1, ice2, 1, kzp1);
+    tketen.init(jci1, jci2, ici1, ici2, 1, kzp1);
+    tkex.init(jce1, jce2, ice1, ice2, 1, kz);
+  }
 
   for (int b = 0; b < 2; ++b) {
     for (F3 *f : {&xtb[b], &xqb[b], &xpaib[b], &xlb[b], &xib[b]})
@@ -364,6 +373,7 @@ void Oracle::reset_tendencies() {
   std::fill(vten.d.begin(), vten.d.end(), 0.0);
   for (auto &f : qxten) std::fill(f.d.begin(), f.d.end(), 0.0);
   for (auto &f : chiten) std::fill(f.d.begin(), f.d.end(), 0.0);
+  if (use_tke) std::fill(tketen.d.begin(), tketen.d.end(), 0.0);
   std::fill(s.d.begin(), s.d.end(), 0.0);
   for (int k = 1; k <= kz; ++k)
     for (int i = ici1; i <= ici2; ++i)
@@ -551,6 +561,7 @@ void Oracle::divergence_damping(double dts) {
 void Oracle::advection(double dta) {
   uvstagtouvx();
   zstagtoh(w, wx);
+  if (use_tke) zstagtoh(tke, tkex);
   wafone(tetav, dta);
   wafone(pai, dta);
   wafone(ux, dta);
@@ -559,6 +570,7 @@ void Oracle::advection(double dta) {
   wafone(qx[0], dta);
   if (prm.ipptls > 0)
     for (int n = 1; n < nqx; ++n) wafone(qx[n], dta);  // iqfrst = iqc
+  if (use_tke) wafone(tkex, dta);
   for (int n = 0; n < ntr; ++n) wafone(trac[n], dta);   // ichem = 1
   // curvature terms :809-825
   if (prm.lrotllr) {
@@ -583,6 +595,7 @@ void Oracle::advection(double dta) {
   }
   uvxtouvstag();
   htozstag(wx, w);
+  if (use_tke) htozstag(tkex, tke);
 }
 
 // Main/mod_moloch.F90:838-1042 (do_vadvtwice = .true.)
@@ -956,6 +969,15 @@ void Oracle::bdyval() {
         bool inflow = side == 0 ? (u(jd, i, k) > 0.0) : (u(jd, i, k) < 0.0);
         w(jb, i, k) = inflow ? 0.0 : w(jin, i, k);
       }
+    if (use_tke) {  // :1684-1695, :1742-1753
+      for (int i = ici1; i <= ici2; ++i) tke(jb, i, 1) = tkemin;
+      for (int k = 2; k <= kz; ++k)
+        for (int i = ici1; i <= ici2; ++i) {
+          double us = u(jd, i, k) + u(jd, i, k - 1);
+          bool inflow = side == 0 ? (us > 0.0) : (us < 0.0);
+          tke(jb, i, k + 1) = inflow ? tkemin : tke(jin, i, k + 1);
+        }
+    }
   }
   // south and north: corners included
   for (int side = 0; side < 2; ++side) {
@@ -993,6 +1015,15 @@ void Oracle::bdyval() {
         bool inflow = side == 0 ? (v(j, id, k) > 0.0) : (v(j, id, k) < 0.0);
         w(j, ib, k) = inflow ? 0.0 : w(j, iin, k);
       }
+    if (use_tke) {  // :1800-1811, :1858-1869
+      for (int j = jce1; j <= jce2; ++j) tke(j, ib, 1) = tkemin;
+      for (int k = 2; k <= kz; ++k)
+        for (int j = jce1; j <= jce2; ++j) {
+          double vs = v(j, id, k) + v(j, id, k - 1);
+          bool inflow = side == 0 ? (vs > 0.0) : (vs < 0.0);
+          tke(j, ib, k + 1) = inflow ? tkemin : tke(j, iin, k + 1);
+        }
+    }
   }
   if (ntr > 0) {
     // chem_bdyval_uncoupled, time-dependent data: x1 = (xbctime + dt)/dtbdys
@@ -1119,7 +1150,7 @@ void Oracle::mkslice() {
           if (trac[n](j, i, k) < 1.0e-50) trac[n](j, i, k) = 0.0;
 }
 
-// Main/mod_moloch.F90:1403-1443 (TKE is out of scope)
+// Main/mod_moloch.F90:1403-1443
 void Oracle::status_update(double dtinc) {
   for (int k = 1; k <= kz; ++k)
     for (int i = ici1; i <= ici2; ++i)
@@ -1134,6 +1165,13 @@ void Oracle::status_update(double dtinc) {
         for (int j = jci1; j <= jci2; ++j) {
           qx[n](j, i, k) = qx[n](j, i, k) + dtinc * qxten[n](j, i, k);
           if (qx[n](j, i, k) < qxcheckval[n]) qx[n](j, i, k) = qxzeroval[n];
+        }
+  if (use_tke)
+    for (int k = 1; k <= kzp1; ++k)
+      for (int i = ici1; i <= ici2; ++i)
+        for (int j = jci1; j <= jci2; ++j) {
+          tke(j, i, k) = tke(j, i, k) + dtinc * tketen(j, i, k);
+          if (tke(j, i, k) < tkemin) tke(j, i, k) = tkemin;
         }
   for (int n = 0; n < ntr; ++n)
     for (int k = 1; k <= kz; ++k)
@@ -1224,6 +1262,7 @@ int orc_set_state(void *h, const mlc_state_ptrs *st) {
   for (int n = 0; n < o.nqx; ++n) o.qx[n].load(st->qx + n * n3);
   for (int n = 0; n < o.ntr; ++n) o.trac[n].load(st->trac + n * n3);
   std::memcpy(o.ps.d.data(), st->ps, o.ps.d.size() * sizeof(double));
+  if (o.use_tke && st->tke) o.tke.load(st->tke);
   // init_moloch: w(:,:,1) = 0 (Main/mod_moloch.F90:264-266)
   for (int i = o.ice1; i <= o.ice2; ++i)
     for (int j = o.jce1; j <= o.jce2; ++j) o.w(j, i, 1) = 0.0;
@@ -1242,6 +1281,7 @@ int orc_get_state(void *h, const mlc_state_ptrs *st) {
   if (st->qx) for (int n = 0; n < o.nqx; ++n) o.qx[n].store(st->qx + n * n3);
   if (st->trac) for (int n = 0; n < o.ntr; ++n) o.trac[n].store(st->trac + n * n3);
   if (st->ps) std::memcpy(st->ps, o.ps.d.data(), o.ps.d.size() * sizeof(double));
+  if (o.use_tke && st->tke) o.tke.store(st->tke);
   return MLC_OK;
 }
 
@@ -1298,6 +1338,7 @@ int orc_set_tendencies(void *h, const mlc_tend_ptrs *tp) {
   if (tp->vten) o.vten.load(tp->vten);
   if (tp->qxten) for (int n = 0; n < o.nqx; ++n) o.qxten[n].load(tp->qxten + n * n3);
   if (tp->chiten) for (int n = 0; n < o.ntr; ++n) o.chiten[n].load(tp->chiten + n * n3);
+  if (o.use_tke && tp->tketen) o.tketen.load(tp->tketen);
   return MLC_OK;
 }
 
@@ -1326,6 +1367,7 @@ int orc_restart_state(const mlc_dims *d, const mlc_sav_fields *f, const mlc_stat
   std::memcpy(st->pai, f->pai, nj * ni * kz * sizeof(double));
   std::memcpy(st->qx, f->qx, nj * ni * kz * d->nqx * sizeof(double));
   if (d->ntr > 0) std::memcpy(st->trac, f->trac, nj * ni * kz * d->ntr * sizeof(double));
+  if (f->tke && st->tke) std::memcpy(st->tke, f->tke, nj * ni * (kz + 1) * sizeof(double));
   std::memcpy(st->ps, f->ps, nj * ni * sizeof(double));
   for (size_t k = 0; k < kz; ++k)
     for (size_t i = 0; i < ni; ++i)

@@ -49,6 +49,9 @@ constexpr double ep1 = amd / amw - d_one;                 // :383-386
 constexpr double ep2 = amw / amd;
 
 // Main/mpplib/mod_runparams.F90:184-192
+// tkemin of the UW PBL (ibltyp = 2): Main/mod_pbl_interface.F90:68 takes
+// uwtkemin, Main/pbllib/mod_pbl_uwtcm.F90:81
+constexpr double tkemin = 1.0e-3;
 constexpr double qxcheckval[10] = {1.0e-8, 1.0e-16, 1.0e-16, 1.0e-16, 1.0e-16,
                                    1.0e-16, 1.0e-16, 1.0e10, 100.0, 0.01};
 constexpr double qxzeroval[10] = {1.0e-8, 0.0, 0.0, 0.0, 0.0,

@@ -76,7 +76,7 @@ class mlc_static_ptrs(C.Structure):
 
 
 STATE_FIELDS = ["u", "v", "w", "pai", "tetav", "t", "tvirt", "ux", "vx", "p", "rho", "qsat",
-                "qx", "trac", "ps"]
+                "qx", "trac", "ps", "tke"]
 
 
 class mlc_state_ptrs(C.Structure):
@@ -91,7 +91,7 @@ class mlc_bdy_ptrs(C.Structure):
 
 
 # physics tendencies on the interior jci x ici, (jx-3, iy-3, kz[, n])
-TEND_FIELDS = ["tten", "uten", "vten", "qxten", "chiten"]
+TEND_FIELDS = ["tten", "uten", "vten", "qxten", "chiten", "tketen"]
 
 
 class mlc_tend_ptrs(C.Structure):
@@ -99,7 +99,7 @@ class mlc_tend_ptrs(C.Structure):
 
 
 # the MOLOCH variables of a SAV restart file
-SAV_FIELDS = ["u", "v", "w", "t", "pai", "qx", "ps", "trac"]
+SAV_FIELDS = ["u", "v", "w", "t", "pai", "qx", "ps", "trac", "tke"]
 
 
 class mlc_sav_fields(C.Structure):

@@ -199,6 +199,8 @@ class Case:
         out["qxten"] = species(self.state["qx"][1:-1, 1:-1], 1e-9)
         if d.ntr:
             out["chiten"] = species(self.state["trac"][1:-1, 1:-1], 1e-7)
+        if self.params.ibltyp == 2:
+            out["tketen"] = species(self.state["tke"][1:-1, 1:-1], 1e-4)
         return out
 
     def empty_sav(self) -> dict:
@@ -207,6 +209,8 @@ class Case:
                for n in ("u", "v", "w", "t", "pai", "qx", "ps")}
         if self.dims.ntr:
             out["trac"] = np.zeros_like(self.state["trac"], order="F")
+        if "tke" in self.state:
+            out["tke"] = np.zeros_like(self.state["tke"], order="F")
         return out
 
     @staticmethod
@@ -241,13 +245,15 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
           theta_noise: float = 0.1, tracer: bool = False, precision: int = abi.MLC_PREC_FP64,
           name: str = "case", debug_level: int = 1, lrotllr: bool = False,
           apply_bdy: bool = True, spectral: bool = False, dtrad: float = 1800.0,
-          lehmann: bool = True, ipptls: int | None = None, setup=None) -> Case:
+          lehmann: bool = True, ipptls: int | None = None, tke: bool = False,
+          setup=None) -> Case:
     """Build one synthetic domain of nx x ny cross points and kz levels.
     `lehmann` picks Lehmann's relaxation weights (else exponential nudging
     with the reference's default strengths 3, 2, 1); `ipptls` the
     microphysics class of a moist domain (default 2; 3-5 add species that
-    start at zero); `setup` is the backend of the static fields (default:
-    the library's)."""
+    start at zero); `tke` runs the UW PBL's TKE (ibltyp = 2: a boundary-
+    layer profile at the interfaces, advected by the step); `setup` is the
+    backend of the static fields (default: the library's)."""
     su = setup or LibrarySetup()
     jx, iy = nx + 1, ny + 1
     if ipptls is None:
@@ -271,7 +277,7 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
     p.precision = precision
     p.dtbdys = 6.0 * 3600.0
     p.bdy_use_lehmann = 1 if lehmann else 0
-    p.ibltyp = 1
+    p.ibltyp = 2 if tke else 1
     p.high_nudge, p.medium_nudge, p.low_nudge = 3.0, 2.0, 1.0
     p.nspgx, p.nspgd = su.nspg(jx, iy, dx / 1000.0, lehmann)
 
@@ -418,6 +424,13 @@ def build(nx: int, ny: int, kz: int, *, dx: float, dt: float, nsound: int, nadv:
     }
     if tracer:
         state["trac"] = np.array(trac, order="F")
+    if tke:
+        # TKE at the interfaces (jx-1, iy-1, kz+1): a boundary-layer profile
+        # decaying over 600 m above the ground, seeded +-10 % noise, over the
+        # UW floor 1e-3 m2/s2
+        zf = st["zetaf"]
+        noise = splitmix64(seed * 7919 + 5, int(zf.size)).reshape(zf.shape, order="F")
+        state["tke"] = np.asfortranarray(1.0e-3 + np.exp(-zf / 600.0) * (0.9 + 0.2 * noise))
     keep = {k: v for k, v in st.items()}
     case = Case(name=name, dims=dims, params=p, static=keep, state=state, bdy=bdy)
     return case

@@ -147,14 +147,14 @@ __device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) 
 }
 
 // The advected fields of a member, in the reference's order (tetav, pai,
-// ux, vx, wx, qv, qx(iqfrst:nqx) when ipptls > 0, trac; advection,
-// Main/mod_moloch.F90:781-807).  Table 0 holds the fields of type R: all of
+// ux, vx, wx, qv, qx(iqfrst:nqx) when ipptls > 0, tkex when ibltyp = 2,
+// trac; advection, Main/mod_moloch.F90:781-807).  Table 0 holds the fields of type R: all of
 // them in FP64, all but theta_v and Exner in a mixed member, whose two FP64
 // fields form table 1.  cur is the field's current half, out the other.
 template <class R>
 __device__ __forceinline__ int n_table_r(const Dom<R> &D) {
   const int nfix = sizeof(R) == sizeof(double) ? 2 : 0;
-  return nfix + 4 + (D.c.ipptls > 0 ? D.g.nqx - 1 : 0) + D.g.ntr;
+  return nfix + 4 + (D.c.ipptls > 0 ? D.g.nqx - 1 : 0) + D.c.tke + D.g.ntr;
 }
 
 template <class R>
@@ -180,6 +180,14 @@ __device__ __forceinline__ void field_r(const Dom<R> &D, int f, int adv, const R
     return;
   }
   f -= nq;
+  if (D.c.tke) {
+    if (f == 0) {
+      cur = D.tkex[adv];
+      out = D.tkex[adv ^ 1];
+      return;
+    }
+    f -= 1;
+  }
   cur = D.trac[adv] + (size_t)f * F;
   out = D.trac[adv ^ 1] + (size_t)f * F;
 }
@@ -241,6 +249,13 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
     else if (k == kz) a = R(0.5) * (w[o + PS] + w[o]);
     else a = R(0.5625) * (w[o + PS] + w[o]) - R(0.0625) * (w[o + 2 * PS] + w[o - PS]);
     wx[o] = a;
+    if (D.c.tke) {
+      // zstagtoh(tke, tkex) (Main/mod_moloch.F90:782-784)
+      const R *__restrict__ tk = D.tke;
+      if (k == 1 || k == kz) a = R(0.5) * (tk[o + PS] + tk[o]);
+      else a = R(0.5625) * (tk[o + PS] + tk[o]) - R(0.0625) * (tk[o + 2 * PS] + tk[o - PS]);
+      D.tkex[adv][o] = a;
+    }
     if constexpr (sizeof(R) == sizeof(double)) {
       // the vertical WAF update's factor s(k)*zu(k) - s(k+1)*zd(k), once for
       // all fields (FP64 arithmetic is the FP64 path's bound)
@@ -862,6 +877,13 @@ __global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advof
       else if (k == kz) a = R(0.5) * (wx[o] + wx[o - PS]);
       else a = R(0.5625) * (wx[o] + wx[o - PS]) - R(0.0625) * (wx[o + PS] + wx[o - 2 * PS]);
       w[o] = a;
+      if (D.c.tke) {
+        // htozstag(tkex, tke) (Main/mod_moloch.F90:831-834)
+        const R *__restrict__ tx = D.tkex[adv];
+        if (k == 2 || k == kz) a = R(0.5) * (tx[o] + tx[o - PS]);
+        else a = R(0.5625) * (tx[o] + tx[o - PS]) - R(0.0625) * (tx[o + PS] + tx[o - 2 * PS]);
+        D.tke[o] = a;
+      }
     }
   }
 }

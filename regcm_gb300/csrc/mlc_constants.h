@@ -66,6 +66,10 @@ MLC_HD inline double qx_zero(int n) {
   }
 }
 
+// Floor of the turbulent kinetic energy with the UW PBL (ibltyp = 2):
+// tkemin = uwtkemin (Main/mod_pbl_interface.F90:68, Main/pbllib/mod_pbl_uwtcm.F90:81).
+constexpr double kTkeMin = 1.0e-3;
+
 // Height above which top nudging and the w sponge act (Main/mod_bdycod.F90:121).
 constexpr double kZzTop = 18000.0;
 // Sponge amplitude (Main/mod_init.F90:62).

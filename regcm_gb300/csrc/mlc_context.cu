@@ -60,7 +60,7 @@ T *W(const T *p) { return const_cast<T *>(p); }
 
 // Advected fields of type R per member (the table order of mlc_advect.cu).
 int n_table_r(const mlc_dims &d, const mlc_params &p, bool f64) {
-  return (f64 ? 2 : 0) + 4 + (p.ipptls > 0 ? d.nqx - 1 : 0) + d.ntr;
+  return (f64 ? 2 : 0) + 4 + (p.ipptls > 0 ? d.nqx - 1 : 0) + (p.ibltyp == 2 ? 1 : 0) + d.ntr;
 }
 
 // Doubles of the packed state of one domain (the staging buffer's size).
@@ -68,7 +68,8 @@ size_t state_elems(const mlc_dims &d) {
   const size_t c2 = (size_t)(d.jx - 1) * (d.iy - 1);
   const size_t u3 = (size_t)d.jx * (d.iy - 1) * d.kz, v3 = (size_t)(d.jx - 1) * d.iy * d.kz;
   const size_t c3 = c2 * d.kz;
-  return u3 + v3 + c2 * (d.kz + 1) + c3 * (9 + d.nqx + d.ntr) + c2;
+  // w and tke (kz+1 levels), the cross-point fields, species and ps
+  return u3 + v3 + 2 * c2 * (d.kz + 1) + c3 * (9 + d.nqx + d.ntr) + c2;
 }
 
 Geom make_geom(const mlc_dims &d, int elem_bytes) {
@@ -124,6 +125,7 @@ Scal make_scal(const mlc_params &p) {
   c.dxrdtf = c.dxf / c.dtsoundf;
   c.spectral = p.mo_spectral_nudge;
   c.dtrad = p.dtrad;
+  c.tke = p.ibltyp == 2 ? 1 : 0;
   return c;
 }
 
@@ -141,7 +143,9 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
     D.qx[h] = cv.take<R>(F * d.nqx);
     D.trac[h] = d.ntr ? cv.take<R>(F * d.ntr) : nullptr;
     D.pai[h] = cv.take<double>(F); D.tetav[h] = cv.take<double>(F);
+    D.tkex[h] = p.ibltyp == 2 ? cv.take<R>(F) : nullptr;
   }
+  D.tke = p.ibltyp == 2 ? cv.take<R>(F1) : nullptr;
   D.w = cv.take<R>(F1); D.t = cv.take<R>(F); D.tvirt = cv.take<R>(F); D.p = cv.take<R>(F);
   D.rho = cv.take<R>(F); D.qsat = cv.take<R>(F); D.ps = cv.take<double>(P2);
   D.s = cv.take<R>(F1); D.zdiv2 = cv.take<R>(F); D.tetavf = cv.take<double>(F1);
@@ -310,6 +314,7 @@ struct GraphKey {
   LaunchGeom L;
   int any_copy;   // some member keeps non-advected species (ipptls = 0)
   int any_curv;   // some member has non-zero curvature terms
+  int any_tke;    // the members carry TKE (ibltyp = 2)
 };
 
 }  // namespace
@@ -498,6 +503,7 @@ int refresh(mlc_ctx *x) {
   L.red_blocks = 0;
   k.any_copy = 0;
   k.any_curv = 0;
+  k.any_tke = 0;
   for (size_t slot = 0; slot < x->mem.size(); ++slot) {
     Member &m = x->mem[slot];
     if (!m.used) continue;
@@ -517,6 +523,7 @@ int refresh(mlc_ctx *x) {
     L.red_blocks = std::max(L.red_blocks, D.red_blocks);
     if (x->prm.ipptls == 0 && m.dims.nqx > 1) k.any_copy = 1;
     if (m.c.curvature) k.any_curv = 1;
+    if (m.c.tke) k.any_tke = 1;
   }
   L.nmem = (int)t.size();
   if (!t.empty()) {
@@ -618,6 +625,7 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr, int phase = kStepAll) {
   } else {
     REC("end_status", K::end_cross_split(L, d, uvo, ao, true, s)); ++nl;
   }
+  if (x->key.any_tke) { REC("end_tke", K::end_tke(L, d, phase == kStepAll, s)); ++nl; }
   REC("end_uvstag", K::end_uvstag(L, d, uvo, ao, s)); ++nl;
   REC("end_reduce", K::end_reduce(L, d, uvo, ao, s)); nl += 2;
   return nl;
@@ -1079,6 +1087,9 @@ int upload_state_impl(mlc_ctx *x, int slot, const mlc_state_ptrs *h) {
     const size_t c2 = (size_t)(jx - 1) * (iy - 1);
     MLC_CHK(put3<double>(x, g, h->ps, st.ps, jx - 1, iy - 1, 1, adv(c2)));
   }
+  if (h->tke && st.tke)
+    MLC_CHK(put3<R>(x, g, h->tke, st.tke, jx - 1, iy - 1, kz + 1,
+                    adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
   // init_moloch: w(:,:,1) = 0 (Main/mod_moloch.F90:264-266)
   if (h->w) MLC_TRY(cudaMemsetAsync(st.w, 0, g.PS * sizeof(R), x->stream));
   return cuda_status(cudaStreamSynchronize(x->stream));
@@ -1117,6 +1128,9 @@ int download_state_impl(mlc_ctx *x, int slot, const mlc_state_ptrs *h) {
     const size_t c2 = (size_t)(jx - 1) * (iy - 1);
     MLC_CHK(get3<double>(x, g, st.ps, h->ps, jx - 1, iy - 1, 1, adv(c2)));
   }
+  if (h->tke && st.tke)
+    MLC_CHK(get3<R>(x, g, st.tke, h->tke, jx - 1, iy - 1, kz + 1,
+                    adv((size_t)(jx - 1) * (iy - 1) * (kz + 1))));
   return cuda_status(cudaStreamSynchronize(x->stream));
 }
 
@@ -1286,8 +1300,10 @@ int set_tendencies_impl(mlc_ctx *x, Member &mb, const mlc_tend_ptrs *t) {
   const Geom &g = mb.g;
   const int nf = 3 + mb.dims.nqx + mb.dims.ntr;
   const size_t F = g.field3();
+  // tketen (kz+1 planes) follows the kz-plane fields when ibltyp = 2
+  const size_t elems = (size_t)nf * F + (mb.c.tke ? F + g.PS : 0);
   if (!mb.tend_raw) {
-    const size_t bytes = (size_t)nf * F * sizeof(R);
+    const size_t bytes = elems * sizeof(R);
     if (x->budget && x->in_use + bytes > x->budget) return MLC_ERR_BUDGET;
     cudaError_t e = cudaMallocFromPoolAsync(&mb.tend_raw, bytes, x->pool, x->stream);
     if (e != cudaSuccess) {
@@ -1300,7 +1316,7 @@ int set_tendencies_impl(mlc_ctx *x, Member &mb, const mlc_tend_ptrs *t) {
   }
   R *base = static_cast<R *>(mb.tend_raw);
   // NULL arrays leave zero, as reset_tendencies does at every step's start
-  MLC_TRY(cudaMemsetAsync(base, 0, (size_t)nf * F * sizeof(R), x->stream));
+  MLC_TRY(cudaMemsetAsync(base, 0, elems * sizeof(R), x->stream));
   const int nj = mb.dims.jx - 3, ni = mb.dims.iy - 3, kz = mb.dims.kz;
   const size_t n3 = (size_t)nj * ni * kz;
   const size_t at22 = g.at2(2, 2);
@@ -1311,6 +1327,8 @@ int set_tendencies_impl(mlc_ctx *x, Member &mb, const mlc_tend_ptrs *t) {
   for (int n = 0; n < mb.dims.ntr && t->chiten; ++n)
     MLC_CHK(put3<R>(x, g, t->chiten + n * n3, base + (size_t)(3 + mb.dims.nqx + n) * F + at22, nj, ni,
                     kz, 0));
+  if (mb.c.tke && t->tketen)
+    MLC_CHK(put3<R>(x, g, t->tketen, base + (size_t)nf * F + at22, nj, ni, kz + 1, 0));
   return cuda_status(cudaStreamSynchronize(x->stream));
 }
 
@@ -1551,12 +1569,15 @@ int mlc_member_write_sav(mlc_ctx *x, int m, const char *path, const char *idatex
   const size_t jx = d.jx, iy = d.iy, kz = d.kz, c3 = (jx - 1) * (iy - 1) * kz;
   std::vector<double> u(jx * (iy - 1) * kz), v((jx - 1) * iy * kz), w((jx - 1) * (iy - 1) * (kz + 1));
   std::vector<double> t(c3), pai(c3), qx(c3 * d.nqx), ps((jx - 1) * (iy - 1)), trac(c3 * d.ntr);
+  const bool tke = x->mem[m].c.tke != 0;
+  std::vector<double> tk(tke ? (jx - 1) * (iy - 1) * (kz + 1) : 0);
   mlc_state_ptrs sp{};
   sp.u = u.data(); sp.v = v.data(); sp.w = w.data(); sp.t = t.data(); sp.pai = pai.data();
   sp.qx = qx.data(); sp.ps = ps.data(); sp.trac = d.ntr ? trac.data() : nullptr;
+  sp.tke = tke ? tk.data() : nullptr;
   MLC_CHK(mlc_member_download_state(x, m, &sp));
   mlc_sav_fields f{u.data(), v.data(), w.data(), t.data(), pai.data(), qx.data(), ps.data(),
-                   d.ntr ? trac.data() : nullptr};
+                   d.ntr ? trac.data() : nullptr, tke ? tk.data() : nullptr};
   return mlc_sav_write(path, &d, &f, idatex, calendar);
 }
 
@@ -1567,8 +1588,10 @@ int mlc_member_read_sav(mlc_ctx *x, int m, const char *path) {
   const size_t jx = d.jx, iy = d.iy, kz = d.kz, c3 = (jx - 1) * (iy - 1) * kz;
   std::vector<double> u(jx * (iy - 1) * kz), v((jx - 1) * iy * kz), w((jx - 1) * (iy - 1) * (kz + 1));
   std::vector<double> t(c3), pai(c3), qx(c3 * d.nqx), ps((jx - 1) * (iy - 1)), trac(c3 * d.ntr);
+  const bool tke = x->mem[m].c.tke != 0;
+  std::vector<double> tk(tke ? (jx - 1) * (iy - 1) * (kz + 1) : 0);
   mlc_sav_fields f{u.data(), v.data(), w.data(), t.data(), pai.data(), qx.data(), ps.data(),
-                   d.ntr ? trac.data() : nullptr};
+                   d.ntr ? trac.data() : nullptr, tke ? tk.data() : nullptr};
   MLC_CHK(mlc_sav_read(path, &d, &f, nullptr, 0));
   std::vector<double> su(u.size()), sv(v.size()), sw(w.size()), s3[9];
   for (auto &a : s3) a.resize(c3);
@@ -1578,6 +1601,7 @@ int mlc_member_read_sav(mlc_ctx *x, int m, const char *path) {
   sp.t = s3[2].data(); sp.tvirt = s3[3].data(); sp.ux = s3[4].data(); sp.vx = s3[5].data();
   sp.p = s3[6].data(); sp.rho = s3[7].data(); sp.qsat = s3[8].data(); sp.qx = sq.data();
   sp.ps = sps.data(); sp.trac = d.ntr ? str.data() : nullptr;
+  sp.tke = tke ? tk.data() : nullptr;  // copied as read
   MLC_CHK(mlc_sav_restart_state(&d, &f, &sp));
   return mlc_member_upload_state(x, m, &sp);
 }

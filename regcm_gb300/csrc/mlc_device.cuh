@@ -43,6 +43,7 @@ struct Scal {
   int curvature;            // curvature terms are not identically zero
   int spectral;             // spectral nudging on
   int km2, lm2;             // sine modes in x and y (2*km, 2*lm)
+  int tke;                  // ibltyp = 2: TKE advected, bounded and updated
   double dtrad;             // spectral nudging interval
 };
 // sine modes of spectral nudging per direction, at most
@@ -93,6 +94,7 @@ struct State {
   double *pai, *tetav;
   R *qx, *trac;  // species blocks
   double *ps;    // 2-D, FP64
+  R *tke;        // (kz+1) planes, ibltyp = 2 (else null)
 };
 
 // Boundary data b0/b1 for one domain.  Temperature and Exner are FP64 (a
@@ -149,6 +151,9 @@ struct Dom {
   double *pai[2], *tetav[2];
   R *w, *t, *tvirt, *p, *rho, *qsat;
   double *ps;
+  // turbulent kinetic energy at the interfaces (kz+1 planes) and its
+  // advected copy at the levels (a ping-pong pair); null unless ibltyp = 2
+  R *tke, *tkex[2];
   R *s, *zdiv2;
   double *tetavf;
   R *wz[kMaxFields];     // per advected R field
@@ -318,6 +323,7 @@ __host__ __device__ __forceinline__ State<R> state_of(const Dom<R> &D, int uv, i
   st.ux = D.ux[adv]; st.vx = D.vx[adv]; st.p = D.p; st.rho = D.rho; st.qsat = D.qsat;
   st.pai = D.pai[adv]; st.tetav = D.tetav[adv]; st.qx = D.qx[adv]; st.trac = D.trac[adv];
   st.ps = D.ps;
+  st.tke = D.tke;
   return st;
 }
 

@@ -169,6 +169,17 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
       st.qx[ob + on] = inflow ? R(qx_zero(n)) : st.qx[oi + on];
     }
     st.w[ob] = inflow ? R(0) : st.w[oi];
+    if (c.tke) {
+      // Main/mod_bdycod.F90:1684-1695 (west), 1742-1753 (east): the floor at
+      // the top interface, below it inflow by u(k) + u(k-1) of the new ring
+      if (k == 1) {
+        st.tke[ob] = R(kTkeMin);
+      } else {
+        const R us = un + blend(bd.dub, od - PS);
+        const bool in2 = side == 0 ? (us > R(0)) : (us < R(0));
+        st.tke[ob + PS] = in2 ? R(kTkeMin) : st.tke[oi + PS];
+      }
+    }
     for (int n = 0; n < g.ntr; ++n) {
       const size_t on = (size_t)n * F;
       st.trac[ob + on] = bdy_blend<R>(R(cx0), R(cx1), bd.chib[0][ob + on], bd.chib[1][ob + on]);
@@ -198,6 +209,16 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
       st.qx[ob + on] = inflow ? R(qx_zero(n)) : st.qx[oi + on];
     }
     st.w[ob] = inflow ? R(0) : st.w[oi];
+    if (c.tke) {
+      // Main/mod_bdycod.F90:1800-1811 (south), 1858-1869 (north)
+      if (k == 1) {
+        st.tke[ob] = R(kTkeMin);
+      } else {
+        const R vs = vn + blend(bd.dvb, od - PS);
+        const bool in2 = side == 0 ? (vs > R(0)) : (vs < R(0));
+        st.tke[ob + PS] = in2 ? R(kTkeMin) : st.tke[oi + PS];
+      }
+    }
     for (int n = 0; n < g.ntr; ++n) {
       const size_t on = (size_t)n * F;
       st.trac[ob + on] = bdy_blend<R>(R(cx0), R(cx1), bd.chib[0][ob + on], bd.chib[1][ob + on]);
@@ -1166,6 +1187,30 @@ int reduce_blocks(const Geom &g) {
   return (int)std::min<size_t>(std::max<size_t>(nb, 1), 152 * 4);
 }
 
+// status_update of the turbulent kinetic energy (Main/mod_moloch.F90:
+// 1419-1424): on jci x ici at the kz+1 interfaces, tke + dtsec * tketen (the
+// physics' tendency; none in a whole step), then the floor tkemin.
+template <class R>
+__global__ void k_end_tke(const Dom<R> *__restrict__ doms, int whole, int tiles_j) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active || !D.c.tke) return;
+  const Geom g = D.g;
+  const Pt q = point_of(tiles_j, 1, 1);
+  if (q.j < 2 || q.j > g.jx - 2 || q.i < 2 || q.i > g.iy - 2 || q.k > g.kz) return;
+  const R *ten = whole ? nullptr : D.tend;
+  // tketen follows the kz-plane tendencies (t, u, v, the species, tracers)
+  const R *tt = ten ? ten + (size_t)(3 + g.nqx + g.ntr) * g.field3() : nullptr;
+  const R dts = pick<R>(D.c.dtsec, D.c.dtsecf);
+  const int klast = q.k + kPtLevels - 1 >= g.kz ? g.kz + 1 : q.k + kPtLevels - 1;
+  for (int k = q.k; k <= klast; ++k) {
+    const size_t o = g.at(q.j, q.i, k);
+    R v = D.tke[o];
+    if (tt) v = v + dts * tt[o];
+    if (v < R(kTkeMin)) v = R(kTkeMin);
+    D.tke[o] = v;
+  }
+}
+
 template <class R>
 void Launch<R>::end_tvirt(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
@@ -1237,6 +1282,14 @@ void Launch<R>::end_uvstag(const LaunchGeom &L, const Dom<R> *d, int uvoff, int 
   int tj;
   const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
   k_end_uvstag<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+}
+
+template <class R>
+void Launch<R>::end_tke(const LaunchGeom &L, const Dom<R> *d, bool whole_step, cudaStream_t s) {
+  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
+  int tj;
+  const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
+  k_end_tke<R><<<grd, b, 0, s>>>(d, whole_step ? 1 : 0, tj);
 }
 
 template <class R>

@@ -61,6 +61,8 @@ template <class R> struct Launch {
   static void end_cross_split(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, bool post,
                               cudaStream_t s);
   static void end_uvstag(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  // status_update of the TKE (ibltyp = 2): tendency (split step) and floor
+  static void end_tke(const LaunchGeom &L, const Dom<R> *d, bool whole_step, cudaStream_t s);
   static void end_reduce(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff,
                          cudaStream_t s);
   // ---- layout conversion (one member, from the host) ----

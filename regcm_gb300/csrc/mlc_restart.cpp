@@ -326,6 +326,7 @@ int mlc_sav_write(const char *path, const mlc_dims *d, const mlc_sav_fields *f, 
   add("atm_t", {KH, IC, JC}, f->t);
   add("atm_pai", {KH, IC, JC}, f->pai);
   add("atm_qx", {NQ, KH, IC, JC}, f->qx);
+  if (f->tke) add("atm_tke", {KF, IC, JC}, f->tke);  // ibltyp = 2 (:884-887)
   add("ps", {IC, JC}, f->ps);
   if (d->ntr > 0) add("trac", {NT, KH, IC, JC}, f->trac);
   std::vector<std::pair<std::string, std::string>> atts;
@@ -351,6 +352,7 @@ int mlc_sav_read(const char *path, const mlc_dims *d, const mlc_sav_fields *f, c
   if (st == MLC_OK) st = read_var(fp, nf, "atm_t", {kz, iy - 1, jx - 1}, f->t);
   if (st == MLC_OK) st = read_var(fp, nf, "atm_pai", {kz, iy - 1, jx - 1}, f->pai);
   if (st == MLC_OK) st = read_var(fp, nf, "atm_qx", {nq, kz, iy - 1, jx - 1}, f->qx);
+  if (st == MLC_OK && f->tke) st = read_var(fp, nf, "atm_tke", {kz + 1, iy - 1, jx - 1}, f->tke);
   if (st == MLC_OK) st = read_var(fp, nf, "ps", {iy - 1, jx - 1}, f->ps);
   if (st == MLC_OK && nt > 0) st = read_var(fp, nf, "trac", {nt, kz, iy - 1, jx - 1}, f->trac);
   std::fclose(fp);
@@ -380,6 +382,8 @@ int mlc_sav_restart_state(const mlc_dims *d, const mlc_sav_fields *f, const mlc_
   std::memcpy(st->qx, f->qx, c3 * (size_t)d->nqx * sizeof(double));
   std::memcpy(st->ps, f->ps, (jx - 1) * (iy - 1) * sizeof(double));
   if (d->ntr > 0) std::memcpy(st->trac, f->trac, c3 * (size_t)d->ntr * sizeof(double));
+  if (f->tke && st->tke && st->tke != f->tke)
+    std::memcpy(st->tke, f->tke, (jx - 1) * (iy - 1) * (kz + 1) * sizeof(double));
   for (size_t e = 0; e < c3; ++e) {
     const double t = f->t[e], pai = f->pai[e];
     const double p = std::pow(pai, kCpovr) * kP00;

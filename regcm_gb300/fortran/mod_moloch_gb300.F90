@@ -65,7 +65,7 @@ module mod_moloch_gb300
 
   type, bind(c) :: mlc_state_ptrs
     type(c_ptr) :: u, v, w, pai, tetav, t, tvirt, ux, vx, p, rho, qsat
-    type(c_ptr) :: qx, trac, ps
+    type(c_ptr) :: qx, trac, ps, tke
   end type mlc_state_ptrs
 
   type, bind(c) :: mlc_bdy_ptrs
@@ -74,7 +74,7 @@ module mod_moloch_gb300
   end type mlc_bdy_ptrs
 
   type, bind(c) :: mlc_tend_ptrs
-    type(c_ptr) :: tten, uten, vten, qxten, chiten
+    type(c_ptr) :: tten, uten, vten, qxten, chiten, tketen
   end type mlc_tend_ptrs
 
   type, bind(c) :: mlc_diag
@@ -313,6 +313,11 @@ module mod_moloch_gb300
     st%qx = c_loc(mo_atm%qx)
     st%trac = c_null_ptr
     st%ps = c_loc(sfs%psa)
+    if ( ibltyp == 2 ) then
+      st%tke = c_loc(mo_atm%tke)
+    else
+      st%tke = c_null_ptr
+    end if
   end subroutine state_ptrs
 
   ! replaces Main/mod_moloch.F90:312-446: the GPU runs the dynamics half
@@ -332,6 +337,7 @@ module mod_moloch_gb300
     mo_atm%uten = d_zero
     mo_atm%vten = d_zero
     mo_atm%qxten = d_zero
+    if ( ibltyp == 2 ) mo_atm%tketen = d_zero
     call mkslice
     if ( do_phys .and. moloch_realcase ) then
       call physical_parametrizations
@@ -341,6 +347,11 @@ module mod_moloch_gb300
     tp%vten = c_loc(mo_atm%vten)
     tp%qxten = c_loc(mo_atm%qxten)
     tp%chiten = c_null_ptr
+    if ( ibltyp == 2 ) then
+      tp%tketen = c_loc(mo_atm%tketen)
+    else
+      tp%tketen = c_null_ptr
+    end if
     call check(mlc_member_set_tendencies(ctx, 0_c_int, tp), 'moloch(tendencies)')
     ist = mlc_step_finish(ctx, dg)
     if ( ist == -6 ) then

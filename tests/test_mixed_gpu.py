@@ -115,6 +115,7 @@ def _variants(prec):
         "moist_exp_nudging": lambda: small_moist(lehmann=False),
         "moist_ipptls4": lambda: small_moist(ipptls=4),
         "moist_ipptls5": lambda: small_moist(ipptls=5),
+        "moist_tke": lambda: small_moist(tke=True),
     }
 
 
@@ -130,6 +131,8 @@ def test_mixed_variants_one_step(name):
               "u": (vel, 1e-5), "v": (vel, 1e-5), "w": (max(np.abs(ref["w"]).max(), 1e-3), 1e-4)}
     if "trac" in ref:
         bounds["trac"] = (np.abs(ref["trac"]).max(), 1e-5)
+    if "tke" in ref:
+        bounds["tke"] = (np.abs(ref["tke"]).max(), 1e-5)
     for n, (scale, tol) in bounds.items():
         d = np.abs(got[n] - ref[n]).max() / scale
         assert d <= tol, (name, n, d)

@@ -34,6 +34,8 @@ def field_errors(a: dict, b: dict, case) -> dict:
             out[f"qx{q}"] = float(np.abs(a["qx"][..., q] - ref).max())
     if case.dims.ntr:
         out["trac"] = rel_l2(a["trac"], b["trac"])
+    if "tke" in b:
+        out["tke"] = rel_l2(a["tke"], b["tke"])
     return out
 
 
@@ -84,6 +86,9 @@ CASES = {
     "moist_ipptls3": lambda: small_moist(ipptls=3),
     "moist_ipptls4": lambda: small_moist(ipptls=4),
     "moist_ipptls5": lambda: small_moist(ipptls=5),
+    # TKE of the UW PBL (ibltyp = 2) advected, bounded and floored
+    "dry_tke": lambda: small_dry(tke=True),
+    "moist_tke": lambda: small_moist(tke=True),
 }
 
 
@@ -102,7 +107,8 @@ def test_one_step(name):
     assert dg.xbctime == do.xbctime
 
 
-@pytest.mark.parametrize("name", ["dry_tracer", "moist", "moist_exp_nudging", "moist_ipptls5"])
+@pytest.mark.parametrize("name", ["dry_tracer", "moist", "moist_exp_nudging", "moist_ipptls5",
+                                  "moist_tke"])
 def test_hundred_steps(name):
     case = CASES[name]()
     g, o, dg, do = run_pair(case, 100, chunk=25)

@@ -84,3 +84,27 @@ def test_open_step_refuses_a_whole_step():
     assert o.step(1)[0] == abi.MLC_ERR_STATE
     assert o.step_dynamics() == abi.MLC_ERR_STATE
     assert o.step_finish()[0] == 0
+
+
+def test_tke_status_update_and_ring():
+    """ibltyp = 2: the interior TKE gains dtsec * tketen and is floored at
+    tkemin = 1e-3 (Main/mod_moloch.F90:1419-1424); on the boundary ring the
+    top interface holds tkemin (Main/mod_bdycod.F90:1684-1869); a constant
+    TKE above the floor in a resting, flat domain stays constant in the
+    interior (the advection of a constant field is exact)."""
+    c = cs.build(24, 22, 10, dx=12000.0, dt=60.0, nsound=3, moist=True, seed=5,
+                 hills=[(12 * 12000.0, 11 * 12000.0, 600.0)], wind=10.0, theta_noise=0.3,
+                 tke=True, name="seam_tke")
+    o = Oracle(c)
+    assert o.step_dynamics() == 0
+    mid = o.state()
+    ten = c.tendencies(seed=2)
+    assert o.set_tendencies(c.tend_ptrs_of(ten)) == 0
+    assert o.step_finish()[0] == 0
+    end = o.state()
+    inner = (slice(1, -1), slice(1, -1))
+    exp = mid["tke"][inner] + c.params.dtsec * ten["tketen"]
+    exp = np.where(exp < 1.0e-3, 1.0e-3, exp)
+    assert np.array_equal(end["tke"][inner], exp)
+    assert np.any(end["tke"][inner] == 1.0e-3)
+    assert np.all(end["tke"][0, 1:-1, 0] == 1.0e-3) and np.all(end["tke"][:, 0, 0] == 1.0e-3)

@@ -9,6 +9,7 @@ mlc_step_finish) on the GPU against the CPU oracle's split.
   to the path's FP64 tolerance, for three consecutive coupled steps with new
   tendencies each; the tendencies move the state by far more than that.
 * A mixed member with tendencies stays within FP32 rounding of the oracle.
+* The same with the UW PBL's TKE (ibltyp = 2) and its tendency tketen.
 * An open step refuses whole steps, uploads and a second dynamics half.
 """
 from __future__ import annotations
@@ -58,8 +59,9 @@ def test_split_without_tendencies_is_the_step(prec):
             assert d <= 2e-6 * max(np.abs(ga[n]).max(), 1e-30), (n, d)
 
 
-def test_coupled_steps_match_oracle():
-    c = seam_case()
+@pytest.mark.parametrize("tke", [False, True])
+def test_coupled_steps_match_oracle(tke):
+    c = seam_case(tke=tke)
     dom, orc = domain_from_case(c), Oracle(c)
     keep = []
     for step in range(3):
@@ -93,8 +95,9 @@ def test_coupled_steps_match_oracle():
     ref.close()
 
 
-def test_coupled_mixed_member():
-    cm, cf = seam_case(abi.MLC_PREC_MIXED), seam_case()
+@pytest.mark.parametrize("tke", [False, True])
+def test_coupled_mixed_member(tke):
+    cm, cf = seam_case(abi.MLC_PREC_MIXED, tke=tke), seam_case(tke=tke)
     dom, orc = domain_from_case(cm), Oracle(cf)
     keep = []
     for step in range(5):
@@ -112,6 +115,8 @@ def test_coupled_mixed_member():
         assert rel_l2(got[n], ref[n]) <= 3e-5, (n, rel_l2(got[n], ref[n]))
     assert rel_l2(got["qx"][..., 0], ref["qx"][..., 0]) <= 3e-5
     assert rel_l2(got["trac"], ref["trac"]) <= 3e-5
+    if tke:
+        assert rel_l2(got["tke"], ref["tke"]) <= 3e-5, rel_l2(got["tke"], ref["tke"])
     dom.close()
     orc.close()
 

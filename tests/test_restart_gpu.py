@@ -27,15 +27,16 @@ NAMES = {"atm_u": "u", "atm_v": "v", "atm_w": "w", "atm_t": "t", "atm_pai": "pai
          "atm_qx": "qx", "ps": "ps", "trac": "trac"}
 
 
-def moist_tracer(precision=abi.MLC_PREC_FP64):
+def moist_tracer(precision=abi.MLC_PREC_FP64, tke=False):
     return cs.build(40, 38, 14, dx=3000.0, dt=20.0, nsound=4, moist=True, seed=4,
                     hills=[(20 * 3000.0, 18 * 3000.0, 1200.0)], jet=True, theta_noise=0.2,
-                    tracer=True, name="restart", precision=precision)
+                    tracer=True, name="restart", precision=precision, tke=tke)
 
 
-@pytest.mark.parametrize("prec", [abi.MLC_PREC_FP64, abi.MLC_PREC_MIXED])
-def test_snapshot_is_the_device_state(tmp_path, prec):
-    c = moist_tracer(prec)
+@pytest.mark.parametrize("prec,tke", [(abi.MLC_PREC_FP64, False), (abi.MLC_PREC_MIXED, False),
+                                      (abi.MLC_PREC_FP64, True)])
+def test_snapshot_is_the_device_state(tmp_path, prec, tke):
+    c = moist_tracer(prec, tke)
     dom = domain_from_case(c)
     dom.step(4)
     path = tmp_path / "SAV.nc"
@@ -47,10 +48,15 @@ def test_snapshot_is_the_device_state(tmp_path, prec):
         assert f.idatex == b"2000010100"
         for v, n in NAMES.items():
             assert np.array_equal(np.asarray(f.variables[v].data).T, g[n]), v
+        # atm_tke only with the UW PBL (Main/mod_savefile.F90:884-887)
+        assert ("atm_tke" in f.variables) == tke
+        if tke:
+            assert np.array_equal(np.asarray(f.variables["atm_tke"].data).T, g["tke"])
 
 
-def test_restart_steps_like_the_oracle(tmp_path):
-    c = moist_tracer()
+@pytest.mark.parametrize("tke", [False, True])
+def test_restart_steps_like_the_oracle(tmp_path, tke):
+    c = moist_tracer(tke=tke)
     dom = domain_from_case(c)
     d4 = dom.step(4)
     path = tmp_path / "SAV.nc"
