@@ -281,9 +281,13 @@ int orc_setup_relaxation(const mlc_dims *d, const mlc_params *p, const double *z
       for (int n = 2; n <= nspgx - 1; ++n) hefc(n, k) = std::exp(-(double)(n - 1) / anudge[k]);
   }
   std::memcpy(hefc_o, hefc.d.data(), hefc.d.size() * 8);
-  fcx_o[0] = 1.0;
-  fcx_o[nspgx - 1] = 0.0;
-  orc_relax_coefficients(nspgx - 2, 0.1, 1.0, fcx_o + 1);
+  if (d->ntr > 0) {  // setup_che_bdycon (ichem = 1)
+    fcx_o[0] = 1.0;
+    fcx_o[nspgx - 1] = 0.0;
+    orc_relax_coefficients(nspgx - 2, 0.1, 1.0, fcx_o + 1);
+  } else {
+    for (int n = 0; n < nspgx; ++n) fcx_o[n] = 0.0;
+  }
   for (int k = 1; k <= kz; ++k) {
     if (p->mo_top_nudge && k <= nztop)
       tnudge_o[k - 1] = std::pow(std::sin(0.5 * mathpi * (gmeanz[k] - 18000.0) / (p->mo_h - 18000.0)), 2);

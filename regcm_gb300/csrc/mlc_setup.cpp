@@ -318,11 +318,14 @@ int mlc_setup_relaxation(const mlc_dims *d, mlc_params *p, const double *zeta, d
     for (int n = 0; n < nsp - 2; ++n) col[n + 1] = w[n];
   }
   }
-  if (fcx) {
+  if (fcx && d->ntr > 0) {
+    // setup_che_bdycon runs with chemistry only (ichem = 1: tracers)
     fcx[0] = 1.0;
     fcx[nsp - 1] = 0.0;
     int st = mlc_relax_coefficients(nsp - 2, 0.1, 1.0, fcx + 1);
     if (st != MLC_OK) return st;
+  } else if (fcx) {
+    for (int n = 0; n < nsp; ++n) fcx[n] = 0.0;
   }
   if (tnudge)
     for (int k = 0; k < kz; ++k) {
