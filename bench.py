@@ -383,6 +383,24 @@ def run_ours(args, rank, world):
     side = None
     if args.precision == "fp64" and not args.no_mixed:
         side = run_mixed_side(args, rank)
+    if args.precision == "fp64" and world == 1 and not args.no_ensemble and args.config == "c1":
+        # the batched form the scope targets, measured in the same run: the
+        # 64-member ensemble of 128x128x30 domains in mixed precision with
+        # autotuned launch shapes, against the plain FP64 single-domain path
+        import copy
+        eargs = copy.copy(args)
+        eargs.config, eargs.members, eargs.size, eargs.precision = "c2", 64, 0, "mixed"
+        eargs.no_tune = False
+        ens = ensemble_line(eargs, rank, world)
+        if ens is not None:
+            side = dict(side or {})
+            side["ensemble"] = {
+                "workload": ens["config"]["workload"], "value": ens["value"], "unit": UNIT,
+                "ms_per_step": ens["ms_per_step"], "dtype": ens["dtype"],
+                "plain_fp64_single_domain": ens["side_by_side"]["plain_fp64_single_domain"],
+                "ratio_to_plain_fp64": ens["side_by_side"]["ratio_to_plain_fp64"],
+                "autotune": ens["side_by_side"]["autotune"], "roofline": ens["roofline"],
+                "gpu_launches": ens["gpu_launches"]}
     if rank != 0:
         return
     cpu = None
@@ -409,10 +427,17 @@ def run_ours(args, rank, world):
 
 
 def run_ensemble(args, rank, world):
+    line = ensemble_line(args, rank, world)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def ensemble_line(args, rank, world):
     """Ensemble workload: members of the dry recipe (128x128x30, dx 12 km,
     dt 60 s, 3 substeps, theta noise +-0.5 K and wind U(5,20) per member)
     advanced by one launch per kernel stage, autotuned launch shapes; next to
-    the plain single-domain FP64 path on one member."""
+    the plain single-domain FP64 path on one member.  Returns the JSON line
+    (rank 0; None elsewhere)."""
     import torch
     from regcm_gb300 import abi
     from regcm_gb300 import case as cs
@@ -465,7 +490,7 @@ def run_ensemble(args, rank, world):
     d.close()
     plain = pts * args.steps / (ms1.value / 1000.0)
     if rank != 0:
-        return
+        return None
     wbytes = 4 if prec == abi.MLC_PREC_MIXED else 8
     dom_name = max(kernels, key=lambda k: kernels[k][1])
     nl, kms = kernels[dom_name]
@@ -494,7 +519,7 @@ def run_ensemble(args, rank, world):
                          "autotune": tune},
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def rel_l2(a, b) -> float:
@@ -810,6 +835,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision side run")
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="skip the 64-member ensemble side run of the default line")
     ap.add_argument("--size", type=int, default=0, help="cross points per side (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -56,6 +56,22 @@ struct Coord {
   }
 };
 
+// The factors of md_fmz/md_zeta that depend only on the level (the
+// exponentials of b(zeta)), formed once per level; the per-point results
+// are the same expressions on the same values.
+struct Level {
+  double gp, bp, gm1, b;
+  Level(const Coord &c, double z) : gp(c.gp(z)), bp(c.bp(z)), gm1(gzita(z, c.ztop, c.a0) - 1.0), b(c.b(z)) {}
+  double fmz(double geopot) const {
+    double orog = geopot * kRegrav;
+    return 1.0 / (gp * orog + bp);
+  }
+  double zeta(double geopot) const {
+    double orog = geopot * kRegrav;
+    return orog * gm1 + b;
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -137,31 +153,33 @@ int mlc_setup_metric(const mlc_dims *d, const mlc_params *p, const double *ht, c
         hy[g.cross2(j, i)] = v;  // (jx-1, iy)
       }
   // vertical metric, Main/mod_params.F90:3358-3390
-  for (int k = 1; k <= kz; ++k)
+  for (int k = 1; k <= kz; ++k) {
+    const Level lv(c, zitah[k - 1]);
     for (int i = 1; i <= iy - 1; ++i)
       for (int j = 1; j <= jx - 1; ++j) {
         double h = ht[g.dot(j, i)];
-        if (zeta) zeta[g.cross3(j, i, k)] = c.zeta(zitah[k - 1], h);
-        if (fmz) fmz[g.cross3(j, i, k)] = c.fmz(zitah[k - 1], h);
+        if (zeta) zeta[g.cross3(j, i, k)] = lv.zeta(h);
+        if (fmz) fmz[g.cross3(j, i, k)] = lv.fmz(h);
       }
-  if (rfmzu)
-    for (int k = 1; k <= kz; ++k)
+    if (rfmzu)
       for (int i = 1; i <= iy - 1; ++i)
-        for (int j = 1; j <= jx; ++j) rfmzu[g.upt3(j, i, k)] = 1.0 / c.fmz(zitah[k - 1], htu[g.dot(j, i)]);
-  if (rfmzv)
-    for (int k = 1; k <= kz; ++k)
+        for (int j = 1; j <= jx; ++j) rfmzu[g.upt3(j, i, k)] = 1.0 / lv.fmz(htu[g.dot(j, i)]);
+    if (rfmzv)
       for (int i = 1; i <= iy; ++i)
-        for (int j = 1; j <= jx - 1; ++j) rfmzv[g.vpt3(j, i, k)] = 1.0 / c.fmz(zitah[k - 1], htv[g.dot(j, i)]);
+        for (int j = 1; j <= jx - 1; ++j) rfmzv[g.vpt3(j, i, k)] = 1.0 / lv.fmz(htv[g.dot(j, i)]);
+  }
   std::vector<double> zf;
   const bool need_zf = (zetaf != nullptr) || (dz != nullptr);
   if (need_zf) zf.assign((size_t)(jx - 1) * (iy - 1) * (kz + 1), 0.0);
-  for (int k = 1; k <= kz + 1; ++k)
+  for (int k = 1; k <= kz + 1; ++k) {
+    const Level lv(c, zita[k - 1]);
     for (int i = 1; i <= iy - 1; ++i)
       for (int j = 1; j <= jx - 1; ++j) {
         double h = ht[g.dot(j, i)];
-        if (fmzf) fmzf[g.cross3(j, i, k)] = c.fmz(zita[k - 1], h);
-        if (need_zf) zf[g.cross3(j, i, k)] = c.zeta(zita[k - 1], h);
+        if (fmzf) fmzf[g.cross3(j, i, k)] = lv.fmz(h);
+        if (need_zf) zf[g.cross3(j, i, k)] = lv.zeta(h);
       }
+  }
   if (zetaf) std::memcpy(zetaf, zf.data(), zf.size() * sizeof(double));
   if (dz)
     for (int k = 1; k <= kz; ++k)
