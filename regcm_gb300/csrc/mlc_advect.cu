@@ -212,8 +212,10 @@ __device__ __forceinline__ void field_t(const Dom<R> &D, int set, int f, int adv
 }
 
 template <class R>
-__global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
@@ -223,7 +225,7 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
   R *__restrict__ ux = D.ux[adv];
   R *__restrict__ vx = D.vx[adv];
   R *__restrict__ wx = D.wx[adv];
-  const Pt q_ = point_of(tiles_j, 1, 1);
+  const Pt q_ = point_at(wi, 1, 1);
   const int j = q_.j, k0 = q_.k;
   if (k0 > g.kz) return;
   const int i = q_.i;
@@ -299,16 +301,20 @@ __device__ __forceinline__ T vupdate_f(T pk, T fb, T fa, T dv, T zu, T zd) {
 // blocks reading one column's s and metric run together), y = row tiles,
 // z = member; block (vert_x, vert_y) columns along (j, i)
 template <class R, class T>
-__global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set, int advoff) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set, int advoff,
+                               const WorkItem *__restrict__ wl) {
+  const WorkItem wi = wl ? wl[blockIdx.x]
+                          : WorkItem{(int16_t)blockIdx.z, (int16_t)(blockIdx.x / (unsigned)nf),
+                                     (int16_t)blockIdx.y, (int16_t)(blockIdx.x % (unsigned)nf)};
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
-  const int f = (int)(blockIdx.x % (unsigned)nf);
-  const int bj = (int)(blockIdx.x / (unsigned)nf);
+  const int f = wi.c;
+  const int bj = wi.a;
   if (set == 0 && f >= n_table_r(D)) return;  // a member with fewer species
   const Geom g = D.g;
   const int kz = g.kz;
   const int j = bj * (int)blockDim.x + (int)threadIdx.x + 1;
-  const int i = (int)blockIdx.y * (int)blockDim.y + (int)threadIdx.y + 1;
+  const int i = (int)wi.b * (int)blockDim.y + (int)threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
   const Scal &c = D.c;
   const int adv = (D.clk->adv_role + advoff) & 1;
@@ -476,7 +482,8 @@ __device__ __forceinline__ void next_col(T (&e)[V], const T (&x)[V]) {
 // reference's, operand for operand.
 template <class R, int V, int NW>
 __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__restrict__ doms,
-                                                           int tiles_j, int uvoff, int advoff) {
+                                                           int tiles_j, int uvoff, int advoff,
+    const WorkItem *__restrict__ wl) {
   using T = R;
   constexpr int W = 32 * V;       // columns of a warp's range
   constexpr int S = W - 4;        // columns it writes: range columns 2 .. W-3
@@ -495,13 +502,14 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
   __shared__ const T *cur_s[kMaxFields];                   // each field's current and other half
   __shared__ T *out_s[kMaxFields];
   // grid: x = tiles along j and i, y = level, z = member
-  const Dom<R> &D = doms[blockIdx.z];
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
-  const int k = blockIdx.y + 1;
+  const int k = wi.c + 1;
   const Geom g = D.g;
   const int jx = g.jx, iy = g.iy;
   if (k > g.kz) return;
-  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int bj = wi.a, bi = wi.b;
   const int ob = bj * S + OB0;  // column offset (j - 1) of the range's first column
   const int I0 = bi * NW + 1;
   if (ob + 3 > jx - 1 || I0 > iy - 1) return;
@@ -778,11 +786,13 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 // Species that are not advected (ipptls = 0: qx(iqfrst:nqx)) keep their
 // values when the advected fields move to the other half of their pairs.
 template <class R>
-__global__ void k_species_copy(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_species_copy(const Dom<R> *__restrict__ doms, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
-  const Pt q = point_of(tiles_j, 1, 1);
+  const Pt q = point_at(wi, 1, 1);
   if (D.c.ipptls > 0 || q.j > g.jx - 1 || q.i > g.iy - 1 || q.k > g.kz) return;
   const int adv = (D.clk->adv_role + advoff) & 1;
   const size_t F = g.field3();
@@ -795,8 +805,10 @@ __global__ void k_species_copy(const Dom<R> *__restrict__ doms, int advoff, int 
 
 // :809-825
 template <class R>
-__global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active || !D.c.curvature) return;
   const Geom g = D.g;
   const Scal &c = D.c;
@@ -804,7 +816,7 @@ __global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff, int
   const int adv = (D.clk->adv_role + advoff) & 1;
   R *__restrict__ ux = D.ux[adv];
   R *__restrict__ vx = D.vx[adv];
-  const Pt q_ = point_of(tiles_j, 2, 2);
+  const Pt q_ = point_at(wi, 2, 2);
   const int j = q_.j, k0 = q_.k;
   if (k0 > g.kz) return;
   const int i = q_.i;
@@ -833,8 +845,10 @@ __global__ void k_adv_curvature(const Dom<R> *__restrict__ doms, int advoff, int
 
 // uvxtouvstag :1477-1522 and htozstag :1461-1475
 template <class R>
-__global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
@@ -844,7 +858,7 @@ __global__ void k_adv_back(const Dom<R> *__restrict__ doms, int uvoff, int advof
   R *__restrict__ u = D.u[uv];
   R *__restrict__ v = D.v[uv];
   R *__restrict__ w = D.w;
-  const Pt q_ = point_of(tiles_j, 1, 1);
+  const Pt q_ = point_at(wi, 1, 1);
   const int j = q_.j, k0 = q_.k;
   if (k0 > g.kz) return;
   const int i = q_.i;
@@ -932,15 +946,19 @@ __device__ __forceinline__ float vupdate_inc(float ek, float flb, float fla, flo
 }
 
 template <class R>
-__global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff,
+                                   const WorkItem *__restrict__ wl) {
+  const WorkItem wi = wl ? wl[blockIdx.x]
+                          : WorkItem{(int16_t)blockIdx.z, (int16_t)(blockIdx.x >> 1), (int16_t)blockIdx.y,
+                                     (int16_t)(blockIdx.x & 1u)};
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
-  const int f = (int)(blockIdx.x & 1u);
-  const int bj = (int)(blockIdx.x >> 1);
+  const int f = wi.c;
+  const int bj = wi.a;
   const Geom g = D.g;
   const int kz = g.kz;
   const int j = bj * (int)blockDim.x + (int)threadIdx.x + 1;
-  const int i = (int)blockIdx.y * (int)blockDim.y + (int)threadIdx.y + 1;
+  const int i = (int)wi.b * (int)blockDim.y + (int)threadIdx.y + 1;
   if (j > g.jx - 1 || i > g.iy - 1) return;
   const Scal &c = D.c;
   const int adv = (D.clk->adv_role + advoff) & 1;
@@ -1043,7 +1061,8 @@ __global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff) 
 template <class R, int V, int NW>
 __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__restrict__ doms,
                                                                int tiles_j, int uvoff,
-                                                               int advoff) {
+                                                               int advoff,
+                                                               const WorkItem *__restrict__ wl) {
   constexpr int W = 32 * V, S = W - 4;
   constexpr int OB0 = hshape_ob0(V);
   constexpr int OFF = hshape_off(4, V);
@@ -1057,13 +1076,14 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
   __shared__ __align__(128) unsigned char tiles[2][4][kBuf];
   __shared__ __align__(16) float fy_s[2][NW + 1][W];  // meridional fluxes, rows I0 .. I0+NW
   __shared__ __align__(8) uint64_t mbar[2];
-  const Dom<R> &D = doms[blockIdx.z];
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
-  const int k = blockIdx.y + 1;
+  const int k = wi.c + 1;
   const Geom g = D.g;
   const int jx = g.jx, iy = g.iy;
   if (k > g.kz) return;
-  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int bj = wi.a, bi = wi.b;
   const int ob = bj * S + OB0;
   const int I0 = bi * NW + 1;
   if (ob + 3 > jx - 1 || I0 > iy - 1) return;
@@ -1370,6 +1390,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__
 // grid of a point kernel over nj x ni points per level
 inline dim3 pt_grid(const LaunchGeom &L, int nj, int ni, int &tiles_j) {
   tiles_j = (nj + L.col_x - 1) / L.col_x;
+  if (L.wl_pt) return dim3((unsigned)L.n_pt, 1, 1);  // one block per work item
   const int ti = (ni + L.col_y - 1) / L.col_y;
   return dim3((unsigned)(tiles_j * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
               (unsigned)L.nmem);
@@ -1382,7 +1403,7 @@ void Launch<R>::adv_prep(const LaunchGeom &L, const Dom<R> *d, int uvoff, int ad
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-  k_adv_prep<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  k_adv_prep<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
 }
 
 template <class R, class T>
@@ -1390,9 +1411,12 @@ void launch_vertical(const LaunchGeom &L, const Dom<R> *d, int nf, int set, int 
                      cudaStream_t s) {
   // one thread per column: blocks of vert_x x vert_y columns along (j, i)
   const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
-  const dim3 grd((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * nf),
-                 (unsigned)((L.iy - 1 + L.vert_y - 1) / L.vert_y), (unsigned)L.nmem);
-  k_adv_vertical<R, T><<<grd, b, 0, s>>>(d, nf, set, advoff);
+  const WorkItem *wl = set == 0 ? L.wl_vert : L.wl_vinc;
+  const int nw = set == 0 ? L.n_vert : L.n_vinc;
+  const dim3 grd = wl ? dim3((unsigned)nw, 1, 1)
+                      : dim3((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * nf),
+                             (unsigned)((L.iy - 1 + L.vert_y - 1) / L.vert_y), (unsigned)L.nmem);
+  k_adv_vertical<R, T><<<grd, b, 0, s>>>(d, nf, set, advoff, wl);
 }
 
 template <class R, int V, int NW>
@@ -1400,8 +1424,9 @@ void launch_tile(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cu
   // tiles along j: tile bj writes j = bj*S + ob0 + 3 .. bj*S + ob0 + S + 2
   constexpr int S = 32 * V - 4;
   const int tj = (L.jx - 3 - hshape_ob0(V) + S - 1) / S, ti = (L.iy - 1 + NW - 1) / NW;
-  const dim3 grd((unsigned)(tj * ti), (unsigned)L.kz, (unsigned)L.nmem);
-  k_adv_horizontal<R, V, NW><<<grd, 32 * NW, 0, s>>>(d, tj, uvoff, advoff);
+  const dim3 grd = L.wl_h ? dim3((unsigned)L.n_h, 1, 1)
+                          : dim3((unsigned)(tj * ti), (unsigned)L.kz, (unsigned)L.nmem);
+  k_adv_horizontal<R, V, NW><<<grd, 32 * NW, 0, s>>>(d, tj, uvoff, advoff, L.wl_h);
 }
 
 template <class R>
@@ -1418,17 +1443,19 @@ void launch_horizontal(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advo
 template <class R>
 void launch_vertical_inc(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.vert_x, (unsigned)L.vert_y);
-  const dim3 grd((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * 2),
-                 (unsigned)((L.iy - 1 + L.vert_y - 1) / L.vert_y), (unsigned)L.nmem);
-  k_adv_vertical_inc<R><<<grd, b, 0, s>>>(d, advoff);
+  const dim3 grd = L.wl_vinc ? dim3((unsigned)L.n_vinc, 1, 1)
+                             : dim3((unsigned)(((L.jx - 1 + L.vert_x - 1) / L.vert_x) * 2),
+                                    (unsigned)((L.iy - 1 + L.vert_y - 1) / L.vert_y), (unsigned)L.nmem);
+  k_adv_vertical_inc<R><<<grd, b, 0, s>>>(d, advoff, L.wl_vinc);
 }
 
 template <class R, int V, int NW>
 void launch_tile_inc(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   constexpr int S = 32 * V - 4;
   const int tj = (L.jx - 3 - hshape_ob0(V) + S - 1) / S, ti = (L.iy - 1 + NW - 1) / NW;
-  const dim3 grd((unsigned)(tj * ti), (unsigned)L.kz, (unsigned)L.nmem);
-  k_adv_horizontal_inc<R, V, NW><<<grd, 32 * NW, 0, s>>>(d, tj, uvoff, advoff);
+  const dim3 grd = L.wl_hinc ? dim3((unsigned)L.n_hinc, 1, 1)
+                             : dim3((unsigned)(tj * ti), (unsigned)L.kz, (unsigned)L.nmem);
+  k_adv_horizontal_inc<R, V, NW><<<grd, 32 * NW, 0, s>>>(d, tj, uvoff, advoff, L.wl_hinc);
 }
 
 template <class R>
@@ -1466,7 +1493,7 @@ void Launch<R>::adv_species_copy(const LaunchGeom &L, const Dom<R> *d, int advof
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-  k_species_copy<R><<<grd, b, 0, s>>>(d, advoff, tj);
+  k_species_copy<R><<<grd, b, 0, s>>>(d, advoff, tj, L.wl_pt);
 }
 
 template <class R>
@@ -1474,7 +1501,7 @@ void Launch<R>::adv_curvature(const LaunchGeom &L, const Dom<R> *d, int advoff, 
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 3, L.iy - 3, tj);
-  k_adv_curvature<R><<<grd, b, 0, s>>>(d, advoff, tj);
+  k_adv_curvature<R><<<grd, b, 0, s>>>(d, advoff, tj, L.wl_pt);
 }
 
 template <class R>
@@ -1482,7 +1509,7 @@ void Launch<R>::adv_back(const LaunchGeom &L, const Dom<R> *d, int uvoff, int ad
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
-  k_adv_back<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  k_adv_back<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
 }
 
 template <class R>

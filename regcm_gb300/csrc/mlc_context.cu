@@ -341,6 +341,14 @@ struct mlc_ctx {
   bool use_graphs = true;
   int launches_per_step = 0;
   bool step_open = false;      // between mlc_step_dynamics and mlc_step_finish
+  // work lists of an uneven batch (one device buffer for all tilings) and the
+  // launch shapes they were built for
+  WorkItem *wl_buf = nullptr;
+  size_t wl_cap = 0;           // entries
+  bool wl_dirty = true;        // members changed since the lists were built
+  int wl_key[6] = {-1, -1, -1, -1, -1, -1};
+  const WorkItem *wl_ptr[7] = {};  // the lists in wl_buf (null: none) ...
+  int wl_n[7] = {};                // ... and their lengths
 };
 
 namespace {
@@ -533,7 +541,142 @@ int refresh(mlc_ctx *x) {
   }
   x->key = k;
   x->table_dirty = false;
+  x->wl_dirty = true;
   return MLC_OK;
+}
+
+// Work lists of an uneven batch (kernels read them through WorkItem; see
+// mlc_device.cuh): one entry per block that has work, for each tiling the
+// step launches, in the order of the grids they replace (tiles along j
+// fastest).  A batch whose members all have the same extents keeps the plain
+// grids.  Called before every launch sequence (never inside a capture); the
+// lists follow the members and the launch shapes of x->key.L.
+template <class R>
+int ensure_lists(mlc_ctx *x) {
+  LaunchGeom &L = x->key.L;
+  std::vector<const Member *> act;
+  for (const Member &m : x->mem)
+    if (m.used) act.push_back(&m);
+  bool uneven = false;
+  for (const Member *m : act)
+    uneven = uneven || m->g.jx != L.jx || m->g.iy != L.iy || m->g.kz != L.kz;
+  const int key[6] = {uneven ? 1 : 0, L.col_x, L.col_y, L.vert_x, L.vert_y, L.htile};
+  // the launch geometry always takes the lists from the context (a copy of
+  // an older geometry may carry stale ones)
+  auto apply = [&]() {
+    L.wl_pt = x->wl_ptr[0]; L.wl_v4 = x->wl_ptr[1]; L.wl_solve = x->wl_ptr[2];
+    L.wl_vert = x->wl_ptr[3]; L.wl_vinc = x->wl_ptr[4]; L.wl_h = x->wl_ptr[5];
+    L.wl_hinc = x->wl_ptr[6];
+    L.n_pt = x->wl_n[0]; L.n_v4 = x->wl_n[1]; L.n_solve = x->wl_n[2]; L.n_vert = x->wl_n[3];
+    L.n_vinc = x->wl_n[4]; L.n_h = x->wl_n[5]; L.n_hinc = x->wl_n[6];
+    return MLC_OK;
+  };
+  if (!x->wl_dirty && std::memcmp(key, x->wl_key, sizeof(key)) == 0) return apply();
+  for (int q = 0; q < 7; ++q) {
+    x->wl_ptr[q] = nullptr;
+    x->wl_n[q] = 0;
+  }
+  std::memcpy(x->wl_key, key, sizeof(key));
+  x->wl_key[0] = -1;  // valid only once the lists are built
+  if (!uneven) {
+    std::memcpy(x->wl_key, key, sizeof(key));
+    x->wl_dirty = false;
+    return apply();
+  }
+  const bool f64 = sizeof(R) == sizeof(double);
+  std::vector<WorkItem> all;
+  auto cdiv = [](int a, int b) { return (a + b - 1) / b; };
+  auto push = [&](int m, int a, int b, int c) {
+    all.push_back(WorkItem{(int16_t)m, (int16_t)a, (int16_t)b, (int16_t)c});
+  };
+  size_t off[7];
+  // point kernels: col_x x col_y tiles over jx x iy, level chunks
+  off[0] = all.size();
+  for (int m = 0; m < (int)act.size(); ++m) {
+    const Geom &g = act[m]->g;
+    for (int kc = 0; kc < cdiv(g.kz, kPtLevels); ++kc)
+      for (int bi = 0; bi < cdiv(g.iy, L.col_y); ++bi)
+        for (int bj = 0; bj < cdiv(g.jx, L.col_x); ++bj) push(m, bj, bi, kc);
+  }
+  // four-column lanes: 128 x 4 tiles (mixed members)
+  off[1] = all.size();
+  if (!f64)
+    for (int m = 0; m < (int)act.size(); ++m) {
+      const Geom &g = act[m]->g;
+      for (int kc = 0; kc < cdiv(g.kz, kPtLevels); ++kc)
+        for (int bi = 0; bi < cdiv(g.iy, 4); ++bi)
+          for (int bj = 0; bj < cdiv(g.jx, 128); ++bj) push(m, bj, bi, kc);
+    }
+  // column solves: 128-column segments of the rows i = 2 .. iy-2
+  off[2] = all.size();
+  for (int m = 0; m < (int)act.size(); ++m) {
+    const Geom &g = act[m]->g;
+    for (int r = 0; r < g.iy - 3; ++r)
+      for (int bj = 0; bj < cdiv(g.jx - 1, 128); ++bj) push(m, bj, r, 0);
+  }
+  // vertical WAF: column tiles, the member's own fields of the R table
+  off[3] = all.size();
+  for (int m = 0; m < (int)act.size(); ++m) {
+    const Geom &g = act[m]->g;
+    const int nf = n_table_r(act[m]->dims, x->prm, f64);
+    for (int bi = 0; bi < cdiv(g.iy - 1, L.vert_y); ++bi)
+      for (int bj = 0; bj < cdiv(g.jx - 1, L.vert_x); ++bj)
+        for (int f = 0; f < nf; ++f) push(m, bj, bi, f);
+  }
+  // the same for theta_v and Exner of mixed members
+  off[4] = all.size();
+  if (!f64)
+    for (int m = 0; m < (int)act.size(); ++m) {
+      const Geom &g = act[m]->g;
+      for (int bi = 0; bi < cdiv(g.iy - 1, L.vert_y); ++bi)
+        for (int bj = 0; bj < cdiv(g.jx - 1, L.vert_x); ++bj)
+          for (int f = 0; f < 2; ++f) push(m, bj, bi, f);
+    }
+  // horizontal WAF tiles of the shape in use, every level
+  auto htiles = [&](HShape h) {
+    const int S = 32 * h.v - 4;
+    for (int m = 0; m < (int)act.size(); ++m) {
+      const Geom &g = act[m]->g;
+      const int tj = cdiv(g.jx - 3 - hshape_ob0(h.v), S), ti = cdiv(g.iy - 1, h.nw);
+      for (int k = 0; k < g.kz; ++k)
+        for (int bi = 0; bi < ti; ++bi)
+          for (int bj = 0; bj < tj; ++bj) push(m, bj, bi, k);
+    }
+  };
+  off[5] = all.size();
+  htiles(hshape((int)sizeof(R), L.htile));
+  off[6] = all.size();
+  if (!f64) htiles(hshape_inc(L.htile));
+  const size_t total = all.size();
+  if (total > x->wl_cap) {
+    if (x->wl_buf) MLC_TRY(cudaFree(x->wl_buf));
+    x->wl_buf = nullptr;
+    x->wl_cap = 0;
+    cudaError_t e = cudaMalloc(&x->wl_buf, total * sizeof(WorkItem));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      x->wl_buf = nullptr;
+      return MLC_ERR_NOMEM;
+    }
+    x->wl_cap = total;
+  }
+  MLC_TRY(cudaMemcpyAsync(x->wl_buf, all.data(), total * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                          x->stream));
+  MLC_TRY(cudaStreamSynchronize(x->stream));
+  for (int q = 0; q < 7; ++q) {
+    const size_t end = q == 6 ? total : off[q + 1];
+    x->wl_n[q] = (int)(end - off[q]);
+    x->wl_ptr[q] = x->wl_n[q] ? x->wl_buf + off[q] : nullptr;
+  }
+  std::memcpy(x->wl_key, key, sizeof(key));
+  x->wl_dirty = false;
+  return apply();
+}
+
+template <class R>
+int refresh_all(mlc_ctx *x) {
+  MLC_CHK(refresh<R>(x));
+  return ensure_lists<R>(x);
 }
 
 // Optional per-launch event recorder (eager steps only, never captured).
@@ -675,7 +818,7 @@ bool ready(const mlc_ctx *x) {
 
 template <class R>
 int step_impl(mlc_ctx *x, int nsteps) {
-  MLC_CHK(refresh<R>(x));
+  MLC_CHK(refresh_all<R>(x));
   if (x->key.L.nmem == 0 || nsteps == 0) return MLC_OK;
   if (x->use_graphs) {
     if (!x->graph_valid || std::memcmp(&x->graph_key, &x->key, sizeof(GraphKey)) != 0)
@@ -1179,6 +1322,7 @@ void release(mlc_ctx *x) {
   if (x->clks) cudaFree(x->clks);
   if (x->diags) cudaFree(x->diags);
   if (x->table) cudaFree(x->table);
+  if (x->wl_buf) cudaFree(x->wl_buf);
   if (x->pool) cudaMemPoolDestroy(x->pool);
   if (x->stream) cudaStreamDestroy(x->stream);
   delete x;
@@ -1519,7 +1663,7 @@ int mlc_step(mlc_ctx *x, int nsteps, mlc_diag *out) {
 int mlc_step_dynamics(mlc_ctx *x) {
   if (!x) return MLC_ERR_INVALID;
   if (x->step_open || !ready(x)) return MLC_ERR_STATE;
-  MLC_CHK(x->mixed ? refresh<float>(x) : refresh<double>(x));
+  MLC_CHK(x->mixed ? refresh_all<float>(x) : refresh_all<double>(x));
   if (x->key.L.nmem == 0) return MLC_OK;
   if (x->mixed) enqueue_step<float>(x, nullptr, kStepDynamics);
   else enqueue_step<double>(x, nullptr, kStepDynamics);
@@ -1542,7 +1686,7 @@ int mlc_member_set_tendencies(mlc_ctx *x, int m, const mlc_tend_ptrs *t) {
 int mlc_step_finish(mlc_ctx *x, mlc_diag *out) {
   if (!x) return MLC_ERR_INVALID;
   if (!x->step_open) return MLC_ERR_STATE;
-  MLC_CHK(x->mixed ? refresh<float>(x) : refresh<double>(x));
+  MLC_CHK(x->mixed ? refresh_all<float>(x) : refresh_all<double>(x));
   if (x->key.L.nmem > 0) {
     if (x->mixed) enqueue_step<float>(x, nullptr, kStepFinish);
     else enqueue_step<double>(x, nullptr, kStepFinish);
@@ -1699,6 +1843,7 @@ bool shapes_fit(const LaunchGeom &L) {
 // Per-group device time (ms) of `steps` eager steps with the shapes in x->key.L.
 template <class R>
 int time_groups(mlc_ctx *x, int steps, double ms[4]) {
+  MLC_CHK(ensure_lists<R>(x));  // the trial's launch shapes
   Recorder rec;
   rec.s = x->stream;
   for (int n = 0; n < steps; ++n) enqueue_step<R>(x, &rec);
@@ -1723,7 +1868,7 @@ void set_shapes(LaunchGeom &L, int col, int solve, int vert, int tile) {
 
 template <class R>
 int autotune_impl(mlc_ctx *x, int steps, mlc_tune_report *rep) {
-  MLC_CHK(refresh<R>(x));
+  MLC_CHK(refresh_all<R>(x));
   if (x->key.L.nmem == 0) return MLC_ERR_STATE;
   // snapshot every member's arena and the clocks; each trial starts from it
   size_t total = x->mem.size() * sizeof(Clock);

@@ -298,6 +298,31 @@ struct DF {
   __device__ __forceinline__ float hi(size_t o) const { return p[o]; }
 };
 
+// ---- work lists of an uneven batch ------------------------------------------
+// A launch over members of different extents covers, by default, the largest
+// member's tiles for every member (blockIdx.z is the member; blocks outside a
+// smaller member return at once).  With a work list the launch has one block
+// per entry instead, and each entry names the member and the block's tile in
+// the kernel's own coordinates, so only the members' own tiles are launched:
+//   point kernels   a = tile along j, b = tile along i, c = level chunk
+//   column solves   a = 128-column segment, b = row index (i - 2)
+//   vertical WAF    a = column tile along j, b = tile along i, c = field
+//   horizontal WAF  a = tile along j, b = tile along i, c = level - 1
+// The lists are built on the host whenever the members or the launch shapes
+// change (all values below 2^15: extents <= 32768, levels <= 128, members
+// <= 4096, fields <= 24).
+struct WorkItem {
+  int16_t m, a, b, c;
+};
+// blockIdx.x of a grid of tiles_j x ti tiles (y: c, z: member) as a work item
+__device__ __forceinline__ WorkItem grid_item(int tiles_j) {
+  return {(int16_t)blockIdx.z, (int16_t)(blockIdx.x % (unsigned)tiles_j),
+          (int16_t)(blockIdx.x / (unsigned)tiles_j), (int16_t)blockIdx.y};
+}
+__device__ __forceinline__ WorkItem work_item(const WorkItem *wl, int tiles_j) {
+  return wl ? wl[blockIdx.x] : grid_item(tiles_j);
+}
+
 // Point kernels run one thread per grid point (j, i, k): blocks of
 // (blockDim.x, blockDim.y) points along (j, i); grid x = the tiles along j
 // times the tiles along i, y = the level, z = the member.  j0, i0 are the
@@ -313,6 +338,11 @@ __device__ __forceinline__ Pt point_of(int tiles_j, int j0, int i0) {
   const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
   return {bj * (int)blockDim.x + (int)threadIdx.x + j0, bi * (int)blockDim.y + (int)threadIdx.y + i0,
           (int)blockIdx.y * kPtLevels + 1};
+}
+// the same for the tile of a work item
+__device__ __forceinline__ Pt point_at(const WorkItem &w, int j0, int i0) {
+  return {(int)w.a * (int)blockDim.x + (int)threadIdx.x + j0,
+          (int)w.b * (int)blockDim.y + (int)threadIdx.y + i0, (int)w.c * kPtLevels + 1};
 }
 
 // The state with the roles the launch works on.

@@ -39,13 +39,15 @@ __device__ __forceinline__ F2 qfactor_df(const float *qx, size_t o, size_t F, in
 
 // dynamical_core :1121-1123 and tvirt_to_temp :1629-1648
 template <class R>
-__global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const Scal &c = D.c;
   const State<R> st = state_of(D, 0, (D.clk->adv_role + advoff) & 1);
-  const Pt q_ = point_of(tiles_j, 1, 1);
+  const Pt q_ = point_at(wi, 1, 1);
   const int j = q_.j, k0 = q_.k;
   if (k0 > g.kz) return;
   const int i = q_.i;
@@ -230,8 +232,10 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
 // (boundary, Main/mod_moloch.F90:478-497), per point; the clock has already
 // moved by dtsec.
 template <class R>
-__global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const Scal &c = D.c;
@@ -239,7 +243,7 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const Bdy<R> &bd = D.bd;
   const Clock *clk = D.clk;
   const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
-  const Pt q_ = point_of(tiles_j, 2, 2);
+  const Pt q_ = point_at(wi, 2, 2);
   const int j = q_.j, k0 = q_.k;
   if (k0 > g.kz) return;
   const int i = q_.i;
@@ -473,14 +477,16 @@ __global__ void __launch_bounds__(256) k_spec_modes(const Dom<R> *__restrict__ d
 // f(j,i,k) += cnudge(k) sum_m bvx(j,m) G(i,m) for t, u and v at one point
 // (j, i from 2), kPtLevels levels per thread.
 template <class R>
-__global__ void k_spec_apply(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_spec_apply(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Scal &c = D.c;
   const Clock *clk = D.clk;
   if (!spectral_due(c, clk)) return;
   const Geom g = D.g;
-  const Pt q_ = point_of(tiles_j, 2, 2);
+  const Pt q_ = point_at(wi, 2, 2);
   const int j = q_.j, i = q_.i, k0 = q_.k;
   if (k0 > g.kz || j > g.jx - 1 || i > g.iy - 1) return;
   const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
@@ -565,14 +571,16 @@ __global__ void k_end_ps(const Dom<R> *__restrict__ doms, int uvoff, int advoff)
 constexpr int kEndAll = 0, kEndPre = 1, kEndPost = 2;
 constexpr double kTracFloor = 1.0e-50;  // mkslice's tracer floor (Main/mod_slice.F90:141-147)
 template <class R, int PH>
-__global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
   const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
-  const Pt q_ = point_of(tiles_j, 1, 1);
+  const Pt q_ = point_at(wi, 1, 1);
   const int j = q_.j, i = q_.i;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
   if (j > jx - 1 || i > iy - 1 || q_.k > kz) return;
@@ -701,16 +709,18 @@ __device__ __forceinline__ void st4f(float *p, const float (&x)[4]) {
 // chunks, z = member.
 template <class R>
 __global__ void __launch_bounds__(128) k_end_cross_v4(const Dom<R> *__restrict__ doms, int uvoff,
-                                                      int advoff, int tiles_j) {
+                                                      int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
   static_assert(sizeof(R) == sizeof(float), "FP32 fields");
-  const Dom<R> &D = doms[blockIdx.z];
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
-  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int bj = wi.a, bi = wi.b;
   const int e0 = (bj * 32 + (int)threadIdx.x) * 4;
   const int i = bi * (int)blockDim.y + (int)threadIdx.y + 1;
-  const int k0 = (int)blockIdx.y * kPtLevels + 1;
+  const int k0 = (int)wi.c * kPtLevels + 1;
   if (e0 + 1 > jx - 1 || i > iy - 1 || k0 > kz) return;
   const Scal &c = D.c;
   const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
@@ -850,8 +860,10 @@ __global__ void __launch_bounds__(128) k_end_cross_v4(const Dom<R> *__restrict__
 
 // uvxtouvstag at the end of status_update (:1440)
 template <class R>
-__global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int uv = (D.clk->uv_role + uvoff) & 1, adv = (D.clk->adv_role + advoff) & 1;
@@ -859,7 +871,7 @@ __global__ void k_end_uvstag(const Dom<R> *__restrict__ doms, int uvoff, int adv
   const R *__restrict__ vx = D.vx[adv];
   R *__restrict__ u = D.u[uv];
   R *__restrict__ v = D.v[uv];
-  const Pt q_ = point_of(tiles_j, 1, 1);
+  const Pt q_ = point_at(wi, 1, 1);
   const int j = q_.j, k0 = q_.k;
   if (k0 > g.kz) return;
   const int i = q_.i;
@@ -1172,6 +1184,7 @@ inline dim3 grid2(int nj, int ni, dim3 b, int nmem) {
 // grid of a point kernel over nj x ni points per level
 inline dim3 pt_grid(const LaunchGeom &L, int nj, int ni, int &tiles_j) {
   tiles_j = (nj + L.col_x - 1) / L.col_x;
+  if (L.wl_pt) return dim3((unsigned)L.n_pt, 1, 1);  // one block per work item
   const int ti = (ni + L.col_y - 1) / L.col_y;
   return dim3((unsigned)(tiles_j * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
               (unsigned)L.nmem);
@@ -1191,11 +1204,13 @@ int reduce_blocks(const Geom &g) {
 // 1419-1424): on jci x ici at the kz+1 interfaces, tke + dtsec * tketen (the
 // physics' tendency; none in a whole step), then the floor tkemin.
 template <class R>
-__global__ void k_end_tke(const Dom<R> *__restrict__ doms, int whole, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_end_tke(const Dom<R> *__restrict__ doms, int whole, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active || !D.c.tke) return;
   const Geom g = D.g;
-  const Pt q = point_of(tiles_j, 1, 1);
+  const Pt q = point_at(wi, 1, 1);
   if (q.j < 2 || q.j > g.jx - 2 || q.i < 2 || q.i > g.iy - 2 || q.k > g.kz) return;
   const R *ten = whole ? nullptr : D.tend;
   // tketen follows the kz-plane tendencies (t, u, v, the species, tracers)
@@ -1216,7 +1231,7 @@ void Launch<R>::end_tvirt(const LaunchGeom &L, const Dom<R> *d, int advoff, cuda
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-  k_end_tvirt<R><<<grd, b, 0, s>>>(d, advoff, tj);
+  k_end_tvirt<R><<<grd, b, 0, s>>>(d, advoff, tj, L.wl_pt);
 }
 
 template <class R>
@@ -1232,7 +1247,7 @@ void Launch<R>::bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int a
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 2, L.iy - 2, tj);
-  k_bdy_relax<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  k_bdy_relax<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
 }
 
 template <class R>
@@ -1244,7 +1259,7 @@ void Launch<R>::bdy_spectral(const LaunchGeom &L, const Dom<R> *d, int uvoff, in
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 2, L.iy - 2, tj);
-  k_spec_apply<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  k_spec_apply<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
 }
 
 template <class R>
@@ -1253,12 +1268,14 @@ void Launch<R>::end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int a
   k_end_ps<R><<<grid2(L.jx - 3, L.iy - 3, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
   if constexpr (sizeof(R) == sizeof(float)) {
     const int tj = (L.jx - 1 + 127) / 128, ti = (L.iy - 1 + 3) / 4;
-    const dim3 grd((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels), (unsigned)L.nmem);
-    k_end_cross_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, advoff, tj);
+    const dim3 grd = L.wl_v4 ? dim3((unsigned)L.n_v4, 1, 1)
+                             : dim3((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
+                                    (unsigned)L.nmem);
+    k_end_cross_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, advoff, tj, L.wl_v4);
   } else {
     int tj;
     const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-    k_end_cross<R, kEndAll><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+    k_end_cross<R, kEndAll><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
   }
 }
 
@@ -1269,10 +1286,10 @@ void Launch<R>::end_cross_split(const LaunchGeom &L, const Dom<R> *d, int uvoff,
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
   if (post) {
-    k_end_cross<R, kEndPost><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+    k_end_cross<R, kEndPost><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
   } else {
     k_end_ps<R><<<grid2(L.jx - 3, L.iy - 3, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
-    k_end_cross<R, kEndPre><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+    k_end_cross<R, kEndPre><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
   }
 }
 
@@ -1281,7 +1298,7 @@ void Launch<R>::end_uvstag(const LaunchGeom &L, const Dom<R> *d, int uvoff, int 
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
-  k_end_uvstag<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj);
+  k_end_uvstag<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
 }
 
 template <class R>
@@ -1289,7 +1306,7 @@ void Launch<R>::end_tke(const LaunchGeom &L, const Dom<R> *d, bool whole_step, c
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
   const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
-  k_end_tke<R><<<grd, b, 0, s>>>(d, whole_step ? 1 : 0, tj);
+  k_end_tke<R><<<grd, b, 0, s>>>(d, whole_step ? 1 : 0, tj, L.wl_pt);
 }
 
 template <class R>

@@ -25,6 +25,16 @@ struct LaunchGeom {
   int nadv_d;            // advected FP64 fields per member (mixed: theta_v, Exner)
   int red_blocks;        // reduction blocks of the largest member
   int solve_df;          // mixed solve: recurrence in double-float (1) or FP32 (0)
+  // work lists of an uneven batch (device arrays; null: grids over the
+  // largest member) and their lengths, one per tiling
+  const WorkItem *wl_pt;     // col_x x col_y tiles, level chunks
+  const WorkItem *wl_v4;     // 128 x 4 tiles, level chunks
+  const WorkItem *wl_solve;  // 128-column row segments
+  const WorkItem *wl_vert;   // vert_x x vert_y column tiles, R fields
+  const WorkItem *wl_vinc;   // the same, the two double-float fields
+  const WorkItem *wl_h;      // horizontal WAF tiles (shape htile), levels
+  const WorkItem *wl_hinc;   // increment-form WAF tiles, levels
+  int n_pt, n_v4, n_solve, n_vert, n_vinc, n_h, n_hinc;
 };
 
 template <class R> struct Launch {

@@ -35,11 +35,13 @@ __device__ __forceinline__ double relax_weight(const int32_t *ibnd, const double
 }
 
 template <class R>
-__global__ void k_sound_prep(const Dom<R> *__restrict__ doms, int advoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_sound_prep(const Dom<R> *__restrict__ doms, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
-  const Pt q = point_of(tiles_j, 1, 1);
+  const Pt q = point_at(wi, 1, 1);
   if (q.j > g.jx - 1 || q.i > g.iy - 1 || q.k > g.kz) return;
   const int adv = (D.clk->adv_role + advoff) & 1;
   const double *__restrict__ tetav = D.tetav[adv];
@@ -64,11 +66,13 @@ __global__ void k_sound_prep(const Dom<R> *__restrict__ doms, int advoff, int ti
 
 // Main/mod_moloch.F90:582-618
 template <class R>
-__global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+__global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
-  const Pt q = point_of(tiles_j, 1, 1);
+  const Pt q = point_at(wi, 1, 1);
   const int j = q.j, i = q.i, kz = g.kz;
   if (j > g.jx - 1 || i > g.iy - 1 || q.k > kz) return;
   const Scal &c = D.c;
@@ -148,17 +152,20 @@ constexpr int kDvW = 128;
 constexpr int kDvZW = kDvW + 4;                   // raw divergence row, 2-column halo each side
 constexpr int kDvStage = 3 * kDvZW + 7 * kDvW;   // doubles of one stage
 template <class R>
-__global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last) {
+__global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last,
+    const WorkItem *__restrict__ wl) {
   static_assert(sizeof(R) == sizeof(double), "FP64 member");
   constexpr int NS = kDvStages;
   extern __shared__ __align__(16) double dv_smem[];
   __shared__ __align__(8) uint64_t mbar[NS];
-  const Dom<R> &D = doms[blockIdx.z];
+  const WorkItem wi = wl ? wl[blockIdx.x]
+                          : WorkItem{(int16_t)blockIdx.z, (int16_t)blockIdx.x, (int16_t)blockIdx.y, 0};
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int t = (int)threadIdx.x;
-  const int x0 = (int)blockIdx.x * kDvW;
-  const int i = (int)blockIdx.y + 2;
+  const int x0 = (int)wi.a * kDvW;
+  const int i = (int)wi.b + 2;
   if (x0 + 1 > g.jx - 2 || i > g.iy - 2) return;  // uniform over the block
   const int j = x0 + t + 1;
   const bool act = j >= 2 && j <= g.jx - 2;
@@ -370,16 +377,19 @@ constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
 // 0.73 ms of solves a step against 0.95 for the same thread-per-column
 // kernel with register prefetch of one level.)
 template <class R, bool DFR>
-__global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last) {
+__global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last,
+    const WorkItem *__restrict__ wl) {
   constexpr int NS = kSvStages;
   extern __shared__ __align__(16) float sv_smem[];
   __shared__ __align__(8) uint64_t mbar[NS];
-  const Dom<R> &D = doms[blockIdx.z];
+  const WorkItem wi = wl ? wl[blockIdx.x]
+                          : WorkItem{(int16_t)blockIdx.z, (int16_t)blockIdx.x, (int16_t)blockIdx.y, 0};
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int t = (int)threadIdx.x;
-  const int x0 = (int)blockIdx.x * kSvW;          // first column (0-based j-1) of the block
-  const int i = (int)blockIdx.y + 2;
+  const int x0 = (int)wi.a * kSvW;          // first column (0-based j-1) of the block
+  const int i = (int)wi.b + 2;
   if (x0 + 1 > g.jx - 2 || i > g.iy - 2) return;  // uniform over the block
   const int j = x0 + t + 1;
   const bool act = j >= 2 && j <= g.jx - 2;
@@ -639,8 +649,10 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
 // Main/mod_moloch.F90:677-721 with divergence_damping :738-765 folded in
 template <class R>
 __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int advoff,
-                                 int tiles_j) {
-  const Dom<R> &D = doms[blockIdx.z];
+                                 int tiles_j,
+    const WorkItem *__restrict__ wl) {
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const Scal &c = D.c;
@@ -654,7 +666,7 @@ __global__ void k_sound_momentum(const Dom<R> *__restrict__ doms, int uvoff, int
   const R *__restrict__ zraw = D.zdiv2;
   const double *__restrict__ pai = D.pai[adv];
   const double *__restrict__ tetav = D.tetav[adv];
-  const Pt q = point_of(tiles_j, 1, 1);
+  const Pt q = point_at(wi, 1, 1);
   const int j = q.j, i = q.i;
   if (j > g.jx || i > g.iy || q.k > g.kz) return;
   constexpr bool mixed = sizeof(R) == sizeof(float);
@@ -781,16 +793,18 @@ struct West4 {
 // element read singly, the level below carried from the previous level.
 template <class R>
 __global__ void __launch_bounds__(128) k_sound_div_v4(const Dom<R> *__restrict__ doms, int uvoff,
-                                                      int tiles_j) {
+                                                      int tiles_j,
+    const WorkItem *__restrict__ wl) {
   static_assert(sizeof(R) == sizeof(float), "FP32 fields");
-  const Dom<R> &D = doms[blockIdx.z];
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
-  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int bj = wi.a, bi = wi.b;
   const int e0 = (bj * 32 + (int)threadIdx.x) * 4;
   const int i = bi * (int)blockDim.y + (int)threadIdx.y + 1;
-  const int k0 = (int)blockIdx.y * kPtLevels + 1;
+  const int k0 = (int)wi.c * kPtLevels + 1;
   if (e0 + 1 > jx - 1 || i > iy - 1 || k0 > kz) return;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
@@ -912,16 +926,18 @@ __global__ void __launch_bounds__(128) k_sound_div_v4(const Dom<R> *__restrict__
 // level chunks, z = member.
 template <class R>
 __global__ void __launch_bounds__(128) k_sound_momentum_v4(const Dom<R> *__restrict__ doms,
-                                                           int uvoff, int advoff, int tiles_j) {
+                                                           int uvoff, int advoff, int tiles_j,
+    const WorkItem *__restrict__ wl) {
   static_assert(sizeof(R) == sizeof(float), "FP32 fields");
-  const Dom<R> &D = doms[blockIdx.z];
+  const WorkItem wi = work_item(wl, tiles_j);
+  const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
-  const int bj = (int)(blockIdx.x % (unsigned)tiles_j), bi = (int)(blockIdx.x / (unsigned)tiles_j);
+  const int bj = wi.a, bi = wi.b;
   const int e0 = (bj * 32 + (int)threadIdx.x) * 4;  // j-1 of the lane's first column
   const int i = bi * (int)blockDim.y + (int)threadIdx.y + 1;
-  const int k0 = (int)blockIdx.y * kPtLevels + 1;
+  const int k0 = (int)wi.c * kPtLevels + 1;
   if (e0 + 1 > jx || i > iy || k0 > kz) return;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
@@ -1051,6 +1067,7 @@ inline dim3 col_block(const LaunchGeom &L) { return dim3((unsigned)L.col_x, (uns
 // grid of a point kernel over nj x ni points per level
 inline dim3 pt_grid(const LaunchGeom &L, int nj, int ni, int &tiles_j) {
   tiles_j = (nj + L.col_x - 1) / L.col_x;
+  if (L.wl_pt) return dim3((unsigned)L.n_pt, 1, 1);  // one block per work item
   const int ti = (ni + L.col_y - 1) / L.col_y;
   return dim3((unsigned)(tiles_j * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
               (unsigned)L.nmem);
@@ -1061,19 +1078,21 @@ template <class R>
 void Launch<R>::sound_prep(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
   int tj;
   const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-  k_sound_prep<R><<<grd, col_block(L), 0, s>>>(d, advoff, tj);
+  k_sound_prep<R><<<grd, col_block(L), 0, s>>>(d, advoff, tj, L.wl_pt);
 }
 
 template <class R>
 void Launch<R>::sound_div(const LaunchGeom &L, const Dom<R> *d, int uvoff, cudaStream_t s) {
   if constexpr (sizeof(R) == sizeof(float)) {
     const int tj = (L.jx - 1 + 127) / 128, ti = (L.iy - 1 + 3) / 4;
-    const dim3 grd((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels), (unsigned)L.nmem);
-    k_sound_div_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, tj);
+    const dim3 grd = L.wl_v4 ? dim3((unsigned)L.n_v4, 1, 1)
+                             : dim3((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
+                                    (unsigned)L.nmem);
+    k_sound_div_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, tj, L.wl_v4);
   } else {
     int tj;
     const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-    k_sound_div<R><<<grd, col_block(L), 0, s>>>(d, uvoff, tj);
+    k_sound_div<R><<<grd, col_block(L), 0, s>>>(d, uvoff, tj, L.wl_pt);
   }
 }
 
@@ -1085,16 +1104,19 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
   // launch shape of LaunchGeom is not used)
   if constexpr (sizeof(R) == sizeof(float)) {
     const int tj = (L.jx - 1 + kSvW - 1) / kSvW;
-    const dim3 grid((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem);
+    const dim3 grid = L.wl_solve ? dim3((unsigned)L.n_solve, 1, 1)
+                                 : dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem);
     const size_t smem = (size_t)kSvStages * kSvStage * sizeof(float);
     if (L.solve_df)
-      k_solve_mixed<R, true><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0);
+      k_solve_mixed<R, true><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
     else
-      k_solve_mixed<R, false><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0);
+      k_solve_mixed<R, false><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
   } else {
     const int tj = (L.jx - 1 + kDvW - 1) / kDvW;
-    k_sound_solve<R><<<dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem), kDvW,
-                       (size_t)kDvStages * kDvStage * sizeof(double), s>>>(d, advoff, last ? 1 : 0);
+    const dim3 grid = L.wl_solve ? dim3((unsigned)L.n_solve, 1, 1)
+                                 : dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem);
+    k_sound_solve<R><<<grid, kDvW, (size_t)kDvStages * kDvStage * sizeof(double), s>>>(
+        d, advoff, last ? 1 : 0, L.wl_solve);
   }
 }
 
@@ -1104,12 +1126,14 @@ void Launch<R>::sound_momentum(const LaunchGeom &L, const Dom<R> *d, int uvoff, 
   if constexpr (sizeof(R) == sizeof(float)) {
     // lanes of four columns: 128 columns by 4 rows a block
     const int tj = (L.jx + 127) / 128, ti = (L.iy + 3) / 4;
-    const dim3 grd((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels), (unsigned)L.nmem);
-    k_sound_momentum_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, advoff, tj);
+    const dim3 grd = L.wl_v4 ? dim3((unsigned)L.n_v4, 1, 1)
+                             : dim3((unsigned)(tj * ti), (unsigned)((L.kz + kPtLevels - 1) / kPtLevels),
+                                    (unsigned)L.nmem);
+    k_sound_momentum_v4<R><<<grd, dim3(32, 4), 0, s>>>(d, uvoff, advoff, tj, L.wl_v4);
   } else {
     int tj;
     const dim3 grd = pt_grid(L, L.jx, L.iy, tj);
-    k_sound_momentum<R><<<grd, col_block(L), 0, s>>>(d, uvoff, advoff, tj);
+    k_sound_momentum<R><<<grd, col_block(L), 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
   }
 }
 

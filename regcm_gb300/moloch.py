@@ -153,7 +153,8 @@ def _set_launch_shapes(lib, ctx, shapes):
 _SHARED_PARAMS = ("dtsec", "dx", "mo_ztop", "mo_h", "mo_a0", "mo_nadv", "mo_nsound",
                   "mo_divdamp", "mo_divfilter", "mo_top_nudge", "mo_spectral_nudge",
                   "do_apply_bdy", "lrotllr", "ipptls", "present_qc", "present_qi", "nspgx",
-                  "nspgd", "debug_level", "precision", "dtrad")
+                  "nspgd", "debug_level", "precision", "dtrad", "bdy_use_lehmann", "ibltyp",
+                  "high_nudge", "medium_nudge", "low_nudge")
 
 
 def _same_params(a: abi.mlc_params, b: abi.mlc_params) -> bool:

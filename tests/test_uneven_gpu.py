@@ -1,8 +1,9 @@
 """Uneven batches and the serving pool.
 
-Domains of different extents and level counts advance together (one launch
-per kernel stage covering the largest member); each one must reach exactly
-the state it reaches alone, and stay at the FP64 oracle's state.  In a pool,
+Domains of different extents and level counts advance together, one launch
+per kernel stage whose blocks come from a work list of the members' own
+tiles; each one must reach exactly the state it reaches alone (where the
+plain grids serve it), and stay at the FP64 oracle's state.  In a pool,
 members join and leave between steps: a member's result is the same whether
 it ran alone or in the mix, and the byte budget and slot count are enforced.
 """
@@ -73,6 +74,26 @@ def test_uneven_batch_against_oracle_fp64():
         got = member_state(b, m, cases[m])
         for n in ("u", "v", "w", "tetav", "pai", "qx"):
             assert rel_l2(got[n], ref[n]) <= 1e-12, (c.name, n)
+    b.close()
+
+
+@pytest.mark.parametrize("col,vert,htile", [((32, 4), (32, 4), 0), ((64, 2), (64, 2), 1),
+                                            ((64, 4), (32, 8), 2), ((16, 8), (128, 1), 3),
+                                            ((128, 1), (32, 2), 0), ((32, 8), (32, 4), 1)])
+def test_uneven_batch_every_launch_shape_fp64(col, vert, htile):
+    """The work lists follow the launch shapes: with every point, column and
+    tile shape an FP64 uneven batch equals its members run alone."""
+    from regcm_gb300.moloch import DEFAULT_SHAPES
+    cases = uneven(abi.MLC_PREC_FP64)
+    b = MolochBatch(cases)
+    b.set_launch_shapes(dict(DEFAULT_SHAPES, col_x=col[0], col_y=col[1], vert_x=vert[0],
+                             vert_y=vert[1], htile=htile))
+    b.step(2)
+    for m, c in enumerate(uneven(abi.MLC_PREC_FP64)):
+        ga = alone_state(c, 2)
+        gb = member_state(b, m, cases[m])
+        for n in ga:
+            assert np.array_equal(ga[n], gb[n]), (c.name, n, col, vert, htile)
     b.close()
 
 
