@@ -662,20 +662,39 @@ def run_serving(args, rank, world):
     budget = int(args.budget_gb * 1e9)
     prec = abi.MLC_PREC_FP64 if args.precision == "fp64" else abi.MLC_PREC_MIXED
     params = cs.config4_request(0, scale=0.05, precision=prec)[0].params
-    steps = [cs.config4_request(r, scale=0.05)[1] for r in range(nreq)]
-    out = {}
+    steps = [cs.config4_shape(r)[1] for r in range(nreq)]
+    workers = max(4, min(16, cpu_threads()))
+    out, wall = {}, {}
     with ClockSampler(dev) as clk:
         for lam in rates:
             arr = poisson_arrivals(lam, nreq, seed=int(lam * 1000) + 7)
             reqs = [Request(r, float(arr[r]), steps[r],
                             (lambda r=r: cs.config4_request(r, precision=prec)[0]))
                     for r in range(nreq)]
-            out[lam] = serve_stream(reqs, params, budget, capacity=args.capacity)
+            out[lam] = serve_stream(reqs, params, budget, capacity=args.capacity,
+                                    workers=workers, prefetch=2 * workers)
+        # the same stream's first `wall_requests` requests on the wall clock:
+        # payloads built before the stream starts (the client's preparation is
+        # not in the latency), arrivals in real time
+        if args.wall_requests:
+            from concurrent.futures import ThreadPoolExecutor
+            nw = min(args.wall_requests, nreq)
+            for lam in rates:
+                arr = poisson_arrivals(lam, nreq, seed=int(lam * 1000) + 7)
+                with ThreadPoolExecutor(max_workers=workers) as ex:
+                    built = list(ex.map(lambda r: cs.config4_request(r, precision=prec)[0],
+                                        range(nw)))
+                reqs = [Request(r, float(arr[r]), steps[r], (lambda c=built[r]: c))
+                        for r in range(nw)]
+                del built
+                wall[lam] = serve_stream(reqs, params, budget, capacity=args.capacity,
+                                         clock="wall", prefetch=nw, workers=1)
         # one request at a time, plain FP64 (service times do not depend on the rate)
         arr = poisson_arrivals(rates[0], nreq, seed=int(rates[0] * 1000) + 7)
         base_reqs = [Request(r, float(arr[r]), steps[r], None) for r in range(nreq)]
         one = serve_one_at_a_time(
-            base_reqs, lambda r: (lambda rid=r.rid: cs.config4_request(rid)[0]))
+            base_reqs, lambda r: (lambda rid=r.rid: cs.config4_request(rid)[0]),
+            workers=workers, prefetch=2 * workers)
     if rank != 0:
         return
     # the FP64 queue's latencies at every rate from the measured service times
@@ -702,6 +721,7 @@ def run_serving(args, rank, world):
                    "precision": args.precision, "requests_per_rate": nreq,
                    "parallelism": f"replicas{world}"},
         "serving": {str(l): v for l, v in out.items()},
+        "serving_wall_clock": {str(l): v for l, v in wall.items()} or None,
         "plain_fp64_one_at_a_time": {"service_rate": one["service_rate"],
                                      "per_rate": {str(l): v for l, v in base.items()}},
         "ratio_to_plain_fp64": {str(l): out[l]["value"] / base[l]["value"] for l in rates},
@@ -828,6 +848,8 @@ def main():
     ap.add_argument("--rates", default="2,8,32", help="arrival rates per second (c4)")
     ap.add_argument("--requests", type=int, default=200, help="requests per rate (c4)")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="arena budget (c4)")
+    ap.add_argument("--wall-requests", type=int, default=0,
+                    help="c4: also serve the first N requests of each stream on the wall clock")
     ap.add_argument("--capacity", type=int, default=256, help="member slots (c4)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],

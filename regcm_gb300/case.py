@@ -487,13 +487,19 @@ def config3_member(m: int, scale: float = 1.0, **kw) -> Case:
     return _moist(nx, ny, kz, 3000 + m, 12000.0, 60.0, 3, f"c3_m{m}_{nx}x{ny}x{kz}", **kw)
 
 
+def config4_shape(r: int, scale: float = 1.0):
+    """(n, steps) of serving request r: nx = ny log-uniform in 32-512 (scaled
+    by `scale`, floor 24 cells), steps uniform in 6-240."""
+    u = splitmix64(4000 + r, 2)
+    n = max(24, int(round(log_uniform_int(float(u[0]), 32, 512) * scale)))
+    return n, 6 + min(234, int(u[1] * 235))
+
+
 def config4_request(r: int, scale: float = 1.0, **kw):
     """Serving request r: (case, steps).  nx = ny log-uniform in 32-512,
     kz 30, steps uniform in 6-240, the moist recipe of the 3 km domain with
     the request's seed; `scale` shrinks the extents (floor 24 cells)."""
-    u = splitmix64(4000 + r, 2)
-    n = max(24, int(round(log_uniform_int(float(u[0]), 32, 512) * scale)))
-    steps = 6 + min(234, int(u[1] * 235))
+    n, steps = config4_shape(r, scale)
     return _moist(n, n, 30, 4000 + r, 3000.0, 20.0, 4, f"c4_r{r}_{n}", **kw), steps
 
 

@@ -77,12 +77,16 @@ extern "C" int mlc_fp64_peak(int repeats, double *flops) {
   }
   double best = 0.0;
   int st = MLC_OK;
-  const int per_sm[3] = {4, 8, 16};
+  // 2, 4 and 8 blocks of 256 threads an SM (8: one full wave of 2048
+  // threads), each with 4, 8 or 16 chains a thread; the same multiply-adds a
+  // thread for every chain count
+  const int per_sm[3] = {2, 4, 8};
   for (int q = 0; q < 3 && st == MLC_OK; ++q) {
-    double r8 = 0.0, r16 = 0.0;
-    // the same multiply-adds per launch for both chain counts
-    st = time_config<8>(s, e0, e1, sms * per_sm[q], 8192, repeats, &r8);
+    double r4 = 0.0, r8 = 0.0, r16 = 0.0;
+    st = time_config<4>(s, e0, e1, sms * per_sm[q], 16384, repeats, &r4);
+    if (st == MLC_OK) st = time_config<8>(s, e0, e1, sms * per_sm[q], 8192, repeats, &r8);
     if (st == MLC_OK) st = time_config<16>(s, e0, e1, sms * per_sm[q], 4096, repeats, &r16);
+    best = best > r4 ? best : r4;
     best = best > r8 ? best : r8;
     best = best > r16 ? best : r16;
   }
