@@ -98,8 +98,7 @@ __device__ __forceinline__ bool positive(T x) {
 // -1 enters as a choice of constants and of den's sign (is*den exactly), not
 // as a multiplication.
 template <class T>
-__device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) {
-  const T den = c - a;
+__device__ __forceinline__ T waf_b(T den, T num) {
   T B;
   if constexpr (sizeof(T) == sizeof(float)) {
     // FP32: the branch-free clamp, signs moved by bit operations; the guard
@@ -132,6 +131,12 @@ __device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) 
     else if (bq < ad + one_exp) B = num;                 // q < 2d
     else B = den + den;
   }
+  return B;
+}
+template <class T>
+__device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) {
+  const T den = c - a;
+  const T B = waf_b<T>(den, num);
   if constexpr (sizeof(T) == sizeof(double)) {
     // is*den as a choice of den's sign (no FP64 multiply); the fused
     // multiply-add and the final product are explicit, so that the compiler
@@ -144,6 +149,16 @@ __device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) 
     const T is = up ? T(1) : T(-1);
     return hvel * ((a + c) - (is * den + (zamu - is) * B));
   }
+}
+// The FP64 flux with hvel and zmi = zamu - is of the interface given (formed
+// once per interface for all fields, k_adv_prep): the same operations on the
+// same values as waf_flux.
+__device__ __forceinline__ double waf_flux_z(double hvel, bool up, double zmi, double a, double c,
+                                             double num) {
+  const double den = c - a;
+  const double B = waf_b<double>(den, num);
+  const double sden = up ? den : -den;
+  return __dmul_rn(hvel, (a + c) - __fma_rn(zmi, B, sden));
 }
 
 // The advected fields of a member, in the reference's order (tetav, pai,
@@ -259,9 +274,17 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
       D.tkex[adv][o] = a;
     }
     if constexpr (sizeof(R) == sizeof(double)) {
-      // the vertical WAF update's factor s(k)*zu(k) - s(k+1)*zd(k), once for
-      // all fields (FP64 arithmetic is the FP64 path's bound)
-      D.vdiv[o] = __fma_rn(-D.s[o + PS], D.sa.zrfmd[o], __dmul_rn(D.s[o], D.sa.zrfmu[o]));
+      // the vertical WAF update's factor s(k)*zu(k) - s(k+1)*zd(k), and the
+      // flux factors of interface k+1 - zamu = s*dtrdz, hvel = 0.5*s and
+      // zamu - is - once for all fields (FP64 arithmetic is the FP64 path's
+      // bound); the same expressions the vertical kernel forms per field
+      const double skp = D.s[o + PS];
+      D.vdiv[o] = __fma_rn(-skp, D.sa.zrfmd[o], __dmul_rn(D.s[o], D.sa.zrfmu[o]));
+      const double dtrdz = 0.5 * (D.c.dtstepa * D.c.rdzita);
+      const double zamu = __dmul_rn(skp, dtrdz);
+      D.vzamu[o] = zamu;
+      D.vhvel[o] = 0.5 * skp;
+      D.vzmi[o] = __dadd_rn(zamu, nonneg(zamu) ? -1.0 : 1.0);
     }
   }
 }
@@ -284,6 +307,18 @@ __device__ __forceinline__ T vflux(T dtrdz, T skp, T cm1, T ck, T cp1, T cp2, in
   if (up) num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
   else num = k >= 2 ? cm1 - ck : ck - ck;
   return waf_flux<T>(T(0.5) * skp, up, zamu, cp1, ck, num);
+}
+// the same with the interface's factors given (an FP64 member, k_adv_prep)
+struct VIf {
+  double zamu, hvel, zmi;
+};
+__device__ __forceinline__ double vflux_p(const VIf &t, double cm1, double ck, double cp1, double cp2,
+                                          int k, int kz) {
+  const bool up = nonneg(t.zamu);
+  double num;
+  if (up) num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
+  else num = k >= 2 ? cm1 - ck : ck - ck;
+  return waf_flux_z(t.hvel, up, t.zmi, cp1, ck, num);
 }
 template <class T>
 __device__ __forceinline__ T vupdate(T pk, T fb, T fa, T sk, T skp, T zu, T zd) {
@@ -343,6 +378,13 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   constexpr bool kPre = sizeof(R) == sizeof(double) && sizeof(T) == sizeof(double);
   const double *__restrict__ dvp = kPre ? D.vdiv + ij : nullptr;
   T dvm2 = T(0), dvm1 = T(0), n_dv = kPre ? T(dvp[0]) : T(0);
+  // FP64 member: the interface factors (zamu, hvel, zmi) of interfaces k+1,
+  // k and k-1 (pass 1 at k, pass 2 at k-2), the next level's loaded ahead
+  const double *__restrict__ zap = kPre ? D.vzamu + ij : nullptr;
+  const double *__restrict__ hvp = kPre ? D.vhvel + ij : nullptr;
+  const double *__restrict__ zmp = kPre ? D.vzmi + ij : nullptr;
+  VIf tkm1{0, 0, 0}, tkm2{0, 0, 0};
+  VIf n_t = kPre ? VIf{zap[0], hvp[0], zmp[0]} : VIf{0, 0, 0};
   // the next level's loads, issued one level ahead
   T n_s = T(sp[PS]), n_c = src[2 * PS], n_zu = T(zup[0]), n_zd = T(zdp[0]);
   // level k; every bound check is known to hold inside the column
@@ -352,15 +394,27 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     const unsigned o = (unsigned)(k - 1) * PS;
     const T skp1 = n_s, c0p2 = (I || k + 2 <= kz) ? n_c : T(0), zuk = n_zu, zdk = n_zd;
     const T dvk = n_dv;
+    const VIf tk = n_t;
     if (I || k < kz) {
-      n_s = T(sp[o + 2 * PS]);
+      if constexpr (kPre) {
+        n_dv = T(dvp[o + PS]);
+        n_t = VIf{zap[o + PS], hvp[o + PS], zmp[o + PS]};
+      } else {
+        n_s = T(sp[o + 2 * PS]);
+      }
       n_zu = T(zup[o + PS]);
       n_zd = T(zdp[o + PS]);
-      if constexpr (kPre) n_dv = T(dvp[o + PS]);
       if (I || k + 3 <= kz) n_c = src[o + 3 * PS];
     }
     T f1kp;
-    if (I) {
+    if constexpr (kPre) {
+      if (I) {
+        const bool up = nonneg(tk.zamu);
+        f1kp = waf_flux_z(tk.hvel, up, tk.zmi, c0p1, c0k, (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
+      } else {
+        f1kp = k <= kz - 1 ? vflux_p(tk, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
+      }
+    } else if (I) {
       const T zamu = skp1 * dtrdz;
       const bool up = nonneg(zamu);
       f1kp = waf_flux<T>(T(0.5) * skp1, up, zamu, c0p1, c0k,
@@ -373,7 +427,15 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     else c1k = vupdate<T>(c0k, f1k, f1kp, sk, skp1, zuk, zdk);
     if (I || k >= 3) {  // pass 2 at level m = k-2
       T f2n;
-      if (I) {
+      if constexpr (kPre) {
+        if (I) {
+          const bool up = nonneg(tkm2.zamu);
+          f2n = waf_flux_z(tkm2.hvel, up, tkm2.zmi, c1m1, c1m2,
+                           (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
+        } else {
+          f2n = vflux_p(tkm2, c1m3, c1m2, c1m1, c1k, k - 2, kz);
+        }
+      } else if (I) {
         const T zamu = sm1 * dtrdz;
         const bool up = nonneg(zamu);
         f2n = waf_flux<T>(T(0.5) * sm1, up, zamu, c1m1, c1m2,
@@ -390,6 +452,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     sm2 = sm1; sm1 = sk; sk = skp1;
     zum2 = zum1; zdm2 = zdm1; zum1 = zuk; zdm1 = zdk;
     dvm2 = dvm1; dvm1 = dvk;
+    tkm2 = tkm1; tkm1 = tk;
     f1k = f1kp;
   };
   using edge = std::integral_constant<bool, false>;
@@ -401,7 +464,9 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   for (int k = k2; k <= kz; ++k) step(k, edge{});
   // pass 2 at levels kz-1 (flux through interface kz) and kz (none above)
   const unsigned ot = (unsigned)(kz - 1) * PS;
-  const T f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
+  T f2n;
+  if constexpr (kPre) f2n = vflux_p(tkm2, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
+  else f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
   if constexpr (kPre) {
     dst[ot - PS] = vupdate_f<T>(c1m2, f2m, f2n, dvm2, zum2, zdm2);
     dst[ot] = vupdate_f<T>(c1m1, f2n, T(0), dvm1, zum1, zdm1);
@@ -650,6 +715,29 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       }
     }
   }
+  // FP64: zamu - is of the lane's three fluxes, once for every field (each
+  // FP64 add is an instruction of the slow FP64 pipe)
+  T zmiy[V], zmie[V], zmix[V];
+#pragma unroll
+  for (int q = 0; q < V; ++q) {
+    if constexpr (sizeof(T) == sizeof(double)) {
+      zmiy[q] = __dadd_rn(zmy[q], positive(zmy[q]) ? -1.0 : 1.0);
+      zmie[q] = __dadd_rn(zmye[q], positive(zmye[q]) ? -1.0 : 1.0);
+      zmix[q] = __dadd_rn(zmx[q], positive(zmx[q]) ? -1.0 : 1.0);
+    } else {
+      zmiy[q] = zmie[q] = zmix[q] = T(0);
+    }
+  }
+  // the flux with the lane's precomputed zamu - is (FP64) or as waf_flux forms it
+  auto flux = [&](T hvel, bool up, T zamu, T zmi, T a, T c, T num) -> T {
+    if constexpr (sizeof(T) == sizeof(double)) {
+      (void)zamu;
+      return waf_flux_z(hvel, up, zmi, a, c, num);
+    } else {
+      (void)zmi;
+      return waf_flux<T>(hvel, up, zamu, a, c, num);
+    }
+  };
   // rows of the halo tile (global row r at tile row r - I0 + 2) the upwind
   // differences use, with the reference's clamps ih = min(i+1, imax),
   // ihm1 = max(ih-1, imin)
@@ -696,8 +784,8 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 #pragma unroll
       for (int q = 0; q < V; ++q) {
         const bool up = positive(zmy[q]);
-        const T y = waf_flux<T>(vv[q], up, zmy[q], wa[q], wzi[q],
-                                (up ? wa[q] : wB[q]) - (up ? wA[q] : wC[q]));
+        const T y = flux(vv[q], up, zmy[q], zmiy[q], wa[q], wzi[q],
+                         (up ? wa[q] : wB[q]) - (up ? wA[q] : wC[q]));
         x[q] = mv[q] ? y : T(0);  // zero outside the flux points
       }
       st_vec<T, V>(&zp[wp][V * lane], x);
@@ -711,8 +799,8 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 #pragma unroll
         for (int q = 0; q < V; ++q) {
           const bool up = positive(zmye[q]);
-          const T y = waf_flux<T>(vve[q], up, zmye[q], xa[q], xc[q],
-                                  (up ? xa[q] : wB[q]) - (up ? wA[q] : wC[q]));
+          const T y = flux(vve[q], up, zmye[q], zmie[q], xa[q], xc[q],
+                           (up ? xa[q] : wB[q]) - (up ? wA[q] : wC[q]));
           x[q] = me[q] ? y : T(0);
         }
         st_vec<T, V>(&zp[NW][V * lane], x);
@@ -761,7 +849,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       // upwind a - p0(jhm1), downwind p0(jh) - p0(jh-1): one subtraction of selected operands
       const T n1 = up ? a : (j == jx - 1 ? cq : p0at(q + 1));
       const T n2 = up ? (j == 2 ? a : p0at(q - 2)) : (j == jx - 1 ? a : cq);
-      const T x = waf_flux<T>(uu[q], up, zmx[q], a, cq, n1 - n2);
+      const T x = flux(uu[q], up, zmx[q], zmix[q], a, cq, n1 - n2);
       zx[q] = xv[q] ? x : T(0);
     }
     T zxe[V];
