@@ -150,15 +150,25 @@ __device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) 
     return hvel * ((a + c) - (is * den + (zamu - is) * B));
   }
 }
-// The FP64 flux with hvel and zmi = zamu - is of the interface given (formed
-// once per interface for all fields, k_adv_prep): the same operations on the
-// same values as waf_flux.
-__device__ __forceinline__ double waf_flux_z(double hvel, bool up, double zmi, double a, double c,
-                                             double num) {
-  const double den = c - a;
-  const double B = waf_b<double>(den, num);
-  const double sden = up ? den : -den;
-  return __dmul_rn(hvel, (a + c) - __fma_rn(zmi, B, sden));
+// The same flux as vel*(x - zmih*B) with vel = 2*hvel (the wind itself),
+// x = a upwind of a positive zamu (is = +1) else c, and zmih = (zamu - is)/2:
+// (a + c) - is*den = 2x exactly, so in exact arithmetic
+//   hvel*((a + c) - (is*den + (zamu - is)*B)) = vel*(x - zmih*B),
+// one fused multiply-add and one product, with the wind and zmih of an
+// interface formed once for every field.
+template <class T>
+__device__ __forceinline__ T waf_flux_h(T vel, bool up, T zmih, T a, T c, T num) {
+  const T den = c - a;
+  const T B = waf_b<T>(den, num);
+  const T x = up ? a : c;
+  if constexpr (sizeof(T) == sizeof(double)) return __dmul_rn(vel, __fma_rn(-zmih, B, x));
+  else return vel * fmaf(-zmih, B, x);
+}
+// zmih = (zamu - is)/2 of an interface (the halving is exact)
+template <class T>
+__device__ __forceinline__ T waf_zmih(T zamu, bool up) {
+  if constexpr (sizeof(T) == sizeof(double)) return __dmul_rn(__dadd_rn(zamu, up ? -1.0 : 1.0), 0.5);
+  else return (zamu - (up ? 1.f : -1.f)) * 0.5f;
 }
 
 // The advected fields of a member, in the reference's order (tetav, pai,
@@ -275,16 +285,14 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
     }
     if constexpr (sizeof(R) == sizeof(double)) {
       // the vertical WAF update's factor s(k)*zu(k) - s(k+1)*zd(k), and the
-      // flux factors of interface k+1 - zamu = s*dtrdz, hvel = 0.5*s and
-      // zamu - is - once for all fields (FP64 arithmetic is the FP64 path's
-      // bound); the same expressions the vertical kernel forms per field
+      // flux factors of interface k+1 - zamu = s*dtrdz and zmih = (zamu -
+      // is)/2 - once for all fields (FP64 arithmetic is the FP64 path's bound)
       const double skp = D.s[o + PS];
       D.vdiv[o] = __fma_rn(-skp, D.sa.zrfmd[o], __dmul_rn(D.s[o], D.sa.zrfmu[o]));
       const double dtrdz = 0.5 * (D.c.dtstepa * D.c.rdzita);
       const double zamu = __dmul_rn(skp, dtrdz);
       D.vzamu[o] = zamu;
-      D.vhvel[o] = 0.5 * skp;
-      D.vzmi[o] = __dadd_rn(zamu, nonneg(zamu) ? -1.0 : 1.0);
+      D.vzmih[o] = waf_zmih<double>(zamu, nonneg(zamu));
     }
   }
 }
@@ -306,19 +314,19 @@ __device__ __forceinline__ T vflux(T dtrdz, T skp, T cm1, T ck, T cp1, T cp2, in
   T num;
   if (up) num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
   else num = k >= 2 ? cm1 - ck : ck - ck;
-  return waf_flux<T>(T(0.5) * skp, up, zamu, cp1, ck, num);
+  return waf_flux_h<T>(skp, up, waf_zmih<T>(zamu, up), cp1, ck, num);
 }
 // the same with the interface's factors given (an FP64 member, k_adv_prep)
 struct VIf {
-  double zamu, hvel, zmi;
+  double zamu, zmih;
 };
-__device__ __forceinline__ double vflux_p(const VIf &t, double cm1, double ck, double cp1, double cp2,
-                                          int k, int kz) {
+__device__ __forceinline__ double vflux_p(double skp, const VIf &t, double cm1, double ck, double cp1,
+                                          double cp2, int k, int kz) {
   const bool up = nonneg(t.zamu);
   double num;
   if (up) num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
   else num = k >= 2 ? cm1 - ck : ck - ck;
-  return waf_flux_z(t.hvel, up, t.zmi, cp1, ck, num);
+  return waf_flux_h<double>(skp, up, t.zmih, cp1, ck, num);
 }
 template <class T>
 __device__ __forceinline__ T vupdate(T pk, T fb, T fa, T sk, T skp, T zu, T zd) {
@@ -381,10 +389,9 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   // FP64 member: the interface factors (zamu, hvel, zmi) of interfaces k+1,
   // k and k-1 (pass 1 at k, pass 2 at k-2), the next level's loaded ahead
   const double *__restrict__ zap = kPre ? D.vzamu + ij : nullptr;
-  const double *__restrict__ hvp = kPre ? D.vhvel + ij : nullptr;
-  const double *__restrict__ zmp = kPre ? D.vzmi + ij : nullptr;
-  VIf tkm1{0, 0, 0}, tkm2{0, 0, 0};
-  VIf n_t = kPre ? VIf{zap[0], hvp[0], zmp[0]} : VIf{0, 0, 0};
+  const double *__restrict__ zmp = kPre ? D.vzmih + ij : nullptr;
+  VIf tkm1{0, 0}, tkm2{0, 0};
+  VIf n_t = kPre ? VIf{zap[0], zmp[0]} : VIf{0, 0};
   // the next level's loads, issued one level ahead
   T n_s = T(sp[PS]), n_c = src[2 * PS], n_zu = T(zup[0]), n_zd = T(zdp[0]);
   // level k; every bound check is known to hold inside the column
@@ -398,10 +405,9 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     if (I || k < kz) {
       if constexpr (kPre) {
         n_dv = T(dvp[o + PS]);
-        n_t = VIf{zap[o + PS], hvp[o + PS], zmp[o + PS]};
-      } else {
-        n_s = T(sp[o + 2 * PS]);
+        n_t = VIf{zap[o + PS], zmp[o + PS]};
       }
+      n_s = T(sp[o + 2 * PS]);
       n_zu = T(zup[o + PS]);
       n_zd = T(zdp[o + PS]);
       if (I || k + 3 <= kz) n_c = src[o + 3 * PS];
@@ -410,15 +416,16 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     if constexpr (kPre) {
       if (I) {
         const bool up = nonneg(tk.zamu);
-        f1kp = waf_flux_z(tk.hvel, up, tk.zmi, c0p1, c0k, (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
+        f1kp = waf_flux_h<double>(skp1, up, tk.zmih, c0p1, c0k,
+                                  (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
       } else {
-        f1kp = k <= kz - 1 ? vflux_p(tk, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
+        f1kp = k <= kz - 1 ? vflux_p(skp1, tk, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
       }
     } else if (I) {
       const T zamu = skp1 * dtrdz;
       const bool up = nonneg(zamu);
-      f1kp = waf_flux<T>(T(0.5) * skp1, up, zamu, c0p1, c0k,
-                         (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
+      f1kp = waf_flux_h<T>(skp1, up, waf_zmih<T>(zamu, up), c0p1, c0k,
+                           (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
     } else {
       f1kp = k <= kz - 1 ? vflux<T>(dtrdz, skp1, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
     }
@@ -430,16 +437,16 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
       if constexpr (kPre) {
         if (I) {
           const bool up = nonneg(tkm2.zamu);
-          f2n = waf_flux_z(tkm2.hvel, up, tkm2.zmi, c1m1, c1m2,
-                           (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
+          f2n = waf_flux_h<double>(sm1, up, tkm2.zmih, c1m1, c1m2,
+                                   (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
         } else {
-          f2n = vflux_p(tkm2, c1m3, c1m2, c1m1, c1k, k - 2, kz);
+          f2n = vflux_p(sm1, tkm2, c1m3, c1m2, c1m1, c1k, k - 2, kz);
         }
       } else if (I) {
         const T zamu = sm1 * dtrdz;
         const bool up = nonneg(zamu);
-        f2n = waf_flux<T>(T(0.5) * sm1, up, zamu, c1m1, c1m2,
-                          (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
+        f2n = waf_flux_h<T>(sm1, up, waf_zmih<T>(zamu, up), c1m1, c1m2,
+                            (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
       } else {
         f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1k, k - 2, kz);
       }
@@ -465,7 +472,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   // pass 2 at levels kz-1 (flux through interface kz) and kz (none above)
   const unsigned ot = (unsigned)(kz - 1) * PS;
   T f2n;
-  if constexpr (kPre) f2n = vflux_p(tkm2, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
+  if constexpr (kPre) f2n = vflux_p(sm1, tkm2, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
   else f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1m1, kz - 1, kz);
   if constexpr (kPre) {
     dst[ot - PS] = vupdate_f<T>(c1m2, f2m, f2n, dvm2, zum2, zdm2);
@@ -641,7 +648,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     for (int q = 0; q < V; ++q) {
       const bool ok = okM && jq[q] >= 1 && jq[q] <= jx - 1;
       mv[q] = ok;
-      vv[q] = ok ? T(0.5) * a[q] : T(0);  // the flux's hvel = v/2 (exact)
+      vv[q] = ok ? a[q] : T(0);  // the flux's wind v (= 2*hvel)
       zmy[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
     }
     // the last warp also forms the fluxes of row I0+NW
@@ -653,7 +660,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
     for (int q = 0; q < V; ++q) {
       const bool ok = okE && jq[q] >= 1 && jq[q] <= jx - 1;
       me[q] = ok;
-      vve[q] = ok ? T(0.5) * a[q] : T(0);
+      vve[q] = ok ? a[q] : T(0);
       zmye[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
     }
   }
@@ -692,7 +699,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
         dvy[q] = vn[q] * rn[q] * zn[q] - vi[q] * ri[q] * zs[q];
         m2[q] = mf[q];
       }
-      uu[q] = xv[q] ? T(0.5) * ui[q] : T(0);  // hvel = u/2 (exact)
+      uu[q] = xv[q] ? ui[q] : T(0);  // the zonal flux's wind u (= 2*hvel)
       zmx[q] = xv[q] ? ui[q] * msu[q] * dtrdx : T(0);
     }
     // the zonal update also needs u, rfmzu and rmu one column east
@@ -715,29 +722,18 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       }
     }
   }
-  // FP64: zamu - is of the lane's three fluxes, once for every field (each
-  // FP64 add is an instruction of the slow FP64 pipe)
-  T zmiy[V], zmie[V], zmix[V];
+  // the three fluxes' factors in the form vel*(x - zmih*B), once for every
+  // field: the upwind flags (zamu > 0) and zmih
+  bool upy[V], upe[V], upx[V];
 #pragma unroll
   for (int q = 0; q < V; ++q) {
-    if constexpr (sizeof(T) == sizeof(double)) {
-      zmiy[q] = __dadd_rn(zmy[q], positive(zmy[q]) ? -1.0 : 1.0);
-      zmie[q] = __dadd_rn(zmye[q], positive(zmye[q]) ? -1.0 : 1.0);
-      zmix[q] = __dadd_rn(zmx[q], positive(zmx[q]) ? -1.0 : 1.0);
-    } else {
-      zmiy[q] = zmie[q] = zmix[q] = T(0);
-    }
+    upy[q] = positive(zmy[q]);
+    upe[q] = positive(zmye[q]);
+    upx[q] = positive(zmx[q]);
+    zmy[q] = waf_zmih<T>(zmy[q], upy[q]);
+    zmye[q] = waf_zmih<T>(zmye[q], upe[q]);
+    zmx[q] = waf_zmih<T>(zmx[q], upx[q]);
   }
-  // the flux with the lane's precomputed zamu - is (FP64) or as waf_flux forms it
-  auto flux = [&](T hvel, bool up, T zamu, T zmi, T a, T c, T num) -> T {
-    if constexpr (sizeof(T) == sizeof(double)) {
-      (void)zamu;
-      return waf_flux_z(hvel, up, zmi, a, c, num);
-    } else {
-      (void)zmi;
-      return waf_flux<T>(hvel, up, zamu, a, c, num);
-    }
-  };
   // rows of the halo tile (global row r at tile row r - I0 + 2) the upwind
   // differences use, with the reference's clamps ih = min(i+1, imax),
   // ihm1 = max(ih-1, imin)
@@ -783,9 +779,9 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       ld_vec<T, V>(wC, &wt[tC][OFF + V * lane]);
 #pragma unroll
       for (int q = 0; q < V; ++q) {
-        const bool up = positive(zmy[q]);
-        const T y = flux(vv[q], up, zmy[q], zmiy[q], wa[q], wzi[q],
-                         (up ? wa[q] : wB[q]) - (up ? wA[q] : wC[q]));
+        const bool up = upy[q];
+        const T y = waf_flux_h<T>(vv[q], up, zmy[q], wa[q], wzi[q],
+                                  (up ? wa[q] : wB[q]) - (up ? wA[q] : wC[q]));
         x[q] = mv[q] ? y : T(0);  // zero outside the flux points
       }
       st_vec<T, V>(&zp[wp][V * lane], x);
@@ -798,9 +794,9 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
         ld_vec<T, V>(wC, &wt[eC][OFF + V * lane]);
 #pragma unroll
         for (int q = 0; q < V; ++q) {
-          const bool up = positive(zmye[q]);
-          const T y = flux(vve[q], up, zmye[q], zmie[q], xa[q], xc[q],
-                           (up ? xa[q] : wB[q]) - (up ? wA[q] : wC[q]));
+          const bool up = upe[q];
+          const T y = waf_flux_h<T>(vve[q], up, zmye[q], xa[q], xc[q],
+                                    (up ? xa[q] : wB[q]) - (up ? wA[q] : wC[q]));
           x[q] = me[q] ? y : T(0);
         }
         st_vec<T, V>(&zp[NW][V * lane], x);
@@ -843,13 +839,13 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 #pragma unroll
     for (int q = 0; q < V; ++q) {
       const int j = jq[q];
-      const bool up = positive(zmx[q]);
+      const bool up = upx[q];
       const T a = p0at(q - 1), cq = p0at(q);
       // jhm1 = max(j-2, jmin) upwind; jh = min(j+1, jmax) downwind
       // upwind a - p0(jhm1), downwind p0(jh) - p0(jh-1): one subtraction of selected operands
       const T n1 = up ? a : (j == jx - 1 ? cq : p0at(q + 1));
       const T n2 = up ? (j == 2 ? a : p0at(q - 2)) : (j == jx - 1 ? a : cq);
-      const T x = flux(uu[q], up, zmx[q], zmix[q], a, cq, n1 - n2);
+      const T x = waf_flux_h<T>(uu[q], up, zmx[q], a, cq, n1 - n2);
       zx[q] = xv[q] ? x : T(0);
     }
     T zxe[V];
