@@ -156,19 +156,53 @@ __device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) 
 //   hvel*((a + c) - (is*den + (zamu - is)*B)) = vel*(x - zmih*B),
 // one fused multiply-add and one product, with the wind and zmih of an
 // interface formed once for every field.
-template <class T>
-__device__ __forceinline__ T waf_flux_h(T vel, bool up, T zmih, T a, T c, T num) {
-  const T den = c - a;
-  const T B = waf_b<T>(den, num);
-  const T x = up ? a : c;
-  if constexpr (sizeof(T) == sizeof(double)) return __dmul_rn(vel, __fma_rn(-zmih, B, x));
-  else return vel * fmaf(-zmih, B, x);
+//
+// FP64 keeps the doubling out of the FP64 pipe: in the regions where B is
+// 2*num or 2*den the flux takes zmi = 2*zmih (exact) as the factor of num or
+// den instead, zmih*(2*sel) = zmi*sel exactly, so only the differences, one
+// fused multiply-add and one product are FP64 instructions.
+__device__ __forceinline__ double waf_sel(double den, double num, bool &dbl) {
+  // the regions of waf_b, tested on the bit patterns
+  const long long bden = __double_as_longlong(den), bnum = __double_as_longlong(num);
+  const long long mag = 0x7fffffffffffffffLL, one_exp = 1LL << 52;
+  const long long ad = bden & mag;
+  const long long bq = bnum ^ (bden & ~mag);
+  const long long eden = __double_as_longlong(FlowEps<double>::den());
+  const long long enum_ = __double_as_longlong(FlowEps<double>::num());
+  dbl = false;
+  if (ad < eden) return (bnum & mag) < enum_ ? den : 0.0;
+  if ((bnum & mag) > 0x7ff0000000000000LL) { dbl = true; return den; }
+  if (bq <= 0) return 0.0;
+  if (bq < ad - one_exp) { dbl = true; return num; }
+  if (bq <= ad) return den;
+  if (bq < ad + one_exp) return num;
+  dbl = true;
+  return den;
 }
-// zmih = (zamu - is)/2 of an interface (the halving is exact)
+template <class T>
+__device__ __forceinline__ T waf_flux_h(T vel, bool up, T zmih, T zmi, T a, T c, T num) {
+  const T den = c - a;
+  const T x = up ? a : c;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    bool dbl;
+    const double sel = waf_sel(den, num, dbl);
+    return __dmul_rn(vel, __fma_rn(dbl ? -zmi : -zmih, sel, x));
+  } else {
+    (void)zmi;
+    const T B = waf_b<T>(den, num);
+    return vel * fmaf(-zmih, B, x);
+  }
+}
+// zmi = zamu - is and zmih = zmi/2 of an interface (the halving is exact)
+template <class T>
+__device__ __forceinline__ T waf_zmi(T zamu, bool up) {
+  if constexpr (sizeof(T) == sizeof(double)) return __dadd_rn(zamu, up ? -1.0 : 1.0);
+  else return zamu - (up ? 1.f : -1.f);
+}
 template <class T>
 __device__ __forceinline__ T waf_zmih(T zamu, bool up) {
-  if constexpr (sizeof(T) == sizeof(double)) return __dmul_rn(__dadd_rn(zamu, up ? -1.0 : 1.0), 0.5);
-  else return (zamu - (up ? 1.f : -1.f)) * 0.5f;
+  if constexpr (sizeof(T) == sizeof(double)) return __dmul_rn(waf_zmi<T>(zamu, up), 0.5);
+  else return waf_zmi<T>(zamu, up) * 0.5f;
 }
 
 // The advected fields of a member, in the reference's order (tetav, pai,
@@ -285,14 +319,17 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
     }
     if constexpr (sizeof(R) == sizeof(double)) {
       // the vertical WAF update's factor s(k)*zu(k) - s(k+1)*zd(k), and the
-      // flux factors of interface k+1 - zamu = s*dtrdz and zmih = (zamu -
-      // is)/2 - once for all fields (FP64 arithmetic is the FP64 path's bound)
+      // flux factors of interface k+1 - zamu = s*dtrdz, zmi = zamu - is and
+      // zmih = zmi/2 - once for all fields (FP64 arithmetic is the FP64
+      // path's bound)
       const double skp = D.s[o + PS];
       D.vdiv[o] = __fma_rn(-skp, D.sa.zrfmd[o], __dmul_rn(D.s[o], D.sa.zrfmu[o]));
       const double dtrdz = 0.5 * (D.c.dtstepa * D.c.rdzita);
       const double zamu = __dmul_rn(skp, dtrdz);
+      const double zmi = waf_zmi<double>(zamu, nonneg(zamu));
       D.vzamu[o] = zamu;
-      D.vzmih[o] = waf_zmih<double>(zamu, nonneg(zamu));
+      D.vzmi[o] = zmi;
+      D.vzmih[o] = __dmul_rn(zmi, 0.5);
     }
   }
 }
@@ -314,11 +351,12 @@ __device__ __forceinline__ T vflux(T dtrdz, T skp, T cm1, T ck, T cp1, T cp2, in
   T num;
   if (up) num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
   else num = k >= 2 ? cm1 - ck : ck - ck;
-  return waf_flux_h<T>(skp, up, waf_zmih<T>(zamu, up), cp1, ck, num);
+  const T zmi = waf_zmi<T>(zamu, up);
+  return waf_flux_h<T>(skp, up, zmi * T(0.5), zmi, cp1, ck, num);
 }
 // the same with the interface's factors given (an FP64 member, k_adv_prep)
 struct VIf {
-  double zamu, zmih;
+  double zamu, zmih, zmi;
 };
 __device__ __forceinline__ double vflux_p(double skp, const VIf &t, double cm1, double ck, double cp1,
                                           double cp2, int k, int kz) {
@@ -326,7 +364,7 @@ __device__ __forceinline__ double vflux_p(double skp, const VIf &t, double cm1, 
   double num;
   if (up) num = k + 2 <= kz ? cp1 - cp2 : cp1 - cp1;
   else num = k >= 2 ? cm1 - ck : ck - ck;
-  return waf_flux_h<double>(skp, up, t.zmih, cp1, ck, num);
+  return waf_flux_h<double>(skp, up, t.zmih, t.zmi, cp1, ck, num);
 }
 template <class T>
 __device__ __forceinline__ T vupdate(T pk, T fb, T fa, T sk, T skp, T zu, T zd) {
@@ -390,8 +428,9 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   // k and k-1 (pass 1 at k, pass 2 at k-2), the next level's loaded ahead
   const double *__restrict__ zap = kPre ? D.vzamu + ij : nullptr;
   const double *__restrict__ zmp = kPre ? D.vzmih + ij : nullptr;
-  VIf tkm1{0, 0}, tkm2{0, 0};
-  VIf n_t = kPre ? VIf{zap[0], zmp[0]} : VIf{0, 0};
+  const double *__restrict__ z2p = kPre ? D.vzmi + ij : nullptr;
+  VIf tkm1{0, 0, 0}, tkm2{0, 0, 0};
+  VIf n_t = kPre ? VIf{zap[0], zmp[0], z2p[0]} : VIf{0, 0, 0};
   // the next level's loads, issued one level ahead
   T n_s = T(sp[PS]), n_c = src[2 * PS], n_zu = T(zup[0]), n_zd = T(zdp[0]);
   // level k; every bound check is known to hold inside the column
@@ -405,7 +444,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     if (I || k < kz) {
       if constexpr (kPre) {
         n_dv = T(dvp[o + PS]);
-        n_t = VIf{zap[o + PS], zmp[o + PS]};
+        n_t = VIf{zap[o + PS], zmp[o + PS], z2p[o + PS]};
       }
       n_s = T(sp[o + 2 * PS]);
       n_zu = T(zup[o + PS]);
@@ -416,7 +455,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     if constexpr (kPre) {
       if (I) {
         const bool up = nonneg(tk.zamu);
-        f1kp = waf_flux_h<double>(skp1, up, tk.zmih, c0p1, c0k,
+        f1kp = waf_flux_h<double>(skp1, up, tk.zmih, tk.zmi, c0p1, c0k,
                                   (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
       } else {
         f1kp = k <= kz - 1 ? vflux_p(skp1, tk, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
@@ -424,7 +463,8 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
     } else if (I) {
       const T zamu = skp1 * dtrdz;
       const bool up = nonneg(zamu);
-      f1kp = waf_flux_h<T>(skp1, up, waf_zmih<T>(zamu, up), c0p1, c0k,
+      const T zmi = waf_zmi<T>(zamu, up);
+      f1kp = waf_flux_h<T>(skp1, up, zmi * T(0.5), zmi, c0p1, c0k,
                            (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
     } else {
       f1kp = k <= kz - 1 ? vflux<T>(dtrdz, skp1, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
@@ -437,7 +477,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
       if constexpr (kPre) {
         if (I) {
           const bool up = nonneg(tkm2.zamu);
-          f2n = waf_flux_h<double>(sm1, up, tkm2.zmih, c1m1, c1m2,
+          f2n = waf_flux_h<double>(sm1, up, tkm2.zmih, tkm2.zmi, c1m1, c1m2,
                                    (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
         } else {
           f2n = vflux_p(sm1, tkm2, c1m3, c1m2, c1m1, c1k, k - 2, kz);
@@ -445,7 +485,8 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
       } else if (I) {
         const T zamu = sm1 * dtrdz;
         const bool up = nonneg(zamu);
-        f2n = waf_flux_h<T>(sm1, up, waf_zmih<T>(zamu, up), c1m1, c1m2,
+        const T zmi = waf_zmi<T>(zamu, up);
+        f2n = waf_flux_h<T>(sm1, up, zmi * T(0.5), zmi, c1m1, c1m2,
                             (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
       } else {
         f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1k, k - 2, kz);
@@ -725,14 +766,18 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
   // the three fluxes' factors in the form vel*(x - zmih*B), once for every
   // field: the upwind flags (zamu > 0) and zmih
   bool upy[V], upe[V], upx[V];
+  T z2y[V], z2e[V], z2x[V];  // zmi = 2*zmih (FP64 only)
 #pragma unroll
   for (int q = 0; q < V; ++q) {
     upy[q] = positive(zmy[q]);
     upe[q] = positive(zmye[q]);
     upx[q] = positive(zmx[q]);
-    zmy[q] = waf_zmih<T>(zmy[q], upy[q]);
-    zmye[q] = waf_zmih<T>(zmye[q], upe[q]);
-    zmx[q] = waf_zmih<T>(zmx[q], upx[q]);
+    z2y[q] = waf_zmi<T>(zmy[q], upy[q]);
+    z2e[q] = waf_zmi<T>(zmye[q], upe[q]);
+    z2x[q] = waf_zmi<T>(zmx[q], upx[q]);
+    zmy[q] = z2y[q] * T(0.5);
+    zmye[q] = z2e[q] * T(0.5);
+    zmx[q] = z2x[q] * T(0.5);
   }
   // rows of the halo tile (global row r at tile row r - I0 + 2) the upwind
   // differences use, with the reference's clamps ih = min(i+1, imax),
@@ -780,7 +825,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 #pragma unroll
       for (int q = 0; q < V; ++q) {
         const bool up = upy[q];
-        const T y = waf_flux_h<T>(vv[q], up, zmy[q], wa[q], wzi[q],
+        const T y = waf_flux_h<T>(vv[q], up, zmy[q], z2y[q], wa[q], wzi[q],
                                   (up ? wa[q] : wB[q]) - (up ? wA[q] : wC[q]));
         x[q] = mv[q] ? y : T(0);  // zero outside the flux points
       }
@@ -795,7 +840,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
 #pragma unroll
         for (int q = 0; q < V; ++q) {
           const bool up = upe[q];
-          const T y = waf_flux_h<T>(vve[q], up, zmye[q], xa[q], xc[q],
+          const T y = waf_flux_h<T>(vve[q], up, zmye[q], z2e[q], xa[q], xc[q],
                                     (up ? xa[q] : wB[q]) - (up ? wA[q] : wC[q]));
           x[q] = me[q] ? y : T(0);
         }
@@ -845,7 +890,7 @@ __global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__rest
       // upwind a - p0(jhm1), downwind p0(jh) - p0(jh-1): one subtraction of selected operands
       const T n1 = up ? a : (j == jx - 1 ? cq : p0at(q + 1));
       const T n2 = up ? (j == 2 ? a : p0at(q - 2)) : (j == jx - 1 ? a : cq);
-      const T x = waf_flux_h<T>(uu[q], up, zmx[q], a, cq, n1 - n2);
+      const T x = waf_flux_h<T>(uu[q], up, zmx[q], z2x[q], a, cq, n1 - n2);
       zx[q] = xv[q] ? x : T(0);
     }
     T zxe[V];

@@ -155,6 +155,7 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
   D.vdiv = f64 ? cv.take<double>(F) : nullptr;
   D.vzamu = f64 ? cv.take<double>(F) : nullptr;
   D.vzmih = f64 ? cv.take<double>(F) : nullptr;
+  D.vzmi = f64 ? cv.take<double>(F) : nullptr;
   Stat<R> &s = D.sa;
   s.fmz = cv.take<R>(F); s.fmzf = cv.take<R>(F1); s.rfmzu = cv.take<R>(F); s.rfmzv = cv.take<R>(F);
   if (f64) {

@@ -166,8 +166,8 @@ struct Dom {
   // (the vertical WAF update's divergence factor, the same for every field)
   double *vdiv;
   // an FP64 member's flux factors of interface k+1 at level k's offset:
-  // zamu = s*dtrdz and zmih = (zamu - is)/2 (the vertical WAF's)
-  double *vzamu, *vzmih;
+  // zamu = s*dtrdz, zmi = zamu - is and zmih = zmi/2 (the vertical WAF's)
+  double *vzamu, *vzmih, *vzmi;
   // physics tendencies of the open step (null: zero), fields of the state's
   // layout: tten, uten, vten, then nqx qxten, then ntr chiten
   const R *tend;
