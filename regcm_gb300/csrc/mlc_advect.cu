@@ -593,8 +593,22 @@ __device__ __forceinline__ void next_col(T (&e)[V], const T (&x)[V]) {
 // middle 32*v - 4 (a column's zonal update needs p0 two columns either
 // side); tiles overlap by four columns.  Per field the expressions are the
 // reference's, operand for operand.
+// Resident warps an SM the FP32 WAF tile kernels are compiled for (the
+// register budget follows: 64 a thread at 32 warps); FP64 ones keep the
+// compiler's own choice (their FP64 pipe is the bound, not latency).
+#ifndef MLC_HWAF_WARPS
+#define MLC_HWAF_WARPS 0
+#endif
+#ifndef MLC_HINC_WARPS
+#define MLC_HINC_WARPS 0
+#endif
+template <class R>
+constexpr int waf_min_blocks(int warps, int nw) {
+  return sizeof(R) == sizeof(float) && warps > 0 ? warps / nw : 1;
+}
 template <class R, int V, int NW>
-__global__ void __launch_bounds__(32 * NW) k_adv_horizontal(const Dom<R> *__restrict__ doms,
+__global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(MLC_HWAF_WARPS, NW))
+    k_adv_horizontal(const Dom<R> *__restrict__ doms,
                                                            int tiles_j, int uvoff, int advoff,
     const WorkItem *__restrict__ wl) {
   using T = R;
@@ -1188,7 +1202,8 @@ __global__ void k_adv_vertical_inc(const Dom<R> *__restrict__ doms, int advoff,
 // + zonal increments).  Fluxes are formed relative to the cell south (west)
 // of the interface, from FP32 increments and neighbour differences.
 template <class R, int V, int NW>
-__global__ void __launch_bounds__(32 * NW) k_adv_horizontal_inc(const Dom<R> *__restrict__ doms,
+__global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(MLC_HINC_WARPS, NW))
+    k_adv_horizontal_inc(const Dom<R> *__restrict__ doms,
                                                                int tiles_j, int uvoff,
                                                                int advoff,
                                                                const WorkItem *__restrict__ wl) {

@@ -787,12 +787,18 @@ struct West4 {
   __device__ __forceinline__ float at(int q) const { return q < 0 ? w : x[q]; }
 };
 
+// Blocks of 128 threads an SM the four-column point kernels are compiled for
+// (1: the compiler's own register choice).
+#ifndef MLC_PT4_BLOCKS
+#define MLC_PT4_BLOCKS 1
+#endif
+
 // The divergence and s of a mixed member (the same equations as
 // k_sound_div) with lanes of four consecutive columns: 16-byte loads at the
 // lane's points and the row north of them, the east neighbour of the last
 // element read singly, the level below carried from the previous level.
 template <class R>
-__global__ void __launch_bounds__(128) k_sound_div_v4(const Dom<R> *__restrict__ doms, int uvoff,
+__global__ void __launch_bounds__(128, MLC_PT4_BLOCKS) k_sound_div_v4(const Dom<R> *__restrict__ doms, int uvoff,
                                                       int tiles_j,
     const WorkItem *__restrict__ wl) {
   static_assert(sizeof(R) == sizeof(float), "FP32 fields");
@@ -925,7 +931,7 @@ __global__ void __launch_bounds__(128) k_sound_div_v4(const Dom<R> *__restrict__
 // block is 32 lanes x 4 rows; grid x = 128-column tiles times row tiles, y =
 // level chunks, z = member.
 template <class R>
-__global__ void __launch_bounds__(128) k_sound_momentum_v4(const Dom<R> *__restrict__ doms,
+__global__ void __launch_bounds__(128, MLC_PT4_BLOCKS) k_sound_momentum_v4(const Dom<R> *__restrict__ doms,
                                                            int uvoff, int advoff, int tiles_j,
     const WorkItem *__restrict__ wl) {
   static_assert(sizeof(R) == sizeof(float), "FP32 fields");
