@@ -593,21 +593,29 @@ __device__ __forceinline__ void next_col(T (&e)[V], const T (&x)[V]) {
 // middle 32*v - 4 (a column's zonal update needs p0 two columns either
 // side); tiles overlap by four columns.  Per field the expressions are the
 // reference's, operand for operand.
-// Resident warps an SM the FP32 WAF tile kernels are compiled for (the
-// register budget follows: 64 a thread at 32 warps); FP64 ones keep the
-// compiler's own choice (their FP64 pipe is the bound, not latency).
+// Resident warps an SM the WAF tile kernels are compiled for; the register
+// budget follows (65536 / (32 * warps) a thread).  Measured on the moist
+// 512x512x41 step: FP32 horizontal WAF at 32 warps (64 registers) 0.46 ms a
+// step against 0.72 at 16 warps (90 registers); the increment form at 24
+// warps (80 registers) 0.29 against 0.37 ms.  FP64 at 16 warps (128
+// registers): the FP64 pipe is the bound, but 8 warps an SM leave it idle.
 #ifndef MLC_HWAF_WARPS
-#define MLC_HWAF_WARPS 0
+#define MLC_HWAF_WARPS 32
+#endif
+#ifndef MLC_HWAF_WARPS_D
+#define MLC_HWAF_WARPS_D 16
 #endif
 #ifndef MLC_HINC_WARPS
-#define MLC_HINC_WARPS 0
+#define MLC_HINC_WARPS 24
 #endif
 template <class R>
 constexpr int waf_min_blocks(int warps, int nw) {
-  return sizeof(R) == sizeof(float) && warps > 0 ? warps / nw : 1;
+  return warps / nw > 1 ? warps / nw : 1;
 }
 template <class R, int V, int NW>
-__global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(MLC_HWAF_WARPS, NW))
+__global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(sizeof(R) == sizeof(float)
+                                                                   ? MLC_HWAF_WARPS
+                                                                   : MLC_HWAF_WARPS_D, NW))
     k_adv_horizontal(const Dom<R> *__restrict__ doms,
                                                            int tiles_j, int uvoff, int advoff,
     const WorkItem *__restrict__ wl) {
