@@ -152,7 +152,7 @@ constexpr int kDvW = 128;
 constexpr int kDvZW = kDvW + 4;                   // raw divergence row, 2-column halo each side
 constexpr int kDvStage = 3 * kDvZW + 7 * kDvW;   // doubles of one stage
 template <class R>
-__global__ void __launch_bounds__(128, 7) k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last,
+__global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last,
     const WorkItem *__restrict__ wl) {
   static_assert(sizeof(R) == sizeof(double), "FP64 member");
   constexpr int NS = kDvStages;
@@ -198,61 +198,42 @@ __global__ void __launch_bounds__(128, 7) k_sound_solve(const Dom<R> *__restrict
   auto stage = [&](int b) { return dv_smem + (size_t)b * kDvStage; };
   auto fld = [&](double *st, int f) { return st + 3 * kDvZW + f * kDvW; };
   const int nd = kz - 1;
-  // A level's copies are issued by warp 0, one copy a lane (lane 0 first
-  // arms the mbarrier with the level's bytes); lane q's plane, stage offset,
-  // size and level are fixed for the kernel.
-  //   down unit u (m = kz-1-u): zraw rows i, i-1, i+1, then s, fmz, pai,
-  //   tetav at level m; w, fmzf, tetavf at interface m+1
-  //   up unit v (m = v+2): w, mul at level m (mul only for m <= kz); pai,
-  //   zfs, fmz, s, fmzf at level m-1
-  // (the table lives in shared memory: written once by the lanes, read back
-  // at each issue, so no thread holds it in registers)
-  __shared__ const double *cp_src[2][16];
-  __shared__ int cp_dst[2][16], cp_at[2][16];
-  __shared__ unsigned cp_nb[16];
-  const int lane = t & 31;
-  if (t < 16) {
-    const double *dn_tab[7] = {s, fmz, pai, tetav, w, fmzf, tetavf};
-    const double *src = nullptr;
-    int dst = 0, at = -1;
-    unsigned nb = wb;
-    if (lane < 3) {
-      if (lane == 0 || filt) src = zraw + (lane == 1 ? -P : lane == 2 ? P : 0) + zs;
-      dst = lane * kDvZW;
-      nb = zb;
-    } else if (lane < 10) {
-      src = dn_tab[lane - 3] + x0;
-      dst = 3 * kDvZW + (lane - 3) * kDvW;
-      at = lane < 7 ? -1 : 0;
-    }
-    cp_src[0][lane] = src; cp_dst[0][lane] = dst; cp_at[0][lane] = at; cp_nb[lane] = nb;
-    // up: at = -1 level m, -2 level m-1 (mul, lane 1, only for m <= kz)
-    const double *up_tab[7] = {w, mul, pai, zfs, fmz, s, fmzf};
-    cp_src[1][lane] = lane < 7 ? up_tab[lane] + x0 : nullptr;
-    cp_dst[1][lane] = 3 * kDvZW + lane * kDvW;
-    cp_at[1][lane] = lane < 2 ? -1 : -2;
-  }
-  auto issue_down = [&](int u, int b) {  // all of warp 0
+  // down unit u (m = kz-1-u): zraw rows, s, fmz, pai, tetav at m; w, fmzf, tetavf at m+1
+  auto issue_down = [&](int u, int b) {
     const int m = kz - 1 - u;
+    double *st = stage(b);
     uint64_t *bar = &mbar[b];
-    if (lane == 0) mbar_expect_tx(bar, (filt ? 3u : 1u) * zb + 7u * wb);
-    __syncwarp();
-    const double *src = lane < 16 ? cp_src[0][lane] : nullptr;
-    if (src) {
-      fence_proxy_async();
-      bulk_load(stage(b) + cp_dst[0][lane], src + (m + cp_at[0][lane]) * PS, cp_nb[lane], bar);
+    fence_proxy_async();
+    mbar_expect_tx(bar, (filt ? 3u : 1u) * zb + 7u * wb);
+    const int o = (m - 1) * PS, ob = m * PS;
+    bulk_load(st, zraw + o + zs, zb, bar);
+    if (filt) {
+      bulk_load(st + kDvZW, zraw + o - P + zs, zb, bar);
+      bulk_load(st + 2 * kDvZW, zraw + o + P + zs, zb, bar);
     }
+    bulk_load(fld(st, 0), s + o + x0, wb, bar);
+    bulk_load(fld(st, 1), fmz + o + x0, wb, bar);
+    bulk_load(fld(st, 2), pai + o + x0, wb, bar);
+    bulk_load(fld(st, 3), tetav + o + x0, wb, bar);
+    bulk_load(fld(st, 4), w + ob + x0, wb, bar);
+    bulk_load(fld(st, 5), fmzf + ob + x0, wb, bar);
+    bulk_load(fld(st, 6), tetavf + ob + x0, wb, bar);
   };
-  auto issue_up = [&](int v, int b) {  // all of warp 0
+  // up unit v (m = v + 2): w(m), mul(m) (m <= kz); pai, zfs, fmz, s, fmzf at m-1
+  auto issue_up = [&](int v, int b) {
     const int m = v + 2;
+    double *st = stage(b);
     uint64_t *bar = &mbar[b];
-    if (lane == 0) mbar_expect_tx(bar, (m <= kz ? 7u : 6u) * wb);
-    __syncwarp();
-    const double *src = lane < 16 ? cp_src[1][lane] : nullptr;
-    if (src && (lane != 1 || m <= kz)) {
-      fence_proxy_async();
-      bulk_load(stage(b) + cp_dst[1][lane], src + (m + cp_at[1][lane]) * PS, wb, bar);
-    }
+    fence_proxy_async();
+    mbar_expect_tx(bar, (m <= kz ? 7u : 6u) * wb);
+    const int o = (m - 1) * PS, op = (m - 2) * PS;
+    bulk_load(fld(st, 0), w + o + x0, wb, bar);
+    if (m <= kz) bulk_load(fld(st, 1), mul + o + x0, wb, bar);
+    bulk_load(fld(st, 2), pai + op + x0, wb, bar);
+    bulk_load(fld(st, 3), zfs + op + x0, wb, bar);
+    bulk_load(fld(st, 4), fmz + op + x0, wb, bar);
+    bulk_load(fld(st, 5), s + op + x0, wb, bar);
+    bulk_load(fld(st, 6), fmzf + op + x0, wb, bar);
   };
   auto bail = [&](int gnext, int gend) {
     if (t == 0) {
@@ -265,7 +246,7 @@ __global__ void __launch_bounds__(128, 7) k_sound_solve(const Dom<R> *__restrict
     fence_mbar_init();
   }
   __syncthreads();
-  if (t < 32)
+  if (t == 0)
     for (int u = 0; u < NS && u < nd; ++u) issue_down(u, u);
   // filtered divergence plus the vertical part of level m (:531-543, :627-630)
   auto zf_of = [&](int m, double z, double lap, double fz, double sm, double sm1) {
@@ -319,13 +300,13 @@ __global__ void __launch_bounds__(128, 7) k_sound_solve(const Dom<R> *__restrict
       bail(u + 1, nd);
       return;
     }
-    if (t < 32 && u + NS < nd) issue_down(u + NS, b);
+    if (t == 0 && u + NS < nd) issue_down(u + NS, b);
   }
   if (act) zfs[ij_off] = zfk;  // level 1
   fence_proxy_async_global();
   __syncthreads();
   const int nu = kz;
-  if (t < 32)
+  if (t == 0)
     for (int v = 0; v < NS && v < nu; ++v) issue_up(v, (nd + v) % NS);
   // Exner (:668-671) of level m once w(m+1) is known, and s (:728-734)
   auto exner = [&](int m, double wm, double wmp, double pk, double zf, double fz, double sm, double fzf) {
@@ -356,7 +337,7 @@ __global__ void __launch_bounds__(128, 7) k_sound_solve(const Dom<R> *__restrict
       bail(gu + 1, nd + nu);
       return;
     }
-    if (t < 32 && v + NS < nu) issue_up(v + NS, b);
+    if (t == 0 && v + NS < nu) issue_up(v + NS, b);
   }
   if (last && act) {
     s[ij_off] = 0.0;
@@ -396,7 +377,7 @@ constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
 // 0.73 ms of solves a step against 0.95 for the same thread-per-column
 // kernel with register prefetch of one level.)
 template <class R, bool DFR>
-__global__ void __launch_bounds__(128, 7) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last,
+__global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last,
     const WorkItem *__restrict__ wl) {
   constexpr int NS = kSvStages;
   extern __shared__ __align__(16) float sv_smem[];
@@ -455,67 +436,53 @@ __global__ void __launch_bounds__(128, 7) k_solve_mixed(const Dom<R> *__restrict
   // stage layout: zraw rows i, i-1, i+1 (kSvZW each), then 11 fields of kSvW
   auto fld = [&](float *st, int f) { return st + 3 * kSvZW + f * kSvW; };
   const int nd = kz - 1;                          // down units: m = kz-1 .. 1
-  // A level's copies are issued by warp 0, one copy a lane (lane 0 first
-  // arms the mbarrier with the level's bytes).  Lane q's plane, stage offset,
-  // size and level are fixed for the kernel; only the level moves.
-  //   down unit u (m = kz-1-u): zraw rows i, i-1, i+1, then s, fmz, pai hi/lo
-  //   at level m; w, fmzf, dtet, tvf hi/lo, cfz hi/lo at interface m+1
-  //   up unit v (m = v+2): w, mul (and their lo parts) at level m (m <= kz);
-  //   pai hi/lo, zfs, fmz, s, fmzf at level m-1
-  // (the table lives in shared memory: written once by the lanes, read back
-  // at each issue, so no thread holds it in registers)
-  __shared__ const float *cp_src[2][16];
-  __shared__ int cp_dst[2][16], cp_at[2][16];
-  __shared__ unsigned cp_nb[2][16];
-  const int lane = t & 31;
-  if (t < 16) {
-    const float *dn_tab[11] = {s, fmz, pai_h, pai_l, w, fmzf, dtet, tvf_h, tvf_l, cfz_h, cfz_l};
-    const float *src = nullptr;
-    int dst = 0, at = -1;
-    unsigned nb = wb;
-    if (lane < 3) {
-      if (lane == 0 || filt) src = zraw + (lane == 1 ? -P : lane == 2 ? P : 0) + zs;
-      dst = lane * kSvZW;
-      nb = zb;
-    } else if (lane < 14) {
-      src = dn_tab[lane - 3] + x0;
-      dst = 3 * kSvZW + (lane - 3) * kSvW;
-      at = lane < 7 ? -1 : 0;
-    }
-    cp_src[0][lane] = src; cp_dst[0][lane] = dst; cp_at[0][lane] = at; cp_nb[0][lane] = nb;
-    // up: at = -1 level m, -2 level m-1; nb = 0 marks a copy made only for m <= kz
-    const float *up_tab[10] = {w, mul, w_lo, mul_lo, pai_h, pai_l, zfs, fmz, s, fmzf};
-    const int up_fld[10] = {0, 1, 8, 9, 2, 3, 4, 5, 6, 7};
-    src = nullptr;
-    dst = 0;
-    if (lane < 10 && (DFR || lane < 2 || lane > 3)) {
-      src = up_tab[lane] + x0;
-      dst = 3 * kSvZW + up_fld[lane] * kSvW;
-    }
-    cp_src[1][lane] = src; cp_dst[1][lane] = dst; cp_at[1][lane] = lane < 4 ? -1 : -2;
-    cp_nb[1][lane] = lane >= 1 && lane < 4 ? 0u : wb;
-  }
-  auto issue_down = [&](int u, int b) {  // all of warp 0
+  // down unit u: A(m) = zraw, s, fmz, pai at level m; B(m+1) = w, fmzf,
+  // dtet, tvf, cfz at interface m+1 (m = kz-1-u)
+  auto issue_down = [&](int u, int b) {
     const int m = kz - 1 - u;
+    float *st = stage(b);
     uint64_t *bar = &mbar[b];
-    if (lane == 0) mbar_expect_tx(bar, (filt ? 3u : 1u) * zb + 11u * wb);
-    __syncwarp();
-    const float *src = lane < 16 ? cp_src[0][lane] : nullptr;
-    if (src) {
-      fence_proxy_async();
-      bulk_load(stage(b) + cp_dst[0][lane], src + (m + cp_at[0][lane]) * PS, cp_nb[0][lane], bar);
+    fence_proxy_async();
+    mbar_expect_tx(bar, (filt ? 3u : 1u) * zb + 11u * wb);
+    const int o = (m - 1) * PS, ob = m * PS;
+    bulk_load(st, zraw + o + zs, zb, bar);
+    if (filt) {
+      bulk_load(st + kSvZW, zraw + o - P + zs, zb, bar);
+      bulk_load(st + 2 * kSvZW, zraw + o + P + zs, zb, bar);
     }
+    bulk_load(fld(st, 0), s + o + x0, wb, bar);
+    bulk_load(fld(st, 1), fmz + o + x0, wb, bar);
+    bulk_load(fld(st, 2), pai_h + o + x0, wb, bar);
+    bulk_load(fld(st, 3), pai_l + o + x0, wb, bar);
+    bulk_load(fld(st, 4), w + ob + x0, wb, bar);
+    bulk_load(fld(st, 5), fmzf + ob + x0, wb, bar);
+    bulk_load(fld(st, 6), dtet + ob + x0, wb, bar);
+    bulk_load(fld(st, 7), tvf_h + ob + x0, wb, bar);
+    bulk_load(fld(st, 8), tvf_l + ob + x0, wb, bar);
+    bulk_load(fld(st, 9), cfz_h + ob + x0, wb, bar);
+    bulk_load(fld(st, 10), cfz_l + ob + x0, wb, bar);
   };
-  auto issue_up = [&](int v, int b) {  // all of warp 0
+  // up unit v (m = v + 2): w(m), mul(m) (m <= kz), and pai, zfs, fmz, s,
+  // fmzf at level m-1
+  auto issue_up = [&](int v, int b) {
     const int m = v + 2;
+    float *st = stage(b);
     uint64_t *bar = &mbar[b];
-    if (lane == 0) mbar_expect_tx(bar, (m <= kz ? (DFR ? 10u : 8u) : 7u) * wb);
-    __syncwarp();
-    const float *src = lane < 16 ? cp_src[1][lane] : nullptr;
-    if (src && (cp_nb[1][lane] != 0u || m <= kz)) {
-      fence_proxy_async();
-      bulk_load(stage(b) + cp_dst[1][lane], src + (m + cp_at[1][lane]) * PS, wb, bar);
+    fence_proxy_async();
+    mbar_expect_tx(bar, (m <= kz ? (DFR ? 10u : 8u) : 7u) * wb);
+    const int o = (m - 1) * PS, op = (m - 2) * PS;
+    bulk_load(fld(st, 0), w + o + x0, wb, bar);
+    if (m <= kz) bulk_load(fld(st, 1), mul + o + x0, wb, bar);
+    if (DFR && m <= kz) {
+      bulk_load(fld(st, 8), w_lo + o + x0, wb, bar);
+      bulk_load(fld(st, 9), mul_lo + o + x0, wb, bar);
     }
+    bulk_load(fld(st, 2), pai_h + op + x0, wb, bar);
+    bulk_load(fld(st, 3), pai_l + op + x0, wb, bar);
+    bulk_load(fld(st, 4), zfs + op + x0, wb, bar);
+    bulk_load(fld(st, 5), fmz + op + x0, wb, bar);
+    bulk_load(fld(st, 6), s + op + x0, wb, bar);
+    bulk_load(fld(st, 7), fmzf + op + x0, wb, bar);
   };
   // a failed wait (a copy that never landed): record it, let the copies in
   // flight land (bounded) and leave
@@ -530,7 +497,7 @@ __global__ void __launch_bounds__(128, 7) k_solve_mixed(const Dom<R> *__restrict
     fence_mbar_init();
   }
   __syncthreads();
-  if (t < 32)
+  if (t == 0)
     for (int u = 0; u < NS && u < nd; ++u) issue_down(u, u);
 
   struct LvA {
@@ -617,14 +584,14 @@ __global__ void __launch_bounds__(128, 7) k_solve_mixed(const Dom<R> *__restrict
       bail(u + 1, nd);
       return;
     }
-    if (t < 32 && u + NS < nd) issue_down(u + NS, b);
+    if (t == 0 && u + NS < nd) issue_down(u + NS, b);
   }
   if (act) zfs[ij_off] = zfk;  // level 1
   // this thread's stores of w, mul and zfs are read back by the copy engine
   fence_proxy_async_global();
   __syncthreads();
   const int nu = kz;  // up units: m = 2 .. kz+1
-  if (t < 32)
+  if (t == 0)
     for (int v = 0; v < NS && v < nu; ++v) issue_up(v, (nd + v) % NS);
   auto exner = [&](int m, float wm, float dw, F2 pk, float zf, float fz, float sm, float fzf) {
     const int o = (m - 1) * PS + ij_off;
@@ -672,7 +639,7 @@ __global__ void __launch_bounds__(128, 7) k_solve_mixed(const Dom<R> *__restrict
       bail(gu + 1, nd + nu);
       return;
     }
-    if (t < 32 && v + NS < nu) issue_up(v + NS, b);
+    if (t == 0 && v + NS < nu) issue_up(v + NS, b);
   }
   if (last && act) {
     s[ij_off] = 0.f;
