@@ -378,12 +378,17 @@ __device__ __forceinline__ T vupdate_f(T pk, T fb, T fa, T dv, T zu, T zd) {
   return __fma_rn(dv, pk, __fma_rn(fa, zd, __fma_rn(-fb, zu, pk)));
 }
 
+// Levels an FP32 column loads ahead of the one it computes (1 or 2).
+#ifndef MLC_VPF_F
+#define MLC_VPF_F 1
+#endif
 // grid: x = column tiles along j times the fields (field fastest, so the
 // blocks reading one column's s and metric run together), y = row tiles,
 // z = member; block (vert_x, vert_y) columns along (j, i)
 template <class R, class T>
 __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set, int advoff,
                                const WorkItem *__restrict__ wl) {
+  constexpr int kVpf = sizeof(T) == sizeof(float) ? MLC_VPF_F : 1;  // levels loaded ahead
   const WorkItem wi = wl ? wl[blockIdx.x]
                           : WorkItem{(int16_t)blockIdx.z, (int16_t)(blockIdx.x / (unsigned)nf),
                                      (int16_t)blockIdx.y, (int16_t)(blockIdx.x % (unsigned)nf)};
@@ -431,17 +436,47 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   const double *__restrict__ z2p = kPre ? D.vzmi + ij : nullptr;
   VIf tkm1{0, 0, 0}, tkm2{0, 0, 0};
   VIf n_t = kPre ? VIf{zap[0], zmp[0], z2p[0]} : VIf{0, 0, 0};
-  // the next level's loads, issued one level ahead
+  // the next level's loads, issued one level ahead (kVpf = 2: the level
+  // after it too, in m_*)
   T n_s = T(sp[PS]), n_c = src[2 * PS], n_zu = T(zup[0]), n_zd = T(zdp[0]);
+  T m_s = T(0), m_c = T(0), m_zu = T(0), m_zd = T(0), m_dv = T(0);
+  VIf m_t{0, 0, 0};
+  if constexpr (kVpf == 2) {
+    if (kz >= 2) {
+      m_s = T(sp[2 * PS]);
+      m_zu = T(zup[PS]);
+      m_zd = T(zdp[PS]);
+      if constexpr (kPre) {
+        m_dv = T(dvp[PS]);
+        m_t = VIf{zap[PS], zmp[PS], z2p[PS]};
+      }
+    }
+    if (kz >= 4) m_c = src[3 * PS];
+  }
   // level k; every bound check is known to hold inside the column
-  // (4 <= k <= kz-3), so the interior steps carry none
+  // (4 <= k <= kz-3, kz-4 with two levels ahead), so the interior steps
+  // carry none
   auto step = [&](int k, auto interior) {
     constexpr bool I = decltype(interior)::value;
     const unsigned o = (unsigned)(k - 1) * PS;
     const T skp1 = n_s, c0p2 = (I || k + 2 <= kz) ? n_c : T(0), zuk = n_zu, zdk = n_zd;
     const T dvk = n_dv;
     const VIf tk = n_t;
-    if (I || k < kz) {
+    if constexpr (kVpf == 2) {
+      // the level after next: s at k+3, the metric at k+2, c at k+4
+      n_s = m_s; n_zu = m_zu; n_zd = m_zd; n_c = m_c;
+      if constexpr (kPre) { n_dv = m_dv; n_t = m_t; }
+      if (I || k + 2 <= kz) {
+        if constexpr (kPre) {
+          m_dv = T(dvp[o + 2 * PS]);
+          m_t = VIf{zap[o + 2 * PS], zmp[o + 2 * PS], z2p[o + 2 * PS]};
+        }
+        m_s = T(sp[o + 3 * PS]);
+        m_zu = T(zup[o + 2 * PS]);
+        m_zd = T(zdp[o + 2 * PS]);
+        if (I || k + 4 <= kz) m_c = src[o + 4 * PS];
+      }
+    } else if (I || k < kz) {
       if constexpr (kPre) {
         n_dv = T(dvp[o + PS]);
         n_t = VIf{zap[o + PS], zmp[o + PS], z2p[o + PS]};
@@ -505,7 +540,7 @@ __global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set,
   };
   using edge = std::integral_constant<bool, false>;
   using mid = std::integral_constant<bool, true>;
-  const int k1 = min(3, kz), k2 = max(4, kz - 2);
+  const int k1 = min(3, kz), k2 = max(4, kz - (kVpf == 2 ? 3 : 2));
   for (int k = 1; k <= k1; ++k) step(k, edge{});
 #pragma unroll 4
   for (int k = 4; k < k2; ++k) step(k, mid{});
