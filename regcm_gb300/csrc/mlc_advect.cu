@@ -378,7 +378,8 @@ __device__ __forceinline__ T vupdate_f(T pk, T fb, T fa, T dv, T zu, T zd) {
   return __fma_rn(dv, pk, __fma_rn(fa, zd, __fma_rn(-fb, zu, pk)));
 }
 
-// Levels an FP32 column loads ahead of the one it computes (1 or 2).
+// Levels an FP32 column loads ahead of the one it computes (1 or 2; two
+// measured no faster on the moist 512x512x41 step, 0.256 ms a step both).
 #ifndef MLC_VPF_F
 #define MLC_VPF_F 1
 #endif
@@ -631,9 +632,10 @@ __device__ __forceinline__ void next_col(T (&e)[V], const T (&x)[V]) {
 // Resident warps an SM the WAF tile kernels are compiled for; the register
 // budget follows (65536 / (32 * warps) a thread).  Measured on the moist
 // 512x512x41 step: FP32 horizontal WAF at 32 warps (64 registers) 0.46 ms a
-// step against 0.72 at 16 warps (90 registers); the increment form at 24
-// warps (80 registers) 0.29 against 0.37 ms.  FP64 at 16 warps (128
-// registers): the FP64 pipe is the bound, but 8 warps an SM leave it idle.
+// step against 0.72 at 16 warps (90 registers); the increment form at 32
+// warps (64 registers, 32 bytes spilled) 0.27 against 0.29 at 24 and 0.37 at
+// 20.  FP64 at 16 warps (128 registers): the FP64 pipe is the bound, but 8
+// warps an SM leave it idle (6.98 against 7.83 ms).
 #ifndef MLC_HWAF_WARPS
 #define MLC_HWAF_WARPS 32
 #endif
@@ -641,7 +643,7 @@ __device__ __forceinline__ void next_col(T (&e)[V], const T (&x)[V]) {
 #define MLC_HWAF_WARPS_D 16
 #endif
 #ifndef MLC_HINC_WARPS
-#define MLC_HINC_WARPS 24
+#define MLC_HINC_WARPS 32
 #endif
 template <class R>
 constexpr int waf_min_blocks(int warps, int nw) {
