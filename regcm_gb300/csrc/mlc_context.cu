@@ -756,11 +756,12 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr, int phase = kStepAll) {
   // ---- step end (Main/mod_moloch.F90:340-446) ----
   const int uvo = nadv * nsound, ao = nadv;
   if (phase != kStepFinish) {
-    REC("end_tvirt", K::end_tvirt(L, d, ao, s)); ++nl;
-    if (x->prm.do_apply_bdy) {
-      REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); nl += 2;
-      REC("bdy_relax", K::bdy_relax(L, d, uvo, ao, s)); ++nl;
-      if (x->prm.mo_spectral_nudge) { REC("bdy_spectral", K::bdy_spectral(L, d, uvo, ao, s)); nl += 3; }
+    // the ring first: the point pass after it does tvirt, t and the relaxation
+    if (x->prm.do_apply_bdy) { REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); nl += 2; }
+    REC("end_relax", K::end_relax(L, d, uvo, ao, s)); ++nl;
+    if (x->prm.do_apply_bdy && x->prm.mo_spectral_nudge) {
+      REC("bdy_spectral", K::bdy_spectral(L, d, uvo, ao, s));
+      nl += 3;
     }
   }
   if (phase == kStepAll) {
@@ -773,7 +774,7 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr, int phase = kStepAll) {
   }
   if (x->key.any_tke) { REC("end_tke", K::end_tke(L, d, phase == kStepAll, s)); ++nl; }
   REC("end_uvstag", K::end_uvstag(L, d, uvo, ao, s)); ++nl;
-  REC("end_reduce", K::end_reduce(L, d, uvo, ao, s)); nl += 2;
+  REC("end_reduce", K::end_reduce(L, d, uvo, ao, s)); ++nl;
   return nl;
 }
 

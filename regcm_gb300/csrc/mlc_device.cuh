@@ -129,6 +129,8 @@ struct Clock {
   int adv_role;      // half of the advected-field pairs holding the state
   int fault;         // sticky: a bounded device wait gave up (1 = TMA tile load)
   double tspectral;  // seconds of boundary updates, for the spectral nudging interval
+  unsigned red_done; // blocks of the step's budget reduction that have finished (0 between steps)
+  int pad;
 };
 
 // Mass budget and ps extrema of the last step (FP64).

@@ -37,49 +37,6 @@ __device__ __forceinline__ F2 qfactor_df(const float *qx, size_t o, size_t F, in
   return fast_two_sum(1.f, d);
 }
 
-// dynamical_core :1121-1123 and tvirt_to_temp :1629-1648
-template <class R>
-__global__ void k_end_tvirt(const Dom<R> *__restrict__ doms, int advoff, int tiles_j,
-    const WorkItem *__restrict__ wl) {
-  const WorkItem wi = work_item(wl, tiles_j);
-  const Dom<R> &D = doms[wi.m];
-  if (!D.active) return;
-  const Geom g = D.g;
-  const Scal &c = D.c;
-  const State<R> st = state_of(D, 0, (D.clk->adv_role + advoff) & 1);
-  const Pt q_ = point_at(wi, 1, 1);
-  const int j = q_.j, k0 = q_.k;
-  if (k0 > g.kz) return;
-  const int i = q_.i;
-  if (j > g.jx - 1 || i > g.iy - 1) return;
-  const bool inner = j >= 2 && j <= g.jx - 2 && i >= 2 && i <= g.iy - 2;
-  const size_t ij = g.at2(j, i), F = g.field3();
-#pragma unroll
-  for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
-    const size_t o = ij + (size_t)(k - 1) * g.PS;
-    const R qf = qfactor(st.qx, o, F, c.ipptls);
-    if constexpr (sizeof(R) == sizeof(float)) {
-      // t as a double-float through the step end: hi in t, lo in wz[1] (the
-      // scratch is free until the next advection); status_update rebuilds
-      // theta_v = t*qf/pai from it, so t's FP32 rounding never reaches theta_v
-      const DF th(st.tetav, F), pa(st.pai, F);
-      const F2 tv = df_mul(th.ld(o), pa.ld(o));
-      st.tvirt[o] = df_f(tv);
-      if (inner) {
-        const F2 t = df_div(tv, qfactor_df(st.qx, o, F, c.ipptls));
-        st.t[o] = t.hi;
-        D.wz[1][o] = t.lo;
-      } else {
-        D.wz[1][o] = 0.f;  // the ring keeps its t (bdyval sets it)
-      }
-    } else {
-      const R tv = R(st.tetav[o] * st.pai[o]);
-      st.tvirt[o] = tv;
-      if (inner) st.t[o] = tv / qf;
-    }
-  }
-}
-
 // bdyval, MOLOCH branch (Main/mod_bdycod.F90:1631-1860).  Phase 0 does the
 // west/east columns (corners excluded), phase 1 the south/north rows
 // (corners included), which read the corner values phase 0 left.
@@ -228,11 +185,19 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
   }
 }
 
-// motopnudge (Main/mod_bdycod.F90:4049-4083) then morelax on every field
-// (boundary, Main/mod_moloch.F90:478-497), per point; the clock has already
-// moved by dtsec.
+// The step end's point pass, after the boundary ring: virtual temperature
+// and temperature of dynamical_core :1121-1123 (tvirt_to_temp :1629-1648),
+// then - with the boundary on - motopnudge (Main/mod_bdycod.F90:4049-4083)
+// and morelax on every field (boundary, Main/mod_moloch.F90:478-497).  Both
+// are per point, so one thread does both at its points and t goes from the
+// first to the second in registers.  The ring (bdyval) runs before this pass
+// although the reference's order is tvirt, bdyval, relaxation: the ring reads
+// only boundary data and the interior values of qx, w and TKE, which the
+// temperature pass does not write, and it writes only ring points, where
+// this pass leaves t alone; tvirt at the ring points is recomputed by the
+// status update.  The relaxation's clock has already moved by dtsec.
 template <class R>
-__global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j,
+__global__ void k_end_relax(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int tiles_j,
     const WorkItem *__restrict__ wl) {
   const WorkItem wi = work_item(wl, tiles_j);
   const Dom<R> &D = doms[wi.m];
@@ -243,12 +208,20 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const Bdy<R> &bd = D.bd;
   const Clock *clk = D.clk;
   const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
-  const Pt q_ = point_at(wi, 2, 2);
+  const Pt q_ = point_at(wi, 1, 1);
   const int j = q_.j, k0 = q_.k;
   if (k0 > g.kz) return;
   const int i = q_.i;
   const int jx = g.jx, iy = g.iy;
   if (j > jx - 1 || i > iy - 1) return;
+  const bool inner = j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2;
+  const size_t ij = g.at2(j, i), PS = g.PS, F = g.field3();
+  // the relaxation's points: jci x ici (t and the cross fields), jdi x ici
+  // (u), jci x idi (v); none without the boundary
+  const bool bdy = c.apply_bdy != 0 && j >= 2 && i >= 2;
+  const bool cr = bdy && j <= jx - 2 && i <= iy - 2;
+  const bool up = bdy && i <= iy - 2;
+  const bool vp = bdy && j <= jx - 2;
   const double xb = clk->xbctime + c.dtsec;
   const double x1 = (xb + c.dt) * c.rtb;
   const double x0 = 1.0 - x1;
@@ -257,10 +230,6 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const R rx0 = R(x0), rx1 = R(x1);
   const double trtau = 1.0 / (2.0 * 3600.0);
   const double wrtau = 1.0 / (3600.0 / 4.0);
-  const size_t ij = g.at2(j, i), PS = g.PS, F = g.field3();
-  const bool cr = j <= jx - 2 && i <= iy - 2;  // jci x ici
-  const bool up = i <= iy - 2;                 // jdi x ici
-  const bool vp = j <= jx - 2;                 // jci x idi
   const int nsp = c.nspgx;
   const int ibc = cr ? sa.ibnd_cr[ij] : -1;
   const int ibu = up ? sa.ibnd_ud[ij] : -1;
@@ -273,6 +242,27 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const R xfn0 = pick<R>(trtau * c.dtsec, float(trtau * c.dtsec));
 #pragma unroll
   for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
+    const size_t o = ij + (size_t)(k - 1) * PS;
+    // ---- tvirt and t (every cross point; t only inside the ring) ----
+    const R qf = qfactor(st.qx, o, F, c.ipptls);
+    F2 tdf{0.f, 0.f};  // a mixed member's double-float t
+    R tr = R(0);       // an FP64 member's t
+    if constexpr (sizeof(R) == sizeof(float)) {
+      // t as a double-float through the step end: hi in t, lo in wz[1] (the
+      // scratch is free until the next advection); status_update rebuilds
+      // theta_v = t*qf/pai from it, so t's FP32 rounding never reaches theta_v
+      const DF th(st.tetav, F), pa(st.pai, F);
+      const F2 tv = df_mul(th.ld(o), pa.ld(o));
+      st.tvirt[o] = df_f(tv);
+      if (inner) tdf = df_div(tv, qfactor_df(st.qx, o, F, c.ipptls));
+      else if (!c.apply_bdy) D.wz[1][o] = 0.f;  // (with the boundary on, the ring wrote it)
+    } else {
+      const R tv = R(st.tetav[o] * st.pai[o]);
+      st.tvirt[o] = tv;
+      if (inner) tr = tv / qf;
+    }
+    (void)qf;
+    // ---- motopnudge and morelax ----
     if (k == 2 && cr && c.top_nudge) {
       const size_t o2 = ij + PS;  // level 2 (w sponge, before the level's relaxation)
       const R xf = R(wrtau * c.dtsec);
@@ -280,7 +270,6 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
       const R fext = R(0) * w2;
       st.w[o2] = bdy_relax_to<R>(w2, xf, fext);
     }
-    const size_t o = ij + (size_t)(k - 1) * PS;
     const bool nud = c.top_nudge && k <= c.nztop;
     R xfn;
     if constexpr (sizeof(R) == sizeof(float)) xfn = nud ? sa.tnudge_r[k - 1] * xfn0 : R(0);
@@ -298,34 +287,38 @@ __global__ void k_bdy_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
       if (ibv > 0) f = relax(f, blend(bd.dvb, o), ibv, k);
       st.v[o] = f;
     }
-    if (!cr || (!nud && ibc <= 0)) continue;
-    if constexpr (sizeof(R) == sizeof(float)) {
-      // (1-x)*t + x*b as t + x*(b - t) on the double-float t
-      F2 f{st.t[o], D.wz[1][o]};
-      const DF b0(bd.xtb[0], F), b1(bd.xtb[1], F);
-      const F2 a = b0.ld(o);
-      const F2 bt = df_add_f(a, float(x1) * df_diff(b1.ld(o), a));
-      if (nud) f = df_add_f(f, xfn * df_diff(bt, f));
-      if (ibc > 0) {
-        const float xf = sa.hefc_r[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
-        f = df_add_f(f, xf * df_diff(bt, f));
+    if (cr && (nud || ibc > 0)) {
+      if constexpr (sizeof(R) == sizeof(float)) {
+        // (1-x)*t + x*b as t + x*(b - t) on the double-float t
+        const DF b0(bd.xtb[0], F), b1(bd.xtb[1], F);
+        const F2 a = b0.ld(o);
+        const F2 bt = df_add_f(a, float(x1) * df_diff(b1.ld(o), a));
+        if (nud) tdf = df_add_f(tdf, xfn * df_diff(bt, tdf));
+        if (ibc > 0) {
+          const float xf = sa.hefc_r[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
+          tdf = df_add_f(tdf, xf * df_diff(bt, tdf));
+        }
+      } else {
+        const double bt = x0 * bd.xtb[0][o] + x1 * bd.xtb[1][o];
+        if (nud) tr = (R(1) - xfn) * tr + xfn * R(bt);
+        if (ibc > 0) tr = relax(tr, R(bt), ibc, k);
       }
-      st.t[o] = f.hi;
-      D.wz[1][o] = f.lo;
-    } else {
-      R f = st.t[o];
-      const double bt = x0 * bd.xtb[0][o] + x1 * bd.xtb[1][o];
-      if (nud) f = (R(1) - xfn) * f + xfn * R(bt);
-      if (ibc > 0) f = relax(f, R(bt), ibc, k);
-      st.t[o] = f;
     }
-    if (ibc <= 0) continue;
+    if (inner) {
+      if constexpr (sizeof(R) == sizeof(float)) {
+        st.t[o] = tdf.hi;
+        D.wz[1][o] = tdf.lo;
+      } else {
+        st.t[o] = tr;
+      }
+    }
+    if (!cr || ibc <= 0) continue;
     if constexpr (sizeof(R) == sizeof(float)) {
       // (1 - xf)*pai + xf*(b0 + x1*(b1 - b0)) as pai + xf*((b0 - pai) + x1*(b1 - b0))
       const float xf = sa.hefc_r[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
       const DF pa(st.pai, F), b0(bd.xpaib[0], F), b1(bd.xpaib[1], F);
-      const F2 p = pa.ld(o), a = b0.ld(o);
-      pa.st(o, df_add_f(p, xf * (df_diff(a, p) + float(x1) * df_diff(b1.ld(o), a))));
+      const F2 pp = pa.ld(o), a = b0.ld(o);
+      pa.st(o, df_add_f(pp, xf * (df_diff(a, pp) + float(x1) * df_diff(b1.ld(o), a))));
     } else {
       const double xf = sa.hefc[(size_t)(ibc - 1) + (size_t)(k - 1) * nsp];
       const double fext = x0 * bd.xpaib[0][o] + x1 * bd.xpaib[1][o];
@@ -932,6 +925,47 @@ __device__ __forceinline__ void ld_vec16(R (&x)[V], const R *p) {
 // dx^2 is applied once per thread.  The lateral fluxes and the ps extrema
 // are grid-stride loops over their own items.  Sums are in a fixed order for
 // a given member, whatever else the launch holds.
+// Per member, by one warp of the reduction's last block: add the partials
+// (lanes stride over the blocks in block order, then a fixed shuffle tree,
+// so the result does not depend on which block finished last), store the
+// diagnostics, then advance the boundary clock and the buffer roles to the
+// next step's and re-arm the block count.
+template <class R>
+__device__ void reduce_finish(const Dom<R> &D, int uvoff, int advoff, int lane) {
+  const double *part = D.partials;
+  const int nblocks = D.red_blocks;
+  double a[4] = {0, 0, 0, 0}, pmax = -INFINITY, pmin = INFINITY, bad = 0;
+  for (int b = lane; b < nblocks; b += 32) {
+    const double *p = part + (size_t)b * kNPart;
+    for (int q = 0; q < 4; ++q) a[q] += __ldcg(p + q);
+    pmax = fmax(pmax, __ldcg(p + 4));
+    pmin = fmin(pmin, __ldcg(p + 5));
+    bad += __ldcg(p + 6);
+  }
+  const unsigned full = 0xffffffffu;
+  for (int off = 16; off > 0; off >>= 1) {
+    for (int q = 0; q < 4; ++q) a[q] += __shfl_down_sync(full, a[q], off);
+    pmax = fmax(pmax, __shfl_down_sync(full, pmax, off));
+    pmin = fmin(pmin, __shfl_down_sync(full, pmin, off));
+    bad += __shfl_down_sync(full, bad, off);
+  }
+  if (lane != 0) return;
+  DiagDev *diag = D.diag;
+  Clock *clk = D.clk;
+  const bool isbad = bad != 0.0;
+  diag->drymass = a[0]; diag->dryadv = a[1]; diag->qmass = a[2]; diag->qadv = a[3];
+  diag->ps_max = isbad ? NAN : pmax;
+  diag->ps_min = isbad ? NAN : pmin;
+  diag->nonfinite = isbad ? 1 : 0;
+  if (isbad && !clk->nonfinite) { clk->nonfinite = 1; clk->bad_step = clk->step; }
+  if (D.c.apply_bdy) clk->xbctime = clk->xbctime + D.c.dtsec;
+  if (D.c.apply_bdy && D.c.spectral) clk->tspectral = clk->tspectral + D.c.dtsec;
+  clk->step = clk->step + 1;
+  clk->uv_role = (clk->uv_role + uvoff) & 1;
+  clk->adv_role = (clk->adv_role + advoff) & 1;
+  clk->red_done = 0u;
+}
+
 template <class R>
 __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__restrict__ doms,
                                                                 int uvoff, int advoff) {
@@ -1071,6 +1105,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
     sh[warp][4] = pmax; sh[warp][5] = pmin; sh[warp][6] = bad;
   }
   __syncthreads();
+  __shared__ bool last;
   if (threadIdx.x == 0) {
     double a[kNPart] = {0, 0, 0, 0, -INFINITY, INFINITY, 0};
     for (int w = 0; w < kRedWarps; ++w) {
@@ -1079,48 +1114,15 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_partial(const Dom<R> *__
     }
     double *p = D.partials + (size_t)blockIdx.x * kNPart;
     for (int q = 0; q < kNPart; ++q) p[q] = a[q];
+    // the member's last block to finish adds the partials: its partials are
+    // visible before its ticket, and every other block's before theirs
+    __threadfence();
+    last = atomicAdd(&D.clk->red_done, 1u) == (unsigned)nb - 1u;
   }
-}
-
-// Per member: add the partials (lanes stride over the blocks, then a fixed
-// shuffle tree), store the diagnostics, then advance the boundary clock and
-// the buffer roles to the next step's.
-template <class R>
-__global__ void k_reduce_final(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
-  const Dom<R> &D = doms[blockIdx.x];
-  if (!D.active) return;
-  const double *part = D.partials;
-  const int nblocks = D.red_blocks;
-  const int lane = threadIdx.x;
-  double a[4] = {0, 0, 0, 0}, pmax = -INFINITY, pmin = INFINITY, bad = 0;
-  for (int b = lane; b < nblocks; b += 32) {
-    const double *p = part + (size_t)b * kNPart;
-    for (int q = 0; q < 4; ++q) a[q] += p[q];
-    pmax = fmax(pmax, p[4]);
-    pmin = fmin(pmin, p[5]);
-    bad += p[6];
-  }
-  const unsigned full = 0xffffffffu;
-  for (int off = 16; off > 0; off >>= 1) {
-    for (int q = 0; q < 4; ++q) a[q] += __shfl_down_sync(full, a[q], off);
-    pmax = fmax(pmax, __shfl_down_sync(full, pmax, off));
-    pmin = fmin(pmin, __shfl_down_sync(full, pmin, off));
-    bad += __shfl_down_sync(full, bad, off);
-  }
-  if (lane != 0) return;
-  DiagDev *diag = D.diag;
-  Clock *clk = D.clk;
-  const bool isbad = bad != 0.0;
-  diag->drymass = a[0]; diag->dryadv = a[1]; diag->qmass = a[2]; diag->qadv = a[3];
-  diag->ps_max = isbad ? NAN : pmax;
-  diag->ps_min = isbad ? NAN : pmin;
-  diag->nonfinite = isbad ? 1 : 0;
-  if (isbad && !clk->nonfinite) { clk->nonfinite = 1; clk->bad_step = clk->step; }
-  if (D.c.apply_bdy) clk->xbctime = clk->xbctime + D.c.dtsec;
-  if (D.c.apply_bdy && D.c.spectral) clk->tspectral = clk->tspectral + D.c.dtsec;
-  clk->step = clk->step + 1;
-  clk->uv_role = (clk->uv_role + uvoff) & 1;
-  clk->adv_role = (clk->adv_role + advoff) & 1;
+  __syncthreads();
+  if (!last || threadIdx.x >= 32) return;
+  __threadfence();
+  reduce_finish<R>(D, uvoff, advoff, (int)threadIdx.x);
 }
 
 template <class R>
@@ -1227,14 +1229,6 @@ __global__ void k_end_tke(const Dom<R> *__restrict__ doms, int whole, int tiles_
 }
 
 template <class R>
-void Launch<R>::end_tvirt(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s) {
-  const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  int tj;
-  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
-  k_end_tvirt<R><<<grd, b, 0, s>>>(d, advoff, tj, L.wl_pt);
-}
-
-template <class R>
 void Launch<R>::bdy_ring(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const int nwe = L.iy - 2, nsn = L.jx;
   const unsigned zz = 2u * (unsigned)L.nmem;
@@ -1243,11 +1237,11 @@ void Launch<R>::bdy_ring(const LaunchGeom &L, const Dom<R> *d, int uvoff, int ad
 }
 
 template <class R>
-void Launch<R>::bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
+void Launch<R>::end_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
   int tj;
-  const dim3 grd = pt_grid(L, L.jx - 2, L.iy - 2, tj);
-  k_bdy_relax<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
+  const dim3 grd = pt_grid(L, L.jx - 1, L.iy - 1, tj);
+  k_end_relax<R><<<grd, b, 0, s>>>(d, uvoff, advoff, tj, L.wl_pt);
 }
 
 template <class R>
@@ -1314,7 +1308,6 @@ void Launch<R>::end_reduce(const LaunchGeom &L, const Dom<R> *d, int uvoff, int 
                            cudaStream_t s) {
   k_reduce_partial<R><<<dim3((unsigned)L.red_blocks, (unsigned)L.nmem), kRedThreads, 0, s>>>(
       d, uvoff, advoff);
-  k_reduce_final<R><<<(unsigned)L.nmem, 32, 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R>

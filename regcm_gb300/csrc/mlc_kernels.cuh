@@ -61,9 +61,8 @@ template <class R> struct Launch {
   static void adv_curvature(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
   static void adv_back(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   // ---- step end (Main/mod_moloch.F90:340-446, mod_bdycod.F90) ----
-  static void end_tvirt(const LaunchGeom &L, const Dom<R> *d, int advoff, cudaStream_t s);
   static void bdy_ring(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
-  static void bdy_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
+  static void end_relax(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void bdy_spectral(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   static void end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s);
   // the step split at the physics: k_end_ps and the cross-point work up to
