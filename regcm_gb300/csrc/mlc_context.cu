@@ -757,7 +757,7 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr, int phase = kStepAll) {
   const int uvo = nadv * nsound, ao = nadv;
   if (phase != kStepFinish) {
     // the ring first: the point pass after it does tvirt, t and the relaxation
-    if (x->prm.do_apply_bdy) { REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); nl += 2; }
+    if (x->prm.do_apply_bdy) { REC("bdy_ring", K::bdy_ring(L, d, uvo, ao, s)); ++nl; }
     REC("end_relax", K::end_relax(L, d, uvo, ao, s)); ++nl;
     if (x->prm.do_apply_bdy && x->prm.mo_spectral_nudge) {
       REC("bdy_spectral", K::bdy_spectral(L, d, uvo, ao, s));

@@ -58,9 +58,15 @@ __device__ __forceinline__ R bdy_relax_to(R f, R x, R fext) {
   else return (R(1) - x) * f + x * fext;
 }
 
+// One block per level and member runs both phases, a block barrier between
+// them: everything phase 1 reads that phase 0 writes (qx, w at the level,
+// TKE one interface up, written by the same level's phase 0) lies in the
+// block's own level.
+constexpr int kRingThreads = 256;
 template <class R>
-__global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advoff, int phase) {
-  const Dom<R> &D = doms[blockIdx.z >> 1];
+__global__ void __launch_bounds__(kRingThreads) k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff,
+                                                           int advoff) {
+  const Dom<R> &D = doms[blockIdx.y];
   if (!D.active) return;
   const Geom g = D.g;
   const Scal &c = D.c;
@@ -68,10 +74,8 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
   const Clock *clk = D.clk;
   const State<R> st = state_of(D, (clk->uv_role + uvoff) & 1, (clk->adv_role + advoff) & 1);
   const int jx = g.jx, iy = g.iy;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;  // position along the side
-  const int k = blockIdx.y + 1;
-  if (k > g.kz) return;                                  // a member with fewer levels
-  const int side = blockIdx.z & 1;                       // 0 = west/south, 1 = east/north
+  const int k = blockIdx.x + 1;
+  if (k > g.kz) return;                                  // a member with fewer levels (whole block)
   const double xb = clk->xbctime;
   const double x1 = (xb + c.dt) * c.rtb;
   const double x0 = 1.0 - x1;
@@ -104,6 +108,8 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
     }
   };
   const int nqx = g.nqx;
+  // side 0 = west/south, 1 = east/north; idx the position along the side
+  auto point = [&](int phase, int side, int idx) {
   if (phase == 0) {
     const int i = idx + 2;  // i in idi = 2..iy-1 (v), ici = 2..iy-2 (others)
     if (i > iy - 1) return;
@@ -183,6 +189,11 @@ __global__ void k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff, int advof
       st.trac[ob + on] = bdy_blend<R>(R(cx0), R(cx1), bd.chib[0][ob + on], bd.chib[1][ob + on]);
     }
   }
+  };
+  const int n0 = iy - 2, n1 = jx;  // positions a side: phase 0 i = 2..iy-1, phase 1 j = 1..jx
+  for (int e = (int)threadIdx.x; e < 2 * n0; e += kRingThreads) point(0, e >= n0 ? 1 : 0, e >= n0 ? e - n0 : e);
+  __syncthreads();
+  for (int e = (int)threadIdx.x; e < 2 * n1; e += kRingThreads) point(1, e >= n1 ? 1 : 0, e >= n1 ? e - n1 : e);
 }
 
 // The step end's point pass, after the boundary ring: virtual temperature
@@ -1230,10 +1241,7 @@ __global__ void k_end_tke(const Dom<R> *__restrict__ doms, int whole, int tiles_
 
 template <class R>
 void Launch<R>::bdy_ring(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
-  const int nwe = L.iy - 2, nsn = L.jx;
-  const unsigned zz = 2u * (unsigned)L.nmem;
-  k_bdy_ring<R><<<dim3((unsigned)((nwe + 63) / 64), (unsigned)L.kz, zz), 64, 0, s>>>(d, uvoff, advoff, 0);
-  k_bdy_ring<R><<<dim3((unsigned)((nsn + 63) / 64), (unsigned)L.kz, zz), 64, 0, s>>>(d, uvoff, advoff, 1);
+  k_bdy_ring<R><<<dim3((unsigned)L.kz, (unsigned)L.nmem), kRingThreads, 0, s>>>(d, uvoff, advoff);
 }
 
 template <class R>
