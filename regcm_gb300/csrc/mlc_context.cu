@@ -765,7 +765,7 @@ int enqueue_step(mlc_ctx *x, Recorder *rec = nullptr, int phase = kStepAll) {
     }
   }
   if (phase == kStepAll) {
-    REC("end_cross", K::end_cross(L, d, uvo, ao, s)); nl += 2;
+    REC("end_cross", K::end_cross(L, d, uvo, ao, s)); ++nl;
   } else if (phase == kStepDynamics) {
     REC("end_mkslice", K::end_cross_split(L, d, uvo, ao, false, s)); nl += 2;
     return nl;

@@ -522,23 +522,16 @@ __global__ void k_spec_apply(const Dom<R> *__restrict__ doms, int uvoff, int adv
   }
 }
 
-// extrapolate_surface_pressure (:1592-1606) per interior column, from t
-// and q at the two lowest levels before status_update clamps q, and p at the
-// lowest level (the same expression k_end_cross stores).
+// extrapolate_surface_pressure (:1592-1606) of the interior column at ij,
+// from t and q at the two lowest levels before status_update clamps q, and p
+// at the lowest level (the same expression k_end_cross stores).
 template <class R>
-__global__ void k_end_ps(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
-  const Dom<R> &D = doms[blockIdx.z];
-  if (!D.active) return;
-  const Geom g = D.g;
+__device__ __forceinline__ void ps_column(const Dom<R> &D, const State<R> &st, size_t ij) {
+  const Geom &g = D.g;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
-  const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  const int jx = g.jx, iy = g.iy, kz = g.kz;
-  if (j > jx - 2 || i > iy - 2) return;
-  const size_t ij = g.at2(j, i), PS = g.PS, F = g.field3();
-  const int ipp = c.ipptls;
+  const size_t PS = g.PS, F = g.field3();
+  const int ipp = c.ipptls, kz = g.kz;
   // tvirt at kz-1, kz before the clamps: from the boundary's temp_to_tvirt,
   // or tetav*pai of dynamical_core when the boundary is off
   const size_t o1 = ij + (size_t)(kz - 2) * PS, o2 = ij + (size_t)(kz - 1) * PS;
@@ -561,11 +554,27 @@ __global__ void k_end_ps(const Dom<R> *__restrict__ doms, int uvoff, int advoff)
   st.ps[ij] = (double)p2 * exp(kGovr * z2 / tv);
 }
 
+// ps of every interior column, for the split step (the whole step's
+// k_end_cross forms it in the thread that owns the column's lowest levels)
+template <class R>
+__global__ void k_end_ps(const Dom<R> *__restrict__ doms, int uvoff, int advoff) {
+  const Dom<R> &D = doms[blockIdx.z];
+  if (!D.active) return;
+  const Geom g = D.g;
+  const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (j > g.jx - 2 || i > g.iy - 2) return;
+  ps_column<R>(D, st, g.at2(j, i));
+}
+
 // Cross-point work after the boundary, per point: uvstagtouvx and
 // temp_to_tvirt of boundary (:520-523), p (:348-352), the edits mkslice
 // makes to the state (Main/mod_slice.F90:136-147: qx and tracer floors),
 // then status_update (:1403-1443): tendencies, q clamps, tvirt, tetav, rho,
-// qsat (the surface pressure is k_end_ps's, launched first).
+// qsat.  The surface pressure is extrapolated before the clamps: in the
+// whole step by the thread holding the column's two lowest levels (chunks
+// of levels are counted from the top), in the split step by k_end_ps.
 //   kEndAll   the whole sequence with zero tendencies (mlc_step).  rho and
 //             qsat of :348-352, and tvirt and tetav of the boundary, are
 //             recomputed from the same inputs by status_update, so they are
@@ -587,12 +596,17 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
   const Pt q_ = point_at(wi, 1, 1);
   const int j = q_.j, i = q_.i;
   const int jx = g.jx, iy = g.iy, kz = g.kz;
-  if (j > jx - 1 || i > iy - 1 || q_.k > kz) return;
+  // level chunks counted from the top, so the chunk holding kz also holds
+  // kz-1 (the levels ps is extrapolated from)
+  const int khi = kz - (int)wi.c * kPtLevels, klo = max(1, khi - kPtLevels + 1);
+  if (j > jx - 1 || i > iy - 1 || khi < 1) return;
   const size_t ij = g.at2(j, i), PS = g.PS, F = g.field3(), S = (size_t)g.P;
   const bool inner = j >= 2 && j <= jx - 2 && i >= 2 && i <= iy - 2;
   const int ipp = c.ipptls;
+  // the whole step: ps before this thread clamps q at kz-1, kz
+  if (PH == kEndAll && khi == kz && inner) ps_column<R>(D, st, ij);
 #pragma unroll
-  for (int k = q_.k; k < q_.k + kPtLevels && k <= kz; ++k) {
+  for (int k = klo; k <= khi; ++k) {
   const size_t o = ij + (size_t)(k - 1) * PS;
   if (PH != kEndPost && c.apply_bdy) {
     {
@@ -724,8 +738,9 @@ __global__ void __launch_bounds__(128) k_end_cross_v4(const Dom<R> *__restrict__
   const int bj = wi.a, bi = wi.b;
   const int e0 = (bj * 32 + (int)threadIdx.x) * 4;
   const int i = bi * (int)blockDim.y + (int)threadIdx.y + 1;
-  const int k0 = (int)wi.c * kPtLevels + 1;
-  if (e0 + 1 > jx - 1 || i > iy - 1 || k0 > kz) return;
+  // level chunks counted from the top (the chunk holding kz holds kz-1)
+  const int khi = kz - (int)wi.c * kPtLevels, klo = max(1, khi - kPtLevels + 1);
+  if (e0 + 1 > jx - 1 || i > iy - 1 || khi < 1) return;
   const Scal &c = D.c;
   const State<R> st = state_of(D, (D.clk->uv_role + uvoff) & 1, (D.clk->adv_role + advoff) & 1);
   const float *__restrict__ u = st.u;
@@ -767,7 +782,12 @@ __global__ void __launch_bounds__(128) k_end_cross_v4(const Dom<R> *__restrict__
         if (has[q]) dst[q] = x[q];
     }
   };
-  for (int k = k0; k < k0 + kPtLevels && k <= kz; ++k) {
+  // ps of the lane's interior columns before this thread clamps q at kz-1, kz
+  if (khi == kz)
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (inner[q]) ps_column<R>(D, st, (size_t)ij + (size_t)q);
+  for (int k = klo; k <= khi; ++k) {
     const unsigned o = ij + (unsigned)(k - 1) * PS;
     if (c.apply_bdy) {
       // u at j-1 .. j+2 and v at rows i-1 .. i+2 (:1535-1566)
@@ -1267,7 +1287,6 @@ void Launch<R>::bdy_spectral(const LaunchGeom &L, const Dom<R> *d, int uvoff, in
 template <class R>
 void Launch<R>::end_cross(const LaunchGeom &L, const Dom<R> *d, int uvoff, int advoff, cudaStream_t s) {
   const dim3 b((unsigned)L.col_x, (unsigned)L.col_y);
-  k_end_ps<R><<<grid2(L.jx - 3, L.iy - 3, b, L.nmem), b, 0, s>>>(d, uvoff, advoff);
   if constexpr (sizeof(R) == sizeof(float)) {
     const int tj = (L.jx - 1 + 127) / 128, ti = (L.iy - 1 + 3) / 4;
     const dim3 grd = L.wl_v4 ? dim3((unsigned)L.n_v4, 1, 1)
