@@ -147,6 +147,12 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tile
 // loop).  The per-level expressions are the reference's, in its order.
 // (Measured on the 512x512x41 step: 3.99 ms of solves a step against 5.68
 // for a column-in-shared-memory form, whose 66 KB a block left 6 warps an SM.)
+// Levels read between two block barriers of the streamed column solves (a
+// barrier frees the stages read since the last one for their refill).
+#ifndef MLC_SOLVE_SYNC
+#define MLC_SOLVE_SYNC 1
+#endif
+constexpr int kSolveSync = MLC_SOLVE_SYNC;
 constexpr int kDvStages = 3;
 constexpr int kDvW = 128;
 constexpr int kDvZW = kDvW + 4;                   // raw divergence row, 2-column halo each side
@@ -266,6 +272,8 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
     tet_k = tetav[o];
     wnext = w[kz * PS + ij_off];  // w(kz+1) = -s(kz+1)
   }
+  bool ok = true;
+  int synced = 0;  // first unit read since the last block barrier
   for (int u = 0; u < nd; ++u) {
     const int k = kz - u, m = k - 1;
     const int b = u % NS;
@@ -296,11 +304,18 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
       zfk = zf_m;
       pai_k = pai_m; tet_k = tet_m; fmz_k = fmz_m; s_k = s_m;
     }
-    if (__syncthreads_or(!landed)) {
-      bail(u + 1, nd);
-      return;
+    ok = ok && landed;
+    if ((u + 1) % kSolveSync == 0 || u + 1 == nd) {
+      if (__syncthreads_or(!ok)) {
+        bail(u + 1, min(nd, synced + NS));  // the units issued and not read
+        return;
+      }
+      // the stages read since the last barrier are free: refill them
+      if (t == 0)
+        for (int r = synced; r <= u; ++r)
+          if (r + NS < nd) issue_down(r + NS, r % NS);
+      synced = u + 1;
     }
-    if (t == 0 && u + NS < nd) issue_down(u + NS, b);
   }
   if (act) zfs[ij_off] = zfk;  // level 1
   fence_proxy_async_global();
@@ -315,6 +330,8 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
     if (last && m >= 2) s[o] = (wm + sm) * fzf;
   };
   double wprev = act ? w[ij_off] : 0.0;  // w(1) = 0
+  ok = true;
+  synced = 0;
   for (int v = 0; v < nu; ++v) {
     const int k = v + 2, gu = nd + v;
     const int b = gu % NS;
@@ -333,11 +350,17 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
         exner(kz, wprev, wel, cp, czf, cfz_, cs, cfzf);
       }
     }
-    if (__syncthreads_or(!landed)) {
-      bail(gu + 1, nd + nu);
-      return;
+    ok = ok && landed;
+    if ((v + 1) % kSolveSync == 0 || v + 1 == nu) {
+      if (__syncthreads_or(!ok)) {
+        bail(gu + 1, nd + min(nu, synced + NS));
+        return;
+      }
+      if (t == 0)
+        for (int r = synced; r <= v; ++r)
+          if (r + NS < nu) issue_up(r + NS, (nd + r) % NS);
+      synced = v + 1;
     }
-    if (t == 0 && v + NS < nu) issue_up(v + NS, b);
   }
   if (last && act) {
     s[ij_off] = 0.0;
@@ -525,6 +548,8 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
   }
   float wkp1 = 0.f;
   F2 wnextd{wnext, 0.f}, wkp1d{0.f, 0.f};
+  bool ok = true;
+  int synced = 0;  // first unit read since the last block barrier
   for (int u = 0; u < nd; ++u) {
     const int k = kz - u, m = k - 1;
     const int b = u % NS;
@@ -580,11 +605,18 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
       zfk = zf_m;
       ak = am;
     }
-    if (__syncthreads_or(!landed)) {
-      bail(u + 1, nd);
-      return;
+    ok = ok && landed;
+    if ((u + 1) % kSolveSync == 0 || u + 1 == nd) {
+      if (__syncthreads_or(!ok)) {
+        bail(u + 1, min(nd, synced + NS));  // the units issued and not read
+        return;
+      }
+      // the stages read since the last barrier are free: refill them
+      if (t == 0)
+        for (int r = synced; r <= u; ++r)
+          if (r + NS < nd) issue_down(r + NS, r % NS);
+      synced = u + 1;
     }
-    if (t == 0 && u + NS < nd) issue_down(u + NS, b);
   }
   if (act) zfs[ij_off] = zfk;  // level 1
   // this thread's stores of w, mul and zfs are read back by the copy engine
@@ -604,6 +636,8 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
   };
   float wprev = act ? w[ij_off] : 0.f;  // w(1) = 0
   F2 wprevd{wprev, 0.f};
+  ok = true;
+  synced = 0;
   for (int v = 0; v < nu; ++v) {
     const int k = v + 2, gu = nd + v;
     const int b = gu % NS;
@@ -635,11 +669,17 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
         }
       }
     }
-    if (__syncthreads_or(!landed)) {
-      bail(gu + 1, nd + nu);
-      return;
+    ok = ok && landed;
+    if ((v + 1) % kSolveSync == 0 || v + 1 == nu) {
+      if (__syncthreads_or(!ok)) {
+        bail(gu + 1, nd + min(nu, synced + NS));
+        return;
+      }
+      if (t == 0)
+        for (int r = synced; r <= v; ++r)
+          if (r + NS < nu) issue_up(r + NS, (nd + r) % NS);
+      synced = v + 1;
     }
-    if (t == 0 && v + NS < nu) issue_up(v + NS, b);
   }
   if (last && act) {
     s[ij_off] = 0.f;
