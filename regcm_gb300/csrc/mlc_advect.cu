@@ -738,8 +738,17 @@ __global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(sizeof(R) == sizeof
   const bool rowM = i >= 2 && i <= iy - 1;  // meridional flux rows
   const bool rowP = i >= 2 && i <= iy - 2;  // p0, zonal flux and update rows
   const bool okM = inrow && rowM, okP = inrow && rowP;
-  T vv[V], zmy[V], vve[V], zmye[V];
-  bool mv[V], me[V];  // meridional flux defined at the column (row i, row I0+NW)
+  // The fluxes of row I0+NW (the tile's north face): with two columns a lane
+  // the last two warps take 32 columns each, one a lane, so that no warp
+  // forms more than three flux rows' worth before the block barrier (the
+  // last warp alone would form four); with one column a lane the last warp
+  // takes them.  ec0 is the range column of the lane's first one there.
+  constexpr int VE = V == 2 && NW >= 2 ? 1 : V;
+  const bool eWarp = VE == 1 && V == 2 ? wp >= NW - 2 : wp == NW - 1;
+  const int ec0 = VE == 1 && V == 2 ? (wp - (NW - 2)) * 32 + lane : V * lane;
+  const int eE0 = ob + ec0;
+  T vv[V], zmy[V], vve[VE], zmye[VE];
+  bool mv[V], me[VE];  // meridional flux defined at the column (row i, row I0+NW)
   {
     T a[V], b[V];
     ld_row<T, V>(a, vk, e0, i, P, okM);
@@ -751,17 +760,18 @@ __global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(sizeof(R) == sizeof
       vv[q] = ok ? a[q] : T(0);  // the flux's wind v (= 2*hvel)
       zmy[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
     }
-    // the last warp also forms the fluxes of row I0+NW
     const int ie = I0 + NW;
-    const bool okE = wp == NW - 1 && inrow && ie >= 2 && ie <= iy - 1;
-    ld_row<T, V>(a, vk, e0, ie, P, okE);
-    ld_row<T, V>(b, sa.msfv, e0, ie, P, okE && !rot);
+    const bool okE = eWarp && eE0 >= 0 && eE0 + VE <= g.P && ie >= 2 && ie <= iy - 1;
+    T ae[VE], be[VE];
+    ld_row<T, VE>(ae, vk, eE0, ie, P, okE);
+    ld_row<T, VE>(be, sa.msfv, eE0, ie, P, okE && !rot);
 #pragma unroll
-    for (int q = 0; q < V; ++q) {
-      const bool ok = okE && jq[q] >= 1 && jq[q] <= jx - 1;
+    for (int q = 0; q < VE; ++q) {
+      const int je = eE0 + q + 1;
+      const bool ok = okE && je >= 1 && je <= jx - 1;
       me[q] = ok;
-      vve[q] = ok ? a[q] : T(0);
-      zmye[q] = ok ? (rot ? a[q] * dtrdy : a[q] * b[q] * dtrdy) : T(0);
+      vve[q] = ok ? ae[q] : T(0);
+      zmye[q] = ok ? (rot ? ae[q] * dtrdy : ae[q] * be[q] * dtrdy) : T(0);
     }
   }
   T zs[V], zn[V], dvy[V], m2[V], uu[V], zmx[V], zw[V], ze[V], dvx[V];
@@ -824,19 +834,22 @@ __global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(sizeof(R) == sizeof
   }
   // the three fluxes' factors in the form vel*(x - zmih*B), once for every
   // field: the upwind flags (zamu > 0) and zmih
-  bool upy[V], upe[V], upx[V];
-  T z2y[V], z2e[V], z2x[V];  // zmi = 2*zmih (FP64 only)
+  bool upy[V], upe[VE], upx[V];
+  T z2y[V], z2e[VE], z2x[V];  // zmi = 2*zmih (FP64 only)
 #pragma unroll
   for (int q = 0; q < V; ++q) {
     upy[q] = positive(zmy[q]);
-    upe[q] = positive(zmye[q]);
     upx[q] = positive(zmx[q]);
     z2y[q] = waf_zmi<T>(zmy[q], upy[q]);
-    z2e[q] = waf_zmi<T>(zmye[q], upe[q]);
     z2x[q] = waf_zmi<T>(zmx[q], upx[q]);
     zmy[q] = z2y[q] * T(0.5);
-    zmye[q] = z2e[q] * T(0.5);
     zmx[q] = z2x[q] * T(0.5);
+  }
+#pragma unroll
+  for (int q = 0; q < VE; ++q) {
+    upe[q] = positive(zmye[q]);
+    z2e[q] = waf_zmi<T>(zmye[q], upe[q]);
+    zmye[q] = z2e[q] * T(0.5);
   }
   // rows of the halo tile (global row r at tile row r - I0 + 2) the upwind
   // differences use, with the reference's clamps ih = min(i+1, imax),
@@ -889,21 +902,21 @@ __global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(sizeof(R) == sizeof
         x[q] = mv[q] ? y : T(0);  // zero outside the flux points
       }
       st_vec<T, V>(&zp[wp][V * lane], x);
-      if (wp == NW - 1) {
-        T xa[V], xc[V];
-        ld_vec<T, V>(xa, &wt[NW + 1][OFF + V * lane]);
-        ld_vec<T, V>(xc, &wt[NW + 2][OFF + V * lane]);
-        ld_vec<T, V>(wA, &wt[eA][OFF + V * lane]);
-        ld_vec<T, V>(wB, &wt[eB][OFF + V * lane]);
-        ld_vec<T, V>(wC, &wt[eC][OFF + V * lane]);
+      if (eWarp) {
+        T xa[VE], xc[VE], eA_[VE], eB_[VE], eC_[VE], xe[VE];
+        ld_vec<T, VE>(xa, &wt[NW + 1][OFF + ec0]);
+        ld_vec<T, VE>(xc, &wt[NW + 2][OFF + ec0]);
+        ld_vec<T, VE>(eA_, &wt[eA][OFF + ec0]);
+        ld_vec<T, VE>(eB_, &wt[eB][OFF + ec0]);
+        ld_vec<T, VE>(eC_, &wt[eC][OFF + ec0]);
 #pragma unroll
-        for (int q = 0; q < V; ++q) {
+        for (int q = 0; q < VE; ++q) {
           const bool up = upe[q];
           const T y = waf_flux_h<T>(vve[q], up, zmye[q], z2e[q], xa[q], xc[q],
-                                    (up ? xa[q] : wB[q]) - (up ? wA[q] : wC[q]));
-          x[q] = me[q] ? y : T(0);
+                                    (up ? xa[q] : eB_[q]) - (up ? eA_[q] : eC_[q]));
+          xe[q] = me[q] ? y : T(0);
         }
-        st_vec<T, V>(&zp[NW][V * lane], x);
+        st_vec<T, VE>(&zp[NW][ec0], xe);
       }
     }
     if (__syncthreads_or(!landed)) {
