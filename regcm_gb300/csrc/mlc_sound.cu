@@ -586,7 +586,7 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
         F2 zw = df_add_f(bal, wold);
         zw = df_add_f(zw, rdrcv * zr * (pm * zf_m - pk * zfk));
         const F2 den = df_add(two_sum(1.f + zd, zu), df_mul_f(F2{-wkp1d.hi, -wkp1d.lo}, zd));
-        const F2 zrapp = df_div(F2{1.f, 0.f}, den);
+        const F2 zrapp = df_recip(den);  // den >= 1: the pivot of a diagonally dominant system
         wnextd = df_mul(zrapp, df_add(zw, df_mul_f(wnextd, zd)));
         wkp1d = df_mul_f(zrapp, zu);
         w[o] = wnextd.hi;
