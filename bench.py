@@ -35,6 +35,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import resource
 import os
 import statistics
 import subprocess
@@ -672,7 +673,7 @@ def run_serving(args, rank, world):
                             (lambda r=r: cs.config4_request(r, precision=prec)[0]))
                     for r in range(nreq)]
             out[lam] = serve_stream(reqs, params, budget, capacity=args.capacity,
-                                    workers=workers, prefetch=2 * workers)
+                                    workers=workers, prefetch=min(16, 2 * workers))
         # the same stream's first `wall_requests` requests on the wall clock:
         # payloads built before the stream starts (the client's preparation is
         # not in the latency), arrivals in real time
@@ -694,7 +695,7 @@ def run_serving(args, rank, world):
         base_reqs = [Request(r, float(arr[r]), steps[r], None) for r in range(nreq)]
         one = serve_one_at_a_time(
             base_reqs, lambda r: (lambda rid=r.rid: cs.config4_request(rid)[0]),
-            workers=workers, prefetch=2 * workers)
+            workers=workers, prefetch=min(16, 2 * workers))
     if rank != 0:
         return
     # the FP64 queue's latencies at every rate from the measured service times
@@ -726,6 +727,7 @@ def run_serving(args, rank, world):
                                      "per_rate": {str(l): v for l, v in base.items()}},
         "ratio_to_plain_fp64": {str(l): out[l]["value"] / base[l]["value"] for l in rates},
         "clocks": clk.summary(),
+        "host_peak_rss_gb": resource.getrusage(resource.RUSAGE_SELF).ru_maxrss / 1e6,
     }
     print(json.dumps(line), flush=True)
 

@@ -334,7 +334,9 @@ class MolochPool:
         except Exception:
             self.lib.mlc_pool_remove(self._ctx, slot.value)
             raise
-        self.cases[slot.value] = case
+        # the uploads are synchronous: the pool keeps the member's extents,
+        # not its host arrays
+        self.cases[slot.value] = case.dims
         self._keep[slot.value] = keep
         return slot.value
 

@@ -24,6 +24,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import abi
+from .case import Case
 from .moloch import MolochPool, domain_from_case
 
 
@@ -39,6 +40,8 @@ class Request:
     t_admit: float = 0.0
     t_done: float = 0.0
     result: dict = field(default_factory=dict)
+    points: int = 0           # grid points of the request's domain (kept after its payload is released)
+    ps_like: object = None    # the surface-pressure array's shape and type, for the result
 
     @property
     def latency(self) -> float:
@@ -131,12 +134,14 @@ def serve_stream(reqs, params, budget_bytes: int, capacity: int = 256,
     while pending or queue or active:
         t = clk.now()
         while pending and pending[0].arrival <= t:
-            r = pending.popleft()
-            r.case = get_case(r)
-            queue.append(r)
-        # admission in arrival order while the head fits
+            queue.append(pending.popleft())
+        # admission in arrival order while the head fits; a request's payload
+        # is taken from the prefetcher only when it reaches the head, so the
+        # host holds the prefetched payloads and the head's, not the queue's
         while queue:
             r = queue[0]
+            if r.case is None:
+                r.case = get_case(r)
             slot = clk.run(pool.join, r.case)
             if slot is None:
                 if not active:
@@ -147,6 +152,10 @@ def serve_stream(reqs, params, budget_bytes: int, capacity: int = 256,
             queue.popleft()
             r.slot = slot
             r.t_admit = clk.now()
+            r.points = r.case.points
+            r.ps_like = r.case.state["ps"]
+            if not keep_results:
+                r.case = None  # the member's data is on the device now
             active[slot] = r
         if not active:
             if pending:
@@ -164,16 +173,17 @@ def serve_stream(reqs, params, budget_bytes: int, capacity: int = 256,
         for slot in list(active):
             r = active[slot]
             r.done_steps += chunk
-            gp_steps += r.case.points * chunk
+            gp_steps += r.points * chunk
             if r.done_steps >= r.steps:
-                out = r.case.empty_state() if keep_results else {"ps": r.case.empty_state()["ps"]}
-                clk.run(pool.download, slot, r.case.state_ptrs_of(out))
+                out = r.case.empty_state() if keep_results else {"ps": np.zeros_like(r.ps_like, order="F")}
+                clk.run(pool.download, slot, Case.state_ptrs_of(out))
                 clk.run(pool.leave, slot)
                 r.t_done = clk.now()
                 if keep_results:
                     r.result = out
                 del active[slot]
                 r.case = None  # release the host arrays
+                r.ps_like = None
     makespan = clk.now()
     ex.shutdown()
     pool.close()
