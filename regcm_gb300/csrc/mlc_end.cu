@@ -62,7 +62,7 @@ __device__ __forceinline__ R bdy_relax_to(R f, R x, R fext) {
 // them: everything phase 1 reads that phase 0 writes (qx, w at the level,
 // TKE one interface up, written by the same level's phase 0) lies in the
 // block's own level.
-constexpr int kRingThreads = 256;
+constexpr int kRingThreads = 1024;
 template <class R>
 __global__ void __launch_bounds__(kRingThreads) k_bdy_ring(const Dom<R> *__restrict__ doms, int uvoff,
                                                            int advoff) {
