@@ -378,6 +378,18 @@ __device__ __forceinline__ T vupdate_f(T pk, T fb, T fa, T dv, T zu, T zd) {
   return __fma_rn(dv, pk, __fma_rn(fa, zd, __fma_rn(-fb, zu, pk)));
 }
 
+// Blocks of 256 threads an SM the vertical WAF is compiled for, FP64 and FP32
+// (0: no bound, the compiler's own register choice).
+#ifndef MLC_VERT_MINB_D
+#define MLC_VERT_MINB_D 0
+#endif
+#ifndef MLC_VERT_MINB_F
+#define MLC_VERT_MINB_F 5
+#endif
+template <class T>
+constexpr int vert_min_blocks() {
+  return sizeof(T) == sizeof(double) ? (MLC_VERT_MINB_D > 0 ? MLC_VERT_MINB_D : 1) : MLC_VERT_MINB_F;
+}
 // Levels an FP32 column loads ahead of the one it computes (1 or 2; two
 // measured no faster on the moist 512x512x41 step, 0.256 ms a step both).
 #ifndef MLC_VPF_F
@@ -387,7 +399,8 @@ __device__ __forceinline__ T vupdate_f(T pk, T fb, T fa, T dv, T zu, T zd) {
 // blocks reading one column's s and metric run together), y = row tiles,
 // z = member; block (vert_x, vert_y) columns along (j, i)
 template <class R, class T>
-__global__ void k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set, int advoff,
+__global__ void __launch_bounds__(256, vert_min_blocks<T>())
+    k_adv_vertical(const Dom<R> *__restrict__ doms, int nf, int set, int advoff,
                                const WorkItem *__restrict__ wl) {
   constexpr int kVpf = sizeof(T) == sizeof(float) ? MLC_VPF_F : 1;  // levels loaded ahead
   const WorkItem wi = wl ? wl[blockIdx.x]
