@@ -367,7 +367,10 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
     s[kz * PS + ij_off] = 0.0;
   }
 }
-constexpr int kSvStages = 4;   // levels in flight ahead of the one being solved
+#ifndef MLC_SV_STAGES
+#define MLC_SV_STAGES 4
+#endif
+constexpr int kSvStages = MLC_SV_STAGES;  // levels in flight ahead of the one being solved
 constexpr int kSvW = 128;            // columns of a block (one row segment)
 constexpr int kSvZW = kSvW + 8;      // raw divergence rows with a 4-column halo each side
 constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
