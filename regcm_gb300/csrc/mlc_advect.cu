@@ -179,6 +179,33 @@ __device__ __forceinline__ double waf_sel(double den, double num, bool &dbl) {
   dbl = true;
   return den;
 }
+// a - a for the limiter's region tests: +0 for a finite a, else a NaN (every
+// NaN takes the same region), formed on the integer pipe in FP64
+template <class T>
+__device__ __forceinline__ T self_diff(T a) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    const long long b = __double_as_longlong(a);
+    const long long e = 0x7ff0000000000000LL;
+    return (b & e) == e ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
+  } else {
+    return a - a;
+  }
+}
+// The same with den = c - a and the upwind value x given (a caller that
+// streams the differences of neighbouring interfaces forms each once: an
+// interface's den is the num of the interfaces on either side)
+template <class T>
+__device__ __forceinline__ T waf_flux_d(T vel, bool up, T zmih, T zmi, T x, T den, T num) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    bool dbl;
+    const double sel = waf_sel(den, num, dbl);
+    return __dmul_rn(vel, __fma_rn(dbl ? -zmi : -zmih, sel, x));
+  } else {
+    (void)zmi;
+    const T B = waf_b<T>(den, num);
+    return vel * fmaf(-zmih, B, x);
+  }
+}
 template <class T>
 __device__ __forceinline__ T waf_flux_h(T vel, bool up, T zmih, T zmi, T a, T c, T num) {
   const T den = c - a;
@@ -384,7 +411,7 @@ __device__ __forceinline__ T vupdate_f(T pk, T fb, T fa, T dv, T zu, T zd) {
 #define MLC_VERT_MINB_D 0
 #endif
 #ifndef MLC_VERT_MINB_F
-#define MLC_VERT_MINB_F 5
+#define MLC_VERT_MINB_F 4
 #endif
 template <class T>
 constexpr int vert_min_blocks() {
@@ -439,6 +466,10 @@ __global__ void __launch_bounds__(256, vert_min_blocks<T>())
   T sm2 = T(0), sm1 = T(0), sk = T(sp[0]);
   T zum2 = T(0), zdm2 = T(0), zum1 = T(0), zdm1 = T(0);
   T f1k = T(0), f2m = T(0);
+  // differences c(k) - c(k+1) of the pass-1 input at interfaces k-1, k (d1p,
+  // d1c) and of the pass-2 input at m-1, m (d2p, d2c): an interface's den is
+  // the num of its neighbours, so each difference is formed once
+  T d1p = T(0), d1c = T(0), d2p = T(0), d2c = T(0);
   // FP64 member: the update's divergence factor, precomputed per level
   constexpr bool kPre = sizeof(R) == sizeof(double) && sizeof(T) == sizeof(double);
   const double *__restrict__ dvp = kPre ? D.vdiv + ij : nullptr;
@@ -501,11 +532,11 @@ __global__ void __launch_bounds__(256, vert_min_blocks<T>())
       if (I || k + 3 <= kz) n_c = src[o + 3 * PS];
     }
     T f1kp;
+    const T d1n = c0p1 - c0p2;  // the next interface's den, this one's upwind num
     if constexpr (kPre) {
       if (I) {
         const bool up = nonneg(tk.zamu);
-        f1kp = waf_flux_h<double>(skp1, up, tk.zmih, tk.zmi, c0p1, c0k,
-                                  (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
+        f1kp = waf_flux_d<double>(skp1, up, tk.zmih, tk.zmi, up ? c0p1 : c0k, d1c, up ? d1n : d1p);
       } else {
         f1kp = k <= kz - 1 ? vflux_p(skp1, tk, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
       }
@@ -513,21 +544,20 @@ __global__ void __launch_bounds__(256, vert_min_blocks<T>())
       const T zamu = skp1 * dtrdz;
       const bool up = nonneg(zamu);
       const T zmi = waf_zmi<T>(zamu, up);
-      f1kp = waf_flux_h<T>(skp1, up, zmi * T(0.5), zmi, c0p1, c0k,
-                           (up ? c0p1 : c0m1) - (up ? c0p2 : c0k));
+      f1kp = waf_flux_d<T>(skp1, up, zmi * T(0.5), zmi, up ? c0p1 : c0k, d1c, up ? d1n : d1p);
     } else {
       f1kp = k <= kz - 1 ? vflux<T>(dtrdz, skp1, c0m1, c0k, c0p1, c0p2, k, kz) : T(0);
     }
     T c1k;
     if constexpr (kPre) c1k = vupdate_f<T>(c0k, f1k, f1kp, dvk, zuk, zdk);
     else c1k = vupdate<T>(c0k, f1k, f1kp, sk, skp1, zuk, zdk);
+    const T d2n = c1m1 - c1k;
     if (I || k >= 3) {  // pass 2 at level m = k-2
       T f2n;
       if constexpr (kPre) {
         if (I) {
           const bool up = nonneg(tkm2.zamu);
-          f2n = waf_flux_h<double>(sm1, up, tkm2.zmih, tkm2.zmi, c1m1, c1m2,
-                                   (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
+          f2n = waf_flux_d<double>(sm1, up, tkm2.zmih, tkm2.zmi, up ? c1m1 : c1m2, d2c, up ? d2n : d2p);
         } else {
           f2n = vflux_p(sm1, tkm2, c1m3, c1m2, c1m1, c1k, k - 2, kz);
         }
@@ -535,8 +565,7 @@ __global__ void __launch_bounds__(256, vert_min_blocks<T>())
         const T zamu = sm1 * dtrdz;
         const bool up = nonneg(zamu);
         const T zmi = waf_zmi<T>(zamu, up);
-        f2n = waf_flux_h<T>(sm1, up, zmi * T(0.5), zmi, c1m1, c1m2,
-                            (up ? c1m1 : c1m3) - (up ? c1k : c1m2));
+        f2n = waf_flux_d<T>(sm1, up, zmi * T(0.5), zmi, up ? c1m1 : c1m2, d2c, up ? d2n : d2p);
       } else {
         f2n = vflux<T>(dtrdz, sm1, c1m3, c1m2, c1m1, c1k, k - 2, kz);
       }
@@ -546,6 +575,7 @@ __global__ void __launch_bounds__(256, vert_min_blocks<T>())
     }
     c0m1 = c0k; c0k = c0p1; c0p1 = c0p2;
     c1m3 = c1m2; c1m2 = c1m1; c1m1 = c1k;
+    d1p = d1c; d1c = d1n; d2p = d2c; d2c = d2n;
     sm2 = sm1; sm1 = sk; sk = skp1;
     zum2 = zum1; zdm2 = zdm1; zum1 = zuk; zdm1 = zdk;
     dvm2 = dvm1; dvm1 = dvk;
@@ -958,24 +988,29 @@ __global__ void __launch_bounds__(32 * NW, waf_min_blocks<R>(sizeof(R) == sizeof
     // zonal fluxes zpbw(j,i): j in jci1..jce2, i in ici; p0 at range
     // columns c-2 .. c+1 (the lane's own, two from the lane to the west, one
     // from the lane to the east)
-    T pw2, pw1, pe1;
-    pw2 = __shfl_up_sync(0xffffffffu, V >= 2 ? p0[V >= 2 ? V - 2 : 0] : p0[0], V >= 2 ? 1 : 2);
-    pw1 = __shfl_up_sync(0xffffffffu, p0[V - 1], 1);
-    pe1 = __shfl_down_sync(0xffffffffu, p0[0], 1);
-    auto p0at = [&](int q) -> T {  // p0 of lane column q, q in -2 .. V
-      return q == -2 ? pw2 : q == -1 ? pw1 : q == V ? pe1 : p0[q < 0 ? 0 : q >= V ? V - 1 : q];
+    T pw1 = __shfl_up_sync(0xffffffffu, p0[V - 1], 1);
+    auto p0at = [&](int q) -> T {  // p0 of lane column q, q in -1 .. V-1
+      return q < 0 ? pw1 : p0[q];
     };
+    // differences p0(c) - p0(c-1) at the lane's columns, and those of the
+    // columns either side from the neighbouring lanes: a column's den is the
+    // num of its neighbours (upwind the one to the west, downwind the east)
+    T dq[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) dq[q] = p0at(q) - p0at(q - 1);
+    const T dw = __shfl_up_sync(0xffffffffu, dq[V - 1], 1);
+    const T de = __shfl_down_sync(0xffffffffu, dq[0], 1);
+    auto dat = [&](int q) -> T { return q < 0 ? dw : q >= V ? de : dq[q]; };
     T zx[V];
 #pragma unroll
     for (int q = 0; q < V; ++q) {
       const int j = jq[q];
       const bool up = upx[q];
       const T a = p0at(q - 1), cq = p0at(q);
-      // jhm1 = max(j-2, jmin) upwind; jh = min(j+1, jmax) downwind
-      // upwind a - p0(jhm1), downwind p0(jh) - p0(jh-1): one subtraction of selected operands
-      const T n1 = up ? a : (j == jx - 1 ? cq : p0at(q + 1));
-      const T n2 = up ? (j == 2 ? a : p0at(q - 2)) : (j == jx - 1 ? a : cq);
-      const T x = waf_flux_h<T>(uu[q], up, zmx[q], z2x[q], a, cq, n1 - n2);
+      // jhm1 = max(j-2, jmin) upwind; jh = min(j+1, jmax) downwind:
+      // upwind a - p0(jhm1), which is a - a at j = 2; downwind p0(jh) - p0(jh-1)
+      const T num = up ? (j == 2 ? self_diff<T>(a) : dat(q - 1)) : (j == jx - 1 ? dq[q] : dat(q + 1));
+      const T x = waf_flux_d<T>(uu[q], up, zmx[q], z2x[q], up ? a : cq, dq[q], num);
       zx[q] = xv[q] ? x : T(0);
     }
     T zxe[V];
