@@ -674,13 +674,14 @@ __device__ __forceinline__ void next_col(T (&e)[V], const T (&x)[V]) {
 // reference's, operand for operand.
 // Resident warps an SM the WAF tile kernels are compiled for; the register
 // budget follows (65536 / (32 * warps) a thread).  Measured on the moist
-// 512x512x41 step: FP32 horizontal WAF at 32 warps (64 registers) 0.46 ms a
-// step against 0.72 at 16 warps (90 registers); the increment form at 32
+// 512x512x41 step: FP32 horizontal WAF at 40 warps (48 registers, 12 bytes
+// spilled) 0.455 ms a step, at 32 (64 registers) 0.464, at 16 warps (90
+// registers) 0.72; the increment form at 32
 // warps (64 registers, 32 bytes spilled) 0.27 against 0.29 at 24 and 0.37 at
 // 20.  FP64 at 16 warps (128 registers): the FP64 pipe is the bound, but 8
 // warps an SM leave it idle (6.98 against 7.83 ms).
 #ifndef MLC_HWAF_WARPS
-#define MLC_HWAF_WARPS 32
+#define MLC_HWAF_WARPS 40
 #endif
 #ifndef MLC_HWAF_WARPS_D
 #define MLC_HWAF_WARPS_D 16
