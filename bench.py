@@ -161,13 +161,13 @@ def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None
 # the line prints them with that label and the kernel build they were taken
 # on.  Keyed by (kernel group, precision, advected fields).
 CAPTURED_TRAFFIC_PER_POINT = {
-    ("adv_horizontal", "fp64", 10): (733.6e6 / (256 * 256 * 41), "41cf599"),
-    ("sound_solve", "mixed", 10): (204.0e6 / (256 * 256 * 41), "a05c4c8"),
+    ("adv_horizontal", "fp64", 10): (732.9e6 / (256 * 256 * 41), "b298cef"),
+    ("sound_solve", "mixed", 10): (242.9e6 / (256 * 256 * 41), "b298cef"),
 }
 # What limits the dominant kernel besides its roofline, from the same captures.
 CAPTURED_LIMITER = {
     ("adv_horizontal", "fp64"): {
-        "pipe": "fp64", "active": 0.85, "counter": "sm__inst_executed_pipe_fp64"},
+        "pipe": "fp64", "active": 0.84, "counter": "sm__inst_executed_pipe_fp64"},
     ("sound_solve", "mixed"): {
         "stall": "block barrier (one a level, freeing a copy stage)", "warps_active": 0.21},
 }
