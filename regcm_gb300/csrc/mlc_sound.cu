@@ -371,9 +371,17 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
 #define MLC_SV_STAGES 4
 #endif
 constexpr int kSvStages = MLC_SV_STAGES;  // levels in flight ahead of the one being solved
+// Warp-specialised mixed solve: a fifth warp issues the copies and the four
+// column warps release each stage through an mbarrier instead of a block
+// barrier a level (1), or one thread issues after a block barrier (0).
+#ifndef MLC_SOLVE_WS
+#define MLC_SOLVE_WS 0
+#endif
+constexpr bool kSolveWS = MLC_SOLVE_WS != 0;
 constexpr int kSvW = 128;            // columns of a block (one row segment)
 constexpr int kSvZW = kSvW + 8;      // raw divergence rows with a 4-column halo each side
 constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
+constexpr int kSvThreads = kSvW + (kSolveWS ? 32 : 0);
 
 // The solve of a mixed member (same equations as k_sound_solve), in FP32
 // only, one thread per column.  Where rounding is amplified the values are
@@ -403,22 +411,28 @@ constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
 // 0.73 ms of solves a step against 0.95 for the same thread-per-column
 // kernel with register prefetch of one level.)
 template <class R, bool DFR>
-__global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last,
+__global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last,
     const WorkItem *__restrict__ wl) {
   constexpr int NS = kSvStages;
+  constexpr bool WS = kSolveWS;
+  constexpr unsigned kCons = kSvW / 32;  // consumer warps
   extern __shared__ __align__(16) float sv_smem[];
   __shared__ __align__(8) uint64_t mbar[NS];
+  __shared__ __align__(8) uint64_t mbar_e[WS ? NS : 1];  // stage released by every consumer warp
+  __shared__ int abort_s;
   const WorkItem wi = wl ? wl[blockIdx.x]
                           : WorkItem{(int16_t)blockIdx.z, (int16_t)blockIdx.x, (int16_t)blockIdx.y, 0};
   const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int t = (int)threadIdx.x;
+  const int lane = t & 31;
+  const bool producer = WS && t >= kSvW;    // the copy-issuing warp (warp-specialised form)
   const int x0 = (int)wi.a * kSvW;          // first column (0-based j-1) of the block
   const int i = (int)wi.b + 2;
   if (x0 + 1 > g.jx - 2 || i > g.iy - 2) return;  // uniform over the block
   const int j = x0 + t + 1;
-  const bool act = j >= 2 && j <= g.jx - 2;
+  const bool act = !producer && j >= 2 && j <= g.jx - 2;
   const int kz = g.kz;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
@@ -520,11 +534,51 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
   };
   if (t == 0) {
     for (int q = 0; q < NS; ++q) mbar_init(&mbar[q], 1);
+    if constexpr (WS)
+      for (int q = 0; q < NS; ++q) mbar_init(&mbar_e[q], kCons);
+    abort_s = 0;
     fence_mbar_init();
   }
   __syncthreads();
-  if (t == 0)
-    for (int u = 0; u < NS && u < nd; ++u) issue_down(u, u);
+  // Warp-specialised form: the producer warp's lane 0 issues every unit's
+  // copies, waiting (bounded) for the consumer warps to release the stage
+  // the unit reuses; the consumer warps wait only for their data and never
+  // for each other.  A wait that runs out sets the fault flag and abort_s;
+  // both roles then skip their remaining waits, and the producer lets the
+  // copies still in flight land before the block leaves.
+  int issued = 0;  // units the producer has issued (global numbering: down, then up)
+  auto produce = [&](int gfirst, int gend, bool upp) {
+    for (int gu = gfirst; gu < gend; ++gu) {
+      const int b = gu % NS;
+      int okp = 1;
+      if (lane == 0) {
+        okp = *(volatile int *)&abort_s == 0;
+        if (okp && gu >= NS) okp = mbar_wait_bounded(&mbar_e[b], (unsigned)(((gu / NS) - 1) & 1));
+        if (okp) {
+          if (upp) issue_up(gu - nd, b);
+          else issue_down(gu, b);
+          issued = gu + 1;
+        } else if (*(volatile int *)&abort_s == 0) {
+          abort_s = 1;
+          atomicOr(&D.clk->fault, 1);
+        }
+      }
+      if (!__shfl_sync(0xffffffffu, okp, 0)) return;
+    }
+  };
+  // a consumer warp's bounded wait for unit gu: false once any wait ran out
+  auto consume_wait = [&](int gu) {
+    bool okc = *(volatile int *)&abort_s == 0 && mbar_wait_bounded(&mbar[gu % NS], (unsigned)((gu / NS) & 1));
+    okc = __all_sync(0xffffffffu, okc);
+    if (!okc && lane == 0 && atomicExch(&abort_s, 1) == 0) atomicOr(&D.clk->fault, 1);
+    return okc;
+  };
+  auto release = [&](int gu) {
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&mbar_e[gu % NS]);
+  };
+  if (WS ? (producer && lane == 0) : t == 0)
+    for (int u = 0; u < NS && u < nd; ++u) { issue_down(u, u); issued = u + 1; }
 
   struct LvA {
     float z, lap, s, fmz;
@@ -553,10 +607,17 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
   F2 wnextd{wnext, 0.f}, wkp1d{0.f, 0.f};
   bool ok = true;
   int synced = 0;  // first unit read since the last block barrier
-  for (int u = 0; u < nd; ++u) {
+  if (producer) produce(NS, nd, false);
+  for (int u = 0; u < nd && !producer; ++u) {
     const int k = kz - u, m = k - 1;
     const int b = u % NS;
-    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((u / NS) & 1));
+    bool landed;
+    if constexpr (WS) {
+      landed = consume_wait(u);
+      if (!landed) break;
+    } else {
+      landed = mbar_wait_bounded(&mbar[b], (unsigned)((u / NS) & 1));
+    }
     const float *st = stage(b);
     if (act) {
       const int o = (k - 1) * PS + ij_off;
@@ -608,6 +669,10 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
       zfk = zf_m;
       ak = am;
     }
+    if constexpr (WS) {
+      release(u);
+      continue;
+    }
     ok = ok && landed;
     if ((u + 1) % kSolveSync == 0 || u + 1 == nd) {
       if (__syncthreads_or(!ok)) {
@@ -626,8 +691,18 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
   fence_proxy_async_global();
   __syncthreads();
   const int nu = kz;  // up units: m = 2 .. kz+1
-  if (t == 0)
+  if constexpr (WS) {
+    if (abort_s) {
+      // let the copies in flight land (at most NS, the last issued) and leave
+      if (producer && lane == 0)
+        for (int q = max(0, issued - NS); q < issued; ++q)
+          mbar_wait_bounded(&mbar[q % NS], (unsigned)((q / NS) & 1));
+      return;
+    }
+    if (producer) produce(nd, nd + nu, true);
+  } else if (t == 0) {
     for (int v = 0; v < NS && v < nu; ++v) issue_up(v, (nd + v) % NS);
+  }
   auto exner = [&](int m, float wm, float dw, F2 pk, float zf, float fz, float sm, float fzf) {
     const int o = (m - 1) * PS + ij_off;
     const float inc = rdrcv * (zf + (dtrdz * fz * dw));
@@ -641,10 +716,16 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
   F2 wprevd{wprev, 0.f};
   ok = true;
   synced = 0;
-  for (int v = 0; v < nu; ++v) {
+  for (int v = 0; v < nu && !producer; ++v) {
     const int k = v + 2, gu = nd + v;
     const int b = gu % NS;
-    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((gu / NS) & 1));
+    bool landed;
+    if constexpr (WS) {
+      landed = consume_wait(gu);
+      if (!landed) break;
+    } else {
+      landed = mbar_wait_bounded(&mbar[b], (unsigned)((gu / NS) & 1));
+    }
     if (act) {
       const float *f0 = stage(b) + 3 * kSvZW + t;
       const float wel = f0[0];
@@ -672,6 +753,10 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
         }
       }
     }
+    if constexpr (WS) {
+      release(gu);
+      continue;
+    }
     ok = ok && landed;
     if ((v + 1) % kSolveSync == 0 || v + 1 == nu) {
       if (__syncthreads_or(!ok)) {
@@ -683,6 +768,12 @@ __global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict
           if (r + NS < nu) issue_up(r + NS, (nd + r) % NS);
       synced = v + 1;
     }
+  }
+  if constexpr (WS) {
+    if (producer && lane == 0 && *(volatile int *)&abort_s)
+      for (int q = max(0, issued - NS); q < issued; ++q)
+        mbar_wait_bounded(&mbar[q % NS], (unsigned)((q / NS) & 1));
+    if (*(volatile int *)&abort_s) return;
   }
   if (last && act) {
     s[ij_off] = 0.f;
@@ -1159,9 +1250,9 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
                                  : dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem);
     const size_t smem = (size_t)kSvStages * kSvStage * sizeof(float);
     if (L.solve_df)
-      k_solve_mixed<R, true><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
+      k_solve_mixed<R, true><<<grid, kSvThreads, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
     else
-      k_solve_mixed<R, false><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
+      k_solve_mixed<R, false><<<grid, kSvThreads, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
   } else {
     const int tj = (L.jx - 1 + kDvW - 1) / kDvW;
     const dim3 grid = L.wl_solve ? dim3((unsigned)L.n_solve, 1, 1)
