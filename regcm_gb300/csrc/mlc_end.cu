@@ -251,28 +251,63 @@ __global__ void k_end_relax(const Dom<R> *__restrict__ doms, int uvoff, int advo
     return bdy_relax_to<R>(f, xf, fext);
   };
   const R xfn0 = pick<R>(trtau * c.dtsec, float(trtau * c.dtsec));
+  // The temperature part's inputs of a level, loaded one level ahead: the
+  // next level's loads are issued before this level's stores (which would
+  // otherwise hold them back, the arrays being reachable through one
+  // descriptor), so each thread keeps two levels' loads in flight.
+  const int ipp = c.ipptls;
+  const int nq = ipp > 1 ? 5 : ipp == 1 ? 2 : 1;
+  struct TvIn {
+    R th, pa, q[5];
+    float thl, pal;  // a mixed member's low parts of theta_v and Exner
+  };
+  auto load_in = [&](size_t o, TvIn &x) {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      const DF th(st.tetav, F), pa(st.pai, F);
+      const F2 a = th.ld(o), b = pa.ld(o);
+      x.th = a.hi; x.thl = a.lo; x.pa = b.hi; x.pal = b.lo;
+    } else {
+      x.th = R(st.tetav[o]); x.pa = R(st.pai[o]); x.thl = x.pal = 0.f;
+    }
+#pragma unroll
+    for (int n = 0; n < 5; ++n) x.q[n] = n < nq ? st.qx[o + (size_t)n * F] : R(0);
+  };
+  // qfactor of the loaded species, in its association
+  auto qf_of = [&](const TvIn &x) -> R {
+    if (ipp > 1) return R(1) + R(kEp1) * x.q[0] - x.q[1] - x.q[2] - x.q[3] - x.q[4];
+    if (ipp == 1) return R(1) + R(kEp1) * x.q[0] - x.q[1];
+    return R(1) + R(kEp1) * x.q[0];
+  };
+  TvIn cur, nxt;
+  load_in(ij + (size_t)(k0 - 1) * PS, cur);
 #pragma unroll
   for (int k = k0; k < k0 + kPtLevels && k <= g.kz; ++k) {
     const size_t o = ij + (size_t)(k - 1) * PS;
+    if (k + 1 < k0 + kPtLevels && k + 1 <= g.kz) load_in(o + PS, nxt);
     // ---- tvirt and t (every cross point; t only inside the ring) ----
-    const R qf = qfactor(st.qx, o, F, c.ipptls);
     F2 tdf{0.f, 0.f};  // a mixed member's double-float t
     R tr = R(0);       // an FP64 member's t
     if constexpr (sizeof(R) == sizeof(float)) {
       // t as a double-float through the step end: hi in t, lo in wz[1] (the
       // scratch is free until the next advection); status_update rebuilds
       // theta_v = t*qf/pai from it, so t's FP32 rounding never reaches theta_v
-      const DF th(st.tetav, F), pa(st.pai, F);
-      const F2 tv = df_mul(th.ld(o), pa.ld(o));
+      const F2 tv = df_mul(F2{cur.th, cur.thl}, F2{cur.pa, cur.pal});
       st.tvirt[o] = df_f(tv);
-      if (inner) tdf = df_div(tv, qfactor_df(st.qx, o, F, c.ipptls));
-      else if (!c.apply_bdy) D.wz[1][o] = 0.f;  // (with the boundary on, the ring wrote it)
+      if (inner) {
+        float d;  // qfactor_df of the loaded species
+        if (ipp > 1) d = float(kEp1) * cur.q[0] - cur.q[1] - cur.q[2] - cur.q[3] - cur.q[4];
+        else if (ipp == 1) d = float(kEp1) * cur.q[0] - cur.q[1];
+        else d = float(kEp1) * cur.q[0];
+        tdf = df_div(tv, fast_two_sum(1.f, d));
+      } else if (!c.apply_bdy) {
+        D.wz[1][o] = 0.f;  // (with the boundary on, the ring wrote it)
+      }
     } else {
-      const R tv = R(st.tetav[o] * st.pai[o]);
+      const R tv = R(cur.th * cur.pa);
       st.tvirt[o] = tv;
-      if (inner) tr = tv / qf;
+      if (inner) tr = tv / qf_of(cur);
     }
-    (void)qf;
+    cur = nxt;
     // ---- motopnudge and morelax ----
     if (k == 2 && cr && c.top_nudge) {
       const size_t o2 = ij + PS;  // level 2 (w sponge, before the level's relaxation)
