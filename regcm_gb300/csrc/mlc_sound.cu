@@ -373,7 +373,10 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
 constexpr int kSvStages = MLC_SV_STAGES;  // levels in flight ahead of the one being solved
 // Warp-specialised mixed solve: a fifth warp issues the copies and the four
 // column warps release each stage through an mbarrier instead of a block
-// barrier a level (1), or one thread issues after a block barrier (0).
+// barrier a level (1), or one thread issues after a block barrier (0).  Both
+// pass the same tests; on the moist 512x512x41 step the warp-specialised form
+// measured 0.857 ms of solves a step against 0.848 (the solve is bound by its
+// issue rate, not by the barrier), so the default is 0.
 #ifndef MLC_SOLVE_WS
 #define MLC_SOLVE_WS 0
 #endif
