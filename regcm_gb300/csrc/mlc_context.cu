@@ -181,8 +181,10 @@ void carve_dom(Carver &cv, Dom<R> &D, const Geom &g, const mlc_dims &d, const ml
     s.mo_du = cv.take<double>(F); s.mo_dv = cv.take<double>(F);
     s.mo_gu = cv.take<double>(F); s.mo_gv = cv.take<double>(F);
     s.mo_cu = cv.take<double>(P2); s.mo_cv = cv.take<double>(P2);
+    s.sv_a = cv.take<double>(F); s.sv_b = cv.take<double>(F); s.sv_c = cv.take<double>(F);
   } else {
     s.dv_cu = s.dv_cv = s.dv_cf = s.mo_du = s.mo_dv = s.mo_gu = s.mo_gv = s.mo_cu = s.mo_cv = nullptr;
+    s.sv_a = s.sv_b = s.sv_c = nullptr;
   }
   if (f64) {
     s.gzitak_r = reinterpret_cast<const R *>(s.gzitak);
@@ -1182,6 +1184,28 @@ int bind_static_impl(mlc_ctx *x, Member &mb, const mlc_static_ptrs *s) {
     MLC_CHK(put3<double>(x, g, fv.data(), W(a.mo_dv), jx - 1, iy, kz, 0));
     MLC_CHK(put3<double>(x, g, cu.data(), W(a.mo_cu), jx, iy - 1, 1, 0));
     MLC_CHK(put3<double>(x, g, cvv.data(), W(a.mo_cv), jx - 1, iy, 1, 0));
+    MLC_TRY(cudaStreamSynchronize(x->stream));
+    // the solve's factors, in the kernel's operand order: (bw*dtrdz)*fmz,
+    // zcs2*fmz and dtrdz*fmz (dtrdz = dtsound*rdzita, zcs2 = dtrdz^2*R/cv)
+    const double sdtrdz = c.dtsound * c.rdzita;
+    const double zcs2 = (sdtrdz * sdtrdz) * kRdrcv;
+    const int nsp = p.nspgx;
+    std::vector<double> fa(nc * kz), fb(nc * kz);
+    for (int k = 0; k < kz; ++k)
+      for (int i = 0; i < iy - 1; ++i)
+        for (int j = 0; j < jx - 1; ++j) {
+          const size_t e2 = (size_t)j + (size_t)i * jx;
+          const size_t e3 = (size_t)j + (size_t)i * (jx - 1) + nc * k;
+          const int ib = s->ibnd_cr[e2];
+          const double bw = ib > 0 ? 1.0 - s->hefc[(size_t)(ib - 1) + (size_t)k * nsp] : 1.0;
+          fa[e3] = (bw * sdtrdz) * s->fmz[e3];
+          fb[e3] = zcs2 * s->fmz[e3];
+        }
+    MLC_CHK(put3<double>(x, g, fa.data(), W(a.sv_a), jx - 1, iy - 1, kz, 0));
+    MLC_CHK(put3<double>(x, g, fb.data(), W(a.sv_b), jx - 1, iy - 1, kz, 0));
+    MLC_TRY(cudaStreamSynchronize(x->stream));
+    for (size_t e = 0; e < nc * kz; ++e) fa[e] = sdtrdz * s->fmz[e];
+    MLC_CHK(put3<double>(x, g, fa.data(), W(a.sv_c), jx - 1, iy - 1, kz, 0));
     MLC_TRY(cudaStreamSynchronize(x->stream));
   }
   if (p.mo_spectral_nudge) {

@@ -78,6 +78,10 @@ struct Stat {
   //              (rotated: dxrdt*xkdamp(k)), g*dts*hx*gzitakh(k) and
   //              g*dts*hy*gzitakh(k) (3-D), coru*dts and corv*dts (2-D)
   const double *dv_cu, *dv_cv, *dv_cf, *mo_du, *mo_dv, *mo_gu, *mo_gv, *mo_cu, *mo_cv;
+  //   sound_solve (3-D, cross points): (bw*dtrdz)*fmz with bw the relaxation
+  //              weight 1 - hefc of the point's zone (1 outside), zcs2*fmz
+  //              and dtrdz*fmz
+  const double *sv_a, *sv_b, *sv_c;
   // spectral nudging: sine bases bvx (km2 rows of jx) and bvy (lm2 rows of
   // iy), the level weights cnudge (kz)
   const R *bvx, *bvy, *cnudge;

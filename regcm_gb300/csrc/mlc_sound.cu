@@ -156,7 +156,14 @@ constexpr int kSolveSync = MLC_SOLVE_SYNC;
 constexpr int kDvStages = 3;
 constexpr int kDvW = 128;
 constexpr int kDvZW = kDvW + 4;                   // raw divergence row, 2-column halo each side
-constexpr int kDvStage = 3 * kDvZW + 7 * kDvW;   // doubles of one stage
+// The FP64 solve reads its metric products from bind time - (bw*dtrdz)*fmz,
+// zcs2*fmz, dtrdz*fmz, the same roundings as forming them per level - (1),
+// or forms them from fmz and the zone weight every level (0).
+#ifndef MLC_SOLVE_PRE
+#define MLC_SOLVE_PRE 1
+#endif
+constexpr bool kSolvePre = MLC_SOLVE_PRE != 0;
+constexpr int kDvStage = 3 * kDvZW + (kSolvePre ? 8 : 7) * kDvW;   // doubles of one stage
 template <class R>
 __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last,
     const WorkItem *__restrict__ wl) {
@@ -187,7 +194,11 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
   double *__restrict__ pai = D.pai[adv] + r0;
   const double *__restrict__ tetav = D.tetav[adv] + r0;
   double *__restrict__ tetavf = D.tetavf + r0;
-  const double *__restrict__ fmz = sa.fmz_d + r0;
+  // with the products from bind time, fmz's place (down pass, up pass) holds
+  // (bw*dtrdz)*fmz and dtrdz*fmz, and zcs2*fmz comes as an eighth plane
+  const double *__restrict__ fmz = (kSolvePre ? sa.sv_a : sa.fmz_d) + r0;
+  const double *__restrict__ fmz_up = (kSolvePre ? sa.sv_c : sa.fmz_d) + r0;
+  const double *__restrict__ fmzb = (kSolvePre ? sa.sv_b : sa.fmz_d) + r0;
   const double *__restrict__ fmzf = sa.fmzf_d + r0;
   double *__restrict__ zfs = D.wz[0] + r0;   // free during the acoustic loop
   double *__restrict__ mul = D.wz[1] + r0;
@@ -210,7 +221,7 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
     double *st = stage(b);
     uint64_t *bar = &mbar[b];
     fence_proxy_async();
-    mbar_expect_tx(bar, (filt ? 3u : 1u) * zb + 7u * wb);
+    mbar_expect_tx(bar, (filt ? 3u : 1u) * zb + (kSolvePre ? 8u : 7u) * wb);
     const int o = (m - 1) * PS, ob = m * PS;
     bulk_load(st, zraw + o + zs, zb, bar);
     if (filt) {
@@ -224,6 +235,7 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
     bulk_load(fld(st, 4), w + ob + x0, wb, bar);
     bulk_load(fld(st, 5), fmzf + ob + x0, wb, bar);
     bulk_load(fld(st, 6), tetavf + ob + x0, wb, bar);
+    if constexpr (kSolvePre) bulk_load(fld(st, 7), fmzb + o + x0, wb, bar);
   };
   // up unit v (m = v + 2): w(m), mul(m) (m <= kz); pai, zfs, fmz, s, fmzf at m-1
   auto issue_up = [&](int v, int b) {
@@ -237,7 +249,7 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
     if (m <= kz) bulk_load(fld(st, 1), mul + o + x0, wb, bar);
     bulk_load(fld(st, 2), pai + op + x0, wb, bar);
     bulk_load(fld(st, 3), zfs + op + x0, wb, bar);
-    bulk_load(fld(st, 4), fmz + op + x0, wb, bar);
+    bulk_load(fld(st, 4), fmz_up + op + x0, wb, bar);
     bulk_load(fld(st, 5), s + op + x0, wb, bar);
     bulk_load(fld(st, 6), fmzf + op + x0, wb, bar);
   };
@@ -255,19 +267,22 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
   if (t == 0)
     for (int u = 0; u < NS && u < nd; ++u) issue_down(u, u);
   // filtered divergence plus the vertical part of level m (:531-543, :627-630)
+  // fz: fmz, or (bw*dtrdz)*fmz from bind time
   auto zf_of = [&](int m, double z, double lap, double fz, double sm, double sm1) {
     if (filt) z = z + sa.xknu[m - 1] * lap;
+    if constexpr (kSolvePre) return z + fz * (sm - sm1);
     const double bw = relax_weight(sa.ibnd_cr, sa.hefc, c.nspgx, ij, m);
     return z + bw * dtrdz * fz * (sm - sm1);
   };
+  // fmz_k: fmz of level k, or zcs2*fmz from bind time
   double wnext = 0.0, wkp1 = 0.0, zfk = 0.0, pai_k = 0.0, tet_k = 0.0, fmz_k = 0.0, s_k = 0.0;
   if (act) {
     const int o = (kz - 1) * PS + ij_off;
     const double z = zraw[o];
     const double lap = filt ? (zraw[o - 1] + zraw[o + 1] + zraw[o - P] + zraw[o + P] - 4.0 * z) : 0.0;
     s_k = s[o];
-    fmz_k = fmz[o];
-    zfk = zf_of(kz, z, lap, fmz_k, s_k, s[kz * PS + ij_off]);
+    fmz_k = fmzb[o];
+    zfk = zf_of(kz, z, lap, fmz[o], s_k, s[kz * PS + ij_off]);
     pai_k = pai[o];
     tet_k = tetav[o];
     wnext = w[kz * PS + ij_off];  // w(kz+1) = -s(kz+1)
@@ -284,9 +299,10 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
       const double z = st[zc];
       const double lap = filt ? (st[zc - 1] + st[zc + 1] + st[kDvZW + zc] + st[2 * kDvZW + zc] - 4.0 * z) : 0.0;
       const double *f0 = st + 3 * kDvZW + t;
-      const double s_m = f0[0], fmz_m = f0[kDvW], pai_m = f0[2 * kDvW], tet_m = f0[3 * kDvW];
+      const double s_m = f0[0], fza_m = f0[kDvW], pai_m = f0[2 * kDvW], tet_m = f0[3 * kDvW];
       const double wold = f0[4 * kDvW], fmzf_k = f0[5 * kDvW], tvf0 = f0[6 * kDvW];
-      const double zf_m = zf_of(m, z, lap, fmz_m, s_m, s_k);
+      const double fmz_m = kSolvePre ? f0[7 * kDvW] : fza_m;
+      const double zf_m = zf_of(m, z, lap, fza_m, s_m, s_k);
       zfs[o] = zfk;
       const double tvf = tvf0 - wold * fmzf_k * dtrdz * (tet_m - tet_k);
       tetavf[o] = tvf;
@@ -294,8 +310,14 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
       double zwexpl = wold - zrom1w * dtrdz * (pai_m - pai_k) - kGrav * dts;
       zwexpl = zwexpl + kRdrcv * zrom1w * dtrdz * (pai_m * zf_m - pai_k * zfk);
       const double ff = sa.ffilt[k - 1];
-      const double zu = zcs2 * fmz_m * zrom1w * pai_m + ff;
-      const double zd = zcs2 * fmz_k * zrom1w * pai_k + ff;
+      double zu, zd;
+      if constexpr (kSolvePre) {
+        zu = fmz_m * zrom1w * pai_m + ff;  // fmz_m = zcs2*fmz
+        zd = fmz_k * zrom1w * pai_k + ff;
+      } else {
+        zu = zcs2 * fmz_m * zrom1w * pai_m + ff;
+        zd = zcs2 * fmz_k * zrom1w * pai_k + ff;
+      }
       const double zrapp = 1.0 / (1.0 + zd + zu - zd * wkp1);
       wnext = zrapp * (zwexpl + zd * wnext);
       wkp1 = zrapp * zu;
@@ -324,9 +346,11 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
   if (t == 0)
     for (int v = 0; v < NS && v < nu; ++v) issue_up(v, (nd + v) % NS);
   // Exner (:668-671) of level m once w(m+1) is known, and s (:728-734)
+  // fz: fmz, or dtrdz*fmz from bind time
   auto exner = [&](int m, double wm, double wmp, double pk, double zf, double fz, double sm, double fzf) {
     const int o = (m - 1) * PS + ij_off;
-    pai[o] = pk * (1.0 - kRdrcv * (zf + (dtrdz * fz * (wm - wmp))));
+    if constexpr (kSolvePre) pai[o] = pk * (1.0 - kRdrcv * (zf + (fz * (wm - wmp))));
+    else pai[o] = pk * (1.0 - kRdrcv * (zf + (dtrdz * fz * (wm - wmp))));
     if (last && m >= 2) s[o] = (wm + sm) * fzf;
   };
   double wprev = act ? w[ij_off] : 0.0;  // w(1) = 0
