@@ -133,6 +133,26 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tile
   }
 }
 
+// 1/d for the FP64 solve's pivot (d >= 1).  MLC_SOLVE_RCP 1: Newton's
+// iteration r' = r + r*(1 - d*r) from the FP32 approximate reciprocal of d
+// (relative error below 2^-21), two steps, each squaring the error (to below
+// 2^-84 before the last rounding: within an ulp of 1/d), four fused
+// multiply-adds and no FP64 division; 0: the IEEE division.
+#ifndef MLC_SOLVE_RCP
+#define MLC_SOLVE_RCP 0
+#endif
+__device__ __forceinline__ double solve_recip(double d) {
+  if constexpr (MLC_SOLVE_RCP != 0) {
+    double r = (double)__fdividef(1.f, (float)d);
+    double e = __fma_rn(-d, r, 1.0);
+    r = __fma_rn(r, e, r);
+    e = __fma_rn(-d, r, 1.0);
+    return __fma_rn(r, e, r);
+  } else {
+    return 1.0 / d;
+  }
+}
+
 // The implicit w-Exner solve of an FP64 member (Main/mod_moloch.F90:627-671,
 // s :728-734): per interior column the filtered divergence plus its vertical
 // part, the Thomas elimination k = kz..2, back substitution, the Exner
@@ -318,7 +338,7 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
         zu = zcs2 * fmz_m * zrom1w * pai_m + ff;
         zd = zcs2 * fmz_k * zrom1w * pai_k + ff;
       }
-      const double zrapp = 1.0 / (1.0 + zd + zu - zd * wkp1);
+      const double zrapp = solve_recip(1.0 + zd + zu - zd * wkp1);
       wnext = zrapp * (zwexpl + zd * wnext);
       wkp1 = zrapp * zu;
       w[o] = wnext;
