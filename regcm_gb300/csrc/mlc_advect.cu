@@ -199,7 +199,7 @@ __device__ __forceinline__ T waf_flux_d(T vel, bool up, T zmih, T zmi, T x, T de
   if constexpr (sizeof(T) == sizeof(double)) {
     bool dbl;
     const double sel = waf_sel(den, num, dbl);
-    return __dmul_rn(vel, __fma_rn(dbl ? -zmi : -zmih, sel, x));
+    return __dmul_rn(vel, __fma_rn(-(dbl ? zmi : zmih), sel, x));
   } else {
     (void)zmi;
     const T B = waf_b<T>(den, num);
@@ -213,7 +213,7 @@ __device__ __forceinline__ T waf_flux_h(T vel, bool up, T zmih, T zmi, T a, T c,
   if constexpr (sizeof(T) == sizeof(double)) {
     bool dbl;
     const double sel = waf_sel(den, num, dbl);
-    return __dmul_rn(vel, __fma_rn(dbl ? -zmi : -zmih, sel, x));
+    return __dmul_rn(vel, __fma_rn(-(dbl ? zmi : zmih), sel, x));
   } else {
     (void)zmi;
     const T B = waf_b<T>(den, num);
