@@ -137,7 +137,9 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tile
 // iteration r' = r + r*(1 - d*r) from the FP32 approximate reciprocal of d
 // (relative error below 2^-21), two steps, each squaring the error (to below
 // 2^-84 before the last rounding: within an ulp of 1/d), four fused
-// multiply-adds and no FP64 division; 0: the IEEE division.
+// multiply-adds and no FP64 division; 0: the IEEE division.  Both pass the
+// FP64 parity tests; on the moist 512x512x41 step the Newton form measured
+// 3.57 ms of solves a step against 3.47 for the division, so the default is 0.
 #ifndef MLC_SOLVE_RCP
 #define MLC_SOLVE_RCP 0
 #endif
