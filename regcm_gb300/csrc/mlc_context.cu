@@ -856,12 +856,7 @@ Clock get_clock(mlc_ctx *x, int slot, int *st) {
 // same staging slice.
 // An FP64 array goes straight between the packed host array and the padded
 // device layout in one pitched copy (rows of nj, ni rows of a plane on the
-// host, iy on the device), or - MLC_FP64_STAGED - as one contiguous copy into
-// the staging buffer and a layout kernel; a conversion to FP32 always goes
-// through the staging buffer.
-#ifndef MLC_FP64_STAGED
-#define MLC_FP64_STAGED 0
-#endif
+// host, iy on the device); a conversion to FP32 goes through the staging buffer.
 cudaMemcpy3DParms pitched(const Geom &g, const double *host, double *dev, int nj, int ni, int nk,
                           bool to_device) {
   cudaMemcpy3DParms c{};
@@ -878,7 +873,7 @@ cudaMemcpy3DParms pitched(const Geom &g, const double *host, double *dev, int nj
 template <class R>
 int put3(mlc_ctx *x, const Geom &g, const double *h, R *dst, int nj, int ni, int nk, size_t soff) {
   if (!h) return MLC_OK;
-  if constexpr (sizeof(R) == sizeof(double) && !MLC_FP64_STAGED) {
+  if constexpr (sizeof(R) == sizeof(double)) {
     const cudaMemcpy3DParms c = pitched(g, h, reinterpret_cast<double *>(dst), nj, ni, nk, true);
     MLC_TRY(cudaMemcpy3DAsync(&c, x->stream));
     return MLC_OK;
@@ -911,7 +906,7 @@ int get3x(mlc_ctx *x, const Geom &g, const double *src, double *h, int nj, int n
 template <class R>
 int get3(mlc_ctx *x, const Geom &g, const R *src, double *h, int nj, int ni, int nk, size_t soff) {
   if (!h) return MLC_OK;
-  if constexpr (sizeof(R) == sizeof(double) && !MLC_FP64_STAGED) {
+  if constexpr (sizeof(R) == sizeof(double)) {
     const cudaMemcpy3DParms c =
         pitched(g, h, reinterpret_cast<double *>(const_cast<R *>(src)), nj, ni, nk, false);
     MLC_TRY(cudaMemcpy3DAsync(&c, x->stream));

@@ -133,28 +133,6 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tile
   }
 }
 
-// 1/d for the FP64 solve's pivot (d >= 1).  MLC_SOLVE_RCP 1: Newton's
-// iteration r' = r + r*(1 - d*r) from the FP32 approximate reciprocal of d
-// (relative error below 2^-21), two steps, each squaring the error (to below
-// 2^-84 before the last rounding: within an ulp of 1/d), four fused
-// multiply-adds and no FP64 division; 0: the IEEE division.  Both pass the
-// FP64 parity tests; on the moist 512x512x41 step the Newton form measured
-// 3.57 ms of solves a step against 3.47 for the division, so the default is 0.
-#ifndef MLC_SOLVE_RCP
-#define MLC_SOLVE_RCP 0
-#endif
-__device__ __forceinline__ double solve_recip(double d) {
-  if constexpr (MLC_SOLVE_RCP != 0) {
-    double r = (double)__fdividef(1.f, (float)d);
-    double e = __fma_rn(-d, r, 1.0);
-    r = __fma_rn(r, e, r);
-    e = __fma_rn(-d, r, 1.0);
-    return __fma_rn(r, e, r);
-  } else {
-    return 1.0 / d;
-  }
-}
-
 // The implicit w-Exner solve of an FP64 member (Main/mod_moloch.F90:627-671,
 // s :728-734): per interior column the filtered divergence plus its vertical
 // part, the Thomas elimination k = kz..2, back substitution, the Exner
@@ -340,7 +318,7 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
         zu = zcs2 * fmz_m * zrom1w * pai_m + ff;
         zd = zcs2 * fmz_k * zrom1w * pai_k + ff;
       }
-      const double zrapp = solve_recip(1.0 + zd + zu - zd * wkp1);
+      const double zrapp = 1.0 / (1.0 + zd + zu - zd * wkp1);
       wnext = zrapp * (zwexpl + zd * wnext);
       wkp1 = zrapp * zu;
       w[o] = wnext;
@@ -417,20 +395,9 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
 #define MLC_SV_STAGES 4
 #endif
 constexpr int kSvStages = MLC_SV_STAGES;  // levels in flight ahead of the one being solved
-// Warp-specialised mixed solve: a fifth warp issues the copies and the four
-// column warps release each stage through an mbarrier instead of a block
-// barrier a level (1), or one thread issues after a block barrier (0).  Both
-// pass the same tests; on the moist 512x512x41 step the warp-specialised form
-// measured 0.857 ms of solves a step against 0.848 (the solve is bound by its
-// issue rate, not by the barrier), so the default is 0.
-#ifndef MLC_SOLVE_WS
-#define MLC_SOLVE_WS 0
-#endif
-constexpr bool kSolveWS = MLC_SOLVE_WS != 0;
 constexpr int kSvW = 128;            // columns of a block (one row segment)
 constexpr int kSvZW = kSvW + 8;      // raw divergence rows with a 4-column halo each side
 constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
-constexpr int kSvThreads = kSvW + (kSolveWS ? 32 : 0);
 
 // The solve of a mixed member (same equations as k_sound_solve), in FP32
 // only, one thread per column.  Where rounding is amplified the values are
@@ -460,28 +427,22 @@ constexpr int kSvThreads = kSvW + (kSolveWS ? 32 : 0);
 // 0.73 ms of solves a step against 0.95 for the same thread-per-column
 // kernel with register prefetch of one level.)
 template <class R, bool DFR>
-__global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last,
+__global__ void __launch_bounds__(128, 4) k_solve_mixed(const Dom<R> *__restrict__ doms, int advoff, int last,
     const WorkItem *__restrict__ wl) {
   constexpr int NS = kSvStages;
-  constexpr bool WS = kSolveWS;
-  constexpr unsigned kCons = kSvW / 32;  // consumer warps
   extern __shared__ __align__(16) float sv_smem[];
   __shared__ __align__(8) uint64_t mbar[NS];
-  __shared__ __align__(8) uint64_t mbar_e[WS ? NS : 1];  // stage released by every consumer warp
-  __shared__ int abort_s;
   const WorkItem wi = wl ? wl[blockIdx.x]
                           : WorkItem{(int16_t)blockIdx.z, (int16_t)blockIdx.x, (int16_t)blockIdx.y, 0};
   const Dom<R> &D = doms[wi.m];
   if (!D.active) return;
   const Geom g = D.g;
   const int t = (int)threadIdx.x;
-  const int lane = t & 31;
-  const bool producer = WS && t >= kSvW;    // the copy-issuing warp (warp-specialised form)
   const int x0 = (int)wi.a * kSvW;          // first column (0-based j-1) of the block
   const int i = (int)wi.b + 2;
   if (x0 + 1 > g.jx - 2 || i > g.iy - 2) return;  // uniform over the block
   const int j = x0 + t + 1;
-  const bool act = !producer && j >= 2 && j <= g.jx - 2;
+  const bool act = j >= 2 && j <= g.jx - 2;
   const int kz = g.kz;
   const Scal &c = D.c;
   const Stat<R> &sa = D.sa;
@@ -583,51 +544,11 @@ __global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(co
   };
   if (t == 0) {
     for (int q = 0; q < NS; ++q) mbar_init(&mbar[q], 1);
-    if constexpr (WS)
-      for (int q = 0; q < NS; ++q) mbar_init(&mbar_e[q], kCons);
-    abort_s = 0;
     fence_mbar_init();
   }
   __syncthreads();
-  // Warp-specialised form: the producer warp's lane 0 issues every unit's
-  // copies, waiting (bounded) for the consumer warps to release the stage
-  // the unit reuses; the consumer warps wait only for their data and never
-  // for each other.  A wait that runs out sets the fault flag and abort_s;
-  // both roles then skip their remaining waits, and the producer lets the
-  // copies still in flight land before the block leaves.
-  int issued = 0;  // units the producer has issued (global numbering: down, then up)
-  auto produce = [&](int gfirst, int gend, bool upp) {
-    for (int gu = gfirst; gu < gend; ++gu) {
-      const int b = gu % NS;
-      int okp = 1;
-      if (lane == 0) {
-        okp = *(volatile int *)&abort_s == 0;
-        if (okp && gu >= NS) okp = mbar_wait_bounded(&mbar_e[b], (unsigned)(((gu / NS) - 1) & 1));
-        if (okp) {
-          if (upp) issue_up(gu - nd, b);
-          else issue_down(gu, b);
-          issued = gu + 1;
-        } else if (*(volatile int *)&abort_s == 0) {
-          abort_s = 1;
-          atomicOr(&D.clk->fault, 1);
-        }
-      }
-      if (!__shfl_sync(0xffffffffu, okp, 0)) return;
-    }
-  };
-  // a consumer warp's bounded wait for unit gu: false once any wait ran out
-  auto consume_wait = [&](int gu) {
-    bool okc = *(volatile int *)&abort_s == 0 && mbar_wait_bounded(&mbar[gu % NS], (unsigned)((gu / NS) & 1));
-    okc = __all_sync(0xffffffffu, okc);
-    if (!okc && lane == 0 && atomicExch(&abort_s, 1) == 0) atomicOr(&D.clk->fault, 1);
-    return okc;
-  };
-  auto release = [&](int gu) {
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&mbar_e[gu % NS]);
-  };
-  if (WS ? (producer && lane == 0) : t == 0)
-    for (int u = 0; u < NS && u < nd; ++u) { issue_down(u, u); issued = u + 1; }
+  if (t == 0)
+    for (int u = 0; u < NS && u < nd; ++u) issue_down(u, u);
 
   struct LvA {
     float z, lap, s, fmz;
@@ -656,17 +577,10 @@ __global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(co
   F2 wnextd{wnext, 0.f}, wkp1d{0.f, 0.f};
   bool ok = true;
   int synced = 0;  // first unit read since the last block barrier
-  if (producer) produce(NS, nd, false);
-  for (int u = 0; u < nd && !producer; ++u) {
+  for (int u = 0; u < nd; ++u) {
     const int k = kz - u, m = k - 1;
     const int b = u % NS;
-    bool landed;
-    if constexpr (WS) {
-      landed = consume_wait(u);
-      if (!landed) break;
-    } else {
-      landed = mbar_wait_bounded(&mbar[b], (unsigned)((u / NS) & 1));
-    }
+    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((u / NS) & 1));
     const float *st = stage(b);
     if (act) {
       const int o = (k - 1) * PS + ij_off;
@@ -718,10 +632,6 @@ __global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(co
       zfk = zf_m;
       ak = am;
     }
-    if constexpr (WS) {
-      release(u);
-      continue;
-    }
     ok = ok && landed;
     if ((u + 1) % kSolveSync == 0 || u + 1 == nd) {
       if (__syncthreads_or(!ok)) {
@@ -740,18 +650,8 @@ __global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(co
   fence_proxy_async_global();
   __syncthreads();
   const int nu = kz;  // up units: m = 2 .. kz+1
-  if constexpr (WS) {
-    if (abort_s) {
-      // let the copies in flight land (at most NS, the last issued) and leave
-      if (producer && lane == 0)
-        for (int q = max(0, issued - NS); q < issued; ++q)
-          mbar_wait_bounded(&mbar[q % NS], (unsigned)((q / NS) & 1));
-      return;
-    }
-    if (producer) produce(nd, nd + nu, true);
-  } else if (t == 0) {
+  if (t == 0)
     for (int v = 0; v < NS && v < nu; ++v) issue_up(v, (nd + v) % NS);
-  }
   auto exner = [&](int m, float wm, float dw, F2 pk, float zf, float fz, float sm, float fzf) {
     const int o = (m - 1) * PS + ij_off;
     const float inc = rdrcv * (zf + (dtrdz * fz * dw));
@@ -765,16 +665,10 @@ __global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(co
   F2 wprevd{wprev, 0.f};
   ok = true;
   synced = 0;
-  for (int v = 0; v < nu && !producer; ++v) {
+  for (int v = 0; v < nu; ++v) {
     const int k = v + 2, gu = nd + v;
     const int b = gu % NS;
-    bool landed;
-    if constexpr (WS) {
-      landed = consume_wait(gu);
-      if (!landed) break;
-    } else {
-      landed = mbar_wait_bounded(&mbar[b], (unsigned)((gu / NS) & 1));
-    }
+    const bool landed = mbar_wait_bounded(&mbar[b], (unsigned)((gu / NS) & 1));
     if (act) {
       const float *f0 = stage(b) + 3 * kSvZW + t;
       const float wel = f0[0];
@@ -802,10 +696,6 @@ __global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(co
         }
       }
     }
-    if constexpr (WS) {
-      release(gu);
-      continue;
-    }
     ok = ok && landed;
     if ((v + 1) % kSolveSync == 0 || v + 1 == nu) {
       if (__syncthreads_or(!ok)) {
@@ -817,12 +707,6 @@ __global__ void __launch_bounds__(kSvThreads, kSolveWS ? 7 : 4) k_solve_mixed(co
           if (r + NS < nu) issue_up(r + NS, (nd + r) % NS);
       synced = v + 1;
     }
-  }
-  if constexpr (WS) {
-    if (producer && lane == 0 && *(volatile int *)&abort_s)
-      for (int q = max(0, issued - NS); q < issued; ++q)
-        mbar_wait_bounded(&mbar[q % NS], (unsigned)((q / NS) & 1));
-    if (*(volatile int *)&abort_s) return;
   }
   if (last && act) {
     s[ij_off] = 0.f;
@@ -1299,9 +1183,9 @@ void Launch<R>::sound_solve(const LaunchGeom &L, const Dom<R> *d, int uvoff, int
                                  : dim3((unsigned)tj, (unsigned)(L.iy - 3), (unsigned)L.nmem);
     const size_t smem = (size_t)kSvStages * kSvStage * sizeof(float);
     if (L.solve_df)
-      k_solve_mixed<R, true><<<grid, kSvThreads, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
+      k_solve_mixed<R, true><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
     else
-      k_solve_mixed<R, false><<<grid, kSvThreads, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
+      k_solve_mixed<R, false><<<grid, kSvW, smem, s>>>(d, advoff, last ? 1 : 0, L.wl_solve);
   } else {
     const int tj = (L.jx - 1 + kDvW - 1) / kDvW;
     const dim3 grid = L.wl_solve ? dim3((unsigned)L.n_solve, 1, 1)

@@ -27,10 +27,6 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
                "r"(bytes)
                : "memory");
 }
-// a plain arrival (no transaction count), e.g. a consumer releasing a stage
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 // one tiled copy of the box at (x, y, z) of the tensor map into shared memory
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z,
                                             uint64_t *bar) {
