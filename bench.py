@@ -300,6 +300,20 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(seconds: float, world: int) -> float:
+    """The slowest rank's time, which is the whole job's: an all-reduce over
+    the process group on its own device (the GPU for NCCL, the host for
+    gloo).  One process alone returns its own time."""
+    if world <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([seconds], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---- our arm -----------------------------------------------------------------
 def pinned_like(arrays: dict) -> dict:
     import torch
@@ -338,10 +352,8 @@ def run_ours(args, rank, world):
     abi.check(st, "mlc_step_timed")
     torch.cuda.synchronize()
     t_dev = ms.value / 1000.0
+    t_dev = max_over_ranks(t_dev, world)
     if world > 1:
-        t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
         torch.distributed.barrier()
     pts = case.points
     value = pts * args.steps * world / t_dev
@@ -373,10 +385,7 @@ def run_ours(args, rank, world):
             dom.step(1)
             dom.download(sp_out)
         te = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([te], device="cuda", dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            te = float(t.item())
+        te = max_over_ranks(te, world)
         e2e = {"value": pts * ne * world / te, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": ne, "ms_per_step": 1000.0 * te / ne}
     dom.close()
@@ -471,10 +480,7 @@ def ensemble_line(args, rank, world):
     with ClockSampler(dev) as clk:
         abi.check(lib.mlc_step_timed(batch._ctx, args.steps, C.byref(diag), C.byref(ms)), "batch")
     t_dev = ms.value / 1000.0
-    if world > 1:
-        t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(t_dev, world)
     value = pts * nmem * args.steps * world / t_dev
     ktab = (KT * 32)()
     nk = C.c_int()
@@ -568,7 +574,7 @@ def run_uneven(args, rank, world):
         torch.distributed.barrier()
     with ClockSampler(dev) as clk:
         ms = batch.step_timed(args.steps)
-    t_dev = ms / 1000.0
+    t_dev = max_over_ranks(ms / 1000.0, world)
     value = sum(pts) * args.steps * world / t_dev
     launches = batch.launches_per_step()
     sample = list(range(0, nmem, 10))
