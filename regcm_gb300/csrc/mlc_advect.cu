@@ -36,6 +36,13 @@ template <> struct FlowEps<double> {
   static __device__ __forceinline__ double num() { return (double)1.0e-30f; }
 };
 
+// -x for an FP64 operand of a fused multiply-add, as a flip of the sign bit
+// in the integer pipe (exact, like the negation itself), so that no FP64
+// instruction forms it (on GB300 every FP64 instruction is 1/64-rate work)
+__device__ __forceinline__ double neg_d(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
+
 // x0 + m*(a*b - c*d + e*f) of the horizontal updates.  For FP64 the products
 // are fused explicitly (the second and third into fused multiply-adds), so the
 // rounding does not depend on how the compiler contracts the expression in
@@ -47,9 +54,9 @@ template <class T>
 __device__ __forceinline__ T stencil_update(T x0, T m, bool rot, bool chain, T a, T b, T c, T d, T e,
                                             T f) {
   if constexpr (sizeof(T) == sizeof(double)) {
-    if (rot && chain) return __fma_rn(e, f, __fma_rn(-c, d, __fma_rn(a, b, x0)));
-    const T t = __fma_rn(e, f, __fma_rn(-c, d, __dmul_rn(a, b)));
-    return rot ? __dadd_rn(x0, t) : __fma_rn(m, t, x0);
+    if (rot && chain) return __fma_rn(e, f, __fma_rn(neg_d(c), d, __fma_rn(a, b, x0)));
+    const T t = __fma_rn(e, f, __fma_rn(neg_d(c), d, __dmul_rn(a, b)));
+    return __fma_rn(m, t, x0);  // rot: m = 1, x0 + t exactly as the sum
   } else {
     const T z = e * f;
     if (rot && chain) return x0 + a * b - c * d + z;
@@ -199,7 +206,7 @@ __device__ __forceinline__ T waf_flux_d(T vel, bool up, T zmih, T zmi, T x, T de
   if constexpr (sizeof(T) == sizeof(double)) {
     bool dbl;
     const double sel = waf_sel(den, num, dbl);
-    return __dmul_rn(vel, __fma_rn(-(dbl ? zmi : zmih), sel, x));
+    return __dmul_rn(vel, __fma_rn(neg_d(dbl ? zmi : zmih), sel, x));
   } else {
     (void)zmi;
     const T B = waf_b<T>(den, num);
@@ -213,7 +220,7 @@ __device__ __forceinline__ T waf_flux_h(T vel, bool up, T zmih, T zmi, T a, T c,
   if constexpr (sizeof(T) == sizeof(double)) {
     bool dbl;
     const double sel = waf_sel(den, num, dbl);
-    return __dmul_rn(vel, __fma_rn(-(dbl ? zmi : zmih), sel, x));
+    return __dmul_rn(vel, __fma_rn(neg_d(dbl ? zmi : zmih), sel, x));
   } else {
     (void)zmi;
     const T B = waf_b<T>(den, num);
@@ -350,7 +357,7 @@ __global__ void k_adv_prep(const Dom<R> *__restrict__ doms, int uvoff, int advof
       // zmih = zmi/2 - once for all fields (FP64 arithmetic is the FP64
       // path's bound)
       const double skp = D.s[o + PS];
-      D.vdiv[o] = __fma_rn(-skp, D.sa.zrfmd[o], __dmul_rn(D.s[o], D.sa.zrfmu[o]));
+      D.vdiv[o] = __fma_rn(neg_d(skp), D.sa.zrfmd[o], __dmul_rn(D.s[o], D.sa.zrfmu[o]));
       const double dtrdz = 0.5 * (D.c.dtstepa * D.c.rdzita);
       const double zamu = __dmul_rn(skp, dtrdz);
       const double zmi = waf_zmi<double>(zamu, nonneg(zamu));
@@ -402,7 +409,7 @@ __device__ __forceinline__ T vupdate(T pk, T fb, T fa, T sk, T skp, T zu, T zd) 
 // products fused explicitly
 template <class T>
 __device__ __forceinline__ T vupdate_f(T pk, T fb, T fa, T dv, T zu, T zd) {
-  return __fma_rn(dv, pk, __fma_rn(fa, zd, __fma_rn(-fb, zu, pk)));
+  return __fma_rn(dv, pk, __fma_rn(fa, zd, __fma_rn(neg_d(fb), zu, pk)));
 }
 
 // Blocks of 256 threads an SM the vertical WAF is compiled for, FP64 and FP32
