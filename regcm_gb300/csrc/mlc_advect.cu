@@ -36,6 +36,16 @@ template <> struct FlowEps<double> {
   static __device__ __forceinline__ double num() { return (double)1.0e-30f; }
 };
 
+// The bit pattern of x through an opaque move, for the sign, region and
+// upwind tests that run on the integer pipe: a plain reinterpretation lets the
+// compiler turn an integer test of the pattern back into an FP64 comparison
+// (an instruction of the 1/64-rate FP64 pipe on GB300)
+__device__ __forceinline__ long long bits_of(double x) {
+  long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+}
+
 // -x for an FP64 operand of a fused multiply-add, as a flip of the sign bit
 // in the integer pipe (exact, like the negation itself), so that no FP64
 // instruction forms it (on GB300 every FP64 instruction is 1/64-rate work)
@@ -71,7 +81,7 @@ __device__ __forceinline__ T stencil_update(T x0, T m, bool rot, bool chain, T a
 template <class T>
 __device__ __forceinline__ bool nonneg(T x) {
   if constexpr (sizeof(T) == sizeof(double)) {
-    const long long b = __double_as_longlong(x);
+    const long long b = bits_of(x);
     return (b >= 0 && b <= 0x7ff0000000000000LL) || b == (long long)0x8000000000000000ULL;
   } else {
     return x >= T(0);
@@ -80,7 +90,7 @@ __device__ __forceinline__ bool nonneg(T x) {
 template <class T>
 __device__ __forceinline__ bool positive(T x) {
   if constexpr (sizeof(T) == sizeof(double)) {
-    const long long b = __double_as_longlong(x);
+    const long long b = bits_of(x);
     return b > 0 && b <= 0x7ff0000000000000LL;
   } else {
     return x > T(0);
@@ -124,7 +134,7 @@ __device__ __forceinline__ T waf_b(T den, T num) {
     // XOR.  The tests are the comparisons above exactly (a NaN num fails every
     // comparison and takes the last region in both forms); only the flux itself
     // uses the FP64 pipe.
-    const long long bden = __double_as_longlong(den), bnum = __double_as_longlong(num);
+    const long long bden = bits_of(den), bnum = bits_of(num);
     const long long mag = 0x7fffffffffffffffLL, one_exp = 1LL << 52;
     const long long ad = bden & mag;                    // |den|
     const long long bq = bnum ^ (bden & ~mag);          // q, as a signed pattern
@@ -170,7 +180,7 @@ __device__ __forceinline__ T waf_flux(T hvel, bool up, T zamu, T a, T c, T num) 
 // fused multiply-add and one product are FP64 instructions.
 __device__ __forceinline__ double waf_sel(double den, double num, bool &dbl) {
   // the regions of waf_b, tested on the bit patterns
-  const long long bden = __double_as_longlong(den), bnum = __double_as_longlong(num);
+  const long long bden = bits_of(den), bnum = bits_of(num);
   const long long mag = 0x7fffffffffffffffLL, one_exp = 1LL << 52;
   const long long ad = bden & mag;
   const long long bq = bnum ^ (bden & ~mag);
@@ -191,7 +201,7 @@ __device__ __forceinline__ double waf_sel(double den, double num, bool &dbl) {
 template <class T>
 __device__ __forceinline__ T self_diff(T a) {
   if constexpr (sizeof(T) == sizeof(double)) {
-    const long long b = __double_as_longlong(a);
+    const long long b = bits_of(a);
     const long long e = 0x7ff0000000000000LL;
     return (b & e) == e ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
   } else {
