@@ -799,7 +799,12 @@ def kernel_roofline(lib, ctx, case, precision):
                     "peak": peak,
                     "peak_source": "measured in this run (mlc_fp64_peak, FP64 FMA chains)",
                     "frac": ach / peak, "algorithmic_fp64_ops": ops, "traffic": traffic,
-                    "hbm": hbm}
+                    "hbm": hbm,
+                    "note": ("achieved counts the reference's FP64 operations for the same "
+                             "results (its limiter's divides, min/max and compares included); "
+                             "the kernel tests the limiter's regions on the integer pipe and "
+                             "divides nowhere, so fewer FP64 instructions do that work and the "
+                             "fraction can exceed 1")}
     else:
         roofline = {"kernel": dom_name, "bound": "hbm", "unit": "GB/s", "peak": hbm_peak,
                     "peak_source": hbm_src, "traffic": traffic}
