@@ -153,7 +153,10 @@ __global__ void k_sound_div(const Dom<R> *__restrict__ doms, int uvoff, int tile
 #define MLC_SOLVE_SYNC 1
 #endif
 constexpr int kSolveSync = MLC_SOLVE_SYNC;
-constexpr int kDvStages = 3;
+#ifndef MLC_DV_STAGES
+#define MLC_DV_STAGES 3
+#endif
+constexpr int kDvStages = MLC_DV_STAGES;  // FP64 solve: levels in flight
 constexpr int kDvW = 128;
 constexpr int kDvZW = kDvW + 4;                   // raw divergence row, 2-column halo each side
 // The FP64 solve reads its metric products from bind time - (bw*dtrdz)*fmz,
