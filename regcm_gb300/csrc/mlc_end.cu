@@ -603,6 +603,27 @@ __global__ void k_end_ps(const Dom<R> *__restrict__ doms, int uvoff, int advoff)
   ps_column<R>(D, st, g.at2(j, i));
 }
 
+// q < c for a positive finite threshold c, exactly as the comparison (false
+// for a NaN q).  FP64: on the bit patterns in the integer pipe, read through
+// an opaque move (a plain reinterpretation would be turned back into an FP64
+// comparison); a negative q, -0 included, has the sign bit set and compares
+// below every positive pattern as a signed integer.  FP32 compares directly.
+__device__ __forceinline__ long long bits_of_d(double x) {
+  long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
+}
+template <class R>
+__device__ __forceinline__ bool below_pos(R q, double c) {
+  if constexpr (sizeof(R) == sizeof(double)) {
+    const long long b = bits_of_d(q);
+    const bool nan = (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+    return !nan && b < __double_as_longlong(c);
+  } else {
+    return q < R(c);
+  }
+}
+
 // Cross-point work after the boundary, per point: uvstagtouvx and
 // temp_to_tvirt of boundary (:520-523), p (:348-352), the edits mkslice
 // makes to the state (Main/mod_slice.F90:136-147: qx and tracer floors),
@@ -681,11 +702,11 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
     if (inner) {
       for (int n = 0; n < g.nqx; ++n) {
         const size_t on = o + (size_t)n * F;
-        if (st.qx[on] < R(qx_check(n))) st.qx[on] = R(qx_zero(n));
+        if (below_pos<R>(st.qx[on], qx_check(n))) st.qx[on] = R(qx_zero(n));
       }
       for (int n = 0; n < g.ntr; ++n) {
         const size_t on = o + (size_t)n * F;
-        if ((double)st.trac[on] < kTracFloor) st.trac[on] = R(0);
+        if (below_pos<double>((double)st.trac[on], kTracFloor)) st.trac[on] = R(0);
       }
     }
     continue;
@@ -709,20 +730,26 @@ __global__ void k_end_cross(const Dom<R> *__restrict__ doms, int uvoff, int advo
         }
       }
       const R dts = pick<R>(c.dtsec, c.dtsecf);
+      // The whole step's mkslice floor and status_update clamp with zero
+      // tendencies are one clamp: after the floor q >= check or q = zero, and
+      // zero < check or zero = check, so the second clamp changes nothing (for
+      // the tracers, the floor leaves no negative value)
       for (int n = 0; n < g.nqx; ++n) {
         const size_t on = o + (size_t)n * F;
         R q = st.qx[on];
-        if (PH == kEndAll && q < R(qx_check(n))) q = R(qx_zero(n));  // mkslice
         if (ten) q = q + dts * ten[o + (size_t)(3 + n) * F];
-        if (q < R(qx_check(n))) q = R(qx_zero(n));
+        if (below_pos<R>(q, qx_check(n))) q = R(qx_zero(n));
         st.qx[on] = q;
       }
       for (int n = 0; n < g.ntr; ++n) {
         const size_t on = o + (size_t)n * F;
         R q = st.trac[on];
-        if (PH == kEndAll && (double)q < kTracFloor) q = R(0);  // mkslice
-        if (ten) q = q + dts * ten[o + (size_t)(3 + g.nqx + n) * F];
-        if (q < R(0)) q = R(0);
+        if (PH == kEndAll) {
+          if (below_pos<double>((double)q, kTracFloor)) q = R(0);  // mkslice
+        } else {
+          if (ten) q = q + dts * ten[o + (size_t)(3 + g.nqx + n) * F];
+          if (q < R(0)) q = R(0);
+        }
         st.trac[on] = q;
       }
     }
