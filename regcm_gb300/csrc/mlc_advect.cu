@@ -186,17 +186,15 @@ __device__ __forceinline__ double waf_sel(double den, double num, bool &dbl) {
   const long long bq = bnum ^ (bden & ~mag);
   const long long eden = __double_as_longlong(FlowEps<double>::den());
   const long long enum_ = __double_as_longlong(FlowEps<double>::num());
-  // the same regions as one set of flags and selects, without branches (the
-  // lanes of a warp fall in different regions): |den| below minden; num NaN;
-  // q <= 0; q < d/2; q <= d; q < 2d (each implying the next, d/2 and 2d being
-  // d's pattern -/+ 2^52 for a d above minden)
-  const bool small = ad < eden;
-  const bool nanq = (bnum & mag) > 0x7ff0000000000000LL;
-  const bool r0 = bq <= 0, r1 = bq < ad - one_exp, r2 = bq <= ad, r3 = bq < ad + one_exp;
-  const bool take_num = !r0 && (r1 || (!r2 && r3));
-  const bool take_den = small ? (bnum & mag) < enum_ : (nanq || (!r0 && !r1 && (r2 || !r3)));
-  dbl = !small && (nanq || (!r0 && (r1 || !r3)));
-  return take_den ? den : (!small && !nanq && take_num) ? num : 0.0;
+  dbl = false;
+  if (ad < eden) return (bnum & mag) < enum_ ? den : 0.0;
+  if ((bnum & mag) > 0x7ff0000000000000LL) { dbl = true; return den; }
+  if (bq <= 0) return 0.0;
+  if (bq < ad - one_exp) { dbl = true; return num; }
+  if (bq <= ad) return den;
+  if (bq < ad + one_exp) return num;
+  dbl = true;
+  return den;
 }
 // a - a for the limiter's region tests: +0 for a finite a, else a NaN (every
 // NaN takes the same region), formed on the integer pipe in FP64
