@@ -161,8 +161,8 @@ def kernel_bytes(name: str, case, nadv_fields: int, wbytes: int) -> float | None
 # the line prints them with that label and the kernel build they were taken
 # on.  Keyed by (kernel group, precision, advected fields).
 CAPTURED_TRAFFIC_PER_POINT = {
-    ("adv_horizontal", "fp64", 10): (733.1e6 / (256 * 256 * 41), "0c33f76"),
-    ("sound_solve", "mixed", 10): (243.0e6 / (256 * 256 * 41), "0c33f76"),
+    ("adv_horizontal", "fp64", 10): (733.3e6 / (256 * 256 * 41), "b130abd"),
+    ("sound_solve", "mixed", 10): (243.0e6 / (256 * 256 * 41), "b130abd"),
 }
 # What limits the dominant kernel besides its roofline, from the same captures.
 CAPTURED_LIMITER = {
