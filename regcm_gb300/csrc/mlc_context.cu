@@ -617,7 +617,7 @@ int ensure_lists(mlc_ctx *x) {
   for (int m = 0; m < (int)act.size(); ++m) {
     const Geom &g = act[m]->g;
     for (int r = 0; r < g.iy - 3; ++r)
-      for (int bj = 0; bj < cdiv(g.jx - 1, 128); ++bj) push(m, bj, r, 0);
+      for (int bj = 0; bj < cdiv(g.jx - 1, f64 ? kSolveColsD : kSolveColsF); ++bj) push(m, bj, r, 0);
   }
   // vertical WAF: column tiles, the member's own fields of the R table
   off[3] = all.size();

@@ -14,6 +14,14 @@
 
 namespace mlc {
 
+// Columns of a column-solve block (one row segment, one thread a column):
+// FP64 members and mixed members.
+#ifndef MLC_DV_W
+#define MLC_DV_W 128
+#endif
+constexpr int kSolveColsD = MLC_DV_W;
+constexpr int kSolveColsF = 128;
+
 // Extents of a launch (maxima over the members) and the launch shapes.
 struct LaunchGeom {
   int jx, iy, kz, nmem;

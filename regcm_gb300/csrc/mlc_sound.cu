@@ -157,7 +157,7 @@ constexpr int kSolveSync = MLC_SOLVE_SYNC;
 #define MLC_DV_STAGES 3
 #endif
 constexpr int kDvStages = MLC_DV_STAGES;  // FP64 solve: levels in flight
-constexpr int kDvW = 128;
+constexpr int kDvW = kSolveColsD;
 constexpr int kDvZW = kDvW + 4;                   // raw divergence row, 2-column halo each side
 // The FP64 solve reads its metric products from bind time - (bw*dtrdz)*fmz,
 // zcs2*fmz, dtrdz*fmz, the same roundings as forming them per level - (1),
@@ -168,7 +168,7 @@ constexpr int kDvZW = kDvW + 4;                   // raw divergence row, 2-colum
 constexpr bool kSolvePre = MLC_SOLVE_PRE != 0;
 constexpr int kDvStage = 3 * kDvZW + (kSolvePre ? 8 : 7) * kDvW;   // doubles of one stage
 template <class R>
-__global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last,
+__global__ void __launch_bounds__(kDvW, 4) k_sound_solve(const Dom<R> *__restrict__ doms, int advoff, int last,
     const WorkItem *__restrict__ wl) {
   static_assert(sizeof(R) == sizeof(double), "FP64 member");
   constexpr int NS = kDvStages;
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(128, 4) k_sound_solve(const Dom<R> *__restrict
 #define MLC_SV_STAGES 4
 #endif
 constexpr int kSvStages = MLC_SV_STAGES;  // levels in flight ahead of the one being solved
-constexpr int kSvW = 128;            // columns of a block (one row segment)
+constexpr int kSvW = kSolveColsF;          // columns of a block (one row segment)
 constexpr int kSvZW = kSvW + 8;      // raw divergence rows with a 4-column halo each side
 constexpr int kSvStage = 3 * kSvZW + 11 * kSvW;  // floats of one stage
 
