@@ -153,3 +153,26 @@ def test_fortran_shim_types_follow_the_headers():
                abi.mlc_bdy_ptrs, abi.mlc_diag, abi.mlc_tend_ptrs):
         want = [(n,) + kind_of(t) for n, t in st._fields_]
         assert types[st.__name__] == want, st.__name__
+
+
+def _gpu_present() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_gpu_present(), reason="checks the behaviour on a host without a GPU")
+def test_no_gpu_means_an_error_not_a_fallback():
+    """Without a device the library refuses to create a domain (there is no
+    CPU path behind the ABI), and the Python mirror raises."""
+    from regcm_gb300 import case as cs
+    from regcm_gb300.moloch import domain_from_case
+    lib = abi.load()
+    c = cs.build(24, 22, 12, dx=12000.0, dt=60.0, nsound=3, moist=False, seed=1, name="nogpu")
+    ctx = C.c_void_p()
+    st = lib.mlc_create(C.byref(c.dims), C.byref(c.params), C.byref(ctx))
+    assert st != abi.MLC_OK and not ctx.value
+    with pytest.raises(abi.MolochError):
+        domain_from_case(c)
