@@ -213,8 +213,11 @@ def kernel_fp64_ops(name: str, case, nadv_fields: int) -> float | None:
 
 
 def n_adv_fields(case) -> int:
+    """Advected fields of a member: theta_v, Exner, ux, vx, wx, qv, the other
+    species when ipptls > 0, TKE when ibltyp = 2, the tracers
+    (Main/mod_moloch.F90:781-807)."""
     p, d = case.params, case.dims
-    return 6 + (d.nqx - 1 if p.ipptls > 0 else 0) + d.ntr
+    return 6 + (d.nqx - 1 if p.ipptls > 0 else 0) + (1 if p.ibltyp == 2 else 0) + d.ntr
 
 
 def make_case(args, rank=0, setup=None):
